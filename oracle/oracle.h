@@ -1,0 +1,82 @@
+/*
+ * CPU oracle for the batched KEM path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * This library restates, in plain C, the algorithms the reference implements on the GPU:
+ * Keccak / FIPS-202, Kyber (round-2 variant as coded in the reference, and the round-3
+ * parameter sets), NewHope-1024 CPA-PKE + CPA-KEM and FrodoKEM-976 (SHAKE).  It is the checker
+ * for the CUDA path: only tests, the smoke check and the CPU-baseline leg of the benchmark
+ * load it.  The product library (libpqcgpu) never links or calls it.
+ *
+ * Parity status:
+ *   - Keccak family: pinned against Python hashlib (tests/test_oracle_fips202.py).
+ *   - Kyber round-2 CPA (k=4) and NewHope-1024 CPA: pinned against golden vectors produced by the
+ *     reference's own device code compiled for the host (oracle/build_ref.sh, tests/golden/).
+ *   - Kyber round-3 parameter sets, all KEM (Fujisaki-Okamoto) layers, NewHope CPA-KEM and
+ *     FrodoKEM-976: restated from the published algorithms and the reference's host flow
+ *     (FrodoKEM_GPU/kem.c); parity unpinned by reference outputs (no KAT files exist in the
+ *     reference tree).
+ */
+#ifndef PQC_ORACLE_H
+#define PQC_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- FIPS-202 ------------------------------------------------------------------------ */
+void oracle_keccakf1600(uint64_t s[25]);
+void oracle_shake128(uint8_t *out, size_t outlen, const uint8_t *in, size_t inlen);
+void oracle_shake256(uint8_t *out, size_t outlen, const uint8_t *in, size_t inlen);
+void oracle_sha3_256(uint8_t out[32], const uint8_t *in, size_t inlen);
+void oracle_sha3_512(uint8_t out[64], const uint8_t *in, size_t inlen);
+
+/* Work counters (Keccak permutations, NTT butterflies) accumulated per calling thread. */
+void oracle_counters_reset(void);
+uint64_t oracle_counter_keccak(void);
+uint64_t oracle_counter_butterfly(void);
+
+/* ---- Kyber ----------------------------------------------------------------------------
+ * variant 2: round-2 semantics as coded in Kyber_GPU_Batched (eta = 2, 16-bit 19q rejection,
+ *            du = 11, dv = 5; only k = 4 is meaningful, as in the reference).
+ * variant 3: round-3 parameter sets (k = 2: eta1 = 3; du/dv 10/4 for k = 2,3 and 11/5 for k = 4).
+ */
+int oracle_kyber_sizes(int variant, int k, size_t *pk, size_t *sk_cpa, size_t *sk, size_t *ct);
+int oracle_kyber_indcpa_keypair(int variant, int k, uint8_t *pk, uint8_t *sk, const uint8_t d[32]);
+int oracle_kyber_indcpa_enc(int variant, int k, uint8_t *ct, const uint8_t m[32], const uint8_t *pk,
+                            const uint8_t coins[32]);
+int oracle_kyber_indcpa_dec(int variant, int k, uint8_t m[32], const uint8_t *ct, const uint8_t *sk);
+int oracle_kyber_kem_keypair(int variant, int k, uint8_t *pk, uint8_t *sk, const uint8_t coins[64]);
+int oracle_kyber_kem_enc(int variant, int k, uint8_t *ct, uint8_t ss[32], const uint8_t *pk,
+                         const uint8_t coins[32]);
+int oracle_kyber_kem_dec(int variant, int k, uint8_t ss[32], const uint8_t *ct, const uint8_t *sk);
+
+/* ---- NewHope-1024 --------------------------------------------------------------------- */
+int oracle_newhope_cpapke_keypair(uint8_t *pk, uint8_t *sk, const uint8_t seed[32]);
+int oracle_newhope_cpapke_enc(uint8_t *ct, const uint8_t m[32], const uint8_t *pk, const uint8_t coin[32]);
+int oracle_newhope_cpapke_dec(uint8_t m[32], const uint8_t *ct, const uint8_t *sk);
+int oracle_newhope_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t coins[32]);
+int oracle_newhope_kem_enc(uint8_t *ct, uint8_t ss[32], const uint8_t *pk, const uint8_t coins[32]);
+int oracle_newhope_kem_dec(uint8_t ss[32], const uint8_t *ct, const uint8_t *sk);
+
+/* ---- FrodoKEM-976 (SHAKE) -------------------------------------------------------------- */
+int oracle_frodo_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t coins[64]);
+int oracle_frodo_kem_enc(uint8_t *ct, uint8_t ss[24], const uint8_t *pk, const uint8_t coins[24]);
+int oracle_frodo_kem_dec(uint8_t ss[24], const uint8_t *ct, const uint8_t *sk);
+
+/* ---- Batched drivers (OpenMP over instances; nthreads <= 0 means all cores) -------------
+ * alg: 0..2 = Kyber-512/768/1024 (round 3), 3 = Kyber-1024 round 2, 4 = NewHope-1024 CPA-KEM,
+ *      5 = FrodoKEM-976.  Buffers are instance-major, each instance at a fixed stride. */
+int oracle_batch_keypair(int alg, size_t n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int nthreads);
+int oracle_batch_enc(int alg, size_t n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *coins,
+                     int nthreads);
+int oracle_batch_dec(int alg, size_t n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, int nthreads);
+int oracle_alg_sizes(int alg, size_t *pk, size_t *sk, size_t *ct, size_t *ss, size_t *kp_coins,
+                     size_t *enc_coins);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

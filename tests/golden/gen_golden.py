@@ -1,0 +1,143 @@
+"""Generate the committed golden fixtures in tests/golden/.
+
+Run here (x86 container with the reference tree) after `oracle/build_ref.sh`:
+    python tests/golden/gen_golden.py
+
+Fixture kinds:
+  * keccak.json     -- FIPS-202 outputs from Python hashlib (independent implementation).
+  * ref_*.json      -- outputs of the reference's OWN device code (Kyber_GPU_Batched for k = 2/3/4,
+                       round-2 semantics; NewHope_NIST_GPU), compiled for the host by
+                       oracle/build_ref.sh and driven with the NIST per-instance seed layout.
+  * restated_*.json -- outputs of the CPU oracle for paths the reference has no code for (Kyber
+                       round-3 KEM, NewHope CPA-KEM, FrodoKEM-976): regression pins, parity
+                       unpinned by reference outputs.
+Inputs come from pqc_gb300.drbg with fixed seeds; every output is stored as SHA-256 per instance,
+and instance 0 is also stored in full.
+"""
+import ctypes
+import hashlib
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import pyoracle as O  # noqa: E402
+from pqc_gb300 import drbg  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref")
+
+
+def h(b):
+    return hashlib.sha256(b).hexdigest()
+
+
+def chunks(b, sz):
+    return [b[i * sz:(i + 1) * sz] for i in range(len(b) // sz)]
+
+
+def dump(name, obj):
+    with open(os.path.join(HERE, name), "w") as f:
+        json.dump(obj, f, indent=1, sort_keys=True)
+        f.write("\n")
+
+
+def keccak():
+    vec = []
+    seed = drbg.seed48(100)
+    for i, n in enumerate([0, 1, 31, 32, 33, 71, 72, 73, 135, 136, 137, 167, 168, 169, 500, 1184, 2400]):
+        data = drbg.stream(seed, b"keccak%d" % i, n)
+        vec.append({
+            "in": data.hex(),
+            "shake128_256": hashlib.shake_128(data).hexdigest(256),
+            "shake256_256": hashlib.shake_256(data).hexdigest(256),
+            "sha3_256": hashlib.sha3_256(data).hexdigest(),
+            "sha3_512": hashlib.sha3_512(data).hexdigest(),
+        })
+    dump("keccak.json", {"source": "python hashlib", "vectors": vec})
+
+
+def ref_kyber(k, n=16, s=1):
+    L = ctypes.CDLL(os.path.join(REF, "librefkyber%d.so" % k))
+    sz = O.kyber_sizes(2, k)
+    seed = drbg.seed48(s)
+    d = drbg.stream(seed, b"d", 32 * n)
+    m = drbg.stream(seed, b"m", 32 * n)
+    coins = drbg.stream(seed, b"coins", 32 * n)
+    pk = ctypes.create_string_buffer(n * sz["pk"])
+    sk = ctypes.create_string_buffer(n * sz["sk_cpa"])
+    ct = ctypes.create_string_buffer(n * sz["ct"])
+    m2 = ctypes.create_string_buffer(32 * n)
+    assert L.ref_kyber_cpa_keypair(n, pk, sk, d) == 0
+    assert L.ref_kyber_cpa_enc(n, ct, m, pk.raw, coins) == 0
+    assert L.ref_kyber_cpa_dec(n, m2, ct.raw, sk.raw) == 0
+    dump("ref_kyber_r2_k%d_cpa.json" % k, {
+        "source": "reference Kyber_GPU_Batched device code (KYBER_K=%d), host-compiled via oracle/build_ref.sh" % k,
+        "variant": 2, "k": k, "n": n, "drbg_seed": s,
+        "d": d.hex(), "m": m.hex(), "coins": coins.hex(),
+        "pk_sha256": [h(x) for x in chunks(pk.raw, sz["pk"])],
+        "sk_sha256": [h(x) for x in chunks(sk.raw, sz["sk_cpa"])],
+        "ct_sha256": [h(x) for x in chunks(ct.raw, sz["ct"])],
+        "m_dec": m2.raw.hex(),
+        "pk0": pk.raw[:sz["pk"]].hex(), "sk0": sk.raw[:sz["sk_cpa"]].hex(), "ct0": ct.raw[:sz["ct"]].hex(),
+    })
+
+
+def ref_newhope(n=16, s=2):
+    L = ctypes.CDLL(os.path.join(REF, "librefnewhope.so"))
+    seed = drbg.seed48(s)
+    kp = drbg.stream(seed, b"d", 32 * n)
+    m = drbg.stream(seed, b"m", 32 * n)
+    coins = drbg.stream(seed, b"coins", 32 * n)
+    pk = ctypes.create_string_buffer(n * 1824)
+    sk = ctypes.create_string_buffer(n * 1792)
+    ct = ctypes.create_string_buffer(n * 2176)
+    m2 = ctypes.create_string_buffer(32 * n)
+    assert L.ref_newhope_cpa_keypair(n, pk, sk, kp) == 0
+    assert L.ref_newhope_cpa_enc(n, ct, m, pk.raw, coins) == 0
+    assert L.ref_newhope_cpa_dec(n, m2, ct.raw, sk.raw) == 0
+    dump("ref_newhope1024_cpa.json", {
+        "source": "reference NewHope_NIST_GPU device code, host-compiled via oracle/build_ref.sh",
+        "n": n, "drbg_seed": s, "seed": kp.hex(), "m": m.hex(), "coins": coins.hex(),
+        "pk_sha256": [h(x) for x in chunks(pk.raw, 1824)],
+        "sk_sha256": [h(x) for x in chunks(sk.raw, 1792)],
+        "ct_sha256": [h(x) for x in chunks(ct.raw, 2176)],
+        "m_dec": m2.raw.hex(),
+        "pk0": pk.raw[:1824].hex(), "sk0": sk.raw[:1792].hex(), "ct0": ct.raw[:2176].hex(),
+    })
+
+
+def restated(name, alg, n, s):
+    sz = O.alg_sizes(alg)
+    seed = drbg.seed48(s)
+    kc = drbg.stream(seed, b"kp", n * sz["kp_coins"])
+    ec = drbg.stream(seed, b"enc", n * sz["enc_coins"])
+    pk, sk = O.batch_keypair(alg, n, kc)
+    ct, ss = O.batch_enc(alg, n, pk, ec)
+    ss2 = O.batch_dec(alg, n, ct, sk)
+    assert ss2 == ss
+    dump("restated_%s.json" % name, {
+        "source": "CPU oracle restatement (parity unpinned by reference outputs)",
+        "alg": name, "n": n, "drbg_seed": s,
+        "labels": {"keypair_coins": "kp", "enc_coins": "enc"},
+        "pk_sha256": [h(x) for x in chunks(pk, sz["pk"])],
+        "sk_sha256": [h(x) for x in chunks(sk, sz["sk"])],
+        "ct_sha256": [h(x) for x in chunks(ct, sz["ct"])],
+        "ss": ss.hex(),
+    })
+
+
+if __name__ == "__main__":
+    keccak()
+    for k in (2, 3, 4):
+        ref_kyber(k)
+    ref_newhope()
+    restated("kyber512", O.KYBER512, 16, 0)
+    restated("kyber768", O.KYBER768, 16, 0)
+    restated("kyber1024", O.KYBER1024, 16, 0)
+    restated("kyber1024r2", O.KYBER1024_R2, 16, 0)
+    restated("newhope1024", O.NEWHOPE1024, 16, 0)
+    restated("frodo976", O.FRODO976, 4, 0)
+    print("fixtures written to", HERE)

@@ -1,0 +1,101 @@
+"""CPU oracle pinned against the golden fixtures (hashlib and the reference's own code)."""
+import hashlib
+
+import pytest
+
+from conftest import load_golden
+from pqc_gb300 import drbg
+
+
+def sha(b):
+    return hashlib.sha256(b).hexdigest()
+
+
+def split(b, sz):
+    return [b[i * sz:(i + 1) * sz] for i in range(len(b) // sz)]
+
+
+def test_keccak_vectors(oracle):
+    g = load_golden("keccak.json")
+    for v in g["vectors"]:
+        data = bytes.fromhex(v["in"])
+        assert oracle.shake128(data, 256).hex() == v["shake128_256"]
+        assert oracle.shake256(data, 256).hex() == v["shake256_256"]
+        assert oracle.sha3_256(data).hex() == v["sha3_256"]
+        assert oracle.sha3_512(data).hex() == v["sha3_512"]
+
+
+@pytest.mark.parametrize("k", [2, 3, 4])
+def test_kyber_r2_cpa_matches_reference(oracle, k):
+    g = load_golden("ref_kyber_r2_k%d_cpa.json" % k)
+    d, m, coins = (bytes.fromhex(g[x]) for x in ("d", "m", "coins"))
+    for x in range(g["n"]):
+        pk, sk = oracle.kyber_indcpa_keypair(2, k, d[32 * x:32 * x + 32])
+        assert sha(pk) == g["pk_sha256"][x]
+        assert sha(sk) == g["sk_sha256"][x]
+        ct = oracle.kyber_indcpa_enc(2, k, m[32 * x:32 * x + 32], pk, coins[32 * x:32 * x + 32])
+        assert sha(ct) == g["ct_sha256"][x]
+        assert oracle.kyber_indcpa_dec(2, k, ct, sk).hex() == g["m_dec"][64 * x:64 * x + 64]
+        if x == 0:
+            assert (pk.hex(), sk.hex(), ct.hex()) == (g["pk0"], g["sk0"], g["ct0"])
+
+
+def test_newhope_cpa_matches_reference(oracle):
+    g = load_golden("ref_newhope1024_cpa.json")
+    seed, m, coins = (bytes.fromhex(g[x]) for x in ("seed", "m", "coins"))
+    for x in range(g["n"]):
+        pk, sk = oracle.newhope_cpapke_keypair(seed[32 * x:32 * x + 32])
+        assert sha(pk) == g["pk_sha256"][x]
+        assert sha(sk) == g["sk_sha256"][x]
+        ct = oracle.newhope_cpapke_enc(m[32 * x:32 * x + 32], pk, coins[32 * x:32 * x + 32])
+        assert sha(ct) == g["ct_sha256"][x]
+        assert oracle.newhope_cpapke_dec(ct, sk).hex() == g["m_dec"][64 * x:64 * x + 64]
+
+
+@pytest.mark.parametrize("name", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "newhope1024", "frodo976"])
+def test_restated_kem_vectors(oracle, name):
+    g = load_golden("restated_%s.json" % name)
+    alg = oracle.ALG_NAMES[name]
+    sz = oracle.alg_sizes(alg)
+    n = g["n"]
+    seed = drbg.seed48(g["drbg_seed"])
+    pk, sk = oracle.batch_keypair(alg, n, drbg.stream(seed, b"kp", n * sz["kp_coins"]))
+    ct, ss = oracle.batch_enc(alg, n, pk, drbg.stream(seed, b"enc", n * sz["enc_coins"]))
+    assert [sha(x) for x in split(pk, sz["pk"])] == g["pk_sha256"]
+    assert [sha(x) for x in split(sk, sz["sk"])] == g["sk_sha256"]
+    assert [sha(x) for x in split(ct, sz["ct"])] == g["ct_sha256"]
+    assert ss.hex() == g["ss"]
+    assert oracle.batch_dec(alg, n, ct, sk) == ss
+
+
+@pytest.mark.parametrize("name", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "frodo976"])
+def test_implicit_rejection(oracle, name):
+    """A tampered ciphertext decapsulates to a different key (Kyber / Frodo: the z / s fallback).
+    NewHope's CPA-KEM has no re-encryption check, so a small ciphertext change may decode to the
+    same message; it is not part of this test."""
+    alg = oracle.ALG_NAMES[name]
+    sz = oracle.alg_sizes(alg)
+    n = 2
+    seed = drbg.seed48(7)
+    pk, sk = oracle.batch_keypair(alg, n, drbg.stream(seed, b"kp", n * sz["kp_coins"]))
+    ct, ss = oracle.batch_enc(alg, n, pk, drbg.stream(seed, b"enc", n * sz["enc_coins"]))
+    bad = bytearray(ct)
+    bad[3] ^= 0x40
+    bad[2 * sz["ct"] - 1] ^= 0x01
+    ss2 = oracle.batch_dec(alg, n, bytes(bad), sk)
+    assert ss2[:sz["ss"]] != ss[:sz["ss"]]
+    assert ss2[sz["ss"]:] != ss[sz["ss"]:]
+    assert oracle.batch_dec(alg, n, ct, sk) == ss
+
+
+def test_work_counters(oracle):
+    """Kyber-768 encaps + decaps: permutation / butterfly counts used as the algorithmic work unit."""
+    sz = oracle.alg_sizes(oracle.KYBER768)
+    seed = drbg.seed48(0)
+    pk, sk = oracle.batch_keypair(oracle.KYBER768, 1, drbg.stream(seed, b"kp", sz["kp_coins"]), nthreads=1)
+    oracle.counters_reset()
+    ct, ss = oracle.batch_enc(oracle.KYBER768, 1, pk, drbg.stream(seed, b"enc", sz["enc_coins"]), nthreads=1)
+    oracle.batch_dec(oracle.KYBER768, 1, ct, sk, nthreads=1)
+    perms, bfly = oracle.counters()
+    assert 90 <= perms <= 110
+    assert bfly == (3 + 4 + 3 + 1 + 3 + 4) * 896
