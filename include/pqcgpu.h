@@ -1,0 +1,123 @@
+/*
+ * pqcgpu -- batched post-quantum KEMs on one NVIDIA GB300 (sm_103a).  C ABI.
+ *
+ * This header is the drop-in boundary for the reference's KEM path.  The reference exposes, per
+ * compile-time parameter set, the NIST/SUPERCOP API
+ *     int crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+ *     int crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+ *     int crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+ * (Kyber_GPU_Batched/api.h:18-22, FrodoKEM_GPU/api.h:20-24, sizes in the CRYPTO_* macros of
+ * Kyber_GPU_Batched/api.h:11-14, NewHope_NIST_GPU/api.h:11-14, FrodoKEM_GPU/api.h:11-14), and
+ * internally batched CPA entry points taking an instance count
+ *     indcpa_keypair / indcpa_enc / indcpa_dec(int COUNT, poly_set4*, ..., cudaStream_t)
+ *       (Kyber_GPU_Batched/indcpa.h:16-26)
+ *     cpapke_keypair / cpapke_enc / cpapke_dec(int COUNT, poly_set4*, ..., cudaStream_t)
+ *       (NewHope_NIST_GPU/cpapke.h:14-24).
+ * Here every parameter set lives in one library, selected at run time by pqcgpu_alg, and the
+ * batch count is an argument.
+ *
+ * Conventions (all functions):
+ *   - Return 0 (PQCGPU_OK) on success or a negative pqcgpu_status; never exit().
+ *   - Buffers are instance-major: instance i of an n-batch starts at i * <size>.
+ *   - Caller owns every buffer.  Without PQCGPU_DEVICE_PTRS the pointers are host memory
+ *     (pinned memory is fastest) and the call is synchronous.  With PQCGPU_DEVICE_PTRS they are
+ *     device pointers on the context's device and the call is asynchronous on the context stream
+ *     (pqcgpu_ctx_wait synchronises).
+ *   - Randomness is explicit: `coins` holds kp_coins / enc_coins bytes per instance (sizes from
+ *     pqcgpu_alg_sizes).  Passing coins == NULL draws them from the library's SHAKE-256 DRBG.
+ *   - A decapsulation whose re-encryption check fails is not an error: it returns 0 with the
+ *     implicit-rejection key, as the NIST API requires.
+ *   - A context may be used from several host threads; calls are serialised internally.
+ */
+#ifndef PQCGPU_H
+#define PQCGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PQCGPU_KYBER512 = 0,     /* round-3 Kyber-512:  k=2, eta1=3, eta2=2, du=10, dv=4 */
+    PQCGPU_KYBER768 = 1,     /* round-3 Kyber-768:  k=3, eta=2, du=10, dv=4 */
+    PQCGPU_KYBER1024 = 2,    /* round-3 Kyber-1024: k=4, eta=2, du=11, dv=5 */
+    PQCGPU_KYBER1024_R2 = 3, /* the reference's round-2 Kyber (Kyber_GPU_Batched/params.h), k=4 */
+    PQCGPU_NEWHOPE1024 = 4,  /* NewHope1024-CPAKEM (NewHope_NIST_GPU) */
+    PQCGPU_FRODO976 = 5,     /* FrodoKEM-976, SHAKE (FrodoKEM_GPU) */
+    PQCGPU_NUM_ALGS = 6
+} pqcgpu_alg;
+
+typedef enum {
+    PQCGPU_OK = 0,
+    PQCGPU_EINVAL = -1,      /* bad argument (unknown alg, null pointer, n out of range) */
+    PQCGPU_ENOMEM = -2,      /* device or pinned-host allocation failed */
+    PQCGPU_ECUDA = -3,       /* a CUDA call failed; pqcgpu_last_error() has the text */
+    PQCGPU_EBUDGET = -4,     /* the request does not fit the context's device-memory budget */
+    PQCGPU_ETIMEOUT = -5,    /* a bounded device-side wait gave up */
+    PQCGPU_EUNSUPPORTED = -6 /* operation not available for this algorithm / variant */
+} pqcgpu_status;
+
+/* flags */
+#define PQCGPU_DEVICE_PTRS 0x1u /* all buffer arguments are device pointers; asynchronous */
+#define PQCGPU_PLAIN 0x2u       /* use the plain per-stage path (one kernel per stage, thread per
+                                   instance, intermediates in HBM) instead of the fused path */
+
+typedef struct pqcgpu_ctx pqcgpu_ctx;
+
+/* ---- context lifecycle ----------------------------------------------------------------- */
+/* Create a context on `device` with a device-memory budget for its arena (0 = 4 GiB). */
+int pqcgpu_ctx_create(pqcgpu_ctx **out, int device, size_t hbm_budget_bytes);
+int pqcgpu_ctx_destroy(pqcgpu_ctx *ctx);
+/* Use an external cudaStream_t (passed as void*) instead of the context's own stream. */
+int pqcgpu_ctx_set_stream(pqcgpu_ctx *ctx, void *cuda_stream);
+void *pqcgpu_ctx_stream(pqcgpu_ctx *ctx);
+int pqcgpu_ctx_wait(pqcgpu_ctx *ctx);
+/* Number of kernels this context launched since creation (for launch accounting). */
+uint64_t pqcgpu_ctx_launches(pqcgpu_ctx *ctx);
+const char *pqcgpu_last_error(void);
+const char *pqcgpu_version(void);
+
+/* ---- sizes ------------------------------------------------------------------------------ */
+int pqcgpu_alg_sizes(pqcgpu_alg alg, size_t *pk, size_t *sk, size_t *ct, size_t *ss, size_t *kp_coins,
+                     size_t *enc_coins);
+
+/* ---- batched KEM (the batched extension of crypto_kem_*) ---------------------------------- */
+int pqcgpu_kem_keypair_batch(pqcgpu_ctx *ctx, pqcgpu_alg alg, size_t n, uint8_t *pk, uint8_t *sk,
+                             const uint8_t *coins, unsigned flags);
+int pqcgpu_kem_enc_batch(pqcgpu_ctx *ctx, pqcgpu_alg alg, size_t n, uint8_t *ct, uint8_t *ss, const uint8_t *pk,
+                         const uint8_t *coins, unsigned flags);
+int pqcgpu_kem_dec_batch(pqcgpu_ctx *ctx, pqcgpu_alg alg, size_t n, uint8_t *ss, const uint8_t *ct,
+                         const uint8_t *sk, unsigned flags);
+
+/* ---- batched CPA-PKE (replaces indcpa_* of Kyber_GPU_Batched/indcpa.h:16-26) -------------
+ * variant 2 = the reference's round-2 arithmetic, variant 3 = round-3 parameter sets; k = 2..4.
+ * keypair: d = 32 bytes per instance; pk = KYBER_INDCPA_PUBLICKEYBYTES, sk = K*384.
+ * enc: m and coins 32 bytes per instance.  dec: m out 32 bytes per instance. */
+int pqcgpu_kyber_indcpa_keypair_batch(pqcgpu_ctx *ctx, int variant, int k, size_t n, uint8_t *pk, uint8_t *sk,
+                                      const uint8_t *d, unsigned flags);
+int pqcgpu_kyber_indcpa_enc_batch(pqcgpu_ctx *ctx, int variant, int k, size_t n, uint8_t *ct, const uint8_t *m,
+                                  const uint8_t *pk, const uint8_t *coins, unsigned flags);
+int pqcgpu_kyber_indcpa_dec_batch(pqcgpu_ctx *ctx, int variant, int k, size_t n, uint8_t *m, const uint8_t *ct,
+                                  const uint8_t *sk, unsigned flags);
+
+/* ---- NIST single-instance API per parameter set (crypto_kem_* of each api.h) -------------
+ * Randomness comes from the library DRBG (pqcgpu_randombytes_init); device 0, default context. */
+int pqcgpu_randombytes_init(const uint8_t seed[48]);
+int pqcgpu_randombytes(uint8_t *out, size_t n);
+
+int pqcgpu_kyber512_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+int pqcgpu_kyber512_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+int pqcgpu_kyber512_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+int pqcgpu_kyber768_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+int pqcgpu_kyber768_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+int pqcgpu_kyber768_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+int pqcgpu_kyber1024_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+int pqcgpu_kyber1024_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+int pqcgpu_kyber1024_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,61 @@
+"""Loader for the in-tree native library pqc_gb300/_build/libpqcgpu.so (C ABI: include/pqcgpu.h).
+
+There is no fallback: if the library is missing or cannot be loaded, every call raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpqcgpu.so")
+
+# Every symbol declared in include/pqcgpu.h with its ctypes signature (restype, argtypes).
+_c = ctypes
+_vp, _sz, _u8p, _int, _uint = _c.c_void_p, _c.c_size_t, _c.c_void_p, _c.c_int, _c.c_uint
+SIGNATURES = {
+    "pqcgpu_ctx_create": (_int, [_c.POINTER(_vp), _int, _sz]),
+    "pqcgpu_ctx_destroy": (_int, [_vp]),
+    "pqcgpu_ctx_set_stream": (_int, [_vp, _vp]),
+    "pqcgpu_ctx_stream": (_vp, [_vp]),
+    "pqcgpu_ctx_wait": (_int, [_vp]),
+    "pqcgpu_ctx_launches": (_c.c_uint64, [_vp]),
+    "pqcgpu_last_error": (_c.c_char_p, []),
+    "pqcgpu_version": (_c.c_char_p, []),
+    "pqcgpu_alg_sizes": (_int, [_int] + [_c.POINTER(_sz)] * 6),
+    "pqcgpu_kem_keypair_batch": (_int, [_vp, _int, _sz, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_kem_enc_batch": (_int, [_vp, _int, _sz, _u8p, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_kem_dec_batch": (_int, [_vp, _int, _sz, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_kyber_indcpa_keypair_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_kyber_indcpa_enc_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_kyber_indcpa_dec_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_randombytes_init": (_int, [_u8p]),
+    "pqcgpu_randombytes": (_int, [_u8p, _sz]),
+}
+for _alg in ("kyber512", "kyber768", "kyber1024"):
+    SIGNATURES["pqcgpu_%s_crypto_kem_keypair" % _alg] = (_int, [_u8p, _u8p])
+    SIGNATURES["pqcgpu_%s_crypto_kem_enc" % _alg] = (_int, [_u8p, _u8p, _u8p])
+    SIGNATURES["pqcgpu_%s_crypto_kem_dec" % _alg] = (_int, [_u8p, _u8p, _u8p])
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load (once) and return the ctypes library; raises if it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libpqcgpu.so is not built (%s); run __graft_entry__.build() or "
+                           "python pqc_gb300/build.py" % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc != 0:
+        raise RuntimeError("pqcgpu error %d: %s" % (rc, load().pqcgpu_last_error().decode()))
+    return rc

@@ -1,0 +1,577 @@
+// C ABI of libpqcgpu: contexts, the device arena, host-buffer staging, the DRBG and the NIST
+// single-instance entry points.  Declarations and conventions: include/pqcgpu.h.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <atomic>
+#include <mutex>
+#include <string>
+
+#include "pqcgpu_internal.h"
+
+namespace pqc {
+std::atomic<uint64_t> g_launch_count{0};
+}
+
+using namespace pqc;
+
+static thread_local std::string g_last_error;
+static int set_err(int code, const char *what) {
+    g_last_error = what;
+    return code;
+}
+static int cuda_err(cudaError_t e, const char *where) {
+    if (e == cudaSuccess) return PQCGPU_OK;
+    g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return PQCGPU_ECUDA;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Host SHAKE-256 (for the DRBG only; all batch hashing runs on the GPU)
+// ---------------------------------------------------------------------------------------------
+namespace {
+struct HostShake {
+    uint64_t s[25];
+    unsigned pos;  // squeeze position within the current block
+    static uint64_t rol(uint64_t v, int n) { return n ? (v << n) | (v >> (64 - n)) : v; }
+    static void permute(uint64_t A[25]) {
+        static uint64_t RC[24];
+        static int R[25];
+        static bool init = false;
+        if (!init) {
+            uint2 rc[24];
+            // same LFSR as the device table
+            for (int ir = 0; ir < 24; ir++) {
+                unsigned long long v = 0;
+                for (int j = 0; j <= 6; j++) {
+                    const int t = j + 7 * ir;
+                    int bit = 1;
+                    if (t % 255) {
+                        int Rr[9] = {1, 0, 0, 0, 0, 0, 0, 0, 0};
+                        for (int i = 1; i <= t % 255; i++) {
+                            int Rn[9];
+                            Rn[0] = 0;
+                            for (int b = 0; b < 8; b++) Rn[b + 1] = Rr[b];
+                            Rn[0] ^= Rn[8];
+                            Rn[4] ^= Rn[8];
+                            Rn[5] ^= Rn[8];
+                            Rn[6] ^= Rn[8];
+                            for (int b = 0; b < 9; b++) Rr[b] = Rn[b];
+                        }
+                        bit = Rr[0];
+                    }
+                    if (bit) v |= 1ULL << ((1u << j) - 1);
+                }
+                rc[ir] = make_uint2((unsigned)v, (unsigned)(v >> 32));
+                RC[ir] = v;
+            }
+            R[0] = 0;
+            int x = 1, y = 0;
+            for (int t = 0; t < 24; t++) {
+                R[x + 5 * y] = ((t + 1) * (t + 2) / 2) % 64;
+                const int nx = y, ny = (2 * x + 3 * y) % 5;
+                x = nx;
+                y = ny;
+            }
+            (void)rc;
+            init = true;
+        }
+        for (int ir = 0; ir < 24; ir++) {
+            uint64_t C[5], D[5], B[25];
+            for (int i = 0; i < 5; i++) C[i] = A[i] ^ A[i + 5] ^ A[i + 10] ^ A[i + 15] ^ A[i + 20];
+            for (int i = 0; i < 5; i++) D[i] = C[(i + 4) % 5] ^ rol(C[(i + 1) % 5], 1);
+            for (int i = 0; i < 25; i++) A[i] ^= D[i % 5];
+            for (int xx = 0; xx < 5; xx++)
+                for (int yy = 0; yy < 5; yy++) B[yy + 5 * ((2 * xx + 3 * yy) % 5)] = rol(A[xx + 5 * yy], R[xx + 5 * yy]);
+            for (int yy = 0; yy < 5; yy++)
+                for (int xx = 0; xx < 5; xx++)
+                    A[xx + 5 * yy] = B[xx + 5 * yy] ^ (~B[(xx + 1) % 5 + 5 * yy] & B[(xx + 2) % 5 + 5 * yy]);
+            A[0] ^= RC[ir];
+        }
+    }
+    void init(const uint8_t *in, size_t len) {
+        memset(s, 0, sizeof s);
+        uint8_t blk[136];
+        while (len >= 136) {
+            for (int i = 0; i < 17; i++) {
+                uint64_t w = 0;
+                for (int b = 0; b < 8; b++) w |= (uint64_t)in[8 * i + b] << (8 * b);
+                s[i] ^= w;
+            }
+            permute(s);
+            in += 136;
+            len -= 136;
+        }
+        memset(blk, 0, sizeof blk);
+        memcpy(blk, in, len);
+        blk[len] ^= 0x1F;
+        blk[135] ^= 0x80;
+        for (int i = 0; i < 17; i++) {
+            uint64_t w = 0;
+            for (int b = 0; b < 8; b++) w |= (uint64_t)blk[8 * i + b] << (8 * b);
+            s[i] ^= w;
+        }
+        pos = 136;
+    }
+    void squeeze(uint8_t *out, size_t n) {
+        while (n) {
+            if (pos == 136) {
+                permute(s);
+                pos = 0;
+            }
+            const size_t take = (n < 136 - pos) ? n : 136 - pos;
+            for (size_t i = 0; i < take; i++) out[i] = (uint8_t)(s[(pos + i) / 8] >> (8 * ((pos + i) % 8)));
+            pos += (unsigned)take;
+            out += take;
+            n -= take;
+        }
+    }
+};
+
+std::mutex g_drbg_mu;
+HostShake g_drbg;
+bool g_drbg_seeded = false;
+
+void drbg_bytes(uint8_t *out, size_t n) {
+    std::lock_guard<std::mutex> lk(g_drbg_mu);
+    if (!g_drbg_seeded) {
+        uint8_t seed[48] = {0};
+        FILE *f = fopen("/dev/urandom", "rb");
+        if (f) {
+            size_t got = fread(seed, 1, sizeof seed, f);
+            (void)got;
+            fclose(f);
+        }
+        g_drbg.init(seed, sizeof seed);
+        g_drbg_seeded = true;
+    }
+    g_drbg.squeeze(out, n);
+}
+
+struct AlgInfo {
+    size_t pk, sk, ct, ss, kpc, encc;
+};
+bool alg_info(int alg, AlgInfo *a) {
+    switch (alg) {
+    case PQCGPU_KYBER512: *a = {800, 1632, 768, 32, 64, 32}; return true;
+    case PQCGPU_KYBER768: *a = {1184, 2400, 1088, 32, 64, 32}; return true;
+    case PQCGPU_KYBER1024: *a = {1568, 3168, 1568, 32, 64, 32}; return true;
+    case PQCGPU_KYBER1024_R2: *a = {1568, 3168, 1568, 32, 64, 32}; return true;
+    case PQCGPU_NEWHOPE1024: *a = {1824, 1792, 2176, 32, 32, 32}; return true;
+    case PQCGPU_FRODO976: *a = {15632, 31296, 15744, 24, 64, 24}; return true;
+    default: return false;
+    }
+}
+bool kyber_alg(int alg, int *variant, int *k) {
+    switch (alg) {
+    case PQCGPU_KYBER512: *variant = 3; *k = 2; return true;
+    case PQCGPU_KYBER768: *variant = 3; *k = 3; return true;
+    case PQCGPU_KYBER1024: *variant = 3; *k = 4; return true;
+    case PQCGPU_KYBER1024_R2: *variant = 2; *k = 4; return true;
+    default: return false;
+    }
+}
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------------------------
+struct pqcgpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t side[2] = {nullptr, nullptr};  // pipelining streams for host-buffer calls
+    bool own_stream = true;
+    size_t budget = 0;
+    uint8_t *arena = nullptr;
+    size_t arena_size = 0;
+    uint64_t launches_at_create = 0;
+    std::recursive_mutex mu;
+
+    // Arena: one device allocation, grown on demand within the budget; sub-buffers are carved
+    // per call (calls on a context are serialised, so a call owns the whole arena).
+    int reserve(size_t bytes) {
+        if (bytes <= arena_size) return PQCGPU_OK;
+        if (bytes > budget) return set_err(PQCGPU_EBUDGET, "request exceeds the context's device-memory budget");
+        if (arena) {
+            cudaStreamSynchronize(stream);
+            for (auto s : side) cudaStreamSynchronize(s);
+            cudaFree(arena);
+            arena = nullptr;
+            arena_size = 0;
+        }
+        size_t want = bytes + bytes / 4;
+        if (want > budget) want = budget;
+        if (cudaMalloc(&arena, want) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(PQCGPU_ENOMEM, "cudaMalloc of the context arena failed");
+        }
+        arena_size = want;
+        return PQCGPU_OK;
+    }
+};
+
+static bool g_constants_ready[64];
+static std::mutex g_init_mu;
+
+static int ensure_device_init(int device) {
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (device < 0 || device >= 64) return set_err(PQCGPU_EINVAL, "bad device");
+    if (g_constants_ready[device]) return PQCGPU_OK;
+    int rc = kyber_init_constants();
+    if (rc) return set_err(rc, "uploading Kyber constants failed");
+    g_constants_ready[device] = true;
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_ctx_create(pqcgpu_ctx **out, int device, size_t budget) {
+    if (!out) return set_err(PQCGPU_EINVAL, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_err(PQCGPU_ECUDA, "no CUDA device available");
+    }
+    if (device < 0 || device >= ndev) return set_err(PQCGPU_EINVAL, "device index out of range");
+    int rc = cuda_err(cudaSetDevice(device), "cudaSetDevice");
+    if (rc) return rc;
+    rc = ensure_device_init(device);
+    if (rc) return rc;
+    pqcgpu_ctx *c = new pqcgpu_ctx();
+    c->device = device;
+    c->budget = budget ? budget : ((size_t)4 << 30);
+    if ((rc = cuda_err(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream")) ||
+        (rc = cuda_err(cudaStreamCreateWithFlags(&c->side[0], cudaStreamNonBlocking), "stream")) ||
+        (rc = cuda_err(cudaStreamCreateWithFlags(&c->side[1], cudaStreamNonBlocking), "stream"))) {
+        delete c;
+        return rc;
+    }
+    c->launches_at_create = g_launch_count.load();
+    *out = c;
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_ctx_destroy(pqcgpu_ctx *c) {
+    if (!c) return PQCGPU_EINVAL;
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    if (c->arena) cudaFree(c->arena);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    for (auto s : c->side)
+        if (s) cudaStreamDestroy(s);
+    delete c;
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_ctx_set_stream(pqcgpu_ctx *c, void *s) {
+    if (!c) return PQCGPU_EINVAL;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    c->stream = (cudaStream_t)s;
+    c->own_stream = false;
+    return PQCGPU_OK;
+}
+extern "C" void *pqcgpu_ctx_stream(pqcgpu_ctx *c) { return c ? (void *)c->stream : nullptr; }
+extern "C" int pqcgpu_ctx_wait(pqcgpu_ctx *c) {
+    if (!c) return PQCGPU_EINVAL;
+    return cuda_err(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+}
+extern "C" uint64_t pqcgpu_ctx_launches(pqcgpu_ctx *c) { return c ? g_launch_count.load() - c->launches_at_create : 0; }
+extern "C" const char *pqcgpu_last_error(void) { return g_last_error.c_str(); }
+extern "C" const char *pqcgpu_version(void) { return "pqcgpu 0.1 (sm_103a)"; }
+
+extern "C" int pqcgpu_alg_sizes(pqcgpu_alg alg, size_t *pk, size_t *sk, size_t *ct, size_t *ss, size_t *kpc,
+                                size_t *encc) {
+    AlgInfo a;
+    if (!alg_info(alg, &a)) return set_err(PQCGPU_EINVAL, "unknown algorithm");
+    if (pk) *pk = a.pk;
+    if (sk) *sk = a.sk;
+    if (ct) *ct = a.ct;
+    if (ss) *ss = a.ss;
+    if (kpc) *kpc = a.kpc;
+    if (encc) *encc = a.encc;
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_randombytes_init(const uint8_t seed[48]) {
+    if (!seed) return PQCGPU_EINVAL;
+    std::lock_guard<std::mutex> lk(g_drbg_mu);
+    g_drbg.init(seed, 48);
+    g_drbg_seeded = true;
+    return PQCGPU_OK;
+}
+extern "C" int pqcgpu_randombytes(uint8_t *out, size_t n) {
+    if (!out && n) return PQCGPU_EINVAL;
+    drbg_bytes(out, n);
+    return PQCGPU_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Operation plumbing.  An op is described by its per-instance input / output sizes and a device
+// function over a contiguous chunk; the host-buffer path pipelines chunks over two streams
+// (H2D of chunk c+1 overlaps the kernels of chunk c and the D2H of chunk c-1).
+// ---------------------------------------------------------------------------------------------
+namespace {
+constexpr int MAXIO = 3;
+struct OpDesc {
+    int nin = 0, nout = 0;
+    const uint8_t *in[MAXIO];
+    size_t in_sz[MAXIO];
+    uint8_t *out[MAXIO];
+    size_t out_sz[MAXIO];
+    size_t scratch_per = 0;
+};
+// run(n, din[], dout[], scratch, stream)
+template <class Run>
+int run_op(pqcgpu_ctx *c, size_t n, const OpDesc &d, unsigned flags, Run run) {
+    if (n == 0) return PQCGPU_OK;
+    if (n > (size_t)1 << 30) return set_err(PQCGPU_EINVAL, "batch too large");
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    int rc = cuda_err(cudaSetDevice(c->device), "cudaSetDevice");
+    if (rc) return rc;
+    for (int i = 0; i < d.nin; i++)
+        if (!d.in[i]) return set_err(PQCGPU_EINVAL, "null input buffer");
+    for (int i = 0; i < d.nout; i++)
+        if (!d.out[i]) return set_err(PQCGPU_EINVAL, "null output buffer");
+    if (flags & PQCGPU_DEVICE_PTRS) {
+        for (int i = 0; i < d.nin; i++)
+            if ((uintptr_t)d.in[i] & 15) return set_err(PQCGPU_EINVAL, "device buffers must be 16-byte aligned");
+        for (int i = 0; i < d.nout; i++)
+            if ((uintptr_t)d.out[i] & 15) return set_err(PQCGPU_EINVAL, "device buffers must be 16-byte aligned");
+        const size_t need = d.scratch_per * n + 256;
+        if ((rc = c->reserve(need))) return rc;
+        rc = run((int)n, d.in, d.out, c->arena, c->stream);
+        if (rc) return rc;
+        return cuda_err(cudaGetLastError(), "kernel launch");
+    }
+    // host buffers: chunked, double-buffered pipeline on the two side streams
+    auto r256 = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t chunk = n < 16384 ? n : 16384;
+    const int nbuf = (n > chunk) ? 2 : 1;
+    size_t set_bytes = r256(d.scratch_per * chunk);
+    for (int i = 0; i < d.nin; i++) set_bytes += r256(d.in_sz[i] * chunk);
+    for (int i = 0; i < d.nout; i++) set_bytes += r256(d.out_sz[i] * chunk);
+    if ((rc = c->reserve(set_bytes * nbuf))) return rc;
+    cudaEvent_t ev;
+    cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    cudaEventRecord(ev, c->stream);  // order after prior work on the main stream
+    for (auto s : c->side) cudaStreamWaitEvent(s, ev, 0);
+    for (size_t off = 0, ci = 0; off < n; off += chunk, ci++) {
+        const size_t m = (n - off < chunk) ? n - off : chunk;
+        cudaStream_t s = c->side[ci % 2];
+        uint8_t *p = c->arena + (size_t)(ci % nbuf) * set_bytes;
+        const uint8_t *din[MAXIO];
+        uint8_t *dout[MAXIO];
+        for (int i = 0; i < d.nin; i++) {
+            uint8_t *q = p;
+            p += r256(d.in_sz[i] * chunk);
+            if ((rc = cuda_err(cudaMemcpyAsync(q, d.in[i] + off * d.in_sz[i], m * d.in_sz[i], cudaMemcpyHostToDevice, s),
+                               "H2D")))
+                break;
+            din[i] = q;
+        }
+        if (rc) break;
+        for (int i = 0; i < d.nout; i++) {
+            dout[i] = p;
+            p += r256(d.out_sz[i] * chunk);
+        }
+        uint8_t *scratch = p;
+        if ((rc = run((int)m, din, dout, scratch, s))) break;
+        for (int i = 0; i < d.nout; i++)
+            if ((rc = cuda_err(cudaMemcpyAsync(d.out[i] + off * d.out_sz[i], dout[i], m * d.out_sz[i],
+                                               cudaMemcpyDeviceToHost, s),
+                               "D2H")))
+                break;
+        if (rc) break;
+    }
+    cudaError_t e1 = cudaStreamSynchronize(c->side[0]);
+    cudaError_t e2 = cudaStreamSynchronize(c->side[1]);
+    cudaEventDestroy(ev);
+    if (rc) return rc;
+    if ((rc = cuda_err(e1, "sync"))) return rc;
+    if ((rc = cuda_err(e2, "sync"))) return rc;
+    return cuda_err(cudaGetLastError(), "kernel");
+}
+
+// coins == NULL: draw from the DRBG into a host buffer (or a temporary device copy)
+struct CoinsHolder {
+    uint8_t *host = nullptr;
+    ~CoinsHolder() { free(host); }
+};
+}  // namespace
+
+static int coins_or_drbg(pqcgpu_ctx *c, const uint8_t *&coins, size_t bytes, unsigned &flags, CoinsHolder &h,
+                         const uint8_t **others, int nothers) {
+    (void)c;
+    (void)others;
+    (void)nothers;
+    if (coins) return PQCGPU_OK;
+    if (flags & PQCGPU_DEVICE_PTRS)
+        return set_err(PQCGPU_EINVAL, "coins == NULL needs host buffers (or pass device coins)");
+    h.host = (uint8_t *)malloc(bytes ? bytes : 1);
+    if (!h.host) return set_err(PQCGPU_ENOMEM, "malloc");
+    drbg_bytes(h.host, bytes);
+    coins = h.host;
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_kem_keypair_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uint8_t *pk, uint8_t *sk,
+                                        const uint8_t *coins, unsigned flags) {
+    AlgInfo ai;
+    if (!c || !alg_info(alg, &ai)) return set_err(PQCGPU_EINVAL, "bad context or algorithm");
+    CoinsHolder h;
+    int rc = coins_or_drbg(c, coins, n * ai.kpc, flags, h, nullptr, 0);
+    if (rc) return rc;
+    int variant, k;
+    if (kyber_alg(alg, &variant, &k)) {
+        OpDesc d;
+        d.nin = 1;
+        d.in[0] = coins;
+        d.in_sz[0] = ai.kpc;
+        d.nout = 2;
+        d.out[0] = pk;
+        d.out_sz[0] = ai.pk;
+        d.out[1] = sk;
+        d.out_sz[1] = ai.sk;
+        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
+            return kyber_keypair_dev(variant, k, m, out[0], out[1], in[0], (int)ai.kpc, 1, s);
+        });
+    }
+    return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
+}
+
+extern "C" int pqcgpu_kem_enc_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uint8_t *ct, uint8_t *ss,
+                                    const uint8_t *pk, const uint8_t *coins, unsigned flags) {
+    AlgInfo ai;
+    if (!c || !alg_info(alg, &ai)) return set_err(PQCGPU_EINVAL, "bad context or algorithm");
+    CoinsHolder h;
+    int rc = coins_or_drbg(c, coins, n * ai.encc, flags, h, nullptr, 0);
+    if (rc) return rc;
+    int variant, k;
+    if (kyber_alg(alg, &variant, &k)) {
+        OpDesc d;
+        d.nin = 2;
+        d.in[0] = pk;
+        d.in_sz[0] = ai.pk;
+        d.in[1] = coins;
+        d.in_sz[1] = ai.encc;
+        d.nout = 2;
+        d.out[0] = ct;
+        d.out_sz[0] = ai.ct;
+        d.out[1] = ss;
+        d.out_sz[1] = ai.ss;
+        d.scratch_per = 96;
+        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
+            return kyber_enc_dev(variant, k, m, out[0], out[1], in[0], nullptr, in[1], scr, 1, s);
+        });
+    }
+    return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
+}
+
+extern "C" int pqcgpu_kem_dec_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uint8_t *ss, const uint8_t *ct,
+                                    const uint8_t *sk, unsigned flags) {
+    AlgInfo ai;
+    if (!c || !alg_info(alg, &ai)) return set_err(PQCGPU_EINVAL, "bad context or algorithm");
+    int variant, k;
+    if (kyber_alg(alg, &variant, &k)) {
+        OpDesc d;
+        d.nin = 2;
+        d.in[0] = ct;
+        d.in_sz[0] = ai.ct;
+        d.in[1] = sk;
+        d.in_sz[1] = ai.sk;
+        d.nout = 1;
+        d.out[0] = ss;
+        d.out_sz[0] = ai.ss;
+        d.scratch_per = 32;
+        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
+            return kyber_dec_dev(variant, k, m, out[0], in[0], in[1], scr, 1, s);
+        });
+    }
+    return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
+}
+
+// ---- CPA level ----
+static bool kyber_vk_ok(int variant, int k) { return (variant == 2 || variant == 3) && k >= 2 && k <= 4; }
+static size_t kyber_cpa_ct(int variant, int k) {
+    const int du = (variant == 2 || k == 4) ? 11 : 10, dv = (variant == 2 || k == 4) ? 5 : 4;
+    return (size_t)k * du * 32 + (size_t)dv * 32;
+}
+
+extern "C" int pqcgpu_kyber_indcpa_keypair_batch(pqcgpu_ctx *c, int variant, int k, size_t n, uint8_t *pk,
+                                                 uint8_t *sk, const uint8_t *dseed, unsigned flags) {
+    if (!c || !kyber_vk_ok(variant, k)) return set_err(PQCGPU_EINVAL, "bad context, variant or k");
+    OpDesc d;
+    d.nin = 1;
+    d.in[0] = dseed;
+    d.in_sz[0] = 32;
+    d.nout = 2;
+    d.out[0] = pk;
+    d.out_sz[0] = 384 * k + 32;
+    d.out[1] = sk;
+    d.out_sz[1] = 384 * k;
+    return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
+        return kyber_keypair_dev(variant, k, m, out[0], out[1], in[0], 32, 0, s);
+    });
+}
+extern "C" int pqcgpu_kyber_indcpa_enc_batch(pqcgpu_ctx *c, int variant, int k, size_t n, uint8_t *ct,
+                                             const uint8_t *msg, const uint8_t *pk, const uint8_t *coins,
+                                             unsigned flags) {
+    if (!c || !kyber_vk_ok(variant, k)) return set_err(PQCGPU_EINVAL, "bad context, variant or k");
+    OpDesc d;
+    d.nin = 3;
+    d.in[0] = pk;
+    d.in_sz[0] = 384 * k + 32;
+    d.in[1] = msg;
+    d.in_sz[1] = 32;
+    d.in[2] = coins;
+    d.in_sz[2] = 32;
+    d.nout = 1;
+    d.out[0] = ct;
+    d.out_sz[0] = kyber_cpa_ct(variant, k);
+    return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
+        return kyber_enc_dev(variant, k, m, out[0], nullptr, in[0], in[1], in[2], nullptr, 0, s);
+    });
+}
+extern "C" int pqcgpu_kyber_indcpa_dec_batch(pqcgpu_ctx *c, int variant, int k, size_t n, uint8_t *msg,
+                                             const uint8_t *ct, const uint8_t *sk, unsigned flags) {
+    if (!c || !kyber_vk_ok(variant, k)) return set_err(PQCGPU_EINVAL, "bad context, variant or k");
+    OpDesc d;
+    d.nin = 2;
+    d.in[0] = ct;
+    d.in_sz[0] = kyber_cpa_ct(variant, k);
+    d.in[1] = sk;
+    d.in_sz[1] = 384 * k;
+    d.nout = 1;
+    d.out[0] = msg;
+    d.out_sz[0] = 32;
+    return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
+        return kyber_dec_dev(variant, k, m, out[0], in[0], in[1], nullptr, 0, s);
+    });
+}
+
+// ---- NIST single-instance API (default context on device 0) ----
+static pqcgpu_ctx *g_default_ctx = nullptr;
+static std::mutex g_default_mu;
+static pqcgpu_ctx *default_ctx() {
+    std::lock_guard<std::mutex> lk(g_default_mu);
+    if (!g_default_ctx) pqcgpu_ctx_create(&g_default_ctx, 0, (size_t)256 << 20);
+    return g_default_ctx;
+}
+#define PQC_NIST(NAME, ALG)                                                                              \
+    extern "C" int pqcgpu_##NAME##_crypto_kem_keypair(unsigned char *pk, unsigned char *sk) {             \
+        pqcgpu_ctx *c = default_ctx();                                                                   \
+        return c ? pqcgpu_kem_keypair_batch(c, ALG, 1, pk, sk, nullptr, 0) : PQCGPU_ECUDA;               \
+    }                                                                                                    \
+    extern "C" int pqcgpu_##NAME##_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk) { \
+        pqcgpu_ctx *c = default_ctx();                                                                   \
+        return c ? pqcgpu_kem_enc_batch(c, ALG, 1, ct, ss, pk, nullptr, 0) : PQCGPU_ECUDA;               \
+    }                                                                                                    \
+    extern "C" int pqcgpu_##NAME##_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk) { \
+        pqcgpu_ctx *c = default_ctx();                                                                   \
+        return c ? pqcgpu_kem_dec_batch(c, ALG, 1, ss, ct, sk, 0) : PQCGPU_ECUDA;                        \
+    }
+PQC_NIST(kyber512, PQCGPU_KYBER512)
+PQC_NIST(kyber768, PQCGPU_KYBER768)
+PQC_NIST(kyber1024, PQCGPU_KYBER1024)

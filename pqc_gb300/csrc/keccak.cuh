@@ -1,0 +1,151 @@
+// Keccak-f[1600] and FIPS-202 sponges for sm_103a, one state per thread, all 25 lanes held in
+// registers as 32-bit halves (uint2 {lo, hi}).
+//
+// Same function as the reference permutation (Kyber_GPU_Batched/fips202.cu:393-447) and sponge
+// (:462-689), laid out for the GPU integer pipe instead of a rolled loop over a local array:
+//   theta parity and chi are single LOP3 instructions (0x96 = a^b^c, 0xD2 = a^(~b&c)),
+//   rho is two funnel shifts (SHF.L.W) per lane, pi is pure register renaming,
+//   the round constants sit in constant memory (uniform access).
+// Every index into the state is a compile-time constant after unrolling, so the state never
+// touches local memory (checked with -Xptxas -v: 0 bytes stack).
+#pragma once
+#include <stdint.h>
+
+namespace pqc {
+
+__device__ __forceinline__ uint32_t lop3_xor3(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t r;
+    asm("lop3.b32 %0, %1, %2, %3, 0x96;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+    return r;
+}
+// a ^ (~b & c)
+__device__ __forceinline__ uint32_t lop3_chi(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t r;
+    asm("lop3.b32 %0, %1, %2, %3, 0xD2;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+    return r;
+}
+
+__device__ __forceinline__ uint2 xor2(uint2 a, uint2 b) { return make_uint2(a.x ^ b.x, a.y ^ b.y); }
+
+// 64-bit rotate-left of {lo, hi} by a compile-time-known n (0..63) via funnel shifts.
+__device__ __forceinline__ uint2 rotl64(uint2 v, const int n) {
+    if (n == 0) return v;
+    if (n == 32) return make_uint2(v.y, v.x);
+    if (n < 32) return make_uint2(__funnelshift_l(v.y, v.x, n), __funnelshift_l(v.x, v.y, n));
+    return make_uint2(__funnelshift_l(v.x, v.y, n - 32), __funnelshift_l(v.y, v.x, n - 32));
+}
+
+// Rotation offsets r[x + 5y] (FIPS 202 Algorithm 2).
+__device__ __forceinline__ constexpr int keccak_rho(int i) {
+    constexpr int R[25] = {0, 1, 62, 28, 27, 36, 44, 6, 55, 20, 3, 10, 43, 25, 39,
+                           41, 45, 15, 21, 8, 18, 2, 61, 56, 14};
+    return R[i];
+}
+
+// Per translation unit; each .cu that includes this header uploads the table in its init function.
+static __constant__ uint2 c_keccak_rc[24];
+
+// Round constants from the rc(t) LFSR of FIPS 202 Algorithm 5 (host side, used at init).
+static inline void keccak_rc_host(uint2 out[24]) {
+    for (int ir = 0; ir < 24; ir++) {
+        unsigned long long rc = 0;
+        for (int j = 0; j <= 6; j++) {
+            const int t = j + 7 * ir;
+            int bit;
+            if (t % 255 == 0) {
+                bit = 1;
+            } else {
+                int R[9] = {1, 0, 0, 0, 0, 0, 0, 0, 0};
+                for (int i = 1; i <= t % 255; i++) {
+                    int Rn[9];
+                    Rn[0] = 0;
+                    for (int b = 0; b < 8; b++) Rn[b + 1] = R[b];
+                    Rn[0] ^= Rn[8];
+                    Rn[4] ^= Rn[8];
+                    Rn[5] ^= Rn[8];
+                    Rn[6] ^= Rn[8];
+                    for (int b = 0; b < 9; b++) R[b] = Rn[b];
+                }
+                bit = R[0];
+            }
+            if (bit) rc |= 1ULL << ((1u << j) - 1);
+        }
+        out[ir] = make_uint2((unsigned)(rc & 0xffffffffu), (unsigned)(rc >> 32));
+    }
+}
+
+// One round: theta, rho+pi into B, chi back into A, iota.
+__device__ __forceinline__ void keccak_round(uint2 (&A)[25], const uint2 rc) {
+    uint2 C[5], D[5], B[25];
+#pragma unroll
+    for (int x = 0; x < 5; x++) {
+        C[x].x = lop3_xor3(lop3_xor3(A[x].x, A[x + 5].x, A[x + 10].x), A[x + 15].x, A[x + 20].x);
+        C[x].y = lop3_xor3(lop3_xor3(A[x].y, A[x + 5].y, A[x + 10].y), A[x + 15].y, A[x + 20].y);
+    }
+#pragma unroll
+    for (int x = 0; x < 5; x++) D[x] = xor2(C[(x + 4) % 5], rotl64(C[(x + 1) % 5], 1));
+    // pi: B[X][Y] = rot(A[(X + 3Y) % 5][X]) -- output lane (X, Y) takes input lane (x, y) with
+    // X = y, Y = 2x + 3y.
+#pragma unroll
+    for (int Y = 0; Y < 5; Y++)
+#pragma unroll
+        for (int X = 0; X < 5; X++) {
+            const int sx = (X + 3 * Y) % 5, sy = X;
+            B[X + 5 * Y] = rotl64(xor2(A[sx + 5 * sy], D[sx]), keccak_rho(sx + 5 * sy));
+        }
+#pragma unroll
+    for (int Y = 0; Y < 5; Y++)
+#pragma unroll
+        for (int X = 0; X < 5; X++) {
+            A[X + 5 * Y].x = lop3_chi(B[X + 5 * Y].x, B[(X + 1) % 5 + 5 * Y].x, B[(X + 2) % 5 + 5 * Y].x);
+            A[X + 5 * Y].y = lop3_chi(B[X + 5 * Y].y, B[(X + 1) % 5 + 5 * Y].y, B[(X + 2) % 5 + 5 * Y].y);
+        }
+    A[0] = xor2(A[0], rc);
+}
+
+__device__ __forceinline__ void keccak_f1600(uint2 (&A)[25]) {
+#pragma unroll 2
+    for (int r = 0; r < 24; r++) keccak_round(A, c_keccak_rc[r]);
+}
+
+__device__ __forceinline__ void keccak_zero(uint2 (&A)[25]) {
+#pragma unroll
+    for (int i = 0; i < 25; i++) A[i] = make_uint2(0, 0);
+}
+
+// XOR `pad` into byte 0 of lane `pos` (runtime pos < rate lanes) and 0x80 into the last rate byte.
+template <int RATE_LANES>
+__device__ __forceinline__ void keccak_pad(uint2 (&A)[25], int pos, uint32_t pad) {
+#pragma unroll
+    for (int i = 0; i < RATE_LANES; i++)
+        if (i == pos) A[i].x ^= pad;
+    A[RATE_LANES - 1].y ^= 0x80000000u;
+}
+
+// Absorb a message of `nlanes` 8-byte lanes (message length = 8 * nlanes) from memory that is
+// 8-byte aligned, apply pad10*1 with domain byte `dom`, and leave the state ready to squeeze
+// (the final permutation is NOT applied).  Works for global or shared pointers.
+template <int RATE_LANES>
+__device__ __forceinline__ void keccak_absorb_lanes(uint2 (&A)[25], const uint2 *in, int nlanes, uint32_t dom) {
+    keccak_zero(A);
+    while (nlanes >= RATE_LANES) {
+#pragma unroll
+        for (int i = 0; i < RATE_LANES; i++) A[i] = xor2(A[i], in[i]);
+        keccak_f1600(A);
+        in += RATE_LANES;
+        nlanes -= RATE_LANES;
+    }
+#pragma unroll
+    for (int i = 0; i < RATE_LANES; i++)
+        if (i < nlanes) A[i] = xor2(A[i], in[i]);
+    keccak_pad<RATE_LANES>(A, nlanes, dom);
+}
+
+constexpr int SHAKE128_LANES = 21;  // rate 168
+constexpr int SHAKE256_LANES = 17;  // rate 136
+constexpr int SHA3_256_LANES = 17;  // rate 136
+constexpr int SHA3_512_LANES = 9;   // rate 72
+constexpr uint32_t DOM_SHAKE = 0x1F;
+constexpr uint32_t DOM_SHA3 = 0x06;
+
+}  // namespace pqc

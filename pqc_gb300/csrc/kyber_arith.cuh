@@ -1,0 +1,198 @@
+// Kyber modular arithmetic and warp-cooperative NTT for sm_103a.
+//
+// The reductions are the reference's (Kyber_GPU_Batched/reduce.cu:21-66): Montgomery with
+// R = 2^16 and QINV = 62209, Barrett with v = floor(2^26 / q) + 1, conditional subtraction.
+// The butterflies follow ntt.cu:152-259 operation for operation (int16 wrap-around included), so
+// every intermediate coefficient equals the reference's.
+#pragma once
+#include <stdint.h>
+
+namespace pqc {
+namespace kyber {
+
+constexpr int N = 256;
+constexpr int Q = 3329;
+constexpr int POLY_PITCH = 296;  // int16 per shared-memory polynomial (256 + 8 per 64, +16 pad)
+
+static __constant__ int16_t c_zetas[128];
+static __constant__ int16_t c_zetas_inv[128];
+
+// zetas[i] = MONT * 17^brv7(i) mod q and the inverse-NTT table of the reference's generation
+// recipe (Kyber_GPU_Batched/ntt.cu:8-48), computed on the host at init.
+static inline void kyber_twiddles_host(int16_t zetas[128], int16_t zetas_inv[128]) {
+    const long MONT = 2285;
+    long pw[129];
+    pw[0] = 1;
+    for (int i = 1; i <= 128; i++) pw[i] = (pw[i - 1] * 17) % Q;
+    auto brv7 = [](int x) { int r = 0; for (int i = 0; i < 7; i++) r |= ((x >> i) & 1) << (6 - i); return r; };
+    auto modq = [](long v) { long r = v % Q; return (int16_t)(r < 0 ? r + Q : r); };
+    for (int i = 0; i < 128; i++) zetas[i] = modq(MONT * pw[brv7(i)]);
+    int k = 0;
+    for (int i = 64; i >= 1; i >>= 1)
+        for (int j = i; j < 2 * i; j++) zetas_inv[k++] = modq(-MONT * pw[128 - brv7(j)]);
+    zetas_inv[127] = (int16_t)((MONT * ((MONT * (Q - 1) * ((Q - 1) / 128)) % Q)) % Q);
+}
+
+__device__ __forceinline__ int16_t mont_reduce(int32_t a) {
+    const int16_t u = (int16_t)((uint32_t)a * 62209u);
+    return (int16_t)((a - (int32_t)u * Q) >> 16);
+}
+__device__ __forceinline__ int16_t fqmul(int16_t a, int16_t b) { return mont_reduce((int32_t)a * b); }
+__device__ __forceinline__ int16_t barrett(int16_t a) {
+    const int32_t t = ((int32_t)20159 * a) >> 26;
+    return (int16_t)(a - t * Q);
+}
+__device__ __forceinline__ int16_t csubq(int16_t a) {
+    a = (int16_t)(a - Q);
+    return (int16_t)(a + ((a >> 15) & Q));
+}
+
+// Physical index of coefficient i inside a shared-memory polynomial: 8 int16 of padding after
+// every 64 coefficients keeps all three NTT access patterns free of bank conflicts while each run
+// of 8 coefficients stays 16-byte aligned.
+__device__ __forceinline__ int phys(int i) { return i + ((i >> 6) << 3); }
+
+// basemul in Z_q[X]/(X^2 - zeta), Kyber_GPU_Batched/ntt.cu:249-259
+__device__ __forceinline__ void basemul(int16_t &r0, int16_t &r1, int16_t a0, int16_t a1, int16_t b0, int16_t b1,
+                                        int16_t zeta) {
+    r0 = fqmul(a1, b1);
+    r0 = fqmul(r0, zeta);
+    r0 = (int16_t)(r0 + fqmul(a0, b0));
+    r1 = fqmul(a0, b1);
+    r1 = (int16_t)(r1 + fqmul(a1, b0));
+}
+// zeta of coefficient pair p (coefficients 2p, 2p+1): +zetas[64 + p/2] for even p, minus for odd.
+__device__ __forceinline__ int16_t pair_zeta(const int16_t *sz, int p) {
+    const int16_t z = sz[64 + (p >> 1)];
+    return (p & 1) ? (int16_t)-z : z;
+}
+
+__device__ __forceinline__ void ct_bfly(int16_t &a, int16_t &b, int16_t z) {
+    const int16_t t = fqmul(z, b);
+    b = (int16_t)(a - t);
+    a = (int16_t)(a + t);
+}
+__device__ __forceinline__ void gs_bfly(int16_t &a, int16_t &b, int16_t z) {
+    const int16_t t = a;
+    a = barrett((int16_t)(t + b));
+    b = (int16_t)(t - b);
+    b = fqmul(z, b);
+}
+
+__device__ __forceinline__ void load8(int16_t (&r)[8], const int16_t *p) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(p);
+    r[0] = (int16_t)(v.x & 0xffff); r[1] = (int16_t)(v.x >> 16);
+    r[2] = (int16_t)(v.y & 0xffff); r[3] = (int16_t)(v.y >> 16);
+    r[4] = (int16_t)(v.z & 0xffff); r[5] = (int16_t)(v.z >> 16);
+    r[6] = (int16_t)(v.w & 0xffff); r[7] = (int16_t)(v.w >> 16);
+}
+__device__ __forceinline__ uint32_t pack2(int16_t a, int16_t b) { return (uint16_t)a | ((uint32_t)(uint16_t)b << 16); }
+__device__ __forceinline__ void store8(int16_t *p, const int16_t (&r)[8]) {
+    *reinterpret_cast<uint4 *>(p) = make_uint4(pack2(r[0], r[1]), pack2(r[2], r[3]), pack2(r[4], r[5]), pack2(r[6], r[7]));
+}
+
+// Forward NTT + Barrett (poly_ntt, poly.cu:153-157) of one shared-memory polynomial by one warp.
+// Three passes, each doing the butterflies of a 3-bit (or 2-bit) slice of the index in registers:
+//   pass 1: lane = bits 4..0, registers = bits 7,6,5   -> layers len 128, 64, 32
+//   pass 2: lane = bits 6,5,2,1,0, registers = 7,4,3   -> layers len 16, 8
+//   pass 3: lane = bits 7..3, registers = bits 2,1,0   -> layers len 4, 2, then Barrett
+// `sz` is the zetas table in shared memory (lane-dependent indices in passes 2 and 3).
+__device__ __forceinline__ void ntt_warp(int16_t *p, const int16_t *sz, int lane) {
+    int16_t r[8];
+#pragma unroll
+    for (int m = 0; m < 8; m++) r[m] = p[phys(32 * m + lane)];
+    {
+        const int16_t z = sz[1];
+#pragma unroll
+        for (int m = 0; m < 4; m++) ct_bfly(r[m], r[m + 4], z);
+    }
+#pragma unroll
+    for (int m = 0; m < 8; m++)
+        if (!(m & 2)) ct_bfly(r[m], r[m + 2], sz[2 + (m >> 2)]);
+#pragma unroll
+    for (int m = 0; m < 8; m += 2) ct_bfly(r[m], r[m + 1], sz[4 + (m >> 1)]);
+#pragma unroll
+    for (int m = 0; m < 8; m++) p[phys(32 * m + lane)] = r[m];
+    __syncwarp();
+
+    const int l65 = lane >> 3, l210 = lane & 7;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        r[q] = p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)];
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        if (!(q & 2)) ct_bfly(r[q], r[q + 2], sz[8 + 4 * (q >> 2) + l65]);
+#pragma unroll
+    for (int q = 0; q < 8; q += 2) ct_bfly(r[q], r[q + 1], sz[16 + 8 * (q >> 2) + 2 * l65 + ((q >> 1) & 1)]);
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)] = r[q];
+    __syncwarp();
+
+    int16_t *p8 = p + phys(8 * lane);
+    load8(r, p8);
+    {
+        const int16_t z = sz[32 + lane];
+#pragma unroll
+        for (int q = 0; q < 4; q++) ct_bfly(r[q], r[q + 4], z);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        if (!(q & 2)) ct_bfly(r[q], r[q + 2], sz[64 + 2 * lane + (q >> 2)]);
+#pragma unroll
+    for (int q = 0; q < 8; q++) r[q] = barrett(r[q]);
+    store8(p8, r);
+    __syncwarp();
+}
+
+// Inverse NTT including the final multiplication by mont^2/128 (invntt, ntt.cu:194-224);
+// the passes mirror ntt_warp in reverse order.  `szi` is zetas_inv in shared memory.
+__device__ __forceinline__ void invntt_warp(int16_t *p, const int16_t *szi, int lane) {
+    int16_t r[8];
+    int16_t *p8 = p + phys(8 * lane);
+    load8(r, p8);
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        if (!(q & 2)) gs_bfly(r[q], r[q + 2], szi[2 * lane + (q >> 2)]);
+    {
+        const int16_t z = szi[64 + lane];
+#pragma unroll
+        for (int q = 0; q < 4; q++) gs_bfly(r[q], r[q + 4], z);
+    }
+    store8(p8, r);
+    __syncwarp();
+
+    const int l65 = lane >> 3, l210 = lane & 7;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        r[q] = p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)];
+#pragma unroll
+    for (int q = 0; q < 8; q += 2) gs_bfly(r[q], r[q + 1], szi[96 + 8 * (q >> 2) + 2 * l65 + ((q >> 1) & 1)]);
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        if (!(q & 2)) gs_bfly(r[q], r[q + 2], szi[112 + 4 * (q >> 2) + l65]);
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)] = r[q];
+    __syncwarp();
+
+#pragma unroll
+    for (int m = 0; m < 8; m++) r[m] = p[phys(32 * m + lane)];
+#pragma unroll
+    for (int m = 0; m < 8; m += 2) gs_bfly(r[m], r[m + 1], szi[120 + (m >> 1)]);
+#pragma unroll
+    for (int m = 0; m < 8; m++)
+        if (!(m & 2)) gs_bfly(r[m], r[m + 2], szi[124 + (m >> 2)]);
+    {
+        const int16_t z = szi[126];
+#pragma unroll
+        for (int m = 0; m < 4; m++) gs_bfly(r[m], r[m + 4], z);
+    }
+    const int16_t f = szi[127];
+#pragma unroll
+    for (int m = 0; m < 8; m++) p[phys(32 * m + lane)] = fqmul(r[m], f);
+    __syncwarp();
+}
+
+}  // namespace kyber
+}  // namespace pqc

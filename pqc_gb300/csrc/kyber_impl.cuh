@@ -1,0 +1,864 @@
+// Batched Kyber (implementation header, instantiated per (k, variant) in kyber_k*_v*.cu)
+// Batched Kyber (round-3 parameter sets k = 2/3/4 and the reference's round-2 k = 4 variant) for
+// sm_103a: keypair, encapsulation and decapsulation.
+//
+// Each operation is a short chain of kernels over the batch:
+//   *_hash kernels: one thread per instance, the long serial sponges (H(pk), H(c), G, KDF);
+//   *_core kernels: one CTA per group of NI instances.  Inside the CTA the work of the CPA
+//     scheme runs as phases separated by __syncthreads:
+//       - noise (PRF + CBD), one thread per polynomial, written straight into shared memory;
+//       - forward / inverse NTT, one warp per polynomial (kyber_arith.cuh);
+//       - the matrix: one thread per row streams SHAKE128 blocks, rejection-samples the entries
+//         and multiplies them into the accumulator as they appear, so A never exists anywhere,
+//         not in HBM and not even whole in shared memory;
+//       - compression / packing, one warp per instance, straight to the output bytes.
+// Shared memory holds only (2K+1) (3K for keypair) polynomials per instance.
+//
+// Reference call stacks replaced: indcpa_keypair / indcpa_enc / indcpa_dec
+// (Kyber_GPU_Batched/indcpa.cu:474-733, ~52 launches at K = 4 with every intermediate in HBM) and
+// the crypto_kem_* entry points the reference declares (Kyber_GPU_Batched/api.h:18-22).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "keccak.cuh"
+#include "kyber_arith.cuh"
+#include "pqcgpu_internal.h"
+
+namespace pqc {
+namespace kyber {
+
+template <int K, int V>
+struct P {
+    static constexpr int ETA1 = (V == 3 && K == 2) ? 3 : 2;
+    static constexpr int ETA2 = 2;
+    static constexpr int DU = (V == 2 || K == 4) ? 11 : 10;
+    static constexpr int DV = (V == 2 || K == 4) ? 5 : 4;
+    static constexpr int POLYVECBYTES = K * 384;
+    static constexpr int PKB = POLYVECBYTES + 32;
+    static constexpr int SKCPA = POLYVECBYTES;
+    static constexpr int SKB = SKCPA + PKB + 64;
+    static constexpr int CTU = K * DU * 32;
+    static constexpr int CTB = CTU + DV * 32;
+};
+
+// ---------------------------------------------------------------------------------------------
+// Sponge helpers on a register state
+// ---------------------------------------------------------------------------------------------
+
+// PRF(seed, nonce) = SHAKE256(seed || nonce); `seed` 8-byte aligned (global or shared).
+__device__ __forceinline__ void prf_absorb(uint2 (&A)[25], const uint2 *seed, int nonce) {
+    keccak_zero(A);
+#pragma unroll
+    for (int i = 0; i < 4; i++) A[i] = seed[i];
+    A[4].x = (uint32_t)nonce | (DOM_SHAKE << 8);
+    A[SHAKE256_LANES - 1].y ^= 0x80000000u;
+    keccak_f1600(A);
+}
+
+// CBD eta=2 from the first 128 squeezed bytes: word w (bytes 4w..4w+3) gives coefficients
+// 8w..8w+7 (cbd.cu:42-63).  Calls emit(c, coeff[8]) for each group of 8.
+template <class F>
+__device__ __forceinline__ void cbd2_from_state(const uint2 (&A)[25], F emit) {
+#pragma unroll
+    for (int w = 0; w < 32; w++) {
+        const uint32_t t = (w & 1) ? A[w >> 1].y : A[w >> 1].x;
+        uint32_t d = t & 0x55555555u;
+        d += (t >> 1) & 0x55555555u;
+        int16_t c[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) c[j] = (int16_t)((int)((d >> (4 * j)) & 3) - (int)((d >> (4 * j + 2)) & 3));
+        emit(w, c);
+    }
+}
+
+// CBD eta=3 from 192 bytes spread over two squeezes (136 + 56 bytes): words wa[0..33] from the
+// first state, wb[0..13] from the second.  Triplet t (bytes 3t..3t+2) gives coefficients 4t..4t+3.
+template <class F>
+__device__ __forceinline__ void cbd3_from_words(const uint32_t (&w)[48], F emit) {
+#pragma unroll
+    for (int g = 0; g < 32; g++) {  // group of 8 coefficients = 2 triplets = 6 bytes
+        int16_t c[8];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int t = 2 * g + h, o = 3 * t, wi = o >> 2, sh = 8 * (o & 3);
+            uint32_t v = (sh <= 8) ? (w[wi] >> sh) : __funnelshift_r(w[wi], w[wi + 1], sh);
+            v &= 0x00ffffffu;
+            uint32_t d = v & 0x00249249u;
+            d += (v >> 1) & 0x00249249u;
+            d += (v >> 2) & 0x00249249u;
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                c[4 * h + j] = (int16_t)((int)((d >> (6 * j)) & 7) - (int)((d >> (6 * j + 3)) & 7));
+        }
+        emit(g, c);
+    }
+}
+
+// Noise polynomial PRF(seed, nonce) -> CBD(eta), delivered to emit(group, coeff[8]).
+template <int ETA, class F>
+__device__ __forceinline__ void noise_poly(const uint2 *seed, int nonce, F emit) {
+    uint2 A[25];
+    prf_absorb(A, seed, nonce);
+    if (ETA == 2) {
+        cbd2_from_state(A, emit);
+    } else {
+        uint32_t w[48];
+#pragma unroll
+        for (int i = 0; i < 17; i++) {
+            w[2 * i] = A[i].x;
+            w[2 * i + 1] = A[i].y;
+        }
+        keccak_f1600(A);
+#pragma unroll
+        for (int i = 0; i < 7; i++) {
+            w[34 + 2 * i] = A[i].x;
+            w[35 + 2 * i] = A[i].y;
+        }
+        cbd3_from_words(w, emit);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Matrix rows: stream SHAKE128(rho || x || y), rejection-sample, multiply into the accumulator.
+// ---------------------------------------------------------------------------------------------
+
+// acc (shared, one polynomial) {=, +=} A_entry o b, with the final Barrett of pointwise_acc when
+// LAST.  Candidates are consumed in order, pairs (2p, 2p+1) are multiplied as soon as complete.
+template <int V>
+struct RowSampler {
+    int ctr;
+    int16_t even;
+    const int16_t *b;  // shared polynomial b (NTT domain)
+    int16_t *acc;
+    const int16_t *sz;
+    bool first, last;
+
+    __device__ __forceinline__ void take(uint32_t d) {
+        const uint32_t bound = (V == 2) ? (uint32_t)(19 * Q) : (uint32_t)Q;
+        if (d < bound && ctr < N) {
+            int16_t a = (V == 2) ? (int16_t)(d - (d >> 12) * Q) : (int16_t)d;
+            if (ctr & 1) {
+                const int p = ctr >> 1;
+                const int o = phys(2 * p);
+                const uint32_t bb = *reinterpret_cast<const uint32_t *>(b + o);
+                int16_t r0, r1;
+                basemul(r0, r1, even, a, (int16_t)(bb & 0xffff), (int16_t)(bb >> 16), pair_zeta(sz, p));
+                uint32_t *ap = reinterpret_cast<uint32_t *>(acc + o);
+                if (!first) {
+                    const uint32_t av = *ap;
+                    r0 = (int16_t)(r0 + (int16_t)(av & 0xffff));
+                    r1 = (int16_t)(r1 + (int16_t)(av >> 16));
+                }
+                if (last) {
+                    r0 = barrett(r0);
+                    r1 = barrett(r1);
+                }
+                *ap = pack2(r0, r1);
+            } else {
+                even = a;
+            }
+            ctr++;
+        }
+    }
+};
+
+template <int K, int V>
+__device__ __forceinline__ void matrix_row(const uint2 *rho, int row, bool transposed, const int16_t *bvec,
+                                           int16_t *acc, const int16_t *sz) {
+    for (int j = 0; j < K; j++) {
+        uint2 A[25];
+        keccak_zero(A);
+#pragma unroll
+        for (int i = 0; i < 4; i++) A[i] = rho[i];
+        // gen_matrix: A[i][j] = XOF(rho || j || i); transposed: XOF(rho || i || j)
+        const uint32_t x = transposed ? row : j, y = transposed ? j : row;
+        A[4].x = x | (y << 8) | (DOM_SHAKE << 16);
+        A[SHAKE128_LANES - 1].y ^= 0x80000000u;
+        RowSampler<V> s;
+        s.ctr = 0;
+        s.even = 0;
+        s.b = bvec + j * POLY_PITCH;
+        s.acc = acc;
+        s.sz = sz;
+        s.first = (j == 0);
+        s.last = (j == K - 1);
+        while (s.ctr < N) {
+            keccak_f1600(A);
+            if (V == 3) {
+                // 56 triplets, two 12-bit candidates each (round-3 Parse)
+#pragma unroll
+                for (int t = 0; t < 56; t++) {
+                    const int o = 3 * t, wi = o >> 2, sh = 8 * (o & 3);
+                    const uint32_t w0 = (wi & 1) ? A[wi >> 1].y : A[wi >> 1].x;
+                    uint32_t v;
+                    if (sh <= 8) {
+                        v = w0 >> sh;
+                    } else {
+                        const uint32_t w1 = ((wi + 1) & 1) ? A[(wi + 1) >> 1].y : A[(wi + 1) >> 1].x;
+                        v = __funnelshift_r(w0, w1, sh);
+                    }
+                    s.take(v & 0xfff);
+                    s.take((v >> 12) & 0xfff);
+                }
+            } else {
+                // 84 little-endian 16-bit candidates (rej_uniform, indcpa.cu:290-322)
+#pragma unroll
+                for (int t = 0; t < 42; t++) {
+                    const uint32_t w0 = (t & 1) ? A[t >> 1].y : A[t >> 1].x;
+                    s.take(w0 & 0xffff);
+                    s.take(w0 >> 16);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Codecs (warp per instance, lane = group of 8 coefficients)
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ uint32_t compress_d(int16_t x) {
+    // x canonical in [0, q)
+    return ((((uint32_t)(uint16_t)x << D) + Q / 2) / Q) & ((1u << D) - 1);
+}
+template <int D>
+__device__ __forceinline__ int16_t decompress_d(uint32_t t) {
+    return (int16_t)((t * Q + (1u << (D - 1))) >> D);
+}
+// 8 D-bit values -> D bytes (little-endian bit order), via a 128-bit accumulator.
+template <int D>
+__device__ __forceinline__ void pack8(uint8_t (&out)[D], const uint32_t (&t)[8]) {
+    uint64_t lo = 0, hi = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const int bit = D * j;
+        if (bit < 64) {
+            lo |= (uint64_t)t[j] << bit;
+            if (bit + D > 64) hi |= (uint64_t)t[j] >> (64 - bit);
+        } else {
+            hi |= (uint64_t)t[j] << (bit - 64);
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < D; b++) out[b] = (uint8_t)(b < 8 ? (lo >> (8 * b)) : (hi >> (8 * (b - 8))));
+}
+template <int D>
+__device__ __forceinline__ void unpack8(uint32_t (&t)[8], const uint8_t *in) {
+    uint64_t lo = 0, hi = 0;
+#pragma unroll
+    for (int b = 0; b < D; b++) {
+        if (b < 8) lo |= (uint64_t)in[b] << (8 * b);
+        else hi |= (uint64_t)in[b] << (8 * (b - 8));
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const int bit = D * j;
+        uint64_t v;
+        if (bit < 64) {
+            v = lo >> bit;
+            if (bit + D > 64) v |= hi << (64 - bit);
+        } else {
+            v = hi >> (bit - 64);
+        }
+        t[j] = (uint32_t)v & ((1u << D) - 1);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Kernel parameters
+// ---------------------------------------------------------------------------------------------
+struct KpArgs {
+    int n;
+    uint8_t *pk;
+    uint8_t *sk;             // CPA: sk_cpa (stride SKCPA); KEM: full sk (stride SKB)
+    const uint8_t *coins;    // d (and z for KEM) per instance
+    int coins_stride;
+    int kem;                 // 1: write sk = sk_cpa || pk || (H(pk) later) || z
+};
+struct EncArgs {
+    int n;
+    uint8_t *ct;
+    const uint8_t *pk;
+    int pk_stride;
+    const uint8_t *m;        // message (32 B) per instance
+    int m_stride;
+    const uint8_t *r;        // noise seed (32 B) per instance
+    int r_stride;
+};
+struct DecArgs {
+    int n;
+    const uint8_t *ct;
+    const uint8_t *sk;       // CPA: sk_cpa (stride SKCPA); KEM: full sk (stride SKB)
+    uint8_t *m_out;          // CPA only: decrypted message
+    uint8_t *ss;             // KEM only
+    const uint8_t *hct;      // KEM only: H(c) per instance (32 B)
+    int kem;
+};
+
+// Shared-memory layout for a CTA of NI instances: twiddles, NPOLY polynomials per instance, and
+// 128 bytes of per-instance seeds / flags.
+template <int NPOLY>
+struct Layout {
+    static __host__ __device__ constexpr size_t bytes(int ni) {
+        return 2 * 128 * sizeof(int16_t) + (size_t)ni * NPOLY * POLY_PITCH * sizeof(int16_t) + (size_t)ni * 128;
+    }
+};
+
+__device__ __forceinline__ void load_twiddles(int16_t *sz, int16_t *szi) {
+    for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+        sz[i] = c_zetas[i];
+        szi[i] = c_zetas_inv[i];
+    }
+}
+
+// 12-bit serialisation of 8 canonical coefficients -> 12 bytes (poly_tobytes, poly.cu:79-97)
+__device__ __forceinline__ void tobytes8(uint8_t *out, const int16_t (&c)[8]) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const uint16_t t0 = (uint16_t)c[2 * i], t1 = (uint16_t)c[2 * i + 1];
+        out[3 * i] = (uint8_t)t0;
+        out[3 * i + 1] = (uint8_t)((t0 >> 8) | ((t1 & 0xf) << 4));
+        out[3 * i + 2] = (uint8_t)(t1 >> 4);
+    }
+}
+__device__ __forceinline__ void frombytes8(int16_t (&c)[8], const uint8_t *in) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        c[2 * i] = (int16_t)(in[3 * i] | (((uint16_t)in[3 * i + 1] & 0x0f) << 8));
+        c[2 * i + 1] = (int16_t)((in[3 * i + 1] >> 4) | ((uint16_t)in[3 * i + 2] << 4));
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Encryption phases shared by encapsulation and the re-encryption inside decapsulation.
+// Polynomial slots per instance: [0, K) = r-hat, [K, 2K) = u accumulators, 2K = v.
+// ---------------------------------------------------------------------------------------------
+template <int K, int V>
+__device__ __forceinline__ int16_t *slot(int16_t *polys, int li, int s) {
+    return polys + ((size_t)li * (2 * K + 1) + s) * POLY_PITCH;
+}
+
+// Per-instance shared seed block (128 B): [0,32) m, [32,64) r / K-bar, [64,96) rho / z, [96] flag
+template <int K, int V, bool DEC>
+__device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz, const int16_t *szi, int ni,
+                               int base, const EncArgs &a, const uint8_t *ct_cmp) {
+    using Pp = P<K, V>;
+    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
+
+    // (1) r = CBD_eta1(PRF(coins, i)), i < K  -> slots [0, K)
+    for (int job = tid; job < ni * K; job += nthr) {
+        const int li = job / K, i = job % K;
+        const uint2 *seed = DEC ? reinterpret_cast<const uint2 *>(seeds + li * 128 + 32)
+                                : reinterpret_cast<const uint2 *>(a.r + (size_t)(base + li) * a.r_stride);
+        int16_t *dst = slot<K, V>(polys, li, i);
+        noise_poly<Pp::ETA1>(seed, i, [&](int g, const int16_t(&c)[8]) { store8(dst + phys(8 * g), c); });
+    }
+    __syncthreads();
+    // (2) r-hat = NTT(r)
+    for (int w = warp; w < ni * K; w += nwarp) ntt_warp(slot<K, V>(polys, w / K, w % K), sz, lane);
+    __syncthreads();
+    // (3) u_i = sum_j A^T[i][j] o r-hat_j, streamed from SHAKE128, one thread per row
+    for (int job = tid; job < ni * K; job += nthr) {
+        const int li = job / K, i = job % K;
+        const uint8_t *pk = DEC ? a.pk + (size_t)(base + li) * a.pk_stride : a.pk + (size_t)(base + li) * a.pk_stride;
+        matrix_row<K, V>(reinterpret_cast<const uint2 *>(pk + Pp::POLYVECBYTES), i, true, slot<K, V>(polys, li, 0),
+                         slot<K, V>(polys, li, K + i), sz);
+    }
+    // (4) v = t-hat o r-hat (warp per instance, t-hat decoded from pk bytes; independent of (3))
+    for (int li = warp; li < ni; li += nwarp) {
+        const uint8_t *pk = a.pk + (size_t)(base + li) * a.pk_stride;
+        int16_t acc[8];
+        for (int j = 0; j < K; j++) {
+            int16_t t[8], b[8], r[8];
+            frombytes8(t, pk + 384 * j + 12 * lane);
+            load8(b, slot<K, V>(polys, li, j) + phys(8 * lane));
+#pragma unroll
+            for (int q = 0; q < 4; q++) basemul(r[2 * q], r[2 * q + 1], t[2 * q], t[2 * q + 1], b[2 * q], b[2 * q + 1],
+                                                 pair_zeta(sz, 4 * lane + q));
+#pragma unroll
+            for (int q = 0; q < 8; q++) acc[q] = (j == 0) ? r[q] : (int16_t)(acc[q] + r[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc[q] = barrett(acc[q]);
+        store8(slot<K, V>(polys, li, 2 * K) + phys(8 * lane), acc);
+    }
+    __syncthreads();
+    // (5) inverse NTT of u (K) and v
+    for (int w = warp; w < ni * (K + 1); w += nwarp)
+        invntt_warp(slot<K, V>(polys, w / (K + 1), K + w % (K + 1)), szi, lane);
+    __syncthreads();
+    // (6) u += e1 (nonce K+i, eta2); v += e2 (nonce 2K) + msg; Barrett; compress in place
+    for (int job = tid; job < ni * (K + 1); job += nthr) {
+        const int li = job / (K + 1), i = job % (K + 1);
+        const uint2 *seed = DEC ? reinterpret_cast<const uint2 *>(seeds + li * 128 + 32)
+                                : reinterpret_cast<const uint2 *>(a.r + (size_t)(base + li) * a.r_stride);
+        const uint8_t *msg = DEC ? seeds + li * 128 : a.m + (size_t)(base + li) * a.m_stride;
+        int16_t *dst = slot<K, V>(polys, li, K + i);
+        const bool isv = (i == K);
+        noise_poly<Pp::ETA2>(seed, K + i, [&](int g, const int16_t(&e)[8]) {
+            int16_t c[8];
+            load8(c, dst + phys(8 * g));
+            const uint8_t mb = isv ? msg[g] : 0;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                int16_t x = (int16_t)(c[q] + e[q]);
+                if (isv) x = (int16_t)(x + (int16_t)(((mb >> q) & 1) ? (Q + 1) / 2 : 0));
+                x = csubq(barrett(x));
+                c[q] = (int16_t)(isv ? compress_d<Pp::DV>(x) : compress_d<Pp::DU>(x));
+            }
+            store8(dst + phys(8 * g), c);
+        });
+    }
+    __syncthreads();
+    // (7) pack (encaps) or compare against the received ciphertext (decaps), warp per instance
+    for (int li = warp; li < ni; li += nwarp) {
+        uint8_t *out = DEC ? nullptr : a.ct + (size_t)(base + li) * Pp::CTB;
+        const uint8_t *cmp = DEC ? ct_cmp + (size_t)(base + li) * Pp::CTB : nullptr;
+        uint32_t diff = 0;
+        for (int i = 0; i <= K; i++) {
+            int16_t c[8];
+            load8(c, slot<K, V>(polys, li, K + i) + phys(8 * lane));
+            uint32_t t[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) t[q] = (uint16_t)c[q];
+            if (i < K) {
+                uint8_t b[Pp::DU];
+                pack8<Pp::DU>(b, t);
+                const size_t off = (size_t)i * Pp::DU * 32 + (size_t)lane * Pp::DU;
+#pragma unroll
+                for (int q = 0; q < Pp::DU; q++) {
+                    if (DEC) diff |= (uint32_t)(b[q] ^ cmp[off + q]);
+                    else out[off + q] = b[q];
+                }
+            } else {
+                uint8_t b[Pp::DV];
+                pack8<Pp::DV>(b, t);
+                const size_t off = (size_t)Pp::CTU + (size_t)lane * Pp::DV;
+#pragma unroll
+                for (int q = 0; q < Pp::DV; q++) {
+                    if (DEC) diff |= (uint32_t)(b[q] ^ cmp[off + q]);
+                    else out[off + q] = b[q];
+                }
+            }
+        }
+        if (DEC) {
+            diff = __any_sync(0xffffffffu, diff != 0);
+            if (lane == 0) seeds[li * 128 + 96] = (uint8_t)diff;
+        }
+    }
+}
+
+
+// ---------------------------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------------------------
+constexpr int CORE_THREADS = 128;
+
+template <int K, int V>
+__global__ void __launch_bounds__(CORE_THREADS) kyber_enc_core(EncArgs a, int NI) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
+    uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (2 * K + 1) * POLY_PITCH);
+    const int base = blockIdx.x * NI;
+    const int ni = min(NI, a.n - base);
+    load_twiddles(sz, szi);
+    __syncthreads();
+    encrypt_phases<K, V, false>(polys, seeds, sz, szi, ni, base, a, nullptr);
+}
+
+template <int K, int V>
+__global__ void __launch_bounds__(CORE_THREADS) kyber_dec_core(DecArgs d, int NI) {
+    using Pp = P<K, V>;
+    extern __shared__ __align__(16) uint8_t smem[];
+    int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
+    uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (2 * K + 1) * POLY_PITCH);
+    const int base = blockIdx.x * NI;
+    const int ni = min(NI, d.n - base);
+    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
+    const int sks = d.kem ? Pp::SKB : Pp::SKCPA;
+    load_twiddles(sz, szi);
+    // (a) decompress u' -> slots [K, 2K), v' -> slot 2K (unpack_ciphertext, indcpa.cu:264-275)
+    for (int li = warp; li < ni; li += nwarp) {
+        const uint8_t *ct = d.ct + (size_t)(base + li) * Pp::CTB;
+        for (int i = 0; i <= K; i++) {
+            uint32_t t[8];
+            int16_t c[8];
+            if (i < K) {
+                unpack8<Pp::DU>(t, ct + (size_t)i * Pp::DU * 32 + (size_t)lane * Pp::DU);
+#pragma unroll
+                for (int q = 0; q < 8; q++) c[q] = decompress_d<Pp::DU>(t[q]);
+            } else {
+                unpack8<Pp::DV>(t, ct + Pp::CTU + (size_t)lane * Pp::DV);
+#pragma unroll
+                for (int q = 0; q < 8; q++) c[q] = decompress_d<Pp::DV>(t[q]);
+            }
+            store8(slot<K, V>(polys, li, K + i) + phys(8 * lane), c);
+        }
+    }
+    __syncthreads();
+    // (b) u-hat = NTT(u')
+    for (int w = warp; w < ni * K; w += nwarp) ntt_warp(slot<K, V>(polys, w / K, K + w % K), sz, lane);
+    __syncthreads();
+    // (c) mp = s-hat o u-hat -> slot 0
+    for (int li = warp; li < ni; li += nwarp) {
+        const uint8_t *sk = d.sk + (size_t)(base + li) * sks;
+        int16_t acc[8];
+        for (int j = 0; j < K; j++) {
+            int16_t s[8], b[8], r[8];
+            frombytes8(s, sk + 384 * j + 12 * lane);
+            load8(b, slot<K, V>(polys, li, K + j) + phys(8 * lane));
+#pragma unroll
+            for (int q = 0; q < 4; q++) basemul(r[2 * q], r[2 * q + 1], s[2 * q], s[2 * q + 1], b[2 * q], b[2 * q + 1],
+                                                 pair_zeta(sz, 4 * lane + q));
+#pragma unroll
+            for (int q = 0; q < 8; q++) acc[q] = (j == 0) ? r[q] : (int16_t)(acc[q] + r[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc[q] = barrett(acc[q]);
+        store8(slot<K, V>(polys, li, 0) + phys(8 * lane), acc);
+    }
+    __syncthreads();
+    for (int w = warp; w < ni; w += nwarp) invntt_warp(slot<K, V>(polys, w, 0), szi, lane);
+    __syncthreads();
+    // (d) m' = tomsg(reduce(v - mp)), lane = message byte
+    for (int li = warp; li < ni; li += nwarp) {
+        int16_t v[8], mp[8];
+        load8(v, slot<K, V>(polys, li, 2 * K) + phys(8 * lane));
+        load8(mp, slot<K, V>(polys, li, 0) + phys(8 * lane));
+        uint32_t byte = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int16_t x = csubq(barrett((int16_t)(v[q] - mp[q])));
+            byte |= (((((uint32_t)x << 1) + Q / 2) / Q) & 1) << q;
+        }
+        seeds[li * 128 + lane] = (uint8_t)byte;
+        if (!d.kem) d.m_out[(size_t)(base + li) * 32 + lane] = (uint8_t)byte;
+    }
+    if (!d.kem) return;
+    __syncthreads();
+    // (e) (K-bar', r') = G(m' || h)
+    for (int li = tid; li < ni; li += nthr) {
+        const uint8_t *sk = d.sk + (size_t)(base + li) * Pp::SKB;
+        uint2 A[25];
+        keccak_zero(A);
+        const uint2 *m2 = reinterpret_cast<const uint2 *>(seeds + li * 128);
+        const uint2 *h2 = reinterpret_cast<const uint2 *>(sk + Pp::SKB - 64);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            A[i] = m2[i];
+            A[4 + i] = h2[i];
+        }
+        A[8].x ^= DOM_SHA3;
+        A[SHA3_512_LANES - 1].y ^= 0x80000000u;
+        keccak_f1600(A);
+        uint2 *kb = reinterpret_cast<uint2 *>(seeds + li * 128 + 64), *rr = reinterpret_cast<uint2 *>(seeds + li * 128 + 32);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            kb[i] = A[i];
+            rr[i] = A[4 + i];
+        }
+    }
+    __syncthreads();
+    // (f) re-encrypt m' with r' under the pk stored in sk and compare with the received ct
+    EncArgs e;
+    e.n = d.n;
+    e.ct = nullptr;
+    e.pk = d.sk + Pp::SKCPA;
+    e.pk_stride = Pp::SKB;
+    e.m = nullptr;
+    e.m_stride = 0;
+    e.r = nullptr;
+    e.r_stride = 0;
+    encrypt_phases<K, V, true>(polys, seeds, sz, szi, ni, base, e, d.ct);
+    __syncthreads();
+    // (g) ss = SHAKE256(fail ? z : K-bar' || H(c)), with a constant-time select
+    for (int li = tid; li < ni; li += nthr) {
+        const uint8_t *sk = d.sk + (size_t)(base + li) * Pp::SKB;
+        const uint32_t mask = 0u - (uint32_t)(seeds[li * 128 + 96] != 0);
+        const uint2 *kb = reinterpret_cast<const uint2 *>(seeds + li * 128 + 64);
+        const uint2 *z = reinterpret_cast<const uint2 *>(sk + Pp::SKB - 32);
+        const uint2 *hc = reinterpret_cast<const uint2 *>(d.hct + (size_t)(base + li) * 32);
+        uint2 A[25];
+        keccak_zero(A);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint2 zk = z[i], kk = kb[i];
+            A[i] = make_uint2(kk.x ^ (mask & (kk.x ^ zk.x)), kk.y ^ (mask & (kk.y ^ zk.y)));
+            A[4 + i] = hc[i];
+        }
+        A[8].x ^= DOM_SHAKE;
+        A[SHAKE256_LANES - 1].y ^= 0x80000000u;
+        keccak_f1600(A);
+        uint2 *out = reinterpret_cast<uint2 *>(d.ss + (size_t)(base + li) * 32);
+#pragma unroll
+        for (int i = 0; i < 4; i++) out[i] = A[i];
+    }
+}
+
+// Keypair: slots [0,K) s, [K,2K) e, [2K,3K) t-hat; seeds [0,32) rho, [32,64) sigma.
+template <int K, int V>
+__global__ void __launch_bounds__(CORE_THREADS) kyber_kp_core(KpArgs a, int NI) {
+    using Pp = P<K, V>;
+    extern __shared__ __align__(16) uint8_t smem[];
+    int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
+    uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (3 * K) * POLY_PITCH);
+    auto kslot = [&](int li, int s) { return polys + ((size_t)li * (3 * K) + s) * POLY_PITCH; };
+    const int base = blockIdx.x * NI;
+    const int ni = min(NI, a.n - base);
+    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
+    load_twiddles(sz, szi);
+    // (a) (rho, sigma) = G(d)
+    for (int li = tid; li < ni; li += nthr) {
+        const uint2 *dd = reinterpret_cast<const uint2 *>(a.coins + (size_t)(base + li) * a.coins_stride);
+        uint2 A[25];
+        keccak_zero(A);
+#pragma unroll
+        for (int i = 0; i < 4; i++) A[i] = dd[i];
+        A[4].x ^= DOM_SHA3;
+        A[SHA3_512_LANES - 1].y ^= 0x80000000u;
+        keccak_f1600(A);
+        uint2 *o = reinterpret_cast<uint2 *>(seeds + li * 128);
+#pragma unroll
+        for (int i = 0; i < 8; i++) o[i] = A[i];
+    }
+    __syncthreads();
+    // (b) s_i = CBD(PRF(sigma, i)), e_i = CBD(PRF(sigma, K + i))
+    for (int job = tid; job < ni * 2 * K; job += nthr) {
+        const int li = job / (2 * K), i = job % (2 * K);
+        int16_t *dst = kslot(li, i);
+        noise_poly<Pp::ETA1>(reinterpret_cast<const uint2 *>(seeds + li * 128 + 32), i,
+                             [&](int g, const int16_t(&c)[8]) { store8(dst + phys(8 * g), c); });
+    }
+    __syncthreads();
+    for (int w = warp; w < ni * 2 * K; w += nwarp) ntt_warp(kslot(w / (2 * K), w % (2 * K)), sz, lane);
+    __syncthreads();
+    // (c) t-hat_i = sum_j A[i][j] o s-hat_j (not transposed)
+    for (int job = tid; job < ni * K; job += nthr) {
+        const int li = job / K, i = job % K;
+        matrix_row<K, V>(reinterpret_cast<const uint2 *>(seeds + li * 128), i, false, kslot(li, 0), kslot(li, 2 * K + i),
+                         sz);
+    }
+    __syncthreads();
+    // (d) t = reduce(frommont(t) + e); pack pk = t || rho and sk_cpa = s (warp per instance)
+    for (int li = warp; li < ni; li += nwarp) {
+        uint8_t *pk = a.pk + (size_t)(base + li) * Pp::PKB;
+        uint8_t *sk = a.sk + (size_t)(base + li) * (a.kem ? Pp::SKB : Pp::SKCPA);
+        for (int i = 0; i < K; i++) {
+            int16_t t[8], e[8], s[8];
+            load8(t, kslot(li, 2 * K + i) + phys(8 * lane));
+            load8(e, kslot(li, K + i) + phys(8 * lane));
+            load8(s, kslot(li, i) + phys(8 * lane));
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                t[q] = csubq(barrett((int16_t)(mont_reduce((int32_t)t[q] * 1353) + e[q])));
+                s[q] = csubq(s[q]);
+            }
+            uint8_t bt[12], bs[12];
+            tobytes8(bt, t);
+            tobytes8(bs, s);
+            const size_t off = (size_t)384 * i + 12 * lane;
+#pragma unroll
+            for (int q = 0; q < 12; q++) {
+                pk[off + q] = bt[q];
+                sk[off + q] = bs[q];
+                if (a.kem) sk[Pp::SKCPA + off + q] = bt[q];
+            }
+        }
+        if (lane < 4) {
+            const uint2 rho = reinterpret_cast<const uint2 *>(seeds + li * 128)[lane];
+            reinterpret_cast<uint2 *>(pk + Pp::POLYVECBYTES)[lane] = rho;
+            if (a.kem) {
+                reinterpret_cast<uint2 *>(sk + Pp::SKCPA + Pp::POLYVECBYTES)[lane] = rho;
+                const uint2 z = reinterpret_cast<const uint2 *>(a.coins + (size_t)(base + li) * a.coins_stride + 32)[lane];
+                reinterpret_cast<uint2 *>(sk + Pp::SKB - 32)[lane] = z;
+            }
+        }
+    }
+}
+
+// ---- flat hash kernels: one thread per instance ----
+// encaps prologue: m = H(coins); (K-bar, r) = G(m || H(pk)); scratch = m || r || K-bar
+template <int K, int V>
+__global__ void __launch_bounds__(128) kyber_enc_hash_pre(int n, const uint8_t *pk, const uint8_t *coins, uint8_t *scratch) {
+    using Pp = P<K, V>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    uint2 A[25], mh[8];
+    keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(coins + (size_t)x * 32), 4, DOM_SHA3);
+    keccak_f1600(A);
+#pragma unroll
+    for (int i = 0; i < 4; i++) mh[i] = A[i];
+    keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(pk + (size_t)x * Pp::PKB), Pp::PKB / 8, DOM_SHA3);
+    keccak_f1600(A);
+#pragma unroll
+    for (int i = 0; i < 4; i++) mh[4 + i] = A[i];
+    keccak_zero(A);
+#pragma unroll
+    for (int i = 0; i < 8; i++) A[i] = mh[i];
+    A[8].x ^= DOM_SHA3;
+    A[SHA3_512_LANES - 1].y ^= 0x80000000u;
+    keccak_f1600(A);
+    uint2 *o = reinterpret_cast<uint2 *>(scratch + (size_t)x * 96);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        o[i] = mh[i];         // m
+        o[4 + i] = A[4 + i];  // r
+        o[8 + i] = A[i];      // K-bar
+    }
+}
+// encaps epilogue: ss = KDF(K-bar || H(c))
+template <int K, int V>
+__global__ void __launch_bounds__(128) kyber_enc_hash_post(int n, const uint8_t *ct, const uint8_t *scratch, uint8_t *ss) {
+    using Pp = P<K, V>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    uint2 A[25], hc[4];
+    keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(ct + (size_t)x * Pp::CTB), Pp::CTB / 8, DOM_SHA3);
+    keccak_f1600(A);
+#pragma unroll
+    for (int i = 0; i < 4; i++) hc[i] = A[i];
+    const uint2 *kb = reinterpret_cast<const uint2 *>(scratch + (size_t)x * 96 + 64);
+    keccak_zero(A);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        A[i] = kb[i];
+        A[4 + i] = hc[i];
+    }
+    A[8].x ^= DOM_SHAKE;
+    A[SHAKE256_LANES - 1].y ^= 0x80000000u;
+    keccak_f1600(A);
+    uint2 *o = reinterpret_cast<uint2 *>(ss + (size_t)x * 32);
+#pragma unroll
+    for (int i = 0; i < 4; i++) o[i] = A[i];
+}
+// decaps prologue: H(c)
+template <int K, int V>
+__global__ void __launch_bounds__(128) kyber_dec_hash_pre(int n, const uint8_t *ct, uint8_t *hct) {
+    using Pp = P<K, V>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    uint2 A[25];
+    keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(ct + (size_t)x * Pp::CTB), Pp::CTB / 8, DOM_SHA3);
+    keccak_f1600(A);
+    uint2 *o = reinterpret_cast<uint2 *>(hct + (size_t)x * 32);
+#pragma unroll
+    for (int i = 0; i < 4; i++) o[i] = A[i];
+}
+// keypair epilogue: sk[SKB-64 .. SKB-32) = H(pk)
+template <int K, int V>
+__global__ void __launch_bounds__(128) kyber_kp_hash_post(int n, const uint8_t *pk, uint8_t *sk) {
+    using Pp = P<K, V>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    uint2 A[25];
+    keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(pk + (size_t)x * Pp::PKB), Pp::PKB / 8, DOM_SHA3);
+    keccak_f1600(A);
+    uint2 *o = reinterpret_cast<uint2 *>(sk + (size_t)x * Pp::SKB + Pp::SKB - 64);
+#pragma unroll
+    for (int i = 0; i < 4; i++) o[i] = A[i];
+}
+
+// ---------------------------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------------------------
+extern int g_ni[3][3];  // [op][k-2]: instances per CTA (kyber.cu)
+
+template <class Kern>
+static cudaError_t ensure_smem(Kern kern, size_t bytes) {
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <int K, int V>
+static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int coins_stride, int kem,
+                          cudaStream_t st) {
+    const int NI = g_ni[0][K - 2];
+    const size_t sm = Layout<3 * K>::bytes(NI);
+    if (ensure_smem(kyber_kp_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
+    KpArgs a{n, pk, sk, coins, coins_stride, kem};
+    g_launch_count += kem ? 2 : 1;
+    kyber_kp_core<K, V><<<(n + NI - 1) / NI, CORE_THREADS, sm, st>>>(a, NI);
+    if (kem) kyber_kp_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, sk);
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
+template <int K, int V>
+static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
+                      uint8_t *scratch, int kem, cudaStream_t st) {
+    const int NI = g_ni[1][K - 2];
+    const size_t sm = Layout<2 * K + 1>::bytes(NI);
+    if (ensure_smem(kyber_enc_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
+    EncArgs a;
+    a.n = n;
+    a.ct = ct;
+    a.pk = pk;
+    a.pk_stride = P<K, V>::PKB;
+    if (kem) {
+        kyber_enc_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, coins, scratch);
+        a.m = scratch;
+        a.m_stride = 96;
+        a.r = scratch + 32;
+        a.r_stride = 96;
+    } else {
+        a.m = m;
+        a.m_stride = 32;
+        a.r = coins;
+        a.r_stride = 32;
+    }
+    g_launch_count += kem ? 3 : 1;
+    kyber_enc_core<K, V><<<(n + NI - 1) / NI, CORE_THREADS, sm, st>>>(a, NI);
+    if (kem) kyber_enc_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, scratch, ss);
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
+template <int K, int V>
+static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, int kem,
+                      cudaStream_t st) {
+    const int NI = g_ni[2][K - 2];
+    const size_t sm = Layout<2 * K + 1>::bytes(NI);
+    if (ensure_smem(kyber_dec_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
+    DecArgs d;
+    d.n = n;
+    d.ct = ct;
+    d.sk = sk;
+    d.m_out = kem ? nullptr : out;
+    d.ss = kem ? out : nullptr;
+    d.hct = scratch;
+    d.kem = kem;
+    g_launch_count += kem ? 2 : 1;
+    if (kem) kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, scratch);
+    kyber_dec_core<K, V><<<(n + NI - 1) / NI, CORE_THREADS, sm, st>>>(d, NI);
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
+}  // namespace kyber
+}  // namespace pqc
+
+// One translation unit per (K, V) instantiates the kernels and exports these entry points.
+#define PQC_KYBER_INSTANTIATE(K, V)                                                                        \
+    namespace pqc {                                                                                        \
+    namespace kyber {                                                                                      \
+    int keypair_##K##_##V(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cs, int kem,         \
+                          cudaStream_t st) {                                                               \
+        return launch_keypair<K, V>(n, pk, sk, coins, cs, kem, st);                                       \
+    }                                                                                                      \
+    int enc_##K##_##V(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m,               \
+                      const uint8_t *coins, uint8_t *scratch, int kem, cudaStream_t st) {                  \
+        return launch_enc<K, V>(n, ct, ss, pk, m, coins, scratch, kem, st);                               \
+    }                                                                                                      \
+    int dec_##K##_##V(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, int kem, \
+                      cudaStream_t st) {                                                                   \
+        return launch_dec<K, V>(n, out, ct, sk, scratch, kem, st);                                        \
+    }                                                                                                      \
+    int init_##K##_##V() {                                                                                 \
+        uint2 rc[24];                                                                                      \
+        keccak_rc_host(rc);                                                                                \
+        int16_t z[128], zi[128];                                                                           \
+        kyber_twiddles_host(z, zi);                                                                        \
+        if (cudaMemcpyToSymbol(c_keccak_rc, rc, sizeof rc) != cudaSuccess) return PQCGPU_ECUDA;           \
+        if (cudaMemcpyToSymbol(c_zetas, z, sizeof z) != cudaSuccess) return PQCGPU_ECUDA;                 \
+        if (cudaMemcpyToSymbol(c_zetas_inv, zi, sizeof zi) != cudaSuccess) return PQCGPU_ECUDA;           \
+        return PQCGPU_OK;                                                                                  \
+    }                                                                                                      \
+    }                                                                                                      \
+    }

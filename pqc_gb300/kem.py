@@ -1,0 +1,126 @@
+"""Python mirror of the batched KEM C ABI (include/pqcgpu.h), used by the tests and the benchmark.
+
+Host path: methods take / return `bytes` (instance-major), synchronous.
+Device path: the *_dev methods take torch.uint8 CUDA tensors (instance-major, 16-byte aligned),
+asynchronous on the context stream.
+"""
+import ctypes
+
+from . import _lib
+
+ALGS = {"kyber512": 0, "kyber768": 1, "kyber1024": 2, "kyber1024r2": 3, "newhope1024": 4, "frodo976": 5}
+DEVICE_PTRS = 0x1
+PLAIN = 0x2
+
+
+def alg_id(alg):
+    return ALGS[alg] if isinstance(alg, str) else int(alg)
+
+
+def sizes(alg):
+    lib = _lib.load()
+    v = [ctypes.c_size_t() for _ in range(6)]
+    _lib.check(lib.pqcgpu_alg_sizes(alg_id(alg), *[ctypes.byref(x) for x in v]))
+    return dict(zip(("pk", "sk", "ct", "ss", "kp_coins", "enc_coins"), (x.value for x in v)))
+
+
+def kyber_cpa_sizes(variant, k):
+    du, dv = (11, 5) if (variant == 2 or k == 4) else (10, 4)
+    return {"pk": 384 * k + 32, "sk": 384 * k, "ct": k * du * 32 + dv * 32}
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class Context:
+    def __init__(self, device=0, budget=0):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.pqcgpu_ctx_create(ctypes.byref(h), device, budget))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.pqcgpu_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def wait(self):
+        _lib.check(self.lib.pqcgpu_ctx_wait(self.h))
+
+    @property
+    def launches(self):
+        return int(self.lib.pqcgpu_ctx_launches(self.h))
+
+    @property
+    def stream(self):
+        return self.lib.pqcgpu_ctx_stream(self.h)
+
+    def set_stream(self, stream_handle):
+        _lib.check(self.lib.pqcgpu_ctx_set_stream(self.h, ctypes.c_void_p(stream_handle)))
+
+    # ---- host buffers (bytes) ----
+    def keypair(self, alg, n, coins=None, flags=0):
+        s = sizes(alg)
+        pk = ctypes.create_string_buffer(n * s["pk"])
+        sk = ctypes.create_string_buffer(n * s["sk"])
+        _lib.check(self.lib.pqcgpu_kem_keypair_batch(self.h, alg_id(alg), n, pk, sk, coins, flags))
+        return pk.raw, sk.raw
+
+    def enc(self, alg, n, pk, coins=None, flags=0):
+        s = sizes(alg)
+        ct = ctypes.create_string_buffer(n * s["ct"])
+        ss = ctypes.create_string_buffer(n * s["ss"])
+        _lib.check(self.lib.pqcgpu_kem_enc_batch(self.h, alg_id(alg), n, ct, ss, pk, coins, flags))
+        return ct.raw, ss.raw
+
+    def dec(self, alg, n, ct, sk, flags=0):
+        s = sizes(alg)
+        ss = ctypes.create_string_buffer(n * s["ss"])
+        _lib.check(self.lib.pqcgpu_kem_dec_batch(self.h, alg_id(alg), n, ss, ct, sk, flags))
+        return ss.raw
+
+    def kyber_cpa_keypair(self, variant, k, n, d, flags=0):
+        s = kyber_cpa_sizes(variant, k)
+        pk = ctypes.create_string_buffer(n * s["pk"])
+        sk = ctypes.create_string_buffer(n * s["sk"])
+        _lib.check(self.lib.pqcgpu_kyber_indcpa_keypair_batch(self.h, variant, k, n, pk, sk, d, flags))
+        return pk.raw, sk.raw
+
+    def kyber_cpa_enc(self, variant, k, n, m, pk, coins, flags=0):
+        s = kyber_cpa_sizes(variant, k)
+        ct = ctypes.create_string_buffer(n * s["ct"])
+        _lib.check(self.lib.pqcgpu_kyber_indcpa_enc_batch(self.h, variant, k, n, ct, m, pk, coins, flags))
+        return ct.raw
+
+    def kyber_cpa_dec(self, variant, k, n, ct, sk, flags=0):
+        m = ctypes.create_string_buffer(n * 32)
+        _lib.check(self.lib.pqcgpu_kyber_indcpa_dec_batch(self.h, variant, k, n, m, ct, sk, flags))
+        return m.raw
+
+    # ---- device tensors (torch.uint8 on this context's device), asynchronous ----
+    def keypair_dev(self, alg, n, pk, sk, coins, flags=0):
+        _lib.check(self.lib.pqcgpu_kem_keypair_batch(self.h, alg_id(alg), n, _ptr(pk), _ptr(sk), _ptr(coins),
+                                                     flags | DEVICE_PTRS))
+
+    def enc_dev(self, alg, n, ct, ss, pk, coins, flags=0):
+        _lib.check(self.lib.pqcgpu_kem_enc_batch(self.h, alg_id(alg), n, _ptr(ct), _ptr(ss), _ptr(pk), _ptr(coins),
+                                                 flags | DEVICE_PTRS))
+
+    def dec_dev(self, alg, n, ss, ct, sk, flags=0):
+        _lib.check(self.lib.pqcgpu_kem_dec_batch(self.h, alg_id(alg), n, _ptr(ss), _ptr(ct), _ptr(sk),
+                                                 flags | DEVICE_PTRS))
+
+    # host-pointer call on raw addresses (pinned torch tensors), synchronous
+    def enc_host_ptrs(self, alg, n, ct, ss, pk, coins, flags=0):
+        _lib.check(self.lib.pqcgpu_kem_enc_batch(self.h, alg_id(alg), n, _ptr(ct), _ptr(ss), _ptr(pk), _ptr(coins),
+                                                 flags))
+
+    def dec_host_ptrs(self, alg, n, ss, ct, sk, flags=0):
+        _lib.check(self.lib.pqcgpu_kem_dec_batch(self.h, alg_id(alg), n, _ptr(ss), _ptr(ct), _ptr(sk), flags))
