@@ -1,0 +1,395 @@
+"""Benchmark: Kyber-768 encapsulation + decapsulation throughput on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--batch B]
+                    [--path fused|plain]
+
+One step = one Kyber-768 encapsulation batch of B instances followed by the decapsulation of its
+ciphertexts (B = 65536 per GPU), keys resident in HBM (generated once before timing), fresh
+encapsulation coins for every step.  `value` is enc+dec pairs per second over all ranks with the
+inputs already in HBM, timed with CUDA events on the library's stream; `e2e` is the same metric
+through the host-buffer C ABI (pinned host memory; H2D of pk, coins, ct, sk and D2H of ct and both
+shared secrets inside the timed region).  The fused path is the headline; the plain per-stage path
+(one kernel per stage, thread per instance, intermediates in HBM) is timed beside it.
+
+Multi-GPU (torchrun): every rank runs an independent replica on its own GPU (KEM instances are
+independent; no collective on the data path), `value` = pairs of all ranks / max rank time.
+--impl reference: times the CPU restatement of the same workload (the reference has no round-3
+Kyber-768 KEM code) on all host cores of rank 0 and prints the reference line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALG = "kyber768"
+METRIC = "Kyber-768 encaps+decaps/sec (batched, bit-exact)"
+UNIT = "enc+dec pairs/s"
+# Keccak-f[1600] cost in this implementation's 32-bit formulation, per permutation:
+# 24 rounds x (theta 20 LOP3 + D 20 + theta-apply 50 XOR + rho 48 SHF + chi 50 LOP3 + iota 2) = 4560
+OPS_PER_PERM = 4560
+# One Kyber butterfly: Montgomery multiply (2 IMAD + sign-extend + IMAD + shift) + add + sub
+OPS_PER_BUTTERFLY = 8
+# Serial sponges of a Kyber-768 KEM (SHA3 rate 136, SHA3-512 rate 72): permutations per instance
+# H(coins) 1, H(pk) 9, G 1 (encaps prologue); H(c) 9, KDF 1 (encaps epilogue / decaps)
+ENC_HASH_PERMS = 1 + 9 + 1 + 9 + 1
+DEC_HASH_PRE_PERMS = 9
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=60)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--batch", type=int, default=65536)
+    p.add_argument("--path", default="fused", choices=["fused", "plain"])
+    p.add_argument("--no-plain", action="store_true", help="skip timing the plain path beside the fused one")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks / throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(nsample=16384, nthreads=0):
+    """The CPU restatement (oracle/, C with OpenMP) on a bounded sample of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    from pqc_gb300 import drbg
+    a = O.KYBER768
+    s = O.alg_sizes(a)
+    seed = drbg.seed48(12345)
+    pk, sk = O.batch_keypair(a, nsample, drbg.stream(seed, b"kp", nsample * s["kp_coins"]), nthreads)
+    ec = drbg.stream(seed, b"enc", nsample * s["enc_coins"])
+    t0 = time.perf_counter()
+    ct, ss = O.batch_enc(a, nsample, pk, ec, nthreads)
+    ss2 = O.batch_dec(a, nsample, ct, sk, nthreads)
+    el = time.perf_counter() - t0
+    assert ss == ss2
+    cores = nthreads if nthreads > 0 else os.cpu_count()
+    return {"value": nsample / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d Kyber-768 enc+dec pairs, keys pre-generated, OpenMP over instances" % nsample,
+            "seconds": el}
+
+
+def work_per_pair():
+    """Keccak permutations and NTT butterflies per Kyber-768 enc and dec, counted by the oracle's
+    instrumented permutation / butterfly functions on 64 instances (single thread)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    from pqc_gb300 import drbg
+    a = O.KYBER768
+    s = O.alg_sizes(a)
+    n = 64
+    seed = drbg.seed48(4242)
+    pk, sk = O.batch_keypair(a, n, drbg.stream(seed, b"kp", n * s["kp_coins"]), 1)
+    O.counters_reset()
+    ct, _ = O.batch_enc(a, n, pk, drbg.stream(seed, b"enc", n * s["enc_coins"]), 1)
+    ep, eb = O.counters()
+    O.counters_reset()
+    O.batch_dec(a, n, ct, sk, 1)
+    dp, db = O.counters()
+    return {"enc_perms": ep / n, "enc_bfly": eb / n, "dec_perms": dp / n, "dec_bfly": db / n}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    nthreads = 0
+    sample = 16384
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    from pqc_gb300 import drbg
+    a = O.KYBER768
+    s = O.alg_sizes(a)
+    seed = drbg.seed48(777)
+    pk, sk = O.batch_keypair(a, sample, drbg.stream(seed, b"kp", sample * s["kp_coins"]), nthreads)
+    times = []
+    for step in range(args.warmup + args.steps):
+        ec = drbg.stream(seed, b"enc%d" % step, sample * s["enc_coins"])
+        t0 = time.perf_counter()
+        ct, ss = O.batch_enc(a, sample, pk, ec, nthreads)
+        ss2 = O.batch_dec(a, sample, ct, sk, nthreads)
+        el = time.perf_counter() - t0
+        assert ss == ss2
+        if step >= args.warmup:
+            times.append(el)
+    tot = sum(times)
+    v = sample * len(times) / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
+        "data": "synthetic (SHAKE-256 DRBG seeded coins)",
+        "config": {"workload": "kyber768 enc+dec, %d-pair sample per step on host cores" % sample,
+                   "alg": ALG, "batch": args.batch, "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                         "sample": "%d pairs per step; the reference tree has no round-3 Kyber-768 KEM, so its "
+                                   "CPU restatement (oracle/, C + OpenMP) is timed" % sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    from pqc_gb300 import _lib, drbg, kem
+    lib = _lib.load()
+    B, K, W = args.batch, args.steps, args.warmup
+    s = kem.sizes(ALG)
+    ctx = kem.Context(local)
+    st = torch.cuda.ExternalStream(ctx.stream, device=dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+
+    seed = drbg.seed48(1000 + rank)
+    up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
+    pk = torch.empty(B * s["pk"], dtype=torch.uint8, device=dev)
+    sk = torch.empty(B * s["sk"], dtype=torch.uint8, device=dev)
+    ct = torch.empty(B * s["ct"], dtype=torch.uint8, device=dev)
+    ss = torch.empty(B * s["ss"], dtype=torch.uint8, device=dev)
+    ss2 = torch.empty_like(ss)
+    kc = up(drbg.stream(seed, b"kp", B * s["kp_coins"]))
+    coins = [up(drbg.stream(seed, b"enc%d" % i, B * s["enc_coins"])) for i in range(W + K)]
+    torch.cuda.synchronize(dev)
+    ctx.keypair_dev(ALG, B, pk, sk, kc)
+    ctx.wait()
+    flags = kem.PLAIN if args.path == "plain" else 0
+
+    def step(i, fl=flags):
+        ctx.enc_dev(ALG, B, ct, ss, pk, coins[i], fl)
+        ctx.dec_dev(ALG, B, ss2, ct, sk, fl)
+
+    for i in range(W):
+        step(i)
+    ctx.wait()
+    barrier()
+    ok = torch.equal(ss, ss2)
+
+    # ---- timed region (device-resident inputs) ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    lib.pqcgpu_profile_enable(1)
+    launches0 = ctx.launches
+    barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    for i in range(K):
+        evs[i][0].record(st)
+        step(W + i)
+        evs[i][1].record(st)
+    ctx.wait()
+    barrier()
+    launches = ctx.launches - launches0
+    lib.pqcgpu_profile_enable(0)
+    buf = __import__("ctypes").create_string_buffer(1 << 16)
+    _lib.check(lib.pqcgpu_profile_read(buf, len(buf)))
+    prof = json.loads(buf.value.decode())
+    clk = clocks.stop()
+    ok = ok and torch.equal(ss, ss2)
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = evs[0][0].elapsed_time(evs[-1][1])
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * B * K / (total_ms * 1e-3)
+
+    # ---- plain path beside it (same inputs, same outputs) ----
+    plain = None
+    if not args.no_plain and args.path == "fused":
+        try:
+            step(0, kem.PLAIN)
+            ctx.wait()
+            ref_ss = ss.clone()
+            step(0, 0)
+            ctx.wait()
+            same = torch.equal(ref_ss, ss)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for i in range(min(K, 3)):
+                step(W + i, kem.PLAIN)
+            e1.record(st)
+            ctx.wait()
+            pms = e0.elapsed_time(e1) / min(K, 3)
+            plain = {"value": B / (pms * 1e-3), "unit": UNIT, "ms_per_step": pms, "bit_exact_vs_fused": same}
+        except RuntimeError as e:
+            plain = {"unavailable": str(e)}
+
+    # ---- end to end through the host-buffer C ABI ----
+    e2e = None
+    if not args.no_e2e:
+        h = {k: torch.empty(B * s[k], dtype=torch.uint8).pin_memory() for k in ("pk", "sk", "ct")}
+        h["ss"] = torch.empty(B * s["ss"], dtype=torch.uint8).pin_memory()
+        h["ss2"] = torch.empty(B * s["ss"], dtype=torch.uint8).pin_memory()
+        h["pk"].copy_(pk.cpu())
+        h["sk"].copy_(sk.cpu())
+        hcoins = [c.cpu().pin_memory() for c in coins]
+
+        def hstep(i):
+            ctx.enc_host_ptrs(ALG, B, h["ct"], h["ss"], h["pk"], hcoins[i])
+            ctx.dec_host_ptrs(ALG, B, h["ss2"], h["ct"], h["sk"])
+
+        for i in range(min(W, 2)):
+            hstep(i)
+        barrier()
+        t0 = time.perf_counter()
+        for i in range(K):
+            hstep(W + i)
+        el = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([el], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        ok = ok and torch.equal(h["ss"], h["ss2"])
+        e2e = {"value": world * B * K / el, "unit": UNIT,
+               "h2d_bytes_per_step": B * (s["pk"] + s["enc_coins"] + s["ct"] + s["sk"]),
+               "d2h_bytes_per_step": B * (s["ct"] + 2 * s["ss"]), "ms_per_step": 1e3 * el / K}
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel (integer pipe) ----
+    w = work_per_pair()
+    io = ctypes_peaks(lib, local)
+    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
+    roof = None
+    if dom:
+        name, (nl, tms) = dom
+        per_launch_ms = tms / nl
+        if "enc_core" in name:
+            perms, bfly = w["enc_perms"] - ENC_HASH_PERMS, w["enc_bfly"]
+        elif "dec_core" in name:
+            perms, bfly = w["dec_perms"] - DEC_HASH_PRE_PERMS, w["dec_bfly"]
+        else:
+            perms, bfly = ENC_HASH_PERMS, 0
+        ops = B * (perms * OPS_PER_PERM + bfly * OPS_PER_BUTTERFLY)
+        achieved = ops / (per_launch_ms * 1e-3) / 1e12
+        peak = io["int_ops_per_s"] / 1e12
+        traffic = None
+        tfile = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tfile):
+            tj = json.load(open(tfile))
+            if name in tj:
+                traffic = tj[name]["dram_bytes_per_instance"] * B
+        roof = {"bound": "alu", "kernel": name, "achieved": achieved, "peak": peak, "unit": "Tops/s (int32)",
+                "frac": achieved / peak, "traffic": traffic,
+                "peak_source": "measured in this run: LOP3 throughput probe (pqcgpu_probe_peaks)",
+                "algorithmic_ops_per_launch": ops, "launch_ms": per_launch_ms,
+                "keccak_perms_per_s": B * perms / (per_launch_ms * 1e-3),
+                "keccak_perm_peak_per_s": io["keccak_perms_per_s"],
+                "hbm_gbs_io": None}
+    base = cpu_baseline()
+    lat = sorted(step_ms)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int16", "data": "synthetic (keys and coins from a seeded SHAKE-256 DRBG)",
+        "config": {"workload": "kyber768 encaps+decaps, batch %d per GPU, keys resident in HBM" % B,
+                   "alg": ALG, "batch": B, "path": args.path, "parallelism": "replicas x%d" % world,
+                   "l2": "inputs larger than L2 (%.0f MB of pk/sk/ct/coins per step)" %
+                         (B * (s["pk"] + s["sk"] + s["ct"] + s["enc_coins"]) / 1e6)},
+        "bit_exact_check": bool(ok),
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                       "what": "one enc+dec batch of %d" % B},
+        "plain": plain,
+        "fused_over_plain": (value / world / plain["value"]) if plain and "value" in plain else None,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
+        "roofline": roof,
+        "cpu_baseline": base,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def ctypes_peaks(lib, device):
+    import ctypes
+    a, b = ctypes.c_double(), ctypes.c_double()
+    rc = lib.pqcgpu_probe_peaks(device, ctypes.byref(a), ctypes.byref(b))
+    if rc != 0:
+        raise RuntimeError("peak probe failed")
+    return {"int_ops_per_s": a.value, "keccak_perms_per_s": b.value}
+
+
+if __name__ == "__main__":
+    main()

@@ -102,6 +102,22 @@ int pqcgpu_kyber_indcpa_enc_batch(pqcgpu_ctx *ctx, int variant, int k, size_t n,
 int pqcgpu_kyber_indcpa_dec_batch(pqcgpu_ctx *ctx, int variant, int k, size_t n, uint8_t *m, const uint8_t *ct,
                                   const uint8_t *sk, unsigned flags);
 
+/* ---- launch-shape tuning (used by the autotuner) -----------------------------------------
+ * Kyber core kernels: op 0 keypair, 1 encaps, 2 decaps; k = 2..4; ni = instances per CTA (1..128),
+ * threads per CTA (multiple of 32, 32..512).  Applies to all contexts of the process. */
+int pqcgpu_kyber_set_shape(int op, int k, int ni, int threads);
+int pqcgpu_kyber_get_shape(int op, int k, int *ni, int *threads);
+
+/* ---- tracing and roofline probes ------------------------------------------------------------
+ * pqcgpu_profile_enable(1): every kernel launch is bracketed by CUDA events on its stream.
+ * pqcgpu_profile_read: JSON {"kernel<k,v>": [launches, total_ms], ...} of the records since the
+ * last read (synchronises on them), then clears them.
+ * pqcgpu_probe_peaks: measured integer-pipe (LOP3) op rate and register-resident Keccak-f[1600]
+ * permutation rate of `device`, the denominators of the integer roofline. */
+int pqcgpu_profile_enable(int on);
+int pqcgpu_profile_read(char *buf, size_t len);
+int pqcgpu_probe_peaks(int device, double *int_ops_per_s, double *keccak_perms_per_s);
+
 /* ---- NIST single-instance API per parameter set (crypto_kem_* of each api.h) -------------
  * Randomness comes from the library DRBG (pqcgpu_randombytes_init); device 0, default context. */
 int pqcgpu_randombytes_init(const uint8_t seed[48]);

@@ -27,6 +27,11 @@ SIGNATURES = {
     "pqcgpu_kyber_indcpa_keypair_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_kyber_indcpa_enc_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_kyber_indcpa_dec_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_kyber_set_shape": (_int, [_int, _int, _int, _int]),
+    "pqcgpu_kyber_get_shape": (_int, [_int, _int, _c.POINTER(_int), _c.POINTER(_int)]),
+    "pqcgpu_profile_enable": (_int, [_int]),
+    "pqcgpu_profile_read": (_int, [_c.c_char_p, _sz]),
+    "pqcgpu_probe_peaks": (_int, [_int, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]),
     "pqcgpu_randombytes_init": (_int, [_u8p]),
     "pqcgpu_randombytes": (_int, [_u8p, _sz]),
 }

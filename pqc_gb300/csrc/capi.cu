@@ -434,8 +434,10 @@ extern "C" int pqcgpu_kem_keypair_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n,
         d.out_sz[0] = ai.pk;
         d.out[1] = sk;
         d.out_sz[1] = ai.sk;
-        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
-            return kyber_keypair_dev(variant, k, m, out[0], out[1], in[0], (int)ai.kpc, 1, s);
+        const int plain = (flags & PQCGPU_PLAIN) ? 1 : 0;
+        d.scratch_per = kyber_scratch_bytes(k, 0, plain);
+        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
+            return kyber_keypair_dev(variant, k, m, out[0], out[1], in[0], (int)ai.kpc, 1, scr, plain, s);
         });
     }
     return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
@@ -461,9 +463,10 @@ extern "C" int pqcgpu_kem_enc_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uin
         d.out_sz[0] = ai.ct;
         d.out[1] = ss;
         d.out_sz[1] = ai.ss;
-        d.scratch_per = 96;
+        const int plain = (flags & PQCGPU_PLAIN) ? 1 : 0;
+        d.scratch_per = kyber_scratch_bytes(k, 1, plain);
         return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
-            return kyber_enc_dev(variant, k, m, out[0], out[1], in[0], nullptr, in[1], scr, 1, s);
+            return kyber_enc_dev(variant, k, m, out[0], out[1], in[0], nullptr, in[1], scr, 1, plain, s);
         });
     }
     return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
@@ -484,9 +487,10 @@ extern "C" int pqcgpu_kem_dec_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uin
         d.nout = 1;
         d.out[0] = ss;
         d.out_sz[0] = ai.ss;
-        d.scratch_per = 32;
+        const int plain = (flags & PQCGPU_PLAIN) ? 1 : 0;
+        d.scratch_per = kyber_scratch_bytes(k, 2, plain);
         return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
-            return kyber_dec_dev(variant, k, m, out[0], in[0], in[1], scr, 1, s);
+            return kyber_dec_dev(variant, k, m, out[0], in[0], in[1], scr, 1, plain, s);
         });
     }
     return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
@@ -512,7 +516,7 @@ extern "C" int pqcgpu_kyber_indcpa_keypair_batch(pqcgpu_ctx *c, int variant, int
     d.out[1] = sk;
     d.out_sz[1] = 384 * k;
     return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
-        return kyber_keypair_dev(variant, k, m, out[0], out[1], in[0], 32, 0, s);
+        return kyber_keypair_dev(variant, k, m, out[0], out[1], in[0], 32, 0, nullptr, 0, s);
     });
 }
 extern "C" int pqcgpu_kyber_indcpa_enc_batch(pqcgpu_ctx *c, int variant, int k, size_t n, uint8_t *ct,
@@ -531,7 +535,7 @@ extern "C" int pqcgpu_kyber_indcpa_enc_batch(pqcgpu_ctx *c, int variant, int k, 
     d.out[0] = ct;
     d.out_sz[0] = kyber_cpa_ct(variant, k);
     return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
-        return kyber_enc_dev(variant, k, m, out[0], nullptr, in[0], in[1], in[2], nullptr, 0, s);
+        return kyber_enc_dev(variant, k, m, out[0], nullptr, in[0], in[1], in[2], nullptr, 0, 0, s);
     });
 }
 extern "C" int pqcgpu_kyber_indcpa_dec_batch(pqcgpu_ctx *c, int variant, int k, size_t n, uint8_t *msg,
@@ -547,8 +551,32 @@ extern "C" int pqcgpu_kyber_indcpa_dec_batch(pqcgpu_ctx *c, int variant, int k, 
     d.out[0] = msg;
     d.out_sz[0] = 32;
     return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
-        return kyber_dec_dev(variant, k, m, out[0], in[0], in[1], nullptr, 0, s);
+        return kyber_dec_dev(variant, k, m, out[0], in[0], in[1], nullptr, 0, 0, s);
     });
+}
+
+extern "C" int pqcgpu_kyber_set_shape(int op, int k, int ni, int threads) {
+    const int rc = kyber_set_shape(op, k, ni, threads);
+    return rc ? set_err(rc, "bad launch shape") : PQCGPU_OK;
+}
+extern "C" int pqcgpu_kyber_get_shape(int op, int k, int *ni, int *threads) {
+    if (!ni || !threads) return set_err(PQCGPU_EINVAL, "null output");
+    return kyber_get_shape(op, k, ni, threads);
+}
+
+extern "C" int pqcgpu_profile_enable(int on) {
+    prof_enable(on != 0);
+    return PQCGPU_OK;
+}
+extern "C" int pqcgpu_profile_read(char *buf, size_t len) {
+    const std::string s = prof_read();
+    if (!buf || len < s.size() + 1) return set_err(PQCGPU_EINVAL, "profile buffer too small");
+    memcpy(buf, s.c_str(), s.size() + 1);
+    return PQCGPU_OK;
+}
+extern "C" int pqcgpu_probe_peaks(int device, double *int_ops_per_s, double *keccak_perms_per_s) {
+    const int rc = probe_peaks(device, int_ops_per_s, keccak_perms_per_s);
+    return rc ? set_err(rc, "probe failed") : PQCGPU_OK;
 }
 
 // ---- NIST single-instance API (default context on device 0) ----

@@ -3,13 +3,16 @@
 
 namespace pqc {
 namespace kyber {
-int g_ni[3][3] = {{16, 16, 16}, {16, 16, 16}, {16, 16, 16}};
+// Launch shape of the core kernels, [op][k-2] with op 0 keypair, 1 enc, 2 dec.  One thread per
+// matrix entry (NI * k^2 jobs) sized against the shared memory each instance needs.
+int g_ni[3][3] = {{28, 28, 16}, {32, 28, 32}, {48, 28, 32}};
+int g_threads[3][3] = {{128, 256, 256}, {128, 256, 256}, {224, 256, 256}};
 
 #define PQC_KYBER_DECL(K, V)                                                                               \
-    int keypair_##K##_##V(int, uint8_t *, uint8_t *, const uint8_t *, int, int, cudaStream_t);            \
+    int keypair_##K##_##V(int, uint8_t *, uint8_t *, const uint8_t *, int, int, uint8_t *, int, cudaStream_t); \
     int enc_##K##_##V(int, uint8_t *, uint8_t *, const uint8_t *, const uint8_t *, const uint8_t *, uint8_t *, int, \
-                      cudaStream_t);                                                                       \
-    int dec_##K##_##V(int, uint8_t *, const uint8_t *, const uint8_t *, uint8_t *, int, cudaStream_t);     \
+                      int, cudaStream_t);                                                                  \
+    int dec_##K##_##V(int, uint8_t *, const uint8_t *, const uint8_t *, uint8_t *, int, int, cudaStream_t); \
     int init_##K##_##V();
 PQC_KYBER_DECL(2, 3)
 PQC_KYBER_DECL(3, 3)
@@ -31,16 +34,20 @@ PQC_KYBER_DECL(4, 2)
     }
 
 int kyber_keypair_dev(int variant, int k, int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int coins_stride,
-                      int kem, cudaStream_t st) {
-    PQC_KYBER_DISPATCH(keypair, n, pk, sk, coins, coins_stride, kem, st)
+                      int kem, uint8_t *scratch, int plain, cudaStream_t st) {
+    PQC_KYBER_DISPATCH(keypair, n, pk, sk, coins, coins_stride, kem, scratch, plain, st)
 }
 int kyber_enc_dev(int variant, int k, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m,
-                  const uint8_t *coins, uint8_t *scratch, int kem, cudaStream_t st) {
-    PQC_KYBER_DISPATCH(enc, n, ct, ss, pk, m, coins, scratch, kem, st)
+                  const uint8_t *coins, uint8_t *scratch, int kem, int plain, cudaStream_t st) {
+    PQC_KYBER_DISPATCH(enc, n, ct, ss, pk, m, coins, scratch, kem, plain, st)
 }
 int kyber_dec_dev(int variant, int k, int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch,
-                  int kem, cudaStream_t st) {
-    PQC_KYBER_DISPATCH(dec, n, out, ct, sk, scratch, kem, st)
+                  int kem, int plain, cudaStream_t st) {
+    PQC_KYBER_DISPATCH(dec, n, out, ct, sk, scratch, kem, plain, st)
+}
+size_t kyber_scratch_bytes(int k, int op, int plain) {
+    if (plain) return (size_t)(k * k + 4 * k + 4) * 256 * 2 + 208;
+    return op == 1 ? 96 : (op == 2 ? 32 : 0);
 }
 int kyber_init_constants() {
     int (*inits[])() = {kyber::init_2_3, kyber::init_3_3, kyber::init_4_3,
@@ -51,9 +58,18 @@ int kyber_init_constants() {
     }
     return PQCGPU_OK;
 }
-void kyber_set_ni(int op, int k, int ni) {
-    if (op >= 0 && op < 3 && k >= 2 && k <= 4 && ni > 0) kyber::g_ni[op][k - 2] = ni;
+int kyber_set_shape(int op, int k, int ni, int threads) {
+    if (op < 0 || op > 2 || k < 2 || k > 4 || ni <= 0 || ni > 128 || threads < 32 || threads > 512 || threads % 32)
+        return PQCGPU_EINVAL;
+    kyber::g_ni[op][k - 2] = ni;
+    kyber::g_threads[op][k - 2] = threads;
+    return PQCGPU_OK;
 }
-int kyber_get_ni(int op, int k) { return (op >= 0 && op < 3 && k >= 2 && k <= 4) ? kyber::g_ni[op][k - 2] : -1; }
+int kyber_get_shape(int op, int k, int *ni, int *threads) {
+    if (op < 0 || op > 2 || k < 2 || k > 4) return PQCGPU_EINVAL;
+    *ni = kyber::g_ni[op][k - 2];
+    *threads = kyber::g_threads[op][k - 2];
+    return PQCGPU_OK;
+}
 
 }  // namespace pqc

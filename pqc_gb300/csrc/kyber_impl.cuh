@@ -123,38 +123,34 @@ __device__ __forceinline__ void noise_poly(const uint2 *seed, int nonce, F emit)
 // Matrix rows: stream SHAKE128(rho || x || y), rejection-sample, multiply into the accumulator.
 // ---------------------------------------------------------------------------------------------
 
-// acc (shared, one polynomial) {=, +=} A_entry o b, with the final Barrett of pointwise_acc when
-// LAST.  Candidates are consumed in order, pairs (2p, 2p+1) are multiplied as soon as complete.
+// One matrix entry per thread: stream SHAKE128(rho || x || y), rejection-sample in order, and as
+// soon as a coefficient pair (2p, 2p+1) is complete multiply it with b (basemul) and add it into
+// the shared accumulator with one 32-bit shared-memory atomic.  The two int16 products are packed
+// with a bias of 2q each: a basemul output lies in (-2q, 2q), so a biased term lies in (0, 4q) and
+// the sum of at most four terms stays below 2^16 -- the halves never carry into each other.  The
+// consumer subtracts K * 2q from each half, which yields exactly the reference's int16 sum of the
+// K products (that sum cannot wrap: |sum| < 8q < 2^15), before the Barrett of pointwise_acc.
+constexpr uint32_t ACC_BIAS = 2 * Q;
+
 template <int V>
-struct RowSampler {
+struct EntrySampler {
     int ctr;
     int16_t even;
     const int16_t *b;  // shared polynomial b (NTT domain)
-    int16_t *acc;
+    uint32_t *acc;     // shared accumulator polynomial viewed as packed pairs
     const int16_t *sz;
-    bool first, last;
 
     __device__ __forceinline__ void take(uint32_t d) {
         const uint32_t bound = (V == 2) ? (uint32_t)(19 * Q) : (uint32_t)Q;
         if (d < bound && ctr < N) {
-            int16_t a = (V == 2) ? (int16_t)(d - (d >> 12) * Q) : (int16_t)d;
+            const int16_t a = (V == 2) ? (int16_t)(d - (d >> 12) * Q) : (int16_t)d;
             if (ctr & 1) {
                 const int p = ctr >> 1;
                 const int o = phys(2 * p);
                 const uint32_t bb = *reinterpret_cast<const uint32_t *>(b + o);
                 int16_t r0, r1;
                 basemul(r0, r1, even, a, (int16_t)(bb & 0xffff), (int16_t)(bb >> 16), pair_zeta(sz, p));
-                uint32_t *ap = reinterpret_cast<uint32_t *>(acc + o);
-                if (!first) {
-                    const uint32_t av = *ap;
-                    r0 = (int16_t)(r0 + (int16_t)(av & 0xffff));
-                    r1 = (int16_t)(r1 + (int16_t)(av >> 16));
-                }
-                if (last) {
-                    r0 = barrett(r0);
-                    r1 = barrett(r1);
-                }
-                *ap = pack2(r0, r1);
+                atomicAdd(acc + (o >> 1), (uint32_t)((int)r0 + (int)ACC_BIAS) | ((uint32_t)((int)r1 + (int)ACC_BIAS) << 16));
             } else {
                 even = a;
             }
@@ -163,55 +159,65 @@ struct RowSampler {
     }
 };
 
-template <int K, int V>
-__device__ __forceinline__ void matrix_row(const uint2 *rho, int row, bool transposed, const int16_t *bvec,
-                                           int16_t *acc, const int16_t *sz) {
-    for (int j = 0; j < K; j++) {
-        uint2 A[25];
-        keccak_zero(A);
+// Accumulate A[row][col] o b into acc, where A[i][j] = XOF(rho || j || i) (gen_matrix,
+// indcpa.cu:339-403) and the transposed matrix uses XOF(rho || i || j).
+template <int V>
+__device__ __forceinline__ void matrix_entry(const uint2 *rho, int row, int col, bool transposed, const int16_t *b,
+                                             int16_t *acc, const int16_t *sz) {
+    uint2 A[25];
+    keccak_zero(A);
 #pragma unroll
-        for (int i = 0; i < 4; i++) A[i] = rho[i];
-        // gen_matrix: A[i][j] = XOF(rho || j || i); transposed: XOF(rho || i || j)
-        const uint32_t x = transposed ? row : j, y = transposed ? j : row;
-        A[4].x = x | (y << 8) | (DOM_SHAKE << 16);
-        A[SHAKE128_LANES - 1].y ^= 0x80000000u;
-        RowSampler<V> s;
-        s.ctr = 0;
-        s.even = 0;
-        s.b = bvec + j * POLY_PITCH;
-        s.acc = acc;
-        s.sz = sz;
-        s.first = (j == 0);
-        s.last = (j == K - 1);
-        while (s.ctr < N) {
-            keccak_f1600(A);
-            if (V == 3) {
-                // 56 triplets, two 12-bit candidates each (round-3 Parse)
+    for (int i = 0; i < 4; i++) A[i] = rho[i];
+    const uint32_t x = transposed ? row : col, y = transposed ? col : row;
+    A[4].x = x | (y << 8) | (DOM_SHAKE << 16);
+    A[SHAKE128_LANES - 1].y ^= 0x80000000u;
+    EntrySampler<V> s;
+    s.ctr = 0;
+    s.even = 0;
+    s.b = b;
+    s.acc = reinterpret_cast<uint32_t *>(acc);
+    s.sz = sz;
+    while (s.ctr < N) {
+        keccak_f1600(A);
+        if (V == 3) {
+            // 56 triplets, two 12-bit candidates each (round-3 Parse)
 #pragma unroll
-                for (int t = 0; t < 56; t++) {
-                    const int o = 3 * t, wi = o >> 2, sh = 8 * (o & 3);
-                    const uint32_t w0 = (wi & 1) ? A[wi >> 1].y : A[wi >> 1].x;
-                    uint32_t v;
-                    if (sh <= 8) {
-                        v = w0 >> sh;
-                    } else {
-                        const uint32_t w1 = ((wi + 1) & 1) ? A[(wi + 1) >> 1].y : A[(wi + 1) >> 1].x;
-                        v = __funnelshift_r(w0, w1, sh);
-                    }
-                    s.take(v & 0xfff);
-                    s.take((v >> 12) & 0xfff);
+            for (int t = 0; t < 56; t++) {
+                const int o = 3 * t, wi = o >> 2, sh = 8 * (o & 3);
+                const uint32_t w0 = (wi & 1) ? A[wi >> 1].y : A[wi >> 1].x;
+                uint32_t v;
+                if (sh <= 8) {
+                    v = w0 >> sh;
+                } else {
+                    const uint32_t w1 = ((wi + 1) & 1) ? A[(wi + 1) >> 1].y : A[(wi + 1) >> 1].x;
+                    v = __funnelshift_r(w0, w1, sh);
                 }
-            } else {
-                // 84 little-endian 16-bit candidates (rej_uniform, indcpa.cu:290-322)
+                s.take(v & 0xfff);
+                s.take((v >> 12) & 0xfff);
+            }
+        } else {
+            // 84 little-endian 16-bit candidates (rej_uniform, indcpa.cu:290-322)
 #pragma unroll
-                for (int t = 0; t < 42; t++) {
-                    const uint32_t w0 = (t & 1) ? A[t >> 1].y : A[t >> 1].x;
-                    s.take(w0 & 0xffff);
-                    s.take(w0 >> 16);
-                }
+            for (int t = 0; t < 42; t++) {
+                const uint32_t w0 = (t & 1) ? A[t >> 1].y : A[t >> 1].x;
+                s.take(w0 & 0xffff);
+                s.take(w0 >> 16);
             }
         }
     }
+}
+
+// Undo the accumulator bias of K terms and apply pointwise_acc's Barrett.
+template <int K>
+__device__ __forceinline__ int16_t unbias(int16_t biased) {
+    return barrett((int16_t)((int)(uint16_t)biased - (int)(K * ACC_BIAS)));
+}
+
+// Zero `npoly` consecutive shared polynomials starting at p (all threads of the CTA).
+__device__ __forceinline__ void zero_polys(int16_t *p, int npoly) {
+    uint4 *q = reinterpret_cast<uint4 *>(p);
+    const int n16 = npoly * (POLY_PITCH / 8);
+    for (int i = threadIdx.x; i < n16; i += blockDim.x) q[i] = make_uint4(0, 0, 0, 0);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -346,7 +352,8 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
     using Pp = P<K, V>;
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
 
-    // (1) r = CBD_eta1(PRF(coins, i)), i < K  -> slots [0, K)
+    // (1) r = CBD_eta1(PRF(coins, i)), i < K  -> slots [0, K); zero the u accumulators
+    for (int li = 0; li < ni; li++) zero_polys(slot<K, V>(polys, li, K), K);
     for (int job = tid; job < ni * K; job += nthr) {
         const int li = job / K, i = job % K;
         const uint2 *seed = DEC ? reinterpret_cast<const uint2 *>(seeds + li * 128 + 32)
@@ -358,12 +365,12 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
     // (2) r-hat = NTT(r)
     for (int w = warp; w < ni * K; w += nwarp) ntt_warp(slot<K, V>(polys, w / K, w % K), sz, lane);
     __syncthreads();
-    // (3) u_i = sum_j A^T[i][j] o r-hat_j, streamed from SHAKE128, one thread per row
-    for (int job = tid; job < ni * K; job += nthr) {
-        const int li = job / K, i = job % K;
-        const uint8_t *pk = DEC ? a.pk + (size_t)(base + li) * a.pk_stride : a.pk + (size_t)(base + li) * a.pk_stride;
-        matrix_row<K, V>(reinterpret_cast<const uint2 *>(pk + Pp::POLYVECBYTES), i, true, slot<K, V>(polys, li, 0),
-                         slot<K, V>(polys, li, K + i), sz);
+    // (3) u_i += A^T[i][j] o r-hat_j, streamed from SHAKE128, one thread per matrix entry
+    for (int job = tid; job < ni * K * K; job += nthr) {
+        const int li = job / (K * K), i = (job / K) % K, j = job % K;
+        const uint8_t *pk = a.pk + (size_t)(base + li) * a.pk_stride;
+        matrix_entry<V>(reinterpret_cast<const uint2 *>(pk + Pp::POLYVECBYTES), i, j, true, slot<K, V>(polys, li, j),
+                        slot<K, V>(polys, li, K + i), sz);
     }
     // (4) v = t-hat o r-hat (warp per instance, t-hat decoded from pk bytes; independent of (3))
     for (int li = warp; li < ni; li += nwarp) {
@@ -384,9 +391,19 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
         store8(slot<K, V>(polys, li, 2 * K) + phys(8 * lane), acc);
     }
     __syncthreads();
-    // (5) inverse NTT of u (K) and v
-    for (int w = warp; w < ni * (K + 1); w += nwarp)
-        invntt_warp(slot<K, V>(polys, w / (K + 1), K + w % (K + 1)), szi, lane);
+    // (5) inverse NTT of u (K, accumulators unbiased + reduced on load) and v
+    for (int w = warp; w < ni * (K + 1); w += nwarp) {
+        int16_t *p = slot<K, V>(polys, w / (K + 1), K + w % (K + 1));
+        if (w % (K + 1) < K) {
+            int16_t c[8];
+            load8(c, p + phys(8 * lane));
+#pragma unroll
+            for (int q = 0; q < 8; q++) c[q] = unbias<K>(c[q]);
+            store8(p + phys(8 * lane), c);
+            __syncwarp();
+        }
+        invntt_warp(p, szi, lane);
+    }
     __syncthreads();
     // (6) u += e1 (nonce K+i, eta2); v += e2 (nonce 2K) + msg; Barrett; compress in place
     for (int job = tid; job < ni * (K + 1); job += nthr) {
@@ -453,10 +470,10 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
 // ---------------------------------------------------------------------------------------------
 // Kernels
 // ---------------------------------------------------------------------------------------------
-constexpr int CORE_THREADS = 128;
+constexpr int CORE_MAX_THREADS = 512;
 
 template <int K, int V>
-__global__ void __launch_bounds__(CORE_THREADS) kyber_enc_core(EncArgs a, int NI) {
+__global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_enc_core(EncArgs a, int NI) {
     extern __shared__ __align__(16) uint8_t smem[];
     int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
     uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (2 * K + 1) * POLY_PITCH);
@@ -468,7 +485,7 @@ __global__ void __launch_bounds__(CORE_THREADS) kyber_enc_core(EncArgs a, int NI
 }
 
 template <int K, int V>
-__global__ void __launch_bounds__(CORE_THREADS) kyber_dec_core(DecArgs d, int NI) {
+__global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, int NI) {
     using Pp = P<K, V>;
     extern __shared__ __align__(16) uint8_t smem[];
     int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
@@ -598,7 +615,7 @@ __global__ void __launch_bounds__(CORE_THREADS) kyber_dec_core(DecArgs d, int NI
 
 // Keypair: slots [0,K) s, [K,2K) e, [2K,3K) t-hat; seeds [0,32) rho, [32,64) sigma.
 template <int K, int V>
-__global__ void __launch_bounds__(CORE_THREADS) kyber_kp_core(KpArgs a, int NI) {
+__global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int NI) {
     using Pp = P<K, V>;
     extern __shared__ __align__(16) uint8_t smem[];
     int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
@@ -623,7 +640,8 @@ __global__ void __launch_bounds__(CORE_THREADS) kyber_kp_core(KpArgs a, int NI) 
         for (int i = 0; i < 8; i++) o[i] = A[i];
     }
     __syncthreads();
-    // (b) s_i = CBD(PRF(sigma, i)), e_i = CBD(PRF(sigma, K + i))
+    // (b) s_i = CBD(PRF(sigma, i)), e_i = CBD(PRF(sigma, K + i)); zero the t-hat accumulators
+    for (int li = 0; li < ni; li++) zero_polys(kslot(li, 2 * K), K);
     for (int job = tid; job < ni * 2 * K; job += nthr) {
         const int li = job / (2 * K), i = job % (2 * K);
         int16_t *dst = kslot(li, i);
@@ -633,11 +651,11 @@ __global__ void __launch_bounds__(CORE_THREADS) kyber_kp_core(KpArgs a, int NI) 
     __syncthreads();
     for (int w = warp; w < ni * 2 * K; w += nwarp) ntt_warp(kslot(w / (2 * K), w % (2 * K)), sz, lane);
     __syncthreads();
-    // (c) t-hat_i = sum_j A[i][j] o s-hat_j (not transposed)
-    for (int job = tid; job < ni * K; job += nthr) {
-        const int li = job / K, i = job % K;
-        matrix_row<K, V>(reinterpret_cast<const uint2 *>(seeds + li * 128), i, false, kslot(li, 0), kslot(li, 2 * K + i),
-                         sz);
+    // (c) t-hat_i += A[i][j] o s-hat_j (not transposed), one thread per matrix entry
+    for (int job = tid; job < ni * K * K; job += nthr) {
+        const int li = job / (K * K), i = (job / K) % K, j = job % K;
+        matrix_entry<V>(reinterpret_cast<const uint2 *>(seeds + li * 128), i, j, false, kslot(li, j), kslot(li, 2 * K + i),
+                        sz);
     }
     __syncthreads();
     // (d) t = reduce(frommont(t) + e); pack pk = t || rho and sk_cpa = s (warp per instance)
@@ -651,7 +669,7 @@ __global__ void __launch_bounds__(CORE_THREADS) kyber_kp_core(KpArgs a, int NI) 
             load8(s, kslot(li, i) + phys(8 * lane));
 #pragma unroll
             for (int q = 0; q < 8; q++) {
-                t[q] = csubq(barrett((int16_t)(mont_reduce((int32_t)t[q] * 1353) + e[q])));
+                t[q] = csubq(barrett((int16_t)(mont_reduce((int32_t)unbias<K>(t[q]) * 1353) + e[q])));
                 s[q] = csubq(s[q]);
             }
             uint8_t bt[12], bs[12];
@@ -759,10 +777,16 @@ __global__ void __launch_bounds__(128) kyber_kp_hash_post(int n, const uint8_t *
     for (int i = 0; i < 4; i++) o[i] = A[i];
 }
 
+}  // namespace kyber
+}  // namespace pqc
+#include "kyber_plain.cuh"
+namespace pqc {
+namespace kyber {
 // ---------------------------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------------------------
-extern int g_ni[3][3];  // [op][k-2]: instances per CTA (kyber.cu)
+extern int g_ni[3][3];       // [op][k-2]: instances per CTA (kyber.cu)
+extern int g_threads[3][3];  // [op][k-2]: threads per CTA (kyber.cu)
 
 template <class Kern>
 static cudaError_t ensure_smem(Kern kern, size_t bytes) {
@@ -771,21 +795,22 @@ static cudaError_t ensure_smem(Kern kern, size_t bytes) {
 
 template <int K, int V>
 static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int coins_stride, int kem,
-                          cudaStream_t st) {
-    const int NI = g_ni[0][K - 2];
+                          uint8_t *scratch, int plain, cudaStream_t st) {
+    if (plain) return kem ? plain_keypair<K, V>(n, pk, sk, coins, coins_stride, scratch, st) : PQCGPU_EUNSUPPORTED;
+    const int NI = g_ni[0][K - 2], NT = g_threads[0][K - 2];
     const size_t sm = Layout<3 * K>::bytes(NI);
     if (ensure_smem(kyber_kp_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     KpArgs a{n, pk, sk, coins, coins_stride, kem};
-    g_launch_count += kem ? 2 : 1;
-    kyber_kp_core<K, V><<<(n + NI - 1) / NI, CORE_THREADS, sm, st>>>(a, NI);
-    if (kem) kyber_kp_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, sk);
+    PQC_LAUNCH(st, "kyber_kp_core", K, V, kyber_kp_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
+    if (kem) PQC_LAUNCH(st, "kyber_kp_hash_post", K, V, kyber_kp_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, sk));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
 template <int K, int V>
 static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
-                      uint8_t *scratch, int kem, cudaStream_t st) {
-    const int NI = g_ni[1][K - 2];
+                      uint8_t *scratch, int kem, int plain, cudaStream_t st) {
+    if (plain) return kem ? plain_enc<K, V>(n, ct, ss, pk, coins, scratch, st) : PQCGPU_EUNSUPPORTED;
+    const int NI = g_ni[1][K - 2], NT = g_threads[1][K - 2];
     const size_t sm = Layout<2 * K + 1>::bytes(NI);
     if (ensure_smem(kyber_enc_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     EncArgs a;
@@ -794,7 +819,8 @@ static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const 
     a.pk = pk;
     a.pk_stride = P<K, V>::PKB;
     if (kem) {
-        kyber_enc_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, coins, scratch);
+        PQC_LAUNCH(st, "kyber_enc_hash_pre", K, V,
+                   kyber_enc_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, coins, scratch));
         a.m = scratch;
         a.m_stride = 96;
         a.r = scratch + 32;
@@ -805,16 +831,18 @@ static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const 
         a.r = coins;
         a.r_stride = 32;
     }
-    g_launch_count += kem ? 3 : 1;
-    kyber_enc_core<K, V><<<(n + NI - 1) / NI, CORE_THREADS, sm, st>>>(a, NI);
-    if (kem) kyber_enc_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, scratch, ss);
+    PQC_LAUNCH(st, "kyber_enc_core", K, V, kyber_enc_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
+    if (kem)
+        PQC_LAUNCH(st, "kyber_enc_hash_post", K, V,
+                   kyber_enc_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, scratch, ss));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
 template <int K, int V>
 static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, int kem,
-                      cudaStream_t st) {
-    const int NI = g_ni[2][K - 2];
+                      int plain, cudaStream_t st) {
+    if (plain) return kem ? plain_dec<K, V>(n, out, ct, sk, scratch, st) : PQCGPU_EUNSUPPORTED;
+    const int NI = g_ni[2][K - 2], NT = g_threads[2][K - 2];
     const size_t sm = Layout<2 * K + 1>::bytes(NI);
     if (ensure_smem(kyber_dec_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     DecArgs d;
@@ -825,9 +853,8 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
     d.ss = kem ? out : nullptr;
     d.hct = scratch;
     d.kem = kem;
-    g_launch_count += kem ? 2 : 1;
-    if (kem) kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, scratch);
-    kyber_dec_core<K, V><<<(n + NI - 1) / NI, CORE_THREADS, sm, st>>>(d, NI);
+    if (kem) PQC_LAUNCH(st, "kyber_dec_hash_pre", K, V, kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, scratch));
+    PQC_LAUNCH(st, "kyber_dec_core", K, V, kyber_dec_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
@@ -839,16 +866,16 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
     namespace pqc {                                                                                        \
     namespace kyber {                                                                                      \
     int keypair_##K##_##V(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cs, int kem,         \
-                          cudaStream_t st) {                                                               \
-        return launch_keypair<K, V>(n, pk, sk, coins, cs, kem, st);                                       \
+                          uint8_t *scratch, int plain, cudaStream_t st) {                                  \
+        return launch_keypair<K, V>(n, pk, sk, coins, cs, kem, scratch, plain, st);                       \
     }                                                                                                      \
     int enc_##K##_##V(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m,               \
-                      const uint8_t *coins, uint8_t *scratch, int kem, cudaStream_t st) {                  \
-        return launch_enc<K, V>(n, ct, ss, pk, m, coins, scratch, kem, st);                               \
+                      const uint8_t *coins, uint8_t *scratch, int kem, int plain, cudaStream_t st) {       \
+        return launch_enc<K, V>(n, ct, ss, pk, m, coins, scratch, kem, plain, st);                        \
     }                                                                                                      \
     int dec_##K##_##V(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, int kem, \
-                      cudaStream_t st) {                                                                   \
-        return launch_dec<K, V>(n, out, ct, sk, scratch, kem, st);                                        \
+                      int plain, cudaStream_t st) {                                                        \
+        return launch_dec<K, V>(n, out, ct, sk, scratch, kem, plain, st);                                 \
     }                                                                                                      \
     int init_##K##_##V() {                                                                                 \
         uint2 rc[24];                                                                                      \

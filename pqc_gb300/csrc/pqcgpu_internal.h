@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <string>
 
 #include "pqcgpu.h"
 
@@ -12,19 +13,38 @@ namespace pqc {
 // Kernel launches issued by this library (all contexts); contexts report deltas.
 extern std::atomic<uint64_t> g_launch_count;
 
+// Launch profiler (probe.cu): CUDA events around each launch on its stream when enabled.
+bool prof_enabled();
+void *prof_begin(cudaStream_t st, const char *name, int k, int v);
+void prof_end(cudaStream_t st, void *tok);
+void prof_enable(bool on);
+std::string prof_read();
+int probe_peaks(int device, double *int_ops, double *keccak_perms);
+
+// Every kernel launch of the library goes through this macro: counted, and timed when profiling.
+#define PQC_LAUNCH(st, name, k, v, ...)                                      \
+    do {                                                                     \
+        void *pqc_tok_ = ::pqc::prof_enabled() ? ::pqc::prof_begin(st, name, k, v) : nullptr; \
+        __VA_ARGS__;                                                         \
+        if (pqc_tok_) ::pqc::prof_end(st, pqc_tok_);                         \
+        ::pqc::g_launch_count++;                                             \
+    } while (0)
+
 // ---- Kyber (kyber.cu) ----
 int kyber_init_constants();
-// op: 0 keypair, 1 enc, 2 dec.  ni = instances per CTA of the core kernel.
-void kyber_set_ni(int op, int k, int ni);
-int kyber_get_ni(int op, int k);
+// op: 0 keypair, 1 enc, 2 dec.  ni = instances per CTA of the core kernel, threads per CTA.
+int kyber_set_shape(int op, int k, int ni, int threads);
+int kyber_get_shape(int op, int k, int *ni, int *threads);
+// Scratch bytes per instance (op 0 keypair, 1 enc, 2 dec; plain = the per-stage baseline path).
+size_t kyber_scratch_bytes(int k, int op, int plain);
 // coins: d (CPA) or d||z (KEM) at `coins_stride`.  kem=1 writes the full KEM secret key.
 int kyber_keypair_dev(int variant, int k, int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int coins_stride,
-                      int kem, cudaStream_t st);
-// kem=1: coins 32 B/instance, scratch >= 96 B/instance, m ignored.  kem=0: CPA enc with m, coins.
+                      int kem, uint8_t *scratch, int plain, cudaStream_t st);
+// kem=1: coins 32 B/instance, m ignored.  kem=0: CPA enc with m, coins.
 int kyber_enc_dev(int variant, int k, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m,
-                  const uint8_t *coins, uint8_t *scratch, int kem, cudaStream_t st);
-// kem=1: out = ss, scratch >= 32 B/instance.  kem=0: out = m (CPA decryption).
+                  const uint8_t *coins, uint8_t *scratch, int kem, int plain, cudaStream_t st);
+// kem=1: out = ss.  kem=0: out = m (CPA decryption).
 int kyber_dec_dev(int variant, int k, int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch,
-                  int kem, cudaStream_t st);
+                  int kem, int plain, cudaStream_t st);
 
 }  // namespace pqc

@@ -174,3 +174,24 @@ def test_nist_single_instance_api(oracle):
         assert pk.raw == opk and sk.raw == osk
         oct_, oss = oracle.batch_enc(a, 1, opk, stream[s["kp_coins"]:])
         assert ct.raw == oct_ and ss.raw == oss
+
+
+@pytest.mark.parametrize("alg", ["kyber512", "kyber768", "kyber1024", "kyber1024r2"])
+def test_plain_path_matches_oracle(ctx, oracle, alg):
+    """The per-stage baseline path (flag PQCGPU_PLAIN) produces the same bytes as the oracle."""
+    from pqc_gb300 import kem
+    s = kem.sizes(alg)
+    a = oracle.ALG_NAMES[alg]
+    n = 300
+    seed = drbg.seed48(31)
+    kc = drbg.stream(seed, b"kp", n * s["kp_coins"])
+    ec = drbg.stream(seed, b"enc", n * s["enc_coins"])
+    pk, sk = ctx.keypair(alg, n, kc, flags=kem.PLAIN)
+    opk, osk = oracle.batch_keypair(a, n, kc)
+    assert (pk, sk) == (opk, osk)
+    ct, ss = ctx.enc(alg, n, pk, ec, flags=kem.PLAIN)
+    oct_, oss = oracle.batch_enc(a, n, pk, ec)
+    assert (ct, ss) == (oct_, oss)
+    bad = bytearray(ct)
+    bad[7] ^= 4
+    assert ctx.dec(alg, n, bytes(bad), sk, flags=kem.PLAIN) == oracle.batch_dec(a, n, bytes(bad), sk)
