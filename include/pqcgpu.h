@@ -91,6 +91,23 @@ int pqcgpu_kem_enc_batch(pqcgpu_ctx *ctx, pqcgpu_alg alg, size_t n, uint8_t *ct,
 int pqcgpu_kem_dec_batch(pqcgpu_ctx *ctx, pqcgpu_alg alg, size_t n, uint8_t *ss, const uint8_t *ct,
                          const uint8_t *sk, unsigned flags);
 
+/* ---- encapsulation without allocation --------------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc (code running inside
+ * another framework's allocator or memory pool, plugins handed fixed device buffers, real-time
+ * paths that forbid allocation after start-up): a Kyber encapsulation (alg = one of the Kyber
+ * algorithms) that allocates nothing and needs no context.  All pointers are caller-owned device
+ * buffers on the current device (16-byte aligned, coins required); work is enqueued on `stream`
+ * (a cudaStream_t, NULL = legacy default stream) and the call returns without waiting.
+ * Its scratch is one fixed 6 MiB device array (96 bytes for each of up to 65536 instances), held
+ * by every GPU that loads the library until the process exits; n > 65536 returns PQCGPU_EINVAL.
+ * Every call shares that array: calls whose work overlaps on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller.  Each call writes every scratch byte it
+ * reads before reading it, so nothing left by an earlier call needs clearing.  The first call on
+ * a device does the set-up (constant tables, lookup of the array's device address); make that
+ * first call before any stream capture.  Leave the launch profiler off for this call. */
+int pqcgpu_kem_enc_batch_noalloc(pqcgpu_alg alg, size_t n, uint8_t *ct, uint8_t *ss, const uint8_t *pk,
+                                 const uint8_t *coins, void *stream);
+
 /* ---- batched CPA-PKE (replaces indcpa_* of Kyber_GPU_Batched/indcpa.h:16-26) -------------
  * variant 2 = the reference's round-2 arithmetic, variant 3 = round-3 parameter sets; k = 2..4.
  * keypair: d = 32 bytes per instance; pk = KYBER_INDCPA_PUBLICKEYBYTES, sk = K*384.

@@ -225,6 +225,13 @@ static int ensure_device_init(int device) {
     return PQCGPU_OK;
 }
 
+namespace pqc {
+// Per-device set-up shared with entry points that work without a context: uploads the constant
+// tables once per device (the current device must be `device`).
+int device_ready(int device) { return ensure_device_init(device); }
+int set_error(int code, const char *what) { return set_err(code, what); }
+}  // namespace pqc
+
 extern "C" int pqcgpu_ctx_create(pqcgpu_ctx **out, int device, size_t budget) {
     if (!out) return set_err(PQCGPU_EINVAL, "out is NULL");
     *out = nullptr;

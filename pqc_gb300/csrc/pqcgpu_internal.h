@@ -30,6 +30,10 @@ int probe_peaks(int device, double *int_ops, double *keccak_perms);
         ::pqc::g_launch_count++;                                             \
     } while (0)
 
+// Once-per-device set-up (constant tables) and the thread-local error text (capi.cu).
+int device_ready(int device);
+int set_error(int code, const char *what);
+
 // ---- Kyber (kyber.cu) ----
 int kyber_init_constants();
 // op: 0 keypair, 1 enc, 2 dec.  ni = instances per CTA of the core kernel, threads per CTA.
