@@ -132,38 +132,76 @@ __device__ __forceinline__ void noise_poly(const uint2 *seed, int nonce, F emit)
 // K products (that sum cannot wrap: |sum| < 8q < 2^15), before the Barrett of pointwise_acc.
 constexpr uint32_t ACC_BIAS = 2 * Q;
 
-template <int V>
-struct EntrySampler {
-    int ctr;
-    int16_t even;
-    const int16_t *b;  // shared polynomial b (NTT domain)
-    uint32_t *acc;     // shared accumulator polynomial viewed as packed pairs
-    const int16_t *sz;
+// Per-thread staging of accepted candidates in shared memory: each Keccak block is parsed in two
+// halves; a half yields at most 56 accepted coefficients, plus one carried over from the previous
+// half (an unpaired even coefficient), so 58 int16 per thread suffice.
+constexpr int STAGE_INT16 = 58;
 
-    __device__ __forceinline__ void take(uint32_t d) {
-        const uint32_t bound = (V == 2) ? (uint32_t)(19 * Q) : (uint32_t)Q;
-        if (d < bound && ctr < N) {
-            const int16_t a = (V == 2) ? (int16_t)(d - (d >> 12) * Q) : (int16_t)d;
-            if (ctr & 1) {
-                const int p = ctr >> 1;
-                const int o = phys(2 * p);
-                const uint32_t bb = *reinterpret_cast<const uint32_t *>(b + o);
-                int16_t r0, r1;
-                basemul(r0, r1, even, a, (int16_t)(bb & 0xffff), (int16_t)(bb >> 16), pair_zeta(sz, p));
-                atomicAdd(acc + (o >> 1), (uint32_t)((int)r0 + (int)ACC_BIAS) | ((uint32_t)((int)r1 + (int)ACC_BIAS) << 16));
+// Append the accepted candidates of one half-block to stg[n...] without branches (the store is
+// unconditional, the count advances only on acceptance), in the order of the byte stream.
+template <int V, int HALF>
+__device__ __forceinline__ void compact_half(const uint2 (&A)[25], int16_t *stg, int &n) {
+    if (V == 3) {
+        // 56 triplets per block, two 12-bit candidates each (round-3 Parse); this half: 28 triplets
+#pragma unroll
+        for (int tt = 0; tt < 28; tt++) {
+            const int t = 28 * HALF + tt, o = 3 * t, wi = o >> 2, sh = 8 * (o & 3);
+            const uint32_t w0 = (wi & 1) ? A[wi >> 1].y : A[wi >> 1].x;
+            uint32_t v;
+            if (sh <= 8) {
+                v = w0 >> sh;
             } else {
-                even = a;
+                const uint32_t w1 = ((wi + 1) & 1) ? A[(wi + 1) >> 1].y : A[(wi + 1) >> 1].x;
+                v = __funnelshift_r(w0, w1, sh);
             }
-            ctr++;
+            const uint32_t d0 = v & 0xfff, d1 = (v >> 12) & 0xfff;
+            stg[n] = (int16_t)d0;
+            n += (d0 < (uint32_t)Q);
+            stg[n] = (int16_t)d1;
+            n += (d1 < (uint32_t)Q);
+        }
+    } else {
+        // 84 little-endian 16-bit candidates per block, v < 19q kept as v - (v >> 12) q
+        // (rej_uniform, indcpa.cu:290-322); this half: 42 candidates
+#pragma unroll
+        for (int tt = 0; tt < 21; tt++) {
+            const int t = 21 * HALF + tt;
+            const uint32_t w0 = (t & 1) ? A[t >> 1].y : A[t >> 1].x;
+            const uint32_t d0 = w0 & 0xffff, d1 = w0 >> 16;
+            stg[n] = (int16_t)(d0 - (d0 >> 12) * Q);
+            n += (d0 < (uint32_t)(19 * Q));
+            stg[n] = (int16_t)(d1 - (d1 >> 12) * Q);
+            n += (d1 < (uint32_t)(19 * Q));
         }
     }
-};
+}
 
-// Accumulate A[row][col] o b into acc, where A[i][j] = XOF(rho || j || i) (gen_matrix,
-// indcpa.cu:339-403) and the transposed matrix uses XOF(rho || i || j).
+// Multiply the complete pairs staged in stg[0..n) into the accumulator (pair index from ctr),
+// stopping at 256 coefficients; an unpaired last coefficient moves to stg[0].
+__device__ __forceinline__ void consume_pairs(int16_t *stg, int &n, int &ctr, const int16_t *b, uint32_t *acc,
+                                              const int16_t *sz) {
+    int i = 0;
+    for (; i + 1 < n && ctr < N; i += 2, ctr += 2) {
+        const uint32_t av = *reinterpret_cast<const uint32_t *>(stg + i);
+        const int p = ctr >> 1, o = phys(2 * p);
+        const uint32_t bb = *reinterpret_cast<const uint32_t *>(b + o);
+        int16_t r0, r1;
+        basemul(r0, r1, (int16_t)(av & 0xffff), (int16_t)(av >> 16), (int16_t)(bb & 0xffff), (int16_t)(bb >> 16),
+                pair_zeta(sz, p));
+        atomicAdd(acc + (o >> 1), (uint32_t)((int)r0 + (int)ACC_BIAS) | ((uint32_t)((int)r1 + (int)ACC_BIAS) << 16));
+    }
+    const bool carry = (i < n) && (ctr < N);
+    if (carry) stg[0] = stg[i];
+    n = carry ? 1 : 0;
+}
+
+// Accumulate A[row][col] o b into acc (packed, biased pairs), where A[i][j] = XOF(rho || j || i)
+// (gen_matrix, indcpa.cu:339-403) and the transposed matrix uses XOF(rho || i || j).  One thread
+// per entry; the candidate stream is consumed strictly in order, so the entry equals the
+// reference's rejection sampling coefficient for coefficient.
 template <int V>
 __device__ __forceinline__ void matrix_entry(const uint2 *rho, int row, int col, bool transposed, const int16_t *b,
-                                             int16_t *acc, const int16_t *sz) {
+                                             int16_t *acc16, const int16_t *sz, int16_t *stg) {
     uint2 A[25];
     keccak_zero(A);
 #pragma unroll
@@ -171,39 +209,15 @@ __device__ __forceinline__ void matrix_entry(const uint2 *rho, int row, int col,
     const uint32_t x = transposed ? row : col, y = transposed ? col : row;
     A[4].x = x | (y << 8) | (DOM_SHAKE << 16);
     A[SHAKE128_LANES - 1].y ^= 0x80000000u;
-    EntrySampler<V> s;
-    s.ctr = 0;
-    s.even = 0;
-    s.b = b;
-    s.acc = reinterpret_cast<uint32_t *>(acc);
-    s.sz = sz;
-    while (s.ctr < N) {
+    uint32_t *acc = reinterpret_cast<uint32_t *>(acc16);
+    int ctr = 0, n = 0;
+    while (ctr < N) {
         keccak_f1600(A);
-        if (V == 3) {
-            // 56 triplets, two 12-bit candidates each (round-3 Parse)
-#pragma unroll
-            for (int t = 0; t < 56; t++) {
-                const int o = 3 * t, wi = o >> 2, sh = 8 * (o & 3);
-                const uint32_t w0 = (wi & 1) ? A[wi >> 1].y : A[wi >> 1].x;
-                uint32_t v;
-                if (sh <= 8) {
-                    v = w0 >> sh;
-                } else {
-                    const uint32_t w1 = ((wi + 1) & 1) ? A[(wi + 1) >> 1].y : A[(wi + 1) >> 1].x;
-                    v = __funnelshift_r(w0, w1, sh);
-                }
-                s.take(v & 0xfff);
-                s.take((v >> 12) & 0xfff);
-            }
-        } else {
-            // 84 little-endian 16-bit candidates (rej_uniform, indcpa.cu:290-322)
-#pragma unroll
-            for (int t = 0; t < 42; t++) {
-                const uint32_t w0 = (t & 1) ? A[t >> 1].y : A[t >> 1].x;
-                s.take(w0 & 0xffff);
-                s.take(w0 >> 16);
-            }
-        }
+        compact_half<V, 0>(A, stg, n);
+        consume_pairs(stg, n, ctr, b, acc, sz);
+        if (ctr >= N) break;
+        compact_half<V, 1>(A, stg, n);
+        consume_pairs(stg, n, ctr, b, acc, sz);
     }
 }
 
@@ -306,10 +320,15 @@ struct DecArgs {
 // 128 bytes of per-instance seeds / flags.
 template <int NPOLY>
 struct Layout {
-    static __host__ __device__ constexpr size_t bytes(int ni) {
-        return 2 * 128 * sizeof(int16_t) + (size_t)ni * NPOLY * POLY_PITCH * sizeof(int16_t) + (size_t)ni * 128;
+    static __host__ __device__ constexpr size_t bytes(int ni, int threads) {
+        return 2 * 128 * sizeof(int16_t) + (size_t)ni * NPOLY * POLY_PITCH * sizeof(int16_t) + (size_t)ni * 128 +
+               (size_t)threads * STAGE_INT16 * sizeof(int16_t);
     }
 };
+// Per-thread staging area (after the seeds block).
+__device__ __forceinline__ int16_t *stage_of(uint8_t *seeds, int ni) {
+    return reinterpret_cast<int16_t *>(seeds + (size_t)ni * 128) + (size_t)threadIdx.x * STAGE_INT16;
+}
 
 __device__ __forceinline__ void load_twiddles(int16_t *sz, int16_t *szi) {
     for (int i = threadIdx.x; i < 128; i += blockDim.x) {
@@ -348,7 +367,7 @@ __device__ __forceinline__ int16_t *slot(int16_t *polys, int li, int s) {
 // Per-instance shared seed block (128 B): [0,32) m, [32,64) r / K-bar, [64,96) rho / z, [96] flag
 template <int K, int V, bool DEC>
 __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz, const int16_t *szi, int ni,
-                               int base, const EncArgs &a, const uint8_t *ct_cmp) {
+                               int ni_alloc, int base, const EncArgs &a, const uint8_t *ct_cmp) {
     using Pp = P<K, V>;
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
 
@@ -370,7 +389,7 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
         const int li = job / (K * K), i = (job / K) % K, j = job % K;
         const uint8_t *pk = a.pk + (size_t)(base + li) * a.pk_stride;
         matrix_entry<V>(reinterpret_cast<const uint2 *>(pk + Pp::POLYVECBYTES), i, j, true, slot<K, V>(polys, li, j),
-                        slot<K, V>(polys, li, K + i), sz);
+                        slot<K, V>(polys, li, K + i), sz, stage_of(seeds, ni_alloc));
     }
     // (4) v = t-hat o r-hat (warp per instance, t-hat decoded from pk bytes; independent of (3))
     for (int li = warp; li < ni; li += nwarp) {
@@ -481,7 +500,7 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_enc_core(EncArgs a, in
     const int ni = min(NI, a.n - base);
     load_twiddles(sz, szi);
     __syncthreads();
-    encrypt_phases<K, V, false>(polys, seeds, sz, szi, ni, base, a, nullptr);
+    encrypt_phases<K, V, false>(polys, seeds, sz, szi, ni, NI, base, a, nullptr);
 }
 
 template <int K, int V>
@@ -587,7 +606,7 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, in
     e.m_stride = 0;
     e.r = nullptr;
     e.r_stride = 0;
-    encrypt_phases<K, V, true>(polys, seeds, sz, szi, ni, base, e, d.ct);
+    encrypt_phases<K, V, true>(polys, seeds, sz, szi, ni, NI, base, e, d.ct);
     __syncthreads();
     // (g) ss = SHAKE256(fail ? z : K-bar' || H(c)), with a constant-time select
     for (int li = tid; li < ni; li += nthr) {
@@ -655,7 +674,7 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int 
     for (int job = tid; job < ni * K * K; job += nthr) {
         const int li = job / (K * K), i = (job / K) % K, j = job % K;
         matrix_entry<V>(reinterpret_cast<const uint2 *>(seeds + li * 128), i, j, false, kslot(li, j), kslot(li, 2 * K + i),
-                        sz);
+                        sz, stage_of(seeds, NI));
     }
     __syncthreads();
     // (d) t = reduce(frommont(t) + e); pack pk = t || rho and sk_cpa = s (warp per instance)
@@ -798,7 +817,7 @@ static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins,
                           uint8_t *scratch, int plain, cudaStream_t st) {
     if (plain) return kem ? plain_keypair<K, V>(n, pk, sk, coins, coins_stride, scratch, st) : PQCGPU_EUNSUPPORTED;
     const int NI = g_ni[0][K - 2], NT = g_threads[0][K - 2];
-    const size_t sm = Layout<3 * K>::bytes(NI);
+    const size_t sm = Layout<3 * K>::bytes(NI, NT);
     if (ensure_smem(kyber_kp_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     KpArgs a{n, pk, sk, coins, coins_stride, kem};
     PQC_LAUNCH(st, "kyber_kp_core", K, V, kyber_kp_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
@@ -811,7 +830,7 @@ static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const 
                       uint8_t *scratch, int kem, int plain, cudaStream_t st) {
     if (plain) return kem ? plain_enc<K, V>(n, ct, ss, pk, coins, scratch, st) : PQCGPU_EUNSUPPORTED;
     const int NI = g_ni[1][K - 2], NT = g_threads[1][K - 2];
-    const size_t sm = Layout<2 * K + 1>::bytes(NI);
+    const size_t sm = Layout<2 * K + 1>::bytes(NI, NT);
     if (ensure_smem(kyber_enc_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     EncArgs a;
     a.n = n;
@@ -843,7 +862,7 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
                       int plain, cudaStream_t st) {
     if (plain) return kem ? plain_dec<K, V>(n, out, ct, sk, scratch, st) : PQCGPU_EUNSUPPORTED;
     const int NI = g_ni[2][K - 2], NT = g_threads[2][K - 2];
-    const size_t sm = Layout<2 * K + 1>::bytes(NI);
+    const size_t sm = Layout<2 * K + 1>::bytes(NI, NT);
     if (ensure_smem(kyber_dec_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     DecArgs d;
     d.n = n;
