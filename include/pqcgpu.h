@@ -119,6 +119,16 @@ int pqcgpu_kyber_indcpa_enc_batch(pqcgpu_ctx *ctx, int variant, int k, size_t n,
 int pqcgpu_kyber_indcpa_dec_batch(pqcgpu_ctx *ctx, int variant, int k, size_t n, uint8_t *m, const uint8_t *ct,
                                   const uint8_t *sk, unsigned flags);
 
+/* ---- batched NewHope-1024 CPA-PKE (replaces cpapke_* of NewHope_NIST_GPU/cpapke.h:14-24) ----
+ * keypair: seed 32 bytes per instance -> pk 1824, sk 1792; enc: msg and coin 32 bytes per instance
+ * -> ct 2176; dec: msg out 32 bytes per instance. */
+int pqcgpu_newhope_cpapke_keypair_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *pk, uint8_t *sk, const uint8_t *seed,
+                                        unsigned flags);
+int pqcgpu_newhope_cpapke_enc_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *ct, const uint8_t *msg, const uint8_t *pk,
+                                    const uint8_t *coin, unsigned flags);
+int pqcgpu_newhope_cpapke_dec_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *msg, const uint8_t *ct, const uint8_t *sk,
+                                    unsigned flags);
+
 /* ---- launch-shape tuning (used by the autotuner) -----------------------------------------
  * Kyber core kernels: op 0 keypair, 1 encaps, 2 decaps; k = 2..4; ni = instances per CTA (1..128),
  * threads per CTA (multiple of 32, 32..512).  Applies to all contexts of the process. */
@@ -149,6 +159,9 @@ int pqcgpu_kyber768_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, c
 int pqcgpu_kyber1024_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
 int pqcgpu_kyber1024_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
 int pqcgpu_kyber1024_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+int pqcgpu_newhope1024_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+int pqcgpu_newhope1024_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+int pqcgpu_newhope1024_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
 
 #ifdef __cplusplus
 }

@@ -28,6 +28,9 @@ SIGNATURES = {
     "pqcgpu_kyber_indcpa_keypair_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_kyber_indcpa_enc_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_kyber_indcpa_dec_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_newhope_cpapke_keypair_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_newhope_cpapke_enc_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_newhope_cpapke_dec_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_kyber_set_shape": (_int, [_int, _int, _int, _int]),
     "pqcgpu_kyber_get_shape": (_int, [_int, _int, _c.POINTER(_int), _c.POINTER(_int)]),
     "pqcgpu_profile_enable": (_int, [_int]),
@@ -36,7 +39,7 @@ SIGNATURES = {
     "pqcgpu_randombytes_init": (_int, [_u8p]),
     "pqcgpu_randombytes": (_int, [_u8p, _sz]),
 }
-for _alg in ("kyber512", "kyber768", "kyber1024"):
+for _alg in ("kyber512", "kyber768", "kyber1024", "newhope1024"):
     SIGNATURES["pqcgpu_%s_crypto_kem_keypair" % _alg] = (_int, [_u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_enc" % _alg] = (_int, [_u8p, _u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_dec" % _alg] = (_int, [_u8p, _u8p, _u8p])

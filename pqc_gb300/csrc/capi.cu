@@ -221,6 +221,8 @@ static int ensure_device_init(int device) {
     if (g_constants_ready[device]) return PQCGPU_OK;
     int rc = kyber_init_constants();
     if (rc) return set_err(rc, "uploading Kyber constants failed");
+    rc = newhope_init_constants();
+    if (rc) return set_err(rc, "uploading NewHope constants failed");
     g_constants_ready[device] = true;
     return PQCGPU_OK;
 }
@@ -447,6 +449,21 @@ extern "C" int pqcgpu_kem_keypair_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n,
             return kyber_keypair_dev(variant, k, m, out[0], out[1], in[0], (int)ai.kpc, 1, scr, plain, s);
         });
     }
+    if (flags & PQCGPU_PLAIN) return set_err(PQCGPU_EUNSUPPORTED, "the plain path covers Kyber only");
+    if (alg == PQCGPU_NEWHOPE1024) {
+        OpDesc d;
+        d.nin = 1;
+        d.in[0] = coins;
+        d.in_sz[0] = ai.kpc;
+        d.nout = 2;
+        d.out[0] = pk;
+        d.out_sz[0] = ai.pk;
+        d.out[1] = sk;
+        d.out_sz[1] = ai.sk;
+        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
+            return newhope_keypair_dev(m, out[0], out[1], in[0], 32, s);
+        });
+    }
     return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
 }
 
@@ -476,6 +493,24 @@ extern "C" int pqcgpu_kem_enc_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uin
             return kyber_enc_dev(variant, k, m, out[0], out[1], in[0], nullptr, in[1], scr, 1, plain, s);
         });
     }
+    if (flags & PQCGPU_PLAIN) return set_err(PQCGPU_EUNSUPPORTED, "the plain path covers Kyber only");
+    if (alg == PQCGPU_NEWHOPE1024) {
+        OpDesc d;
+        d.nin = 2;
+        d.in[0] = pk;
+        d.in_sz[0] = ai.pk;
+        d.in[1] = coins;
+        d.in_sz[1] = ai.encc;
+        d.nout = 2;
+        d.out[0] = ct;
+        d.out_sz[0] = ai.ct;
+        d.out[1] = ss;
+        d.out_sz[1] = ai.ss;
+        d.scratch_per = 64;
+        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
+            return newhope_enc_dev(m, out[0], out[1], in[0], nullptr, in[1], scr, 1, s);
+        });
+    }
     return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
 }
 
@@ -498,6 +533,21 @@ extern "C" int pqcgpu_kem_dec_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uin
         d.scratch_per = kyber_scratch_bytes(k, 2, plain);
         return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
             return kyber_dec_dev(variant, k, m, out[0], in[0], in[1], scr, 1, plain, s);
+        });
+    }
+    if (flags & PQCGPU_PLAIN) return set_err(PQCGPU_EUNSUPPORTED, "the plain path covers Kyber only");
+    if (alg == PQCGPU_NEWHOPE1024) {
+        OpDesc d;
+        d.nin = 2;
+        d.in[0] = ct;
+        d.in_sz[0] = ai.ct;
+        d.in[1] = sk;
+        d.in_sz[1] = ai.sk;
+        d.nout = 1;
+        d.out[0] = ss;
+        d.out_sz[0] = ai.ss;
+        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
+            return newhope_dec_dev(m, out[0], in[0], in[1], 1, s);
         });
     }
     return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
@@ -586,6 +636,58 @@ extern "C" int pqcgpu_probe_peaks(int device, double *int_ops_per_s, double *kec
     return rc ? set_err(rc, "probe failed") : PQCGPU_OK;
 }
 
+// ---- NewHope CPA level (replaces cpapke_* of NewHope_NIST_GPU/cpapke.h:14-24) ----
+extern "C" int pqcgpu_newhope_cpapke_keypair_batch(pqcgpu_ctx *c, size_t n, uint8_t *pk, uint8_t *sk,
+                                                   const uint8_t *seed, unsigned flags) {
+    if (!c) return set_err(PQCGPU_EINVAL, "bad context");
+    OpDesc d;
+    d.nin = 1;
+    d.in[0] = seed;
+    d.in_sz[0] = 32;
+    d.nout = 2;
+    d.out[0] = pk;
+    d.out_sz[0] = 1824;
+    d.out[1] = sk;
+    d.out_sz[1] = 1792;
+    return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
+        return newhope_keypair_dev(m, out[0], out[1], in[0], 32, s);
+    });
+}
+extern "C" int pqcgpu_newhope_cpapke_enc_batch(pqcgpu_ctx *c, size_t n, uint8_t *ct, const uint8_t *msg,
+                                               const uint8_t *pk, const uint8_t *coin, unsigned flags) {
+    if (!c) return set_err(PQCGPU_EINVAL, "bad context");
+    OpDesc d;
+    d.nin = 3;
+    d.in[0] = pk;
+    d.in_sz[0] = 1824;
+    d.in[1] = msg;
+    d.in_sz[1] = 32;
+    d.in[2] = coin;
+    d.in_sz[2] = 32;
+    d.nout = 1;
+    d.out[0] = ct;
+    d.out_sz[0] = 2176;
+    return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
+        return newhope_enc_dev(m, out[0], nullptr, in[0], in[1], in[2], nullptr, 0, s);
+    });
+}
+extern "C" int pqcgpu_newhope_cpapke_dec_batch(pqcgpu_ctx *c, size_t n, uint8_t *msg, const uint8_t *ct,
+                                               const uint8_t *sk, unsigned flags) {
+    if (!c) return set_err(PQCGPU_EINVAL, "bad context");
+    OpDesc d;
+    d.nin = 2;
+    d.in[0] = ct;
+    d.in_sz[0] = 2176;
+    d.in[1] = sk;
+    d.in_sz[1] = 1792;
+    d.nout = 1;
+    d.out[0] = msg;
+    d.out_sz[0] = 32;
+    return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
+        return newhope_dec_dev(m, out[0], in[0], in[1], 0, s);
+    });
+}
+
 // ---- NIST single-instance API (default context on device 0) ----
 static pqcgpu_ctx *g_default_ctx = nullptr;
 static std::mutex g_default_mu;
@@ -610,3 +712,4 @@ static pqcgpu_ctx *default_ctx() {
 PQC_NIST(kyber512, PQCGPU_KYBER512)
 PQC_NIST(kyber768, PQCGPU_KYBER768)
 PQC_NIST(kyber1024, PQCGPU_KYBER1024)
+PQC_NIST(newhope1024, PQCGPU_NEWHOPE1024)

@@ -51,4 +51,14 @@ int kyber_enc_dev(int variant, int k, int n, uint8_t *ct, uint8_t *ss, const uin
 int kyber_dec_dev(int variant, int k, int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch,
                   int kem, int plain, cudaStream_t st);
 
+// ---- NewHope-1024 (newhope.cu) ----
+int newhope_init_constants();
+int newhope_set_shape(int op, int ni, int threads);
+int newhope_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st);
+// kem=1: coins 32 B/instance, scratch >= 64 B/instance, ss written; kem=0: CPA with m and coins
+int newhope_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
+                    uint8_t *scratch, int kem, cudaStream_t st);
+// kem=1: out = ss (32 B); kem=0: out = message
+int newhope_dec_dev(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st);
+
 }  // namespace pqc

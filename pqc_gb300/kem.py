@@ -104,6 +104,22 @@ class Context:
         _lib.check(self.lib.pqcgpu_kyber_indcpa_dec_batch(self.h, variant, k, n, m, ct, sk, flags))
         return m.raw
 
+    def newhope_cpa_keypair(self, n, seed, flags=0):
+        pk = ctypes.create_string_buffer(n * 1824)
+        sk = ctypes.create_string_buffer(n * 1792)
+        _lib.check(self.lib.pqcgpu_newhope_cpapke_keypair_batch(self.h, n, pk, sk, seed, flags))
+        return pk.raw, sk.raw
+
+    def newhope_cpa_enc(self, n, m, pk, coin, flags=0):
+        ct = ctypes.create_string_buffer(n * 2176)
+        _lib.check(self.lib.pqcgpu_newhope_cpapke_enc_batch(self.h, n, ct, m, pk, coin, flags))
+        return ct.raw
+
+    def newhope_cpa_dec(self, n, ct, sk, flags=0):
+        m = ctypes.create_string_buffer(n * 32)
+        _lib.check(self.lib.pqcgpu_newhope_cpapke_dec_batch(self.h, n, m, ct, sk, flags))
+        return m.raw
+
     # ---- device tensors (torch.uint8 on this context's device), asynchronous ----
     def keypair_dev(self, alg, n, pk, sk, coins, flags=0):
         _lib.check(self.lib.pqcgpu_kem_keypair_batch(self.h, alg_id(alg), n, _ptr(pk), _ptr(sk), _ptr(coins),
