@@ -162,6 +162,9 @@ int pqcgpu_kyber1024_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, 
 int pqcgpu_newhope1024_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
 int pqcgpu_newhope1024_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
 int pqcgpu_newhope1024_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+int pqcgpu_frodo976_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+int pqcgpu_frodo976_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+int pqcgpu_frodo976_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
 
 #ifdef __cplusplus
 }

@@ -39,7 +39,7 @@ SIGNATURES = {
     "pqcgpu_randombytes_init": (_int, [_u8p]),
     "pqcgpu_randombytes": (_int, [_u8p, _sz]),
 }
-for _alg in ("kyber512", "kyber768", "kyber1024", "newhope1024"):
+for _alg in ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976"):
     SIGNATURES["pqcgpu_%s_crypto_kem_keypair" % _alg] = (_int, [_u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_enc" % _alg] = (_int, [_u8p, _u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_dec" % _alg] = (_int, [_u8p, _u8p, _u8p])

@@ -223,6 +223,8 @@ static int ensure_device_init(int device) {
     if (rc) return set_err(rc, "uploading Kyber constants failed");
     rc = newhope_init_constants();
     if (rc) return set_err(rc, "uploading NewHope constants failed");
+    rc = frodo_init_constants();
+    if (rc) return set_err(rc, "uploading FrodoKEM constants failed");
     g_constants_ready[device] = true;
     return PQCGPU_OK;
 }
@@ -464,6 +466,21 @@ extern "C" int pqcgpu_kem_keypair_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n,
             return newhope_keypair_dev(m, out[0], out[1], in[0], 32, s);
         });
     }
+    if (alg == PQCGPU_FRODO976) {
+        OpDesc d;
+        d.nin = 1;
+        d.in[0] = coins;
+        d.in_sz[0] = ai.kpc;
+        d.nout = 2;
+        d.out[0] = pk;
+        d.out_sz[0] = ai.pk;
+        d.out[1] = sk;
+        d.out_sz[1] = ai.sk;
+        d.scratch_per = frodo_scratch_bytes();
+        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
+            return frodo_keypair_dev(m, out[0], out[1], in[0], (int)ai.kpc, scr, s);
+        });
+    }
     return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
 }
 
@@ -511,6 +528,23 @@ extern "C" int pqcgpu_kem_enc_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uin
             return newhope_enc_dev(m, out[0], out[1], in[0], nullptr, in[1], scr, 1, s);
         });
     }
+    if (alg == PQCGPU_FRODO976) {
+        OpDesc d;
+        d.nin = 2;
+        d.in[0] = pk;
+        d.in_sz[0] = ai.pk;
+        d.in[1] = coins;
+        d.in_sz[1] = ai.encc;
+        d.nout = 2;
+        d.out[0] = ct;
+        d.out_sz[0] = ai.ct;
+        d.out[1] = ss;
+        d.out_sz[1] = ai.ss;
+        d.scratch_per = frodo_scratch_bytes();
+        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
+            return frodo_enc_dev(m, out[0], out[1], in[0], in[1], scr, s);
+        });
+    }
     return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
 }
 
@@ -548,6 +582,21 @@ extern "C" int pqcgpu_kem_dec_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uin
         d.out_sz[0] = ai.ss;
         return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
             return newhope_dec_dev(m, out[0], in[0], in[1], 1, s);
+        });
+    }
+    if (alg == PQCGPU_FRODO976) {
+        OpDesc d;
+        d.nin = 2;
+        d.in[0] = ct;
+        d.in_sz[0] = ai.ct;
+        d.in[1] = sk;
+        d.in_sz[1] = ai.sk;
+        d.nout = 1;
+        d.out[0] = ss;
+        d.out_sz[0] = ai.ss;
+        d.scratch_per = frodo_scratch_bytes();
+        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
+            return frodo_dec_dev(m, out[0], in[0], in[1], scr, s);
         });
     }
     return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
@@ -713,3 +762,4 @@ PQC_NIST(kyber512, PQCGPU_KYBER512)
 PQC_NIST(kyber768, PQCGPU_KYBER768)
 PQC_NIST(kyber1024, PQCGPU_KYBER1024)
 PQC_NIST(newhope1024, PQCGPU_NEWHOPE1024)
+PQC_NIST(frodo976, PQCGPU_FRODO976)

@@ -1,0 +1,499 @@
+// Batched FrodoKEM-976 (SHAKE) for sm_103a.
+//
+// Replaces crypto_kem_keypair_gpu / enc / dec (FrodoKEM_GPU/frodo976.cu:87-690: one instance per
+// call, A written to and re-read from HBM, host SHAKE for pk / ct) with, per operation:
+//   * a thread-per-instance kernel for the serial sponges -- the S/E noise stream
+//     (SHAKE256(0x5F / 0x96 || seedSE), 230-231 permutations), G1 = SHAKE256(pk) (115), G2 and
+//     the final F = SHAKE256(ct || k) (116) -- the noise sampled with the CDF table on the fly;
+//   * a core kernel that regenerates A row by row from SHAKE128(le16(i) || seedA) and multiplies
+//     it as it appears, so A (1.9 MB per key) never exists in HBM or whole in shared memory:
+//       - keypair, B = A S + E: one thread per row, which owns the 8 outputs of that row;
+//       - encaps / decaps, B' = S' A + E': each thread squeezes one 168-byte block of its row per
+//         round into shared memory, then the CTA contracts the staged 84 columns over its rows
+//         (exact mod 2^16 with uint32 multiply-accumulate) and adds the partial sums into the
+//         8 x 976 accumulator with shared-memory atomics;
+//   * codecs (16-bit big-endian pack, 3-bit key encode / decode) inside the same kernels.
+// Host flow and arithmetic follow FrodoKEM_GPU/kem.c:13-214, frodo_macrify_reference.cu:55-360,
+// util.cu:18-113, noise.c:10-29 and the CDF table of frodo976.cu:21.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "keccak.cuh"
+#include "pqcgpu_internal.h"
+
+namespace pqc {
+namespace frodo {
+
+constexpr int N = 976, NB = 8;
+constexpr int PKB = 15632, SKB = 31296, CTB = 15744, SSB = 24, SEEDA = 16, MUB = 24;
+constexpr int C1B = 2 * N * NB;  // 15616: packed N x NBAR (or NBAR x N) matrix
+constexpr int ROW_BLOCKS = 12;   // 1952 bytes of SHAKE128 per row = 11 full blocks + 104 bytes
+// scratch per instance: noise (Sp 7808 + Ep 7808 + Epp 64 u16) + seeds (seedSE/k 48, mu 24, flag)
+constexpr int NOISE_U16 = 2 * N * NB + NB * NB;
+constexpr size_t SCRATCH = (size_t)NOISE_U16 * 2 + 128;
+
+static __constant__ uint16_t c_cdf[11];
+
+// ---- sponge helpers -------------------------------------------------------------------------
+// Absorb the concatenation of two lane-aligned byte strings (n1 and n2 lanes of 8 bytes), pad.
+template <int R>
+__device__ __forceinline__ void absorb2(uint2 (&A)[25], const uint2 *p1, int n1, const uint2 *p2, int n2, uint32_t dom) {
+    keccak_zero(A);
+    int total = n1 + n2, done = 0;
+    while (total - done >= R) {
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+            const int idx = done + i;
+            A[i] = xor2(A[i], idx < n1 ? p1[idx] : p2[idx - n1]);
+        }
+        keccak_f1600(A);
+        done += R;
+    }
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+        const int idx = done + i;
+        if (idx < total) A[i] = xor2(A[i], idx < n1 ? p1[idx] : p2[idx - n1]);
+    }
+    keccak_pad<R>(A, total - done, dom);
+}
+// Absorb `len` (< rate) bytes given in registers as little-endian lanes with a leading domain byte.
+__device__ __forceinline__ void absorb_prefixed24(uint2 (&A)[25], uint8_t prefix, const uint8_t *seed24) {
+    // message = prefix || seed (25 bytes), SHAKE256
+    uint8_t b[32];
+    b[0] = prefix;
+#pragma unroll
+    for (int i = 0; i < 24; i++) b[1 + i] = seed24[i];
+#pragma unroll
+    for (int i = 25; i < 32; i++) b[i] = 0;
+    b[25] = (uint8_t)DOM_SHAKE;
+    keccak_zero(A);
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+        uint32_t lo = 0, hi = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            lo |= (uint32_t)b[8 * l + q] << (8 * q);
+            hi |= (uint32_t)b[8 * l + 4 + q] << (8 * q);
+        }
+        A[l] = make_uint2(lo, hi);
+    }
+    A[SHAKE256_LANES - 1].y ^= 0x80000000u;
+}
+
+// CDF sampler of one 16-bit value (noise.c:10-29)
+__device__ __forceinline__ uint16_t cdf_sample(uint32_t r) {
+    uint32_t sample = 0;
+    const uint32_t prnd = (r & 0xffff) >> 1, sign = r & 1;
+#pragma unroll
+    for (int j = 0; j < 10; j++) sample += ((uint32_t)c_cdf[j] - prnd) >> 31 & 1;
+    return (uint16_t)((((0u - sign) ^ sample) + sign) & 0xffff);
+}
+
+// Squeeze the SHAKE256 noise stream (state after absorb), sample every u16 and hand value v at
+// stream position p to emit(p, v).
+template <class F>
+__device__ __forceinline__ void noise_stream(uint2 (&A)[25], int count, F emit) {
+    for (int base = 0; base < count; base += 68) {  // 136 bytes = 68 values per block
+        keccak_f1600(A);
+#pragma unroll
+        for (int w = 0; w < 34; w++) {
+            const uint32_t t = (w & 1) ? A[w >> 1].y : A[w >> 1].x;
+            const int p = base + 2 * w;
+            if (p < count) emit(p, cdf_sample(t & 0xffff));
+            if (p + 1 < count) emit(p + 1, cdf_sample(t >> 16));
+        }
+    }
+}
+
+// SHAKE128 row generator for A: absorb le16(row) || seedA, squeeze block by block.
+__device__ __forceinline__ void row_absorb(uint2 (&A)[25], int row, const uint2 *seedA) {
+    keccak_zero(A);
+    // bytes: row_lo row_hi seedA[0..15] -> lanes
+    const uint2 s0 = seedA[0], s1 = seedA[1];
+    A[0] = make_uint2((uint32_t)(row & 0xffff) | (s0.x << 16), (s0.x >> 16) | (s0.y << 16));
+    A[1] = make_uint2((s0.y >> 16) | (s1.x << 16), (s1.x >> 16) | (s1.y << 16));
+    A[2] = make_uint2((s1.y >> 16) | (DOM_SHAKE << 16), 0);
+    A[SHAKE128_LANES - 1].y ^= 0x80000000u;
+}
+
+__device__ __forceinline__ uint32_t ld_be16(const uint8_t *p) { return ((uint32_t)p[0] << 8) | p[1]; }
+
+// ---------------------------------------------------------------------------------------------
+// Serial sponges (thread per instance)
+// ---------------------------------------------------------------------------------------------
+// keypair: seedA = SHAKE256(z, 16) -> pk[0..16); S (as St[j][k], N x 8) and E (N x 8) -> scratch
+__global__ void __launch_bounds__(64) fr_kp_pre(int n, const uint8_t *coins, int cstride, uint8_t *pk, uint8_t *scratch) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    const uint8_t *c = coins + (size_t)x * cstride;  // s(24) || seedSE(24) || z(16)
+    uint2 A[25];
+    keccak_absorb_lanes<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(c + 48), 2, DOM_SHAKE);
+    keccak_f1600(A);
+    reinterpret_cast<uint2 *>(pk + (size_t)x * PKB)[0] = A[0];
+    reinterpret_cast<uint2 *>(pk + (size_t)x * PKB)[1] = A[1];
+    uint16_t *St = reinterpret_cast<uint16_t *>(scratch + (size_t)x * SCRATCH), *E = St + N * NB;
+    uint8_t seed[24];
+#pragma unroll
+    for (int i = 0; i < 24; i++) seed[i] = c[24 + i];
+    absorb_prefixed24(A, 0x5F, seed);
+    // stream order: S[k*N + j] (k < 8, j < N) then E[i*8 + k]
+    noise_stream(A, 2 * N * NB, [&](int p, uint16_t v) {
+        if (p < N * NB) St[(p % N) * NB + p / N] = v;
+        else E[p - N * NB] = v;
+    });
+}
+
+// encaps prologue: pkh = G1(pk); (seedSE || k) = G2(pkh || mu); S', E', E'' sampled -> scratch.
+// scratch: Spt (N x 8: Spt[k][i] = S'[i][k]), Ep (8 x N), Epp (8 x 8), then k (24) at +NOISE*2,
+// mu (24) at +NOISE*2 + 32.
+__device__ __forceinline__ void enc_noise(uint8_t *scr, const uint8_t *seedSE) {
+    uint2 A[25];
+    absorb_prefixed24(A, 0x96, seedSE);
+    uint16_t *Spt = reinterpret_cast<uint16_t *>(scr), *Ep = Spt + N * NB, *Epp = Ep + N * NB;
+    noise_stream(A, NOISE_U16, [&](int p, uint16_t v) {
+        if (p < N * NB) Spt[(p % N) * NB + p / N] = v;  // stream S'[i*N + k] -> Spt[k*8 + i]
+        else if (p < 2 * N * NB) Ep[p - N * NB] = v;
+        else Epp[p - 2 * N * NB] = v;
+    });
+}
+
+__global__ void __launch_bounds__(64) fr_enc_pre(int n, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    uint8_t *scr = scratch + (size_t)x * SCRATCH;
+    uint2 A[25], in[6];
+    keccak_absorb_lanes<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(pk + (size_t)x * PKB), PKB / 8, DOM_SHAKE);
+    keccak_f1600(A);
+    in[0] = A[0];
+    in[1] = A[1];
+    in[2] = A[2];
+    const uint2 *m = reinterpret_cast<const uint2 *>(mu + (size_t)x * MUB);
+    in[3] = m[0];
+    in[4] = m[1];
+    in[5] = m[2];
+    keccak_absorb_lanes<SHAKE256_LANES>(A, in, 6, DOM_SHAKE);
+    keccak_f1600(A);
+    uint2 *kk = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2);
+    kk[0] = A[3];
+    kk[1] = A[4];
+    kk[2] = A[5];  // k
+    uint2 *mm = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2 + 32);
+    mm[0] = m[0];
+    mm[1] = m[1];
+    mm[2] = m[2];
+    uint8_t seed[24];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            seed[8 * i + q] = (uint8_t)(A[i].x >> (8 * q));
+            seed[8 * i + 4 + q] = (uint8_t)(A[i].y >> (8 * q));
+        }
+    }
+    enc_noise(scr, seed);
+}
+
+// decaps prologue: W = C - B' S; mu' = decode(W); (seedSE' || k') = G2(pkh || mu'); noise.
+__global__ void __launch_bounds__(64) fr_dec_pre(int n, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    const uint8_t *c = ct + (size_t)x * CTB, *s = sk + (size_t)x * SKB;
+    const uint8_t *sS = s + SSB + PKB;  // S as u16 LE, S[k*N + j]
+    uint8_t *scr = scratch + (size_t)x * SCRATCH;
+    uint8_t mu[MUB];
+    // W[i][j] = C[i][j] - sum_k B'[i][k] S[j][k]  (frodo_mul_bs: out[i*8+j] = sum_k b[i*N+k] s[j*N+k])
+    for (int g = 0; g < 8; g++) {  // word g of the key: 8 pieces of 3 bits from W[8g .. 8g+7]
+        uint32_t templong = 0;
+        for (int jj = 0; jj < 8; jj++) {
+            const int i = g, j = jj;  // W index 8g + jj = i*8 + j
+            uint32_t sum = 0;
+            for (int k = 0; k < N; k++)
+                sum += ld_be16(c + 2 * (i * N + k)) * (uint32_t)(sS[2 * (j * N + k)] | (sS[2 * (j * N + k) + 1] << 8));
+            const uint32_t w = (ld_be16(c + C1B + 2 * (i * NB + j)) - sum) & 0xffff;
+            const uint32_t t = ((w & 0xffff) + (1u << 12)) >> 13;
+            templong |= (t & 7) << (3 * jj);
+        }
+        mu[3 * g] = (uint8_t)templong;
+        mu[3 * g + 1] = (uint8_t)(templong >> 8);
+        mu[3 * g + 2] = (uint8_t)(templong >> 16);
+    }
+    uint2 A[25], in[6];
+    const uint2 *pkh = reinterpret_cast<const uint2 *>(s + SSB + PKB + C1B);
+    in[0] = pkh[0];
+    in[1] = pkh[1];
+    in[2] = pkh[2];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        uint32_t lo = 0, hi = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            lo |= (uint32_t)mu[8 * i + q] << (8 * q);
+            hi |= (uint32_t)mu[8 * i + 4 + q] << (8 * q);
+        }
+        in[3 + i] = make_uint2(lo, hi);
+    }
+    keccak_absorb_lanes<SHAKE256_LANES>(A, in, 6, DOM_SHAKE);
+    keccak_f1600(A);
+    uint2 *kk = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2), *mm = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2 + 32);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        kk[i] = A[3 + i];
+        mm[i] = in[3 + i];
+    }
+    uint8_t seed[24];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            seed[8 * i + q] = (uint8_t)(A[i].x >> (8 * q));
+            seed[8 * i + 4 + q] = (uint8_t)(A[i].y >> (8 * q));
+        }
+    }
+    enc_noise(scr, seed);
+}
+
+// F = SHAKE256(ct || key, 24): encaps key = k; decaps key = fail ? s : k'
+__global__ void __launch_bounds__(64) fr_post(int n, const uint8_t *ct, const uint8_t *scratch, const uint8_t *sk,
+                                              uint8_t *ss) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    const uint8_t *scr = scratch + (size_t)x * SCRATCH;
+    const uint2 *k = reinterpret_cast<const uint2 *>(scr + NOISE_U16 * 2);
+    uint2 key[3];
+    if (sk) {
+        const uint32_t mask = 0u - (uint32_t)(scr[NOISE_U16 * 2 + 64] != 0);
+        const uint2 *s = reinterpret_cast<const uint2 *>(sk + (size_t)x * SKB);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            key[i] = make_uint2(k[i].x ^ (mask & (k[i].x ^ s[i].x)), k[i].y ^ (mask & (k[i].y ^ s[i].y)));
+    } else {
+#pragma unroll
+        for (int i = 0; i < 3; i++) key[i] = k[i];
+    }
+    uint2 A[25];
+    absorb2<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(ct + (size_t)x * CTB), CTB / 8, key, 3, DOM_SHAKE);
+    keccak_f1600(A);
+    uint2 *o = reinterpret_cast<uint2 *>(ss + (size_t)x * SSB);
+    o[0] = A[0];
+    o[1] = A[1];
+    o[2] = A[2];
+}
+
+// keypair epilogue: sk = s || pk || S (u16 LE, S[k*N + j]) || SHAKE256(pk, 24)
+__global__ void __launch_bounds__(64) fr_kp_post(int n, const uint8_t *coins, int cstride, const uint8_t *pk,
+                                                 const uint8_t *scratch, uint8_t *sk) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    uint8_t *s = sk + (size_t)x * SKB;
+    const uint8_t *p = pk + (size_t)x * PKB;
+    const uint16_t *St = reinterpret_cast<const uint16_t *>(scratch + (size_t)x * SCRATCH);
+    for (int i = 0; i < 3; i++)
+        reinterpret_cast<uint2 *>(s)[i] = reinterpret_cast<const uint2 *>(coins + (size_t)x * cstride)[i];
+    for (int i = 0; i < PKB / 8; i++) reinterpret_cast<uint2 *>(s + SSB)[i] = reinterpret_cast<const uint2 *>(p)[i];
+    uint16_t *dS = reinterpret_cast<uint16_t *>(s + SSB + PKB);
+    for (int k = 0; k < NB; k++)
+        for (int j = 0; j < N; j++) dS[k * N + j] = St[j * NB + k];
+    uint2 A[25];
+    keccak_absorb_lanes<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(p), PKB / 8, DOM_SHAKE);
+    keccak_f1600(A);
+    uint2 *h = reinterpret_cast<uint2 *>(s + SSB + PKB + C1B);
+    h[0] = A[0];
+    h[1] = A[1];
+    h[2] = A[2];
+}
+
+// ---------------------------------------------------------------------------------------------
+// Core kernels: A generated on the fly
+// ---------------------------------------------------------------------------------------------
+// B = A S + E, one thread per row of A; CTA = (instance, group of rows); St in shared memory.
+__global__ void __launch_bounds__(256) fr_kp_core(int n, uint8_t *pk, const uint8_t *scratch) {
+    __shared__ __align__(16) uint16_t St[N * NB];
+    const int x = blockIdx.y;
+    const uint16_t *gSt = reinterpret_cast<const uint16_t *>(scratch + (size_t)x * SCRATCH), *E = gSt + N * NB;
+    for (int i = threadIdx.x; i < N * NB / 8; i += blockDim.x)
+        reinterpret_cast<uint4 *>(St)[i] = reinterpret_cast<const uint4 *>(gSt)[i];
+    __syncthreads();
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= N) return;
+    uint8_t *p = pk + (size_t)x * PKB;
+    uint2 A[25];
+    row_absorb(A, row, reinterpret_cast<const uint2 *>(p));
+    uint32_t acc[NB];
+#pragma unroll
+    for (int k = 0; k < NB; k++) acc[k] = E[row * NB + k];
+    for (int blk = 0; blk < ROW_BLOCKS; blk++) {
+        keccak_f1600(A);
+        const int j0 = blk * 84;
+#pragma unroll
+        for (int w = 0; w < 42; w++) {
+            const uint32_t t = (w & 1) ? A[w >> 1].y : A[w >> 1].x;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int j = j0 + 2 * w + h;
+                if (j < N) {
+                    const uint32_t a = h ? (t >> 16) : (t & 0xffff);
+                    const uint4 sv = reinterpret_cast<const uint4 *>(St)[j];
+                    acc[0] += a * (sv.x & 0xffff);
+                    acc[1] += a * (sv.x >> 16);
+                    acc[2] += a * (sv.y & 0xffff);
+                    acc[3] += a * (sv.y >> 16);
+                    acc[4] += a * (sv.z & 0xffff);
+                    acc[5] += a * (sv.z >> 16);
+                    acc[6] += a * (sv.w & 0xffff);
+                    acc[7] += a * (sv.w >> 16);
+                }
+            }
+        }
+    }
+    // pack B row (8 values, 16-bit big-endian) at pk[16 + 16 row]
+    uint8_t *o = p + SEEDA + 16 * row;
+#pragma unroll
+    for (int k = 0; k < NB; k++) {
+        o[2 * k] = (uint8_t)(acc[k] >> 8);
+        o[2 * k + 1] = (uint8_t)acc[k];
+    }
+}
+
+// B' = S' A + E' (and V = S' B + E'', C = V + encode(mu)), CTA per instance.  cmp == nullptr:
+// pack into ct; else compare with ct and store the fail flag in scratch.
+constexpr int SA_THREADS = 256;
+constexpr int STAGE_PITCH = 86;  // u16 per staged row block (84 used; odd word pitch)
+__global__ void __launch_bounds__(SA_THREADS) fr_sa_core(int n, uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *pk,
+                                                         int pk_stride, uint8_t *scratch) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint16_t *Spt = reinterpret_cast<uint16_t *>(smem);                       // N x 8
+    uint32_t *acc = reinterpret_cast<uint32_t *>(smem + N * NB * 2);          // 8 x N (+64 for V)
+    uint16_t *stage = reinterpret_cast<uint16_t *>(smem + N * NB * 2 + (NB * N + 64) * 4);  // threads x 86
+    const int x = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x;
+    uint8_t *scr = scratch + (size_t)x * SCRATCH;
+    const uint16_t *gSpt = reinterpret_cast<const uint16_t *>(scr), *Ep = gSpt + N * NB, *Epp = Ep + N * NB;
+    const uint8_t *p = pk + (size_t)x * pk_stride;
+    for (int i = tid; i < N * NB / 8; i += nthr) reinterpret_cast<uint4 *>(Spt)[i] = reinterpret_cast<const uint4 *>(gSpt)[i];
+    for (int i = tid; i < NB * N; i += nthr) acc[i] = Ep[i];
+    for (int i = tid; i < 64; i += nthr) acc[NB * N + i] = Epp[i];
+    __syncthreads();
+    // rows pass by pass; within a pass each thread owns one row and squeezes one block per round
+    const int ncol_slices = nthr / 84;  // threads (j, slice): j = tid % 84, slice = tid / 84
+    for (int r0 = 0; r0 < N; r0 += nthr) {
+        const int rows = min(nthr, N - r0);
+        uint2 A[25];
+        const int myrow = r0 + tid;
+        if (tid < rows) row_absorb(A, myrow, reinterpret_cast<const uint2 *>(p));
+        for (int blk = 0; blk < ROW_BLOCKS; blk++) {
+            if (tid < rows) {
+                keccak_f1600(A);
+                uint32_t *st = reinterpret_cast<uint32_t *>(stage + tid * STAGE_PITCH);
+#pragma unroll
+                for (int w = 0; w < 42; w++) st[w] = (w & 1) ? A[w >> 1].y : A[w >> 1].x;
+            }
+            __syncthreads();
+            const int j = tid % 84, slice = tid / 84, col = blk * 84 + j;
+            if (slice < ncol_slices && col < N) {
+                const int per = (rows + ncol_slices - 1) / ncol_slices;
+                const int k0 = slice * per, k1 = min(rows, k0 + per);
+                uint32_t s[NB] = {0, 0, 0, 0, 0, 0, 0, 0};
+                for (int k = k0; k < k1; k++) {
+                    const uint32_t a = stage[k * STAGE_PITCH + j];
+                    const uint4 sv = reinterpret_cast<const uint4 *>(Spt)[r0 + k];
+                    s[0] += a * (sv.x & 0xffff);
+                    s[1] += a * (sv.x >> 16);
+                    s[2] += a * (sv.y & 0xffff);
+                    s[3] += a * (sv.y >> 16);
+                    s[4] += a * (sv.z & 0xffff);
+                    s[5] += a * (sv.z >> 16);
+                    s[6] += a * (sv.w & 0xffff);
+                    s[7] += a * (sv.w >> 16);
+                }
+#pragma unroll
+                for (int i = 0; i < NB; i++) atomicAdd(acc + i * N + col, s[i]);
+            }
+            __syncthreads();
+        }
+    }
+    // V = S' B + E'' (B = unpack(pk_b), N x 8): 64 outputs, k split over the CTA
+    {
+        const uint8_t *pb = p + SEEDA;
+        for (int t = tid; t < 64 * 4; t += nthr) {
+            const int o = t & 63, part = t >> 6, i = o >> 3, l = o & 7;
+            uint32_t sum = 0;
+            for (int k = part; k < N; k += 4) sum += (uint32_t)Spt[k * NB + i] * ld_be16(pb + 2 * (k * NB + l));
+            atomicAdd(acc + NB * N + o, sum);
+        }
+    }
+    __syncthreads();
+    const uint8_t *mu = scr + NOISE_U16 * 2 + 32;
+    uint32_t diff = 0;
+    // B' (8 x N, row-major) -> c1, 16-bit big-endian
+    for (int e = tid; e < NB * N; e += nthr) {
+        const uint32_t v = acc[e] & 0xffff;
+        if (ct_cmp) diff |= v ^ ld_be16(ct_cmp + (size_t)x * CTB + 2 * e);
+        else {
+            ct[(size_t)x * CTB + 2 * e] = (uint8_t)(v >> 8);
+            ct[(size_t)x * CTB + 2 * e + 1] = (uint8_t)v;
+        }
+    }
+    // C = V + encode(mu) -> c2
+    for (int e = tid; e < 64; e += nthr) {
+        const int g = e >> 3, j = e & 7;
+        const uint32_t temp = (uint32_t)mu[3 * g] | ((uint32_t)mu[3 * g + 1] << 8) | ((uint32_t)mu[3 * g + 2] << 16);
+        const uint32_t enc = ((temp >> (3 * j)) & 7) << 13;
+        const uint32_t v = (acc[NB * N + e] + enc) & 0xffff;
+        if (ct_cmp) diff |= v ^ ld_be16(ct_cmp + (size_t)x * CTB + C1B + 2 * e);
+        else {
+            ct[(size_t)x * CTB + C1B + 2 * e] = (uint8_t)(v >> 8);
+            ct[(size_t)x * CTB + C1B + 2 * e + 1] = (uint8_t)v;
+        }
+    }
+    if (ct_cmp) {
+        const int any = __syncthreads_or(diff != 0);
+        if (tid == 0) scr[NOISE_U16 * 2 + 64] = (uint8_t)any;
+    }
+}
+
+static size_t sa_smem(int threads) { return (size_t)N * NB * 2 + ((size_t)NB * N + 64) * 4 + (size_t)threads * STAGE_PITCH * 2; }
+
+}  // namespace frodo
+
+using namespace frodo;
+
+int frodo_init_constants() {
+    const uint16_t cdf[11] = {5638, 15915, 23689, 28571, 31116, 32217, 32613, 32731, 32760, 32766, 32767};
+    uint2 rc[24];
+    keccak_rc_host(rc);
+    if (cudaMemcpyToSymbol(c_keccak_rc, rc, sizeof rc) != cudaSuccess) return PQCGPU_ECUDA;
+    if (cudaMemcpyToSymbol(c_cdf, cdf, sizeof cdf) != cudaSuccess) return PQCGPU_ECUDA;
+    return PQCGPU_OK;
+}
+size_t frodo_scratch_bytes() { return SCRATCH; }
+
+int frodo_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
+                      cudaStream_t st) {
+    PQC_LAUNCH(st, "fr_kp_pre", 976, 0, fr_kp_pre<<<(n + 63) / 64, 64, 0, st>>>(n, coins, cstride, pk, scratch));
+    PQC_LAUNCH(st, "fr_kp_core", 976, 0, fr_kp_core<<<dim3((N + 255) / 256, n), 256, 0, st>>>(n, pk, scratch));
+    PQC_LAUNCH(st, "fr_kp_post", 976, 0, fr_kp_post<<<(n + 63) / 64, 64, 0, st>>>(n, coins, cstride, pk, scratch, sk));
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
+int frodo_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
+                  cudaStream_t st) {
+    const size_t sm = sa_smem(SA_THREADS);
+    if (cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+        return PQCGPU_ECUDA;
+    PQC_LAUNCH(st, "fr_enc_pre", 976, 0, fr_enc_pre<<<(n + 63) / 64, 64, 0, st>>>(n, pk, mu, scratch));
+    PQC_LAUNCH(st, "fr_sa_core", 976, 0, fr_sa_core<<<n, SA_THREADS, sm, st>>>(n, ct, nullptr, pk, PKB, scratch));
+    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 63) / 64, 64, 0, st>>>(n, ct, scratch, nullptr, ss));
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
+int frodo_dec_dev(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, cudaStream_t st) {
+    const size_t sm = sa_smem(SA_THREADS);
+    if (cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+        return PQCGPU_ECUDA;
+    PQC_LAUNCH(st, "fr_dec_pre", 976, 0, fr_dec_pre<<<(n + 63) / 64, 64, 0, st>>>(n, ct, sk, scratch));
+    PQC_LAUNCH(st, "fr_sa_core", 976, 0,
+               fr_sa_core<<<n, SA_THREADS, sm, st>>>(n, nullptr, ct, sk + SSB, SKB, scratch));
+    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 63) / 64, 64, 0, st>>>(n, ct, scratch, sk, ss));
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
+}  // namespace pqc

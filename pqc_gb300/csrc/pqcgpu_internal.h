@@ -61,4 +61,13 @@ int newhope_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const ui
 // kem=1: out = ss (32 B); kem=0: out = message
 int newhope_dec_dev(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st);
 
+// ---- FrodoKEM-976 (frodo.cu) ----
+int frodo_init_constants();
+size_t frodo_scratch_bytes();  // per instance, all three operations
+int frodo_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
+                      cudaStream_t st);
+int frodo_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
+                  cudaStream_t st);
+int frodo_dec_dev(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, cudaStream_t st);
+
 }  // namespace pqc
