@@ -122,7 +122,7 @@ __device__ __forceinline__ uint32_t ld_be16(const uint8_t *p) { return ((uint32_
 // Serial sponges (thread per instance)
 // ---------------------------------------------------------------------------------------------
 // keypair: seedA = SHAKE256(z, 16) -> pk[0..16); S (as St[j][k], N x 8) and E (N x 8) -> scratch
-__global__ void __launch_bounds__(64) fr_kp_pre(int n, const uint8_t *coins, int cstride, uint8_t *pk, uint8_t *scratch) {
+__global__ void __launch_bounds__(32) fr_kp_pre(int n, const uint8_t *coins, int cstride, uint8_t *pk, uint8_t *scratch) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
     const uint8_t *c = coins + (size_t)x * cstride;  // s(24) || seedSE(24) || z(16)
@@ -157,7 +157,7 @@ __device__ __forceinline__ void enc_noise(uint8_t *scr, const uint8_t *seedSE) {
     });
 }
 
-__global__ void __launch_bounds__(64) fr_enc_pre(int n, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch) {
+__global__ void __launch_bounds__(32) fr_enc_pre(int n, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
     uint8_t *scr = scratch + (size_t)x * SCRATCH;
@@ -193,53 +193,62 @@ __global__ void __launch_bounds__(64) fr_enc_pre(int n, const uint8_t *pk, const
     enc_noise(scr, seed);
 }
 
-// decaps prologue: W = C - B' S; mu' = decode(W); (seedSE' || k') = G2(pkh || mu'); noise.
-__global__ void __launch_bounds__(64) fr_dec_pre(int n, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= n) return;
-    const uint8_t *c = ct + (size_t)x * CTB, *s = sk + (size_t)x * SKB;
-    const uint8_t *sS = s + SSB + PKB;  // S as u16 LE, S[k*N + j]
-    uint8_t *scr = scratch + (size_t)x * SCRATCH;
-    uint8_t mu[MUB];
-    // W[i][j] = C[i][j] - sum_k B'[i][k] S[j][k]  (frodo_mul_bs: out[i*8+j] = sum_k b[i*N+k] s[j*N+k])
-    for (int g = 0; g < 8; g++) {  // word g of the key: 8 pieces of 3 bits from W[8g .. 8g+7]
+// decaps, step 1 (CTA per instance): W = C - B' S (frodo_mul_bs + frodo_sub), mu' = decode(W)
+// -> scratch mu' slot.  B' and S are staged in shared memory with coalesced loads.
+__global__ void __launch_bounds__(256) fr_dec_w(int n, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch) {
+    __shared__ __align__(16) uint16_t Bp[NB * N];
+    __shared__ __align__(16) uint16_t S[NB * N];
+    __shared__ uint32_t W[64];
+    const int x = blockIdx.x, tid = threadIdx.x;
+    const uint8_t *c = ct + (size_t)x * CTB, *sS = sk + (size_t)x * SKB + SSB + PKB;
+    for (int e = tid; e < NB * N; e += blockDim.x) {
+        Bp[e] = (uint16_t)ld_be16(c + 2 * e);
+        S[e] = (uint16_t)(sS[2 * e] | (sS[2 * e + 1] << 8));
+    }
+    if (tid < 64) W[tid] = 0;
+    __syncthreads();
+    // W[i][j] = sum_k Bp[i][k] S[j][k]: 4 threads per output, k interleaved
+    {
+        const int o = tid & 63, part = tid >> 6, i = o >> 3, j = o & 7;
+        uint32_t sum = 0;
+        for (int k = part; k < N; k += 4) sum += (uint32_t)Bp[i * N + k] * S[j * N + k];
+        atomicAdd(&W[o], sum);
+    }
+    __syncthreads();
+    if (tid < 8) {  // word g = tid: 8 pieces of 3 bits (key_decode)
+        const int g = tid;
         uint32_t templong = 0;
         for (int jj = 0; jj < 8; jj++) {
-            const int i = g, j = jj;  // W index 8g + jj = i*8 + j
-            uint32_t sum = 0;
-            for (int k = 0; k < N; k++)
-                sum += ld_be16(c + 2 * (i * N + k)) * (uint32_t)(sS[2 * (j * N + k)] | (sS[2 * (j * N + k) + 1] << 8));
-            const uint32_t w = (ld_be16(c + C1B + 2 * (i * NB + j)) - sum) & 0xffff;
-            const uint32_t t = ((w & 0xffff) + (1u << 12)) >> 13;
+            const uint32_t w = (ld_be16(c + C1B + 2 * (g * NB + jj)) - W[g * NB + jj]) & 0xffff;
+            const uint32_t t = (w + (1u << 12)) >> 13;
             templong |= (t & 7) << (3 * jj);
         }
+        uint8_t *mu = scratch + (size_t)x * SCRATCH + NOISE_U16 * 2 + 32;
         mu[3 * g] = (uint8_t)templong;
         mu[3 * g + 1] = (uint8_t)(templong >> 8);
         mu[3 * g + 2] = (uint8_t)(templong >> 16);
     }
+}
+
+// decaps, step 2 (thread per instance): (seedSE' || k') = G2(pkh || mu'); S', E', E'' -> scratch
+__global__ void __launch_bounds__(32) fr_dec_pre(int n, const uint8_t *sk, uint8_t *scratch) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    const uint8_t *s = sk + (size_t)x * SKB;
+    uint8_t *scr = scratch + (size_t)x * SCRATCH;
     uint2 A[25], in[6];
     const uint2 *pkh = reinterpret_cast<const uint2 *>(s + SSB + PKB + C1B);
-    in[0] = pkh[0];
-    in[1] = pkh[1];
-    in[2] = pkh[2];
+    const uint2 *mu = reinterpret_cast<const uint2 *>(scr + NOISE_U16 * 2 + 32);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        uint32_t lo = 0, hi = 0;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            lo |= (uint32_t)mu[8 * i + q] << (8 * q);
-            hi |= (uint32_t)mu[8 * i + 4 + q] << (8 * q);
-        }
-        in[3 + i] = make_uint2(lo, hi);
+        in[i] = pkh[i];
+        in[3 + i] = mu[i];
     }
     keccak_absorb_lanes<SHAKE256_LANES>(A, in, 6, DOM_SHAKE);
     keccak_f1600(A);
-    uint2 *kk = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2), *mm = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2 + 32);
+    uint2 *kk = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2);
 #pragma unroll
-    for (int i = 0; i < 3; i++) {
-        kk[i] = A[3 + i];
-        mm[i] = in[3 + i];
-    }
+    for (int i = 0; i < 3; i++) kk[i] = A[3 + i];
     uint8_t seed[24];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -253,7 +262,7 @@ __global__ void __launch_bounds__(64) fr_dec_pre(int n, const uint8_t *ct, const
 }
 
 // F = SHAKE256(ct || key, 24): encaps key = k; decaps key = fail ? s : k'
-__global__ void __launch_bounds__(64) fr_post(int n, const uint8_t *ct, const uint8_t *scratch, const uint8_t *sk,
+__global__ void __launch_bounds__(32) fr_post(int n, const uint8_t *ct, const uint8_t *scratch, const uint8_t *sk,
                                               uint8_t *ss) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
@@ -280,7 +289,7 @@ __global__ void __launch_bounds__(64) fr_post(int n, const uint8_t *ct, const ui
 }
 
 // keypair epilogue: sk = s || pk || S (u16 LE, S[k*N + j]) || SHAKE256(pk, 24)
-__global__ void __launch_bounds__(64) fr_kp_post(int n, const uint8_t *coins, int cstride, const uint8_t *pk,
+__global__ void __launch_bounds__(32) fr_kp_post(int n, const uint8_t *coins, int cstride, const uint8_t *pk,
                                                  const uint8_t *scratch, uint8_t *sk) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
@@ -468,9 +477,9 @@ size_t frodo_scratch_bytes() { return SCRATCH; }
 
 int frodo_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
                       cudaStream_t st) {
-    PQC_LAUNCH(st, "fr_kp_pre", 976, 0, fr_kp_pre<<<(n + 63) / 64, 64, 0, st>>>(n, coins, cstride, pk, scratch));
+    PQC_LAUNCH(st, "fr_kp_pre", 976, 0, fr_kp_pre<<<(n + 15) / 16, 16, 0, st>>>(n, coins, cstride, pk, scratch));
     PQC_LAUNCH(st, "fr_kp_core", 976, 0, fr_kp_core<<<dim3((N + 255) / 256, n), 256, 0, st>>>(n, pk, scratch));
-    PQC_LAUNCH(st, "fr_kp_post", 976, 0, fr_kp_post<<<(n + 63) / 64, 64, 0, st>>>(n, coins, cstride, pk, scratch, sk));
+    PQC_LAUNCH(st, "fr_kp_post", 976, 0, fr_kp_post<<<(n + 15) / 16, 16, 0, st>>>(n, coins, cstride, pk, scratch, sk));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
@@ -479,9 +488,9 @@ int frodo_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint
     const size_t sm = sa_smem(SA_THREADS);
     if (cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return PQCGPU_ECUDA;
-    PQC_LAUNCH(st, "fr_enc_pre", 976, 0, fr_enc_pre<<<(n + 63) / 64, 64, 0, st>>>(n, pk, mu, scratch));
+    PQC_LAUNCH(st, "fr_enc_pre", 976, 0, fr_enc_pre<<<(n + 15) / 16, 16, 0, st>>>(n, pk, mu, scratch));
     PQC_LAUNCH(st, "fr_sa_core", 976, 0, fr_sa_core<<<n, SA_THREADS, sm, st>>>(n, ct, nullptr, pk, PKB, scratch));
-    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 63) / 64, 64, 0, st>>>(n, ct, scratch, nullptr, ss));
+    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 15) / 16, 16, 0, st>>>(n, ct, scratch, nullptr, ss));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
@@ -489,10 +498,11 @@ int frodo_dec_dev(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint
     const size_t sm = sa_smem(SA_THREADS);
     if (cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return PQCGPU_ECUDA;
-    PQC_LAUNCH(st, "fr_dec_pre", 976, 0, fr_dec_pre<<<(n + 63) / 64, 64, 0, st>>>(n, ct, sk, scratch));
+    PQC_LAUNCH(st, "fr_dec_w", 976, 0, fr_dec_w<<<n, 256, 0, st>>>(n, ct, sk, scratch));
+    PQC_LAUNCH(st, "fr_dec_pre", 976, 0, fr_dec_pre<<<(n + 15) / 16, 16, 0, st>>>(n, sk, scratch));
     PQC_LAUNCH(st, "fr_sa_core", 976, 0,
                fr_sa_core<<<n, SA_THREADS, sm, st>>>(n, nullptr, ct, sk + SSB, SKB, scratch));
-    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 63) / 64, 64, 0, st>>>(n, ct, scratch, sk, ss));
+    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 15) / 16, 16, 0, st>>>(n, ct, scratch, sk, ss));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
