@@ -129,11 +129,39 @@ int pqcgpu_newhope_cpapke_enc_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *ct, cons
 int pqcgpu_newhope_cpapke_dec_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *msg, const uint8_t *ct, const uint8_t *sk,
                                     unsigned flags);
 
-/* ---- launch-shape tuning (used by the autotuner) -----------------------------------------
- * Kyber core kernels: op 0 keypair, 1 encaps, 2 decaps; k = 2..4; ni = instances per CTA (1..128),
- * threads per CTA (multiple of 32, 32..512).  Applies to all contexts of the process. */
-int pqcgpu_kyber_set_shape(int op, int k, int ni, int threads);
-int pqcgpu_kyber_get_shape(int op, int k, int *ni, int *threads);
+/* ---- mixed batches and CUDA graphs --------------------------------------------------------
+ * A job is one (algorithm, operation, batch) with its device buffers:
+ *   op PQCGPU_OP_KEYPAIR: in0 coins          -> out0 pk, out1 sk
+ *   op PQCGPU_OP_ENC:     in0 pk,  in1 coins -> out0 ct, out1 ss
+ *   op PQCGPU_OP_DEC:     in0 ct,  in1 sk    -> out0 ss
+ * pqcgpu_kem_mixed_batch runs any mix of jobs (parameter sets, operations, uneven sizes) at once:
+ * the jobs are spread over the context's concurrent streams after the work already queued on the
+ * context stream and joined back into it (asynchronous; device pointers only, PQCGPU_DEVICE_PTRS).
+ * pqcgpu_graph_capture records such a job list once into a CUDA graph (with its own scratch) and
+ * pqcgpu_graph_launch replays it on the context stream: same buffers, no per-kernel launch cost. */
+#define PQCGPU_OP_KEYPAIR 0
+#define PQCGPU_OP_ENC 1
+#define PQCGPU_OP_DEC 2
+typedef struct {
+    int32_t alg; /* pqcgpu_alg */
+    int32_t op;  /* PQCGPU_OP_* */
+    uint64_t n;  /* instances */
+    const uint8_t *in0, *in1;
+    uint8_t *out0, *out1;
+} pqcgpu_job;
+typedef struct pqcgpu_graph pqcgpu_graph;
+int pqcgpu_kem_mixed_batch(pqcgpu_ctx *ctx, const pqcgpu_job *jobs, size_t njobs, unsigned flags);
+int pqcgpu_graph_capture(pqcgpu_ctx *ctx, const pqcgpu_job *jobs, size_t njobs, unsigned flags, pqcgpu_graph **out);
+int pqcgpu_graph_launch(pqcgpu_graph *graph);
+int pqcgpu_graph_destroy(pqcgpu_graph *graph);
+
+/* ---- launch-shape tuning (used by the autotuner, pqc_gb300/autotune.py) --------------------
+ * Core-kernel launch shape per (algorithm, operation): ni = instances per CTA, threads per CTA
+ * (multiple of 32).  Kyber: ni 1..128, threads 32..512 (shared by the round-2 and round-3 sets of
+ * the same k); NewHope: ni 1..64, threads 32..256; FrodoKEM has a fixed shape (PQCGPU_EUNSUPPORTED).
+ * Applies to all contexts of the process. */
+int pqcgpu_set_launch_shape(pqcgpu_alg alg, int op, int ni, int threads);
+int pqcgpu_get_launch_shape(pqcgpu_alg alg, int op, int *ni, int *threads);
 
 /* ---- tracing and roofline probes ------------------------------------------------------------
  * pqcgpu_profile_enable(1): every kernel launch is bracketed by CUDA events on its stream.

@@ -31,8 +31,12 @@ SIGNATURES = {
     "pqcgpu_newhope_cpapke_keypair_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_newhope_cpapke_enc_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_newhope_cpapke_dec_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _uint]),
-    "pqcgpu_kyber_set_shape": (_int, [_int, _int, _int, _int]),
-    "pqcgpu_kyber_get_shape": (_int, [_int, _int, _c.POINTER(_int), _c.POINTER(_int)]),
+    "pqcgpu_kem_mixed_batch": (_int, [_vp, _vp, _sz, _uint]),
+    "pqcgpu_graph_capture": (_int, [_vp, _vp, _sz, _uint, _c.POINTER(_vp)]),
+    "pqcgpu_graph_launch": (_int, [_vp]),
+    "pqcgpu_graph_destroy": (_int, [_vp]),
+    "pqcgpu_set_launch_shape": (_int, [_int, _int, _int, _int]),
+    "pqcgpu_get_launch_shape": (_int, [_int, _int, _c.POINTER(_int), _c.POINTER(_int)]),
     "pqcgpu_profile_enable": (_int, [_int]),
     "pqcgpu_profile_read": (_int, [_c.c_char_p, _sz]),
     "pqcgpu_probe_peaks": (_int, [_int, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]),
@@ -43,6 +47,14 @@ for _alg in ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976"):
     SIGNATURES["pqcgpu_%s_crypto_kem_keypair" % _alg] = (_int, [_u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_enc" % _alg] = (_int, [_u8p, _u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_dec" % _alg] = (_int, [_u8p, _u8p, _u8p])
+
+
+
+class Job(_c.Structure):
+    """pqcgpu_job of include/pqcgpu.h."""
+    _fields_ = [("alg", _c.c_int32), ("op", _c.c_int32), ("n", _c.c_uint64), ("in0", _c.c_void_p),
+                ("in1", _c.c_void_p), ("out0", _c.c_void_p), ("out1", _c.c_void_p)]
+
 
 _lib = None
 

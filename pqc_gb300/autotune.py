@@ -1,0 +1,128 @@
+"""Autotuner for the core-kernel launch shapes (instances per CTA, threads per CTA).
+
+Replaces the reference's ANALYSIS_MODE block-size sweep (Kyber_GPU_Batched/indcpa.cu:21-70), which
+re-ran every launch over ten block sizes and printed the best: here each (algorithm, operation) is
+timed with CUDA events over a candidate grid at a given batch size, the fastest shape is applied
+through pqcgpu_set_launch_shape, and the choice is persisted in a JSON cache keyed by GPU name so
+later processes load it instead of re-tuning.
+
+    python -m pqc_gb300.autotune [--batch 65536] [--out tuning.json]
+"""
+import argparse
+import ctypes
+import json
+import os
+
+from . import _lib, drbg, kem
+
+DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "tuning.json")
+TUNABLE = ("kyber512", "kyber768", "kyber1024", "newhope1024")
+
+
+def candidates(alg, op):
+    if alg.startswith("kyber"):
+        k = {"kyber512": 2, "kyber768": 3, "kyber1024": 4}[alg]
+        out = []
+        for ni in (4, 6, 8, 10, 12, 14, 16, 20, 24, 28, 32, 40, 48):
+            jobs = ni * k * k
+            for thr in (64, 96, 128, 160, 192, 224, 256, 320, 384):
+                lo = min(((jobs + 31) // 32) * 32, 384) - 64
+                if lo <= thr <= ((jobs + 31) // 32) * 32 + 32:
+                    out.append((ni, thr))
+        return out
+    return [(ni, thr) for ni in (1, 2, 4, 8) for thr in (64, 128, 256) if thr // 32 >= 1]
+
+
+def get_shape(lib, alg, op):
+    a, b = ctypes.c_int(), ctypes.c_int()
+    if lib.pqcgpu_get_launch_shape(kem.alg_id(alg), op, ctypes.byref(a), ctypes.byref(b)) != 0:
+        return None
+    return a.value, b.value
+
+
+def tune(batch=65536, algs=TUNABLE, reps=3, device=0, log=print):
+    import torch
+    lib = _lib.load()
+    ctx = kem.Context(device)
+    dev = torch.device("cuda", device)
+    st = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    result = {}
+    for alg in algs:
+        s = kem.sizes(alg)
+        n = batch if alg != "newhope1024" else min(batch, 16384)
+        seed = drbg.seed48(99)
+        up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
+        kc = up(drbg.stream(seed, b"kp", n * s["kp_coins"]))
+        ec = up(drbg.stream(seed, b"enc", n * s["enc_coins"]))
+        pk, sk = (torch.empty(n * s[x], dtype=torch.uint8, device=dev) for x in ("pk", "sk"))
+        ct = torch.empty(n * s["ct"], dtype=torch.uint8, device=dev)
+        ss, ss2 = (torch.empty(n * s["ss"], dtype=torch.uint8, device=dev) for _ in range(2))
+        torch.cuda.synchronize(dev)
+        ctx.keypair_dev(alg, n, pk, sk, kc)
+        ctx.enc_dev(alg, n, ct, ss, pk, ec)
+        ctx.wait()
+        fns = {0: lambda: ctx.keypair_dev(alg, n, pk, sk, kc), 1: lambda: ctx.enc_dev(alg, n, ct, ss, pk, ec),
+               2: lambda: ctx.dec_dev(alg, n, ss2, ct, sk)}
+        for op in (0, 1, 2):
+            best = None
+            for ni, thr in candidates(alg, op):
+                if lib.pqcgpu_set_launch_shape(kem.alg_id(alg), op, ni, thr) != 0:
+                    continue
+                try:
+                    fns[op]()
+                    ctx.wait()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(st)
+                    for _ in range(reps):
+                        fns[op]()
+                    e1.record(st)
+                    e1.synchronize()
+                    ms = e0.elapsed_time(e1) / reps
+                except RuntimeError:
+                    continue
+                if best is None or ms < best[0]:
+                    best = (ms, ni, thr)
+            lib.pqcgpu_set_launch_shape(kem.alg_id(alg), op, best[1], best[2])
+            result["%s/%d" % (alg, op)] = {"ni": best[1], "threads": best[2], "ms": best[0], "batch": n}
+            log("%s op %d: ni=%d threads=%d  %.3f ms" % (alg, op, best[1], best[2], best[0]))
+    ctx.close()
+    return {"gpu": torch.cuda.get_device_name(dev), "shapes": result}
+
+
+def save(tuning, path=DEFAULT_CACHE):
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    with open(path, "w") as f:
+        json.dump(tuning, f, indent=1)
+
+
+def apply(tuning):
+    """Apply a tuning dict (or a path to its JSON) to the loaded library."""
+    if isinstance(tuning, str):
+        with open(tuning) as f:
+            tuning = json.load(f)
+    lib = _lib.load()
+    for key, v in tuning["shapes"].items():
+        alg, op = key.split("/")
+        _lib.check(lib.pqcgpu_set_launch_shape(kem.alg_id(alg), int(op), v["ni"], v["threads"]))
+    return tuning
+
+
+def load_cached(path=DEFAULT_CACHE, gpu_name=None):
+    """Apply the cached tuning if it exists and was made on this GPU model; returns it or None."""
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        t = json.load(f)
+    if gpu_name is not None and t.get("gpu") != gpu_name:
+        return None
+    return apply(t)
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--batch", type=int, default=65536)
+    ap.add_argument("--out", default=DEFAULT_CACHE)
+    a = ap.parse_args()
+    t = tune(a.batch)
+    save(t, a.out)
+    print("saved", a.out)

@@ -8,6 +8,7 @@
 #include <atomic>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "pqcgpu_internal.h"
 
@@ -182,6 +183,9 @@ struct pqcgpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t side[2] = {nullptr, nullptr};  // pipelining streams for host-buffer calls
+    static constexpr int NPAR = 8;              // concurrent streams for mixed batches
+    cudaStream_t par[NPAR] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[NPAR] = {};
     bool own_stream = true;
     size_t budget = 0;
     uint8_t *arena = nullptr;
@@ -258,6 +262,17 @@ extern "C" int pqcgpu_ctx_create(pqcgpu_ctx **out, int device, size_t budget) {
         delete c;
         return rc;
     }
+    for (int i = 0; i < pqcgpu_ctx::NPAR; i++) {
+        if ((rc = cuda_err(cudaStreamCreateWithFlags(&c->par[i], cudaStreamNonBlocking), "stream")) ||
+            (rc = cuda_err(cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming), "event"))) {
+            pqcgpu_ctx_destroy(c);
+            return rc;
+        }
+    }
+    if ((rc = cuda_err(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming), "event"))) {
+        pqcgpu_ctx_destroy(c);
+        return rc;
+    }
     c->launches_at_create = g_launch_count.load();
     *out = c;
     return PQCGPU_OK;
@@ -271,6 +286,11 @@ extern "C" int pqcgpu_ctx_destroy(pqcgpu_ctx *c) {
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     for (auto s : c->side)
         if (s) cudaStreamDestroy(s);
+    for (int i = 0; i < pqcgpu_ctx::NPAR; i++) {
+        if (c->par[i]) cudaStreamDestroy(c->par[i]);
+        if (c->join_ev[i]) cudaEventDestroy(c->join_ev[i]);
+    }
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     delete c;
     return PQCGPU_OK;
 }
@@ -427,6 +447,77 @@ static int coins_or_drbg(pqcgpu_ctx *c, const uint8_t *&coins, size_t bytes, uns
     return PQCGPU_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// One device operation: op 0 keypair (in0 coins -> out0 pk, out1 sk), 1 encaps (in0 pk, in1 coins ->
+// out0 ct, out1 ss), 2 decaps (in0 ct, in1 sk -> out0 ss).  All pointers on the device.
+// ---------------------------------------------------------------------------------------------
+namespace pqc {
+size_t op_scratch_bytes(int alg, int op, int plain) {
+    int variant, k;
+    if (kyber_alg(alg, &variant, &k)) return kyber_scratch_bytes(k, op, plain);
+    if (alg == PQCGPU_NEWHOPE1024) return op == 1 ? 64 : 0;
+    if (alg == PQCGPU_FRODO976) return frodo_scratch_bytes();
+    return 0;
+}
+int op_dev(int alg, int op, int n, const uint8_t *in0, const uint8_t *in1, uint8_t *out0, uint8_t *out1,
+           uint8_t *scr, int plain, cudaStream_t s) {
+    AlgInfo ai;
+    if (!alg_info(alg, &ai) || op < 0 || op > 2) return PQCGPU_EINVAL;
+    if (n <= 0) return PQCGPU_OK;
+    int variant, k;
+    if (kyber_alg(alg, &variant, &k)) {
+        if (op == 0) return kyber_keypair_dev(variant, k, n, out0, out1, in0, (int)ai.kpc, 1, scr, plain, s);
+        if (op == 1) return kyber_enc_dev(variant, k, n, out0, out1, in0, nullptr, in1, scr, 1, plain, s);
+        return kyber_dec_dev(variant, k, n, out0, in0, in1, scr, 1, plain, s);
+    }
+    if (plain) return PQCGPU_EUNSUPPORTED;
+    if (alg == PQCGPU_NEWHOPE1024) {
+        if (op == 0) return newhope_keypair_dev(n, out0, out1, in0, 32, s);
+        if (op == 1) return newhope_enc_dev(n, out0, out1, in0, nullptr, in1, scr, 1, s);
+        return newhope_dec_dev(n, out0, in0, in1, 1, s);
+    }
+    if (op == 0) return frodo_keypair_dev(n, out0, out1, in0, (int)ai.kpc, scr, s);
+    if (op == 1) return frodo_enc_dev(n, out0, out1, in0, in1, scr, s);
+    return frodo_dec_dev(n, out0, in0, in1, scr, s);
+}
+// Per-instance byte sizes of the op's buffers (in0, in1, out0, out1; 0 = unused).
+void op_io_sizes(int alg, int op, size_t sz[4]) {
+    AlgInfo ai{};
+    alg_info(alg, &ai);
+    if (op == 0) { sz[0] = ai.kpc; sz[1] = 0; sz[2] = ai.pk; sz[3] = ai.sk; }
+    else if (op == 1) { sz[0] = ai.pk; sz[1] = ai.encc; sz[2] = ai.ct; sz[3] = ai.ss; }
+    else { sz[0] = ai.ct; sz[1] = ai.sk; sz[2] = ai.ss; sz[3] = 0; }
+}
+}  // namespace pqc
+
+static int kem_op(pqcgpu_ctx *c, int alg, int op, size_t n, const uint8_t *in0, const uint8_t *in1, uint8_t *out0,
+                  uint8_t *out1, unsigned flags) {
+    AlgInfo ai;
+    if (!c || !alg_info(alg, &ai)) return set_err(PQCGPU_EINVAL, "bad context or algorithm");
+    const int plain = (flags & PQCGPU_PLAIN) ? 1 : 0;
+    int variant, k;
+    if (plain && !kyber_alg(alg, &variant, &k)) return set_err(PQCGPU_EUNSUPPORTED, "the plain path covers Kyber only");
+    size_t sz[4];
+    op_io_sizes(alg, op, sz);
+    OpDesc d;
+    const uint8_t *ins[2] = {in0, in1};
+    uint8_t *outs[2] = {out0, out1};
+    for (int i = 0; i < 2; i++)
+        if (sz[i]) {
+            d.in[d.nin] = ins[i];
+            d.in_sz[d.nin++] = sz[i];
+        }
+    for (int i = 0; i < 2; i++)
+        if (sz[2 + i]) {
+            d.out[d.nout] = outs[i];
+            d.out_sz[d.nout++] = sz[2 + i];
+        }
+    d.scratch_per = op_scratch_bytes(alg, op, plain);
+    return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
+        return op_dev(alg, op, m, in[0], d.nin > 1 ? in[1] : nullptr, out[0], d.nout > 1 ? out[1] : nullptr, scr, plain, s);
+    });
+}
+
 extern "C" int pqcgpu_kem_keypair_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uint8_t *pk, uint8_t *sk,
                                         const uint8_t *coins, unsigned flags) {
     AlgInfo ai;
@@ -434,54 +525,7 @@ extern "C" int pqcgpu_kem_keypair_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n,
     CoinsHolder h;
     int rc = coins_or_drbg(c, coins, n * ai.kpc, flags, h, nullptr, 0);
     if (rc) return rc;
-    int variant, k;
-    if (kyber_alg(alg, &variant, &k)) {
-        OpDesc d;
-        d.nin = 1;
-        d.in[0] = coins;
-        d.in_sz[0] = ai.kpc;
-        d.nout = 2;
-        d.out[0] = pk;
-        d.out_sz[0] = ai.pk;
-        d.out[1] = sk;
-        d.out_sz[1] = ai.sk;
-        const int plain = (flags & PQCGPU_PLAIN) ? 1 : 0;
-        d.scratch_per = kyber_scratch_bytes(k, 0, plain);
-        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
-            return kyber_keypair_dev(variant, k, m, out[0], out[1], in[0], (int)ai.kpc, 1, scr, plain, s);
-        });
-    }
-    if (flags & PQCGPU_PLAIN) return set_err(PQCGPU_EUNSUPPORTED, "the plain path covers Kyber only");
-    if (alg == PQCGPU_NEWHOPE1024) {
-        OpDesc d;
-        d.nin = 1;
-        d.in[0] = coins;
-        d.in_sz[0] = ai.kpc;
-        d.nout = 2;
-        d.out[0] = pk;
-        d.out_sz[0] = ai.pk;
-        d.out[1] = sk;
-        d.out_sz[1] = ai.sk;
-        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
-            return newhope_keypair_dev(m, out[0], out[1], in[0], 32, s);
-        });
-    }
-    if (alg == PQCGPU_FRODO976) {
-        OpDesc d;
-        d.nin = 1;
-        d.in[0] = coins;
-        d.in_sz[0] = ai.kpc;
-        d.nout = 2;
-        d.out[0] = pk;
-        d.out_sz[0] = ai.pk;
-        d.out[1] = sk;
-        d.out_sz[1] = ai.sk;
-        d.scratch_per = frodo_scratch_bytes();
-        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
-            return frodo_keypair_dev(m, out[0], out[1], in[0], (int)ai.kpc, scr, s);
-        });
-    }
-    return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
+    return kem_op(c, alg, 0, n, coins, nullptr, pk, sk, flags);
 }
 
 extern "C" int pqcgpu_kem_enc_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uint8_t *ct, uint8_t *ss,
@@ -491,115 +535,152 @@ extern "C" int pqcgpu_kem_enc_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uin
     CoinsHolder h;
     int rc = coins_or_drbg(c, coins, n * ai.encc, flags, h, nullptr, 0);
     if (rc) return rc;
-    int variant, k;
-    if (kyber_alg(alg, &variant, &k)) {
-        OpDesc d;
-        d.nin = 2;
-        d.in[0] = pk;
-        d.in_sz[0] = ai.pk;
-        d.in[1] = coins;
-        d.in_sz[1] = ai.encc;
-        d.nout = 2;
-        d.out[0] = ct;
-        d.out_sz[0] = ai.ct;
-        d.out[1] = ss;
-        d.out_sz[1] = ai.ss;
-        const int plain = (flags & PQCGPU_PLAIN) ? 1 : 0;
-        d.scratch_per = kyber_scratch_bytes(k, 1, plain);
-        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
-            return kyber_enc_dev(variant, k, m, out[0], out[1], in[0], nullptr, in[1], scr, 1, plain, s);
-        });
-    }
-    if (flags & PQCGPU_PLAIN) return set_err(PQCGPU_EUNSUPPORTED, "the plain path covers Kyber only");
-    if (alg == PQCGPU_NEWHOPE1024) {
-        OpDesc d;
-        d.nin = 2;
-        d.in[0] = pk;
-        d.in_sz[0] = ai.pk;
-        d.in[1] = coins;
-        d.in_sz[1] = ai.encc;
-        d.nout = 2;
-        d.out[0] = ct;
-        d.out_sz[0] = ai.ct;
-        d.out[1] = ss;
-        d.out_sz[1] = ai.ss;
-        d.scratch_per = 64;
-        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
-            return newhope_enc_dev(m, out[0], out[1], in[0], nullptr, in[1], scr, 1, s);
-        });
-    }
-    if (alg == PQCGPU_FRODO976) {
-        OpDesc d;
-        d.nin = 2;
-        d.in[0] = pk;
-        d.in_sz[0] = ai.pk;
-        d.in[1] = coins;
-        d.in_sz[1] = ai.encc;
-        d.nout = 2;
-        d.out[0] = ct;
-        d.out_sz[0] = ai.ct;
-        d.out[1] = ss;
-        d.out_sz[1] = ai.ss;
-        d.scratch_per = frodo_scratch_bytes();
-        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
-            return frodo_enc_dev(m, out[0], out[1], in[0], in[1], scr, s);
-        });
-    }
-    return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
+    return kem_op(c, alg, 1, n, pk, coins, ct, ss, flags);
 }
 
 extern "C" int pqcgpu_kem_dec_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uint8_t *ss, const uint8_t *ct,
                                     const uint8_t *sk, unsigned flags) {
-    AlgInfo ai;
-    if (!c || !alg_info(alg, &ai)) return set_err(PQCGPU_EINVAL, "bad context or algorithm");
+    return kem_op(c, alg, 2, n, ct, sk, ss, nullptr, flags);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Mixed batches and CUDA graphs
+// ---------------------------------------------------------------------------------------------
+static int check_jobs(const pqcgpu_job *jobs, size_t njobs, int plain, size_t *scratch_total, size_t *offs) {
+    if (!jobs && njobs) return set_err(PQCGPU_EINVAL, "jobs is NULL");
+    size_t tot = 0;
+    for (size_t i = 0; i < njobs; i++) {
+        AlgInfo ai;
+        const pqcgpu_job &j = jobs[i];
+        if (!alg_info(j.alg, &ai) || j.op < 0 || j.op > 2 || j.n > ((uint64_t)1 << 30))
+            return set_err(PQCGPU_EINVAL, "bad job (alg, op or n)");
+        size_t sz[4];
+        op_io_sizes(j.alg, j.op, sz);
+        const void *ptrs[4] = {j.in0, j.in1, j.out0, j.out1};
+        for (int q = 0; q < 4; q++) {
+            if (sz[q] && j.n && !ptrs[q]) return set_err(PQCGPU_EINVAL, "null buffer in a job");
+            if (sz[q] && ((uintptr_t)ptrs[q] & 15)) return set_err(PQCGPU_EINVAL, "device buffers must be 16-byte aligned");
+        }
+        if (offs) offs[i] = tot;
+        tot += (op_scratch_bytes(j.alg, j.op, plain) * j.n + 255) & ~(size_t)255;
+    }
+    *scratch_total = tot;
+    return PQCGPU_OK;
+}
+
+// Fork the jobs over the context's parallel streams after the work already on `main`, join back.
+static int launch_jobs(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, uint8_t *scratch, const size_t *offs,
+                       int plain, cudaStream_t main) {
+    int rc = cuda_err(cudaEventRecord(c->fork_ev, main), "event record");
+    if (rc) return rc;
+    const int used = (int)(njobs < (size_t)pqcgpu_ctx::NPAR ? njobs : pqcgpu_ctx::NPAR);
+    for (int i = 0; i < used; i++)
+        if ((rc = cuda_err(cudaStreamWaitEvent(c->par[i], c->fork_ev, 0), "wait event"))) return rc;
+    for (size_t i = 0; i < njobs; i++) {
+        const pqcgpu_job &j = jobs[i];
+        rc = op_dev(j.alg, j.op, (int)j.n, j.in0, j.in1, j.out0, j.out1, scratch + offs[i], plain,
+                    c->par[i % pqcgpu_ctx::NPAR]);
+        if (rc) return set_err(rc, "job launch failed");
+    }
+    for (int i = 0; i < used; i++) {
+        if ((rc = cuda_err(cudaEventRecord(c->join_ev[i], c->par[i]), "event record"))) return rc;
+        if ((rc = cuda_err(cudaStreamWaitEvent(main, c->join_ev[i], 0), "wait event"))) return rc;
+    }
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_kem_mixed_batch(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, unsigned flags) {
+    if (!c) return set_err(PQCGPU_EINVAL, "bad context");
+    if (!(flags & PQCGPU_DEVICE_PTRS)) return set_err(PQCGPU_EINVAL, "mixed batches take device pointers");
+    const int plain = (flags & PQCGPU_PLAIN) ? 1 : 0;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    int rc = cuda_err(cudaSetDevice(c->device), "cudaSetDevice");
+    if (rc) return rc;
+    std::vector<size_t> offs(njobs + 1);
+    size_t tot = 0;
+    if ((rc = check_jobs(jobs, njobs, plain, &tot, offs.data()))) return rc;
+    if ((rc = c->reserve(tot + 256))) return rc;
+    return launch_jobs(c, jobs, njobs, c->arena, offs.data(), plain, c->stream);
+}
+
+struct pqcgpu_graph {
+    pqcgpu_ctx *ctx = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint8_t *scratch = nullptr;
+};
+
+extern "C" int pqcgpu_graph_capture(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, unsigned flags,
+                                    pqcgpu_graph **out) {
+    if (!c || !out) return set_err(PQCGPU_EINVAL, "bad context or output");
+    *out = nullptr;
+    if (!(flags & PQCGPU_DEVICE_PTRS)) return set_err(PQCGPU_EINVAL, "graphs take device pointers");
+    const int plain = (flags & PQCGPU_PLAIN) ? 1 : 0;
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    int rc = cuda_err(cudaSetDevice(c->device), "cudaSetDevice");
+    if (rc) return rc;
+    std::vector<size_t> offs(njobs + 1);
+    size_t tot = 0;
+    if ((rc = check_jobs(jobs, njobs, plain, &tot, offs.data()))) return rc;
+    pqcgpu_graph *g = new pqcgpu_graph();
+    g->ctx = c;
+    if (cudaMalloc(&g->scratch, tot + 256) != cudaSuccess) {
+        cudaGetLastError();
+        delete g;
+        return set_err(PQCGPU_ENOMEM, "graph scratch allocation failed");
+    }
+    // one uncaptured pass: loads the kernels and sets their shared-memory attributes
+    rc = launch_jobs(c, jobs, njobs, g->scratch, offs.data(), plain, c->stream);
+    if (!rc) rc = cuda_err(cudaStreamSynchronize(c->stream), "warm-up");
+    if (!rc) {
+        set_capturing(true);
+        rc = cuda_err(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        if (!rc) {
+            const int lrc = launch_jobs(c, jobs, njobs, g->scratch, offs.data(), plain, c->stream);
+            const int erc = cuda_err(cudaStreamEndCapture(c->stream, &g->graph), "end capture");
+            rc = lrc ? lrc : erc;
+        }
+        set_capturing(false);
+    }
+    if (!rc) rc = cuda_err(cudaGraphInstantiate(&g->exec, g->graph, 0), "graph instantiate");
+    if (rc) {
+        if (g->graph) cudaGraphDestroy(g->graph);
+        cudaFree(g->scratch);
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return PQCGPU_OK;
+}
+extern "C" int pqcgpu_graph_launch(pqcgpu_graph *g) {
+    if (!g) return set_err(PQCGPU_EINVAL, "null graph");
+    std::lock_guard<std::recursive_mutex> lk(g->ctx->mu);
+    return cuda_err(cudaGraphLaunch(g->exec, g->ctx->stream), "graph launch");
+}
+extern "C" int pqcgpu_graph_destroy(pqcgpu_graph *g) {
+    if (!g) return PQCGPU_EINVAL;
+    cudaStreamSynchronize(g->ctx->stream);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    if (g->scratch) cudaFree(g->scratch);
+    delete g;
+    return PQCGPU_OK;
+}
+
+// ---- launch shapes (autotuner) ----
+extern "C" int pqcgpu_set_launch_shape(pqcgpu_alg alg, int op, int ni, int threads) {
+    int variant, k, rc;
+    if (kyber_alg(alg, &variant, &k)) rc = kyber_set_shape(op, k, ni, threads);
+    else if (alg == PQCGPU_NEWHOPE1024) rc = newhope_set_shape(op, ni, threads);
+    else rc = PQCGPU_EUNSUPPORTED;
+    return rc ? set_err(rc, "launch shape not accepted") : PQCGPU_OK;
+}
+extern "C" int pqcgpu_get_launch_shape(pqcgpu_alg alg, int op, int *ni, int *threads) {
     int variant, k;
-    if (kyber_alg(alg, &variant, &k)) {
-        OpDesc d;
-        d.nin = 2;
-        d.in[0] = ct;
-        d.in_sz[0] = ai.ct;
-        d.in[1] = sk;
-        d.in_sz[1] = ai.sk;
-        d.nout = 1;
-        d.out[0] = ss;
-        d.out_sz[0] = ai.ss;
-        const int plain = (flags & PQCGPU_PLAIN) ? 1 : 0;
-        d.scratch_per = kyber_scratch_bytes(k, 2, plain);
-        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
-            return kyber_dec_dev(variant, k, m, out[0], in[0], in[1], scr, 1, plain, s);
-        });
-    }
-    if (flags & PQCGPU_PLAIN) return set_err(PQCGPU_EUNSUPPORTED, "the plain path covers Kyber only");
-    if (alg == PQCGPU_NEWHOPE1024) {
-        OpDesc d;
-        d.nin = 2;
-        d.in[0] = ct;
-        d.in_sz[0] = ai.ct;
-        d.in[1] = sk;
-        d.in_sz[1] = ai.sk;
-        d.nout = 1;
-        d.out[0] = ss;
-        d.out_sz[0] = ai.ss;
-        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
-            return newhope_dec_dev(m, out[0], in[0], in[1], 1, s);
-        });
-    }
-    if (alg == PQCGPU_FRODO976) {
-        OpDesc d;
-        d.nin = 2;
-        d.in[0] = ct;
-        d.in_sz[0] = ai.ct;
-        d.in[1] = sk;
-        d.in_sz[1] = ai.sk;
-        d.nout = 1;
-        d.out[0] = ss;
-        d.out_sz[0] = ai.ss;
-        d.scratch_per = frodo_scratch_bytes();
-        return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *scr, cudaStream_t s) {
-            return frodo_dec_dev(m, out[0], in[0], in[1], scr, s);
-        });
-    }
-    return set_err(PQCGPU_EUNSUPPORTED, "algorithm not built yet");
+    if (!ni || !threads) return set_err(PQCGPU_EINVAL, "null output");
+    if (kyber_alg(alg, &variant, &k)) return kyber_get_shape(op, k, ni, threads);
+    if (alg == PQCGPU_NEWHOPE1024) return newhope_get_shape(op, ni, threads);
+    return set_err(PQCGPU_EUNSUPPORTED, "no tunable launch shape for this algorithm");
 }
 
 // ---- CPA level ----
@@ -659,15 +740,6 @@ extern "C" int pqcgpu_kyber_indcpa_dec_batch(pqcgpu_ctx *c, int variant, int k, 
     return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
         return kyber_dec_dev(variant, k, m, out[0], in[0], in[1], nullptr, 0, 0, s);
     });
-}
-
-extern "C" int pqcgpu_kyber_set_shape(int op, int k, int ni, int threads) {
-    const int rc = kyber_set_shape(op, k, ni, threads);
-    return rc ? set_err(rc, "bad launch shape") : PQCGPU_OK;
-}
-extern "C" int pqcgpu_kyber_get_shape(int op, int k, int *ni, int *threads) {
-    if (!ni || !threads) return set_err(PQCGPU_EINVAL, "null output");
-    return kyber_get_shape(op, k, ni, threads);
 }
 
 extern "C" int pqcgpu_profile_enable(int on) {

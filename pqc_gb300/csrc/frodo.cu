@@ -486,7 +486,8 @@ int frodo_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int
 int frodo_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
                   cudaStream_t st) {
     const size_t sm = sa_smem(SA_THREADS);
-    if (cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+    if (!capturing() &&
+        cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return PQCGPU_ECUDA;
     PQC_LAUNCH(st, "fr_enc_pre", 976, 0, fr_enc_pre<<<(n + 15) / 16, 16, 0, st>>>(n, pk, mu, scratch));
     PQC_LAUNCH(st, "fr_sa_core", 976, 0, fr_sa_core<<<n, SA_THREADS, sm, st>>>(n, ct, nullptr, pk, PKB, scratch));
@@ -496,7 +497,8 @@ int frodo_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint
 
 int frodo_dec_dev(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, cudaStream_t st) {
     const size_t sm = sa_smem(SA_THREADS);
-    if (cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+    if (!capturing() &&
+        cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return PQCGPU_ECUDA;
     PQC_LAUNCH(st, "fr_dec_w", 976, 0, fr_dec_w<<<n, 256, 0, st>>>(n, ct, sk, scratch));
     PQC_LAUNCH(st, "fr_dec_pre", 976, 0, fr_dec_pre<<<(n + 15) / 16, 16, 0, st>>>(n, sk, scratch));

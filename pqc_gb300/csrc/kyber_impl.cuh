@@ -809,6 +809,7 @@ extern int g_threads[3][3];  // [op][k-2]: threads per CTA (kyber.cu)
 
 template <class Kern>
 static cudaError_t ensure_smem(Kern kern, size_t bytes) {
+    if (capturing()) return cudaSuccess;  // set by the uncaptured warm-up pass
     return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 

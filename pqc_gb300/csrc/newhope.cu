@@ -471,6 +471,7 @@ static int g_shape[3][2] = {{4, 128}, {4, 128}, {8, 256}};  // [op] = {instances
 
 template <class Kern>
 static int prep(Kern k, size_t sm) {
+    if (capturing()) return PQCGPU_OK;
     return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess ? PQCGPU_OK
                                                                                                        : PQCGPU_ECUDA;
 }
@@ -510,6 +511,13 @@ int newhope_set_shape(int op, int ni, int threads) {
     if (op < 0 || op > 2 || ni < 1 || ni > 64 || threads < 32 || threads > 256 || threads % 32) return PQCGPU_EINVAL;
     g_shape[op][0] = ni;
     g_shape[op][1] = threads;
+    return PQCGPU_OK;
+}
+
+int newhope_get_shape(int op, int *ni, int *threads) {
+    if (op < 0 || op > 2) return PQCGPU_EINVAL;
+    *ni = g_shape[op][0];
+    *threads = g_shape[op][1];
     return PQCGPU_OK;
 }
 

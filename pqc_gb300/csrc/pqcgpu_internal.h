@@ -14,6 +14,10 @@ namespace pqc {
 extern std::atomic<uint64_t> g_launch_count;
 
 // Launch profiler (probe.cu): CUDA events around each launch on its stream when enabled.
+// Set while a CUDA graph is being captured on this host thread: launch helpers then skip the
+// profiler and attribute calls (both were done by the uncaptured warm-up pass).
+void set_capturing(bool on);
+bool capturing();
 bool prof_enabled();
 void *prof_begin(cudaStream_t st, const char *name, int k, int v);
 void prof_end(cudaStream_t st, void *tok);
@@ -29,6 +33,13 @@ int probe_peaks(int device, double *int_ops, double *keccak_perms);
         if (pqc_tok_) ::pqc::prof_end(st, pqc_tok_);                         \
         ::pqc::g_launch_count++;                                             \
     } while (0)
+
+// One device KEM operation (capi.cu): op 0 keypair (in0 coins -> out0 pk, out1 sk), 1 encaps (in0 pk,
+// in1 coins -> out0 ct, out1 ss), 2 decaps (in0 ct, in1 sk -> out0 ss); device pointers.
+int op_dev(int alg, int op, int n, const uint8_t *in0, const uint8_t *in1, uint8_t *out0, uint8_t *out1,
+           uint8_t *scr, int plain, cudaStream_t s);
+size_t op_scratch_bytes(int alg, int op, int plain);
+void op_io_sizes(int alg, int op, size_t sz[4]);
 
 // Once-per-device set-up (constant tables) and the thread-local error text (capi.cu).
 int device_ready(int device);
@@ -54,6 +65,7 @@ int kyber_dec_dev(int variant, int k, int n, uint8_t *out, const uint8_t *ct, co
 // ---- NewHope-1024 (newhope.cu) ----
 int newhope_init_constants();
 int newhope_set_shape(int op, int ni, int threads);
+int newhope_get_shape(int op, int *ni, int *threads);
 int newhope_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st);
 // kem=1: coins 32 B/instance, scratch >= 64 B/instance, ss written; kem=0: CPA with m and coins
 int newhope_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,

@@ -108,7 +108,10 @@ std::vector<Rec> g_recs;
 bool g_prof_on = false;
 }  // namespace
 
-bool prof_enabled() { return g_prof_on; }
+static thread_local bool g_capturing = false;
+void set_capturing(bool on) { g_capturing = on; }
+bool capturing() { return g_capturing; }
+bool prof_enabled() { return g_prof_on && !g_capturing; }
 void *prof_begin(cudaStream_t st, const char *name, int k, int v) {
     Rec *r = new Rec();
     char buf[96];

@@ -29,8 +29,42 @@ def kyber_cpa_sizes(variant, k):
     return {"pk": 384 * k + 32, "sk": 384 * k, "ct": k * du * 32 + dv * 32}
 
 
+OPS = {"keypair": 0, "enc": 1, "dec": 2}
+
+
 def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def make_jobs(jobs):
+    """jobs: iterable of (alg, op, n, in0, in1, out0, out1) with torch CUDA tensors (or None)."""
+    arr = (_lib.Job * len(jobs))()
+    for i, (alg, op, n, in0, in1, out0, out1) in enumerate(jobs):
+        arr[i].alg = alg_id(alg)
+        arr[i].op = OPS[op] if isinstance(op, str) else int(op)
+        arr[i].n = n
+        for name, t in (("in0", in0), ("in1", in1), ("out0", out0), ("out1", out1)):
+            setattr(arr[i], name, t.data_ptr() if t is not None else None)
+    return arr
+
+
+class Graph:
+    """A captured mixed job list (pqcgpu_graph_capture); launch() replays it on the context stream."""
+
+    def __init__(self, ctx, jobs, flags=0):
+        self.ctx = ctx
+        self.arr = make_jobs(jobs)
+        h = ctypes.c_void_p()
+        _lib.check(ctx.lib.pqcgpu_graph_capture(ctx.h, self.arr, len(jobs), flags | DEVICE_PTRS, ctypes.byref(h)))
+        self.h = h
+
+    def launch(self):
+        _lib.check(self.ctx.lib.pqcgpu_graph_launch(self.h))
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.pqcgpu_graph_destroy(self.h)
+            self.h = None
 
 
 class Context:
@@ -132,6 +166,14 @@ class Context:
     def dec_dev(self, alg, n, ss, ct, sk, flags=0):
         _lib.check(self.lib.pqcgpu_kem_dec_batch(self.h, alg_id(alg), n, _ptr(ss), _ptr(ct), _ptr(sk),
                                                  flags | DEVICE_PTRS))
+
+    def mixed_dev(self, jobs, flags=0):
+        """Run a list of (alg, op, n, in0, in1, out0, out1) jobs at once (device tensors, async)."""
+        arr = make_jobs(jobs)
+        _lib.check(self.lib.pqcgpu_kem_mixed_batch(self.h, arr, len(jobs), flags | DEVICE_PTRS))
+
+    def graph(self, jobs, flags=0):
+        return Graph(self, jobs, flags)
 
     # host-pointer call on raw addresses (pinned torch tensors), synchronous
     def enc_host_ptrs(self, alg, n, ct, ss, pk, coins, flags=0):
