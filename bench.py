@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--path", default="fused", choices=["fused", "plain"])
     p.add_argument("--no-plain", action="store_true", help="skip timing the plain path beside the fused one")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--config", default=None,
+                   choices=["kyber512", "newhope1024", "frodo976", "mixed", "serving", "all"],
+                   help="measure another configuration (extra JSON lines) instead of the headline")
     return p.parse_args()
 
 
@@ -194,10 +197,119 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_configs(args):
+    """Secondary configurations, one JSON line each (not the headline metric)."""
+    import torch
+    from pqc_gb300 import drbg, kem
+    dev = torch.device("cuda", 0)
+    ctx = kem.Context(0)
+    st = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
+    which = ["kyber512", "newhope1024", "frodo976", "mixed", "serving"] if args.config == "all" else [args.config]
+
+    def timed(fn, reps):
+        fn()
+        ctx.wait()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    for cfg in which:
+        if cfg in ("kyber512", "newhope1024", "frodo976"):
+            alg = cfg
+            n = {"kyber512": 65536, "newhope1024": 16384, "frodo976": 2048}[cfg]
+            s = kem.sizes(alg)
+            seed = drbg.seed48(5)
+            kc, ec = up(drbg.stream(seed, b"kp", n * s["kp_coins"])), up(drbg.stream(seed, b"enc", n * s["enc_coins"]))
+            pk, sk, ct = (torch.empty(n * s[x], dtype=torch.uint8, device=dev) for x in ("pk", "sk", "ct"))
+            ss, ss2 = (torch.empty(n * s["ss"], dtype=torch.uint8, device=dev) for _ in range(2))
+            torch.cuda.synchronize()
+            reps = 3 if alg == "frodo976" else 10
+            tk = timed(lambda: ctx.keypair_dev(alg, n, pk, sk, kc), reps)
+            te = timed(lambda: ctx.enc_dev(alg, n, ct, ss, pk, ec), reps)
+            td = timed(lambda: ctx.dec_dev(alg, n, ss2, ct, sk), reps)
+            ctx.wait()
+            print(json.dumps({"config": cfg, "batch": n, "metric": "%s ops/s per operation (device-resident)" % alg,
+                              "keypair_per_s": n / tk * 1e3, "enc_per_s": n / te * 1e3, "dec_per_s": n / td * 1e3,
+                              "keypair_enc_dec_chains_per_s": n / (tk + te + td) * 1e3,
+                              "bit_exact_roundtrip": bool(torch.equal(ss, ss2))}), flush=True)
+        elif cfg == "mixed":
+            import random
+            rng = random.Random(12)
+            jobs, total = [], 0
+            keep = []
+            for j in range(24):
+                alg = rng.choices(["kyber512", "kyber768", "kyber1024"], [0.4, 0.4, 0.2])[0]
+                op = rng.choice(["keypair", "enc", "dec"])
+                n = rng.randint(1, 65536)
+                s = kem.sizes(alg)
+                seed = drbg.seed48(200 + j)
+                kc = up(drbg.stream(seed, b"kp", n * s["kp_coins"]))
+                pk, sk = (torch.empty(n * s[x], dtype=torch.uint8, device=dev) for x in ("pk", "sk"))
+                ctx.keypair_dev(alg, n, pk, sk, kc)
+                if op == "keypair":
+                    jobs.append((alg, op, n, kc, None, torch.empty_like(pk), torch.empty_like(sk)))
+                else:
+                    ec = up(drbg.stream(seed, b"enc", n * s["enc_coins"]))
+                    ct = torch.empty(n * s["ct"], dtype=torch.uint8, device=dev)
+                    ss = torch.empty(n * s["ss"], dtype=torch.uint8, device=dev)
+                    ctx.enc_dev(alg, n, ct, ss, pk, ec)
+                    if op == "enc":
+                        jobs.append((alg, op, n, pk, ec, torch.empty_like(ct), torch.empty_like(ss)))
+                    else:
+                        jobs.append((alg, op, n, ct, sk, torch.empty_like(ss), None))
+                        keep.append((len(jobs) - 1, ss))
+                total += n
+            ctx.wait()
+            t_mixed = timed(lambda: ctx.mixed_dev(jobs), 3)
+            ok = all(torch.equal(jobs[i][5], ss) for i, ss in keep)
+            g = ctx.graph(jobs)
+            t_graph = timed(g.launch, 3)
+            ok = ok and all(torch.equal(jobs[i][5], ss) for i, ss in keep)
+            g.close()
+            def sequential():
+                for alg, op, n, in0, in1, out0, out1 in jobs:
+                    if op == "keypair":
+                        ctx.keypair_dev(alg, n, out0, out1, in0)
+                    elif op == "enc":
+                        ctx.enc_dev(alg, n, out0, out1, in0, in1)
+                    else:
+                        ctx.dec_dev(alg, n, out0, in0, in1)
+
+            t_seq = timed(sequential, 3)
+            print(json.dumps({"config": "mixed", "metric": "mixed Kyber batch ops/s", "jobs": len(jobs),
+                              "instances": total, "mixed_batch_per_s": total / t_mixed * 1e3,
+                              "graph_replay_per_s": total / t_graph * 1e3, "sequential_per_s": total / t_seq * 1e3,
+                              "mix": "k=2/3/4 at 40/40/20, n ~ U{1..65536}, ops 1/3 each",
+                              "bit_exact_decaps": bool(ok)}), flush=True)
+        elif cfg == "serving":
+            from pqc_gb300 import serve
+            with serve.Server(0, budget=16 << 30, max_inflight=8, max_batch=4096) as srv:
+                sat = srv.run_poisson(serve.SERVING_MIX, rate=2e6, seconds=1.0, seed=1)
+                peak = sat["achieved_per_s"]
+                points = []
+                for frac in (0.1, 0.3, 0.5, 0.7, 0.9):
+                    r = srv.run_poisson(serve.SERVING_MIX, rate=frac * peak, seconds=1.5, seed=int(frac * 100))
+                    points.append({"load": frac, "offered_per_s": r["offered_per_s"], "achieved_per_s": r["achieved_per_s"],
+                                   "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "max_ms": r["max_ms"],
+                                   "batches": r["batches"]})
+            print(json.dumps({"config": "serving", "metric": "KEM serving latency under Poisson load",
+                              "mix": "60% Kyber-512/768/1024, 20% NewHope-1024, 20% FrodoKEM-976, ops equiprobable",
+                              "keys": "resident on the device", "hbm_budget_gb": 16,
+                              "measured_peak_per_s": peak, "points": points}), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config:
+        return run_configs(args)
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)

@@ -155,6 +155,55 @@ int pqcgpu_graph_capture(pqcgpu_ctx *ctx, const pqcgpu_job *jobs, size_t njobs, 
 int pqcgpu_graph_launch(pqcgpu_graph *graph);
 int pqcgpu_graph_destroy(pqcgpu_graph *graph);
 
+/* ---- serving loop ----------------------------------------------------------------------------
+ * A server owns a dispatcher thread that batches individual requests continuously: whenever one of
+ * its max_inflight slots (stream + staging buffers) is free it takes up to max_batch waiting
+ * requests of the oldest request's (algorithm, operation), runs them as one GPU batch on that
+ * slot's stream, and completes each request when its batch finishes, so requests arriving while
+ * others are on the GPU join the next batch and overlap with them.  Keys stay on the device: a
+ * KEYPAIR request stores pk / sk in the server's key store and returns a handle; ENC / DEC use the
+ * handle (ENC may pass pk bytes instead).  Device memory (key stores + staging) is admitted against
+ * hbm_budget_bytes (0 = 16 GiB); a request that cannot fit while nothing else is in flight fails
+ * with PQCGPU_EBUDGET.  Buffers of a request (host memory) must stay valid until it completes.
+ * Results are byte-identical to the batched entry points for the same inputs. */
+typedef struct pqcgpu_server pqcgpu_server;
+typedef struct {
+    int32_t alg;        /* pqcgpu_alg */
+    int32_t op;         /* PQCGPU_OP_* */
+    uint64_t key;       /* ENC / DEC: key handle (ENC: 0 = use pk) */
+    const uint8_t *pk;  /* ENC without a handle: public key */
+    const uint8_t *in;  /* KEYPAIR / ENC: coins (NULL = library DRBG); DEC: ciphertext */
+    uint8_t *out0;      /* KEYPAIR: pk (may be NULL); ENC: ct; DEC: ss */
+    uint8_t *out1;      /* ENC: ss */
+    uint64_t *key_out;  /* KEYPAIR: receives the key handle (may be NULL) */
+} pqcgpu_request;
+typedef struct {
+    uint64_t completed, batches, keys_resident;
+    size_t hbm_used;
+    double p50_ms, p99_ms, mean_ms, max_ms; /* submit-to-completion latency of completed requests */
+} pqcgpu_server_stats;
+typedef struct {
+    int32_t alg, op;
+    double weight;
+} pqcgpu_mix_entry;
+typedef struct {
+    double offered_per_s, achieved_per_s, seconds, submit_seconds, p50_ms, p99_ms, mean_ms, max_ms;
+    uint64_t submitted, completed, batches;
+} pqcgpu_load_report;
+int pqcgpu_server_create(pqcgpu_server **out, int device, size_t hbm_budget_bytes, int max_inflight, int max_batch);
+int pqcgpu_server_submit(pqcgpu_server *server, const pqcgpu_request *req, uint64_t *ticket);
+/* 0 when done, a negative status if the request failed, PQCGPU_ETIMEOUT (timeout_ms < 0: wait forever) */
+int pqcgpu_server_wait(pqcgpu_server *server, uint64_t ticket, int timeout_ms);
+int pqcgpu_server_drain(pqcgpu_server *server);
+int pqcgpu_server_get_stats(pqcgpu_server *server, pqcgpu_server_stats *out, int reset);
+int pqcgpu_server_key_release(pqcgpu_server *server, uint64_t key);
+int pqcgpu_server_destroy(pqcgpu_server *server);
+/* Open-loop load for the serving benchmark: resident key / ciphertext pools per algorithm of the
+ * mix are prepared first, then requests drawn from the weighted (alg, op) mix are submitted at
+ * Poisson arrival times at rate_per_s for `seconds`, and the server is drained. */
+int pqcgpu_server_run_poisson(pqcgpu_server *server, const pqcgpu_mix_entry *mix, size_t nmix, double rate_per_s,
+                              double seconds, uint64_t seed, pqcgpu_load_report *out);
+
 /* ---- launch-shape tuning (used by the autotuner, pqc_gb300/autotune.py) --------------------
  * Core-kernel launch shape per (algorithm, operation): ni = instances per CTA, threads per CTA
  * (multiple of 32).  Kyber: ni 1..128, threads 32..512 (shared by the round-2 and round-3 sets of

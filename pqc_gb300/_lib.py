@@ -35,6 +35,14 @@ SIGNATURES = {
     "pqcgpu_graph_capture": (_int, [_vp, _vp, _sz, _uint, _c.POINTER(_vp)]),
     "pqcgpu_graph_launch": (_int, [_vp]),
     "pqcgpu_graph_destroy": (_int, [_vp]),
+    "pqcgpu_server_create": (_int, [_c.POINTER(_vp), _int, _sz, _int, _int]),
+    "pqcgpu_server_submit": (_int, [_vp, _vp, _c.POINTER(_c.c_uint64)]),
+    "pqcgpu_server_wait": (_int, [_vp, _c.c_uint64, _int]),
+    "pqcgpu_server_drain": (_int, [_vp]),
+    "pqcgpu_server_get_stats": (_int, [_vp, _vp, _int]),
+    "pqcgpu_server_key_release": (_int, [_vp, _c.c_uint64]),
+    "pqcgpu_server_destroy": (_int, [_vp]),
+    "pqcgpu_server_run_poisson": (_int, [_vp, _vp, _sz, _c.c_double, _c.c_double, _c.c_uint64, _vp]),
     "pqcgpu_set_launch_shape": (_int, [_int, _int, _int, _int]),
     "pqcgpu_get_launch_shape": (_int, [_int, _int, _c.POINTER(_int), _c.POINTER(_int)]),
     "pqcgpu_profile_enable": (_int, [_int]),
@@ -54,6 +62,29 @@ class Job(_c.Structure):
     """pqcgpu_job of include/pqcgpu.h."""
     _fields_ = [("alg", _c.c_int32), ("op", _c.c_int32), ("n", _c.c_uint64), ("in0", _c.c_void_p),
                 ("in1", _c.c_void_p), ("out0", _c.c_void_p), ("out1", _c.c_void_p)]
+
+
+class Request(_c.Structure):
+    """pqcgpu_request of include/pqcgpu.h."""
+    _fields_ = [("alg", _c.c_int32), ("op", _c.c_int32), ("key", _c.c_uint64), ("pk", _c.c_void_p),
+                ("in_", _c.c_void_p), ("out0", _c.c_void_p), ("out1", _c.c_void_p), ("key_out", _c.c_void_p)]
+
+
+class ServerStats(_c.Structure):
+    _fields_ = [("completed", _c.c_uint64), ("batches", _c.c_uint64), ("keys_resident", _c.c_uint64),
+                ("hbm_used", _c.c_size_t), ("p50_ms", _c.c_double), ("p99_ms", _c.c_double),
+                ("mean_ms", _c.c_double), ("max_ms", _c.c_double)]
+
+
+class MixEntry(_c.Structure):
+    _fields_ = [("alg", _c.c_int32), ("op", _c.c_int32), ("weight", _c.c_double)]
+
+
+class LoadReport(_c.Structure):
+    _fields_ = [("offered_per_s", _c.c_double), ("achieved_per_s", _c.c_double), ("seconds", _c.c_double),
+                ("submit_seconds", _c.c_double), ("p50_ms", _c.c_double), ("p99_ms", _c.c_double),
+                ("mean_ms", _c.c_double), ("max_ms", _c.c_double), ("submitted", _c.c_uint64),
+                ("completed", _c.c_uint64), ("batches", _c.c_uint64)]
 
 
 _lib = None

@@ -1,0 +1,646 @@
+// Serving loop: continuous batching of mixed KEM requests with device-resident keys.
+//
+// The reference has no serving path: its drivers run one fixed-size batch at a time from main()
+// (Kyber_GPU_Batched/main.cu:371-503).  Here a dispatcher thread turns a stream of individual
+// requests (keypair / encapsulation / decapsulation, any algorithm) into GPU batches:
+//   * requests queue up; whenever an in-flight slot (a stream + staging buffers) is free, the
+//     dispatcher takes the (algorithm, operation) group of the oldest waiting request, up to
+//     max_batch requests of it, packs their inputs into pinned memory, copies them up, runs the
+//     batched kernels and copies the results back -- all on the slot's stream;
+//   * up to max_inflight batches run at once, so requests that arrive while others are on the GPU
+//     are admitted as soon as a slot is free and overlap with them on the device;
+//   * keys live on the device: a keypair stores pk / sk in a per-algorithm key store and returns a
+//     handle; encapsulation / decapsulation by handle gather the keys on the device;
+//   * admission is by device-memory budget: the key stores and the slots' buffers together stay
+//     within the budget given at creation (a batch is cut short, or waits, when it would not fit).
+// Results are identical to the batched entry points: every instance of a batch is independent,
+// so a request's bytes do not depend on what it was batched with.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <random>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "pqcgpu_internal.h"
+
+namespace pqc {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+// copy rows of `row` bytes (multiple of 16): dst[i] = src[idx[i]] (gather) or dst[idx[i]] = src[i]
+__global__ void rows_gather(uint4 *dst, const uint4 *src, const uint32_t *idx, int n, int row16) {
+    const int r = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (r >= n) return;
+    const uint4 *s = src + (size_t)idx[r] * row16;
+    uint4 *d = dst + (size_t)r * row16;
+    for (int i = threadIdx.x & 31; i < row16; i += 32) d[i] = s[i];
+}
+__global__ void rows_scatter(uint4 *dst, const uint4 *src, const uint32_t *idx, int n, int row16) {
+    const int r = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (r >= n) return;
+    const uint4 *s = src + (size_t)r * row16;
+    uint4 *d = dst + (size_t)idx[r] * row16;
+    for (int i = threadIdx.x & 31; i < row16; i += 32) d[i] = s[i];
+}
+void launch_rows(bool gather, uint8_t *dst, const uint8_t *src, const uint32_t *idx, int n, size_t row, cudaStream_t st) {
+    if (n <= 0) return;
+    const dim3 grid(1, (n + 7) / 8);
+    if (gather)
+        PQC_LAUNCH(st, "rows_gather", 0, 0,
+                   rows_gather<<<grid, 256, 0, st>>>((uint4 *)dst, (const uint4 *)src, idx, n, (int)(row / 16)));
+    else
+        PQC_LAUNCH(st, "rows_scatter", 0, 0,
+                   rows_scatter<<<grid, 256, 0, st>>>((uint4 *)dst, (const uint4 *)src, idx, n, (int)(row / 16)));
+}
+
+struct Req {
+    pqcgpu_request r;
+    uint64_t ticket;
+    Clock::time_point t0;
+    int status = 1;  // 1 pending, 0 done, < 0 error
+    uint32_t key_slot = 0;
+};
+
+struct KeyStore {
+    size_t pkb = 0, skb = 0;
+    uint8_t *dpk = nullptr, *dsk = nullptr;
+    uint32_t cap = 0;
+    std::vector<uint32_t> free_slots;
+    std::vector<uint8_t> used;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    uint8_t *dbuf = nullptr;  // device staging
+    size_t dcap = 0;
+    uint8_t *hbuf = nullptr;  // pinned host staging
+    size_t hcap = 0;
+    bool busy = false;
+    int alg = 0, op = 0, n = 0;
+    std::vector<Req *> reqs;
+    size_t off_in0 = 0, off_in1 = 0, off_out0 = 0, off_out1 = 0, off_idx = 0, off_scr = 0;
+    size_t h_in0 = 0, h_in1 = 0, h_out0 = 0, h_out1 = 0, h_idx = 0;
+};
+
+size_t r256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+}  // namespace pqc
+
+using namespace pqc;
+
+struct pqcgpu_server {
+    int device = 0;
+    size_t budget = 0, used = 0;
+    int max_inflight = 4, max_batch = 4096;
+    std::vector<Slot> slots;
+    KeyStore ks[PQCGPU_NUM_ALGS];
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Req *> queue;
+    std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
+    uint64_t next_ticket = 1;
+    bool stop = false;
+    std::thread th;
+    std::vector<double> lat_ms;
+    uint64_t completed = 0, batches = 0;
+    std::string error;
+
+    int alloc_dev(uint8_t **p, size_t bytes) {
+        if (used + bytes > budget) return PQCGPU_EBUDGET;
+        if (cudaMalloc(p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return PQCGPU_ENOMEM;
+        }
+        used += bytes;
+        return PQCGPU_OK;
+    }
+    void free_dev(uint8_t *p, size_t bytes) {
+        if (p) {
+            cudaFree(p);
+            used -= bytes;
+        }
+    }
+    // grow the key store of `alg` to at least `need` slots (called by the dispatcher only)
+    int grow_keys(int alg, uint32_t need) {
+        KeyStore &k = ks[alg];
+        if (need <= k.cap) return PQCGPU_OK;
+        uint32_t cap = std::max<uint32_t>(need, std::max<uint32_t>(1024, k.cap * 2));
+        uint8_t *npk = nullptr, *nsk = nullptr;
+        int rc = alloc_dev(&npk, (size_t)cap * k.pkb);
+        if (rc) return rc;
+        if ((rc = alloc_dev(&nsk, (size_t)cap * k.skb))) {
+            free_dev(npk, (size_t)cap * k.pkb);
+            return rc;
+        }
+        if (k.cap) {
+            cudaDeviceSynchronize();
+            cudaMemcpy(npk, k.dpk, (size_t)k.cap * k.pkb, cudaMemcpyDeviceToDevice);
+            cudaMemcpy(nsk, k.dsk, (size_t)k.cap * k.skb, cudaMemcpyDeviceToDevice);
+            free_dev(k.dpk, (size_t)k.cap * k.pkb);
+            free_dev(k.dsk, (size_t)k.cap * k.skb);
+        }
+        for (uint32_t i = cap; i > k.cap; i--) k.free_slots.push_back(i - 1);
+        k.used.resize(cap, 0);
+        k.dpk = npk;
+        k.dsk = nsk;
+        k.cap = cap;
+        return PQCGPU_OK;
+    }
+    bool key_ok(uint64_t h, int alg, uint32_t *slot) {
+        if ((int)(h >> 48) != alg) return false;
+        const uint64_t s = (h & 0xffffffffffffull);
+        if (s == 0 || s > ks[alg].cap || !ks[alg].used[s - 1]) return false;
+        *slot = (uint32_t)(s - 1);
+        return true;
+    }
+
+    void finish(Req *q, int status, double ms) {
+        q->status = status;
+        if (status == 0) {
+            lat_ms.push_back(ms);
+            completed++;
+        }
+    }
+
+    // Reap finished batches: scatter results to the requests' host buffers.
+    void reap(std::unique_lock<std::mutex> &lk) {
+        for (auto &s : slots) {
+            if (!s.busy || cudaEventQuery(s.done) != cudaSuccess) continue;
+            size_t sz[4];
+            op_io_sizes(s.alg, s.op, sz);
+            const auto now = Clock::now();
+            for (int i = 0; i < s.n; i++) {
+                Req *q = s.reqs[i];
+                if (s.op == PQCGPU_OP_KEYPAIR) {
+                    if (q->r.out0) memcpy(q->r.out0, s.hbuf + s.h_out0 + (size_t)i * sz[2], sz[2]);
+                    if (q->r.key_out) *q->r.key_out = ((uint64_t)s.alg << 48) | (uint64_t)(q->key_slot + 1);
+                } else if (s.op == PQCGPU_OP_ENC) {
+                    memcpy(q->r.out0, s.hbuf + s.h_out0 + (size_t)i * sz[2], sz[2]);
+                    memcpy(q->r.out1, s.hbuf + s.h_out1 + (size_t)i * sz[3], sz[3]);
+                } else {
+                    memcpy(q->r.out0, s.hbuf + s.h_out0 + (size_t)i * sz[2], sz[2]);
+                }
+                finish(q, 0, std::chrono::duration<double, std::milli>(now - q->t0).count());
+            }
+            s.reqs.clear();
+            s.busy = false;
+            batches++;
+            cv_done.notify_all();
+        }
+        (void)lk;
+    }
+
+    // Form and launch one batch on a free slot; returns false if nothing was launched.
+    bool launch_one(std::unique_lock<std::mutex> &lk) {
+        if (queue.empty()) return false;
+        Slot *slot = nullptr;
+        for (auto &s : slots)
+            if (!s.busy) {
+                slot = &s;
+                break;
+            }
+        if (!slot) return false;
+        const int alg = queue.front()->r.alg, op = queue.front()->r.op;
+        // FrodoKEM instances cost ~10^4 Keccak permutations each: cap its batches for latency
+        const int cap = (alg == PQCGPU_FRODO976) ? std::min(max_batch, 256) : max_batch;
+        std::vector<Req *> take;
+        for (auto it = queue.begin(); it != queue.end() && (int)take.size() < cap;) {
+            if ((*it)->r.alg == alg && (*it)->r.op == op) {
+                take.push_back(*it);
+                it = queue.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        size_t sz[4];
+        op_io_sizes(alg, op, sz);
+        const size_t scr = op_scratch_bytes(alg, op, 0);
+        KeyStore &k = ks[alg];
+        // keys: keypair reserves slots; enc / dec by handle resolve them (invalid -> error now)
+        std::vector<uint32_t> idx;
+        std::vector<Req *> ok;
+        for (Req *q : take) {
+            uint32_t ksl = 0;
+            if (op == PQCGPU_OP_KEYPAIR) {
+                if (k.free_slots.empty() && grow_keys(alg, k.cap + (uint32_t)take.size())) {
+                    finish(q, PQCGPU_EBUDGET, 0);
+                    continue;
+                }
+                ksl = k.free_slots.back();
+                k.free_slots.pop_back();
+                k.used[ksl] = 1;
+            } else if (q->r.key || op == PQCGPU_OP_DEC) {
+                if (!key_ok(q->r.key, alg, &ksl)) {
+                    finish(q, PQCGPU_EINVAL, 0);
+                    continue;
+                }
+            }
+            q->key_slot = ksl;
+            idx.push_back(ksl);
+            ok.push_back(q);
+        }
+        if (ok.empty()) {
+            cv_done.notify_all();
+            return true;
+        }
+        const int n = (int)ok.size();
+        const bool by_handle = (op == PQCGPU_OP_DEC) || (op == PQCGPU_OP_ENC && ok[0]->r.key != 0);
+        // staging layout (device and pinned host alike)
+        Slot &s = *slot;
+        size_t d = 0;
+        s.off_in0 = d; d += r256(sz[0] * n);
+        s.off_in1 = d; d += r256(sz[1] * n);
+        s.off_out0 = d; d += r256(sz[2] * n);
+        s.off_out1 = d; d += r256(sz[3] * n);
+        s.off_idx = d; d += r256(4 * (size_t)n);
+        s.off_scr = d; d += r256(scr * n);
+        if (d > s.dcap) {
+            free_dev(s.dbuf, s.dcap);
+            s.dbuf = nullptr;
+            s.dcap = 0;
+            size_t want = d + d / 2;
+            if (alloc_dev(&s.dbuf, want) && alloc_dev(&s.dbuf, d)) {
+                bool others = false;
+                for (auto &o : slots) others |= o.busy;
+                for (auto it = ok.rbegin(); it != ok.rend(); ++it) {
+                    Req *q = *it;
+                    if (op == PQCGPU_OP_KEYPAIR) {
+                        k.used[q->key_slot] = 0;
+                        k.free_slots.push_back(q->key_slot);
+                    }
+                    if (others) queue.push_front(q);  // wait for in-flight batches to free memory
+                    else finish(q, PQCGPU_EBUDGET, 0);  // nothing will free memory: refuse
+                }
+                if (!others) cv_done.notify_all();
+                return !others;
+            }
+            s.dcap = (s.dbuf && used >= want) ? want : d;
+        }
+        if (d > s.hcap) {
+            if (s.hbuf) cudaFreeHost(s.hbuf);
+            s.hbuf = nullptr;
+            s.hcap = 0;
+            if (cudaMallocHost(&s.hbuf, d + d / 2) != cudaSuccess) {
+                cudaGetLastError();
+                for (Req *q : ok) finish(q, PQCGPU_ENOMEM, 0);
+                cv_done.notify_all();
+                return true;
+            }
+            s.hcap = d + d / 2;
+        }
+        s.h_in0 = s.off_in0;
+        s.h_in1 = s.off_in1;
+        s.h_out0 = s.off_out0;
+        s.h_out1 = s.off_out1;
+        s.h_idx = s.off_idx;
+        // pack host inputs
+        for (int i = 0; i < n; i++) {
+            const pqcgpu_request &r = ok[i]->r;
+            if (op == PQCGPU_OP_KEYPAIR) {
+                if (r.in) memcpy(s.hbuf + s.h_in0 + (size_t)i * sz[0], r.in, sz[0]);
+                else pqcgpu_randombytes(s.hbuf + s.h_in0 + (size_t)i * sz[0], sz[0]);
+            } else if (op == PQCGPU_OP_ENC) {
+                if (!by_handle) memcpy(s.hbuf + s.h_in0 + (size_t)i * sz[0], r.pk, sz[0]);
+                if (r.in) memcpy(s.hbuf + s.h_in1 + (size_t)i * sz[1], r.in, sz[1]);
+                else pqcgpu_randombytes(s.hbuf + s.h_in1 + (size_t)i * sz[1], sz[1]);
+            } else {
+                memcpy(s.hbuf + s.h_in0 + (size_t)i * sz[0], r.in, sz[0]);
+            }
+        }
+        memcpy(s.hbuf + s.h_idx, idx.data(), 4 * (size_t)n);
+        s.alg = alg;
+        s.op = op;
+        s.n = n;
+        s.reqs = ok;
+        s.busy = true;
+        lk.unlock();
+        // device work on the slot stream
+        cudaStream_t st = s.stream;
+        uint8_t *D = s.dbuf, *H = s.hbuf;
+        const uint32_t *didx = (const uint32_t *)(D + s.off_idx);
+        cudaMemcpyAsync(D + s.off_idx, H + s.h_idx, 4 * (size_t)n, cudaMemcpyHostToDevice, st);
+        if (op == PQCGPU_OP_KEYPAIR) {
+            cudaMemcpyAsync(D + s.off_in0, H + s.h_in0, sz[0] * n, cudaMemcpyHostToDevice, st);
+            op_dev(alg, op, n, D + s.off_in0, nullptr, D + s.off_out0, D + s.off_out1, D + s.off_scr, 0, st);
+            launch_rows(false, k.dpk, D + s.off_out0, didx, n, k.pkb, st);
+            launch_rows(false, k.dsk, D + s.off_out1, didx, n, k.skb, st);
+            cudaMemcpyAsync(H + s.h_out0, D + s.off_out0, sz[2] * n, cudaMemcpyDeviceToHost, st);
+        } else if (op == PQCGPU_OP_ENC) {
+            if (by_handle) launch_rows(true, D + s.off_in0, k.dpk, didx, n, k.pkb, st);
+            else cudaMemcpyAsync(D + s.off_in0, H + s.h_in0, sz[0] * n, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(D + s.off_in1, H + s.h_in1, sz[1] * n, cudaMemcpyHostToDevice, st);
+            op_dev(alg, op, n, D + s.off_in0, D + s.off_in1, D + s.off_out0, D + s.off_out1, D + s.off_scr, 0, st);
+            cudaMemcpyAsync(H + s.h_out0, D + s.off_out0, sz[2] * n, cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(H + s.h_out1, D + s.off_out1, sz[3] * n, cudaMemcpyDeviceToHost, st);
+        } else {
+            cudaMemcpyAsync(D + s.off_in0, H + s.h_in0, sz[0] * n, cudaMemcpyHostToDevice, st);
+            launch_rows(true, D + s.off_in1, k.dsk, didx, n, k.skb, st);
+            op_dev(alg, op, n, D + s.off_in0, D + s.off_in1, D + s.off_out0, nullptr, D + s.off_scr, 0, st);
+            cudaMemcpyAsync(H + s.h_out0, D + s.off_out0, sz[2] * n, cudaMemcpyDeviceToHost, st);
+        }
+        cudaEventRecord(s.done, st);
+        lk.lock();
+        return true;
+    }
+
+    void run() {
+        cudaSetDevice(device);
+        std::unique_lock<std::mutex> lk(mu);
+        while (true) {
+            reap(lk);
+            bool launched = false;
+            while (launch_one(lk)) launched = true;
+            bool any_busy = false;
+            for (auto &s : slots) any_busy |= s.busy;
+            if (stop && queue.empty() && !any_busy) break;
+            if (!launched) {
+                if (any_busy) {
+                    // poll the in-flight batches; new requests wake us immediately
+                    cv_work.wait_for(lk, std::chrono::microseconds(20));
+                } else {
+                    cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+                }
+            }
+        }
+    }
+};
+
+extern "C" int pqcgpu_server_create(pqcgpu_server **out, int device, size_t budget, int max_inflight, int max_batch) {
+    if (!out) return set_error(PQCGPU_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(PQCGPU_ECUDA, "no such CUDA device");
+    }
+    int rc = device_ready(device);
+    if (rc) return rc;
+    auto *s = new pqcgpu_server();
+    s->device = device;
+    s->budget = budget ? budget : ((size_t)16 << 30);
+    s->max_inflight = max_inflight > 0 ? std::min(max_inflight, 16) : 4;
+    s->max_batch = max_batch > 0 ? max_batch : 4096;
+    s->slots.resize(s->max_inflight);
+    for (auto &sl : s->slots) {
+        cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+    }
+    for (int a = 0; a < PQCGPU_NUM_ALGS; a++) {
+        size_t sz[4];
+        op_io_sizes(a, PQCGPU_OP_KEYPAIR, sz);
+        s->ks[a].pkb = sz[2];
+        s->ks[a].skb = sz[3];
+    }
+    s->th = std::thread([s] { s->run(); });
+    *out = s;
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_server_submit(pqcgpu_server *s, const pqcgpu_request *req, uint64_t *ticket) {
+    if (!s || !req) return set_error(PQCGPU_EINVAL, "null server or request");
+    size_t sz[4];
+    if (req->alg < 0 || req->alg >= PQCGPU_NUM_ALGS || req->op < 0 || req->op > 2)
+        return set_error(PQCGPU_EINVAL, "bad algorithm or operation");
+    op_io_sizes(req->alg, req->op, sz);
+    if (req->op == PQCGPU_OP_ENC && !req->key && !req->pk) return set_error(PQCGPU_EINVAL, "encapsulation needs a key or pk");
+    if ((req->op == PQCGPU_OP_ENC && (!req->out0 || !req->out1)) || (req->op == PQCGPU_OP_DEC && (!req->in || !req->out0)))
+        return set_error(PQCGPU_EINVAL, "missing buffer");
+    auto q = std::make_unique<Req>();
+    q->r = *req;
+    q->t0 = Clock::now();
+    Req *raw = q.get();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->stop) return set_error(PQCGPU_EINVAL, "server is shutting down");
+        raw->ticket = s->next_ticket++;
+        s->reqs[raw->ticket] = std::move(q);
+        s->queue.push_back(raw);
+    }
+    s->cv_work.notify_one();
+    if (ticket) *ticket = raw->ticket;
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_server_wait(pqcgpu_server *s, uint64_t ticket, int timeout_ms) {
+    if (!s) return PQCGPU_EINVAL;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return set_error(PQCGPU_EINVAL, "unknown ticket");
+    Req *q = it->second.get();
+    auto pred = [&] { return q->status != 1; };
+    if (timeout_ms < 0) s->cv_done.wait(lk, pred);
+    else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) return PQCGPU_ETIMEOUT;
+    const int st = q->status;
+    s->reqs.erase(it);
+    return st;
+}
+
+extern "C" int pqcgpu_server_drain(pqcgpu_server *s) {
+    if (!s) return PQCGPU_EINVAL;
+    std::unique_lock<std::mutex> lk(s->mu);
+    s->cv_done.wait(lk, [&] {
+        if (!s->queue.empty()) return false;
+        for (auto &sl : s->slots)
+            if (sl.busy) return false;
+        return true;
+    });
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_server_key_release(pqcgpu_server *s, uint64_t key) {
+    if (!s) return PQCGPU_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    const int alg = (int)(key >> 48);
+    uint32_t slot;
+    if (alg < 0 || alg >= PQCGPU_NUM_ALGS || !s->key_ok(key, alg, &slot)) return set_error(PQCGPU_EINVAL, "unknown key");
+    s->ks[alg].used[slot] = 0;
+    s->ks[alg].free_slots.push_back(slot);
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_server_get_stats(pqcgpu_server *s, pqcgpu_server_stats *out, int reset) {
+    if (!s || !out) return PQCGPU_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    memset(out, 0, sizeof *out);
+    out->completed = s->completed;
+    out->batches = s->batches;
+    out->hbm_used = s->used;
+    for (auto &k : s->ks)
+        for (auto u : k.used) out->keys_resident += u;
+    std::vector<double> v = s->lat_ms;
+    if (!v.empty()) {
+        std::sort(v.begin(), v.end());
+        out->p50_ms = v[v.size() / 2];
+        out->p99_ms = v[std::min(v.size() - 1, (size_t)(0.99 * v.size()))];
+        out->max_ms = v.back();
+        double sum = 0;
+        for (double x : v) sum += x;
+        out->mean_ms = sum / v.size();
+    }
+    if (reset) {
+        s->lat_ms.clear();
+        s->completed = 0;
+        s->batches = 0;
+    }
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_server_destroy(pqcgpu_server *s) {
+    if (!s) return PQCGPU_EINVAL;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    if (s->th.joinable()) s->th.join();
+    cudaSetDevice(s->device);
+    cudaDeviceSynchronize();
+    for (auto &sl : s->slots) {
+        s->free_dev(sl.dbuf, sl.dcap);
+        if (sl.hbuf) cudaFreeHost(sl.hbuf);
+        cudaStreamDestroy(sl.stream);
+        cudaEventDestroy(sl.done);
+    }
+    for (auto &k : s->ks) {
+        s->free_dev(k.dpk, (size_t)k.cap * k.pkb);
+        s->free_dev(k.dsk, (size_t)k.cap * k.skb);
+    }
+    delete s;
+    return PQCGPU_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Open-loop Poisson load: keys and ciphertexts are prepared first (resident keys), then requests
+// are submitted at exponential inter-arrival times for `seconds`, then the server is drained.
+// ---------------------------------------------------------------------------------------------
+extern "C" int pqcgpu_server_run_poisson(pqcgpu_server *s, const pqcgpu_mix_entry *mix, size_t nmix, double rate,
+                                         double seconds, uint64_t seed, pqcgpu_load_report *out) {
+    if (!s || !mix || !nmix || rate <= 0 || seconds <= 0 || !out) return set_error(PQCGPU_EINVAL, "bad load arguments");
+    std::mt19937_64 rng(seed);
+    // per-algorithm pools: resident keys and matching ciphertexts
+    constexpr int POOL = 64;
+    struct Pool {
+        std::vector<uint64_t> keys;
+        std::vector<std::vector<uint8_t>> cts;
+    } pools[PQCGPU_NUM_ALGS];
+    for (size_t m = 0; m < nmix; m++) {
+        const int a = mix[m].alg;
+        if (a < 0 || a >= PQCGPU_NUM_ALGS || mix[m].op < 0 || mix[m].op > 2) return set_error(PQCGPU_EINVAL, "bad mix entry");
+        if (!pools[a].keys.empty()) continue;
+        size_t kz[4], ez[4];
+        op_io_sizes(a, PQCGPU_OP_KEYPAIR, kz);
+        op_io_sizes(a, PQCGPU_OP_ENC, ez);
+        pools[a].keys.resize(POOL);
+        std::vector<uint64_t> tk(POOL);
+        for (int i = 0; i < POOL; i++) {
+            pqcgpu_request r{};
+            r.alg = a;
+            r.op = PQCGPU_OP_KEYPAIR;
+            r.key_out = &pools[a].keys[i];
+            int rc = pqcgpu_server_submit(s, &r, &tk[i]);
+            if (rc) return rc;
+        }
+        for (int i = 0; i < POOL; i++)
+            if (pqcgpu_server_wait(s, tk[i], -1) != 0) return set_error(PQCGPU_ECUDA, "pool keypair failed");
+        pools[a].cts.assign(POOL, std::vector<uint8_t>(ez[2]));
+        std::vector<uint8_t> ss(ez[3]);
+        for (int i = 0; i < POOL; i++) {
+            pqcgpu_request r{};
+            r.alg = a;
+            r.op = PQCGPU_OP_ENC;
+            r.key = pools[a].keys[i];
+            r.out0 = pools[a].cts[i].data();
+            r.out1 = ss.data();
+            int rc = pqcgpu_server_submit(s, &r, &tk[i]);
+            if (rc) return rc;
+            if (pqcgpu_server_wait(s, tk[i], -1) != 0) return set_error(PQCGPU_ECUDA, "pool encaps failed");
+        }
+    }
+    pqcgpu_server_drain(s);
+    {
+        pqcgpu_server_stats st;
+        pqcgpu_server_get_stats(s, &st, 1);
+    }
+    double wsum = 0;
+    for (size_t m = 0; m < nmix; m++) wsum += mix[m].weight;
+    std::exponential_distribution<double> gap(rate);
+    std::uniform_real_distribution<double> uni(0.0, wsum);
+    // output sinks (results are discarded; one buffer per alg/op, largest sizes)
+    static thread_local std::vector<uint8_t> sink0(1 << 16), sink1(1 << 16);
+    std::vector<uint64_t> new_keys;
+    new_keys.reserve(1024);
+    std::vector<uint64_t> *keyslots = &new_keys;
+    std::deque<uint64_t> key_outs;
+    const auto t_start = Clock::now();
+    double t = 0;
+    uint64_t submitted = 0;
+    while (t < seconds) {
+        t += gap(rng);
+        const auto due = t_start + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(t));
+        while (Clock::now() < due) {
+            const auto left = due - Clock::now();
+            if (left > std::chrono::microseconds(200)) std::this_thread::sleep_for(left - std::chrono::microseconds(100));
+        }
+        double u = uni(rng);
+        size_t m = 0;
+        while (m + 1 < nmix && u >= mix[m].weight) {
+            u -= mix[m].weight;
+            m++;
+        }
+        const int a = mix[m].alg, op = mix[m].op;
+        const int i = (int)(rng() % POOL);
+        pqcgpu_request r{};
+        r.alg = a;
+        r.op = op;
+        if (op == PQCGPU_OP_KEYPAIR) {
+            key_outs.push_back(0);
+            r.key_out = &key_outs.back();
+        } else if (op == PQCGPU_OP_ENC) {
+            r.key = pools[a].keys[i];
+            r.out0 = sink0.data();
+            r.out1 = sink1.data();
+        } else {
+            r.key = pools[a].keys[i];
+            r.in = pools[a].cts[i].data();
+            r.out0 = sink0.data();
+        }
+        uint64_t tk;
+        if (pqcgpu_server_submit(s, &r, &tk) == 0) submitted++;
+    }
+    const auto t_sub = Clock::now();
+    pqcgpu_server_drain(s);
+    const auto t_end = Clock::now();
+    pqcgpu_server_stats st;
+    pqcgpu_server_get_stats(s, &st, 1);
+    {
+        // forget the tickets of the load run and release the keys it generated
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->reqs.clear();
+    }
+    for (uint64_t k : key_outs)
+        if (k) pqcgpu_server_key_release(s, k);
+    (void)keyslots;
+    out->offered_per_s = rate;
+    out->seconds = std::chrono::duration<double>(t_end - t_start).count();
+    out->submit_seconds = std::chrono::duration<double>(t_sub - t_start).count();
+    out->submitted = submitted;
+    out->completed = st.completed;
+    out->batches = st.batches;
+    out->achieved_per_s = st.completed / out->seconds;
+    out->p50_ms = st.p50_ms;
+    out->p99_ms = st.p99_ms;
+    out->mean_ms = st.mean_ms;
+    out->max_ms = st.max_ms;
+    return PQCGPU_OK;
+}
