@@ -2,9 +2,10 @@
 //
 // Replaces crypto_kem_keypair_gpu / enc / dec (FrodoKEM_GPU/frodo976.cu:87-690: one instance per
 // call, A written to and re-read from HBM, host SHAKE for pk / ct) with, per operation:
-//   * a thread-per-instance kernel for the serial sponges -- the S/E noise stream
+//   * a warp-per-instance kernel for the serial sponges -- the S/E noise stream
 //     (SHAKE256(0x5F / 0x96 || seedSE), 230-231 permutations), G1 = SHAKE256(pk) (115), G2 and
-//     the final F = SHAKE256(ct || k) (116) -- the noise sampled with the CDF table on the fly;
+//     the final F = SHAKE256(ct || k) (116) -- with the Keccak state spread over the warp to cut
+//     the latency of these chains, the noise sampled with the CDF table on the fly;
 //   * a core kernel that regenerates A row by row from SHAKE128(le16(i) || seedA) and multiplies
 //     it as it appears, so A (1.9 MB per key) never exists in HBM or whole in shared memory:
 //       - keypair, B = A S + E: one thread per row, which owns the 8 outputs of that row;
@@ -34,52 +35,7 @@ constexpr size_t SCRATCH = (size_t)NOISE_U16 * 2 + 128;
 
 static __constant__ uint16_t c_cdf[11];
 
-// ---- sponge helpers -------------------------------------------------------------------------
-// Absorb the concatenation of two lane-aligned byte strings (n1 and n2 lanes of 8 bytes), pad.
-template <int R>
-__device__ __forceinline__ void absorb2(uint2 (&A)[25], const uint2 *p1, int n1, const uint2 *p2, int n2, uint32_t dom) {
-    keccak_zero(A);
-    int total = n1 + n2, done = 0;
-    while (total - done >= R) {
-#pragma unroll
-        for (int i = 0; i < R; i++) {
-            const int idx = done + i;
-            A[i] = xor2(A[i], idx < n1 ? p1[idx] : p2[idx - n1]);
-        }
-        keccak_f1600(A);
-        done += R;
-    }
-#pragma unroll
-    for (int i = 0; i < R; i++) {
-        const int idx = done + i;
-        if (idx < total) A[i] = xor2(A[i], idx < n1 ? p1[idx] : p2[idx - n1]);
-    }
-    keccak_pad<R>(A, total - done, dom);
-}
-// Absorb `len` (< rate) bytes given in registers as little-endian lanes with a leading domain byte.
-__device__ __forceinline__ void absorb_prefixed24(uint2 (&A)[25], uint8_t prefix, const uint8_t *seed24) {
-    // message = prefix || seed (25 bytes), SHAKE256
-    uint8_t b[32];
-    b[0] = prefix;
-#pragma unroll
-    for (int i = 0; i < 24; i++) b[1 + i] = seed24[i];
-#pragma unroll
-    for (int i = 25; i < 32; i++) b[i] = 0;
-    b[25] = (uint8_t)DOM_SHAKE;
-    keccak_zero(A);
-#pragma unroll
-    for (int l = 0; l < 4; l++) {
-        uint32_t lo = 0, hi = 0;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            lo |= (uint32_t)b[8 * l + q] << (8 * q);
-            hi |= (uint32_t)b[8 * l + 4 + q] << (8 * q);
-        }
-        A[l] = make_uint2(lo, hi);
-    }
-    A[SHAKE256_LANES - 1].y ^= 0x80000000u;
-}
-
+// ---- helpers ---------------------------------------------------------------------------------
 // CDF sampler of one 16-bit value (noise.c:10-29)
 __device__ __forceinline__ uint16_t cdf_sample(uint32_t r) {
     uint32_t sample = 0;
@@ -87,22 +43,6 @@ __device__ __forceinline__ uint16_t cdf_sample(uint32_t r) {
 #pragma unroll
     for (int j = 0; j < 10; j++) sample += ((uint32_t)c_cdf[j] - prnd) >> 31 & 1;
     return (uint16_t)((((0u - sign) ^ sample) + sign) & 0xffff);
-}
-
-// Squeeze the SHAKE256 noise stream (state after absorb), sample every u16 and hand value v at
-// stream position p to emit(p, v).
-template <class F>
-__device__ __forceinline__ void noise_stream(uint2 (&A)[25], int count, F emit) {
-    for (int base = 0; base < count; base += 68) {  // 136 bytes = 68 values per block
-        keccak_f1600(A);
-#pragma unroll
-        for (int w = 0; w < 34; w++) {
-            const uint32_t t = (w & 1) ? A[w >> 1].y : A[w >> 1].x;
-            const int p = base + 2 * w;
-            if (p < count) emit(p, cdf_sample(t & 0xffff));
-            if (p + 1 < count) emit(p + 1, cdf_sample(t >> 16));
-        }
-    }
 }
 
 // SHAKE128 row generator for A: absorb le16(row) || seedA, squeeze block by block.
@@ -119,78 +59,102 @@ __device__ __forceinline__ void row_absorb(uint2 (&A)[25], int row, const uint2 
 __device__ __forceinline__ uint32_t ld_be16(const uint8_t *p) { return ((uint32_t)p[0] << 8) | p[1]; }
 
 // ---------------------------------------------------------------------------------------------
-// Serial sponges (thread per instance)
+// Serial sponges: one warp per instance (warp-cooperative Keccak, keccak.cuh)
 // ---------------------------------------------------------------------------------------------
-// keypair: seedA = SHAKE256(z, 16) -> pk[0..16); S (as St[j][k], N x 8) and E (N x 8) -> scratch
-__global__ void __launch_bounds__(32) fr_kp_pre(int n, const uint8_t *coins, int cstride, uint8_t *pk, uint8_t *scratch) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= n) return;
-    const uint8_t *c = coins + (size_t)x * cstride;  // s(24) || seedSE(24) || z(16)
-    uint2 A[25];
-    keccak_absorb_lanes<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(c + 48), 2, DOM_SHAKE);
-    keccak_f1600(A);
-    reinterpret_cast<uint2 *>(pk + (size_t)x * PKB)[0] = A[0];
-    reinterpret_cast<uint2 *>(pk + (size_t)x * PKB)[1] = A[1];
-    uint16_t *St = reinterpret_cast<uint16_t *>(scratch + (size_t)x * SCRATCH), *E = St + N * NB;
-    uint8_t seed[24];
+// Message lane m (0..3) of prefix || seed (25 bytes) followed by the SHAKE domain byte, where the
+// 24-byte seed is given as three little-endian 64-bit words.
+__device__ __forceinline__ uint2 prefixed_lane(int m, uint32_t prefix, uint64_t s0, uint64_t s1, uint64_t s2) {
+    uint64_t v;
+    if (m == 0) v = prefix | (s0 << 8);
+    else if (m == 1) v = (s0 >> 56) | (s1 << 8);
+    else if (m == 2) v = (s1 >> 56) | (s2 << 8);
+    else v = (s2 >> 56) | ((uint64_t)DOM_SHAKE << 8);
+    return make_uint2((uint32_t)v, (uint32_t)(v >> 32));
+}
+__device__ __forceinline__ uint64_t u64(uint2 v) { return (uint64_t)v.x | ((uint64_t)v.y << 32); }
+
+// State absorbing prefix || seed (one block, not yet permuted).
+__device__ __forceinline__ uint2 seeded_state(uint32_t prefix, uint64_t s0, uint64_t s1, uint64_t s2, const WarpKeccak &w) {
+    uint2 a = w.lane < 4 ? prefixed_lane(w.lane, prefix, s0, s1, s2) : make_uint2(0, 0);
+    if (w.lane == SHAKE256_LANES - 1) a.y ^= 0x80000000u;
+    return a;
+}
+
+// Squeeze the noise stream (state absorbed, not permuted): lanes 0..16 hold 4 u16 values each per
+// block; value at stream position p is CDF-sampled and handed to emit(p, v).
+template <class F>
+__device__ __forceinline__ void warp_noise_stream(uint2 &a, int count, const WarpKeccak &w, F emit) {
+    for (int base = 0; base < count; base += 68) {
+        keccak_f1600_warp(a, w);
+        if (w.lane < 17) {
 #pragma unroll
-    for (int i = 0; i < 24; i++) seed[i] = c[24 + i];
-    absorb_prefixed24(A, 0x5F, seed);
+            for (int q = 0; q < 4; q++) {
+                const int p = base + 4 * w.lane + q;
+                const uint32_t word = q < 2 ? a.x : a.y;
+                if (p < count) emit(p, cdf_sample((word >> (16 * (q & 1))) & 0xffff));
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void write_spt(uint8_t *scr, int p, uint16_t v) {
+    uint16_t *Spt = reinterpret_cast<uint16_t *>(scr), *Ep = Spt + N * NB, *Epp = Ep + N * NB;
+    if (p < N * NB) Spt[(p % N) * NB + p / N] = v;  // stream S'[i*N + k] -> Spt[k*8 + i]
+    else if (p < 2 * N * NB) Ep[p - N * NB] = v;
+    else Epp[p - 2 * N * NB] = v;
+}
+
+#define FR_WARP_INSTANCE                                         \
+    const int x = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  \
+    if (x >= n) return;                                          \
+    const WarpKeccak w(threadIdx.x & 31)
+
+// keypair: seedA = SHAKE256(z, 16) -> pk[0..16); S (as St[j][k], N x 8) and E (N x 8) -> scratch
+__global__ void __launch_bounds__(128) fr_kp_pre(int n, const uint8_t *coins, int cstride, uint8_t *pk, uint8_t *scratch) {
+    FR_WARP_INSTANCE;
+    const uint8_t *c = coins + (size_t)x * cstride;  // s(24) || seedSE(24) || z(16)
+    uint2 a;
+    warp_absorb2<SHAKE256_LANES>(a, reinterpret_cast<const uint2 *>(c + 48), 2, nullptr, 0, DOM_SHAKE, w);
+    keccak_f1600_warp(a, w);
+    if (w.lane < 2) reinterpret_cast<uint2 *>(pk + (size_t)x * PKB)[w.lane] = a;
+    const uint64_t *sd = reinterpret_cast<const uint64_t *>(c + 24);
+    a = seeded_state(0x5F, sd[0], sd[1], sd[2], w);
+    uint16_t *St = reinterpret_cast<uint16_t *>(scratch + (size_t)x * SCRATCH), *E = St + N * NB;
     // stream order: S[k*N + j] (k < 8, j < N) then E[i*8 + k]
-    noise_stream(A, 2 * N * NB, [&](int p, uint16_t v) {
+    warp_noise_stream(a, 2 * N * NB, w, [&](int p, uint16_t v) {
         if (p < N * NB) St[(p % N) * NB + p / N] = v;
         else E[p - N * NB] = v;
     });
 }
 
+// G2(pkh || mu) with pkh in lanes 0..2 of `a`, mu at `mu`; then the S' / E' / E'' noise stream.
+// Writes k (24 B) and mu (24 B) into the scratch seed area.
+__device__ __forceinline__ void g2_and_noise(uint2 a, const uint8_t *mu, uint8_t *scr, const WarpKeccak &w) {
+    const uint2 *m = reinterpret_cast<const uint2 *>(mu);
+    uint2 g = w.lane < 3 ? a : (w.lane < 6 ? m[w.lane - 3] : make_uint2(0, 0));
+    if (w.lane == 6) g.x ^= DOM_SHAKE;
+    if (w.lane == SHAKE256_LANES - 1) g.y ^= 0x80000000u;
+    keccak_f1600_warp(g, w);
+    uint2 *kk = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2), *mm = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2 + 32);
+    if (w.lane >= 3 && w.lane < 6) kk[w.lane - 3] = g;
+    const uint2 mv = w.lane < 3 ? m[w.lane] : make_uint2(0, 0);
+    __syncwarp();
+    if (w.lane < 3 && mu != scr + NOISE_U16 * 2 + 32) mm[w.lane] = mv;
+    const uint64_t s0 = u64(shfl2(g, 0)), s1 = u64(shfl2(g, 1)), s2 = u64(shfl2(g, 2));
+    uint2 st = seeded_state(0x96, s0, s1, s2, w);
+    warp_noise_stream(st, NOISE_U16, w, [&](int p, uint16_t v) { write_spt(scr, p, v); });
+}
+
 // encaps prologue: pkh = G1(pk); (seedSE || k) = G2(pkh || mu); S', E', E'' sampled -> scratch.
 // scratch: Spt (N x 8: Spt[k][i] = S'[i][k]), Ep (8 x N), Epp (8 x 8), then k (24) at +NOISE*2,
 // mu (24) at +NOISE*2 + 32.
-__device__ __forceinline__ void enc_noise(uint8_t *scr, const uint8_t *seedSE) {
-    uint2 A[25];
-    absorb_prefixed24(A, 0x96, seedSE);
-    uint16_t *Spt = reinterpret_cast<uint16_t *>(scr), *Ep = Spt + N * NB, *Epp = Ep + N * NB;
-    noise_stream(A, NOISE_U16, [&](int p, uint16_t v) {
-        if (p < N * NB) Spt[(p % N) * NB + p / N] = v;  // stream S'[i*N + k] -> Spt[k*8 + i]
-        else if (p < 2 * N * NB) Ep[p - N * NB] = v;
-        else Epp[p - 2 * N * NB] = v;
-    });
-}
-
-__global__ void __launch_bounds__(32) fr_enc_pre(int n, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= n) return;
-    uint8_t *scr = scratch + (size_t)x * SCRATCH;
-    uint2 A[25], in[6];
-    keccak_absorb_lanes<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(pk + (size_t)x * PKB), PKB / 8, DOM_SHAKE);
-    keccak_f1600(A);
-    in[0] = A[0];
-    in[1] = A[1];
-    in[2] = A[2];
-    const uint2 *m = reinterpret_cast<const uint2 *>(mu + (size_t)x * MUB);
-    in[3] = m[0];
-    in[4] = m[1];
-    in[5] = m[2];
-    keccak_absorb_lanes<SHAKE256_LANES>(A, in, 6, DOM_SHAKE);
-    keccak_f1600(A);
-    uint2 *kk = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2);
-    kk[0] = A[3];
-    kk[1] = A[4];
-    kk[2] = A[5];  // k
-    uint2 *mm = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2 + 32);
-    mm[0] = m[0];
-    mm[1] = m[1];
-    mm[2] = m[2];
-    uint8_t seed[24];
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            seed[8 * i + q] = (uint8_t)(A[i].x >> (8 * q));
-            seed[8 * i + 4 + q] = (uint8_t)(A[i].y >> (8 * q));
-        }
-    }
-    enc_noise(scr, seed);
+__global__ void __launch_bounds__(128) fr_enc_pre(int n, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch) {
+    FR_WARP_INSTANCE;
+    uint2 a;
+    warp_absorb2<SHAKE256_LANES>(a, reinterpret_cast<const uint2 *>(pk + (size_t)x * PKB), PKB / 8, nullptr, 0,
+                                 DOM_SHAKE, w);
+    keccak_f1600_warp(a, w);
+    g2_and_noise(a, mu + (size_t)x * MUB, scratch + (size_t)x * SCRATCH, w);
 }
 
 // decaps, step 1 (CTA per instance): W = C - B' S (frodo_mul_bs + frodo_sub), mu' = decode(W)
@@ -219,8 +183,8 @@ __global__ void __launch_bounds__(256) fr_dec_w(int n, const uint8_t *ct, const 
         const int g = tid;
         uint32_t templong = 0;
         for (int jj = 0; jj < 8; jj++) {
-            const uint32_t w = (ld_be16(c + C1B + 2 * (g * NB + jj)) - W[g * NB + jj]) & 0xffff;
-            const uint32_t t = (w + (1u << 12)) >> 13;
+            const uint32_t wv = (ld_be16(c + C1B + 2 * (g * NB + jj)) - W[g * NB + jj]) & 0xffff;
+            const uint32_t t = (wv + (1u << 12)) >> 13;
             templong |= (t & 7) << (3 * jj);
         }
         uint8_t *mu = scratch + (size_t)x * SCRATCH + NOISE_U16 * 2 + 32;
@@ -230,85 +194,55 @@ __global__ void __launch_bounds__(256) fr_dec_w(int n, const uint8_t *ct, const 
     }
 }
 
-// decaps, step 2 (thread per instance): (seedSE' || k') = G2(pkh || mu'); S', E', E'' -> scratch
-__global__ void __launch_bounds__(32) fr_dec_pre(int n, const uint8_t *sk, uint8_t *scratch) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= n) return;
-    const uint8_t *s = sk + (size_t)x * SKB;
+// decaps, step 2 (warp per instance): (seedSE' || k') = G2(pkh || mu'); S', E', E'' -> scratch
+__global__ void __launch_bounds__(128) fr_dec_pre(int n, const uint8_t *sk, uint8_t *scratch) {
+    FR_WARP_INSTANCE;
     uint8_t *scr = scratch + (size_t)x * SCRATCH;
-    uint2 A[25], in[6];
-    const uint2 *pkh = reinterpret_cast<const uint2 *>(s + SSB + PKB + C1B);
-    const uint2 *mu = reinterpret_cast<const uint2 *>(scr + NOISE_U16 * 2 + 32);
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        in[i] = pkh[i];
-        in[3 + i] = mu[i];
-    }
-    keccak_absorb_lanes<SHAKE256_LANES>(A, in, 6, DOM_SHAKE);
-    keccak_f1600(A);
-    uint2 *kk = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2);
-#pragma unroll
-    for (int i = 0; i < 3; i++) kk[i] = A[3 + i];
-    uint8_t seed[24];
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            seed[8 * i + q] = (uint8_t)(A[i].x >> (8 * q));
-            seed[8 * i + 4 + q] = (uint8_t)(A[i].y >> (8 * q));
-        }
-    }
-    enc_noise(scr, seed);
+    const uint2 *pkh = reinterpret_cast<const uint2 *>(sk + (size_t)x * SKB + SSB + PKB + C1B);
+    const uint2 a = w.lane < 3 ? pkh[w.lane] : make_uint2(0, 0);
+    g2_and_noise(a, scr + NOISE_U16 * 2 + 32, scr, w);
 }
 
-// F = SHAKE256(ct || key, 24): encaps key = k; decaps key = fail ? s : k'
-__global__ void __launch_bounds__(32) fr_post(int n, const uint8_t *ct, const uint8_t *scratch, const uint8_t *sk,
-                                              uint8_t *ss) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= n) return;
-    const uint8_t *scr = scratch + (size_t)x * SCRATCH;
+// F = SHAKE256(ct || key, 24): encaps key = k; decaps key = fail ? s : k' (constant-time select)
+__global__ void __launch_bounds__(128) fr_post(int n, const uint8_t *ct, uint8_t *scratch, const uint8_t *sk, uint8_t *ss) {
+    FR_WARP_INSTANCE;
+    uint8_t *scr = scratch + (size_t)x * SCRATCH;
     const uint2 *k = reinterpret_cast<const uint2 *>(scr + NOISE_U16 * 2);
-    uint2 key[3];
-    if (sk) {
-        const uint32_t mask = 0u - (uint32_t)(scr[NOISE_U16 * 2 + 64] != 0);
-        const uint2 *s = reinterpret_cast<const uint2 *>(sk + (size_t)x * SKB);
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-            key[i] = make_uint2(k[i].x ^ (mask & (k[i].x ^ s[i].x)), k[i].y ^ (mask & (k[i].y ^ s[i].y)));
-    } else {
-#pragma unroll
-        for (int i = 0; i < 3; i++) key[i] = k[i];
+    uint2 *key = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2 + 72);
+    if (w.lane < 3) {
+        uint2 kv = k[w.lane];
+        if (sk) {
+            const uint32_t mask = 0u - (uint32_t)(scr[NOISE_U16 * 2 + 64] != 0);
+            const uint2 sv = reinterpret_cast<const uint2 *>(sk + (size_t)x * SKB)[w.lane];
+            kv = make_uint2(kv.x ^ (mask & (kv.x ^ sv.x)), kv.y ^ (mask & (kv.y ^ sv.y)));
+        }
+        key[w.lane] = kv;
     }
-    uint2 A[25];
-    absorb2<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(ct + (size_t)x * CTB), CTB / 8, key, 3, DOM_SHAKE);
-    keccak_f1600(A);
-    uint2 *o = reinterpret_cast<uint2 *>(ss + (size_t)x * SSB);
-    o[0] = A[0];
-    o[1] = A[1];
-    o[2] = A[2];
+    __syncwarp();
+    uint2 a;
+    warp_absorb2<SHAKE256_LANES>(a, reinterpret_cast<const uint2 *>(ct + (size_t)x * CTB), CTB / 8, key, 3, DOM_SHAKE, w);
+    keccak_f1600_warp(a, w);
+    if (w.lane < 3) reinterpret_cast<uint2 *>(ss + (size_t)x * SSB)[w.lane] = a;
 }
 
 // keypair epilogue: sk = s || pk || S (u16 LE, S[k*N + j]) || SHAKE256(pk, 24)
-__global__ void __launch_bounds__(32) fr_kp_post(int n, const uint8_t *coins, int cstride, const uint8_t *pk,
-                                                 const uint8_t *scratch, uint8_t *sk) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= n) return;
+__global__ void __launch_bounds__(128) fr_kp_post(int n, const uint8_t *coins, int cstride, const uint8_t *pk,
+                                                  const uint8_t *scratch, uint8_t *sk) {
+    FR_WARP_INSTANCE;
     uint8_t *s = sk + (size_t)x * SKB;
     const uint8_t *p = pk + (size_t)x * PKB;
     const uint16_t *St = reinterpret_cast<const uint16_t *>(scratch + (size_t)x * SCRATCH);
-    for (int i = 0; i < 3; i++)
-        reinterpret_cast<uint2 *>(s)[i] = reinterpret_cast<const uint2 *>(coins + (size_t)x * cstride)[i];
-    for (int i = 0; i < PKB / 8; i++) reinterpret_cast<uint2 *>(s + SSB)[i] = reinterpret_cast<const uint2 *>(p)[i];
+    if (w.lane < 3) reinterpret_cast<uint2 *>(s)[w.lane] = reinterpret_cast<const uint2 *>(coins + (size_t)x * cstride)[w.lane];
+    for (int i = w.lane; i < PKB / 8; i += 32) reinterpret_cast<uint2 *>(s + SSB)[i] = reinterpret_cast<const uint2 *>(p)[i];
     uint16_t *dS = reinterpret_cast<uint16_t *>(s + SSB + PKB);
-    for (int k = 0; k < NB; k++)
-        for (int j = 0; j < N; j++) dS[k * N + j] = St[j * NB + k];
-    uint2 A[25];
-    keccak_absorb_lanes<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(p), PKB / 8, DOM_SHAKE);
-    keccak_f1600(A);
-    uint2 *h = reinterpret_cast<uint2 *>(s + SSB + PKB + C1B);
-    h[0] = A[0];
-    h[1] = A[1];
-    h[2] = A[2];
+    for (int e = w.lane; e < N * NB; e += 32) {
+        const int k = e / N, j = e % N;
+        dS[e] = St[j * NB + k];
+    }
+    uint2 a;
+    warp_absorb2<SHAKE256_LANES>(a, reinterpret_cast<const uint2 *>(p), PKB / 8, nullptr, 0, DOM_SHAKE, w);
+    keccak_f1600_warp(a, w);
+    if (w.lane < 3) reinterpret_cast<uint2 *>(s + SSB + PKB + C1B)[w.lane] = a;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -477,9 +411,9 @@ size_t frodo_scratch_bytes() { return SCRATCH; }
 
 int frodo_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
                       cudaStream_t st) {
-    PQC_LAUNCH(st, "fr_kp_pre", 976, 0, fr_kp_pre<<<(n + 15) / 16, 16, 0, st>>>(n, coins, cstride, pk, scratch));
+    PQC_LAUNCH(st, "fr_kp_pre", 976, 0, fr_kp_pre<<<(n + 3) / 4, 128, 0, st>>>(n, coins, cstride, pk, scratch));
     PQC_LAUNCH(st, "fr_kp_core", 976, 0, fr_kp_core<<<dim3((N + 255) / 256, n), 256, 0, st>>>(n, pk, scratch));
-    PQC_LAUNCH(st, "fr_kp_post", 976, 0, fr_kp_post<<<(n + 15) / 16, 16, 0, st>>>(n, coins, cstride, pk, scratch, sk));
+    PQC_LAUNCH(st, "fr_kp_post", 976, 0, fr_kp_post<<<(n + 3) / 4, 128, 0, st>>>(n, coins, cstride, pk, scratch, sk));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
@@ -489,9 +423,9 @@ int frodo_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint
     if (!capturing() &&
         cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return PQCGPU_ECUDA;
-    PQC_LAUNCH(st, "fr_enc_pre", 976, 0, fr_enc_pre<<<(n + 15) / 16, 16, 0, st>>>(n, pk, mu, scratch));
+    PQC_LAUNCH(st, "fr_enc_pre", 976, 0, fr_enc_pre<<<(n + 3) / 4, 128, 0, st>>>(n, pk, mu, scratch));
     PQC_LAUNCH(st, "fr_sa_core", 976, 0, fr_sa_core<<<n, SA_THREADS, sm, st>>>(n, ct, nullptr, pk, PKB, scratch));
-    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 15) / 16, 16, 0, st>>>(n, ct, scratch, nullptr, ss));
+    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, nullptr, ss));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
@@ -501,10 +435,10 @@ int frodo_dec_dev(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint
         cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return PQCGPU_ECUDA;
     PQC_LAUNCH(st, "fr_dec_w", 976, 0, fr_dec_w<<<n, 256, 0, st>>>(n, ct, sk, scratch));
-    PQC_LAUNCH(st, "fr_dec_pre", 976, 0, fr_dec_pre<<<(n + 15) / 16, 16, 0, st>>>(n, sk, scratch));
+    PQC_LAUNCH(st, "fr_dec_pre", 976, 0, fr_dec_pre<<<(n + 3) / 4, 128, 0, st>>>(n, sk, scratch));
     PQC_LAUNCH(st, "fr_sa_core", 976, 0,
                fr_sa_core<<<n, SA_THREADS, sm, st>>>(n, nullptr, ct, sk + SSB, SKB, scratch));
-    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 15) / 16, 16, 0, st>>>(n, ct, scratch, sk, ss));
+    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, sk, ss));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 

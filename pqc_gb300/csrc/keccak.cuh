@@ -149,3 +149,83 @@ constexpr uint32_t DOM_SHAKE = 0x1F;
 constexpr uint32_t DOM_SHA3 = 0x06;
 
 }  // namespace pqc
+
+// ---------------------------------------------------------------------------------------------
+// One Keccak state spread over a warp: lane l < 25 holds state lane l (x = l % 5, y = l / 5).
+// For long serial sponges (FrodoKEM's noise stream, G1 over a 15.6 KB key, F over a 15.7 KB
+// ciphertext) the permutation's latency, not its throughput, bounds the batch: spreading the
+// state over 25 lanes cuts the instructions on the critical path about six-fold, and message
+// lanes are loaded (and output lanes stored) by consecutive threads.
+// ---------------------------------------------------------------------------------------------
+namespace pqc {
+
+__device__ __forceinline__ uint2 shfl2(uint2 v, int src) {
+    return make_uint2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+// rotate-left by a per-lane amount n in [0, 63]
+__device__ __forceinline__ uint2 rotl64_var(uint2 v, int n) {
+    const bool sw = n >= 32;
+    const uint32_t lo = sw ? v.y : v.x, hi = sw ? v.x : v.y;
+    n &= 31;
+    return make_uint2(__funnelshift_l(hi, lo, n), __funnelshift_l(lo, hi, n));
+}
+
+struct WarpKeccak {
+    int lane, rho, src_pi, col0, col1, col2, col3, xm1, xp1, xp2;
+    __device__ __forceinline__ explicit WarpKeccak(int ln) {
+        lane = ln;
+        const int l = ln < 25 ? ln : 0;  // lanes 25..31 mirror lane 0; their values are never read
+        const int x = l % 5, y = l / 5;
+        constexpr int R[25] = {0, 1, 62, 28, 27, 36, 44, 6, 55, 20, 3, 10, 43, 25, 39,
+                               41, 45, 15, 21, 8, 18, 2, 61, 56, 14};
+        int r = 0;
+#pragma unroll
+        for (int i = 0; i < 25; i++)
+            if (i == l) r = R[i];
+        rho = r;
+        src_pi = (x + 3 * y) % 5 + 5 * x;  // pi: lane (X, Y) takes A[(X + 3Y) % 5][X]
+        col0 = x + 5 * ((y + 1) % 5);
+        col1 = x + 5 * ((y + 2) % 5);
+        col2 = x + 5 * ((y + 3) % 5);
+        col3 = x + 5 * ((y + 4) % 5);
+        xm1 = (x + 4) % 5 + 5 * y;
+        xp1 = (x + 1) % 5 + 5 * y;
+        xp2 = (x + 2) % 5 + 5 * y;
+    }
+};
+
+__device__ __forceinline__ void keccak_f1600_warp(uint2 &a, const WarpKeccak &w) {
+#pragma unroll 1
+    for (int r = 0; r < 24; r++) {
+        uint2 c = xor2(xor2(a, shfl2(a, w.col0)), xor2(shfl2(a, w.col1), xor2(shfl2(a, w.col2), shfl2(a, w.col3))));
+        const uint2 cm = shfl2(c, w.xm1), cp = shfl2(c, w.xp1);
+        a = xor2(a, xor2(cm, rotl64(cp, 1)));
+        a = rotl64_var(a, w.rho);
+        const uint2 b = shfl2(a, w.src_pi);
+        const uint2 b1 = shfl2(b, w.xp1), b2 = shfl2(b, w.xp2);
+        a.x = lop3_chi(b.x, b1.x, b2.x);
+        a.y = lop3_chi(b.y, b1.y, b2.y);
+        if (w.lane == 0) a = xor2(a, c_keccak_rc[r]);
+    }
+}
+
+// Absorb the concatenation of two lane-aligned messages (n1 + n2 lanes) into a fresh warp state,
+// with pad10*1 and domain byte `dom`; the final permutation is left to the caller.
+template <int R>
+__device__ __forceinline__ void warp_absorb2(uint2 &a, const uint2 *p1, int n1, const uint2 *p2, int n2, uint32_t dom,
+                                             const WarpKeccak &w) {
+    a = make_uint2(0, 0);
+    const int total = n1 + n2;
+    int done = 0;
+    for (; total - done >= R; done += R) {
+        const int i = done + w.lane;
+        if (w.lane < R) a = xor2(a, i < n1 ? p1[i] : p2[i - n1]);
+        keccak_f1600_warp(a, w);
+    }
+    const int i = done + w.lane;
+    if (w.lane < total - done) a = xor2(a, i < n1 ? p1[i] : p2[i - n1]);
+    if (w.lane == total - done) a.x ^= dom;
+    if (w.lane == R - 1) a.y ^= 0x80000000u;
+}
+
+}  // namespace pqc

@@ -108,7 +108,10 @@ struct pqcgpu_server {
     KeyStore ks[PQCGPU_NUM_ALGS];
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::deque<Req *> queue;
+    // one FIFO per (algorithm, operation); the dispatcher serves the group with the oldest head
+    std::deque<Req *> groups[PQCGPU_NUM_ALGS][3];
+    size_t pending = 0;
+    int heavy_running = 0;  // in-flight FrodoKEM batches (may hold at most half of the slots)
     std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
     uint64_t next_ticket = 1;
     bool stop = false;
@@ -196,6 +199,7 @@ struct pqcgpu_server {
             }
             s.reqs.clear();
             s.busy = false;
+            if (s.alg == PQCGPU_FRODO976) heavy_running--;
             batches++;
             cv_done.notify_all();
         }
@@ -204,7 +208,7 @@ struct pqcgpu_server {
 
     // Form and launch one batch on a free slot; returns false if nothing was launched.
     bool launch_one(std::unique_lock<std::mutex> &lk) {
-        if (queue.empty()) return false;
+        if (!pending) return false;
         Slot *slot = nullptr;
         for (auto &s : slots)
             if (!s.busy) {
@@ -212,18 +216,30 @@ struct pqcgpu_server {
                 break;
             }
         if (!slot) return false;
-        const int alg = queue.front()->r.alg, op = queue.front()->r.op;
-        // FrodoKEM instances cost ~10^4 Keccak permutations each: cap its batches for latency
+        // oldest group head; FrodoKEM (heavy: ~10^4 Keccak permutations per instance) may hold at
+        // most half of the slots so that the light algorithms always find one
+        const int heavy_max = std::max(1, max_inflight / 2);
+        int alg = -1, op = -1;
+        Clock::time_point oldest;
+        for (int a = 0; a < PQCGPU_NUM_ALGS; a++)
+            for (int o = 0; o < 3; o++) {
+                auto &g = groups[a][o];
+                if (g.empty() || (a == PQCGPU_FRODO976 && heavy_running >= heavy_max)) continue;
+                if (alg < 0 || g.front()->t0 < oldest) {
+                    alg = a;
+                    op = o;
+                    oldest = g.front()->t0;
+                }
+            }
+        if (alg < 0) return false;
         const int cap = (alg == PQCGPU_FRODO976) ? std::min(max_batch, 256) : max_batch;
         std::vector<Req *> take;
-        for (auto it = queue.begin(); it != queue.end() && (int)take.size() < cap;) {
-            if ((*it)->r.alg == alg && (*it)->r.op == op) {
-                take.push_back(*it);
-                it = queue.erase(it);
-            } else {
-                ++it;
-            }
+        auto &grp = groups[alg][op];
+        while (!grp.empty() && (int)take.size() < cap) {
+            take.push_back(grp.front());
+            grp.pop_front();
         }
+        pending -= take.size();
         size_t sz[4];
         op_io_sizes(alg, op, sz);
         const size_t scr = op_scratch_bytes(alg, op, 0);
@@ -280,8 +296,12 @@ struct pqcgpu_server {
                         k.used[q->key_slot] = 0;
                         k.free_slots.push_back(q->key_slot);
                     }
-                    if (others) queue.push_front(q);  // wait for in-flight batches to free memory
-                    else finish(q, PQCGPU_EBUDGET, 0);  // nothing will free memory: refuse
+                    if (others) {  // wait for in-flight batches to free memory
+                        groups[alg][op].push_front(q);
+                        pending++;
+                    } else {
+                        finish(q, PQCGPU_EBUDGET, 0);  // nothing will free memory: refuse
+                    }
                 }
                 if (!others) cv_done.notify_all();
                 return !others;
@@ -325,6 +345,7 @@ struct pqcgpu_server {
         s.n = n;
         s.reqs = ok;
         s.busy = true;
+        if (alg == PQCGPU_FRODO976) heavy_running++;
         lk.unlock();
         // device work on the slot stream
         cudaStream_t st = s.stream;
@@ -364,13 +385,13 @@ struct pqcgpu_server {
             while (launch_one(lk)) launched = true;
             bool any_busy = false;
             for (auto &s : slots) any_busy |= s.busy;
-            if (stop && queue.empty() && !any_busy) break;
+            if (stop && !pending && !any_busy) break;
             if (!launched) {
                 if (any_busy) {
                     // poll the in-flight batches; new requests wake us immediately
                     cv_work.wait_for(lk, std::chrono::microseconds(20));
                 } else {
-                    cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+                    cv_work.wait(lk, [&] { return stop || pending; });
                 }
             }
         }
@@ -425,7 +446,8 @@ extern "C" int pqcgpu_server_submit(pqcgpu_server *s, const pqcgpu_request *req,
         if (s->stop) return set_error(PQCGPU_EINVAL, "server is shutting down");
         raw->ticket = s->next_ticket++;
         s->reqs[raw->ticket] = std::move(q);
-        s->queue.push_back(raw);
+        s->groups[req->alg][req->op].push_back(raw);
+        s->pending++;
     }
     s->cv_work.notify_one();
     if (ticket) *ticket = raw->ticket;
@@ -450,7 +472,7 @@ extern "C" int pqcgpu_server_drain(pqcgpu_server *s) {
     if (!s) return PQCGPU_EINVAL;
     std::unique_lock<std::mutex> lk(s->mu);
     s->cv_done.wait(lk, [&] {
-        if (!s->queue.empty()) return false;
+        if (s->pending) return false;
         for (auto &sl : s->slots)
             if (sl.busy) return false;
         return true;
