@@ -5,8 +5,8 @@ namespace pqc {
 namespace kyber {
 // Launch shape of the core kernels, [op][k-2] with op 0 keypair, 1 enc, 2 dec.  One thread per
 // matrix entry (NI * k^2 jobs) sized against the shared memory each instance needs.
-int g_ni[3][3] = {{16, 14, 8}, {32, 20, 12}, {32, 20, 14}};
-int g_threads[3][3] = {{64, 160, 128}, {128, 192, 192}, {128, 192, 256}};
+int g_ni[3][3] = {{16, 14, 8}, {24, 14, 14}, {24, 14, 14}};
+int g_threads[3][3] = {{64, 160, 128}, {128, 128, 256}, {128, 160, 256}};
 
 #define PQC_KYBER_DECL(K, V)                                                                               \
     int keypair_##K##_##V(int, uint8_t *, uint8_t *, const uint8_t *, int, int, uint8_t *, int, cudaStream_t); \

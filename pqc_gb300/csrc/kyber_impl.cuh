@@ -316,18 +316,25 @@ struct DecArgs {
     int kem;
 };
 
-// Shared-memory layout for a CTA of NI instances: twiddles, NPOLY polynomials per instance, and
-// 128 bytes of per-instance seeds / flags.
-template <int NPOLY>
+// Shared-memory layout for a CTA of NI instances: twiddles, NPOLY polynomials per instance,
+// SEEDB bytes of per-instance seeds / flags / noise bytes, and the per-thread staging areas.
+template <int NPOLY, int SEEDB>
 struct Layout {
     static __host__ __device__ constexpr size_t bytes(int ni, int threads) {
-        return 2 * 128 * sizeof(int16_t) + (size_t)ni * NPOLY * POLY_PITCH * sizeof(int16_t) + (size_t)ni * 128 +
+        return 2 * 128 * sizeof(int16_t) + (size_t)ni * NPOLY * POLY_PITCH * sizeof(int16_t) + (size_t)ni * SEEDB +
                (size_t)threads * STAGE_INT16 * sizeof(int16_t);
     }
 };
 // Per-thread staging area (after the seeds block).
+template <int SEEDB>
 __device__ __forceinline__ int16_t *stage_of(uint8_t *seeds, int ni) {
-    return reinterpret_cast<int16_t *>(seeds + (size_t)ni * 128) + (size_t)threadIdx.x * STAGE_INT16;
+    return reinterpret_cast<int16_t *>(seeds + (size_t)ni * SEEDB) + (size_t)threadIdx.x * STAGE_INT16;
+}
+// Encryption seed block per instance: [0,32) m, [32,64) r, [64,96) K-bar, [96] flag, then the
+// 128-byte PRF outputs of the K + 1 error polynomials e1_0..e1_{K-1}, e2 (eta2 = 2).
+template <int K>
+__host__ __device__ constexpr int enc_seed_bytes() {
+    return 128 + 128 * (K + 1);
 }
 
 __device__ __forceinline__ void load_twiddles(int16_t *sz, int16_t *szi) {
@@ -364,21 +371,31 @@ __device__ __forceinline__ int16_t *slot(int16_t *polys, int li, int s) {
     return polys + ((size_t)li * (2 * K + 1) + s) * POLY_PITCH;
 }
 
-// Per-instance shared seed block (128 B): [0,32) m, [32,64) r / K-bar, [64,96) rho / z, [96] flag
 template <int K, int V, bool DEC>
 __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz, const int16_t *szi, int ni,
                                int ni_alloc, int base, const EncArgs &a, const uint8_t *ct_cmp) {
     using Pp = P<K, V>;
+    constexpr int SB = enc_seed_bytes<K>();
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
 
-    // (1) r = CBD_eta1(PRF(coins, i)), i < K  -> slots [0, K); zero the u accumulators
+    // (1) all 2K + 1 PRF permutations: r_i = CBD_eta1(PRF(coins, i)) -> slots [0, K); the error
+    //     polynomials' PRF(coins, K + i) output bytes -> seed block (CBD applied in (5));
+    //     zero the u accumulators
     for (int li = 0; li < ni; li++) zero_polys(slot<K, V>(polys, li, K), K);
-    for (int job = tid; job < ni * K; job += nthr) {
-        const int li = job / K, i = job % K;
-        const uint2 *seed = DEC ? reinterpret_cast<const uint2 *>(seeds + li * 128 + 32)
+    for (int job = tid; job < ni * (2 * K + 1); job += nthr) {
+        const int li = job / (2 * K + 1), i = job % (2 * K + 1);
+        const uint2 *seed = DEC ? reinterpret_cast<const uint2 *>(seeds + li * SB + 32)
                                 : reinterpret_cast<const uint2 *>(a.r + (size_t)(base + li) * a.r_stride);
-        int16_t *dst = slot<K, V>(polys, li, i);
-        noise_poly<Pp::ETA1>(seed, i, [&](int g, const int16_t(&c)[8]) { store8(dst + phys(8 * g), c); });
+        if (i < K) {
+            int16_t *dst = slot<K, V>(polys, li, i);
+            noise_poly<Pp::ETA1>(seed, i, [&](int g, const int16_t(&c)[8]) { store8(dst + phys(8 * g), c); });
+        } else {
+            uint2 A[25];
+            prf_absorb(A, seed, i);  // nonce K + (i - K) = i
+            uint4 *o = reinterpret_cast<uint4 *>(seeds + li * SB + 128 + 128 * (i - K));
+#pragma unroll
+            for (int q = 0; q < 8; q++) o[q] = make_uint4(A[2 * q].x, A[2 * q].y, A[2 * q + 1].x, A[2 * q + 1].y);
+        }
     }
     __syncthreads();
     // (2) r-hat = NTT(r)
@@ -389,9 +406,9 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
         const int li = job / (K * K), i = (job / K) % K, j = job % K;
         const uint8_t *pk = a.pk + (size_t)(base + li) * a.pk_stride;
         matrix_entry<V>(reinterpret_cast<const uint2 *>(pk + Pp::POLYVECBYTES), i, j, true, slot<K, V>(polys, li, j),
-                        slot<K, V>(polys, li, K + i), sz, stage_of(seeds, ni_alloc));
+                        slot<K, V>(polys, li, K + i), sz, stage_of<SB>(seeds, ni_alloc));
     }
-    // (4) v = t-hat o r-hat (warp per instance, t-hat decoded from pk bytes; independent of (3))
+    //     v = t-hat o r-hat (warp per instance, t-hat decoded from pk bytes; independent of (3))
     for (int li = warp; li < ni; li += nwarp) {
         const uint8_t *pk = a.pk + (size_t)(base + li) * a.pk_stride;
         int16_t acc[8];
@@ -410,7 +427,7 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
         store8(slot<K, V>(polys, li, 2 * K) + phys(8 * lane), acc);
     }
     __syncthreads();
-    // (5) inverse NTT of u (K, accumulators unbiased + reduced on load) and v
+    // (4) inverse NTT of u (K, accumulators unbiased + reduced on load) and v
     for (int w = warp; w < ni * (K + 1); w += nwarp) {
         int16_t *p = slot<K, V>(polys, w / (K + 1), K + w % (K + 1));
         if (w % (K + 1) < K) {
@@ -424,43 +441,33 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
         invntt_warp(p, szi, lane);
     }
     __syncthreads();
-    // (6) u += e1 (nonce K+i, eta2); v += e2 (nonce 2K) + msg; Barrett; compress in place
-    for (int job = tid; job < ni * (K + 1); job += nthr) {
-        const int li = job / (K + 1), i = job % (K + 1);
-        const uint2 *seed = DEC ? reinterpret_cast<const uint2 *>(seeds + li * 128 + 32)
-                                : reinterpret_cast<const uint2 *>(a.r + (size_t)(base + li) * a.r_stride);
-        const uint8_t *msg = DEC ? seeds + li * 128 : a.m + (size_t)(base + li) * a.m_stride;
-        int16_t *dst = slot<K, V>(polys, li, K + i);
-        const bool isv = (i == K);
-        noise_poly<Pp::ETA2>(seed, K + i, [&](int g, const int16_t(&e)[8]) {
-            int16_t c[8];
-            load8(c, dst + phys(8 * g));
-            const uint8_t mb = isv ? msg[g] : 0;
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-                int16_t x = (int16_t)(c[q] + e[q]);
-                if (isv) x = (int16_t)(x + (int16_t)(((mb >> q) & 1) ? (Q + 1) / 2 : 0));
-                x = csubq(barrett(x));
-                c[q] = (int16_t)(isv ? compress_d<Pp::DV>(x) : compress_d<Pp::DU>(x));
-            }
-            store8(dst + phys(8 * g), c);
-        });
-    }
-    __syncthreads();
-    // (7) pack (encaps) or compare against the received ciphertext (decaps), warp per instance
+    // (5) warp per instance, lane = 8 coefficients: u += e1, v += e2 + msg (CBD_eta2 of the stored
+    //     PRF bytes, cbd.cu:42-63), Barrett, compress, and pack (encaps) or compare with the
+    //     received ciphertext (decaps)
     for (int li = warp; li < ni; li += nwarp) {
         uint8_t *out = DEC ? nullptr : a.ct + (size_t)(base + li) * Pp::CTB;
         const uint8_t *cmp = DEC ? ct_cmp + (size_t)(base + li) * Pp::CTB : nullptr;
+        const uint8_t *msg = DEC ? seeds + li * SB : a.m + (size_t)(base + li) * a.m_stride;
+        const uint8_t mb = msg[lane];
         uint32_t diff = 0;
         for (int i = 0; i <= K; i++) {
+            const uint32_t t = reinterpret_cast<const uint32_t *>(seeds + li * SB + 128 + 128 * i)[lane];
+            uint32_t d = t & 0x55555555u;
+            d += (t >> 1) & 0x55555555u;
             int16_t c[8];
             load8(c, slot<K, V>(polys, li, K + i) + phys(8 * lane));
-            uint32_t t[8];
+            uint32_t cv[8];
 #pragma unroll
-            for (int q = 0; q < 8; q++) t[q] = (uint16_t)c[q];
+            for (int q = 0; q < 8; q++) {
+                const int16_t e = (int16_t)((int)((d >> (4 * q)) & 3) - (int)((d >> (4 * q + 2)) & 3));
+                int16_t x = (int16_t)(c[q] + e);
+                if (i == K) x = (int16_t)(x + (int16_t)(((mb >> q) & 1) ? (Q + 1) / 2 : 0));
+                x = csubq(barrett(x));
+                cv[q] = (i < K) ? compress_d<Pp::DU>(x) : compress_d<Pp::DV>(x);
+            }
             if (i < K) {
                 uint8_t b[Pp::DU];
-                pack8<Pp::DU>(b, t);
+                pack8<Pp::DU>(b, cv);
                 const size_t off = (size_t)i * Pp::DU * 32 + (size_t)lane * Pp::DU;
 #pragma unroll
                 for (int q = 0; q < Pp::DU; q++) {
@@ -469,7 +476,7 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
                 }
             } else {
                 uint8_t b[Pp::DV];
-                pack8<Pp::DV>(b, t);
+                pack8<Pp::DV>(b, cv);
                 const size_t off = (size_t)Pp::CTU + (size_t)lane * Pp::DV;
 #pragma unroll
                 for (int q = 0; q < Pp::DV; q++) {
@@ -480,7 +487,7 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
         }
         if (DEC) {
             diff = __any_sync(0xffffffffu, diff != 0);
-            if (lane == 0) seeds[li * 128 + 96] = (uint8_t)diff;
+            if (lane == 0) seeds[li * SB + 96] = (uint8_t)diff;
         }
     }
 }
@@ -493,6 +500,7 @@ constexpr int CORE_MAX_THREADS = 512;
 
 template <int K, int V>
 __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_enc_core(EncArgs a, int NI) {
+
     extern __shared__ __align__(16) uint8_t smem[];
     int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
     uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (2 * K + 1) * POLY_PITCH);
@@ -506,6 +514,7 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_enc_core(EncArgs a, in
 template <int K, int V>
 __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, int NI) {
     using Pp = P<K, V>;
+    constexpr int SB = enc_seed_bytes<K>();
     extern __shared__ __align__(16) uint8_t smem[];
     int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
     uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (2 * K + 1) * POLY_PITCH);
@@ -568,7 +577,7 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, in
             const int16_t x = csubq(barrett((int16_t)(v[q] - mp[q])));
             byte |= (((((uint32_t)x << 1) + Q / 2) / Q) & 1) << q;
         }
-        seeds[li * 128 + lane] = (uint8_t)byte;
+        seeds[li * SB + lane] = (uint8_t)byte;
         if (!d.kem) d.m_out[(size_t)(base + li) * 32 + lane] = (uint8_t)byte;
     }
     if (!d.kem) return;
@@ -578,7 +587,7 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, in
         const uint8_t *sk = d.sk + (size_t)(base + li) * Pp::SKB;
         uint2 A[25];
         keccak_zero(A);
-        const uint2 *m2 = reinterpret_cast<const uint2 *>(seeds + li * 128);
+        const uint2 *m2 = reinterpret_cast<const uint2 *>(seeds + li * SB);
         const uint2 *h2 = reinterpret_cast<const uint2 *>(sk + Pp::SKB - 64);
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -588,7 +597,7 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, in
         A[8].x ^= DOM_SHA3;
         A[SHA3_512_LANES - 1].y ^= 0x80000000u;
         keccak_f1600(A);
-        uint2 *kb = reinterpret_cast<uint2 *>(seeds + li * 128 + 64), *rr = reinterpret_cast<uint2 *>(seeds + li * 128 + 32);
+        uint2 *kb = reinterpret_cast<uint2 *>(seeds + li * SB + 64), *rr = reinterpret_cast<uint2 *>(seeds + li * SB + 32);
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             kb[i] = A[i];
@@ -611,8 +620,8 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, in
     // (g) ss = SHAKE256(fail ? z : K-bar' || H(c)), with a constant-time select
     for (int li = tid; li < ni; li += nthr) {
         const uint8_t *sk = d.sk + (size_t)(base + li) * Pp::SKB;
-        const uint32_t mask = 0u - (uint32_t)(seeds[li * 128 + 96] != 0);
-        const uint2 *kb = reinterpret_cast<const uint2 *>(seeds + li * 128 + 64);
+        const uint32_t mask = 0u - (uint32_t)(seeds[li * SB + 96] != 0);
+        const uint2 *kb = reinterpret_cast<const uint2 *>(seeds + li * SB + 64);
         const uint2 *z = reinterpret_cast<const uint2 *>(sk + Pp::SKB - 32);
         const uint2 *hc = reinterpret_cast<const uint2 *>(d.hct + (size_t)(base + li) * 32);
         uint2 A[25];
@@ -674,7 +683,7 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int 
     for (int job = tid; job < ni * K * K; job += nthr) {
         const int li = job / (K * K), i = (job / K) % K, j = job % K;
         matrix_entry<V>(reinterpret_cast<const uint2 *>(seeds + li * 128), i, j, false, kslot(li, j), kslot(li, 2 * K + i),
-                        sz, stage_of(seeds, NI));
+                        sz, stage_of<128>(seeds, NI));
     }
     __syncthreads();
     // (d) t = reduce(frommont(t) + e); pack pk = t || rho and sk_cpa = s (warp per instance)
@@ -818,7 +827,7 @@ static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins,
                           uint8_t *scratch, int plain, cudaStream_t st) {
     if (plain) return kem ? plain_keypair<K, V>(n, pk, sk, coins, coins_stride, scratch, st) : PQCGPU_EUNSUPPORTED;
     const int NI = g_ni[0][K - 2], NT = g_threads[0][K - 2];
-    const size_t sm = Layout<3 * K>::bytes(NI, NT);
+    const size_t sm = Layout<3 * K, 128>::bytes(NI, NT);
     if (ensure_smem(kyber_kp_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     KpArgs a{n, pk, sk, coins, coins_stride, kem};
     PQC_LAUNCH(st, "kyber_kp_core", K, V, kyber_kp_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
@@ -831,7 +840,7 @@ static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const 
                       uint8_t *scratch, int kem, int plain, cudaStream_t st) {
     if (plain) return kem ? plain_enc<K, V>(n, ct, ss, pk, coins, scratch, st) : PQCGPU_EUNSUPPORTED;
     const int NI = g_ni[1][K - 2], NT = g_threads[1][K - 2];
-    const size_t sm = Layout<2 * K + 1>::bytes(NI, NT);
+    const size_t sm = Layout<2 * K + 1, enc_seed_bytes<K>()>::bytes(NI, NT);
     if (ensure_smem(kyber_enc_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     EncArgs a;
     a.n = n;
@@ -863,7 +872,7 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
                       int plain, cudaStream_t st) {
     if (plain) return kem ? plain_dec<K, V>(n, out, ct, sk, scratch, st) : PQCGPU_EUNSUPPORTED;
     const int NI = g_ni[2][K - 2], NT = g_threads[2][K - 2];
-    const size_t sm = Layout<2 * K + 1>::bytes(NI, NT);
+    const size_t sm = Layout<2 * K + 1, enc_seed_bytes<K>()>::bytes(NI, NT);
     if (ensure_smem(kyber_dec_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     DecArgs d;
     d.n = n;
