@@ -53,7 +53,7 @@ def parse():
     p.add_argument("--no-plain", action="store_true", help="skip timing the plain path beside the fused one")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--config", default=None,
-                   choices=["kyber512", "newhope1024", "frodo976", "mixed", "serving", "all"],
+                   choices=["kyber512", "newhope1024", "frodo976", "mixed", "serving", "refgpu", "all"],
                    help="measure another configuration (extra JSON lines) instead of the headline")
     return p.parse_args()
 
@@ -205,7 +205,8 @@ def run_configs(args):
     ctx = kem.Context(0)
     st = torch.cuda.ExternalStream(ctx.stream, device=dev)
     up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
-    which = ["kyber512", "newhope1024", "frodo976", "mixed", "serving"] if args.config == "all" else [args.config]
+    which = (["kyber512", "newhope1024", "frodo976", "mixed", "serving", "refgpu"] if args.config == "all"
+             else [args.config])
 
     def timed(fn, reps):
         fn()
@@ -286,6 +287,8 @@ def run_configs(args):
                               "graph_replay_per_s": total / t_graph * 1e3, "sequential_per_s": total / t_seq * 1e3,
                               "mix": "k=2/3/4 at 40/40/20, n ~ U{1..65536}, ops 1/3 each",
                               "bit_exact_decaps": bool(ok)}), flush=True)
+        elif cfg == "refgpu":
+            run_refgpu(ctx, dev, up, timed)
         elif cfg == "serving":
             from pqc_gb300 import serve
             with serve.Server(0, budget=16 << 30, max_inflight=8, max_batch=4096) as srv:
@@ -294,14 +297,86 @@ def run_configs(args):
                 points = []
                 for frac in (0.1, 0.3, 0.5, 0.7, 0.9):
                     r = srv.run_poisson(serve.SERVING_MIX, rate=frac * peak, seconds=1.5, seed=int(frac * 100))
+                    groups = {"%s/%s" % (alg, op): srv.group_stats(alg, op) for alg, op, _ in serve.SERVING_MIX}
                     points.append({"load": frac, "offered_per_s": r["offered_per_s"], "achieved_per_s": r["achieved_per_s"],
                                    "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "max_ms": r["max_ms"],
-                                   "batches": r["batches"]})
+                                   "batches": r["batches"],
+                                   "p99_ms_by_group": {g: round(v["p99_ms"], 3) for g, v in groups.items()},
+                                   "p50_ms_by_group": {g: round(v["p50_ms"], 3) for g, v in groups.items()}})
             print(json.dumps({"config": "serving", "metric": "KEM serving latency under Poisson load",
                               "mix": "60% Kyber-512/768/1024, 20% NewHope-1024, 20% FrodoKEM-976, ops equiprobable",
                               "keys": "resident on the device", "hbm_budget_gb": 16,
                               "measured_peak_per_s": peak, "points": points}), flush=True)
     ctx.close()
+
+
+def run_refgpu(ctx, dev, up, timed):
+    """The reference's own batched Kyber kernels (round-2 CPA, k = 4 and 3) recompiled for sm_103a
+    (baseline/_ref) beside this library's fused kernels on the same GPU, same inputs, same batch
+    (the reference's maximum, N_TESTS = 16384); outputs compared byte for byte."""
+    import ctypes
+
+    import torch
+    from pqc_gb300 import drbg, kem
+    sys.path.insert(0, os.path.join(ROOT, "baseline"))
+    import refgpu
+    for k in (4, 3):
+        if not refgpu.available(k):
+            print(json.dumps({"config": "refgpu", "k": k, "unavailable": "reference kernels not built "
+                              "(baseline/build_ref_gpu.sh had no staged sources)"}), flush=True)
+            continue
+        ref = refgpu.RefGPU(k)
+        n = ref.max_count
+        cs = kem.kyber_cpa_sizes(2, k)
+        seed = drbg.seed48(31 + k)
+        d, m, coins = (up(drbg.stream(seed, lab, 32 * n)) for lab in (b"d", b"m", b"coins"))
+        rng = up(drbg.stream(seed, b"rng", 64 * n))
+        buf = lambda sz: torch.zeros(n * sz, dtype=torch.uint8, device=dev)  # noqa: E731
+        pk_r, sk_r, ct_r, m_r, pk_t, sk_t = (buf(cs[x]) if x in cs else buf(32)
+                                             for x in ("pk", "sk", "ct", "m", "pk", "sk"))
+        pk_o, sk_o, ct_o, m_o = (buf(cs[x]) if x in cs else buf(32) for x in ("pk", "sk", "ct", "m"))
+        sh = ctypes.c_void_p(ctx.stream)
+        L, F = ctx.lib, kem.DEVICE_PTRS
+        P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+        def ok(rc):
+            if rc != 0:
+                raise RuntimeError("pqcgpu call returned %d" % rc)
+
+        ours = {
+            "keypair": lambda: ok(L.pqcgpu_kyber_indcpa_keypair_batch(ctx.h, 2, k, n, P(pk_o), P(sk_o), P(d), F)),
+            "enc": lambda: ok(L.pqcgpu_kyber_indcpa_enc_batch(ctx.h, 2, k, n, P(ct_o), P(m), P(pk_o), P(coins), F)),
+            "dec": lambda: ok(L.pqcgpu_kyber_indcpa_dec_batch(ctx.h, 2, k, n, P(m_o), P(ct_o), P(sk_o), F)),
+        }
+        theirs = {
+            # indcpa_keypair as the reference runs it (its in-place G makes these keys timing-only)
+            "keypair": lambda: ref.keypair(n, pk_t, sk_t, rng, sh),
+            "enc": lambda: ref.enc(n, ct_r, m, pk_r, coins, sh),
+            "dec": lambda: ref.dec(n, m_r, ct_r, sk_r, sh),
+        }
+        torch.cuda.synchronize()
+        ref.keypair_nist(n, pk_r, sk_r, d, sh)
+        for op in ("keypair", "enc", "dec"):
+            if op != "keypair":  # the reference's keys for parity come from keypair_nist above
+                theirs[op]()
+            ours[op]()
+        ctx.wait()
+        same = {"pk": torch.equal(pk_r, pk_o), "sk": torch.equal(sk_r, sk_o), "ct": torch.equal(ct_r, ct_o),
+                "m_dec_ref": torch.equal(m_r, m), "m_dec_ours": torch.equal(m_o, m)}
+        tr = {op: timed(f, 10) for op, f in theirs.items()}
+        to = {op: timed(f, 10) for op, f in ours.items()}
+        ref.close()
+        chains = lambda t: n / (t["keypair"] + t["enc"] + t["dec"]) * 1e3  # noqa: E731
+        print(json.dumps({
+            "config": "refgpu", "metric": "Kyber round-2 CPA (k=%d) keypair+enc+dec chains/s, device-resident" % k,
+            "k": k, "batch": n,
+            "reference_kernels_sm103a": {"ms": tr, "chains_per_s": chains(tr),
+                                         "what": "Kyber_GPU_Batched indcpa_* recompiled by nvcc for sm_103a, V100 "
+                                                 "block sizes, thread per instance, intermediates in HBM"},
+            "ours_fused": {"ms": to, "chains_per_s": chains(to)},
+            "speedup": {op: tr[op] / to[op] for op in tr},
+            "speedup_chain": chains(to) / chains(tr),
+            "bit_exact": same}), flush=True)
 
 
 def main():

@@ -196,6 +196,9 @@ int pqcgpu_server_submit(pqcgpu_server *server, const pqcgpu_request *req, uint6
 int pqcgpu_server_wait(pqcgpu_server *server, uint64_t ticket, int timeout_ms);
 int pqcgpu_server_drain(pqcgpu_server *server);
 int pqcgpu_server_get_stats(pqcgpu_server *server, pqcgpu_server_stats *out, int reset);
+/* Latency of the completed requests of one (algorithm, operation) since the last reset;
+ * `completed` counts them, `batches` and `keys_resident` are 0. */
+int pqcgpu_server_get_group_stats(pqcgpu_server *server, int alg, int op, pqcgpu_server_stats *out);
 int pqcgpu_server_key_release(pqcgpu_server *server, uint64_t key);
 int pqcgpu_server_destroy(pqcgpu_server *server);
 /* Open-loop load for the serving benchmark: resident key / ciphertext pools per algorithm of the

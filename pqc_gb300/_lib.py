@@ -40,6 +40,7 @@ SIGNATURES = {
     "pqcgpu_server_wait": (_int, [_vp, _c.c_uint64, _int]),
     "pqcgpu_server_drain": (_int, [_vp]),
     "pqcgpu_server_get_stats": (_int, [_vp, _vp, _int]),
+    "pqcgpu_server_get_group_stats": (_int, [_vp, _int, _int, _vp]),
     "pqcgpu_server_key_release": (_int, [_vp, _c.c_uint64]),
     "pqcgpu_server_destroy": (_int, [_vp]),
     "pqcgpu_server_run_poisson": (_int, [_vp, _vp, _sz, _c.c_double, _c.c_double, _c.c_uint64, _vp]),

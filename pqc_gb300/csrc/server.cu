@@ -117,6 +117,7 @@ struct pqcgpu_server {
     bool stop = false;
     std::thread th;
     std::vector<double> lat_ms;
+    std::vector<double> lat_grp[PQCGPU_NUM_ALGS][3];  // the same samples per (algorithm, operation)
     uint64_t completed = 0, batches = 0;
     std::string error;
 
@@ -173,6 +174,7 @@ struct pqcgpu_server {
         q->status = status;
         if (status == 0) {
             lat_ms.push_back(ms);
+            lat_grp[q->r.alg][q->r.op].push_back(ms);
             completed++;
         }
     }
@@ -491,6 +493,19 @@ extern "C" int pqcgpu_server_key_release(pqcgpu_server *s, uint64_t key) {
     return PQCGPU_OK;
 }
 
+namespace {
+void fill_latency(std::vector<double> v, pqcgpu_server_stats *out) {
+    if (v.empty()) return;
+    std::sort(v.begin(), v.end());
+    out->p50_ms = v[v.size() / 2];
+    out->p99_ms = v[std::min(v.size() - 1, (size_t)(0.99 * v.size()))];
+    out->max_ms = v.back();
+    double sum = 0;
+    for (double x : v) sum += x;
+    out->mean_ms = sum / v.size();
+}
+}  // namespace
+
 extern "C" int pqcgpu_server_get_stats(pqcgpu_server *s, pqcgpu_server_stats *out, int reset) {
     if (!s || !out) return PQCGPU_EINVAL;
     std::lock_guard<std::mutex> lk(s->mu);
@@ -500,21 +515,24 @@ extern "C" int pqcgpu_server_get_stats(pqcgpu_server *s, pqcgpu_server_stats *ou
     out->hbm_used = s->used;
     for (auto &k : s->ks)
         for (auto u : k.used) out->keys_resident += u;
-    std::vector<double> v = s->lat_ms;
-    if (!v.empty()) {
-        std::sort(v.begin(), v.end());
-        out->p50_ms = v[v.size() / 2];
-        out->p99_ms = v[std::min(v.size() - 1, (size_t)(0.99 * v.size()))];
-        out->max_ms = v.back();
-        double sum = 0;
-        for (double x : v) sum += x;
-        out->mean_ms = sum / v.size();
-    }
+    fill_latency(s->lat_ms, out);
     if (reset) {
         s->lat_ms.clear();
+        for (auto &a : s->lat_grp)
+            for (auto &g : a) g.clear();
         s->completed = 0;
         s->batches = 0;
     }
+    return PQCGPU_OK;
+}
+
+extern "C" int pqcgpu_server_get_group_stats(pqcgpu_server *s, int alg, int op, pqcgpu_server_stats *out) {
+    if (!s || !out || alg < 0 || alg >= PQCGPU_NUM_ALGS || op < 0 || op > 2) return PQCGPU_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    memset(out, 0, sizeof *out);
+    out->completed = s->lat_grp[alg][op].size();
+    out->hbm_used = s->used;
+    fill_latency(s->lat_grp[alg][op], out);
     return PQCGPU_OK;
 }
 
@@ -644,7 +662,7 @@ extern "C" int pqcgpu_server_run_poisson(pqcgpu_server *s, const pqcgpu_mix_entr
     pqcgpu_server_drain(s);
     const auto t_end = Clock::now();
     pqcgpu_server_stats st;
-    pqcgpu_server_get_stats(s, &st, 1);
+    pqcgpu_server_get_stats(s, &st, 0);  // samples stay readable (per group too) until the next reset
     {
         // forget the tickets of the load run and release the keys it generated
         std::lock_guard<std::mutex> lk(s->mu);

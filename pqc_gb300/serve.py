@@ -91,8 +91,16 @@ class Server:
         _lib.check(self.lib.pqcgpu_server_get_stats(self.h, ctypes.byref(st), 1 if reset else 0))
         return {f: getattr(st, f) for f, _ in _lib.ServerStats._fields_}
 
+    def group_stats(self, alg, op):
+        """Latency of the completed (alg, op) requests since the last reset."""
+        st = _lib.ServerStats()
+        _lib.check(self.lib.pqcgpu_server_get_group_stats(self.h, kem.alg_id(alg), kem.OPS[op] if isinstance(op, str)
+                                                          else op, ctypes.byref(st)))
+        return {f: getattr(st, f) for f in ("completed", "p50_ms", "p99_ms", "mean_ms", "max_ms")}
+
     def run_poisson(self, mix, rate, seconds, seed=0):
-        """mix: list of (alg, op, weight).  Returns the load report as a dict."""
+        """mix: list of (alg, op, weight).  Returns the load report as a dict; the latency samples of
+        the run stay readable through stats() / group_stats() until the next reset."""
         arr = (_lib.MixEntry * len(mix))()
         for i, (alg, op, w) in enumerate(mix):
             arr[i].alg, arr[i].op, arr[i].weight = kem.alg_id(alg), kem.OPS[op] if isinstance(op, str) else op, w

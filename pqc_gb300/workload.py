@@ -1,0 +1,80 @@
+"""Fixed-size batched KEM workload on one GPU, for throughput checks and profiler captures.
+
+    python -m pqc_gb300.workload --alg kyber768 --n 16384 --reps 2
+
+Generates n key pairs once, then runs `reps` rounds of encapsulation + decapsulation of n
+instances through the C ABI with device buffers (`PQCGPU_DEVICE_PTRS`), timing each operation with
+CUDA events on the library stream.  Inputs come from the seeded SHAKE-256 DRBG, so every run of the
+same command launches the same kernels on the same data.  Exits non-zero if any decapsulated key
+differs from the encapsulated one.
+"""
+import argparse
+import sys
+
+import torch
+
+from . import drbg, kem
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--alg", default="kyber768", choices=sorted(kem.ALGS))
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--ops", default="enc,dec", help="comma list of keypair, enc, dec to repeat")
+    ap.add_argument("--plain", action="store_true", help="per-stage path instead of the fused kernels")
+    args = ap.parse_args(argv)
+
+    n, alg = args.n, args.alg
+    ctx = kem.Context(0)
+    s = kem.sizes(alg)
+    dev = torch.device("cuda:0")
+    seed = drbg.seed48(0)
+
+    def dev_bytes(label, nbytes):
+        return torch.frombuffer(bytearray(drbg.stream(seed, label, nbytes)), dtype=torch.uint8).to(dev)
+
+    kc = dev_bytes(b"kp", n * s["kp_coins"])
+    ec = dev_bytes(b"enc", n * s["enc_coins"])
+    pk = torch.empty(n * s["pk"], dtype=torch.uint8, device=dev)
+    sk = torch.empty(n * s["sk"], dtype=torch.uint8, device=dev)
+    ct = torch.empty(n * s["ct"], dtype=torch.uint8, device=dev)
+    ss = torch.empty(n * s["ss"], dtype=torch.uint8, device=dev)
+    ss2 = torch.empty_like(ss)
+    torch.cuda.synchronize()
+    fl = kem.PLAIN if args.plain else 0
+    st = torch.cuda.ExternalStream(ctx.stream)
+    ops = {
+        "keypair": lambda: ctx.keypair_dev(alg, n, pk, sk, kc, fl),
+        "enc": lambda: ctx.enc_dev(alg, n, ct, ss, pk, ec, fl),
+        "dec": lambda: ctx.dec_dev(alg, n, ss2, ct, sk, fl),
+    }
+    ops["keypair"]()
+    ctx.wait()
+    want = [o for o in args.ops.split(",") if o]
+    for o in want:
+        if o not in ops:
+            ap.error("unknown op %r" % o)
+    ok = True
+    for rep in range(args.reps):
+        line = []
+        for o in want:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            ops[o]()
+            e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            line.append("%s %.3f ms (%.2f M/s)" % (o, ms, n / ms / 1e3))
+        if "enc" in want and "dec" in want:
+            ctx.wait()
+            same = torch.equal(ss, ss2)
+            ok = ok and same
+            line.append("ss match %s" % same)
+        print("%s n=%d rep %d: %s" % (alg, n, rep, ", ".join(line)), flush=True)
+    return 0 if ok else 1
+
+
+if __name__ == "__main__":
+    sys.exit(main())
