@@ -46,7 +46,10 @@ typedef enum {
     PQCGPU_KYBER1024_R2 = 3, /* the reference's round-2 Kyber (Kyber_GPU_Batched/params.h), k=4 */
     PQCGPU_NEWHOPE1024 = 4,  /* NewHope1024-CPAKEM (NewHope_NIST_GPU) */
     PQCGPU_FRODO976 = 5,     /* FrodoKEM-976, SHAKE (FrodoKEM_GPU) */
-    PQCGPU_NUM_ALGS = 6
+    PQCGPU_MLKEM512 = 6,     /* ML-KEM-512 (FIPS 203): round-3 Kyber-512 K-PKE with G(d || k), K direct, */
+    PQCGPU_MLKEM768 = 7,     /*   rejection key J(z || c); same sizes as the round-3 sets.  The FIPS 203 */
+    PQCGPU_MLKEM1024 = 8,    /*   input checks (ek modulus, dk hash) are left to the caller. */
+    PQCGPU_NUM_ALGS = 9
 } pqcgpu_alg;
 
 typedef enum {
@@ -210,7 +213,9 @@ int pqcgpu_server_run_poisson(pqcgpu_server *server, const pqcgpu_mix_entry *mix
 /* ---- launch-shape tuning (used by the autotuner, pqc_gb300/autotune.py) --------------------
  * Core-kernel launch shape per (algorithm, operation): ni = instances per CTA, threads per CTA
  * (multiple of 32).  Kyber: ni 1..128, threads 32..512 (shared by the round-2 and round-3 sets of
- * the same k); NewHope: ni 1..64, threads 32..256; FrodoKEM has a fixed shape (PQCGPU_EUNSUPPORTED).
+ * the same k); NewHope: ni 1..64, threads 32..256.  FrodoKEM: keypair ni 0 or 1, threads 64 / 128 /
+ * 256 (one row of A per thread); encaps / decaps ni = CTAs per instance sharing the rows of A
+ * (1, 2, 4, 8, 16) with threads 128 / 256, or ni = 0 to choose by batch size (the default).
  * Applies to all contexts of the process. */
 int pqcgpu_set_launch_shape(pqcgpu_alg alg, int op, int ni, int threads);
 int pqcgpu_get_launch_shape(pqcgpu_alg alg, int op, int *ni, int *threads);
@@ -229,6 +234,14 @@ int pqcgpu_probe_peaks(int device, double *int_ops_per_s, double *keccak_perms_p
  * Randomness comes from the library DRBG (pqcgpu_randombytes_init); device 0, default context. */
 int pqcgpu_randombytes_init(const uint8_t seed[48]);
 int pqcgpu_randombytes(uint8_t *out, size_t n);
+/* Switch the library DRBG to the NIST KAT generator's AES-256 CTR_DRBG (SP 800-90A, no derivation
+ * function), instantiated with entropy[48] xor personalization[48] (NULL: none).
+ * pqcgpu_randombytes_init returns to the SHAKE-256 DRBG. */
+int pqcgpu_randombytes_init_nist(const uint8_t entropy[48], const uint8_t *personalization);
+/* The coins of one crypto_kem_keypair (op 0) or crypto_kem_enc (op 1) of `alg`, drawn from the
+ * library DRBG in the randombytes calls of that algorithm's submission package; kp_coins or
+ * enc_coins bytes (pqcgpu_alg_sizes) are written. */
+int pqcgpu_nist_coins(pqcgpu_alg alg, int op, uint8_t *coins);
 
 int pqcgpu_kyber512_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
 int pqcgpu_kyber512_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
@@ -245,6 +258,15 @@ int pqcgpu_newhope1024_crypto_kem_dec(unsigned char *ss, const unsigned char *ct
 int pqcgpu_frodo976_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
 int pqcgpu_frodo976_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
 int pqcgpu_frodo976_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+int pqcgpu_mlkem512_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+int pqcgpu_mlkem512_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+int pqcgpu_mlkem512_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+int pqcgpu_mlkem768_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+int pqcgpu_mlkem768_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+int pqcgpu_mlkem768_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+int pqcgpu_mlkem1024_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+int pqcgpu_mlkem1024_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+int pqcgpu_mlkem1024_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
 
 #ifdef __cplusplus
 }

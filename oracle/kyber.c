@@ -354,11 +354,15 @@ static void gen_matrix(kpoly *a, const uint8_t rho[32], int transposed, const kp
 }
 
 /* ---- CPA-PKE ---- */
-static void cpa_keypair(const kparams *p, uint8_t *pk, uint8_t *sk, const uint8_t d[32]) {
+/* (rho, sigma) = G(d) for Kyber (indcpa.cu:495-500); ML-KEM (FIPS 203, K-PKE.KeyGen) hashes
+ * d || k, the module rank as one byte, for domain separation between parameter sets. */
+static void cpa_keypair_g(const kparams *p, uint8_t *pk, uint8_t *sk, const uint8_t d[32], int mlkem) {
     int k = p->k;
-    uint8_t buf[64];
+    uint8_t buf[64], din[33];
     kpoly a[16], s[4], e[4], t[4];
-    oracle_sha3_512(buf, d, 32);
+    memcpy(din, d, 32);
+    din[32] = (uint8_t)k;
+    oracle_sha3_512(buf, din, mlkem ? 33 : 32);
     const uint8_t *rho = buf, *sigma = buf + 32;
     gen_matrix(a, rho, 0, p);
     uint8_t nonce = 0;
@@ -377,10 +381,13 @@ static void cpa_keypair(const kparams *p, uint8_t *pk, uint8_t *sk, const uint8_
     for (int i = 0; i < k; i++) poly_tobytes(pk + 384 * i, &t[i]);
     memcpy(pk + p->polyvecbytes, rho, 32);
 }
+static void cpa_keypair(const kparams *p, uint8_t *pk, uint8_t *sk, const uint8_t d[32]) {
+    cpa_keypair_g(p, pk, sk, d, 0);
+}
 
 static void cpa_enc(const kparams *p, uint8_t *ct, const uint8_t m[32], const uint8_t *pk, const uint8_t coins[32]) {
     int k = p->k;
-    kpoly at[16], sp[4], ep[4], bp[4], pkpv[4], v, kmsg, epp;
+    kpoly at[16], sp[4] = {{{0}}}, ep[4], bp[4], pkpv[4], v, kmsg, epp;
     uint8_t rho[32];
     for (int i = 0; i < k; i++) poly_frombytes(&pkpv[i], pk + 384 * i);
     memcpy(rho, pk + p->polyvecbytes, 32);
@@ -477,5 +484,50 @@ int oracle_kyber_kem_dec(int variant, int k, uint8_t ss[32], const uint8_t *ct, 
     oracle_sha3_256(kr + 32, ct, p.ct);
     if (diff) memcpy(kr, sk + p.sk - 32, 32);
     oracle_shake256(ss, 32, kr, 64);
+    return 0;
+}
+
+/* ---- ML-KEM (FIPS 203): the same K-PKE with G(d || k), and a KEM layer without the message
+ * pre-hash and without the final KDF.  Keys are laid out as in round 3:
+ * dk = dk_pke || ek || H(ek) || z; the shared key is K from (K, r) = G(m || H(ek)); decapsulation
+ * rejects to J(z || c) = SHAKE256(z || c, 32).  Sizes equal the round-3 sets (k = 2, 3, 4). ---- */
+int oracle_mlkem_keypair(int k, uint8_t *pk, uint8_t *sk, const uint8_t coins[64]) {
+    kparams p;
+    if (kparams_get(3, k, &p)) return -1;
+    cpa_keypair_g(&p, pk, sk, coins, 1);
+    memcpy(sk + p.skcpa, pk, p.pk);
+    oracle_sha3_256(sk + p.sk - 64, pk, p.pk);
+    memcpy(sk + p.sk - 32, coins + 32, 32);
+    return 0;
+}
+
+int oracle_mlkem_enc(int k, uint8_t *ct, uint8_t ss[32], const uint8_t *pk, const uint8_t m[32]) {
+    kparams p;
+    if (kparams_get(3, k, &p)) return -1;
+    uint8_t buf[64], kr[64];
+    memcpy(buf, m, 32);
+    oracle_sha3_256(buf + 32, pk, p.pk);  /* H(ek) */
+    oracle_sha3_512(kr, buf, 64);         /* (K, r) = G(m || H(ek)) */
+    cpa_enc(&p, ct, m, pk, kr + 32);
+    memcpy(ss, kr, 32);
+    return 0;
+}
+
+int oracle_mlkem_dec(int k, uint8_t ss[32], const uint8_t *ct, const uint8_t *sk) {
+    kparams p;
+    if (kparams_get(3, k, &p)) return -1;
+    uint8_t buf[64], kr[64], kbar[32], cmp[1568 + 16], zc[32 + 1568];
+    const uint8_t *pk = sk + p.skcpa;
+    cpa_dec(&p, buf, ct, sk);
+    memcpy(buf + 32, sk + p.sk - 64, 32);  /* h = H(ek) */
+    oracle_sha3_512(kr, buf, 64);          /* (K', r') = G(m' || h) */
+    memcpy(zc, sk + p.sk - 32, 32);
+    memcpy(zc + 32, ct, p.ct);
+    oracle_shake256(kbar, 32, zc, 32 + p.ct);  /* J(z || c) */
+    cpa_enc(&p, cmp, buf, pk, kr + 32);
+    uint8_t diff = 0;
+    for (size_t i = 0; i < p.ct; i++) diff |= (uint8_t)(ct[i] ^ cmp[i]);
+    const uint8_t mask = (uint8_t)(0u - (uint8_t)(diff != 0));
+    for (int i = 0; i < 32; i++) ss[i] = (uint8_t)(kr[i] ^ (mask & (kr[i] ^ kbar[i])));
     return 0;
 }

@@ -52,6 +52,10 @@ int oracle_kyber_kem_keypair(int variant, int k, uint8_t *pk, uint8_t *sk, const
 int oracle_kyber_kem_enc(int variant, int k, uint8_t *ct, uint8_t ss[32], const uint8_t *pk,
                          const uint8_t coins[32]);
 int oracle_kyber_kem_dec(int variant, int k, uint8_t ss[32], const uint8_t *ct, const uint8_t *sk);
+/* ML-KEM (FIPS 203), k = 2, 3, 4: coins = d || z (keypair), m (encapsulation) */
+int oracle_mlkem_keypair(int k, uint8_t *pk, uint8_t *sk, const uint8_t coins[64]);
+int oracle_mlkem_enc(int k, uint8_t *ct, uint8_t ss[32], const uint8_t *pk, const uint8_t m[32]);
+int oracle_mlkem_dec(int k, uint8_t ss[32], const uint8_t *ct, const uint8_t *sk);
 
 /* ---- NewHope-1024 --------------------------------------------------------------------- */
 int oracle_newhope_cpapke_keypair(uint8_t *pk, uint8_t *sk, const uint8_t seed[32]);
@@ -68,6 +72,7 @@ int oracle_frodo_kem_dec(uint8_t ss[24], const uint8_t *ct, const uint8_t *sk);
 
 /* ---- Batched drivers (OpenMP over instances; nthreads <= 0 means all cores) -------------
  * alg: 0..2 = Kyber-512/768/1024 (round 3), 3 = Kyber-1024 round 2, 4 = NewHope-1024 CPA-KEM,
+ * 6..8 = ML-KEM-512/768/1024 (FIPS 203),
  *      5 = FrodoKEM-976.  Buffers are instance-major, each instance at a fixed stride. */
 int oracle_batch_keypair(int alg, size_t n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int nthreads);
 int oracle_batch_enc(int alg, size_t n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *coins,

@@ -12,7 +12,11 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 # alg ids shared with the batched drivers in batch.c
 KYBER512, KYBER768, KYBER1024, KYBER1024_R2, NEWHOPE1024, FRODO976 = range(6)
+MLKEM512, MLKEM768, MLKEM1024 = 6, 7, 8
 ALG_NAMES = {
+    "mlkem512": MLKEM512,
+    "mlkem768": MLKEM768,
+    "mlkem1024": MLKEM1024,
     "kyber512": KYBER512,
     "kyber768": KYBER768,
     "kyber1024": KYBER1024,

@@ -51,8 +51,10 @@ SIGNATURES = {
     "pqcgpu_probe_peaks": (_int, [_int, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]),
     "pqcgpu_randombytes_init": (_int, [_u8p]),
     "pqcgpu_randombytes": (_int, [_u8p, _sz]),
+    "pqcgpu_randombytes_init_nist": (_int, [_u8p, _u8p]),
+    "pqcgpu_nist_coins": (_int, [_int, _int, _u8p]),
 }
-for _alg in ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976"):
+for _alg in ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976", "mlkem512", "mlkem768", "mlkem1024"):
     SIGNATURES["pqcgpu_%s_crypto_kem_keypair" % _alg] = (_int, [_u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_enc" % _alg] = (_int, [_u8p, _u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_dec" % _alg] = (_int, [_u8p, _u8p, _u8p])

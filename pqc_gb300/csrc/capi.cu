@@ -134,9 +134,15 @@ struct HostShake {
 std::mutex g_drbg_mu;
 HostShake g_drbg;
 bool g_drbg_seeded = false;
+bool g_drbg_nist = false;  // pqcgpu_randombytes_init_nist: AES-256 CTR_DRBG (kat.cu) instead of SHAKE256
+pqc::CtrDrbg g_ctr;
 
 void drbg_bytes(uint8_t *out, size_t n) {
     std::lock_guard<std::mutex> lk(g_drbg_mu);
+    if (g_drbg_nist) {
+        g_ctr.generate(out, n);
+        return;
+    }
     if (!g_drbg_seeded) {
         uint8_t seed[48] = {0};
         FILE *f = fopen("/dev/urandom", "rb");
@@ -160,6 +166,9 @@ bool alg_info(int alg, AlgInfo *a) {
     case PQCGPU_KYBER768: *a = {1184, 2400, 1088, 32, 64, 32}; return true;
     case PQCGPU_KYBER1024: *a = {1568, 3168, 1568, 32, 64, 32}; return true;
     case PQCGPU_KYBER1024_R2: *a = {1568, 3168, 1568, 32, 64, 32}; return true;
+    case PQCGPU_MLKEM512: *a = {800, 1632, 768, 32, 64, 32}; return true;
+    case PQCGPU_MLKEM768: *a = {1184, 2400, 1088, 32, 64, 32}; return true;
+    case PQCGPU_MLKEM1024: *a = {1568, 3168, 1568, 32, 64, 32}; return true;
     case PQCGPU_NEWHOPE1024: *a = {1824, 1792, 2176, 32, 32, 32}; return true;
     case PQCGPU_FRODO976: *a = {15632, 31296, 15744, 24, 64, 24}; return true;
     default: return false;
@@ -171,10 +180,17 @@ bool kyber_alg(int alg, int *variant, int *k) {
     case PQCGPU_KYBER768: *variant = 3; *k = 3; return true;
     case PQCGPU_KYBER1024: *variant = 3; *k = 4; return true;
     case PQCGPU_KYBER1024_R2: *variant = 2; *k = 4; return true;
+    case PQCGPU_MLKEM512: *variant = 3; *k = 2; return true;
+    case PQCGPU_MLKEM768: *variant = 3; *k = 3; return true;
+    case PQCGPU_MLKEM1024: *variant = 3; *k = 4; return true;
     default: return false;
     }
 }
 }  // namespace
+namespace pqc {
+// KEM layer of a Kyber-family algorithm: 1 = Fujisaki-Okamoto as in rounds 2 / 3, 2 = FIPS 203
+int kyber_kem_mode(int alg) { return (alg >= PQCGPU_MLKEM512 && alg <= PQCGPU_MLKEM1024) ? 2 : 1; }
+}  // namespace pqc
 
 // ---------------------------------------------------------------------------------------------
 // Context
@@ -330,6 +346,14 @@ extern "C" int pqcgpu_randombytes_init(const uint8_t seed[48]) {
     std::lock_guard<std::mutex> lk(g_drbg_mu);
     g_drbg.init(seed, 48);
     g_drbg_seeded = true;
+    g_drbg_nist = false;
+    return PQCGPU_OK;
+}
+extern "C" int pqcgpu_randombytes_init_nist(const uint8_t entropy[48], const uint8_t *personalization) {
+    if (!entropy) return PQCGPU_EINVAL;
+    std::lock_guard<std::mutex> lk(g_drbg_mu);
+    g_ctr.instantiate(entropy, personalization);
+    g_drbg_nist = true;
     return PQCGPU_OK;
 }
 extern "C" int pqcgpu_randombytes(uint8_t *out, size_t n) {
@@ -466,9 +490,10 @@ int op_dev(int alg, int op, int n, const uint8_t *in0, const uint8_t *in1, uint8
     if (n <= 0) return PQCGPU_OK;
     int variant, k;
     if (kyber_alg(alg, &variant, &k)) {
-        if (op == 0) return kyber_keypair_dev(variant, k, n, out0, out1, in0, (int)ai.kpc, 1, scr, plain, s);
-        if (op == 1) return kyber_enc_dev(variant, k, n, out0, out1, in0, nullptr, in1, scr, 1, plain, s);
-        return kyber_dec_dev(variant, k, n, out0, in0, in1, scr, 1, plain, s);
+        const int kem = kyber_kem_mode(alg);
+        if (op == 0) return kyber_keypair_dev(variant, k, n, out0, out1, in0, (int)ai.kpc, kem, scr, plain, s);
+        if (op == 1) return kyber_enc_dev(variant, k, n, out0, out1, in0, nullptr, in1, scr, kem, plain, s);
+        return kyber_dec_dev(variant, k, n, out0, in0, in1, scr, kem, plain, s);
     }
     if (plain) return PQCGPU_EUNSUPPORTED;
     if (alg == PQCGPU_NEWHOPE1024) {
@@ -496,7 +521,8 @@ static int kem_op(pqcgpu_ctx *c, int alg, int op, size_t n, const uint8_t *in0, 
     if (!c || !alg_info(alg, &ai)) return set_err(PQCGPU_EINVAL, "bad context or algorithm");
     const int plain = (flags & PQCGPU_PLAIN) ? 1 : 0;
     int variant, k;
-    if (plain && !kyber_alg(alg, &variant, &k)) return set_err(PQCGPU_EUNSUPPORTED, "the plain path covers Kyber only");
+    if (plain && (!kyber_alg(alg, &variant, &k) || kyber_kem_mode(alg) != 1))
+        return set_err(PQCGPU_EUNSUPPORTED, "the plain path covers the round-2 / round-3 Kyber KEMs only");
     size_t sz[4];
     op_io_sizes(alg, op, sz);
     OpDesc d;
@@ -672,6 +698,7 @@ extern "C" int pqcgpu_set_launch_shape(pqcgpu_alg alg, int op, int ni, int threa
     int variant, k, rc;
     if (kyber_alg(alg, &variant, &k)) rc = kyber_set_shape(op, k, ni, threads);
     else if (alg == PQCGPU_NEWHOPE1024) rc = newhope_set_shape(op, ni, threads);
+    else if (alg == PQCGPU_FRODO976) rc = frodo_set_shape(op, ni, threads);
     else rc = PQCGPU_EUNSUPPORTED;
     return rc ? set_err(rc, "launch shape not accepted") : PQCGPU_OK;
 }
@@ -680,6 +707,7 @@ extern "C" int pqcgpu_get_launch_shape(pqcgpu_alg alg, int op, int *ni, int *thr
     if (!ni || !threads) return set_err(PQCGPU_EINVAL, "null output");
     if (kyber_alg(alg, &variant, &k)) return kyber_get_shape(op, k, ni, threads);
     if (alg == PQCGPU_NEWHOPE1024) return newhope_get_shape(op, ni, threads);
+    if (alg == PQCGPU_FRODO976) return frodo_get_shape(op, ni, threads);
     return set_err(PQCGPU_EUNSUPPORTED, "no tunable launch shape for this algorithm");
 }
 
@@ -817,19 +845,48 @@ static pqcgpu_ctx *default_ctx() {
     if (!g_default_ctx) pqcgpu_ctx_create(&g_default_ctx, 0, (size_t)256 << 20);
     return g_default_ctx;
 }
+// The coins of one NIST crypto_kem_* call are drawn from the library DRBG in the calls the
+// algorithm's submission package makes to randombytes, so that with the CTR_DRBG of the NIST KAT
+// generator (pqcgpu_randombytes_init_nist) the keys and ciphertexts are those of its .rsp files:
+// Kyber (rounds 2 / 3) keypair d then z (32 + 32: indcpa_keypair, then crypto_kem_keypair);
+// ML-KEM keypair d || z in one call (the derandomized FIPS 203 API); FrodoKEM s || seedSE || z in
+// one call; one call for every encapsulation (m, or mu for FrodoKEM).
+extern "C" int pqcgpu_nist_coins(pqcgpu_alg alg, int op, uint8_t *coins) {
+    AlgInfo ai;
+    if (!coins || !alg_info(alg, &ai) || op < 0 || op > 1) return PQCGPU_EINVAL;
+    int variant, k;
+    const bool split = op == 0 && kyber_alg(alg, &variant, &k) && kyber_kem_mode(alg) == 1;
+    if (split) {
+        drbg_bytes(coins, 32);
+        drbg_bytes(coins + 32, 32);
+    } else {
+        drbg_bytes(coins, op == 0 ? ai.kpc : ai.encc);
+    }
+    return PQCGPU_OK;
+}
+
 #define PQC_NIST(NAME, ALG)                                                                              \
     extern "C" int pqcgpu_##NAME##_crypto_kem_keypair(unsigned char *pk, unsigned char *sk) {             \
         pqcgpu_ctx *c = default_ctx();                                                                   \
-        return c ? pqcgpu_kem_keypair_batch(c, ALG, 1, pk, sk, nullptr, 0) : PQCGPU_ECUDA;               \
+        uint8_t coins[64];                                                                               \
+        if (!c) return PQCGPU_ECUDA;                                                                     \
+        pqcgpu_nist_coins(ALG, 0, coins);                                                                \
+        return pqcgpu_kem_keypair_batch(c, ALG, 1, pk, sk, coins, 0);                                    \
     }                                                                                                    \
     extern "C" int pqcgpu_##NAME##_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk) { \
         pqcgpu_ctx *c = default_ctx();                                                                   \
-        return c ? pqcgpu_kem_enc_batch(c, ALG, 1, ct, ss, pk, nullptr, 0) : PQCGPU_ECUDA;               \
+        uint8_t coins[64];                                                                               \
+        if (!c) return PQCGPU_ECUDA;                                                                     \
+        pqcgpu_nist_coins(ALG, 1, coins);                                                                \
+        return pqcgpu_kem_enc_batch(c, ALG, 1, ct, ss, pk, coins, 0);                                    \
     }                                                                                                    \
     extern "C" int pqcgpu_##NAME##_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk) { \
         pqcgpu_ctx *c = default_ctx();                                                                   \
         return c ? pqcgpu_kem_dec_batch(c, ALG, 1, ss, ct, sk, 0) : PQCGPU_ECUDA;                        \
     }
+PQC_NIST(mlkem512, PQCGPU_MLKEM512)
+PQC_NIST(mlkem768, PQCGPU_MLKEM768)
+PQC_NIST(mlkem1024, PQCGPU_MLKEM1024)
 PQC_NIST(kyber512, PQCGPU_KYBER512)
 PQC_NIST(kyber768, PQCGPU_KYBER768)
 PQC_NIST(kyber1024, PQCGPU_KYBER1024)

@@ -29,9 +29,11 @@ constexpr int N = 976, NB = 8;
 constexpr int PKB = 15632, SKB = 31296, CTB = 15744, SSB = 24, SEEDA = 16, MUB = 24;
 constexpr int C1B = 2 * N * NB;  // 15616: packed N x NBAR (or NBAR x N) matrix
 constexpr int ROW_BLOCKS = 12;   // 1952 bytes of SHAKE128 per row = 11 full blocks + 104 bytes
-// scratch per instance: noise (Sp 7808 + Ep 7808 + Epp 64 u16) + seeds (seedSE/k 48, mu 24, flag)
+// scratch per instance: noise (Sp 7808 + Ep 7808 + Epp 64 u16) + seeds (seedSE/k 48, mu 24, flag),
+// then the u32 accumulator of B' (8 x N) used when the rows of A are split over several CTAs
 constexpr int NOISE_U16 = 2 * N * NB + NB * NB;
-constexpr size_t SCRATCH = (size_t)NOISE_U16 * 2 + 128;
+constexpr size_t GACC_OFF = (size_t)NOISE_U16 * 2 + 128;
+constexpr size_t SCRATCH = GACC_OFF + (size_t)NB * N * 4;
 
 static __constant__ uint16_t c_cdf[11];
 
@@ -148,12 +150,26 @@ __device__ __forceinline__ void g2_and_noise(uint2 a, const uint8_t *mu, uint8_t
 // encaps prologue: pkh = G1(pk); (seedSE || k) = G2(pkh || mu); S', E', E'' sampled -> scratch.
 // scratch: Spt (N x 8: Spt[k][i] = S'[i][k]), Ep (8 x N), Epp (8 x 8), then k (24) at +NOISE*2,
 // mu (24) at +NOISE*2 + 32.
-__global__ void __launch_bounds__(128) fr_enc_pre(int n, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch) {
+__device__ __forceinline__ void zero_gacc(uint8_t *scr, int lane) {
+    uint4 *g = reinterpret_cast<uint4 *>(scr + GACC_OFF);
+    for (int i = lane; i < NB * N / 4; i += 32) g[i] = make_uint4(0, 0, 0, 0);
+}
+
+// pkh != nullptr: pkh = SHAKE256(pk, 24) is given (the tail of a resident secret key, 24 bytes at
+// pkh + x * 24), which skips the 115 serial permutations of hashing the public key.
+__global__ void __launch_bounds__(128) fr_enc_pre(int n, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
+                                                  int split, const uint8_t *pkh) {
     FR_WARP_INSTANCE;
+    if (split > 1) zero_gacc(scratch + (size_t)x * SCRATCH, w.lane);
     uint2 a;
-    warp_absorb2<SHAKE256_LANES>(a, reinterpret_cast<const uint2 *>(pk + (size_t)x * PKB), PKB / 8, nullptr, 0,
-                                 DOM_SHAKE, w);
-    keccak_f1600_warp(a, w);
+    if (pkh) {
+        const uint2 *h = reinterpret_cast<const uint2 *>(pkh + (size_t)x * 24);
+        a = w.lane < 3 ? h[w.lane] : make_uint2(0, 0);
+    } else {
+        warp_absorb2<SHAKE256_LANES>(a, reinterpret_cast<const uint2 *>(pk + (size_t)x * PKB), PKB / 8, nullptr, 0,
+                                     DOM_SHAKE, w);
+        keccak_f1600_warp(a, w);
+    }
     g2_and_noise(a, mu + (size_t)x * MUB, scratch + (size_t)x * SCRATCH, w);
 }
 
@@ -195,9 +211,10 @@ __global__ void __launch_bounds__(256) fr_dec_w(int n, const uint8_t *ct, const 
 }
 
 // decaps, step 2 (warp per instance): (seedSE' || k') = G2(pkh || mu'); S', E', E'' -> scratch
-__global__ void __launch_bounds__(128) fr_dec_pre(int n, const uint8_t *sk, uint8_t *scratch) {
+__global__ void __launch_bounds__(128) fr_dec_pre(int n, const uint8_t *sk, uint8_t *scratch, int split) {
     FR_WARP_INSTANCE;
     uint8_t *scr = scratch + (size_t)x * SCRATCH;
+    if (split > 1) zero_gacc(scr, w.lane);
     const uint2 *pkh = reinterpret_cast<const uint2 *>(sk + (size_t)x * SKB + SSB + PKB + C1B);
     const uint2 a = w.lane < 3 ? pkh[w.lane] : make_uint2(0, 0);
     g2_and_noise(a, scr + NOISE_U16 * 2 + 32, scr, w);
@@ -297,31 +314,80 @@ __global__ void __launch_bounds__(256) fr_kp_core(int n, uint8_t *pk, const uint
     }
 }
 
-// B' = S' A + E' (and V = S' B + E'', C = V + encode(mu)), CTA per instance.  cmp == nullptr:
-// pack into ct; else compare with ct and store the fail flag in scratch.
+// Epilogue of B' = S' A + E': V = S' B + E'' (B = unpack(pk_b), N x 8; 64 outputs, k split over
+// the CTA, into acc[NB*N ..]), then B' -> c1 and C = V + encode(mu) -> c2, 16-bit big-endian, or
+// compared with the received ciphertext (cmp != nullptr; the fail flag goes to scratch).
+// acc holds B' (8 x N, u32, wrapped mod 2^32) and E'' in its last 64 words; Spt is S' (N x 8).
+__device__ void sa_epilogue(uint32_t *acc, const uint16_t *Spt, const uint8_t *p, uint8_t *scr, uint8_t *ct,
+                            const uint8_t *ct_cmp, int x) {
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    {
+        const uint8_t *pb = p + SEEDA;
+        for (int t = tid; t < 64 * 4; t += nthr) {
+            const int o = t & 63, part = t >> 6, i = o >> 3, l = o & 7;
+            uint32_t sum = 0;
+            for (int k = part; k < N; k += 4) sum += (uint32_t)Spt[k * NB + i] * ld_be16(pb + 2 * (k * NB + l));
+            atomicAdd(acc + NB * N + o, sum);
+        }
+    }
+    __syncthreads();
+    const uint8_t *mu = scr + NOISE_U16 * 2 + 32;
+    uint32_t diff = 0;
+    for (int e = tid; e < NB * N; e += nthr) {
+        const uint32_t v = acc[e] & 0xffff;
+        if (ct_cmp) diff |= v ^ ld_be16(ct_cmp + (size_t)x * CTB + 2 * e);
+        else {
+            ct[(size_t)x * CTB + 2 * e] = (uint8_t)(v >> 8);
+            ct[(size_t)x * CTB + 2 * e + 1] = (uint8_t)v;
+        }
+    }
+    for (int e = tid; e < 64; e += nthr) {
+        const int g = e >> 3, j = e & 7;
+        const uint32_t temp = (uint32_t)mu[3 * g] | ((uint32_t)mu[3 * g + 1] << 8) | ((uint32_t)mu[3 * g + 2] << 16);
+        const uint32_t enc = ((temp >> (3 * j)) & 7) << 13;
+        const uint32_t v = (acc[NB * N + e] + enc) & 0xffff;
+        if (ct_cmp) diff |= v ^ ld_be16(ct_cmp + (size_t)x * CTB + C1B + 2 * e);
+        else {
+            ct[(size_t)x * CTB + C1B + 2 * e] = (uint8_t)(v >> 8);
+            ct[(size_t)x * CTB + C1B + 2 * e + 1] = (uint8_t)v;
+        }
+    }
+    if (ct_cmp) {
+        const int any = __syncthreads_or(diff != 0);
+        if (tid == 0) scr[NOISE_U16 * 2 + 64] = (uint8_t)any;
+    }
+}
+
+// B' = S' A + E' (and V, C), CTA (instance x = blockIdx.x, row part blockIdx.y of gridDim.y).
+// With one part the CTA owns the whole product and runs the epilogue.  With several, the CTA
+// contracts only its rows of A and adds its partial B' into the instance's u32 accumulator in
+// scratch (zeroed by the prologue kernel); fr_sa_final then finishes.  Sums are mod 2^32, hence
+// exact mod 2^16 in any order.  cmp == nullptr: pack into ct; else compare with ct.
 constexpr int SA_THREADS = 256;
 constexpr int STAGE_PITCH = 86;  // u16 per staged row block (84 used; odd word pitch)
+constexpr int BLK_COLS = 84;     // u16 values per SHAKE128 block
 __global__ void __launch_bounds__(SA_THREADS) fr_sa_core(int n, uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *pk,
                                                          int pk_stride, uint8_t *scratch) {
     extern __shared__ __align__(16) uint8_t smem[];
     uint16_t *Spt = reinterpret_cast<uint16_t *>(smem);                       // N x 8
     uint32_t *acc = reinterpret_cast<uint32_t *>(smem + N * NB * 2);          // 8 x N (+64 for V)
     uint16_t *stage = reinterpret_cast<uint16_t *>(smem + N * NB * 2 + (NB * N + 64) * 4);  // threads x 86
-    const int x = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x;
+    const int x = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x, parts = gridDim.y;
+    const int rows_per = (N + parts - 1) / parts, rbeg = blockIdx.y * rows_per, rend = min(N, rbeg + rows_per);
     uint8_t *scr = scratch + (size_t)x * SCRATCH;
     const uint16_t *gSpt = reinterpret_cast<const uint16_t *>(scr), *Ep = gSpt + N * NB, *Epp = Ep + N * NB;
     const uint8_t *p = pk + (size_t)x * pk_stride;
     for (int i = tid; i < N * NB / 8; i += nthr) reinterpret_cast<uint4 *>(Spt)[i] = reinterpret_cast<const uint4 *>(gSpt)[i];
-    for (int i = tid; i < NB * N; i += nthr) acc[i] = Ep[i];
+    for (int i = tid; i < NB * N; i += nthr) acc[i] = parts == 1 ? Ep[i] : 0u;
     for (int i = tid; i < 64; i += nthr) acc[NB * N + i] = Epp[i];
     __syncthreads();
-    // rows pass by pass; within a pass each thread owns one row and squeezes one block per round
-    const int ncol_slices = nthr / 84;  // threads (j, slice): j = tid % 84, slice = tid / 84
-    for (int r0 = 0; r0 < N; r0 += nthr) {
-        const int rows = min(nthr, N - r0);
+    // rows pass by pass; within a pass each thread owns one row and squeezes one block per round,
+    // then the CTA contracts the staged block: work item (column j, row slice) per thread
+    const int nslice = max(1, nthr / BLK_COLS);
+    for (int r0 = rbeg; r0 < rend; r0 += nthr) {
+        const int rows = min(nthr, rend - r0);
         uint2 A[25];
-        const int myrow = r0 + tid;
-        if (tid < rows) row_absorb(A, myrow, reinterpret_cast<const uint2 *>(p));
+        if (tid < rows) row_absorb(A, r0 + tid, reinterpret_cast<const uint2 *>(p));
         for (int blk = 0; blk < ROW_BLOCKS; blk++) {
             if (tid < rows) {
                 keccak_f1600(A);
@@ -330,9 +396,10 @@ __global__ void __launch_bounds__(SA_THREADS) fr_sa_core(int n, uint8_t *ct, con
                 for (int w = 0; w < 42; w++) st[w] = (w & 1) ? A[w >> 1].y : A[w >> 1].x;
             }
             __syncthreads();
-            const int j = tid % 84, slice = tid / 84, col = blk * 84 + j;
-            if (slice < ncol_slices && col < N) {
-                const int per = (rows + ncol_slices - 1) / ncol_slices;
+            const int per = (rows + nslice - 1) / nslice;
+            for (int t = tid; t < BLK_COLS * nslice; t += nthr) {
+                const int j = t % BLK_COLS, slice = t / BLK_COLS, col = blk * BLK_COLS + j;
+                if (col >= N) continue;
                 const int k0 = slice * per, k1 = min(rows, k0 + per);
                 uint32_t s[NB] = {0, 0, 0, 0, 0, 0, 0, 0};
                 for (int k = k0; k < k1; k++) {
@@ -353,47 +420,33 @@ __global__ void __launch_bounds__(SA_THREADS) fr_sa_core(int n, uint8_t *ct, con
             __syncthreads();
         }
     }
-    // V = S' B + E'' (B = unpack(pk_b), N x 8): 64 outputs, k split over the CTA
-    {
-        const uint8_t *pb = p + SEEDA;
-        for (int t = tid; t < 64 * 4; t += nthr) {
-            const int o = t & 63, part = t >> 6, i = o >> 3, l = o & 7;
-            uint32_t sum = 0;
-            for (int k = part; k < N; k += 4) sum += (uint32_t)Spt[k * NB + i] * ld_be16(pb + 2 * (k * NB + l));
-            atomicAdd(acc + NB * N + o, sum);
-        }
+    if (parts > 1) {
+        uint32_t *g = reinterpret_cast<uint32_t *>(scr + GACC_OFF);
+        for (int i = tid; i < NB * N; i += nthr) atomicAdd(g + i, acc[i]);
+        return;
     }
+    sa_epilogue(acc, Spt, p, scr, ct, ct_cmp, x);
+}
+
+// Finish a split product: acc = (sum of the parts) + E', then the same epilogue.  CTA per instance.
+__global__ void __launch_bounds__(SA_THREADS) fr_sa_final(int n, uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *pk,
+                                                          int pk_stride, uint8_t *scratch) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint16_t *Spt = reinterpret_cast<uint16_t *>(smem);
+    uint32_t *acc = reinterpret_cast<uint32_t *>(smem + N * NB * 2);
+    const int x = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x;
+    uint8_t *scr = scratch + (size_t)x * SCRATCH;
+    const uint16_t *gSpt = reinterpret_cast<const uint16_t *>(scr), *Ep = gSpt + N * NB, *Epp = Ep + N * NB;
+    const uint32_t *g = reinterpret_cast<const uint32_t *>(scr + GACC_OFF);
+    for (int i = tid; i < N * NB / 8; i += nthr) reinterpret_cast<uint4 *>(Spt)[i] = reinterpret_cast<const uint4 *>(gSpt)[i];
+    for (int i = tid; i < NB * N; i += nthr) acc[i] = g[i] + Ep[i];
+    for (int i = tid; i < 64; i += nthr) acc[NB * N + i] = Epp[i];
     __syncthreads();
-    const uint8_t *mu = scr + NOISE_U16 * 2 + 32;
-    uint32_t diff = 0;
-    // B' (8 x N, row-major) -> c1, 16-bit big-endian
-    for (int e = tid; e < NB * N; e += nthr) {
-        const uint32_t v = acc[e] & 0xffff;
-        if (ct_cmp) diff |= v ^ ld_be16(ct_cmp + (size_t)x * CTB + 2 * e);
-        else {
-            ct[(size_t)x * CTB + 2 * e] = (uint8_t)(v >> 8);
-            ct[(size_t)x * CTB + 2 * e + 1] = (uint8_t)v;
-        }
-    }
-    // C = V + encode(mu) -> c2
-    for (int e = tid; e < 64; e += nthr) {
-        const int g = e >> 3, j = e & 7;
-        const uint32_t temp = (uint32_t)mu[3 * g] | ((uint32_t)mu[3 * g + 1] << 8) | ((uint32_t)mu[3 * g + 2] << 16);
-        const uint32_t enc = ((temp >> (3 * j)) & 7) << 13;
-        const uint32_t v = (acc[NB * N + e] + enc) & 0xffff;
-        if (ct_cmp) diff |= v ^ ld_be16(ct_cmp + (size_t)x * CTB + C1B + 2 * e);
-        else {
-            ct[(size_t)x * CTB + C1B + 2 * e] = (uint8_t)(v >> 8);
-            ct[(size_t)x * CTB + C1B + 2 * e + 1] = (uint8_t)v;
-        }
-    }
-    if (ct_cmp) {
-        const int any = __syncthreads_or(diff != 0);
-        if (tid == 0) scr[NOISE_U16 * 2 + 64] = (uint8_t)any;
-    }
+    sa_epilogue(acc, Spt, pk + (size_t)x * pk_stride, scr, ct, ct_cmp, x);
 }
 
 static size_t sa_smem(int threads) { return (size_t)N * NB * 2 + ((size_t)NB * N + 64) * 4 + (size_t)threads * STAGE_PITCH * 2; }
+static size_t sa_final_smem() { return (size_t)N * NB * 2 + ((size_t)NB * N + 64) * 4; }
 
 }  // namespace frodo
 
@@ -409,35 +462,101 @@ int frodo_init_constants() {
 }
 size_t frodo_scratch_bytes() { return SCRATCH; }
 
+// Launch shapes.  Keypair: threads per CTA of fr_kp_core (one row of A per thread).  Encaps /
+// decaps: row parts per instance for B' = S' A + E' and threads per CTA of fr_sa_core.  0 = chosen
+// by batch size: small batches split an instance over several CTAs (latency), large ones keep one
+// CTA per instance (no split traffic).  Set through pqcgpu_set_launch_shape (the autotuner).
+static int g_fr_parts[3] = {0, 0, 0}, g_fr_threads[3] = {0, 0, 0};
+
+static void fr_shape(int op, int n, int *parts, int *threads) {
+    if (op == 0) {
+        *parts = 1;
+        *threads = g_fr_threads[0] ? g_fr_threads[0] : (n >= 152 ? 256 : 64);
+        return;
+    }
+    if (g_fr_parts[op]) {
+        *parts = g_fr_parts[op];
+        *threads = g_fr_threads[op];
+        return;
+    }
+    if (n >= 304) *parts = 1, *threads = 256;
+    else if (n >= 152) *parts = 2, *threads = 256;
+    else if (n >= 76) *parts = 4, *threads = 256;
+    else *parts = 8, *threads = 128;
+}
+
+int frodo_set_shape(int op, int parts, int threads) {
+    if (op == 0) {
+        if (parts > 1 || !(threads == 0 || threads == 64 || threads == 128 || threads == 256)) return PQCGPU_EINVAL;
+        g_fr_threads[0] = threads;
+        return PQCGPU_OK;
+    }
+    if (op != 1 && op != 2) return PQCGPU_EINVAL;
+    if (parts == 0) {
+        g_fr_parts[op] = g_fr_threads[op] = 0;
+        return PQCGPU_OK;
+    }
+    if (!(parts == 1 || parts == 2 || parts == 4 || parts == 8 || parts == 16) || !(threads == 128 || threads == 256))
+        return PQCGPU_EINVAL;
+    g_fr_parts[op] = parts;
+    g_fr_threads[op] = threads;
+    return PQCGPU_OK;
+}
+
+int frodo_get_shape(int op, int *parts, int *threads) {
+    if (op < 0 || op > 2) return PQCGPU_EINVAL;
+    *parts = op == 0 ? 1 : g_fr_parts[op];
+    *threads = g_fr_threads[op];
+    return PQCGPU_OK;
+}
+
 int frodo_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
                       cudaStream_t st) {
+    int parts, thr;
+    fr_shape(0, n, &parts, &thr);
     PQC_LAUNCH(st, "fr_kp_pre", 976, 0, fr_kp_pre<<<(n + 3) / 4, 128, 0, st>>>(n, coins, cstride, pk, scratch));
-    PQC_LAUNCH(st, "fr_kp_core", 976, 0, fr_kp_core<<<dim3((N + 255) / 256, n), 256, 0, st>>>(n, pk, scratch));
+    PQC_LAUNCH(st, "fr_kp_core", 976, 0, fr_kp_core<<<dim3((N + thr - 1) / thr, n), thr, 0, st>>>(n, pk, scratch));
     PQC_LAUNCH(st, "fr_kp_post", 976, 0, fr_kp_post<<<(n + 3) / 4, 128, 0, st>>>(n, coins, cstride, pk, scratch, sk));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
-int frodo_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
-                  cudaStream_t st) {
-    const size_t sm = sa_smem(SA_THREADS);
-    if (!capturing() &&
-        cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+// B' = S' A + E' and the ciphertext epilogue: one CTA per instance, or `parts` CTAs per instance
+// plus fr_sa_final.
+static void launch_sa(int n, uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *pk, int pk_stride, uint8_t *scratch,
+                      int parts, int thr, cudaStream_t st) {
+    PQC_LAUNCH(st, "fr_sa_core", 976, 0,
+               fr_sa_core<<<dim3(n, parts), thr, sa_smem(thr), st>>>(n, ct, ct_cmp, pk, pk_stride, scratch));
+    if (parts > 1)
+        PQC_LAUNCH(st, "fr_sa_final", 976, 0,
+                   fr_sa_final<<<n, SA_THREADS, sa_final_smem(), st>>>(n, ct, ct_cmp, pk, pk_stride, scratch));
+}
+
+static int sa_attrs() {
+    if (capturing()) return PQCGPU_OK;
+    if (cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sa_smem(SA_THREADS)) !=
+        cudaSuccess)
         return PQCGPU_ECUDA;
-    PQC_LAUNCH(st, "fr_enc_pre", 976, 0, fr_enc_pre<<<(n + 3) / 4, 128, 0, st>>>(n, pk, mu, scratch));
-    PQC_LAUNCH(st, "fr_sa_core", 976, 0, fr_sa_core<<<n, SA_THREADS, sm, st>>>(n, ct, nullptr, pk, PKB, scratch));
+    return PQCGPU_OK;
+}
+
+int frodo_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
+                  cudaStream_t st, const uint8_t *pkh) {
+    if (sa_attrs()) return PQCGPU_ECUDA;
+    int parts, thr;
+    fr_shape(1, n, &parts, &thr);
+    PQC_LAUNCH(st, "fr_enc_pre", 976, 0, fr_enc_pre<<<(n + 3) / 4, 128, 0, st>>>(n, pk, mu, scratch, parts, pkh));
+    launch_sa(n, ct, nullptr, pk, PKB, scratch, parts, thr, st);
     PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, nullptr, ss));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
 int frodo_dec_dev(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, cudaStream_t st) {
-    const size_t sm = sa_smem(SA_THREADS);
-    if (!capturing() &&
-        cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-        return PQCGPU_ECUDA;
+    if (sa_attrs()) return PQCGPU_ECUDA;
+    int parts, thr;
+    fr_shape(2, n, &parts, &thr);
     PQC_LAUNCH(st, "fr_dec_w", 976, 0, fr_dec_w<<<n, 256, 0, st>>>(n, ct, sk, scratch));
-    PQC_LAUNCH(st, "fr_dec_pre", 976, 0, fr_dec_pre<<<(n + 3) / 4, 128, 0, st>>>(n, sk, scratch));
-    PQC_LAUNCH(st, "fr_sa_core", 976, 0,
-               fr_sa_core<<<n, SA_THREADS, sm, st>>>(n, nullptr, ct, sk + SSB, SKB, scratch));
+    PQC_LAUNCH(st, "fr_dec_pre", 976, 0, fr_dec_pre<<<(n + 3) / 4, 128, 0, st>>>(n, sk, scratch, parts));
+    launch_sa(n, nullptr, ct, sk + SSB, SKB, scratch, parts, thr, st);
     PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, sk, ss));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }

@@ -141,6 +141,31 @@ __device__ __forceinline__ void keccak_absorb_lanes(uint2 (&A)[25], const uint2 
     keccak_pad<RATE_LANES>(A, nlanes, dom);
 }
 
+// Absorb pre[0..npre) || in[0..nlanes) (whole lanes) and pad; the state is ready to permute.
+template <int RATE_LANES>
+__device__ __forceinline__ void keccak_absorb_lanes2(uint2 (&A)[25], const uint2 *pre, int npre, const uint2 *in,
+                                                     int nlanes, uint32_t dom) {
+    keccak_zero(A);
+    const int total = npre + nlanes;
+    int pos = 0;
+    for (; total - pos >= RATE_LANES; pos += RATE_LANES) {
+#pragma unroll
+        for (int i = 0; i < RATE_LANES; i++) {
+            const int g = pos + i;
+            A[i] = xor2(A[i], g < npre ? pre[g] : in[g - npre]);
+        }
+        keccak_f1600(A);
+    }
+    const int rem = total - pos;
+#pragma unroll
+    for (int i = 0; i < RATE_LANES; i++)
+        if (i < rem) {
+            const int g = pos + i;
+            A[i] = xor2(A[i], g < npre ? pre[g] : in[g - npre]);
+        }
+    keccak_pad<RATE_LANES>(A, rem, dom);
+}
+
 constexpr int SHAKE128_LANES = 21;  // rate 168
 constexpr int SHAKE256_LANES = 17;  // rate 136
 constexpr int SHA3_256_LANES = 17;  // rate 136

@@ -288,6 +288,10 @@ __device__ __forceinline__ void unpack8(uint32_t (&t)[8], const uint8_t *in) {
 // ---------------------------------------------------------------------------------------------
 // Kernel parameters
 // ---------------------------------------------------------------------------------------------
+// KEM layer: KEM_FO = the round-2 / round-3 Fujisaki-Okamoto transform (H(coins), KDF(K || H(c)));
+// KEM_MLKEM = FIPS 203 (G(d || k), no message pre-hash, K used directly, rejection key J(z || c)).
+constexpr int KEM_FO = 1, KEM_MLKEM = 2;
+
 struct KpArgs {
     int n;
     uint8_t *pk;
@@ -312,8 +316,8 @@ struct DecArgs {
     const uint8_t *sk;       // CPA: sk_cpa (stride SKCPA); KEM: full sk (stride SKB)
     uint8_t *m_out;          // CPA only: decrypted message
     uint8_t *ss;             // KEM only
-    const uint8_t *hct;      // KEM only: H(c) per instance (32 B)
-    int kem;
+    const uint8_t *hct;      // KEM only: H(c) per instance (32 B); ML-KEM: J(z || c)
+    int kem;                 // 0 CPA, KEM_FO, KEM_MLKEM
 };
 
 // Shared-memory layout for a CTA of NI instances: twiddles, NPOLY polynomials per instance,
@@ -617,6 +621,21 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, in
     e.r_stride = 0;
     encrypt_phases<K, V, true>(polys, seeds, sz, szi, ni, NI, base, e, d.ct);
     __syncthreads();
+    // (g) ML-KEM: ss = fail ? J(z || c) : K' (constant-time select, no hashing)
+    if (d.kem == KEM_MLKEM) {
+        for (int li = tid; li < ni; li += nthr) {
+            const uint32_t mask = 0u - (uint32_t)(seeds[li * SB + 96] != 0);
+            const uint2 *kb = reinterpret_cast<const uint2 *>(seeds + li * SB + 64);
+            const uint2 *jz = reinterpret_cast<const uint2 *>(d.hct + (size_t)(base + li) * 32);
+            uint2 *out = reinterpret_cast<uint2 *>(d.ss + (size_t)(base + li) * 32);
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const uint2 kk = kb[i], jj = jz[i];
+                out[i] = make_uint2(kk.x ^ (mask & (kk.x ^ jj.x)), kk.y ^ (mask & (kk.y ^ jj.y)));
+            }
+        }
+        return;
+    }
     // (g) ss = SHAKE256(fail ? z : K-bar' || H(c)), with a constant-time select
     for (int li = tid; li < ni; li += nthr) {
         const uint8_t *sk = d.sk + (size_t)(base + li) * Pp::SKB;
@@ -653,14 +672,14 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int 
     const int ni = min(NI, a.n - base);
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
     load_twiddles(sz, szi);
-    // (a) (rho, sigma) = G(d)
+    // (a) (rho, sigma) = G(d); ML-KEM: G(d || k) with the module rank as one byte (FIPS 203)
     for (int li = tid; li < ni; li += nthr) {
         const uint2 *dd = reinterpret_cast<const uint2 *>(a.coins + (size_t)(base + li) * a.coins_stride);
         uint2 A[25];
         keccak_zero(A);
 #pragma unroll
         for (int i = 0; i < 4; i++) A[i] = dd[i];
-        A[4].x ^= DOM_SHA3;
+        A[4].x = a.kem == KEM_MLKEM ? ((uint32_t)K | (DOM_SHA3 << 8)) : DOM_SHA3;
         A[SHA3_512_LANES - 1].y ^= 0x80000000u;
         keccak_f1600(A);
         uint2 *o = reinterpret_cast<uint2 *>(seeds + li * 128);
@@ -725,16 +744,24 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int 
 
 // ---- flat hash kernels: one thread per instance ----
 // encaps prologue: m = H(coins); (K-bar, r) = G(m || H(pk)); scratch = m || r || K-bar
+// ML-KEM: m = coins (no pre-hash)
 template <int K, int V>
-__global__ void __launch_bounds__(128) kyber_enc_hash_pre(int n, const uint8_t *pk, const uint8_t *coins, uint8_t *scratch) {
+__global__ void __launch_bounds__(128) kyber_enc_hash_pre(int n, const uint8_t *pk, const uint8_t *coins, uint8_t *scratch,
+                                                          int kem) {
     using Pp = P<K, V>;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
     uint2 A[25], mh[8];
-    keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(coins + (size_t)x * 32), 4, DOM_SHA3);
-    keccak_f1600(A);
+    const uint2 *cn = reinterpret_cast<const uint2 *>(coins + (size_t)x * 32);
+    if (kem == KEM_MLKEM) {
 #pragma unroll
-    for (int i = 0; i < 4; i++) mh[i] = A[i];
+        for (int i = 0; i < 4; i++) mh[i] = cn[i];
+    } else {
+        keccak_absorb_lanes<SHA3_256_LANES>(A, cn, 4, DOM_SHA3);
+        keccak_f1600(A);
+#pragma unroll
+        for (int i = 0; i < 4; i++) mh[i] = A[i];
+    }
     keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(pk + (size_t)x * Pp::PKB), Pp::PKB / 8, DOM_SHA3);
     keccak_f1600(A);
 #pragma unroll
@@ -754,11 +781,20 @@ __global__ void __launch_bounds__(128) kyber_enc_hash_pre(int n, const uint8_t *
     }
 }
 // encaps epilogue: ss = KDF(K-bar || H(c))
+// ML-KEM: ss = K (copied, no hashing)
 template <int K, int V>
-__global__ void __launch_bounds__(128) kyber_enc_hash_post(int n, const uint8_t *ct, const uint8_t *scratch, uint8_t *ss) {
+__global__ void __launch_bounds__(128) kyber_enc_hash_post(int n, const uint8_t *ct, const uint8_t *scratch, uint8_t *ss,
+                                                           int kem) {
     using Pp = P<K, V>;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
+    if (kem == KEM_MLKEM) {
+        const uint2 *kb = reinterpret_cast<const uint2 *>(scratch + (size_t)x * 96 + 64);
+        uint2 *o = reinterpret_cast<uint2 *>(ss + (size_t)x * 32);
+#pragma unroll
+        for (int i = 0; i < 4; i++) o[i] = kb[i];
+        return;
+    }
     uint2 A[25], hc[4];
     keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(ct + (size_t)x * Pp::CTB), Pp::CTB / 8, DOM_SHA3);
     keccak_f1600(A);
@@ -778,14 +814,20 @@ __global__ void __launch_bounds__(128) kyber_enc_hash_post(int n, const uint8_t 
 #pragma unroll
     for (int i = 0; i < 4; i++) o[i] = A[i];
 }
-// decaps prologue: H(c)
+// decaps prologue: H(c); ML-KEM: the rejection key J(z || c) = SHAKE256(z || c, 32)
 template <int K, int V>
-__global__ void __launch_bounds__(128) kyber_dec_hash_pre(int n, const uint8_t *ct, uint8_t *hct) {
+__global__ void __launch_bounds__(128) kyber_dec_hash_pre(int n, const uint8_t *ct, const uint8_t *sk, uint8_t *hct,
+                                                          int kem) {
     using Pp = P<K, V>;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
     uint2 A[25];
-    keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(ct + (size_t)x * Pp::CTB), Pp::CTB / 8, DOM_SHA3);
+    const uint2 *c = reinterpret_cast<const uint2 *>(ct + (size_t)x * Pp::CTB);
+    if (kem == KEM_MLKEM)
+        keccak_absorb_lanes2<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(sk + (size_t)x * Pp::SKB + Pp::SKB - 32), 4,
+                                             c, Pp::CTB / 8, DOM_SHAKE);
+    else
+        keccak_absorb_lanes<SHA3_256_LANES>(A, c, Pp::CTB / 8, DOM_SHA3);
     keccak_f1600(A);
     uint2 *o = reinterpret_cast<uint2 *>(hct + (size_t)x * 32);
 #pragma unroll
@@ -825,7 +867,7 @@ static cudaError_t ensure_smem(Kern kern, size_t bytes) {
 template <int K, int V>
 static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int coins_stride, int kem,
                           uint8_t *scratch, int plain, cudaStream_t st) {
-    if (plain) return kem ? plain_keypair<K, V>(n, pk, sk, coins, coins_stride, scratch, st) : PQCGPU_EUNSUPPORTED;
+    if (plain) return kem == KEM_FO ? plain_keypair<K, V>(n, pk, sk, coins, coins_stride, scratch, st) : PQCGPU_EUNSUPPORTED;
     const int NI = g_ni[0][K - 2], NT = g_threads[0][K - 2];
     const size_t sm = Layout<3 * K, 128>::bytes(NI, NT);
     if (ensure_smem(kyber_kp_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
@@ -838,7 +880,7 @@ static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins,
 template <int K, int V>
 static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
                       uint8_t *scratch, int kem, int plain, cudaStream_t st) {
-    if (plain) return kem ? plain_enc<K, V>(n, ct, ss, pk, coins, scratch, st) : PQCGPU_EUNSUPPORTED;
+    if (plain) return kem == KEM_FO ? plain_enc<K, V>(n, ct, ss, pk, coins, scratch, st) : PQCGPU_EUNSUPPORTED;
     const int NI = g_ni[1][K - 2], NT = g_threads[1][K - 2];
     const size_t sm = Layout<2 * K + 1, enc_seed_bytes<K>()>::bytes(NI, NT);
     if (ensure_smem(kyber_enc_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
@@ -849,7 +891,7 @@ static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const 
     a.pk_stride = P<K, V>::PKB;
     if (kem) {
         PQC_LAUNCH(st, "kyber_enc_hash_pre", K, V,
-                   kyber_enc_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, coins, scratch));
+                   kyber_enc_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, coins, scratch, kem));
         a.m = scratch;
         a.m_stride = 96;
         a.r = scratch + 32;
@@ -863,14 +905,14 @@ static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const 
     PQC_LAUNCH(st, "kyber_enc_core", K, V, kyber_enc_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
     if (kem)
         PQC_LAUNCH(st, "kyber_enc_hash_post", K, V,
-                   kyber_enc_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, scratch, ss));
+                   kyber_enc_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, scratch, ss, kem));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
 template <int K, int V>
 static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, int kem,
                       int plain, cudaStream_t st) {
-    if (plain) return kem ? plain_dec<K, V>(n, out, ct, sk, scratch, st) : PQCGPU_EUNSUPPORTED;
+    if (plain) return kem == KEM_FO ? plain_dec<K, V>(n, out, ct, sk, scratch, st) : PQCGPU_EUNSUPPORTED;
     const int NI = g_ni[2][K - 2], NT = g_threads[2][K - 2];
     const size_t sm = Layout<2 * K + 1, enc_seed_bytes<K>()>::bytes(NI, NT);
     if (ensure_smem(kyber_dec_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
@@ -882,7 +924,9 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
     d.ss = kem ? out : nullptr;
     d.hct = scratch;
     d.kem = kem;
-    if (kem) PQC_LAUNCH(st, "kyber_dec_hash_pre", K, V, kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, scratch));
+    if (kem)
+        PQC_LAUNCH(st, "kyber_dec_hash_pre", K, V,
+                   kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, sk, scratch, kem));
     PQC_LAUNCH(st, "kyber_dec_core", K, V, kyber_dec_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }

@@ -401,10 +401,10 @@ static int plain_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const u
     using Pp = P<K, V>;
     const int TPB = 128, g = (n + TPB - 1) / TPB;
     uint8_t *seeds = scratch + plain::scratch_per_instance<K>() * n - (size_t)(96 + 64 + 32 + 16) * n;
-    PQC_LAUNCH(st, "plain_enc_hash_pre", K, V, kyber_enc_hash_pre<K, V><<<g, TPB, 0, st>>>(n, pk, coins, seeds));
+    PQC_LAUNCH(st, "plain_enc_hash_pre", K, V, kyber_enc_hash_pre<K, V><<<g, TPB, 0, st>>>(n, pk, coins, seeds, KEM_FO));
     const int rc = plain_encrypt<K, V>(n, scratch, pk, Pp::PKB, seeds, ct, nullptr, nullptr, st);
     if (rc) return rc;
-    PQC_LAUNCH(st, "plain_enc_hash_post", K, V, kyber_enc_hash_post<K, V><<<g, TPB, 0, st>>>(n, ct, seeds, ss));
+    PQC_LAUNCH(st, "plain_enc_hash_post", K, V, kyber_enc_hash_post<K, V><<<g, TPB, 0, st>>>(n, ct, seeds, ss, KEM_FO));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
@@ -417,7 +417,7 @@ static int plain_dec(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, u
     uint8_t *seeds = tail, *hct = tail + (size_t)160 * n, *fail = tail + (size_t)192 * n;
     int16_t *base = reinterpret_cast<int16_t *>(scratch);
     Soa bp{base, n}, skpv = bp.poly(K), v = bp.poly(2 * K), mp = bp.poly(2 * K + 1);
-    PQC_LAUNCH(st, "plain_dec_hash_pre", K, V, kyber_dec_hash_pre<K, V><<<g, TPB, 0, st>>>(n, ct, hct));
+    PQC_LAUNCH(st, "plain_dec_hash_pre", K, V, kyber_dec_hash_pre<K, V><<<g, TPB, 0, st>>>(n, ct, sk, hct, KEM_FO));
     auto uc = k_unpack_ct<K, V>;
     PL("unpack_ct", uc, n, bp, v, ct);
     PL("frombytes", k_frombytes<K>, n, skpv, sk, Pp::SKB, K);

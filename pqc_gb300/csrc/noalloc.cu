@@ -52,6 +52,9 @@ extern "C" int pqcgpu_kem_enc_batch_noalloc(pqcgpu_alg alg, size_t n, uint8_t *c
     case PQCGPU_KYBER768: variant = 3; k = 3; break;
     case PQCGPU_KYBER1024: variant = 3; k = 4; break;
     case PQCGPU_KYBER1024_R2: variant = 2; k = 4; break;
+    case PQCGPU_MLKEM512: variant = 3; k = 2; break;
+    case PQCGPU_MLKEM768: variant = 3; k = 3; break;
+    case PQCGPU_MLKEM1024: variant = 3; k = 4; break;
     default: return pqc::set_error(PQCGPU_EUNSUPPORTED, "the no-allocation encapsulation covers the Kyber algorithms");
     }
     if (n == 0) return PQCGPU_OK;
@@ -66,7 +69,8 @@ extern "C" int pqcgpu_kem_enc_batch_noalloc(pqcgpu_alg alg, size_t n, uint8_t *c
     uint8_t *scratch = nullptr;
     int rc = noalloc_setup(device, &scratch);
     if (rc) return rc;
-    rc = pqc::kyber_enc_dev(variant, k, (int)n, ct, ss, pk, nullptr, coins, scratch, 1, 0, (cudaStream_t)stream);
+    rc = pqc::kyber_enc_dev(variant, k, (int)n, ct, ss, pk, nullptr, coins, scratch, pqc::kyber_kem_mode(alg), 0,
+                            (cudaStream_t)stream);
     if (rc) return pqc::set_error(rc, "kernel launch failed");
     return PQCGPU_OK;
 }

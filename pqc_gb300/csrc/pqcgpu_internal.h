@@ -53,6 +53,15 @@ int kyber_get_shape(int op, int k, int *ni, int *threads);
 // Scratch bytes per instance (op 0 keypair, 1 enc, 2 dec; plain = the per-stage baseline path).
 size_t kyber_scratch_bytes(int k, int op, int plain);
 // coins: d (CPA) or d||z (KEM) at `coins_stride`.  kem=1 writes the full KEM secret key.
+// AES-256 CTR_DRBG without derivation function (SP 800-90A 10.2.1), as in the NIST KAT generator (kat.cu)
+struct CtrDrbg {
+    uint8_t key[32], v[16];
+    uint64_t reseed_counter = 0;
+    void instantiate(const uint8_t entropy[48], const uint8_t *personalization);
+    void generate(uint8_t *out, size_t n);
+    void update(const uint8_t *provided);
+};
+int kyber_kem_mode(int alg);  // 1: round-2 / round-3 FO KEM, 2: ML-KEM (FIPS 203)
 int kyber_keypair_dev(int variant, int k, int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int coins_stride,
                       int kem, uint8_t *scratch, int plain, cudaStream_t st);
 // kem=1: coins 32 B/instance, m ignored.  kem=0: CPA enc with m, coins.
@@ -78,8 +87,11 @@ int frodo_init_constants();
 size_t frodo_scratch_bytes();  // per instance, all three operations
 int frodo_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
                       cudaStream_t st);
+// pkh: optional SHAKE256(pk, 24) per instance (24-byte stride), e.g. from a resident secret key
 int frodo_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
-                  cudaStream_t st);
+                  cudaStream_t st, const uint8_t *pkh = nullptr);
 int frodo_dec_dev(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, cudaStream_t st);
+int frodo_set_shape(int op, int parts, int threads);
+int frodo_get_shape(int op, int *parts, int *threads);
 
 }  // namespace pqc

@@ -52,6 +52,15 @@ __global__ void rows_scatter(uint4 *dst, const uint4 *src, const uint32_t *idx, 
     uint4 *d = dst + (size_t)idx[r] * row16;
     for (int i = threadIdx.x & 31; i < row16; i += 32) d[i] = s[i];
 }
+// dst[i] = `words` 8-byte words at byte offset `off` of row idx[i] of src (row, off 8-byte aligned)
+__global__ void rows_tail_gather(uint2 *dst, const uint8_t *src, const uint32_t *idx, int n, size_t row, size_t off,
+                                 int words) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * words) return;
+    const int i = t / words, w = t % words;
+    dst[t] = reinterpret_cast<const uint2 *>(src + (size_t)idx[i] * row + off)[w];
+}
+
 void launch_rows(bool gather, uint8_t *dst, const uint8_t *src, const uint32_t *idx, int n, size_t row, cudaStream_t st) {
     if (n <= 0) return;
     const dim3 grid(1, (n + 7) / 8);
@@ -79,18 +88,31 @@ struct KeyStore {
     std::vector<uint8_t> used;
 };
 
+// One in-flight batch: a stream, staging buffers and a worker thread that packs the inputs, runs
+// the copies and kernels, waits for them and hands the results back.  The dispatcher fills in the
+// job under the server mutex; the worker runs it without the mutex.
 struct Slot {
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;     // the stream of the current job (hi or lo)
+    cudaStream_t hi = nullptr, lo = nullptr;  // light algorithms run at high priority, FrodoKEM at low
     cudaEvent_t done = nullptr;
     uint8_t *dbuf = nullptr;  // device staging
     size_t dcap = 0;
     uint8_t *hbuf = nullptr;  // pinned host staging
     size_t hcap = 0;
-    bool busy = false;
+    bool busy = false;     // assigned by the dispatcher, until the worker has completed it
+    bool has_job = false;  // handed over, not yet picked up by the worker
+    std::condition_variable cv;
+    std::thread th;
+    // the job
     int alg = 0, op = 0, n = 0;
+    bool by_handle = false;
+    bool use_pkh = false;  // FrodoKEM encaps by handle: pkh = SHAKE256(pk) taken from the resident sk
     std::vector<Req *> reqs;
-    size_t off_in0 = 0, off_in1 = 0, off_out0 = 0, off_out1 = 0, off_idx = 0, off_scr = 0;
-    size_t h_in0 = 0, h_in1 = 0, h_out0 = 0, h_out1 = 0, h_idx = 0;
+    std::vector<uint32_t> idx;
+    uint8_t *kpk = nullptr, *ksk = nullptr;  // key store rows of `alg` (stable while any slot is busy)
+    size_t pkb = 0, skb = 0;
+    // staging layout, device and host alike: [idx | host inputs | gathered input | out0 | out1 | scratch]
+    size_t off_in0 = 0, off_in1 = 0, off_out0 = 0, off_out1 = 0, off_scr = 0, off_pkh = 0, h2d_bytes = 0, d2h_bytes = 0;
 };
 
 size_t r256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -104,17 +126,20 @@ struct pqcgpu_server {
     int device = 0;
     size_t budget = 0, used = 0;
     int max_inflight = 4, max_batch = 4096;
-    std::vector<Slot> slots;
+    std::vector<std::unique_ptr<Slot>> slots;
     KeyStore ks[PQCGPU_NUM_ALGS];
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
+    uint64_t events = 0;  // bumped on every submit and completion; the dispatcher sleeps until it moves
     // one FIFO per (algorithm, operation); the dispatcher serves the group with the oldest head
     std::deque<Req *> groups[PQCGPU_NUM_ALGS][3];
     size_t pending = 0;
     int heavy_running = 0;  // in-flight FrodoKEM batches (may hold at most half of the slots)
+    int grow_alg = -1;      // a key store waits to grow: no new batch starts until all slots are idle
+    uint32_t grow_need = 0;
     std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
     uint64_t next_ticket = 1;
-    bool stop = false;
+    bool stop = false, stop_workers = false;
     std::thread th;
     std::vector<double> lat_ms;
     std::vector<double> lat_grp[PQCGPU_NUM_ALGS][3];  // the same samples per (algorithm, operation)
@@ -136,7 +161,13 @@ struct pqcgpu_server {
             used -= bytes;
         }
     }
-    // grow the key store of `alg` to at least `need` slots (called by the dispatcher only)
+    bool any_busy() const {
+        for (auto &sl : slots)
+            if (sl->busy) return true;
+        return false;
+    }
+    // Grow the key store of `alg` to at least `need` rows.  Only called with every slot idle: the
+    // rows move to new arrays, and no batch may hold the old pointers.
     int grow_keys(int alg, uint32_t need) {
         KeyStore &k = ks[alg];
         if (need <= k.cap) return PQCGPU_OK;
@@ -179,45 +210,32 @@ struct pqcgpu_server {
         }
     }
 
-    // Reap finished batches: scatter results to the requests' host buffers.
-    void reap(std::unique_lock<std::mutex> &lk) {
-        for (auto &s : slots) {
-            if (!s.busy || cudaEventQuery(s.done) != cudaSuccess) continue;
-            size_t sz[4];
-            op_io_sizes(s.alg, s.op, sz);
-            const auto now = Clock::now();
-            for (int i = 0; i < s.n; i++) {
-                Req *q = s.reqs[i];
-                if (s.op == PQCGPU_OP_KEYPAIR) {
-                    if (q->r.out0) memcpy(q->r.out0, s.hbuf + s.h_out0 + (size_t)i * sz[2], sz[2]);
-                    if (q->r.key_out) *q->r.key_out = ((uint64_t)s.alg << 48) | (uint64_t)(q->key_slot + 1);
-                } else if (s.op == PQCGPU_OP_ENC) {
-                    memcpy(q->r.out0, s.hbuf + s.h_out0 + (size_t)i * sz[2], sz[2]);
-                    memcpy(q->r.out1, s.hbuf + s.h_out1 + (size_t)i * sz[3], sz[3]);
-                } else {
-                    memcpy(q->r.out0, s.hbuf + s.h_out0 + (size_t)i * sz[2], sz[2]);
-                }
-                finish(q, 0, std::chrono::duration<double, std::milli>(now - q->t0).count());
-            }
-            s.reqs.clear();
-            s.busy = false;
-            if (s.alg == PQCGPU_FRODO976) heavy_running--;
-            batches++;
-            cv_done.notify_all();
-        }
-        (void)lk;
-    }
-
-    // Form and launch one batch on a free slot; returns false if nothing was launched.
-    bool launch_one(std::unique_lock<std::mutex> &lk) {
+    // Pick the next batch and hand it to a free slot's worker (mutex held).  Returns false when
+    // nothing can start now.
+    bool assign_one() {
         if (!pending) return false;
         Slot *slot = nullptr;
         for (auto &s : slots)
-            if (!s.busy) {
-                slot = &s;
+            if (!s->busy) {
+                slot = s.get();
                 break;
             }
         if (!slot) return false;
+        if (grow_alg >= 0) {
+            if (any_busy()) return false;
+            const int ga = grow_alg;
+            grow_alg = -1;
+            if (grow_keys(ga, ks[ga].cap + grow_need)) {
+                // no memory for more keys: refuse the waiting keypair requests of that algorithm
+                auto &g = groups[ga][PQCGPU_OP_KEYPAIR];
+                while (!g.empty() && ks[ga].free_slots.empty()) {
+                    finish(g.front(), PQCGPU_EBUDGET, 0);
+                    g.pop_front();
+                    pending--;
+                }
+                cv_done.notify_all();
+            }
+        }
         // oldest group head; FrodoKEM (heavy: ~10^4 Keccak permutations per instance) may hold at
         // most half of the slots so that the light algorithms always find one
         const int heavy_max = std::max(1, max_inflight / 2);
@@ -235,63 +253,88 @@ struct pqcgpu_server {
             }
         if (alg < 0) return false;
         const int cap = (alg == PQCGPU_FRODO976) ? std::min(max_batch, 256) : max_batch;
-        std::vector<Req *> take;
         auto &grp = groups[alg][op];
-        while (!grp.empty() && (int)take.size() < cap) {
-            take.push_back(grp.front());
-            grp.pop_front();
-        }
-        pending -= take.size();
-        size_t sz[4];
-        op_io_sizes(alg, op, sz);
-        const size_t scr = op_scratch_bytes(alg, op, 0);
         KeyStore &k = ks[alg];
-        // keys: keypair reserves slots; enc / dec by handle resolve them (invalid -> error now)
-        std::vector<uint32_t> idx;
+        const size_t take_n = std::min<size_t>(grp.size(), (size_t)cap);
+        if (op == PQCGPU_OP_KEYPAIR && k.free_slots.size() < take_n) {
+            if (any_busy()) {  // grow once every in-flight batch is done
+                grow_alg = alg;
+                grow_need = (uint32_t)(take_n - k.free_slots.size());
+                return false;
+            }
+            if (grow_keys(alg, k.cap + (uint32_t)(take_n - k.free_slots.size())) && k.free_slots.empty()) {
+                finish(grp.front(), PQCGPU_EBUDGET, 0);
+                grp.pop_front();
+                pending--;
+                cv_done.notify_all();
+                return true;
+            }
+        }
         std::vector<Req *> ok;
-        for (Req *q : take) {
+        std::vector<uint32_t> idx;
+        while (!grp.empty() && (int)ok.size() < cap) {
+            Req *q = grp.front();
             uint32_t ksl = 0;
             if (op == PQCGPU_OP_KEYPAIR) {
-                if (k.free_slots.empty() && grow_keys(alg, k.cap + (uint32_t)take.size())) {
-                    finish(q, PQCGPU_EBUDGET, 0);
-                    continue;
-                }
+                if (k.free_slots.empty()) break;
                 ksl = k.free_slots.back();
                 k.free_slots.pop_back();
                 k.used[ksl] = 1;
             } else if (q->r.key || op == PQCGPU_OP_DEC) {
                 if (!key_ok(q->r.key, alg, &ksl)) {
+                    grp.pop_front();
+                    pending--;
                     finish(q, PQCGPU_EINVAL, 0);
+                    cv_done.notify_all();
                     continue;
                 }
             }
+            // an encapsulation batch is either all by handle or all by explicit pk
+            if (op == PQCGPU_OP_ENC && !ok.empty() && ((q->r.key != 0) != (ok[0]->r.key != 0))) break;
+            grp.pop_front();
+            pending--;
             q->key_slot = ksl;
             idx.push_back(ksl);
             ok.push_back(q);
         }
-        if (ok.empty()) {
-            cv_done.notify_all();
-            return true;
-        }
+        if (ok.empty()) return true;
         const int n = (int)ok.size();
         const bool by_handle = (op == PQCGPU_OP_DEC) || (op == PQCGPU_OP_ENC && ok[0]->r.key != 0);
-        // staging layout (device and pinned host alike)
+        size_t sz[4];
+        op_io_sizes(alg, op, sz);
         Slot &s = *slot;
-        size_t d = 0;
-        s.off_in0 = d; d += r256(sz[0] * n);
-        s.off_in1 = d; d += r256(sz[1] * n);
-        s.off_out0 = d; d += r256(sz[2] * n);
-        s.off_out1 = d; d += r256(sz[3] * n);
-        s.off_idx = d; d += r256(4 * (size_t)n);
-        s.off_scr = d; d += r256(scr * n);
+        // staging layout: idx, host-packed inputs, gathered input, outputs, scratch
+        size_t d = r256(4 * (size_t)n), in0 = 0, in1 = 0;
+        if (op == PQCGPU_OP_KEYPAIR) {
+            in0 = d; d += r256(sz[0] * n);
+        } else if (op == PQCGPU_OP_ENC) {
+            in1 = d; d += r256(sz[1] * n);            // coins
+            if (!by_handle) { in0 = d; d += r256(sz[0] * n); }
+        } else {
+            in0 = d; d += r256(sz[0] * n);            // ct
+        }
+        const size_t h2d = d;
+        if (op == PQCGPU_OP_ENC && by_handle) { in0 = d; d += r256(sz[0] * n); }   // pk gathered
+        if (op == PQCGPU_OP_DEC) { in1 = d; d += r256(sz[1] * n); }                // sk gathered
+        // FrodoKEM keeps pkh = SHAKE256(pk, 24) as the last 24 bytes of its secret key
+        const bool use_pkh = alg == PQCGPU_FRODO976 && op == PQCGPU_OP_ENC && by_handle;
+        size_t pkh = 0;
+        if (use_pkh) { pkh = d; d += r256(24 * (size_t)n); }
+        const size_t out0 = d;
+        d += r256(sz[2] * n);
+        const size_t out1 = d;
+        d += r256(sz[3] * n);
+        const size_t hneed = d;
+        const size_t d2h = (op == PQCGPU_OP_KEYPAIR) ? sz[2] * n : (op == PQCGPU_OP_ENC ? out1 + sz[3] * n - out0 : sz[2] * n);
+        const size_t scr = d;
+        d += r256(op_scratch_bytes(alg, op, 0) * n);
         if (d > s.dcap) {
             free_dev(s.dbuf, s.dcap);
             s.dbuf = nullptr;
             s.dcap = 0;
             size_t want = d + d / 2;
             if (alloc_dev(&s.dbuf, want) && alloc_dev(&s.dbuf, d)) {
-                bool others = false;
-                for (auto &o : slots) others |= o.busy;
+                const bool others = any_busy();
                 for (auto it = ok.rbegin(); it != ok.rend(); ++it) {
                     Req *q = *it;
                     if (op == PQCGPU_OP_KEYPAIR) {
@@ -299,7 +342,7 @@ struct pqcgpu_server {
                         k.free_slots.push_back(q->key_slot);
                     }
                     if (others) {  // wait for in-flight batches to free memory
-                        groups[alg][op].push_front(q);
+                        grp.push_front(q);
                         pending++;
                     } else {
                         finish(q, PQCGPU_EBUDGET, 0);  // nothing will free memory: refuse
@@ -310,92 +353,167 @@ struct pqcgpu_server {
             }
             s.dcap = (s.dbuf && used >= want) ? want : d;
         }
-        if (d > s.hcap) {
+        if (hneed > s.hcap) {
             if (s.hbuf) cudaFreeHost(s.hbuf);
             s.hbuf = nullptr;
             s.hcap = 0;
-            if (cudaMallocHost(&s.hbuf, d + d / 2) != cudaSuccess) {
+            if (cudaMallocHost(&s.hbuf, hneed + hneed / 2) != cudaSuccess) {
                 cudaGetLastError();
-                for (Req *q : ok) finish(q, PQCGPU_ENOMEM, 0);
+                for (Req *q : ok) {
+                    if (op == PQCGPU_OP_KEYPAIR) {
+                        k.used[q->key_slot] = 0;
+                        k.free_slots.push_back(q->key_slot);
+                    }
+                    finish(q, PQCGPU_ENOMEM, 0);
+                }
                 cv_done.notify_all();
                 return true;
             }
-            s.hcap = d + d / 2;
+            s.hcap = hneed + hneed / 2;
         }
-        s.h_in0 = s.off_in0;
-        s.h_in1 = s.off_in1;
-        s.h_out0 = s.off_out0;
-        s.h_out1 = s.off_out1;
-        s.h_idx = s.off_idx;
-        // pack host inputs
-        for (int i = 0; i < n; i++) {
-            const pqcgpu_request &r = ok[i]->r;
-            if (op == PQCGPU_OP_KEYPAIR) {
-                if (r.in) memcpy(s.hbuf + s.h_in0 + (size_t)i * sz[0], r.in, sz[0]);
-                else pqcgpu_randombytes(s.hbuf + s.h_in0 + (size_t)i * sz[0], sz[0]);
-            } else if (op == PQCGPU_OP_ENC) {
-                if (!by_handle) memcpy(s.hbuf + s.h_in0 + (size_t)i * sz[0], r.pk, sz[0]);
-                if (r.in) memcpy(s.hbuf + s.h_in1 + (size_t)i * sz[1], r.in, sz[1]);
-                else pqcgpu_randombytes(s.hbuf + s.h_in1 + (size_t)i * sz[1], sz[1]);
-            } else {
-                memcpy(s.hbuf + s.h_in0 + (size_t)i * sz[0], r.in, sz[0]);
-            }
-        }
-        memcpy(s.hbuf + s.h_idx, idx.data(), 4 * (size_t)n);
         s.alg = alg;
         s.op = op;
         s.n = n;
-        s.reqs = ok;
+        s.by_handle = by_handle;
+        s.reqs.swap(ok);
+        s.idx.swap(idx);
+        s.kpk = k.dpk;
+        s.ksk = k.dsk;
+        s.pkb = k.pkb;
+        s.skb = k.skb;
+        s.off_in0 = in0;
+        s.off_in1 = in1;
+        s.off_out0 = out0;
+        s.off_out1 = out1;
+        s.off_scr = scr;
+        s.use_pkh = use_pkh;
+        s.off_pkh = pkh;
+        s.h2d_bytes = h2d;
+        s.d2h_bytes = d2h;
+        s.stream = (alg == PQCGPU_FRODO976) ? s.lo : s.hi;
         s.busy = true;
+        s.has_job = true;
         if (alg == PQCGPU_FRODO976) heavy_running++;
-        lk.unlock();
-        // device work on the slot stream
-        cudaStream_t st = s.stream;
-        uint8_t *D = s.dbuf, *H = s.hbuf;
-        const uint32_t *didx = (const uint32_t *)(D + s.off_idx);
-        cudaMemcpyAsync(D + s.off_idx, H + s.h_idx, 4 * (size_t)n, cudaMemcpyHostToDevice, st);
-        if (op == PQCGPU_OP_KEYPAIR) {
-            cudaMemcpyAsync(D + s.off_in0, H + s.h_in0, sz[0] * n, cudaMemcpyHostToDevice, st);
-            op_dev(alg, op, n, D + s.off_in0, nullptr, D + s.off_out0, D + s.off_out1, D + s.off_scr, 0, st);
-            launch_rows(false, k.dpk, D + s.off_out0, didx, n, k.pkb, st);
-            launch_rows(false, k.dsk, D + s.off_out1, didx, n, k.skb, st);
-            cudaMemcpyAsync(H + s.h_out0, D + s.off_out0, sz[2] * n, cudaMemcpyDeviceToHost, st);
-        } else if (op == PQCGPU_OP_ENC) {
-            if (by_handle) launch_rows(true, D + s.off_in0, k.dpk, didx, n, k.pkb, st);
-            else cudaMemcpyAsync(D + s.off_in0, H + s.h_in0, sz[0] * n, cudaMemcpyHostToDevice, st);
-            cudaMemcpyAsync(D + s.off_in1, H + s.h_in1, sz[1] * n, cudaMemcpyHostToDevice, st);
-            op_dev(alg, op, n, D + s.off_in0, D + s.off_in1, D + s.off_out0, D + s.off_out1, D + s.off_scr, 0, st);
-            cudaMemcpyAsync(H + s.h_out0, D + s.off_out0, sz[2] * n, cudaMemcpyDeviceToHost, st);
-            cudaMemcpyAsync(H + s.h_out1, D + s.off_out1, sz[3] * n, cudaMemcpyDeviceToHost, st);
-        } else {
-            cudaMemcpyAsync(D + s.off_in0, H + s.h_in0, sz[0] * n, cudaMemcpyHostToDevice, st);
-            launch_rows(true, D + s.off_in1, k.dsk, didx, n, k.skb, st);
-            op_dev(alg, op, n, D + s.off_in0, D + s.off_in1, D + s.off_out0, nullptr, D + s.off_scr, 0, st);
-            cudaMemcpyAsync(H + s.h_out0, D + s.off_out0, sz[2] * n, cudaMemcpyDeviceToHost, st);
-        }
-        cudaEventRecord(s.done, st);
-        lk.lock();
+        s.cv.notify_one();
         return true;
+    }
+
+    // The worker's half of a batch (no mutex): pack, copy up, run, copy down, wait, unpack.
+    int execute(Slot &s) {
+        size_t sz[4];
+        op_io_sizes(s.alg, s.op, sz);
+        const int n = s.n, op = s.op, alg = s.alg;
+        uint8_t *H = s.hbuf, *D = s.dbuf;
+        memcpy(H, s.idx.data(), 4 * (size_t)n);
+        size_t missing = 0;  // coins drawn from the library DRBG in one call
+        for (int i = 0; i < n; i++) {
+            const pqcgpu_request &r = s.reqs[i]->r;
+            if (op == PQCGPU_OP_KEYPAIR) {
+                if (r.in) memcpy(H + s.off_in0 + (size_t)i * sz[0], r.in, sz[0]);
+                else missing++;
+            } else if (op == PQCGPU_OP_ENC) {
+                if (!s.by_handle) memcpy(H + s.off_in0 + (size_t)i * sz[0], r.pk, sz[0]);
+                if (r.in) memcpy(H + s.off_in1 + (size_t)i * sz[1], r.in, sz[1]);
+                else missing++;
+            } else {
+                memcpy(H + s.off_in0 + (size_t)i * sz[0], r.in, sz[0]);
+            }
+        }
+        if (missing) {
+            const size_t off = op == PQCGPU_OP_KEYPAIR ? s.off_in0 : s.off_in1, b = sz[op == PQCGPU_OP_KEYPAIR ? 0 : 1];
+            for (int i = 0; i < n; i++)
+                if (!s.reqs[i]->r.in) pqcgpu_randombytes(H + off + (size_t)i * b, b);
+        }
+        cudaStream_t st = s.stream;
+        const uint32_t *didx = (const uint32_t *)D;
+        cudaMemcpyAsync(D, H, s.h2d_bytes, cudaMemcpyHostToDevice, st);
+        int rc = PQCGPU_OK;
+        if (op == PQCGPU_OP_KEYPAIR) {
+            rc = op_dev(alg, op, n, D + s.off_in0, nullptr, D + s.off_out0, D + s.off_out1, D + s.off_scr, 0, st);
+            launch_rows(false, s.kpk, D + s.off_out0, didx, n, s.pkb, st);
+            launch_rows(false, s.ksk, D + s.off_out1, didx, n, s.skb, st);
+        } else if (op == PQCGPU_OP_ENC) {
+            if (s.by_handle) launch_rows(true, D + s.off_in0, s.kpk, didx, n, s.pkb, st);
+            if (s.use_pkh) {
+                const int words = 3;
+                PQC_LAUNCH(st, "rows_tail_gather", 0, 0,
+                           rows_tail_gather<<<(n * words + 255) / 256, 256, 0, st>>>(
+                               (uint2 *)(D + s.off_pkh), s.ksk, didx, n, s.skb, s.skb - 24, words));
+                rc = frodo_enc_dev(n, D + s.off_out0, D + s.off_out1, D + s.off_in0, D + s.off_in1, D + s.off_scr, st,
+                                   D + s.off_pkh);
+            } else {
+                rc = op_dev(alg, op, n, D + s.off_in0, D + s.off_in1, D + s.off_out0, D + s.off_out1, D + s.off_scr, 0,
+                            st);
+            }
+        } else {
+            launch_rows(true, D + s.off_in1, s.ksk, didx, n, s.skb, st);
+            rc = op_dev(alg, op, n, D + s.off_in0, D + s.off_in1, D + s.off_out0, nullptr, D + s.off_scr, 0, st);
+        }
+        cudaMemcpyAsync(H + s.off_out0, D + s.off_out0, s.d2h_bytes, cudaMemcpyDeviceToHost, st);
+        cudaEventRecord(s.done, st);
+        // poll, yielding the core between polls: up to 16 workers share the host's cores
+        cudaError_t q;
+        while ((q = cudaEventQuery(s.done)) == cudaErrorNotReady) std::this_thread::yield();
+        if (q != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = PQCGPU_ECUDA;
+        if (rc) return rc;
+        for (int i = 0; i < n; i++) {
+            Req *q = s.reqs[i];
+            if (op == PQCGPU_OP_KEYPAIR) {
+                if (q->r.out0) memcpy(q->r.out0, H + s.off_out0 + (size_t)i * sz[2], sz[2]);
+                if (q->r.key_out) *q->r.key_out = ((uint64_t)alg << 48) | (uint64_t)(q->key_slot + 1);
+            } else if (op == PQCGPU_OP_ENC) {
+                memcpy(q->r.out0, H + s.off_out0 + (size_t)i * sz[2], sz[2]);
+                memcpy(q->r.out1, H + s.off_out1 + (size_t)i * sz[3], sz[3]);
+            } else {
+                memcpy(q->r.out0, H + s.off_out0 + (size_t)i * sz[2], sz[2]);
+            }
+        }
+        return PQCGPU_OK;
+    }
+
+    // Record the batch's outcome and free the slot (mutex held).
+    void complete(Slot &s, int rc) {
+        const auto now = Clock::now();
+        for (Req *q : s.reqs) {
+            if (rc && s.op == PQCGPU_OP_KEYPAIR) {
+                ks[s.alg].used[q->key_slot] = 0;
+                ks[s.alg].free_slots.push_back(q->key_slot);
+            }
+            finish(q, rc, std::chrono::duration<double, std::milli>(now - q->t0).count());
+        }
+        if (rc && error.empty()) error = "a batch failed on the device";
+        s.reqs.clear();
+        s.busy = false;
+        if (s.alg == PQCGPU_FRODO976) heavy_running--;
+        batches++;
+        events++;
+        cv_work.notify_one();
+        cv_done.notify_all();
+    }
+
+    void work(Slot *s) {
+        cudaSetDevice(device);
+        std::unique_lock<std::mutex> lk(mu);
+        while (true) {
+            s->cv.wait(lk, [&] { return s->has_job || stop_workers; });
+            if (!s->has_job) break;
+            s->has_job = false;
+            lk.unlock();
+            const int rc = execute(*s);
+            lk.lock();
+            complete(*s, rc);
+        }
     }
 
     void run() {
         cudaSetDevice(device);
         std::unique_lock<std::mutex> lk(mu);
         while (true) {
-            reap(lk);
-            bool launched = false;
-            while (launch_one(lk)) launched = true;
-            bool any_busy = false;
-            for (auto &s : slots) any_busy |= s.busy;
-            if (stop && !pending && !any_busy) break;
-            if (!launched) {
-                if (any_busy) {
-                    // poll the in-flight batches; new requests wake us immediately
-                    cv_work.wait_for(lk, std::chrono::microseconds(20));
-                } else {
-                    cv_work.wait(lk, [&] { return stop || pending; });
-                }
+            const uint64_t seen = events;
+            while (assign_one()) {
             }
+            if (stop && !pending && !any_busy()) break;
+            cv_work.wait(lk, [&] { return events != seen || (stop && !pending && !any_busy()); });
         }
     }
 };
@@ -414,16 +532,27 @@ extern "C" int pqcgpu_server_create(pqcgpu_server **out, int device, size_t budg
     s->budget = budget ? budget : ((size_t)16 << 30);
     s->max_inflight = max_inflight > 0 ? std::min(max_inflight, 16) : 4;
     s->max_batch = max_batch > 0 ? max_batch : 4096;
-    s->slots.resize(s->max_inflight);
-    for (auto &sl : s->slots) {
-        cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
-        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+    // light batches (Kyber, NewHope: tens of microseconds of GPU time) get the high-priority
+    // streams so that their CTAs are scheduled ahead of waiting FrodoKEM CTAs
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    for (int i = 0; i < s->max_inflight; i++) {
+        s->slots.emplace_back(new Slot());
+        Slot *sl = s->slots.back().get();
+        cudaStreamCreateWithPriority(&sl->hi, cudaStreamNonBlocking, prio_hi);
+        cudaStreamCreateWithPriority(&sl->lo, cudaStreamNonBlocking, prio_lo);
+        sl->stream = sl->hi;
+        cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming);
     }
     for (int a = 0; a < PQCGPU_NUM_ALGS; a++) {
         size_t sz[4];
         op_io_sizes(a, PQCGPU_OP_KEYPAIR, sz);
         s->ks[a].pkb = sz[2];
         s->ks[a].skb = sz[3];
+    }
+    for (auto &sl : s->slots) {
+        Slot *p = sl.get();
+        p->th = std::thread([s, p] { s->work(p); });
     }
     s->th = std::thread([s] { s->run(); });
     *out = s;
@@ -450,6 +579,7 @@ extern "C" int pqcgpu_server_submit(pqcgpu_server *s, const pqcgpu_request *req,
         s->reqs[raw->ticket] = std::move(q);
         s->groups[req->alg][req->op].push_back(raw);
         s->pending++;
+        s->events++;
     }
     s->cv_work.notify_one();
     if (ticket) *ticket = raw->ticket;
@@ -473,12 +603,7 @@ extern "C" int pqcgpu_server_wait(pqcgpu_server *s, uint64_t ticket, int timeout
 extern "C" int pqcgpu_server_drain(pqcgpu_server *s) {
     if (!s) return PQCGPU_EINVAL;
     std::unique_lock<std::mutex> lk(s->mu);
-    s->cv_done.wait(lk, [&] {
-        if (s->pending) return false;
-        for (auto &sl : s->slots)
-            if (sl.busy) return false;
-        return true;
-    });
+    s->cv_done.wait(lk, [&] { return !s->pending && !s->any_busy(); });
     return PQCGPU_OK;
 }
 
@@ -543,14 +668,23 @@ extern "C" int pqcgpu_server_destroy(pqcgpu_server *s) {
         s->stop = true;
     }
     s->cv_work.notify_all();
-    if (s->th.joinable()) s->th.join();
+    if (s->th.joinable()) s->th.join();  // returns once nothing is pending or in flight
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop_workers = true;
+    }
+    for (auto &sl : s->slots) {
+        sl->cv.notify_all();
+        if (sl->th.joinable()) sl->th.join();
+    }
     cudaSetDevice(s->device);
     cudaDeviceSynchronize();
     for (auto &sl : s->slots) {
-        s->free_dev(sl.dbuf, sl.dcap);
-        if (sl.hbuf) cudaFreeHost(sl.hbuf);
-        cudaStreamDestroy(sl.stream);
-        cudaEventDestroy(sl.done);
+        s->free_dev(sl->dbuf, sl->dcap);
+        if (sl->hbuf) cudaFreeHost(sl->hbuf);
+        cudaStreamDestroy(sl->hi);
+        cudaStreamDestroy(sl->lo);
+        cudaEventDestroy(sl->done);
     }
     for (auto &k : s->ks) {
         s->free_dev(k.dpk, (size_t)k.cap * k.pkb);

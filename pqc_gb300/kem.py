@@ -8,7 +8,8 @@ import ctypes
 
 from . import _lib
 
-ALGS = {"kyber512": 0, "kyber768": 1, "kyber1024": 2, "kyber1024r2": 3, "newhope1024": 4, "frodo976": 5}
+ALGS = {"kyber512": 0, "kyber768": 1, "kyber1024": 2, "kyber1024r2": 3, "newhope1024": 4, "frodo976": 5,
+        "mlkem512": 6, "mlkem768": 7, "mlkem1024": 8}
 DEVICE_PTRS = 0x1
 PLAIN = 0x2
 

@@ -8,8 +8,9 @@ Fixture kinds:
   * ref_*.json      -- outputs of the reference's OWN device code (Kyber_GPU_Batched for k = 2/3/4,
                        round-2 semantics; NewHope_NIST_GPU), compiled for the host by
                        oracle/build_ref.sh and driven with the NIST per-instance seed layout.
+  * kat_*.rsp       -- NIST-format KAT records (AES-256 CTR_DRBG seeds and coins, oracle outputs).
   * restated_*.json -- outputs of the CPU oracle for paths the reference has no code for (Kyber
-                       round-3 KEM, NewHope CPA-KEM, FrodoKEM-976): regression pins, parity
+                       round-3 KEM, NewHope CPA-KEM, FrodoKEM-976, ML-KEM): regression pins, parity
                        unpinned by reference outputs.
 Inputs come from pqc_gb300.drbg with fixed seeds; every output is stored as SHA-256 per instance,
 and instance 0 is also stored in full.
@@ -129,6 +130,24 @@ def restated(name, alg, n, s):
     })
 
 
+def kat_rsp(name, alg, count=3):
+    """A NIST-format .rsp of `count` records, coins from the KAT CTR_DRBG flow (pqc_gb300.kat),
+    keys / ciphertexts from the oracle: a regression pin for the harness and the GPU path."""
+    from pqc_gb300 import kat
+    seed_list = kat.seeds(count)
+    sz = O.alg_sizes(alg)
+    recs = []
+    for i, sd in enumerate(seed_list):
+        kc, ec = kat.coins_for(name, sd)
+        pk, sk = O.batch_keypair(alg, 1, kc)
+        ct, ss = O.batch_enc(alg, 1, pk, ec)
+        assert O.batch_dec(alg, 1, ct, sk) == ss
+        recs.append({"count": i, "seed": sd, "pk": pk, "sk": sk, "ct": ct, "ss": ss})
+    assert all(len(r["pk"]) == sz["pk"] for r in recs)
+    with open(os.path.join(HERE, "kat_%s.rsp" % name), "w") as f:
+        f.write(kat.format_rsp(name, recs))
+
+
 if __name__ == "__main__":
     keccak()
     for k in (2, 3, 4):
@@ -140,4 +159,9 @@ if __name__ == "__main__":
     restated("kyber1024r2", O.KYBER1024_R2, 16, 0)
     restated("newhope1024", O.NEWHOPE1024, 16, 0)
     restated("frodo976", O.FRODO976, 4, 0)
+    restated("mlkem512", O.MLKEM512, 16, 0)
+    restated("mlkem768", O.MLKEM768, 16, 0)
+    restated("mlkem1024", O.MLKEM1024, 16, 0)
+    for name in ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976", "mlkem512", "mlkem768", "mlkem1024"):
+        kat_rsp(name, O.ALG_NAMES[name], 1 if name == "frodo976" else 3)
     print("fixtures written to", HERE)

@@ -66,3 +66,77 @@ def test_no_device_is_a_clean_error(lib):
     rc = lib.pqcgpu_ctx_create(ctypes.byref(h), 0, 0)
     assert rc == -3
     assert b"device" in lib.pqcgpu_last_error() or b"CUDA" in lib.pqcgpu_last_error()
+
+
+def test_frodo_launch_shape_validation():
+    """Shape setting is host-only (no device needed); bad splits / block sizes are refused."""
+    from pqc_gb300 import _lib, kem
+    lib = _lib.load()
+    fr = kem.alg_id("frodo976")
+    assert lib.pqcgpu_set_launch_shape(fr, 1, 3, 256) != 0
+    assert lib.pqcgpu_set_launch_shape(fr, 1, 2, 96) != 0
+    assert lib.pqcgpu_set_launch_shape(fr, 0, 2, 256) != 0
+    assert lib.pqcgpu_set_launch_shape(fr, 0, 0, 0) == 0
+
+
+class _CtrDrbgRestated:
+    """SP 800-90A AES-256 CTR_DRBG (no derivation function), restated over an independent AES
+    (the `cryptography` package) to check the library's own AES and DRBG."""
+
+    def __init__(self, aes_ecb, entropy, personalization=None):
+        self.aes = aes_ecb
+        seed = bytes(a ^ b for a, b in zip(entropy, personalization or bytes(48)))
+        self.key, self.v = bytes(32), bytes(16)
+        self._update(seed)
+
+    def _inc(self):
+        self.v = ((int.from_bytes(self.v, "big") + 1) % (1 << 128)).to_bytes(16, "big")
+
+    def _update(self, provided):
+        temp = b""
+        for _ in range(3):
+            self._inc()
+            temp += self.aes(self.key, self.v)
+        if provided is not None:
+            temp = bytes(a ^ b for a, b in zip(temp, provided))
+        self.key, self.v = temp[:32], temp[32:]
+
+    def generate(self, n):
+        out = b""
+        while len(out) < n:
+            self._inc()
+            out += self.aes(self.key, self.v)
+        self._update(None)
+        return out[:n]
+
+
+def test_nist_ctr_drbg_matches_independent_aes():
+    pytest.importorskip("cryptography")
+    import ctypes
+
+    from cryptography.hazmat.primitives.ciphers import Cipher, algorithms, modes
+
+    from pqc_gb300 import _lib, kem
+
+    def aes(key, block):
+        e = Cipher(algorithms.AES(key), modes.ECB()).encryptor()
+        return e.update(block) + e.finalize()
+
+    lib = _lib.load()
+    entropy = bytes(range(48))
+    pers = bytes((7 * i + 3) & 0xff for i in range(48))
+    for p in (None, pers):
+        ref = _CtrDrbgRestated(aes, entropy, p)
+        assert lib.pqcgpu_randombytes_init_nist(entropy, p) == 0
+        for n in (48, 32, 32, 1, 17, 100, 16):
+            buf = ctypes.create_string_buffer(n)
+            assert lib.pqcgpu_randombytes(buf, n) == 0
+            assert buf.raw == ref.generate(n), (p is not None, n)
+    # coins of one crypto_kem_* call: Kyber keypair = two draws of 32, ML-KEM / FrodoKEM one draw
+    for alg, splits in (("kyber768", (32, 32)), ("mlkem768", (64,)), ("frodo976", (64,))):
+        ref = _CtrDrbgRestated(aes, entropy)
+        lib.pqcgpu_randombytes_init_nist(entropy, None)
+        buf = ctypes.create_string_buffer(64)
+        assert lib.pqcgpu_nist_coins(kem.alg_id(alg), 0, buf) == 0
+        assert buf.raw == b"".join(ref.generate(s) for s in splits), alg
+    lib.pqcgpu_randombytes_init(bytes(48))

@@ -59,3 +59,35 @@ def test_restated_fixture(ctx):
     assert [sha(pk[i * 15632:(i + 1) * 15632]) for i in range(n)] == g["pk_sha256"]
     assert [sha(ct[i * 15744:(i + 1) * 15744]) for i in range(n)] == g["ct_sha256"]
     assert ss.hex() == g["ss"]
+
+
+@pytest.mark.parametrize("parts,threads", [(1, 256), (1, 128), (2, 256), (4, 128), (8, 128), (16, 128), (16, 256)])
+def test_row_split_shapes_match_oracle(ctx, oracle, parts, threads):
+    """Every split of the rows of A over CTAs (and every keypair block size) gives the same bytes."""
+    from pqc_gb300 import _lib, kem
+    lib = _lib.load()
+    alg, a, n = "frodo976", oracle.FRODO976, 5
+    fr = kem.alg_id(alg)
+    seed = drbg.seed48(4400 + parts * 7 + threads)
+    kc = drbg.stream(seed, b"kp", n * 64)
+    ec = drbg.stream(seed, b"enc", n * 24)
+    kp_threads = {128: 64, 256: 256}[threads] if parts != 16 else 128
+    try:
+        assert lib.pqcgpu_set_launch_shape(fr, 0, 0, kp_threads) == 0
+        assert lib.pqcgpu_set_launch_shape(fr, 1, parts, threads) == 0
+        assert lib.pqcgpu_set_launch_shape(fr, 2, parts, threads) == 0
+        pk, sk = ctx.keypair(alg, n, kc)
+        opk, osk = oracle.batch_keypair(a, n, kc)
+        assert (pk, sk) == (opk, osk)
+        ct, ss = ctx.enc(alg, n, pk, ec)
+        oct_, oss = oracle.batch_enc(a, n, pk, ec)
+        assert (ct, ss) == (oct_, oss)
+        assert ctx.dec(alg, n, ct, sk) == oss
+        bad = bytearray(ct)
+        bad[100] ^= 1  # one B' coefficient of instance 0: decaps must reject it implicitly
+        ss_bad = ctx.dec(alg, n, bytes(bad), sk)
+        assert ss_bad[24:] == oss[24:] and ss_bad[:24] != oss[:24]
+    finally:
+        for op in (0, 1, 2):
+            lib.pqcgpu_set_launch_shape(fr, op, 0, 0)
+

@@ -61,7 +61,8 @@ def test_cpa_matches_oracle(ctx, oracle, variant, k, n):
     assert md == m
 
 
-@pytest.mark.parametrize("alg", ["kyber512", "kyber768", "kyber1024", "kyber1024r2"])
+@pytest.mark.parametrize("alg", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "mlkem512", "mlkem768",
+                                 "mlkem1024"])
 @pytest.mark.parametrize("n", [1, 31, 257, 4099])
 def test_kem_matches_oracle(ctx, oracle, alg, n):
     from pqc_gb300 import kem
@@ -81,7 +82,8 @@ def test_kem_matches_oracle(ctx, oracle, alg, n):
     assert ctx.dec(alg, n, ct, sk) == oss
 
 
-@pytest.mark.parametrize("alg", ["kyber512", "kyber768", "kyber1024", "kyber1024r2"])
+@pytest.mark.parametrize("alg", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "mlkem512", "mlkem768",
+                                 "mlkem1024"])
 def test_kem_implicit_rejection(ctx, oracle, alg):
     from pqc_gb300 import kem
     s = kem.sizes(alg)
@@ -100,7 +102,8 @@ def test_kem_implicit_rejection(ctx, oracle, alg):
         assert same == (x % 2 == 1), x
 
 
-@pytest.mark.parametrize("name", ["kyber512", "kyber768", "kyber1024", "kyber1024r2"])
+@pytest.mark.parametrize("name", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "mlkem512", "mlkem768",
+                                  "mlkem1024"])
 def test_restated_fixtures(ctx, name):
     from pqc_gb300 import kem
     g = load_golden("restated_%s.json" % name)

@@ -52,7 +52,8 @@ def test_newhope_cpa_matches_reference(oracle):
         assert oracle.newhope_cpapke_dec(ct, sk).hex() == g["m_dec"][64 * x:64 * x + 64]
 
 
-@pytest.mark.parametrize("name", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "newhope1024", "frodo976"])
+@pytest.mark.parametrize("name", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "newhope1024", "frodo976",
+                                  "mlkem512", "mlkem768", "mlkem1024"])
 def test_restated_kem_vectors(oracle, name):
     g = load_golden("restated_%s.json" % name)
     alg = oracle.ALG_NAMES[name]
@@ -68,7 +69,8 @@ def test_restated_kem_vectors(oracle, name):
     assert oracle.batch_dec(alg, n, ct, sk) == ss
 
 
-@pytest.mark.parametrize("name", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "frodo976"])
+@pytest.mark.parametrize("name", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "frodo976", "mlkem512",
+                                  "mlkem768", "mlkem1024"])
 def test_implicit_rejection(oracle, name):
     """A tampered ciphertext decapsulates to a different key (Kyber / Frodo: the z / s fallback).
     NewHope's CPA-KEM has no re-encryption check, so a small ciphertext change may decode to the
@@ -99,3 +101,31 @@ def test_work_counters(oracle):
     perms, bfly = oracle.counters()
     assert 90 <= perms <= 110
     assert bfly == (3 + 4 + 3 + 1 + 3 + 4) * 896
+
+
+@pytest.mark.parametrize("k", [2, 3, 4])
+def test_mlkem_hash_layer_against_hashlib(oracle, k):
+    """The FIPS 203 steps that differ from round 3, checked with hashlib on the oracle's outputs:
+    rho = G(d || k)[:32] ends the encapsulation key; H(ek) and z sit at the end of dk; the shared
+    key is G(m || H(ek))[:32]; a rejected ciphertext decapsulates to J(z || c) = SHAKE256(z || c, 32)."""
+    import hashlib
+    alg = oracle.ALG_NAMES["mlkem%d" % {2: 512, 3: 768, 4: 1024}[k]]
+    sz = oracle.alg_sizes(alg)
+    seed = drbg.seed48(600 + k)
+    coins = drbg.stream(seed, b"kp", sz["kp_coins"])
+    m = drbg.stream(seed, b"enc", 32)
+    pk, sk = oracle.batch_keypair(alg, 1, coins)
+    d, z = coins[:32], coins[32:64]
+    assert pk[-32:] == hashlib.sha3_512(d + bytes([k])).digest()[:32]
+    assert sk[-64:-32] == hashlib.sha3_256(pk).digest()
+    assert sk[-32:] == z
+    assert sk[384 * k:384 * k + len(pk)] == pk
+    ct, ss = oracle.batch_enc(alg, 1, pk, m)
+    assert ss == hashlib.sha3_512(m + hashlib.sha3_256(pk).digest()).digest()[:32]
+    assert oracle.batch_dec(alg, 1, ct, sk) == ss
+    bad = bytearray(ct)
+    bad[len(bad) // 2] ^= 0x10
+    assert oracle.batch_dec(alg, 1, bytes(bad), sk) == hashlib.shake_256(z + bytes(bad)).digest(32)
+    # the module rank in G separates ML-KEM keys from round-3 keys of the same seed
+    kpk, _ = oracle.batch_keypair(alg - 6, 1, coins)
+    assert kpk != pk
