@@ -56,11 +56,27 @@ def parse():
     p.add_argument("--path", default="fused", choices=["fused", "plain"])
     p.add_argument("--no-plain", action="store_true", help="skip timing the plain path beside the fused one")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--slots", type=int, default=8, help="serving: batches in flight (worker threads)")
+    p.add_argument("--slots", type=int, default=12, help="serving: batches in flight (worker threads)")
     p.add_argument("--config", default=None,
                    choices=["kyber512", "newhope1024", "frodo976", "mixed", "serving", "refgpu", "all"],
                    help="measure another configuration (extra JSON lines) instead of the headline")
     return p.parse_args()
+
+
+def max_over_ranks(x, world, device=None):
+    """The maximum of x over all ranks (x itself on one rank): the slowest replica bounds the job."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, max_ms):
+    """Units of all ranks per second over the slowest rank's time (weak scaling: fixed work per GPU)."""
+    return world * units_per_rank / (max_ms * 1e-3)
 
 
 def dist_env():
@@ -456,11 +472,8 @@ def main():
     ok = ok and torch.equal(ss, ss2)
     step_ms = [a.elapsed_time(b) for a, b in evs]
     total_ms = evs[0][0].elapsed_time(evs[-1][1])
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * B * K / (total_ms * 1e-3)
+    total_ms = max_over_ranks(total_ms, world, dev)
+    value = whole_job_rate(B * K, world, total_ms)
 
     # ---- plain path beside it (same inputs, same outputs) ----
     plain = None
@@ -504,12 +517,9 @@ def main():
         for i in range(K):
             hstep(W + i)
         el = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([el], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            el = float(t.item())
+        el = max_over_ranks(el, world, dev)
         ok = ok and torch.equal(h["ss"], h["ss2"])
-        e2e = {"value": world * B * K / el, "unit": UNIT,
+        e2e = {"value": whole_job_rate(B * K, world, 1e3 * el), "unit": UNIT,
                "h2d_bytes_per_step": B * (s["pk"] + s["enc_coins"] + s["ct"] + s["sk"]),
                "d2h_bytes_per_step": B * (s["ct"] + 2 * s["ss"]), "ms_per_step": 1e3 * el / K}
 

@@ -2,7 +2,8 @@
 
 Replaces the reference's ANALYSIS_MODE block-size sweep (Kyber_GPU_Batched/indcpa.cu:21-70), which
 re-ran every launch over ten block sizes and printed the best: here each (algorithm, operation) is
-timed with CUDA events over a candidate grid at a given batch size, the fastest shape is applied
+timed with CUDA events over a candidate grid at a given batch size (FrodoKEM: the split of an
+instance's rows of A over CTAs, at serving-size batches), the fastest shape is applied
 through pqcgpu_set_launch_shape, and the choice is persisted in a JSON cache keyed by GPU name so
 later processes load it instead of re-tuning.
 
@@ -16,20 +17,25 @@ import os
 from . import _lib, drbg, kem
 
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "tuning.json")
-TUNABLE = ("kyber512", "kyber768", "kyber1024", "newhope1024")
+TUNABLE = ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976")
 
 
 def candidates(alg, op):
     if alg.startswith("kyber"):
         k = {"kyber512": 2, "kyber768": 3, "kyber1024": 4}[alg]
         out = []
-        for ni in (4, 6, 8, 10, 12, 14, 16, 20, 24, 28, 32, 40, 48):
+        for ni in (4, 6, 8, 10, 12, 14, 16, 18, 20, 24, 28, 32, 40, 48):
             jobs = ni * k * k
-            for thr in (64, 96, 128, 160, 192, 224, 256, 320, 384):
+            for thr in (64, 96, 128, 160, 192, 224, 256, 288, 320, 384):
                 lo = min(((jobs + 31) // 32) * 32, 384) - 64
                 if lo <= thr <= ((jobs + 31) // 32) * 32 + 32:
                     out.append((ni, thr))
         return out
+    if alg == "frodo976":
+        # keypair: threads of the row CTAs; encaps / decaps: CTAs per instance (row split) x threads
+        if op == 0:
+            return [(0, thr) for thr in (64, 128, 256)]
+        return [(parts, thr) for parts in (1, 2, 4, 8, 16) for thr in (128, 256)]
     return [(ni, thr) for ni in (1, 2, 4, 8) for thr in (64, 128, 256) if thr // 32 >= 1]
 
 
@@ -49,7 +55,7 @@ def tune(batch=65536, algs=TUNABLE, reps=3, device=0, log=print):
     result = {}
     for alg in algs:
         s = kem.sizes(alg)
-        n = batch if alg != "newhope1024" else min(batch, 16384)
+        n = {"newhope1024": min(batch, 16384), "frodo976": min(batch, 256)}.get(alg, batch)
         seed = drbg.seed48(99)
         up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
         kc = up(drbg.stream(seed, b"kp", n * s["kp_coins"]))
@@ -122,7 +128,8 @@ if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--batch", type=int, default=65536)
     ap.add_argument("--out", default=DEFAULT_CACHE)
+    ap.add_argument("--algs", default=",".join(TUNABLE), help="comma list of algorithms to tune")
     a = ap.parse_args()
-    t = tune(a.batch)
+    t = tune(a.batch, algs=[x for x in a.algs.split(",") if x])
     save(t, a.out)
     print("saved", a.out)

@@ -196,7 +196,7 @@ __device__ __forceinline__ uint2 rotl64_var(uint2 v, int n) {
 }
 
 struct WarpKeccak {
-    int lane, rho, src_pi, col0, col1, col2, col3, xm1, xp1, xp2;
+    int lane, rho, src_pi, src_pi1, src_pi2, col0, col1, col2, col3, xm1, xp1;
     __device__ __forceinline__ explicit WarpKeccak(int ln) {
         lane = ln;
         const int l = ln < 25 ? ln : 0;  // lanes 25..31 mirror lane 0; their values are never read
@@ -208,14 +208,18 @@ struct WarpKeccak {
         for (int i = 0; i < 25; i++)
             if (i == l) r = R[i];
         rho = r;
-        src_pi = (x + 3 * y) % 5 + 5 * x;  // pi: lane (X, Y) takes A[(X + 3Y) % 5][X]
+        // pi: lane (X, Y) takes A[(X + 3Y) % 5][X]; chi also needs what lanes (X+1, Y) and (X+2, Y)
+        // take, so all three are gathered straight from the rotated state in one shuffle step
+        src_pi = (x + 3 * y) % 5 + 5 * x;
+        const int x1 = (x + 1) % 5, x2 = (x + 2) % 5;
+        src_pi1 = (x1 + 3 * y) % 5 + 5 * x1;
+        src_pi2 = (x2 + 3 * y) % 5 + 5 * x2;
         col0 = x + 5 * ((y + 1) % 5);
         col1 = x + 5 * ((y + 2) % 5);
         col2 = x + 5 * ((y + 3) % 5);
         col3 = x + 5 * ((y + 4) % 5);
         xm1 = (x + 4) % 5 + 5 * y;
         xp1 = (x + 1) % 5 + 5 * y;
-        xp2 = (x + 2) % 5 + 5 * y;
     }
 };
 
@@ -226,8 +230,7 @@ __device__ __forceinline__ void keccak_f1600_warp(uint2 &a, const WarpKeccak &w)
         const uint2 cm = shfl2(c, w.xm1), cp = shfl2(c, w.xp1);
         a = xor2(a, xor2(cm, rotl64(cp, 1)));
         a = rotl64_var(a, w.rho);
-        const uint2 b = shfl2(a, w.src_pi);
-        const uint2 b1 = shfl2(b, w.xp1), b2 = shfl2(b, w.xp2);
+        const uint2 b = shfl2(a, w.src_pi), b1 = shfl2(a, w.src_pi1), b2 = shfl2(a, w.src_pi2);
         a.x = lop3_chi(b.x, b1.x, b2.x);
         a.y = lop3_chi(b.y, b1.y, b2.y);
         if (w.lane == 0) a = xor2(a, c_keccak_rc[r]);

@@ -134,7 +134,7 @@ struct pqcgpu_server {
     // one FIFO per (algorithm, operation); the dispatcher serves the group with the oldest head
     std::deque<Req *> groups[PQCGPU_NUM_ALGS][3];
     size_t pending = 0;
-    int heavy_running = 0;  // in-flight FrodoKEM batches (may hold at most half of the slots)
+    int heavy_running = 0;  // in-flight FrodoKEM batches (at most all slots but a quarter)
     int grow_alg = -1;      // a key store waits to grow: no new batch starts until all slots are idle
     uint32_t grow_need = 0;
     std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
@@ -236,9 +236,10 @@ struct pqcgpu_server {
                 cv_done.notify_all();
             }
         }
-        // oldest group head; FrodoKEM (heavy: ~10^4 Keccak permutations per instance) may hold at
-        // most half of the slots so that the light algorithms always find one
-        const int heavy_max = std::max(1, max_inflight / 2);
+        // oldest group head.  FrodoKEM batches are long (about a millisecond of serial sponges) and
+        // its three operations queue separately, so they may use all slots but a quarter (at least
+        // two), which stay for the light algorithms.
+        const int heavy_max = std::max(1, max_inflight - std::max(2, max_inflight / 4));
         int alg = -1, op = -1;
         Clock::time_point oldest;
         for (int a = 0; a < PQCGPU_NUM_ALGS; a++)
