@@ -536,10 +536,15 @@ def main():
     if dom:
         name, (nl, tms) = dom
         per_launch_ms = tms / nl
+        dec_stage1_bfly = 4 * 896  # decryption stage: NTT of u' (k = 3) and the inverse NTT of s^T u
         if "enc_core" in name:
             perms, bfly = w["enc_perms"] - ENC_HASH_PERMS, w["enc_bfly"]
         elif "dec_core" in name:
             perms, bfly = w["dec_perms"] - DEC_HASH_PRE_PERMS, w["dec_bfly"]
+        elif "dec_reencrypt" in name:  # re-encryption stage: all but G and the decryption NTTs
+            perms, bfly = w["dec_perms"] - DEC_HASH_PRE_PERMS - 1, w["dec_bfly"] - dec_stage1_bfly
+        elif "dec_decrypt" in name:
+            perms, bfly = 1, dec_stage1_bfly
         else:
             perms, bfly = ENC_HASH_PERMS, 0
         ops = B * (perms * OPS_PER_PERM + bfly * OPS_PER_BUTTERFLY)

@@ -21,6 +21,8 @@ TUNABLE = ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976")
 
 
 def candidates(alg, op):
+    if alg.startswith("kyber") and op == 3:  # decapsulation, decryption stage (warp-level phases)
+        return [(ni, thr) for ni in (4, 6, 8, 12, 16, 24, 32) for thr in (64, 128, 192, 256, 384)]
     if alg.startswith("kyber"):
         k = {"kyber512": 2, "kyber768": 3, "kyber1024": 4}[alg]
         out = []
@@ -68,8 +70,8 @@ def tune(batch=65536, algs=TUNABLE, reps=3, device=0, log=print):
         ctx.enc_dev(alg, n, ct, ss, pk, ec)
         ctx.wait()
         fns = {0: lambda: ctx.keypair_dev(alg, n, pk, sk, kc), 1: lambda: ctx.enc_dev(alg, n, ct, ss, pk, ec),
-               2: lambda: ctx.dec_dev(alg, n, ss2, ct, sk)}
-        for op in (0, 1, 2):
+               2: lambda: ctx.dec_dev(alg, n, ss2, ct, sk), 3: lambda: ctx.dec_dev(alg, n, ss2, ct, sk)}
+        for op in ((0, 1, 3, 2) if alg.startswith("kyber") else (0, 1, 2)):
             best = None
             for ni, thr in candidates(alg, op):
                 if lib.pqcgpu_set_launch_shape(kem.alg_id(alg), op, ni, thr) != 0:

@@ -534,8 +534,10 @@ static void launch_sa(int n, uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *
 static int sa_attrs() {
     if (capturing()) return PQCGPU_OK;
     if (cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sa_smem(SA_THREADS)) !=
-        cudaSuccess)
+        cudaSuccess) {
+        cudaGetLastError();
         return PQCGPU_ECUDA;
+    }
     return PQCGPU_OK;
 }
 

@@ -3,16 +3,19 @@
 
 namespace pqc {
 namespace kyber {
-// Launch shape of the core kernels, [op][k-2] with op 0 keypair, 1 enc, 2 dec.  One thread per
-// matrix entry (NI * k^2 jobs) sized against the shared memory each instance needs.
-int g_ni[3][3] = {{16, 14, 8}, {24, 14, 14}, {24, 14, 14}};
-int g_threads[3][3] = {{64, 160, 128}, {128, 128, 256}, {128, 160, 256}};
+// Launch shape of the core kernels, [op][k-2] with op 0 keypair, 1 enc, 2 dec (its re-encryption
+// stage).  One thread per matrix entry (NI * k^2 jobs) sized against the shared memory each instance
+// needs.  g_dec1: the decryption stage of decapsulation.  Defaults: the autotuner's GB300 optimum.
+int g_ni[3][3] = {{16, 14, 8}, {28, 14, 24}, {28, 18, 14}};
+int g_threads[3][3] = {{64, 160, 128}, {128, 128, 384}, {128, 192, 256}};
+int g_dec1[3][2] = {{32, 384}, {24, 384}, {6, 128}};
 
 #define PQC_KYBER_DECL(K, V)                                                                               \
     int keypair_##K##_##V(int, uint8_t *, uint8_t *, const uint8_t *, int, int, uint8_t *, int, cudaStream_t); \
     int enc_##K##_##V(int, uint8_t *, uint8_t *, const uint8_t *, const uint8_t *, const uint8_t *, uint8_t *, int, \
                       int, cudaStream_t);                                                                  \
     int dec_##K##_##V(int, uint8_t *, const uint8_t *, const uint8_t *, uint8_t *, int, int, cudaStream_t); \
+    size_t smem_##K##_##V(int, int, int);                                                                \
     int init_##K##_##V();
 PQC_KYBER_DECL(2, 3)
 PQC_KYBER_DECL(3, 3)
@@ -47,7 +50,7 @@ int kyber_dec_dev(int variant, int k, int n, uint8_t *out, const uint8_t *ct, co
 }
 size_t kyber_scratch_bytes(int k, int op, int plain) {
     if (plain) return (size_t)(k * k + 4 * k + 4) * 256 * 2 + 208;
-    return op == 1 ? 96 : (op == 2 ? 32 : 0);
+    return op == 1 ? 96 : (op == 2 ? 128 : 0);  // decaps: H(c) (32) + m' r' K-bar' (96)
 }
 int kyber_init_constants() {
     int (*inits[])() = {kyber::init_2_3, kyber::init_3_3, kyber::init_4_3,
@@ -59,14 +62,30 @@ int kyber_init_constants() {
     return PQCGPU_OK;
 }
 int kyber_set_shape(int op, int k, int ni, int threads) {
-    if (op < 0 || op > 2 || k < 2 || k > 4 || ni <= 0 || ni > 128 || threads < 32 || threads > 512 || threads % 32)
+    if (op < 0 || op > 3 || k < 2 || k > 4 || ni <= 0 || ni > 128 || threads < 32 || threads > 512 || threads % 32)
         return PQCGPU_EINVAL;
+    if (op == 3) {  // decapsulation, decryption stage: NI instances' polynomials, no staging
+        const size_t sm1 = (k == 2 ? kyber::smem_2_3(2, ni, 0) : k == 3 ? kyber::smem_3_3(2, ni, 0) : kyber::smem_4_3(2, ni, 0));
+        if (sm1 > MAX_SMEM_PER_CTA) return PQCGPU_EINVAL;
+        kyber::g_dec1[k - 2][0] = ni;
+        kyber::g_dec1[k - 2][1] = threads;
+        return PQCGPU_OK;
+    }
+    // the CTA's dynamic shared memory must fit the 227 KB a CTA may opt into on sm_103a
+    const size_t sm = k == 2 ? kyber::smem_2_3(op, ni, threads) : k == 3 ? kyber::smem_3_3(op, ni, threads)
+                                                                         : kyber::smem_4_3(op, ni, threads);
+    if (sm > MAX_SMEM_PER_CTA) return PQCGPU_EINVAL;
     kyber::g_ni[op][k - 2] = ni;
     kyber::g_threads[op][k - 2] = threads;
     return PQCGPU_OK;
 }
 int kyber_get_shape(int op, int k, int *ni, int *threads) {
-    if (op < 0 || op > 2 || k < 2 || k > 4) return PQCGPU_EINVAL;
+    if (op < 0 || op > 3 || k < 2 || k > 4) return PQCGPU_EINVAL;
+    if (op == 3) {
+        *ni = kyber::g_dec1[k - 2][0];
+        *threads = kyber::g_dec1[k - 2][1];
+        return PQCGPU_OK;
+    }
     *ni = kyber::g_ni[op][k - 2];
     *threads = kyber::g_threads[op][k - 2];
     return PQCGPU_OK;

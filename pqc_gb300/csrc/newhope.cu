@@ -467,14 +467,17 @@ __global__ void __launch_bounds__(128) nh_enc_hash_pre(int n, const uint8_t *coi
     for (int i = 0; i < 4; i++) s[i] = A[i];
 }
 
-static int g_shape[3][2] = {{4, 128}, {4, 128}, {8, 256}};  // [op] = {instances per CTA, threads}
+static int g_shape[3][2] = {{8, 128}, {4, 64}, {4, 128}};  // [op] = {instances per CTA, threads}
 
 template <class Kern>
 static int prep(Kern k, size_t sm) {
     if (capturing()) return PQCGPU_OK;
-    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess ? PQCGPU_OK
-                                                                                                       : PQCGPU_ECUDA;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess) return PQCGPU_OK;
+    cudaGetLastError();  // leave no error behind for the caller's next CUDA call
+    return PQCGPU_ECUDA;
 }
+// per-instance shared memory of the core kernel of op (0 keypair, 1 encaps, 2 decaps)
+static size_t smem_per_instance(int op) { return op == 0 ? 2 * PITCH * 2 + 128 : op == 1 ? 3 * PITCH * 2 : PITCH * 2; }
 
 }  // namespace newhope
 
@@ -509,6 +512,7 @@ int newhope_init_constants() {
 
 int newhope_set_shape(int op, int ni, int threads) {
     if (op < 0 || op > 2 || ni < 1 || ni > 64 || threads < 32 || threads > 256 || threads % 32) return PQCGPU_EINVAL;
+    if ((size_t)ni * smem_per_instance(op) > MAX_SMEM_PER_CTA) return PQCGPU_EINVAL;
     g_shape[op][0] = ni;
     g_shape[op][1] = threads;
     return PQCGPU_OK;
@@ -523,7 +527,7 @@ int newhope_get_shape(int op, int *ni, int *threads) {
 
 int newhope_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st) {
     const int NI = g_shape[0][0], NT = g_shape[0][1];
-    const size_t sm = (size_t)NI * (2 * PITCH * 2 + 128);
+    const size_t sm = (size_t)NI * smem_per_instance(0);
     if (prep(nh_kp_core, sm)) return PQCGPU_ECUDA;
     KpArgs a{n, pk, sk, seed, seed_stride};
     PQC_LAUNCH(st, "nh_kp_core", 1024, 0, nh_kp_core<<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
@@ -534,7 +538,7 @@ int newhope_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, in
 int newhope_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
                     uint8_t *scratch, int kem, cudaStream_t st) {
     const int NI = g_shape[1][0], NT = g_shape[1][1];
-    const size_t sm = (size_t)NI * 3 * PITCH * 2;
+    const size_t sm = (size_t)NI * smem_per_instance(1);
     if (prep(nh_enc_core, sm)) return PQCGPU_ECUDA;
     EncArgs a{n, ct, pk, m, coins, 32, 32};
     if (kem) {
@@ -549,7 +553,7 @@ int newhope_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const ui
 
 int newhope_dec_dev(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st) {
     const int NI = g_shape[2][0], NT = g_shape[2][1];
-    const size_t sm = (size_t)NI * PITCH * 2;
+    const size_t sm = (size_t)NI * smem_per_instance(2);
     if (prep(nh_dec_core, sm)) return PQCGPU_ECUDA;
     DecArgs d{n, out, ct, sk, kem};
     PQC_LAUNCH(st, "nh_dec_core", 1024, 0, nh_dec_core<<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));

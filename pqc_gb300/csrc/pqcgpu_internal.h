@@ -9,6 +9,8 @@
 #include "pqcgpu.h"
 
 namespace pqc {
+// dynamic shared memory a CTA may opt into on sm_103a (227 KB)
+constexpr size_t MAX_SMEM_PER_CTA = 232448;
 
 // Kernel launches issued by this library (all contexts); contexts report deltas.
 extern std::atomic<uint64_t> g_launch_count;

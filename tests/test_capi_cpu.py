@@ -140,3 +140,20 @@ def test_nist_ctr_drbg_matches_independent_aes():
         assert lib.pqcgpu_nist_coins(kem.alg_id(alg), 0, buf) == 0
         assert buf.raw == b"".join(ref.generate(s) for s in splits), alg
     lib.pqcgpu_randombytes_init(bytes(48))
+
+
+def test_launch_shapes_that_exceed_shared_memory_are_refused():
+    """A shape whose CTA would need more than the 227 KB of shared memory is refused when set
+    (host-only check, no device needed), so no launch can fail on it later."""
+    from pqc_gb300 import _lib, kem
+    lib = _lib.load()
+    import ctypes
+    k768, nh = kem.alg_id("kyber768"), kem.alg_id("newhope1024")
+    ni, thr = ctypes.c_int(), ctypes.c_int()
+    assert lib.pqcgpu_get_launch_shape(k768, 2, ctypes.byref(ni), ctypes.byref(thr)) == 0
+    try:
+        assert lib.pqcgpu_set_launch_shape(k768, 2, 48, 384) != 0  # 48 x 4.8 KB + staging > 227 KB
+        assert lib.pqcgpu_set_launch_shape(k768, 2, 30, 384) == 0
+        assert lib.pqcgpu_set_launch_shape(nh, 1, 64, 256) != 0   # 64 x 7.5 KB
+    finally:
+        lib.pqcgpu_set_launch_shape(k768, 2, ni.value, thr.value)

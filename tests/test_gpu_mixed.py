@@ -119,7 +119,7 @@ def test_graph_replay(env):
 def test_autotune_roundtrip(env, tmp_path):
     from pqc_gb300 import autotune
     t = autotune.tune(batch=2048, algs=("kyber768",), reps=1, log=lambda *a: None)
-    assert set(t["shapes"]) == {"kyber768/0", "kyber768/1", "kyber768/2"}
+    assert set(t["shapes"]) == {"kyber768/0", "kyber768/1", "kyber768/2", "kyber768/3"}
     p = str(tmp_path / "tuning.json")
     autotune.save(t, p)
     assert autotune.load_cached(p, gpu_name=t["gpu"]) is not None
