@@ -6,8 +6,8 @@ namespace kyber {
 // Launch shape of the core kernels, [op][k-2] with op 0 keypair, 1 enc, 2 dec (its re-encryption
 // stage).  One thread per matrix entry (NI * k^2 jobs) sized against the shared memory each instance
 // needs.  g_dec1: the decryption stage of decapsulation.  Defaults: the autotuner's GB300 optimum.
-int g_ni[3][3] = {{16, 14, 8}, {28, 14, 24}, {28, 18, 14}};
-int g_threads[3][3] = {{64, 160, 128}, {128, 128, 384}, {128, 192, 256}};
+int g_ni[3][3] = {{16, 14, 8}, {28, 14, 14}, {28, 18, 14}};
+int g_threads[3][3] = {{64, 160, 128}, {128, 128, 256}, {128, 192, 256}};
 int g_dec1[3][2] = {{32, 384}, {24, 384}, {6, 128}};
 
 #define PQC_KYBER_DECL(K, V)                                                                               \

@@ -343,8 +343,10 @@ __device__ __forceinline__ int16_t *stage_of(uint8_t *seeds, int ni) {
     return reinterpret_cast<int16_t *>(seeds + (size_t)ni * SEEDB) + (size_t)threadIdx.x * STAGE_INT16;
 }
 // Encryption seed block per instance: [0,32) m, [32,64) r, [64,96) K-bar, [96] flag, then the
-// 128-byte PRF outputs of the K + 1 error polynomials e1_0..e1_{K-1}, e2 (eta2 = 2).
-template <int K>
+// 128-byte PRF outputs of the K + 1 error polynomials e1_0..e1_{K-1}, e2 (eta2 = 2), whose CBD is
+// applied in the packing phase.  The PRF output of r_i (64 eta1 bytes) is parked in the shared
+// slot of the accumulator u_i, which is zeroed only after the NTT phase has consumed it.
+template <int K, int V>
 __host__ __device__ constexpr int enc_seed_bytes() {
     return 128 + 128 * (K + 1);
 }
@@ -387,35 +389,69 @@ template <int K, int V, bool DEC>
 __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz, const int16_t *szi, int ni,
                                int ni_alloc, int base, const EncArgs &a, const uint8_t *ct_cmp) {
     using Pp = P<K, V>;
-    constexpr int SB = enc_seed_bytes<K>();
+    constexpr int SB = enc_seed_bytes<K, V>();
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
 
-    // (1) all 2K + 1 PRF permutations: r_i = CBD_eta1(PRF(coins, i)) -> slots [0, K); the error
-    //     polynomials' PRF(coins, K + i) output bytes -> seed block (CBD applied in (5));
-    //     zero the u accumulators
-    //     Jobs are numbered by type (first the ni * K noise polynomials, then the ni * (K + 1) PRF
-    //     outputs), so that a warp runs one permutation body rather than both, one after the other.
-    for (int li = 0; li < ni; li++) zero_polys(slot<K, V>(polys, li, K), K);
+    // (1) all 2K + 1 PRF permutations, one thread each: PRF(coins, i) output bytes -> the slot of
+    //     u_i for r_i, the seed block for the errors (CBD applied in (2) for r, in (5) for the
+    //     errors).  Every job runs the same code (eta1 = 3 needs a second squeeze: those r jobs come
+    //     first, so a warp mixes the two lengths at most once).
     for (int job = tid; job < ni * (2 * K + 1); job += nthr) {
-        const bool noise = job < ni * K;
-        const int li = noise ? job / K : (job - ni * K) / (K + 1);
-        const int i = noise ? job % K : K + (job - ni * K) % (K + 1);
+        const bool rj = job < ni * K;
+        const int li = rj ? job / K : (job - ni * K) / (K + 1);
+        const int i = rj ? job % K : K + (job - ni * K) % (K + 1);
         const uint2 *seed = DEC ? reinterpret_cast<const uint2 *>(seeds + li * SB + 32)
                                 : reinterpret_cast<const uint2 *>(a.r + (size_t)(base + li) * a.r_stride);
-        if (i < K) {
-            int16_t *dst = slot<K, V>(polys, li, i);
-            noise_poly<Pp::ETA1>(seed, i, [&](int g, const int16_t(&c)[8]) { store8(dst + phys(8 * g), c); });
-        } else {
-            uint2 A[25];
-            prf_absorb(A, seed, i);  // nonce K + (i - K) = i
-            uint4 *o = reinterpret_cast<uint4 *>(seeds + li * SB + 128 + 128 * (i - K));
+        uint2 A[25];
+        prf_absorb(A, seed, i);
+        uint2 *o = rj ? reinterpret_cast<uint2 *>(slot<K, V>(polys, li, K + i))
+                      : reinterpret_cast<uint2 *>(seeds + li * SB + 128 + 128 * (i - K));
+        if (Pp::ETA1 == 3 && rj) {  // 192 bytes: the first squeeze (136) and 56 of the second
 #pragma unroll
-            for (int q = 0; q < 8; q++) o[q] = make_uint4(A[2 * q].x, A[2 * q].y, A[2 * q + 1].x, A[2 * q + 1].y);
+            for (int q = 0; q < 17; q++) o[q] = A[q];
+            keccak_f1600(A);
+#pragma unroll
+            for (int q = 0; q < 7; q++) o[17 + q] = A[q];
+        } else {
+#pragma unroll
+            for (int q = 0; q < 16; q++) o[q] = A[q];
         }
     }
     __syncthreads();
-    // (2) r-hat = NTT(r)
-    for (int w = warp; w < ni * K; w += nwarp) ntt_warp(slot<K, V>(polys, w / K, w % K), sz, lane);
+    // (2) r_i = CBD_eta1(PRF bytes in the slot of u_i), then zero u_i and r-hat_i = NTT(r_i): warp per
+    //     polynomial, lane = 8 coefficients
+    for (int w = warp; w < ni * K; w += nwarp) {
+        const int li = w / K, i = w % K;
+        int16_t *u = slot<K, V>(polys, li, K + i);
+        const uint8_t *b = reinterpret_cast<const uint8_t *>(u);
+        int16_t c[8];
+        if (Pp::ETA1 == 2) {  // 4 bytes -> 8 coefficients (cbd.cu:42-63)
+            const uint32_t t = reinterpret_cast<const uint32_t *>(b)[lane];
+            uint32_t d = t & 0x55555555u;
+            d += (t >> 1) & 0x55555555u;
+#pragma unroll
+            for (int q = 0; q < 8; q++) c[q] = (int16_t)((int)((d >> (4 * q)) & 3) - (int)((d >> (4 * q + 2)) & 3));
+        } else {  // 6 bytes (two 3-byte groups) -> 8 coefficients
+            const uint16_t *h = reinterpret_cast<const uint16_t *>(b + 6 * lane);
+            const uint32_t lo = h[0] | ((uint32_t)h[1] << 16), hi = h[2];
+#pragma unroll
+            for (int g = 0; g < 2; g++) {
+                const uint32_t v = g ? ((lo >> 24) | (hi << 8)) & 0x00ffffffu : lo & 0x00ffffffu;
+                uint32_t d = v & 0x00249249u;
+                d += (v >> 1) & 0x00249249u;
+                d += (v >> 2) & 0x00249249u;
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    c[4 * g + j] = (int16_t)((int)((d >> (6 * j)) & 7) - (int)((d >> (6 * j + 3)) & 7));
+            }
+        }
+        int16_t *p = slot<K, V>(polys, li, i);
+        store8(p + phys(8 * lane), c);
+        __syncwarp();
+        uint4 *uz = reinterpret_cast<uint4 *>(u);
+        for (int q = lane; q < POLY_PITCH / 8; q += 32) uz[q] = make_uint4(0, 0, 0, 0);
+        ntt_warp(p, sz, lane);
+    }
     __syncthreads();
     // (3) u_i += A^T[i][j] o r-hat_j, streamed from SHAKE128, one thread per matrix entry
     for (int job = tid; job < ni * K * K; job += nthr) {
@@ -530,7 +566,7 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_enc_core(EncArgs a, in
 template <int K, int V, int STAGE>
 __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, int NI) {
     using Pp = P<K, V>;
-    constexpr int SB = enc_seed_bytes<K>();
+    constexpr int SB = enc_seed_bytes<K, V>();
     extern __shared__ __align__(16) uint8_t smem[];
     int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
     uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (2 * K + 1) * POLY_PITCH);
@@ -899,9 +935,9 @@ static cudaError_t ensure_smem(Kern kern, size_t bytes) {
 }
 
 // Dynamic shared memory of the core kernel of `op` (0 keypair, 1 encaps, 2 decaps) at a launch shape.
-template <int K>
+template <int K, int V>
 static size_t core_smem_bytes(int op, int ni, int threads) {
-    return op == 0 ? Layout<3 * K, 128>::bytes(ni, threads) : Layout<2 * K + 1, enc_seed_bytes<K>()>::bytes(ni, threads);
+    return op == 0 ? Layout<3 * K, 128>::bytes(ni, threads) : Layout<2 * K + 1, enc_seed_bytes<K, V>()>::bytes(ni, threads);
 }
 
 template <int K, int V>
@@ -922,7 +958,7 @@ static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const 
                       uint8_t *scratch, int kem, int plain, cudaStream_t st) {
     if (plain) return kem == KEM_FO ? plain_enc<K, V>(n, ct, ss, pk, coins, scratch, st) : PQCGPU_EUNSUPPORTED;
     const int NI = g_ni[1][K - 2], NT = g_threads[1][K - 2];
-    const size_t sm = Layout<2 * K + 1, enc_seed_bytes<K>()>::bytes(NI, NT);
+    const size_t sm = Layout<2 * K + 1, enc_seed_bytes<K, V>()>::bytes(NI, NT);
     if (ensure_smem(kyber_enc_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     EncArgs a;
     a.n = n;
@@ -954,7 +990,7 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
                       int plain, cudaStream_t st) {
     if (plain) return kem == KEM_FO ? plain_dec<K, V>(n, out, ct, sk, scratch, st) : PQCGPU_EUNSUPPORTED;
     const int NI = g_ni[2][K - 2], NT = g_threads[2][K - 2];
-    const size_t sm = Layout<2 * K + 1, enc_seed_bytes<K>()>::bytes(NI, NT);
+    const size_t sm = Layout<2 * K + 1, enc_seed_bytes<K, V>()>::bytes(NI, NT);
     DecArgs d;
     d.n = n;
     d.ct = ct;
@@ -973,7 +1009,7 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
     PQC_LAUNCH(st, "kyber_dec_hash_pre", K, V,
                kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, sk, scratch, kem));
     const int NI1 = g_dec1[K - 2][0], NT1 = g_dec1[K - 2][1];
-    const size_t sm1 = Layout<2 * K + 1, enc_seed_bytes<K>()>::bytes(NI1, 0);
+    const size_t sm1 = Layout<2 * K + 1, enc_seed_bytes<K, V>()>::bytes(NI1, 0);
     if (ensure_smem(kyber_dec_core<K, V, DEC_DECRYPT>, sm1) != cudaSuccess) return PQCGPU_ECUDA;
     if (ensure_smem(kyber_dec_core<K, V, DEC_REENCRYPT>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     PQC_LAUNCH(st, "kyber_dec_decrypt", K, V,
@@ -1002,7 +1038,7 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
                       int plain, cudaStream_t st) {                                                        \
         return launch_dec<K, V>(n, out, ct, sk, scratch, kem, plain, st);                                 \
     }                                                                                                      \
-    size_t smem_##K##_##V(int op, int ni, int threads) { return core_smem_bytes<K>(op, ni, threads); }     \
+    size_t smem_##K##_##V(int op, int ni, int threads) { return core_smem_bytes<K, V>(op, ni, threads); }     \
     int init_##K##_##V() {                                                                                 \
         uint2 rc[24];                                                                                      \
         keccak_rc_host(rc);                                                                                \
