@@ -10,6 +10,8 @@
 #include <string>
 #include <vector>
 
+#include <sys/random.h>
+
 #include "pqcgpu_internal.h"
 
 namespace pqc {
@@ -137,24 +139,42 @@ bool g_drbg_seeded = false;
 bool g_drbg_nist = false;  // pqcgpu_randombytes_init_nist: AES-256 CTR_DRBG (kat.cu) instead of SHAKE256
 pqc::CtrDrbg g_ctr;
 
-void drbg_bytes(uint8_t *out, size_t n) {
-    std::lock_guard<std::mutex> lk(g_drbg_mu);
+// 48 bytes of operating-system entropy (getrandom, else /dev/urandom); false if neither works.
+bool os_entropy(uint8_t seed[48]) {
+    size_t got = 0;
+    while (got < 48) {
+        const ssize_t r = getrandom(seed + got, 48 - got, 0);
+        if (r <= 0) break;
+        got += (size_t)r;
+    }
+    if (got == 48) return true;
+    FILE *f = fopen("/dev/urandom", "rb");
+    if (!f) return false;
+    got = fread(seed, 1, 48, f);
+    fclose(f);
+    return got == 48;
+}
+
+// Fills out from the library DRBG (the caller holds g_drbg_mu).  The SHAKE-256 DRBG seeds itself
+// from the operating system on first use; without an entropy source it refuses (returns false)
+// rather than produce predictable keys.
+bool drbg_bytes_locked(uint8_t *out, size_t n) {
     if (g_drbg_nist) {
         g_ctr.generate(out, n);
-        return;
+        return true;
     }
     if (!g_drbg_seeded) {
-        uint8_t seed[48] = {0};
-        FILE *f = fopen("/dev/urandom", "rb");
-        if (f) {
-            size_t got = fread(seed, 1, sizeof seed, f);
-            (void)got;
-            fclose(f);
-        }
+        uint8_t seed[48];
+        if (!os_entropy(seed)) return false;
         g_drbg.init(seed, sizeof seed);
         g_drbg_seeded = true;
     }
     g_drbg.squeeze(out, n);
+    return true;
+}
+bool drbg_bytes(uint8_t *out, size_t n) {
+    std::lock_guard<std::mutex> lk(g_drbg_mu);
+    return drbg_bytes_locked(out, n);
 }
 
 struct AlgInfo {
@@ -358,7 +378,7 @@ extern "C" int pqcgpu_randombytes_init_nist(const uint8_t entropy[48], const uin
 }
 extern "C" int pqcgpu_randombytes(uint8_t *out, size_t n) {
     if (!out && n) return PQCGPU_EINVAL;
-    drbg_bytes(out, n);
+    if (!drbg_bytes(out, n)) return set_err(PQCGPU_EUNSUPPORTED, "no operating-system entropy to seed the DRBG");
     return PQCGPU_OK;
 }
 
@@ -466,7 +486,8 @@ static int coins_or_drbg(pqcgpu_ctx *c, const uint8_t *&coins, size_t bytes, uns
         return set_err(PQCGPU_EINVAL, "coins == NULL needs host buffers (or pass device coins)");
     h.host = (uint8_t *)malloc(bytes ? bytes : 1);
     if (!h.host) return set_err(PQCGPU_ENOMEM, "malloc");
-    drbg_bytes(h.host, bytes);
+    if (!drbg_bytes(h.host, bytes))
+        return set_err(PQCGPU_EUNSUPPORTED, "no operating-system entropy to seed the DRBG");
     coins = h.host;
     return PQCGPU_OK;
 }
@@ -856,13 +877,14 @@ extern "C" int pqcgpu_nist_coins(pqcgpu_alg alg, int op, uint8_t *coins) {
     if (!coins || !alg_info(alg, &ai) || op < 0 || op > 1) return PQCGPU_EINVAL;
     int variant, k;
     const bool split = op == 0 && kyber_alg(alg, &variant, &k) && kyber_kem_mode(alg) == 1;
-    if (split) {
-        drbg_bytes(coins, 32);
-        drbg_bytes(coins + 32, 32);
+    bool ok;
+    if (split) {  // two draws, not interleaved with other threads' draws
+        std::lock_guard<std::mutex> lk(g_drbg_mu);
+        ok = drbg_bytes_locked(coins, 32) && drbg_bytes_locked(coins + 32, 32);
     } else {
-        drbg_bytes(coins, op == 0 ? ai.kpc : ai.encc);
+        ok = drbg_bytes(coins, op == 0 ? ai.kpc : ai.encc);
     }
-    return PQCGPU_OK;
+    return ok ? PQCGPU_OK : set_err(PQCGPU_EUNSUPPORTED, "no operating-system entropy to seed the DRBG");
 }
 
 #define PQC_NIST(NAME, ALG)                                                                              \
@@ -870,14 +892,14 @@ extern "C" int pqcgpu_nist_coins(pqcgpu_alg alg, int op, uint8_t *coins) {
         pqcgpu_ctx *c = default_ctx();                                                                   \
         uint8_t coins[64];                                                                               \
         if (!c) return PQCGPU_ECUDA;                                                                     \
-        pqcgpu_nist_coins(ALG, 0, coins);                                                                \
+        if (int rc_ = pqcgpu_nist_coins(ALG, 0, coins)) return rc_;                                      \
         return pqcgpu_kem_keypair_batch(c, ALG, 1, pk, sk, coins, 0);                                    \
     }                                                                                                    \
     extern "C" int pqcgpu_##NAME##_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk) { \
         pqcgpu_ctx *c = default_ctx();                                                                   \
         uint8_t coins[64];                                                                               \
         if (!c) return PQCGPU_ECUDA;                                                                     \
-        pqcgpu_nist_coins(ALG, 1, coins);                                                                \
+        if (int rc_ = pqcgpu_nist_coins(ALG, 1, coins)) return rc_;                                      \
         return pqcgpu_kem_enc_batch(c, ALG, 1, ct, ss, pk, coins, 0);                                    \
     }                                                                                                    \
     extern "C" int pqcgpu_##NAME##_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk) { \

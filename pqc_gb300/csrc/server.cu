@@ -423,7 +423,8 @@ struct pqcgpu_server {
         if (missing) {
             const size_t off = op == PQCGPU_OP_KEYPAIR ? s.off_in0 : s.off_in1, b = sz[op == PQCGPU_OP_KEYPAIR ? 0 : 1];
             for (int i = 0; i < n; i++)
-                if (!s.reqs[i]->r.in) pqcgpu_randombytes(H + off + (size_t)i * b, b);
+                if (!s.reqs[i]->r.in && pqcgpu_randombytes(H + off + (size_t)i * b, b) != PQCGPU_OK)
+                    return PQCGPU_EUNSUPPORTED;  // no entropy: fail the batch rather than use weak coins
         }
         cudaStream_t st = s.stream;
         const uint32_t *didx = (const uint32_t *)D;
