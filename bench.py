@@ -58,7 +58,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--slots", type=int, default=12, help="serving: batches in flight (worker threads)")
     p.add_argument("--config", default=None,
-                   choices=["kyber512", "newhope1024", "frodo976", "mixed", "serving", "refgpu", "all"],
+                   choices=["kyber512", "newhope1024", "frodo976", "mixed", "serving", "refgpu", "latency", "all"],
                    help="measure another configuration (extra JSON lines) instead of the headline")
     return p.parse_args()
 
@@ -226,7 +226,7 @@ def run_configs(args):
     ctx = kem.Context(0)
     st = torch.cuda.ExternalStream(ctx.stream, device=dev)
     up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
-    which = (["kyber512", "newhope1024", "frodo976", "mixed", "serving", "refgpu"] if args.config == "all"
+    which = (["kyber512", "newhope1024", "frodo976", "mixed", "serving", "refgpu", "latency"] if args.config == "all"
              else [args.config])
 
     def timed(fn, reps):
@@ -310,6 +310,8 @@ def run_configs(args):
                               "bit_exact_decaps": bool(ok)}), flush=True)
         elif cfg == "refgpu":
             run_refgpu(ctx, dev, up, timed)
+        elif cfg == "latency":
+            run_latency(ctx, dev, up)
         elif cfg == "serving":
             from pqc_gb300 import serve
             with serve.Server(0, budget=16 << 30, max_inflight=args.slots, max_batch=4096) as srv:
@@ -330,6 +332,42 @@ def run_configs(args):
                               "keys": "resident on the device", "hbm_budget_gb": 16,
                               "measured_peak_per_s": peak, "points": points}), flush=True)
     ctx.close()
+
+
+def run_latency(ctx, dev, up, reps=50):
+    """Single-instance latency (n = 1) of every operation of every algorithm, device-resident buffers,
+    CUDA events around each call on the library stream: p50 and p99 over `reps` calls."""
+    import torch
+    from pqc_gb300 import drbg, kem
+    st = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    out = {}
+    for alg in ("kyber512", "kyber768", "kyber1024", "mlkem768", "newhope1024", "frodo976"):
+        s = kem.sizes(alg)
+        seed = drbg.seed48(77)
+        kc, ec = up(drbg.stream(seed, b"kp", s["kp_coins"])), up(drbg.stream(seed, b"enc", s["enc_coins"]))
+        pk, sk, ct = (torch.empty(s[x], dtype=torch.uint8, device=dev) for x in ("pk", "sk", "ct"))
+        ss, ss2 = (torch.empty(s["ss"], dtype=torch.uint8, device=dev) for _ in range(2))
+        ops = {"keypair": lambda: ctx.keypair_dev(alg, 1, pk, sk, kc), "enc": lambda: ctx.enc_dev(alg, 1, ct, ss, pk, ec),
+               "dec": lambda: ctx.dec_dev(alg, 1, ss2, ct, sk)}
+        res = {}
+        for op, f in ops.items():
+            f()
+            ctx.wait()
+            ts = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                f()
+                e1.record(st)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ts.sort()
+            res[op] = {"p50_ms": ts[len(ts) // 2], "p99_ms": ts[min(len(ts) - 1, int(0.99 * len(ts)))]}
+        ctx.wait()
+        res["roundtrip_ok"] = bool(torch.equal(ss, ss2))
+        out[alg] = res
+    print(json.dumps({"config": "latency", "metric": "single-instance latency (n = 1), device-resident",
+                      "reps": reps, "algs": out}), flush=True)
 
 
 def run_refgpu(ctx, dev, up, timed):

@@ -914,6 +914,97 @@ __global__ void __launch_bounds__(128) kyber_kp_hash_post(int n, const uint8_t *
     for (int i = 0; i < 4; i++) o[i] = A[i];
 }
 
+// ---- the same serial hashes with one warp per instance: the latency path for small batches ----
+// A thread-per-instance sponge of 9-11 permutations is a chain of ~50k dependent instructions; the
+// 25-lane warp permutation (keccak.cuh) runs each permutation in about 60 % of the time, at ~7x the
+// issue slots, so it is used while the batch is too small to fill the GPU (n <= WARP_HASH_MAX).
+constexpr int WARP_HASH_MAX = 1024;
+#define KY_WARP_INSTANCE                                         \
+    const int x = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  \
+    if (x >= n) return;                                          \
+    const WarpKeccak w(threadIdx.x & 31)
+
+template <int K, int V>
+__global__ void __launch_bounds__(128) kyber_enc_hash_pre_w(int n, const uint8_t *pk, const uint8_t *coins,
+                                                            uint8_t *scratch, int kem) {
+    using Pp = P<K, V>;
+    KY_WARP_INSTANCE;
+    const uint2 *cn = reinterpret_cast<const uint2 *>(coins + (size_t)x * 32);
+    uint2 m;
+    if (kem == KEM_MLKEM) {
+        m = w.lane < 4 ? cn[w.lane] : make_uint2(0, 0);
+    } else {
+        warp_absorb2<SHA3_256_LANES>(m, cn, 4, nullptr, 0, DOM_SHA3, w);
+        keccak_f1600_warp(m, w);
+    }
+    uint2 h;
+    warp_absorb2<SHA3_256_LANES>(h, reinterpret_cast<const uint2 *>(pk + (size_t)x * Pp::PKB), Pp::PKB / 8, nullptr, 0,
+                                 DOM_SHA3, w);
+    keccak_f1600_warp(h, w);
+    const uint2 hs = shfl2(h, (w.lane - 4) & 31);
+    uint2 g = w.lane < 4 ? m : (w.lane < 8 ? hs : make_uint2(0, 0));  // G(m || H(pk))
+    if (w.lane == SHA3_512_LANES - 1) {
+        g.x ^= DOM_SHA3;
+        g.y ^= 0x80000000u;
+    }
+    keccak_f1600_warp(g, w);
+    uint2 *o = reinterpret_cast<uint2 *>(scratch + (size_t)x * 96);
+    if (w.lane < 4) {
+        o[w.lane] = m;      // m
+        o[8 + w.lane] = g;  // K-bar
+    } else if (w.lane < 8) {
+        o[w.lane] = g;  // r
+    }
+}
+template <int K, int V>
+__global__ void __launch_bounds__(128) kyber_enc_hash_post_w(int n, const uint8_t *ct, const uint8_t *scratch,
+                                                             uint8_t *ss, int kem) {
+    using Pp = P<K, V>;
+    KY_WARP_INSTANCE;
+    const uint2 *kb = reinterpret_cast<const uint2 *>(scratch + (size_t)x * 96 + 64);
+    uint2 *o = reinterpret_cast<uint2 *>(ss + (size_t)x * 32);
+    if (kem == KEM_MLKEM) {
+        if (w.lane < 4) o[w.lane] = kb[w.lane];
+        return;
+    }
+    uint2 h;
+    warp_absorb2<SHA3_256_LANES>(h, reinterpret_cast<const uint2 *>(ct + (size_t)x * Pp::CTB), Pp::CTB / 8, nullptr, 0,
+                                 DOM_SHA3, w);
+    keccak_f1600_warp(h, w);
+    const uint2 hs = shfl2(h, (w.lane - 4) & 31);
+    uint2 a = w.lane < 4 ? kb[w.lane] : (w.lane < 8 ? hs : make_uint2(0, 0));  // KDF(K-bar || H(c))
+    if (w.lane == 8) a.x ^= DOM_SHAKE;
+    if (w.lane == SHAKE256_LANES - 1) a.y ^= 0x80000000u;
+    keccak_f1600_warp(a, w);
+    if (w.lane < 4) o[w.lane] = a;
+}
+template <int K, int V>
+__global__ void __launch_bounds__(128) kyber_dec_hash_pre_w(int n, const uint8_t *ct, const uint8_t *sk, uint8_t *hct,
+                                                            int kem) {
+    using Pp = P<K, V>;
+    KY_WARP_INSTANCE;
+    const uint2 *c = reinterpret_cast<const uint2 *>(ct + (size_t)x * Pp::CTB);
+    uint2 a;
+    if (kem == KEM_MLKEM)
+        warp_absorb2<SHAKE256_LANES>(a, reinterpret_cast<const uint2 *>(sk + (size_t)x * Pp::SKB + Pp::SKB - 32), 4, c,
+                                     Pp::CTB / 8, DOM_SHAKE, w);
+    else
+        warp_absorb2<SHA3_256_LANES>(a, c, Pp::CTB / 8, nullptr, 0, DOM_SHA3, w);
+    keccak_f1600_warp(a, w);
+    if (w.lane < 4) reinterpret_cast<uint2 *>(hct + (size_t)x * 32)[w.lane] = a;
+}
+template <int K, int V>
+__global__ void __launch_bounds__(128) kyber_kp_hash_post_w(int n, const uint8_t *pk, uint8_t *sk) {
+    using Pp = P<K, V>;
+    KY_WARP_INSTANCE;
+    uint2 a;
+    warp_absorb2<SHA3_256_LANES>(a, reinterpret_cast<const uint2 *>(pk + (size_t)x * Pp::PKB), Pp::PKB / 8, nullptr, 0,
+                                 DOM_SHA3, w);
+    keccak_f1600_warp(a, w);
+    if (w.lane < 4) reinterpret_cast<uint2 *>(sk + (size_t)x * Pp::SKB + Pp::SKB - 64)[w.lane] = a;
+}
+#undef KY_WARP_INSTANCE
+
 }  // namespace kyber
 }  // namespace pqc
 #include "kyber_plain.cuh"
@@ -949,7 +1040,10 @@ static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins,
     if (ensure_smem(kyber_kp_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     KpArgs a{n, pk, sk, coins, coins_stride, kem};
     PQC_LAUNCH(st, "kyber_kp_core", K, V, kyber_kp_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
-    if (kem) PQC_LAUNCH(st, "kyber_kp_hash_post", K, V, kyber_kp_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, sk));
+    if (kem && n <= WARP_HASH_MAX)
+        PQC_LAUNCH(st, "kyber_kp_hash_post", K, V, kyber_kp_hash_post_w<K, V><<<(n + 3) / 4, 128, 0, st>>>(n, pk, sk));
+    else if (kem)
+        PQC_LAUNCH(st, "kyber_kp_hash_post", K, V, kyber_kp_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, sk));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
@@ -966,8 +1060,12 @@ static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const 
     a.pk = pk;
     a.pk_stride = P<K, V>::PKB;
     if (kem) {
-        PQC_LAUNCH(st, "kyber_enc_hash_pre", K, V,
-                   kyber_enc_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, coins, scratch, kem));
+        if (n <= WARP_HASH_MAX)
+            PQC_LAUNCH(st, "kyber_enc_hash_pre", K, V,
+                       kyber_enc_hash_pre_w<K, V><<<(n + 3) / 4, 128, 0, st>>>(n, pk, coins, scratch, kem));
+        else
+            PQC_LAUNCH(st, "kyber_enc_hash_pre", K, V,
+                       kyber_enc_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, coins, scratch, kem));
         a.m = scratch;
         a.m_stride = 96;
         a.r = scratch + 32;
@@ -979,9 +1077,14 @@ static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const 
         a.r_stride = 32;
     }
     PQC_LAUNCH(st, "kyber_enc_core", K, V, kyber_enc_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
-    if (kem)
-        PQC_LAUNCH(st, "kyber_enc_hash_post", K, V,
-                   kyber_enc_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, scratch, ss, kem));
+    if (kem) {
+        if (n <= WARP_HASH_MAX)
+            PQC_LAUNCH(st, "kyber_enc_hash_post", K, V,
+                       kyber_enc_hash_post_w<K, V><<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, ss, kem));
+        else
+            PQC_LAUNCH(st, "kyber_enc_hash_post", K, V,
+                       kyber_enc_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, scratch, ss, kem));
+    }
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
@@ -1006,8 +1109,12 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
                    kyber_dec_core<K, V, DEC_FUSED><<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));
         return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
     }
-    PQC_LAUNCH(st, "kyber_dec_hash_pre", K, V,
-               kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, sk, scratch, kem));
+    if (n <= WARP_HASH_MAX)
+        PQC_LAUNCH(st, "kyber_dec_hash_pre", K, V,
+                   kyber_dec_hash_pre_w<K, V><<<(n + 3) / 4, 128, 0, st>>>(n, ct, sk, scratch, kem));
+    else
+        PQC_LAUNCH(st, "kyber_dec_hash_pre", K, V,
+                   kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, sk, scratch, kem));
     const int NI1 = g_dec1[K - 2][0], NT1 = g_dec1[K - 2][1];
     const size_t sm1 = Layout<2 * K + 1, enc_seed_bytes<K, V>()>::bytes(NI1, 0);
     if (ensure_smem(kyber_dec_core<K, V, DEC_DECRYPT>, sm1) != cudaSuccess) return PQCGPU_ECUDA;
