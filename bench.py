@@ -289,6 +289,8 @@ def run_configs(args):
             ctx.wait()
             t_mixed = timed(lambda: ctx.mixed_dev(jobs), 3)
             ok = all(torch.equal(jobs[i][5], ss) for i, ss in keep)
+            t_stage = timed(lambda: ctx.mixed_dev(jobs, kem.STAGE_KERNELS), 3)
+            ok = ok and all(torch.equal(jobs[i][5], ss) for i, ss in keep)
             g = ctx.graph(jobs)
             t_graph = timed(g.launch, 3)
             ok = ok and all(torch.equal(jobs[i][5], ss) for i, ss in keep)
@@ -306,6 +308,10 @@ def run_configs(args):
             print(json.dumps({"config": "mixed", "metric": "mixed Kyber batch ops/s", "jobs": len(jobs),
                               "instances": total, "mixed_batch_per_s": total / t_mixed * 1e3,
                               "graph_replay_per_s": total / t_graph * 1e3, "sequential_per_s": total / t_seq * 1e3,
+                              "stage_kernels_per_s": total / t_stage * 1e3,
+                              "what": "mixed_batch (default): every job's own kernels over 8 streams; stage_kernels: "
+                                      "one kernel per Kyber core stage for all jobs; sequential: the single-job "
+                                      "calls one after another",
                               "mix": "k=2/3/4 at 40/40/20, n ~ U{1..65536}, ops 1/3 each",
                               "bit_exact_decaps": bool(ok)}), flush=True)
         elif cfg == "refgpu":

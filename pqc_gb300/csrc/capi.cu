@@ -222,6 +222,7 @@ struct pqcgpu_ctx {
     static constexpr int NPAR = 8;              // concurrent streams for mixed batches
     cudaStream_t par[NPAR] = {};
     cudaEvent_t fork_ev = nullptr, join_ev[NPAR] = {};
+    cudaEvent_t stage_ev[NPAR] = {}, core_ev = nullptr;  // mixed Kyber stages: hashes -> core -> hashes
     bool own_stream = true;
     size_t budget = 0;
     uint8_t *arena = nullptr;
@@ -300,12 +301,14 @@ extern "C" int pqcgpu_ctx_create(pqcgpu_ctx **out, int device, size_t budget) {
     }
     for (int i = 0; i < pqcgpu_ctx::NPAR; i++) {
         if ((rc = cuda_err(cudaStreamCreateWithFlags(&c->par[i], cudaStreamNonBlocking), "stream")) ||
-            (rc = cuda_err(cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming), "event"))) {
+            (rc = cuda_err(cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming), "event")) ||
+            (rc = cuda_err(cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming), "event"))) {
             pqcgpu_ctx_destroy(c);
             return rc;
         }
     }
-    if ((rc = cuda_err(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming), "event"))) {
+    if ((rc = cuda_err(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming), "event")) ||
+        (rc = cuda_err(cudaEventCreateWithFlags(&c->core_ev, cudaEventDisableTiming), "event"))) {
         pqcgpu_ctx_destroy(c);
         return rc;
     }
@@ -325,8 +328,10 @@ extern "C" int pqcgpu_ctx_destroy(pqcgpu_ctx *c) {
     for (int i = 0; i < pqcgpu_ctx::NPAR; i++) {
         if (c->par[i]) cudaStreamDestroy(c->par[i]);
         if (c->join_ev[i]) cudaEventDestroy(c->join_ev[i]);
+        if (c->stage_ev[i]) cudaEventDestroy(c->stage_ev[i]);
     }
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    if (c->core_ev) cudaEventDestroy(c->core_ev);
     delete c;
     return PQCGPU_OK;
 }
@@ -617,17 +622,61 @@ static int check_jobs(const pqcgpu_job *jobs, size_t njobs, int plain, size_t *s
 
 // Fork the jobs over the context's parallel streams after the work already on `main`, join back.
 static int launch_jobs(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, uint8_t *scratch, const size_t *offs,
-                       int plain, cudaStream_t main) {
+                       int plain, cudaStream_t main, bool stage_kernels) {
     int rc = cuda_err(cudaEventRecord(c->fork_ev, main), "event record");
     if (rc) return rc;
-    const int used = (int)(njobs < (size_t)pqcgpu_ctx::NPAR ? njobs : pqcgpu_ctx::NPAR);
+    const int used = pqcgpu_ctx::NPAR;  // every parallel stream joins back (some may stay idle)
     for (int i = 0; i < used; i++)
         if ((rc = cuda_err(cudaStreamWaitEvent(c->par[i], c->fork_ev, 0), "wait event"))) return rc;
+    // With stage_kernels, the Kyber encapsulations / decapsulations of round-3 arithmetic (all k, FO
+    // or ML-KEM) get one kernel per core stage for all of them: their per-job hash kernels spread
+    // over the first HS parallel streams, the core launches run on par[0] once those are done, and
+    // the other jobs round-robin over the remaining streams.  Otherwise every job's own kernels
+    // round-robin over all streams (measured faster on GB300: each k keeps its tuned shape).
+    constexpr int HS = pqcgpu_ctx::NPAR / 2;
+    std::vector<MixedKyberJob> mix[3];
+    std::vector<size_t> rest;
     for (size_t i = 0; i < njobs; i++) {
         const pqcgpu_job &j = jobs[i];
-        rc = op_dev(j.alg, j.op, (int)j.n, j.in0, j.in1, j.out0, j.out1, scratch + offs[i], plain,
-                    c->par[i % pqcgpu_ctx::NPAR]);
+        int variant = 0, k = 0;
+        if (!plain && stage_kernels && (j.op == 1 || j.op == 2) && kyber_alg(j.alg, &variant, &k) && variant == 3)
+            mix[j.op].push_back(MixedKyberJob{k, kyber_kem_mode(j.alg), (int)j.n, j.in0, j.in1, j.out0, j.out1,
+                                              scratch + offs[i]});
+        else
+            rest.push_back(i);
+    }
+    const bool mixed = mix[1].size() + mix[2].size() >= 2;
+    if (!mixed) {
+        rest.clear();
+        for (size_t i = 0; i < njobs; i++) rest.push_back(i);
+    }
+    const int first = mixed ? HS : 0, nrest = pqcgpu_ctx::NPAR - first;
+    for (size_t q = 0; q < rest.size(); q++) {
+        const pqcgpu_job &j = jobs[rest[q]];
+        rc = op_dev(j.alg, j.op, (int)j.n, j.in0, j.in1, j.out0, j.out1, scratch + offs[rest[q]], plain,
+                    c->par[first + (int)(q % (size_t)nrest)]);
         if (rc) return set_err(rc, "job launch failed");
+    }
+    if (mixed) {
+        int q = 0;
+        for (int op = 1; op <= 2; op++)
+            for (const auto &j : mix[op])
+                if ((rc = kyber_mixed_hash(op, true, j, c->par[q++ % HS]))) return set_err(rc, "job launch failed");
+        for (int i = 1; i < HS; i++) {
+            if ((rc = cuda_err(cudaEventRecord(c->stage_ev[i], c->par[i]), "event record"))) return rc;
+            if ((rc = cuda_err(cudaStreamWaitEvent(c->par[0], c->stage_ev[i], 0), "wait event"))) return rc;
+        }
+        for (int op = 1; op <= 2; op++)
+            if (!mix[op].empty() && (rc = kyber_mixed_core(op, mix[op].data(), (int)mix[op].size(), c->par[0])))
+                return set_err(rc, "mixed Kyber launch failed");
+        if (!mix[1].empty()) {
+            if ((rc = cuda_err(cudaEventRecord(c->core_ev, c->par[0]), "event record"))) return rc;
+            for (int i = 1; i < HS; i++)
+                if ((rc = cuda_err(cudaStreamWaitEvent(c->par[i], c->core_ev, 0), "wait event"))) return rc;
+            q = 0;
+            for (const auto &j : mix[1])
+                if ((rc = kyber_mixed_hash(1, false, j, c->par[q++ % HS]))) return set_err(rc, "job launch failed");
+        }
     }
     for (int i = 0; i < used; i++) {
         if ((rc = cuda_err(cudaEventRecord(c->join_ev[i], c->par[i]), "event record"))) return rc;
@@ -647,7 +696,7 @@ extern "C" int pqcgpu_kem_mixed_batch(pqcgpu_ctx *c, const pqcgpu_job *jobs, siz
     size_t tot = 0;
     if ((rc = check_jobs(jobs, njobs, plain, &tot, offs.data()))) return rc;
     if ((rc = c->reserve(tot + 256))) return rc;
-    return launch_jobs(c, jobs, njobs, c->arena, offs.data(), plain, c->stream);
+    return launch_jobs(c, jobs, njobs, c->arena, offs.data(), plain, c->stream, (flags & PQCGPU_STAGE_KERNELS) != 0);
 }
 
 struct pqcgpu_graph {
@@ -677,13 +726,14 @@ extern "C" int pqcgpu_graph_capture(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_
         return set_err(PQCGPU_ENOMEM, "graph scratch allocation failed");
     }
     // one uncaptured pass: loads the kernels and sets their shared-memory attributes
-    rc = launch_jobs(c, jobs, njobs, g->scratch, offs.data(), plain, c->stream);
+    rc = launch_jobs(c, jobs, njobs, g->scratch, offs.data(), plain, c->stream, (flags & PQCGPU_STAGE_KERNELS) != 0);
     if (!rc) rc = cuda_err(cudaStreamSynchronize(c->stream), "warm-up");
     if (!rc) {
         set_capturing(true);
         rc = cuda_err(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         if (!rc) {
-            const int lrc = launch_jobs(c, jobs, njobs, g->scratch, offs.data(), plain, c->stream);
+            const int lrc = launch_jobs(c, jobs, njobs, g->scratch, offs.data(), plain, c->stream,
+                                        (flags & PQCGPU_STAGE_KERNELS) != 0);
             const int erc = cuda_err(cudaStreamEndCapture(c->stream, &g->graph), "end capture");
             rc = lrc ? lrc : erc;
         }

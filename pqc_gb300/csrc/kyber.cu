@@ -59,7 +59,7 @@ int kyber_init_constants() {
         const int rc = f();
         if (rc) return rc;
     }
-    return PQCGPU_OK;
+    return kyber_mixed_init();
 }
 int kyber_set_shape(int op, int k, int ni, int threads) {
     if (op < 0 || op > 3 || k < 2 || k > 4 || ni <= 0 || ni > 128 || threads < 32 || threads > 512 || threads % 32)

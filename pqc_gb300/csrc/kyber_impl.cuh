@@ -550,27 +550,31 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
 // ---------------------------------------------------------------------------------------------
 constexpr int CORE_MAX_THREADS = 512;
 
+// Encapsulation of instances [base, base + NI) of `a` by the calling CTA (dynamic shared memory
+// laid out for NI instances of this K).
 template <int K, int V>
-__global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_enc_core(EncArgs a, int NI) {
-
+__device__ __forceinline__ void enc_core_body(const EncArgs &a, int NI, int base) {
     extern __shared__ __align__(16) uint8_t smem[];
     int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
     uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (2 * K + 1) * POLY_PITCH);
-    const int base = blockIdx.x * NI;
     const int ni = min(NI, a.n - base);
     load_twiddles(sz, szi);
     __syncthreads();
     encrypt_phases<K, V, false>(polys, seeds, sz, szi, ni, NI, base, a, nullptr);
 }
+template <int K, int V>
+__global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_enc_core(EncArgs a, int NI) {
+    enc_core_body<K, V>(a, NI, blockIdx.x * NI);
+}
 
+// Decapsulation (stage STAGE) of instances [base, base + NI) of `d` by the calling CTA.
 template <int K, int V, int STAGE>
-__global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, int NI) {
+__device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base) {
     using Pp = P<K, V>;
     constexpr int SB = enc_seed_bytes<K, V>();
     extern __shared__ __align__(16) uint8_t smem[];
     int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
     uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (2 * K + 1) * POLY_PITCH);
-    const int base = blockIdx.x * NI;
     const int ni = min(NI, d.n - base);
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
     const int sks = d.kem ? Pp::SKB : Pp::SKCPA;
@@ -726,6 +730,11 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, in
         for (int i = 0; i < 4; i++) out[i] = A[i];
     }
 }
+template <int K, int V, int STAGE>
+__global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, int NI) {
+    dec_core_body<K, V, STAGE>(d, NI, blockIdx.x * NI);
+}
+
 
 // Keypair: slots [0,K) s, [K,2K) e, [2K,3K) t-hat; seeds [0,32) rho, [32,64) sigma.
 template <int K, int V>

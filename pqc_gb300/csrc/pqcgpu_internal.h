@@ -63,6 +63,19 @@ struct CtrDrbg {
     void generate(uint8_t *out, size_t n);
     void update(const uint8_t *provided);
 };
+// One Kyber job of a mixed batch (round-3 arithmetic, k = 2, 3, 4; kem 1 FO or 2 ML-KEM), device
+// pointers as in op_dev; scratch per kyber_scratch_bytes.  For encapsulation (op 1) or
+// decapsulation (op 2) jobs: kyber_mixed_hash issues one job's hash kernels before (pre) or after
+// the core stages; kyber_mixed_core runs the core stages of all the jobs, one kernel per stage
+// (kyber_mixed.cu).
+struct MixedKyberJob {
+    int k, kem, n;
+    const uint8_t *in0, *in1;
+    uint8_t *out0, *out1, *scratch;
+};
+int kyber_mixed_hash(int op, bool pre, const MixedKyberJob &job, cudaStream_t st);
+int kyber_mixed_core(int op, const MixedKyberJob *jobs, int njobs, cudaStream_t st);
+int kyber_mixed_init();  // constant tables of kyber_mixed.cu
 int kyber_kem_mode(int alg);  // 1: round-2 / round-3 FO KEM, 2: ML-KEM (FIPS 203)
 int kyber_keypair_dev(int variant, int k, int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int coins_stride,
                       int kem, uint8_t *scratch, int plain, cudaStream_t st);

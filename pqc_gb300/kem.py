@@ -12,6 +12,7 @@ ALGS = {"kyber512": 0, "kyber768": 1, "kyber1024": 2, "kyber1024r2": 3, "newhope
         "mlkem512": 6, "mlkem768": 7, "mlkem1024": 8}
 DEVICE_PTRS = 0x1
 PLAIN = 0x2
+STAGE_KERNELS = 0x4
 
 
 def alg_id(alg):

@@ -75,27 +75,34 @@ def test_mixed_batch_all_algorithms(env):
     check(jobs, expected)
 
 
-def test_mixed_kyber_uneven_sizes(env):
-    """The mixed-Kyber configuration: k = 2/3/4 at 40/40/20, uneven sizes, ops 1/3 each."""
+@pytest.mark.parametrize("stage_kernels", [False, True])
+def test_mixed_kyber_uneven_sizes(env, stage_kernels):
+    """The mixed-Kyber configuration: k = 2/3/4 at 40/40/20 (plus ML-KEM), uneven sizes, ops 1/3
+    each; every job's own kernels, or one kernel per core stage for the Kyber jobs (STAGE_KERNELS)."""
+    from pqc_gb300 import kem
     ctx, torch, dev = env
     rng = random.Random(11)
     spec = []
     for _ in range(12):
         alg = rng.choices(["kyber512", "kyber768", "kyber1024"], [0.4, 0.4, 0.2])[0]
         spec.append((alg, rng.choice(["keypair", "enc", "dec"]), rng.randint(1, 5000)))
+    spec += [("mlkem768", "enc", 333), ("mlkem1024", "dec", 1500), ("kyber1024r2", "dec", 257)]
     jobs, expected = build_jobs(ctx, torch, dev, spec, 4000)
     torch.cuda.synchronize()
-    ctx.mixed_dev(jobs)
+    ctx.mixed_dev(jobs, kem.STAGE_KERNELS if stage_kernels else 0)
     ctx.wait()
     check(jobs, expected)
 
 
-def test_graph_replay(env):
+@pytest.mark.parametrize("stage_kernels", [False, True])
+def test_graph_replay(env, stage_kernels):
+    from pqc_gb300 import kem
     ctx, torch, dev = env
-    spec = [("kyber768", "enc", 3000), ("kyber768", "dec", 3000), ("kyber512", "keypair", 777), ("newhope1024", "enc", 100)]
+    spec = [("kyber768", "enc", 3000), ("kyber768", "dec", 3000), ("kyber512", "keypair", 777), ("newhope1024", "enc", 100),
+            ("kyber1024", "enc", 500)]
     jobs, expected = build_jobs(ctx, torch, dev, spec, 5000)
     torch.cuda.synchronize()
-    g = ctx.graph(jobs)
+    g = ctx.graph(jobs, kem.STAGE_KERNELS if stage_kernels else 0)
     check(jobs, expected)  # the warm-up pass already computed the outputs
     for t in (j[5] for j in jobs):
         t.zero_()
