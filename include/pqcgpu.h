@@ -227,14 +227,35 @@ int pqcgpu_server_run_poisson(pqcgpu_server *server, const pqcgpu_mix_entry *mix
 int pqcgpu_set_launch_shape(pqcgpu_alg alg, int op, int ni, int threads);
 int pqcgpu_get_launch_shape(pqcgpu_alg alg, int op, int *ni, int *threads);
 
+/* Shape of the host-buffer pipeline; there is no counterpart in the reference, whose drivers copy a
+ * whole batch before and after the kernels. A host-buffer call splits its batch into chunks:
+ * `chunk_first` instances, doubling up to `chunk_max`, an even split of the middle into chunks of
+ * at most `chunk_max`, then doubling down to `chunk_last`.
+ * Copies in run in order on one stream and copies out on another. Each chunk's kernels start as
+ * soon as its inputs are in, on one of `streams` compute streams (1..8) in turn. Each chunk has
+ * its own device buffers, up to 16 chunks and the context budget; later chunks reuse them.
+ * Zeros select the defaults: chunk_max 16384, chunk_first = chunk_last = chunk_max / 4, 8 streams.
+ * Applies to all contexts of the process. */
+int pqcgpu_set_host_pipeline(size_t chunk_max, size_t chunk_first, size_t chunk_last, int streams);
+int pqcgpu_get_host_pipeline(size_t *chunk_max, size_t *chunk_first, size_t *chunk_last, int *streams);
+
 /* ---- tracing and roofline probes ------------------------------------------------------------
- * pqcgpu_profile_enable(1): every kernel launch is bracketed by CUDA events on its stream.
+ * These replace the reference's TIMING_START / TIMING_END event pairs
+ * (Kyber_GPU_Batched/indcpa.cu:21-84).
+ * pqcgpu_profile_enable(1): every kernel launch, and every copy of a host-buffer call ("copy H2D",
+ * "copy D2H"), is bracketed by CUDA events on its stream.
  * pqcgpu_profile_read: JSON {"kernel<k,v>": [launches, total_ms], ...} of the records since the
  * last read (synchronises on them), then clears them.
+ * pqcgpu_profile_trace: the same records as a timeline in the Chrome trace-event format
+ * ({"traceEvents": [{"name", "ph": "X", "tid" = stream, "ts", "dur"}]}, microseconds from the
+ * earliest record), for chrome://tracing or Perfetto. *len: in, the capacity of buf; out, the bytes
+ * needed with the NUL. If buf is NULL or too small, PQCGPU_EINVAL and the records are kept.
+ * Otherwise it clears them.
  * pqcgpu_probe_peaks: measured integer-pipe (LOP3) op rate and register-resident Keccak-f[1600]
  * permutation rate of `device`, the denominators of the integer roofline. */
 int pqcgpu_profile_enable(int on);
 int pqcgpu_profile_read(char *buf, size_t len);
+int pqcgpu_profile_trace(char *buf, size_t *len);
 int pqcgpu_probe_peaks(int device, double *int_ops_per_s, double *keccak_perms_per_s);
 
 /* ---- NIST single-instance API per parameter set (crypto_kem_* of each api.h) -------------

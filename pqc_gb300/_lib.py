@@ -48,6 +48,9 @@ SIGNATURES = {
     "pqcgpu_get_launch_shape": (_int, [_int, _int, _c.POINTER(_int), _c.POINTER(_int)]),
     "pqcgpu_profile_enable": (_int, [_int]),
     "pqcgpu_profile_read": (_int, [_c.c_char_p, _sz]),
+    "pqcgpu_profile_trace": (_int, [_c.c_char_p, _c.POINTER(_sz)]),
+    "pqcgpu_set_host_pipeline": (_int, [_sz, _sz, _sz, _int]),
+    "pqcgpu_get_host_pipeline": (_int, [_c.POINTER(_sz), _c.POINTER(_sz), _c.POINTER(_sz), _c.POINTER(_int)]),
     "pqcgpu_probe_peaks": (_int, [_int, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]),
     "pqcgpu_randombytes_init": (_int, [_u8p]),
     "pqcgpu_randombytes": (_int, [_u8p, _sz]),

@@ -218,9 +218,16 @@ int kyber_kem_mode(int alg) { return (alg >= PQCGPU_MLKEM512 && alg <= PQCGPU_ML
 struct pqcgpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
-    cudaStream_t side[2] = {nullptr, nullptr};  // pipelining streams for host-buffer calls
-    static constexpr int NPAR = 8;              // concurrent streams for mixed batches
+    static constexpr int NPAR = 8;  // concurrent streams for mixed batches
     cudaStream_t par[NPAR] = {};
+    // Host-buffer calls: ordered copies in and out on their own streams; chunk i uses buffer slot
+    // i % (slots of the call).  Its kernels run on one of the pipeline streams, whose priorities
+    // fall from pipe[0] to pipe[NPAR - 1]; chunks map to them in order, so earlier chunks take the
+    // SMs first and later ones fill the gaps.
+    static constexpr int NSLOT = 16;
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaStream_t pipe[NPAR] = {};
+    cudaEvent_t in_ev[NSLOT] = {}, done_ev[NSLOT] = {}, free_ev[NSLOT] = {};
     cudaEvent_t fork_ev = nullptr, join_ev[NPAR] = {};
     cudaEvent_t stage_ev[NPAR] = {}, core_ev = nullptr;  // mixed Kyber stages: hashes -> core -> hashes
     bool own_stream = true;
@@ -237,7 +244,10 @@ struct pqcgpu_ctx {
         if (bytes > budget) return set_err(PQCGPU_EBUDGET, "request exceeds the context's device-memory budget");
         if (arena) {
             cudaStreamSynchronize(stream);
-            for (auto s : side) cudaStreamSynchronize(s);
+            cudaStreamSynchronize(copy_in);
+            cudaStreamSynchronize(copy_out);
+            for (auto s : par) cudaStreamSynchronize(s);
+            for (auto s : pipe) cudaStreamSynchronize(s);
             cudaFree(arena);
             arena = nullptr;
             arena_size = 0;
@@ -294,15 +304,35 @@ extern "C" int pqcgpu_ctx_create(pqcgpu_ctx **out, int device, size_t budget) {
     c->device = device;
     c->budget = budget ? budget : ((size_t)4 << 30);
     if ((rc = cuda_err(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream")) ||
-        (rc = cuda_err(cudaStreamCreateWithFlags(&c->side[0], cudaStreamNonBlocking), "stream")) ||
-        (rc = cuda_err(cudaStreamCreateWithFlags(&c->side[1], cudaStreamNonBlocking), "stream"))) {
-        delete c;
+        (rc = cuda_err(cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking), "stream")) ||
+        (rc = cuda_err(cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking), "stream"))) {
+        pqcgpu_ctx_destroy(c);
         return rc;
     }
     for (int i = 0; i < pqcgpu_ctx::NPAR; i++) {
         if ((rc = cuda_err(cudaStreamCreateWithFlags(&c->par[i], cudaStreamNonBlocking), "stream")) ||
             (rc = cuda_err(cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming), "event")) ||
             (rc = cuda_err(cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming), "event"))) {
+            pqcgpu_ctx_destroy(c);
+            return rc;
+        }
+    }
+    int least = 0, greatest = 0;
+    if ((rc = cuda_err(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities"))) {
+        pqcgpu_ctx_destroy(c);
+        return rc;
+    }
+    for (int i = 0; i < pqcgpu_ctx::NPAR; i++) {
+        const int prio = greatest + (int)(((long)(least - greatest) * i + (pqcgpu_ctx::NPAR - 1) / 2) / (pqcgpu_ctx::NPAR - 1));
+        if ((rc = cuda_err(cudaStreamCreateWithPriority(&c->pipe[i], cudaStreamNonBlocking, prio), "stream"))) {
+            pqcgpu_ctx_destroy(c);
+            return rc;
+        }
+    }
+    for (int i = 0; i < pqcgpu_ctx::NSLOT; i++) {
+        if ((rc = cuda_err(cudaEventCreateWithFlags(&c->in_ev[i], cudaEventDisableTiming), "event")) ||
+            (rc = cuda_err(cudaEventCreateWithFlags(&c->done_ev[i], cudaEventDisableTiming), "event")) ||
+            (rc = cuda_err(cudaEventCreateWithFlags(&c->free_ev[i], cudaEventDisableTiming), "event"))) {
             pqcgpu_ctx_destroy(c);
             return rc;
         }
@@ -323,8 +353,15 @@ extern "C" int pqcgpu_ctx_destroy(pqcgpu_ctx *c) {
     cudaDeviceSynchronize();
     if (c->arena) cudaFree(c->arena);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
-    for (auto s : c->side)
+    if (c->copy_in) cudaStreamDestroy(c->copy_in);
+    for (auto s : c->pipe)
         if (s) cudaStreamDestroy(s);
+    if (c->copy_out) cudaStreamDestroy(c->copy_out);
+    for (int i = 0; i < pqcgpu_ctx::NSLOT; i++) {
+        if (c->in_ev[i]) cudaEventDestroy(c->in_ev[i]);
+        if (c->done_ev[i]) cudaEventDestroy(c->done_ev[i]);
+        if (c->free_ev[i]) cudaEventDestroy(c->free_ev[i]);
+    }
     for (int i = 0; i < pqcgpu_ctx::NPAR; i++) {
         if (c->par[i]) cudaStreamDestroy(c->par[i]);
         if (c->join_ev[i]) cudaEventDestroy(c->join_ev[i]);
@@ -389,8 +426,9 @@ extern "C" int pqcgpu_randombytes(uint8_t *out, size_t n) {
 
 // ---------------------------------------------------------------------------------------------
 // Operation plumbing.  An op is described by its per-instance input / output sizes and a device
-// function over a contiguous chunk; the host-buffer path pipelines chunks over two streams
-// (H2D of chunk c+1 overlaps the kernels of chunk c and the D2H of chunk c-1).
+// function over a contiguous chunk.  The host-buffer path pipelines chunks: copies in run in
+// order on one stream, copies out on another, and the kernels of consecutive chunks on different
+// streams, so the copies of one chunk overlap the kernels of its neighbours.
 // ---------------------------------------------------------------------------------------------
 namespace {
 constexpr int MAXIO = 3;
@@ -402,6 +440,61 @@ struct OpDesc {
     size_t out_sz[MAXIO];
     size_t scratch_per = 0;
 };
+// Shape of the host-buffer pipeline (process-wide, pqcgpu_set_host_pipeline): the largest chunk,
+// the first and the last chunk, and the number of compute streams.  A chunk's device buffers are
+// also capped at SLOT_BYTES_MAX, which caps FrodoKEM chunks at 2048 instances.
+struct PipeShape {
+    size_t chunk_max = 16384, chunk_first = 4096, chunk_last = 4096;
+    int streams = 8;
+};
+PipeShape g_pipe;
+std::mutex g_pipe_mu;
+constexpr size_t SLOT_BYTES_MAX = (size_t)256 << 20;
+
+// Chunk sizes for a host-buffer call of n instances.  The first chunk's copies in and the last
+// chunk's copies out overlap no kernels, so chunks may start at `first` and double up to cmax, and
+// shrink from cmax to `last` at the end; the middle is split evenly into chunks of at most cmax.
+// 65536 instances with cmax = 16384, first = last = 4096 (the default): 4096, 8192, 13654, 13654,
+// 13652, 8192, 4096; with cmax = 8192, first = 4096, last = 8192: 4096, 8 x 7680.
+std::vector<size_t> chunk_plan(size_t n, size_t cmax, size_t first, size_t last) {
+    std::vector<size_t> head, tail;
+    size_t ramp = 0;
+    for (size_t c = first; c < cmax; c *= 2) {
+        head.push_back(c);
+        ramp += c;
+    }
+    for (size_t c = last; c < cmax; c *= 2) {
+        tail.push_back(c);
+        ramp += c;
+    }
+    while (ramp > n) {  // drop the largest ramp chunks until the ramps fit
+        std::vector<size_t> &v = (tail.empty() || (!head.empty() && head.back() >= tail.back())) ? head : tail;
+        ramp -= v.back();
+        v.pop_back();
+    }
+    std::vector<size_t> plan(head);
+    const size_t mid = n - ramp;
+    if (mid) {
+        const size_t parts = (mid + cmax - 1) / cmax, each = (mid + parts - 1) / parts;
+        for (size_t left = mid; left;) {
+            const size_t m = left < each ? left : each;
+            plan.push_back(m);
+            left -= m;
+        }
+    }
+    plan.insert(plan.end(), tail.rbegin(), tail.rend());
+    return plan;
+}
+
+// One copy of the host-buffer pipeline, recorded by the launch profiler when it is on.
+cudaError_t copy_async(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s) {
+    const bool h2d = kind == cudaMemcpyHostToDevice;
+    void *tok = prof_enabled() ? prof_begin(s, h2d ? "copy H2D" : "copy D2H", -1, 0) : nullptr;
+    const cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, s);
+    if (tok) prof_end(s, tok);
+    return e;
+}
+
 // run(n, din[], dout[], scratch, stream)
 template <class Run>
 int run_op(pqcgpu_ctx *c, size_t n, const OpDesc &d, unsigned flags, Run run) {
@@ -425,52 +518,99 @@ int run_op(pqcgpu_ctx *c, size_t n, const OpDesc &d, unsigned flags, Run run) {
         if (rc) return rc;
         return cuda_err(cudaGetLastError(), "kernel launch");
     }
-    // host buffers: chunked, double-buffered pipeline on the two side streams
+    // host buffers: the pipeline
     auto r256 = [](size_t v) { return (v + 255) & ~(size_t)255; };
-    const size_t chunk = n < 16384 ? n : 16384;
-    const int nbuf = (n > chunk) ? 2 : 1;
-    size_t set_bytes = r256(d.scratch_per * chunk);
-    for (int i = 0; i < d.nin; i++) set_bytes += r256(d.in_sz[i] * chunk);
-    for (int i = 0; i < d.nout; i++) set_bytes += r256(d.out_sz[i] * chunk);
-    if ((rc = c->reserve(set_bytes * nbuf))) return rc;
+    auto slot_bytes = [&](size_t m) {
+        size_t b = r256(d.scratch_per * m);
+        for (int i = 0; i < d.nin; i++) b += r256(d.in_sz[i] * m);
+        for (int i = 0; i < d.nout; i++) b += r256(d.out_sz[i] * m);
+        return b;
+    };
+    PipeShape shape;
+    {
+        std::lock_guard<std::mutex> lk(g_pipe_mu);
+        shape = g_pipe;
+    }
+    size_t cmax = shape.chunk_max, first = shape.chunk_first, last = shape.chunk_last;
+    while (cmax > 64 && slot_bytes(cmax) > SLOT_BYTES_MAX) cmax /= 2;
+    // slots: one per chunk up to NSLOT (a slot is reused only by a later chunk), fewer if the
+    // budget says so; chunks halve only when not even one slot fits
+    std::vector<size_t> plan;
+    size_t set_bytes = 0, mc = 0;
+    int nslot = 1;
+    for (;;) {
+        if (first > cmax) first = cmax;
+        if (last > cmax) last = cmax;
+        plan = chunk_plan(n, cmax, first, last);
+        mc = 0;
+        for (size_t m : plan) mc = m > mc ? m : mc;
+        set_bytes = slot_bytes(mc);
+        size_t fit = c->budget / set_bytes;
+        if (fit > plan.size()) fit = plan.size();
+        if (fit > (size_t)pqcgpu_ctx::NSLOT) fit = pqcgpu_ctx::NSLOT;
+        nslot = fit ? (int)fit : 1;
+        if (fit || cmax <= 64) break;
+        cmax /= 2;
+    }
+    // compute streams: nstream of the pipeline streams spread over the priority range; chunk ci
+    // goes to bin ci * nstream / chunks, so the bins follow the chunk order
+    const int nstream = (size_t)shape.streams < plan.size() ? shape.streams : (int)plan.size();
+    cudaStream_t cst[pqcgpu_ctx::NPAR];
+    for (int i = 0; i < nstream; i++) cst[i] = c->pipe[nstream > 1 ? i * (pqcgpu_ctx::NPAR - 1) / (nstream - 1) : 0];
+    if ((rc = c->reserve(set_bytes * nslot))) return rc;
     cudaEvent_t ev;
-    cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if ((rc = cuda_err(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event"))) return rc;
     cudaEventRecord(ev, c->stream);  // order after prior work on the main stream
-    for (auto s : c->side) cudaStreamWaitEvent(s, ev, 0);
-    for (size_t off = 0, ci = 0; off < n; off += chunk, ci++) {
-        const size_t m = (n - off < chunk) ? n - off : chunk;
-        cudaStream_t s = c->side[ci % 2];
-        uint8_t *p = c->arena + (size_t)(ci % nbuf) * set_bytes;
+    cudaStreamWaitEvent(c->copy_in, ev, 0);
+    cudaStreamWaitEvent(c->copy_out, ev, 0);
+    for (int i = 0; i < nstream; i++) cudaStreamWaitEvent(cst[i], ev, 0);
+    size_t off = 0;
+    for (size_t ci = 0; ci < plan.size() && !rc; off += plan[ci], ci++) {
+        const size_t m = plan[ci];
+        const int sl = (int)(ci % (size_t)nslot);
+        cudaStream_t cs = cst[ci * (size_t)nstream / plan.size()];
+        // a slot's buffers sit at the same offsets for every chunk (sized for the largest), so a
+        // chunk's copies in never touch the previous chunk's results still being copied out
+        uint8_t *p = c->arena + (size_t)sl * set_bytes;
         const uint8_t *din[MAXIO];
         uint8_t *dout[MAXIO];
-        for (int i = 0; i < d.nin; i++) {
+        // inputs: once the kernels of the slot's previous chunk have consumed theirs
+        if (ci >= (size_t)nslot) cudaStreamWaitEvent(c->copy_in, c->done_ev[sl], 0);
+        for (int i = 0; i < d.nin && !rc; i++) {
             uint8_t *q = p;
-            p += r256(d.in_sz[i] * chunk);
-            if ((rc = cuda_err(cudaMemcpyAsync(q, d.in[i] + off * d.in_sz[i], m * d.in_sz[i], cudaMemcpyHostToDevice, s),
-                               "H2D")))
-                break;
+            p += r256(d.in_sz[i] * mc);
+            rc = cuda_err(copy_async(q, d.in[i] + off * d.in_sz[i], m * d.in_sz[i], cudaMemcpyHostToDevice, c->copy_in),
+                          "H2D");
             din[i] = q;
         }
         if (rc) break;
+        cudaEventRecord(c->in_ev[sl], c->copy_in);
         for (int i = 0; i < d.nout; i++) {
             dout[i] = p;
-            p += r256(d.out_sz[i] * chunk);
+            p += r256(d.out_sz[i] * mc);
         }
-        uint8_t *scratch = p;
-        if ((rc = run((int)m, din, dout, scratch, s))) break;
-        for (int i = 0; i < d.nout; i++)
-            if ((rc = cuda_err(cudaMemcpyAsync(d.out[i] + off * d.out_sz[i], dout[i], m * d.out_sz[i],
-                                               cudaMemcpyDeviceToHost, s),
-                               "D2H")))
-                break;
-        if (rc) break;
+        // kernels: once the inputs are in and the slot's previous results are out
+        cudaStreamWaitEvent(cs, c->in_ev[sl], 0);
+        if (ci >= (size_t)nslot) cudaStreamWaitEvent(cs, c->free_ev[sl], 0);
+        if ((rc = run((int)m, din, dout, p, cs))) break;
+        cudaEventRecord(c->done_ev[sl], cs);
+        cudaStreamWaitEvent(c->copy_out, c->done_ev[sl], 0);
+        for (int i = 0; i < d.nout && !rc; i++)
+            rc = cuda_err(copy_async(d.out[i] + off * d.out_sz[i], dout[i], m * d.out_sz[i], cudaMemcpyDeviceToHost,
+                                     c->copy_out),
+                          "D2H");
+        cudaEventRecord(c->free_ev[sl], c->copy_out);
     }
-    cudaError_t e1 = cudaStreamSynchronize(c->side[0]);
-    cudaError_t e2 = cudaStreamSynchronize(c->side[1]);
+    cudaError_t e = cudaStreamSynchronize(c->copy_out);
+    cudaError_t e_in = cudaStreamSynchronize(c->copy_in);
+    for (int i = 0; i < nstream; i++) {
+        cudaError_t ei = cudaStreamSynchronize(cst[i]);
+        if (e == cudaSuccess) e = ei;
+    }
+    if (e == cudaSuccess) e = e_in;
     cudaEventDestroy(ev);
     if (rc) return rc;
-    if ((rc = cuda_err(e1, "sync"))) return rc;
-    if ((rc = cuda_err(e2, "sync"))) return rc;
+    if ((rc = cuda_err(e, "sync"))) return rc;
     return cuda_err(cudaGetLastError(), "kernel");
 }
 
@@ -841,6 +981,31 @@ extern "C" int pqcgpu_kyber_indcpa_dec_batch(pqcgpu_ctx *c, int variant, int k, 
     });
 }
 
+extern "C" int pqcgpu_set_host_pipeline(size_t chunk_max, size_t chunk_first, size_t chunk_last, int streams) {
+    PipeShape p;
+    if (chunk_max) p.chunk_max = chunk_max;
+    p.chunk_first = chunk_first ? chunk_first : p.chunk_max / 4;
+    p.chunk_last = chunk_last ? chunk_last : p.chunk_max / 4;
+    if (streams) p.streams = streams;
+    if (p.chunk_max < 64 || p.chunk_max > ((size_t)1 << 24))
+        return set_err(PQCGPU_EINVAL, "chunk_max must lie in [64, 2^24]");
+    if (p.chunk_first < 1 || p.chunk_first > p.chunk_max || p.chunk_last < 1 || p.chunk_last > p.chunk_max)
+        return set_err(PQCGPU_EINVAL, "chunk_first and chunk_last must lie in [1, chunk_max]");
+    if (p.streams < 1 || p.streams > pqcgpu_ctx::NPAR) return set_err(PQCGPU_EINVAL, "streams must lie in [1, 8]");
+    std::lock_guard<std::mutex> lk(g_pipe_mu);
+    g_pipe = p;
+    return PQCGPU_OK;
+}
+extern "C" int pqcgpu_get_host_pipeline(size_t *chunk_max, size_t *chunk_first, size_t *chunk_last, int *streams) {
+    if (!chunk_max || !chunk_first || !chunk_last || !streams) return set_err(PQCGPU_EINVAL, "NULL argument");
+    std::lock_guard<std::mutex> lk(g_pipe_mu);
+    *chunk_max = g_pipe.chunk_max;
+    *chunk_first = g_pipe.chunk_first;
+    *chunk_last = g_pipe.chunk_last;
+    *streams = g_pipe.streams;
+    return PQCGPU_OK;
+}
+
 extern "C" int pqcgpu_profile_enable(int on) {
     prof_enable(on != 0);
     return PQCGPU_OK;
@@ -850,6 +1015,13 @@ extern "C" int pqcgpu_profile_read(char *buf, size_t len) {
     if (!buf || len < s.size() + 1) return set_err(PQCGPU_EINVAL, "profile buffer too small");
     memcpy(buf, s.c_str(), s.size() + 1);
     return PQCGPU_OK;
+}
+extern "C" int pqcgpu_profile_trace(char *buf, size_t *len) {
+    if (!len) return set_err(PQCGPU_EINVAL, "len is NULL");
+    size_t need = 0;
+    const bool ok = prof_trace(buf, *len, &need);
+    *len = need;
+    return ok ? PQCGPU_OK : set_err(PQCGPU_EINVAL, "trace buffer too small (the records are kept; *len = bytes needed)");
 }
 extern "C" int pqcgpu_probe_peaks(int device, double *int_ops_per_s, double *keccak_perms_per_s) {
     const int rc = probe_peaks(device, int_ops_per_s, keccak_perms_per_s);

@@ -1026,6 +1026,33 @@ extern int g_ni[3][3];       // [op][k-2]: instances per CTA (kyber.cu)
 extern int g_threads[3][3];  // [op][k-2]: threads per CTA (kyber.cu)
 extern int g_dec1[3][2];     // [k-2]: {instances, threads} of the decapsulation's decryption stage
 
+// Every Kyber kernel asks for the largest shared-memory carveout of the SM's unified L1 / shared
+// storage.  Kernels that run concurrently (the chunks of a host-buffer call, the jobs of a mixed
+// batch, serving slots) then share one SM configuration: a hash kernel's CTAs, which need no shared
+// memory, do not leave an SM configured with too little shared memory for a core kernel's CTAs.
+template <class Kern>
+static void prefer_shared(Kern kern) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared) !=
+        cudaSuccess)
+        cudaGetLastError();
+}
+template <int K, int V>
+static void prefer_shared_all() {
+    prefer_shared(kyber_enc_core<K, V>);
+    prefer_shared(kyber_dec_core<K, V, DEC_FUSED>);
+    prefer_shared(kyber_dec_core<K, V, DEC_DECRYPT>);
+    prefer_shared(kyber_dec_core<K, V, DEC_REENCRYPT>);
+    prefer_shared(kyber_kp_core<K, V>);
+    prefer_shared(kyber_enc_hash_pre<K, V>);
+    prefer_shared(kyber_enc_hash_post<K, V>);
+    prefer_shared(kyber_dec_hash_pre<K, V>);
+    prefer_shared(kyber_kp_hash_post<K, V>);
+    prefer_shared(kyber_enc_hash_pre_w<K, V>);
+    prefer_shared(kyber_enc_hash_post_w<K, V>);
+    prefer_shared(kyber_dec_hash_pre_w<K, V>);
+    prefer_shared(kyber_kp_hash_post_w<K, V>);
+}
+
 template <class Kern>
 static cudaError_t ensure_smem(Kern kern, size_t bytes) {
     if (capturing()) return cudaSuccess;  // set by the uncaptured warm-up pass
@@ -1163,6 +1190,7 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
         if (cudaMemcpyToSymbol(c_keccak_rc, rc, sizeof rc) != cudaSuccess) return PQCGPU_ECUDA;           \
         if (cudaMemcpyToSymbol(c_zetas, z, sizeof z) != cudaSuccess) return PQCGPU_ECUDA;                 \
         if (cudaMemcpyToSymbol(c_zetas_inv, zi, sizeof zi) != cudaSuccess) return PQCGPU_ECUDA;           \
+        prefer_shared_all<K, V>();                                                                         \
         return PQCGPU_OK;                                                                                  \
     }                                                                                                      \
     }                                                                                                      \

@@ -25,6 +25,7 @@ void *prof_begin(cudaStream_t st, const char *name, int k, int v);
 void prof_end(cudaStream_t st, void *tok);
 void prof_enable(bool on);
 std::string prof_read();
+bool prof_trace(char *buf, size_t cap, size_t *need);
 int probe_peaks(int device, double *int_ops, double *keccak_perms);
 
 // Every kernel launch of the library goes through this macro: counted, and timed when profiling.

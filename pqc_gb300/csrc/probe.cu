@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <string.h>
 
 #include <mutex>
 #include <string>
@@ -101,6 +102,7 @@ int probe_peaks(int device, double *int_ops, double *keccak_perms) {
 namespace {
 struct Rec {
     std::string name;
+    cudaStream_t st;
     cudaEvent_t e0, e1;
 };
 std::mutex g_prof_mu;
@@ -115,8 +117,12 @@ bool prof_enabled() { return g_prof_on && !g_capturing; }
 void *prof_begin(cudaStream_t st, const char *name, int k, int v) {
     Rec *r = new Rec();
     char buf[96];
-    snprintf(buf, sizeof buf, "%s<%d,%d>", name, k, v);
+    if (k < 0)  // copies and other non-kernel records carry no template arguments
+        snprintf(buf, sizeof buf, "%s", name);
+    else
+        snprintf(buf, sizeof buf, "%s<%d,%d>", name, k, v);
     r->name = buf;
+    r->st = st;
     cudaEventCreate(&r->e0);
     cudaEventCreate(&r->e1);
     cudaEventRecord(r->e0, st);
@@ -161,6 +167,46 @@ std::string prof_read() {
         s += buf;
     }
     return s + "}";
+}
+
+
+// The records as a timeline in the Chrome trace-event format: one complete event ("ph": "X") per
+// record, times in microseconds from the earliest record, one "tid" per stream in order of first
+// use.  Returns false (records kept) when `cap` is too small; *need = the bytes with the NUL.
+bool prof_trace(char *buf, size_t cap, size_t *need) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    std::vector<double> t0(g_recs.size()), t1(g_recs.size());
+    std::vector<cudaStream_t> streams;
+    double lo = 0;
+    for (size_t i = 0; i < g_recs.size(); i++) {
+        float a = 0, b = 0;
+        cudaEventSynchronize(g_recs[i].e1);
+        cudaEventElapsedTime(&a, g_recs[0].e0, g_recs[i].e0);
+        cudaEventElapsedTime(&b, g_recs[0].e0, g_recs[i].e1);
+        t0[i] = a;
+        t1[i] = b;
+        lo = i == 0 || a < lo ? a : lo;
+    }
+    std::string s = "{\"traceEvents\": [";
+    for (size_t i = 0; i < g_recs.size(); i++) {
+        size_t tid = 0;
+        while (tid < streams.size() && streams[tid] != g_recs[i].st) tid++;
+        if (tid == streams.size()) streams.push_back(g_recs[i].st);
+        char b[256];
+        snprintf(b, sizeof b, "%s{\"name\": \"%s\", \"ph\": \"X\", \"pid\": 0, \"tid\": %zu, \"ts\": %.3f, \"dur\": %.3f}",
+                 i ? ", " : "", g_recs[i].name.c_str(), tid, 1e3 * (t0[i] - lo), 1e3 * (t1[i] - t0[i]));
+        s += b;
+    }
+    s += "]}";
+    *need = s.size() + 1;
+    if (!buf || cap < s.size() + 1) return false;
+    memcpy(buf, s.c_str(), s.size() + 1);
+    for (auto &r : g_recs) {
+        cudaEventDestroy(r.e0);
+        cudaEventDestroy(r.e1);
+    }
+    g_recs.clear();
+    return true;
 }
 
 }  // namespace pqc

@@ -5,6 +5,7 @@ Device path: the *_dev methods take torch.uint8 CUDA tensors (instance-major, 16
 asynchronous on the context stream.
 """
 import ctypes
+import json
 
 from . import _lib
 
@@ -32,6 +33,37 @@ def kyber_cpa_sizes(variant, k):
 
 
 OPS = {"keypair": 0, "enc": 1, "dec": 2}
+
+
+def profile_enable(on=True):
+    """Bracket every kernel launch and host-buffer copy with CUDA events (all contexts)."""
+    _lib.check(_lib.load().pqcgpu_profile_enable(1 if on else 0))
+
+
+def profile_trace():
+    """The profiler's records since the last read as a Chrome trace-event dict, then clears them.
+    Write it with json.dump and open it in chrome://tracing or Perfetto."""
+    lib = _lib.load()
+    need = ctypes.c_size_t(0)
+    while True:
+        buf = ctypes.create_string_buffer(need.value) if need.value else None
+        if lib.pqcgpu_profile_trace(buf, ctypes.byref(need)) == 0:
+            return json.loads(buf.value.decode())
+        if buf is not None and len(buf) >= need.value:
+            _lib.check(-1)  # failed for another reason
+
+
+def set_host_pipeline(chunk_max=0, chunk_first=0, chunk_last=0, streams=0):
+    """Chunking of host-buffer calls (all contexts); zeros select the defaults."""
+    _lib.check(_lib.load().pqcgpu_set_host_pipeline(chunk_max, chunk_first, chunk_last, streams))
+
+
+def get_host_pipeline():
+    """(chunk_max, chunk_first, chunk_last, streams) of host-buffer calls."""
+    a, b, c, d = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_int()
+    _lib.check(_lib.load().pqcgpu_get_host_pipeline(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                                    ctypes.byref(d)))
+    return a.value, b.value, c.value, d.value
 
 
 def _ptr(t):

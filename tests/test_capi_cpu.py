@@ -157,3 +157,35 @@ def test_launch_shapes_that_exceed_shared_memory_are_refused():
         assert lib.pqcgpu_set_launch_shape(nh, 1, 64, 256) != 0   # 64 x 7.5 KB
     finally:
         lib.pqcgpu_set_launch_shape(k768, 2, ni.value, thr.value)
+
+
+def test_host_pipeline_shape_validation():
+    """The host-buffer pipeline shape: zeros select the defaults, out-of-range values are refused
+    and leave the shape unchanged."""
+    from pqc_gb300 import kem
+    from pqc_gb300 import _lib
+    lib = _lib.load()
+    default = kem.get_host_pipeline()
+    assert default == (16384, 4096, 4096, 8)
+    try:
+        kem.set_host_pipeline(32768, 0, 0, 4)
+        assert kem.get_host_pipeline() == (32768, 8192, 8192, 4)
+        kem.set_host_pipeline(8192, 2048, 8192, 8)
+        assert kem.get_host_pipeline() == (8192, 2048, 8192, 8)
+        assert lib.pqcgpu_set_host_pipeline(32, 0, 0, 0) != 0         # chunk_max < 64
+        assert lib.pqcgpu_set_host_pipeline(4096, 8192, 0, 0) != 0     # chunk_first > chunk_max
+        assert lib.pqcgpu_set_host_pipeline(4096, 0, 8192, 0) != 0     # chunk_last > chunk_max
+        assert lib.pqcgpu_set_host_pipeline(0, 0, 0, 9) != 0           # more streams than the context has
+        assert kem.get_host_pipeline() == (8192, 2048, 8192, 8)
+    finally:
+        kem.set_host_pipeline(*default)
+    assert kem.get_host_pipeline() == default
+
+
+def test_profile_trace_without_records(lib):
+    """The trace call reports the size it needs and returns an empty timeline when nothing ran."""
+    from pqc_gb300 import kem
+    need = ctypes.c_size_t(0)
+    assert lib.pqcgpu_profile_trace(None, ctypes.byref(need)) != 0
+    assert need.value == len('{"traceEvents": []}') + 1
+    assert kem.profile_trace() == {"traceEvents": []}
