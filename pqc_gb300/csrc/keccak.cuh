@@ -108,6 +108,13 @@ __device__ __forceinline__ void keccak_f1600(uint2 (&A)[25]) {
     for (int r = 0; r < 24; r++) keccak_round(A, c_keccak_rc[r]);
 }
 
+// The same permutation with the round loop rolled: half the code of keccak_f1600, for kernels whose
+// several call sites would otherwise overflow the instruction cache.
+__device__ __forceinline__ void keccak_f1600_rolled(uint2 (&A)[25]) {
+#pragma unroll 1
+    for (int r = 0; r < 24; r++) keccak_round(A, c_keccak_rc[r]);
+}
+
 __device__ __forceinline__ void keccak_zero(uint2 (&A)[25]) {
 #pragma unroll
     for (int i = 0; i < 25; i++) A[i] = make_uint2(0, 0);

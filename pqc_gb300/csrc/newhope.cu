@@ -8,7 +8,9 @@
 //     into shared memory or consumed on the spot (a-hat never exists whole);
 //   - the 1024-point NTT by one warp per polynomial, 32 coefficients per lane, two passes of five
 //     layers in registers with one transpose through shared memory;
-//   - packing by one warp per instance.
+//   - packing by one warp per instance;
+//   - Keccak with the round loop rolled (keccak_f1600_rolled): the kernels have several sampler
+//     call sites, and the unrolled copies stalled instruction fetch (encapsulation +2.5 %).
 // Arithmetic mirrors the reference operation for operation (NewHope_NIST_GPU/reduce.cu:22-47,
 // ntt.cu:92-234, poly.cu:19-508), uint16 truncations and uint32 wrap-around included, so every
 // intermediate value equals the reference's.
@@ -152,7 +154,7 @@ __device__ __forceinline__ void sample_chunk(const uint2 *seed, int nonce, int c
     for (int i = 0; i < 4; i++) A[i] = seed[i];
     A[4].x = (uint32_t)nonce | ((uint32_t)chunk << 8) | (DOM_SHAKE << 16);
     A[SHAKE256_LANES - 1].y ^= 0x80000000u;
-    keccak_f1600(A);
+    keccak_f1600_rolled(A);
 #pragma unroll
     for (int w = 0; w < 32; w++) {  // word w = bytes 4w..4w+3 -> coefficients 2w, 2w+1
         const uint32_t t = (w & 1) ? A[w >> 1].y : A[w >> 1].x;
@@ -172,7 +174,7 @@ __device__ __forceinline__ void uniform_chunk(const uint2 *seed, int chunk, F em
     A[SHAKE128_LANES - 1].y ^= 0x80000000u;
     int ctr = 0;
     while (ctr < 64) {
-        keccak_f1600(A);
+        keccak_f1600_rolled(A);
 #pragma unroll
         for (int w = 0; w < 42; w++) {
             const uint32_t t = (w & 1) ? A[w >> 1].y : A[w >> 1].x;
@@ -255,7 +257,7 @@ __global__ void __launch_bounds__(256) nh_kp_core(KpArgs a, int NI) {
         uint2 A[25];
         keccak_absorb_lanes<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(a.seed + (size_t)(base + li) * a.seed_stride),
                                             4, DOM_SHAKE);
-        keccak_f1600(A);
+        keccak_f1600_rolled(A);
         uint2 *o = reinterpret_cast<uint2 *>(seeds + li * 128);
 #pragma unroll
         for (int i = 0; i < 8; i++) o[i] = A[i];
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(256) nh_dec_core(DecArgs d, int NI) {
             if (lane == 0) {
                 A[4].x ^= DOM_SHAKE;
                 A[SHAKE256_LANES - 1].y ^= 0x80000000u;
-                keccak_f1600(A);
+                keccak_f1600_rolled(A);
                 uint2 *o = reinterpret_cast<uint2 *>(out);
 #pragma unroll
                 for (int w = 0; w < 4; w++) o[w] = A[w];
@@ -450,7 +452,7 @@ __global__ void __launch_bounds__(128) nh_enc_hash_pre(int n, const uint8_t *coi
     if (x >= n) return;
     uint2 A[25], buf[8];
     keccak_absorb_lanes<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(coins + (size_t)x * 32), 4, DOM_SHAKE);
-    keccak_f1600(A);
+    keccak_f1600_rolled(A);
 #pragma unroll
     for (int i = 0; i < 8; i++) buf[i] = A[i];
     uint2 *o = reinterpret_cast<uint2 *>(scratch + (size_t)x * 64);
@@ -461,7 +463,7 @@ __global__ void __launch_bounds__(128) nh_enc_hash_pre(int n, const uint8_t *coi
     for (int i = 0; i < 4; i++) A[i] = buf[i];
     A[4].x ^= DOM_SHAKE;
     A[SHAKE256_LANES - 1].y ^= 0x80000000u;
-    keccak_f1600(A);
+    keccak_f1600_rolled(A);
     uint2 *s = reinterpret_cast<uint2 *>(ss + (size_t)x * 32);
 #pragma unroll
     for (int i = 0; i < 4; i++) s[i] = A[i];
