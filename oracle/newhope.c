@@ -1,18 +1,23 @@
 /*
- * NewHope-1024 CPA-PKE and CPA-KEM restated in plain C -- TEST INFRASTRUCTURE (CPU oracle).
+ * NewHope-1024 and NewHope-512 CPA-PKE and CPA-KEM restated in plain C -- TEST INFRASTRUCTURE
+ * (CPU oracle).
  *
  * Every integer step mirrors the reference so intermediate (lazily reduced) values agree:
  *   montgomery_reduce (R = 2^18, qinv = 12287), barrett (a*5 >> 16)
  *                                         NewHope_NIST_GPU/reduce.cu:22-47
- *   twiddle tables, generated here from g = 7 (primitive 2048-th root of unity mod 12289) and
- *   mont = 2^18 mod q with the formulas documented at NewHope_NIST_GPU/precomp.cu:27-29, :69-71:
+ *   twiddle tables, generated here from g = 7 (n = 1024; a primitive 2048-th root of unity mod
+ *   12289) or g = 10968 (n = 512; a primitive 1024-th root) and mont = 2^18 mod q with the formulas
+ *   documented at NewHope_NIST_GPU/precomp.cu:27-29, :69-71:
  *     gammas_bitrev[i] = g^brv(i) * mont, omegas_inv_bitrev[i] = g^(-2 brv(2i)) * mont,
  *     gammas_inv[i] = g^(-i) * n^-1 * mont   (all lifted to [0, q))
- *   bitrev_vector, mul_coefficients, lazy 10-layer ntt
- *                                         NewHope_NIST_GPU/ntt.cu:92-234
- *   poly_uniform (16 x SHAKE128(seed||i), 16-bit samples < 5q)
- *   poly_sample (16 x SHAKE256(seed||nonce||i) 128 B, HW(a) + q - HW(b))
- *   pointwise (3186 = R^2 mod q), add / sub with %, codecs, msg
+ *   These equal the reference's tables for both n (precomp.cu:75-183 for n = 512).
+ *   bitrev_vector, mul_coefficients, lazy ntt: 10 layers with barrett_reduce on odd layers for
+ *   n = 1024 (NewHope_NIST_GPU/ntt.cu:92-234); 9 layers with `% q` on odd layers for n = 512,
+ *   the reference's scalar n = 512 transform (ntt.cu:143-181)
+ *   poly_uniform (n/64 x SHAKE128(seed||i), 16-bit samples < 5q)
+ *   poly_sample (n/64 x SHAKE256(seed||nonce||i) 128 B, HW(a) + q - HW(b))
+ *   pointwise (3186 = R^2 mod q), add / sub with %, codecs, msg (each message bit in n/256
+ *   coefficients; tomsg subtracts q for n = 1024, q/2 for n = 512, poly.cu:226-291)
  *                                         NewHope_NIST_GPU/poly.cu:19-508
  *   cpapke_keypair / enc / dec            NewHope_NIST_GPU/cpapke.cu:265-476, with the seed layout
  *     of the NIST flow (publicseed || noiseseed = SHAKE256(seed, 64) per instance; the
@@ -25,14 +30,24 @@
 #include <string.h>
 #include "oracle.h"
 
-#define NN 1024
+#define NMAX 1024
 #define NQ 12289
-#define NPOLYBYTES 1792
-#define NPOLYCOMP 384
 
 extern _Thread_local uint64_t oracle_g_butterfly_count;
 
-static uint16_t bitrev[NN], gammas_bitrev[NN], omegas_inv_bitrev[NN / 2], gammas_inv[NN];
+/* per-n tables; NN, NPOLYBYTES below refer to the parameter set in use */
+typedef struct {
+    int n, logn;
+    uint16_t br[NMAX], gb[NMAX], oib[NMAX / 2], gi[NMAX];
+} NhTables;
+static NhTables T1024, T512;
+static _Thread_local const NhTables *T = &T1024;
+#define NN (T->n)
+#define NPOLYBYTES (14 * NN / 8)
+#define bitrev (T->br)
+#define gammas_bitrev (T->gb)
+#define omegas_inv_bitrev (T->oib)
+#define gammas_inv (T->gi)
 
 static long powmod(long b, long e, long m) {
     long r = 1;
@@ -46,18 +61,23 @@ static long powmod(long b, long e, long m) {
     return r;
 }
 
-__attribute__((constructor)) static void newhope_tables_init(void) {
-    const long g = 7, mont = (1L << 18) % NQ;
-    const long ginv = powmod(g, NQ - 2, NQ), ninv = powmod(NN, NQ - 2, NQ);
-    for (int i = 0; i < NN; i++) {
+static void tables_init(NhTables *t, int n, int logn, long g) {
+    const long mont = (1L << 18) % NQ;
+    const long ginv = powmod(g, NQ - 2, NQ), ninv = powmod(n, NQ - 2, NQ);
+    t->n = n;
+    t->logn = logn;
+    for (int i = 0; i < n; i++) {
         int r = 0;
-        for (int b = 0; b < 10; b++) r |= ((i >> b) & 1) << (9 - b);
-        bitrev[i] = (uint16_t)r;
+        for (int b = 0; b < logn; b++) r |= ((i >> b) & 1) << (logn - 1 - b);
+        t->br[i] = (uint16_t)r;
     }
-    for (int i = 0; i < NN; i++) gammas_bitrev[i] = (uint16_t)(powmod(g, bitrev[i], NQ) * mont % NQ);
-    for (int i = 0; i < NN / 2; i++)
-        omegas_inv_bitrev[i] = (uint16_t)(powmod(ginv, 2L * bitrev[2 * i], NQ) * mont % NQ);
-    for (int i = 0; i < NN; i++) gammas_inv[i] = (uint16_t)(powmod(ginv, i, NQ) * ninv % NQ * mont % NQ);
+    for (int i = 0; i < n; i++) t->gb[i] = (uint16_t)(powmod(g, t->br[i], NQ) * mont % NQ);
+    for (int i = 0; i < n / 2; i++) t->oib[i] = (uint16_t)(powmod(ginv, 2L * t->br[2 * i], NQ) * mont % NQ);
+    for (int i = 0; i < n; i++) t->gi[i] = (uint16_t)(powmod(ginv, i, NQ) * ninv % NQ * mont % NQ);
+}
+__attribute__((constructor)) static void newhope_tables_init(void) {
+    tables_init(&T1024, 1024, 10, 7);
+    tables_init(&T512, 512, 9, 10968);
 }
 
 static uint16_t nh_mont(uint32_t a) {
@@ -101,7 +121,8 @@ static void bitrev_vec(uint16_t *p) {
     }
 }
 static void nh_ntt(uint16_t *a, const uint16_t *omega) {
-    for (int i = 0; i < 10; i += 2) {
+    const int layers = T->logn;
+    for (int i = 0; i < layers; i += 2) {
         int distance = 1 << i;
         for (int start = 0; start < distance; start++) {
             int jt = 0;
@@ -112,12 +133,16 @@ static void nh_ntt(uint16_t *a, const uint16_t *omega) {
                 oracle_g_butterfly_count++;
             }
         }
+        if (i + 1 >= layers) break;
         distance <<= 1;
         for (int start = 0; start < distance; start++) {
             int jt = 0;
             for (int j = start; j < NN - 1; j += 2 * distance) {
                 uint16_t W = omega[jt++], temp = a[j];
-                a[j] = nh_barrett((uint16_t)(temp + a[j + distance]));
+                if (NN == 1024)
+                    a[j] = nh_barrett((uint16_t)(temp + a[j + distance]));
+                else
+                    a[j] = (uint16_t)((temp + a[j + distance]) % NQ);
                 a[j + distance] = nh_mont((uint32_t)W * ((uint32_t)temp + 3 * NQ - a[j + distance]));
                 oracle_g_butterfly_count++;
             }
@@ -198,17 +223,15 @@ static void poly_frommsg(uint16_t *r, const uint8_t *msg) {
         for (int j = 0; j < 8; j++) {
             uint16_t mask = (uint16_t)-((msg[i] >> j) & 1);
             uint16_t v = (uint16_t)(mask & (NQ / 2));
-            r[8 * i + j] = r[8 * i + j + 256] = r[8 * i + j + 512] = r[8 * i + j + 768] = v;
+            for (int c = 8 * i + j; c < NN; c += 256) r[c] = v;
         }
 }
 static void poly_tomsg(uint8_t *msg, const uint16_t *x) {
     memset(msg, 0, 32);
     for (int i = 0; i < 256; i++) {
-        uint16_t t = flipabs(x[i]);
-        t = (uint16_t)(t + flipabs(x[i + 256]));
-        t = (uint16_t)(t + flipabs(x[i + 512]));
-        t = (uint16_t)(t + flipabs(x[i + 768]));
-        t = (uint16_t)(t - NQ);
+        uint16_t t = 0;
+        for (int c = i; c < NN; c += 256) t = (uint16_t)(t + flipabs(x[c]));
+        t = (uint16_t)(t - (NN == 1024 ? NQ : NQ / 2));
         t >>= 15;
         msg[i >> 3] |= (uint8_t)(t << (i & 7));
     }
@@ -259,8 +282,8 @@ static void poly_sample(uint16_t *r, const uint8_t *seed, uint8_t nonce) {
     }
 }
 
-int oracle_newhope_cpapke_keypair(uint8_t *pk, uint8_t *sk, const uint8_t seed[32]) {
-    static _Thread_local uint16_t ahat[NN], ehat[NN], ahat_shat[NN], bhat[NN], shat[NN];
+static int cpa_keypair(uint8_t *pk, uint8_t *sk, const uint8_t seed[32]) {
+    static _Thread_local uint16_t ahat[NMAX], ehat[NMAX], ahat_shat[NMAX], bhat[NMAX], shat[NMAX];
     uint8_t z[64];
     oracle_shake256(z, 64, seed, 32);
     const uint8_t *publicseed = z, *noiseseed = z + 32;
@@ -277,8 +300,8 @@ int oracle_newhope_cpapke_keypair(uint8_t *pk, uint8_t *sk, const uint8_t seed[3
     return 0;
 }
 
-int oracle_newhope_cpapke_enc(uint8_t *ct, const uint8_t m[32], const uint8_t *pk, const uint8_t coin[32]) {
-    static _Thread_local uint16_t sprime[NN], eprime[NN], vprime[NN], ahat[NN], bhat[NN], epp[NN], uhat[NN], v[NN];
+static int cpa_enc(uint8_t *ct, const uint8_t m[32], const uint8_t *pk, const uint8_t coin[32]) {
+    static _Thread_local uint16_t sprime[NMAX], eprime[NMAX], vprime[NMAX], ahat[NMAX], bhat[NMAX], epp[NMAX], uhat[NMAX], v[NMAX];
     poly_frommsg(v, m);
     poly_frombytes(bhat, pk);
     poly_uniform(ahat, pk + NPOLYBYTES);
@@ -298,8 +321,8 @@ int oracle_newhope_cpapke_enc(uint8_t *ct, const uint8_t m[32], const uint8_t *p
     return 0;
 }
 
-int oracle_newhope_cpapke_dec(uint8_t m[32], const uint8_t *ct, const uint8_t *sk) {
-    static _Thread_local uint16_t vprime[NN], uhat[NN], tmp[NN], shat[NN];
+static int cpa_dec(uint8_t m[32], const uint8_t *ct, const uint8_t *sk) {
+    static _Thread_local uint16_t vprime[NMAX], uhat[NMAX], tmp[NMAX], shat[NMAX];
     poly_frombytes(shat, sk);
     poly_frombytes(uhat, ct);
     poly_decompress(vprime, ct + NPOLYBYTES);
@@ -310,19 +333,45 @@ int oracle_newhope_cpapke_dec(uint8_t m[32], const uint8_t *ct, const uint8_t *s
     return 0;
 }
 
-int oracle_newhope_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t coins[32]) {
-    return oracle_newhope_cpapke_keypair(pk, sk, coins);
-}
-int oracle_newhope_kem_enc(uint8_t *ct, uint8_t ss[32], const uint8_t *pk, const uint8_t coins[32]) {
+static int kem_enc(uint8_t *ct, uint8_t ss[32], const uint8_t *pk, const uint8_t coins[32]) {
     uint8_t buf[64];
     oracle_shake256(buf, 64, coins, 32);
-    oracle_newhope_cpapke_enc(ct, buf, pk, buf + 32);
+    cpa_enc(ct, buf, pk, buf + 32);
     oracle_shake256(ss, 32, buf, 32);
     return 0;
 }
-int oracle_newhope_kem_dec(uint8_t ss[32], const uint8_t *ct, const uint8_t *sk) {
+static int kem_dec(uint8_t ss[32], const uint8_t *ct, const uint8_t *sk) {
     uint8_t m[32];
-    oracle_newhope_cpapke_dec(m, ct, sk);
+    cpa_dec(m, ct, sk);
     oracle_shake256(ss, 32, m, 32);
     return 0;
 }
+
+/* public entry points: NewHope-1024 (oracle_newhope_*) and NewHope-512 (oracle_newhope512_*) */
+#define NH_ENTRY(prefix, tables)                                                                         \
+    int prefix##_cpapke_keypair(uint8_t *pk, uint8_t *sk, const uint8_t seed[32]) {                      \
+        T = &tables;                                                                                     \
+        return cpa_keypair(pk, sk, seed);                                                                \
+    }                                                                                                    \
+    int prefix##_cpapke_enc(uint8_t *ct, const uint8_t m[32], const uint8_t *pk, const uint8_t coin[32]) { \
+        T = &tables;                                                                                     \
+        return cpa_enc(ct, m, pk, coin);                                                                 \
+    }                                                                                                    \
+    int prefix##_cpapke_dec(uint8_t m[32], const uint8_t *ct, const uint8_t *sk) {                       \
+        T = &tables;                                                                                     \
+        return cpa_dec(m, ct, sk);                                                                       \
+    }                                                                                                    \
+    int prefix##_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t coins[32]) {                       \
+        T = &tables;                                                                                     \
+        return cpa_keypair(pk, sk, coins);                                                               \
+    }                                                                                                    \
+    int prefix##_kem_enc(uint8_t *ct, uint8_t ss[32], const uint8_t *pk, const uint8_t coins[32]) {      \
+        T = &tables;                                                                                     \
+        return kem_enc(ct, ss, pk, coins);                                                               \
+    }                                                                                                    \
+    int prefix##_kem_dec(uint8_t ss[32], const uint8_t *ct, const uint8_t *sk) {                         \
+        T = &tables;                                                                                     \
+        return kem_dec(ss, ct, sk);                                                                      \
+    }
+NH_ENTRY(oracle_newhope, T1024)
+NH_ENTRY(oracle_newhope512, T512)

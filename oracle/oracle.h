@@ -57,13 +57,19 @@ int oracle_mlkem_keypair(int k, uint8_t *pk, uint8_t *sk, const uint8_t coins[64
 int oracle_mlkem_enc(int k, uint8_t *ct, uint8_t ss[32], const uint8_t *pk, const uint8_t m[32]);
 int oracle_mlkem_dec(int k, uint8_t ss[32], const uint8_t *ct, const uint8_t *sk);
 
-/* ---- NewHope-1024 --------------------------------------------------------------------- */
+/* ---- NewHope-1024 (oracle_newhope_*) and NewHope-512 (oracle_newhope512_*) -------------- */
 int oracle_newhope_cpapke_keypair(uint8_t *pk, uint8_t *sk, const uint8_t seed[32]);
 int oracle_newhope_cpapke_enc(uint8_t *ct, const uint8_t m[32], const uint8_t *pk, const uint8_t coin[32]);
 int oracle_newhope_cpapke_dec(uint8_t m[32], const uint8_t *ct, const uint8_t *sk);
 int oracle_newhope_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t coins[32]);
 int oracle_newhope_kem_enc(uint8_t *ct, uint8_t ss[32], const uint8_t *pk, const uint8_t coins[32]);
 int oracle_newhope_kem_dec(uint8_t ss[32], const uint8_t *ct, const uint8_t *sk);
+int oracle_newhope512_cpapke_keypair(uint8_t *pk, uint8_t *sk, const uint8_t seed[32]);
+int oracle_newhope512_cpapke_enc(uint8_t *ct, const uint8_t m[32], const uint8_t *pk, const uint8_t coin[32]);
+int oracle_newhope512_cpapke_dec(uint8_t m[32], const uint8_t *ct, const uint8_t *sk);
+int oracle_newhope512_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t coins[32]);
+int oracle_newhope512_kem_enc(uint8_t *ct, uint8_t ss[32], const uint8_t *pk, const uint8_t coins[32]);
+int oracle_newhope512_kem_dec(uint8_t ss[32], const uint8_t *ct, const uint8_t *sk);
 
 /* ---- FrodoKEM-976 (SHAKE) -------------------------------------------------------------- */
 int oracle_frodo_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t coins[64]);
@@ -72,8 +78,8 @@ int oracle_frodo_kem_dec(uint8_t ss[24], const uint8_t *ct, const uint8_t *sk);
 
 /* ---- Batched drivers (OpenMP over instances; nthreads <= 0 means all cores) -------------
  * alg: 0..2 = Kyber-512/768/1024 (round 3), 3 = Kyber-1024 round 2, 4 = NewHope-1024 CPA-KEM,
- * 6..8 = ML-KEM-512/768/1024 (FIPS 203),
- *      5 = FrodoKEM-976.  Buffers are instance-major, each instance at a fixed stride. */
+ * 5 = FrodoKEM-976, 6..8 = ML-KEM-512/768/1024 (FIPS 203), 9 = NewHope-512 CPA-KEM.
+ * Buffers are instance-major, each instance at a fixed stride. */
 int oracle_batch_keypair(int alg, size_t n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int nthreads);
 int oracle_batch_enc(int alg, size_t n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *coins,
                      int nthreads);

@@ -13,7 +13,9 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 # alg ids shared with the batched drivers in batch.c
 KYBER512, KYBER768, KYBER1024, KYBER1024_R2, NEWHOPE1024, FRODO976 = range(6)
 MLKEM512, MLKEM768, MLKEM1024 = 6, 7, 8
+NEWHOPE512 = 9
 ALG_NAMES = {
+    "newhope512": NEWHOPE512,
     "mlkem512": MLKEM512,
     "mlkem768": MLKEM768,
     "mlkem1024": MLKEM1024,
@@ -56,9 +58,10 @@ def lib():
         L.oracle_kyber_indcpa_keypair.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, u8p]
         L.oracle_kyber_indcpa_enc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, u8p, u8p, u8p]
         L.oracle_kyber_indcpa_dec.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, u8p, u8p]
-        L.oracle_newhope_cpapke_keypair.argtypes = [ctypes.c_void_p, ctypes.c_void_p, u8p]
-        L.oracle_newhope_cpapke_enc.argtypes = [ctypes.c_void_p, u8p, u8p, u8p]
-        L.oracle_newhope_cpapke_dec.argtypes = [ctypes.c_void_p, u8p, u8p]
+        for pre in ("oracle_newhope", "oracle_newhope512"):
+            getattr(L, pre + "_cpapke_keypair").argtypes = [ctypes.c_void_p, ctypes.c_void_p, u8p]
+            getattr(L, pre + "_cpapke_enc").argtypes = [ctypes.c_void_p, u8p, u8p, u8p]
+            getattr(L, pre + "_cpapke_dec").argtypes = [ctypes.c_void_p, u8p, u8p]
         _lib = L
     return _lib
 
@@ -148,22 +151,31 @@ def kyber_indcpa_dec(variant, k, ct, sk):
     return m.raw
 
 
-def newhope_cpapke_keypair(seed):
-    pk = ctypes.create_string_buffer(1824)
-    sk = ctypes.create_string_buffer(1792)
-    lib().oracle_newhope_cpapke_keypair(pk, sk, bytes(seed))
+# NewHope CPA-PKE sizes by n: (pk, sk, ct)
+NEWHOPE_CPA_SIZES = {1024: (1824, 1792, 2176), 512: (928, 896, 1088)}
+
+
+def _nh(n):
+    return "oracle_newhope" if n == 1024 else "oracle_newhope512"
+
+
+def newhope_cpapke_keypair(seed, n=1024):
+    pkb, skb, _ = NEWHOPE_CPA_SIZES[n]
+    pk = ctypes.create_string_buffer(pkb)
+    sk = ctypes.create_string_buffer(skb)
+    getattr(lib(), _nh(n) + "_cpapke_keypair")(pk, sk, bytes(seed))
     return pk.raw, sk.raw
 
 
-def newhope_cpapke_enc(m, pk, coin):
-    ct = ctypes.create_string_buffer(2176)
-    lib().oracle_newhope_cpapke_enc(ct, bytes(m), bytes(pk), bytes(coin))
+def newhope_cpapke_enc(m, pk, coin, n=1024):
+    ct = ctypes.create_string_buffer(NEWHOPE_CPA_SIZES[n][2])
+    getattr(lib(), _nh(n) + "_cpapke_enc")(ct, bytes(m), bytes(pk), bytes(coin))
     return ct.raw
 
 
-def newhope_cpapke_dec(ct, sk):
+def newhope_cpapke_dec(ct, sk, n=1024):
     m = ctypes.create_string_buffer(32)
-    lib().oracle_newhope_cpapke_dec(m, bytes(ct), bytes(sk))
+    getattr(lib(), _nh(n) + "_cpapke_dec")(m, bytes(ct), bytes(sk))
     return m.raw
 
 

@@ -6,8 +6,9 @@ Run here (x86 container with the reference tree) after `oracle/build_ref.sh`:
 Fixture kinds:
   * keccak.json     -- FIPS-202 outputs from Python hashlib (independent implementation).
   * ref_*.json      -- outputs of the reference's OWN device code (Kyber_GPU_Batched for k = 2/3/4,
-                       round-2 semantics; NewHope_NIST_GPU), compiled for the host by
-                       oracle/build_ref.sh and driven with the NIST per-instance seed layout.
+                       round-2 semantics; NewHope_NIST_GPU for n = 1024 and n = 512), compiled for
+                       the host by oracle/build_ref.sh and driven with the NIST per-instance seed
+                       layout.
   * kat_*.rsp       -- NIST-format KAT records (AES-256 CTR_DRBG seeds and coins, oracle outputs).
   * restated_*.json -- outputs of the CPU oracle for paths the reference has no code for (Kyber
                        round-3 KEM, NewHope CPA-KEM, FrodoKEM-976, ML-KEM): regression pins, parity
@@ -86,27 +87,31 @@ def ref_kyber(k, n=16, s=1):
     })
 
 
-def ref_newhope(n=16, s=2):
-    L = ctypes.CDLL(os.path.join(REF, "librefnewhope.so"))
+def ref_newhope(n=16, s=2, poly_n=1024):
+    L = ctypes.CDLL(os.path.join(REF, "librefnewhope.so" if poly_n == 1024 else "librefnewhope512.so"))
+    pkb, skb, ctb = O.NEWHOPE_CPA_SIZES[poly_n]
     seed = drbg.seed48(s)
     kp = drbg.stream(seed, b"d", 32 * n)
     m = drbg.stream(seed, b"m", 32 * n)
     coins = drbg.stream(seed, b"coins", 32 * n)
-    pk = ctypes.create_string_buffer(n * 1824)
-    sk = ctypes.create_string_buffer(n * 1792)
-    ct = ctypes.create_string_buffer(n * 2176)
+    pk = ctypes.create_string_buffer(n * pkb)
+    sk = ctypes.create_string_buffer(n * skb)
+    ct = ctypes.create_string_buffer(n * ctb)
     m2 = ctypes.create_string_buffer(32 * n)
     assert L.ref_newhope_cpa_keypair(n, pk, sk, kp) == 0
     assert L.ref_newhope_cpa_enc(n, ct, m, pk.raw, coins) == 0
     assert L.ref_newhope_cpa_dec(n, m2, ct.raw, sk.raw) == 0
-    dump("ref_newhope1024_cpa.json", {
-        "source": "reference NewHope_NIST_GPU device code, host-compiled via oracle/build_ref.sh",
+    src = "reference NewHope_NIST_GPU device code, host-compiled via oracle/build_ref.sh"
+    if poly_n == 512:
+        src += " (NEWHOPE_N=512, with the reference's scalar n = 512 ntt applied per instance)"
+    dump("ref_newhope%d_cpa.json" % poly_n, {
+        "source": src,
         "n": n, "drbg_seed": s, "seed": kp.hex(), "m": m.hex(), "coins": coins.hex(),
-        "pk_sha256": [h(x) for x in chunks(pk.raw, 1824)],
-        "sk_sha256": [h(x) for x in chunks(sk.raw, 1792)],
-        "ct_sha256": [h(x) for x in chunks(ct.raw, 2176)],
+        "pk_sha256": [h(x) for x in chunks(pk.raw, pkb)],
+        "sk_sha256": [h(x) for x in chunks(sk.raw, skb)],
+        "ct_sha256": [h(x) for x in chunks(ct.raw, ctb)],
         "m_dec": m2.raw.hex(),
-        "pk0": pk.raw[:1824].hex(), "sk0": sk.raw[:1792].hex(), "ct0": ct.raw[:2176].hex(),
+        "pk0": pk.raw[:pkb].hex(), "sk0": sk.raw[:skb].hex(), "ct0": ct.raw[:ctb].hex(),
     })
 
 
@@ -153,11 +158,13 @@ if __name__ == "__main__":
     for k in (2, 3, 4):
         ref_kyber(k)
     ref_newhope()
+    ref_newhope(16, 3, 512)
     restated("kyber512", O.KYBER512, 16, 0)
     restated("kyber768", O.KYBER768, 16, 0)
     restated("kyber1024", O.KYBER1024, 16, 0)
     restated("kyber1024r2", O.KYBER1024_R2, 16, 0)
     restated("newhope1024", O.NEWHOPE1024, 16, 0)
+    restated("newhope512", O.NEWHOPE512, 16, 0)
     restated("frodo976", O.FRODO976, 4, 0)
     restated("mlkem512", O.MLKEM512, 16, 0)
     restated("mlkem768", O.MLKEM768, 16, 0)

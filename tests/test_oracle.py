@@ -40,20 +40,23 @@ def test_kyber_r2_cpa_matches_reference(oracle, k):
             assert (pk.hex(), sk.hex(), ct.hex()) == (g["pk0"], g["sk0"], g["ct0"])
 
 
-def test_newhope_cpa_matches_reference(oracle):
-    g = load_golden("ref_newhope1024_cpa.json")
+@pytest.mark.parametrize("poly_n", [1024, 512])
+def test_newhope_cpa_matches_reference(oracle, poly_n):
+    """The CPA-PKE restatement against the reference's own NewHope_NIST_GPU code (n = 512: built
+    with NEWHOPE_N=512 and the reference's scalar 512-point transform)."""
+    g = load_golden("ref_newhope%d_cpa.json" % poly_n)
     seed, m, coins = (bytes.fromhex(g[x]) for x in ("seed", "m", "coins"))
     for x in range(g["n"]):
-        pk, sk = oracle.newhope_cpapke_keypair(seed[32 * x:32 * x + 32])
+        pk, sk = oracle.newhope_cpapke_keypair(seed[32 * x:32 * x + 32], poly_n)
         assert sha(pk) == g["pk_sha256"][x]
         assert sha(sk) == g["sk_sha256"][x]
-        ct = oracle.newhope_cpapke_enc(m[32 * x:32 * x + 32], pk, coins[32 * x:32 * x + 32])
+        ct = oracle.newhope_cpapke_enc(m[32 * x:32 * x + 32], pk, coins[32 * x:32 * x + 32], poly_n)
         assert sha(ct) == g["ct_sha256"][x]
-        assert oracle.newhope_cpapke_dec(ct, sk).hex() == g["m_dec"][64 * x:64 * x + 64]
+        assert oracle.newhope_cpapke_dec(ct, sk, poly_n).hex() == g["m_dec"][64 * x:64 * x + 64]
 
 
 @pytest.mark.parametrize("name", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "newhope1024", "frodo976",
-                                  "mlkem512", "mlkem768", "mlkem1024"])
+                                  "mlkem512", "mlkem768", "mlkem1024", "newhope512"])
 def test_restated_kem_vectors(oracle, name):
     g = load_golden("restated_%s.json" % name)
     alg = oracle.ALG_NAMES[name]
