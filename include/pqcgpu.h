@@ -49,7 +49,8 @@ typedef enum {
     PQCGPU_MLKEM512 = 6,     /* ML-KEM-512 (FIPS 203): round-3 Kyber-512 K-PKE with G(d || k), K direct, */
     PQCGPU_MLKEM768 = 7,     /*   rejection key J(z || c); same sizes as the round-3 sets.  The FIPS 203 */
     PQCGPU_MLKEM1024 = 8,    /*   input checks (ek modulus, dk hash) are left to the caller. */
-    PQCGPU_NUM_ALGS = 9
+    PQCGPU_NEWHOPE512 = 9,   /* NewHope512-CPAKEM (NewHope_NIST_GPU built with NEWHOPE_N = 512) */
+    PQCGPU_NUM_ALGS = 10
 } pqcgpu_alg;
 
 typedef enum {
@@ -124,15 +125,23 @@ int pqcgpu_kyber_indcpa_enc_batch(pqcgpu_ctx *ctx, int variant, int k, size_t n,
 int pqcgpu_kyber_indcpa_dec_batch(pqcgpu_ctx *ctx, int variant, int k, size_t n, uint8_t *m, const uint8_t *ct,
                                   const uint8_t *sk, unsigned flags);
 
-/* ---- batched NewHope-1024 CPA-PKE (replaces cpapke_* of NewHope_NIST_GPU/cpapke.h:14-24) ----
- * keypair: seed 32 bytes per instance -> pk 1824, sk 1792; enc: msg and coin 32 bytes per instance
- * -> ct 2176; dec: msg out 32 bytes per instance. */
+/* ---- batched NewHope CPA-PKE (replaces cpapke_* of NewHope_NIST_GPU/cpapke.h:14-24) ----------
+ * NewHope-1024 (pqcgpu_newhope_*): keypair: seed 32 bytes per instance -> pk 1824, sk 1792; enc: msg
+ * and coin 32 bytes per instance -> ct 2176; dec: msg out 32 bytes per instance.
+ * NewHope-512 (pqcgpu_newhope512_*, the reference's NEWHOPE_N = 512 build, params.h:9-11): pk 928,
+ * sk 896, ct 1088. */
 int pqcgpu_newhope_cpapke_keypair_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *pk, uint8_t *sk, const uint8_t *seed,
                                         unsigned flags);
 int pqcgpu_newhope_cpapke_enc_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *ct, const uint8_t *msg, const uint8_t *pk,
                                     const uint8_t *coin, unsigned flags);
 int pqcgpu_newhope_cpapke_dec_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *msg, const uint8_t *ct, const uint8_t *sk,
                                     unsigned flags);
+int pqcgpu_newhope512_cpapke_keypair_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *pk, uint8_t *sk, const uint8_t *seed,
+                                           unsigned flags);
+int pqcgpu_newhope512_cpapke_enc_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *ct, const uint8_t *msg, const uint8_t *pk,
+                                       const uint8_t *coin, unsigned flags);
+int pqcgpu_newhope512_cpapke_dec_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *msg, const uint8_t *ct, const uint8_t *sk,
+                                       unsigned flags);
 
 /* ---- mixed batches and CUDA graphs --------------------------------------------------------
  * A job is one (algorithm, operation, batch) with its device buffers:
@@ -283,6 +292,9 @@ int pqcgpu_kyber1024_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, 
 int pqcgpu_newhope1024_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
 int pqcgpu_newhope1024_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
 int pqcgpu_newhope1024_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+int pqcgpu_newhope512_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+int pqcgpu_newhope512_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+int pqcgpu_newhope512_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
 int pqcgpu_frodo976_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
 int pqcgpu_frodo976_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
 int pqcgpu_frodo976_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);

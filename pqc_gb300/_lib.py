@@ -31,6 +31,9 @@ SIGNATURES = {
     "pqcgpu_newhope_cpapke_keypair_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_newhope_cpapke_enc_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_newhope_cpapke_dec_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_newhope512_cpapke_keypair_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_newhope512_cpapke_enc_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _u8p, _uint]),
+    "pqcgpu_newhope512_cpapke_dec_batch": (_int, [_vp, _sz, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_kem_mixed_batch": (_int, [_vp, _vp, _sz, _uint]),
     "pqcgpu_graph_capture": (_int, [_vp, _vp, _sz, _uint, _c.POINTER(_vp)]),
     "pqcgpu_graph_launch": (_int, [_vp]),
@@ -57,7 +60,8 @@ SIGNATURES = {
     "pqcgpu_randombytes_init_nist": (_int, [_u8p, _u8p]),
     "pqcgpu_nist_coins": (_int, [_int, _int, _u8p]),
 }
-for _alg in ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976", "mlkem512", "mlkem768", "mlkem1024"):
+for _alg in ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976", "mlkem512", "mlkem768", "mlkem1024",
+             "newhope512"):
     SIGNATURES["pqcgpu_%s_crypto_kem_keypair" % _alg] = (_int, [_u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_enc" % _alg] = (_int, [_u8p, _u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_dec" % _alg] = (_int, [_u8p, _u8p, _u8p])

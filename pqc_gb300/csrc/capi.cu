@@ -190,6 +190,7 @@ bool alg_info(int alg, AlgInfo *a) {
     case PQCGPU_MLKEM768: *a = {1184, 2400, 1088, 32, 64, 32}; return true;
     case PQCGPU_MLKEM1024: *a = {1568, 3168, 1568, 32, 64, 32}; return true;
     case PQCGPU_NEWHOPE1024: *a = {1824, 1792, 2176, 32, 32, 32}; return true;
+    case PQCGPU_NEWHOPE512: *a = {928, 896, 1088, 32, 32, 32}; return true;
     case PQCGPU_FRODO976: *a = {15632, 31296, 15744, 24, 64, 24}; return true;
     default: return false;
     }
@@ -645,7 +646,7 @@ namespace pqc {
 size_t op_scratch_bytes(int alg, int op, int plain) {
     int variant, k;
     if (kyber_alg(alg, &variant, &k)) return kyber_scratch_bytes(k, op, plain);
-    if (alg == PQCGPU_NEWHOPE1024) return op == 1 ? 64 : 0;
+    if (alg == PQCGPU_NEWHOPE1024 || alg == PQCGPU_NEWHOPE512) return op == 1 ? 64 : 0;
     if (alg == PQCGPU_FRODO976) return frodo_scratch_bytes();
     return 0;
 }
@@ -662,10 +663,11 @@ int op_dev(int alg, int op, int n, const uint8_t *in0, const uint8_t *in1, uint8
         return kyber_dec_dev(variant, k, n, out0, in0, in1, scr, kem, plain, s);
     }
     if (plain) return PQCGPU_EUNSUPPORTED;
-    if (alg == PQCGPU_NEWHOPE1024) {
-        if (op == 0) return newhope_keypair_dev(n, out0, out1, in0, 32, s);
-        if (op == 1) return newhope_enc_dev(n, out0, out1, in0, nullptr, in1, scr, 1, s);
-        return newhope_dec_dev(n, out0, in0, in1, 1, s);
+    if (alg == PQCGPU_NEWHOPE1024 || alg == PQCGPU_NEWHOPE512) {
+        const int N = alg == PQCGPU_NEWHOPE1024 ? 1024 : 512;
+        if (op == 0) return newhope_keypair_dev(N, n, out0, out1, in0, 32, s);
+        if (op == 1) return newhope_enc_dev(N, n, out0, out1, in0, nullptr, in1, scr, 1, s);
+        return newhope_dec_dev(N, n, out0, in0, in1, 1, s);
     }
     if (op == 0) return frodo_keypair_dev(n, out0, out1, in0, (int)ai.kpc, scr, s);
     if (op == 1) return frodo_enc_dev(n, out0, out1, in0, in1, scr, s);
@@ -908,7 +910,8 @@ extern "C" int pqcgpu_graph_destroy(pqcgpu_graph *g) {
 extern "C" int pqcgpu_set_launch_shape(pqcgpu_alg alg, int op, int ni, int threads) {
     int variant, k, rc;
     if (kyber_alg(alg, &variant, &k)) rc = kyber_set_shape(op, k, ni, threads);
-    else if (alg == PQCGPU_NEWHOPE1024) rc = newhope_set_shape(op, ni, threads);
+    else if (alg == PQCGPU_NEWHOPE1024) rc = newhope_set_shape(1024, op, ni, threads);
+    else if (alg == PQCGPU_NEWHOPE512) rc = newhope_set_shape(512, op, ni, threads);
     else if (alg == PQCGPU_FRODO976) rc = frodo_set_shape(op, ni, threads);
     else rc = PQCGPU_EUNSUPPORTED;
     return rc ? set_err(rc, "launch shape not accepted") : PQCGPU_OK;
@@ -917,7 +920,8 @@ extern "C" int pqcgpu_get_launch_shape(pqcgpu_alg alg, int op, int *ni, int *thr
     int variant, k;
     if (!ni || !threads) return set_err(PQCGPU_EINVAL, "null output");
     if (kyber_alg(alg, &variant, &k)) return kyber_get_shape(op, k, ni, threads);
-    if (alg == PQCGPU_NEWHOPE1024) return newhope_get_shape(op, ni, threads);
+    if (alg == PQCGPU_NEWHOPE1024) return newhope_get_shape(1024, op, ni, threads);
+    if (alg == PQCGPU_NEWHOPE512) return newhope_get_shape(512, op, ni, threads);
     if (alg == PQCGPU_FRODO976) return frodo_get_shape(op, ni, threads);
     return set_err(PQCGPU_EUNSUPPORTED, "no tunable launch shape for this algorithm");
 }
@@ -1028,56 +1032,83 @@ extern "C" int pqcgpu_probe_peaks(int device, double *int_ops_per_s, double *kec
     return rc ? set_err(rc, "probe failed") : PQCGPU_OK;
 }
 
-// ---- NewHope CPA level (replaces cpapke_* of NewHope_NIST_GPU/cpapke.h:14-24) ----
-extern "C" int pqcgpu_newhope_cpapke_keypair_batch(pqcgpu_ctx *c, size_t n, uint8_t *pk, uint8_t *sk,
-                                                   const uint8_t *seed, unsigned flags) {
+// ---- NewHope CPA level (replaces cpapke_* of NewHope_NIST_GPU/cpapke.h:14-24; N = 1024 or 512
+// as the reference's NEWHOPE_N, params.h:9-11) ----
+static int nh_cpa_keypair(int N, pqcgpu_ctx *c, size_t n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, unsigned flags) {
     if (!c) return set_err(PQCGPU_EINVAL, "bad context");
+    const size_t pb = 14 * (size_t)N / 8;
     OpDesc d;
     d.nin = 1;
     d.in[0] = seed;
     d.in_sz[0] = 32;
     d.nout = 2;
     d.out[0] = pk;
-    d.out_sz[0] = 1824;
+    d.out_sz[0] = pb + 32;
     d.out[1] = sk;
-    d.out_sz[1] = 1792;
+    d.out_sz[1] = pb;
     return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
-        return newhope_keypair_dev(m, out[0], out[1], in[0], 32, s);
+        return newhope_keypair_dev(N, m, out[0], out[1], in[0], 32, s);
     });
 }
-extern "C" int pqcgpu_newhope_cpapke_enc_batch(pqcgpu_ctx *c, size_t n, uint8_t *ct, const uint8_t *msg,
-                                               const uint8_t *pk, const uint8_t *coin, unsigned flags) {
+static int nh_cpa_enc(int N, pqcgpu_ctx *c, size_t n, uint8_t *ct, const uint8_t *msg, const uint8_t *pk,
+                      const uint8_t *coin, unsigned flags) {
     if (!c) return set_err(PQCGPU_EINVAL, "bad context");
+    const size_t pb = 14 * (size_t)N / 8;
     OpDesc d;
     d.nin = 3;
     d.in[0] = pk;
-    d.in_sz[0] = 1824;
+    d.in_sz[0] = pb + 32;
     d.in[1] = msg;
     d.in_sz[1] = 32;
     d.in[2] = coin;
     d.in_sz[2] = 32;
     d.nout = 1;
     d.out[0] = ct;
-    d.out_sz[0] = 2176;
+    d.out_sz[0] = pb + 3 * (size_t)N / 8;
     return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
-        return newhope_enc_dev(m, out[0], nullptr, in[0], in[1], in[2], nullptr, 0, s);
+        return newhope_enc_dev(N, m, out[0], nullptr, in[0], in[1], in[2], nullptr, 0, s);
     });
 }
-extern "C" int pqcgpu_newhope_cpapke_dec_batch(pqcgpu_ctx *c, size_t n, uint8_t *msg, const uint8_t *ct,
-                                               const uint8_t *sk, unsigned flags) {
+static int nh_cpa_dec(int N, pqcgpu_ctx *c, size_t n, uint8_t *msg, const uint8_t *ct, const uint8_t *sk,
+                      unsigned flags) {
     if (!c) return set_err(PQCGPU_EINVAL, "bad context");
+    const size_t pb = 14 * (size_t)N / 8;
     OpDesc d;
     d.nin = 2;
     d.in[0] = ct;
-    d.in_sz[0] = 2176;
+    d.in_sz[0] = pb + 3 * (size_t)N / 8;
     d.in[1] = sk;
-    d.in_sz[1] = 1792;
+    d.in_sz[1] = pb;
     d.nout = 1;
     d.out[0] = msg;
     d.out_sz[0] = 32;
     return run_op(c, n, d, flags, [&](int m, const uint8_t *const *in, uint8_t *const *out, uint8_t *, cudaStream_t s) {
-        return newhope_dec_dev(m, out[0], in[0], in[1], 0, s);
+        return newhope_dec_dev(N, m, out[0], in[0], in[1], 0, s);
     });
+}
+extern "C" int pqcgpu_newhope_cpapke_keypair_batch(pqcgpu_ctx *c, size_t n, uint8_t *pk, uint8_t *sk,
+                                                   const uint8_t *seed, unsigned flags) {
+    return nh_cpa_keypair(1024, c, n, pk, sk, seed, flags);
+}
+extern "C" int pqcgpu_newhope_cpapke_enc_batch(pqcgpu_ctx *c, size_t n, uint8_t *ct, const uint8_t *msg,
+                                               const uint8_t *pk, const uint8_t *coin, unsigned flags) {
+    return nh_cpa_enc(1024, c, n, ct, msg, pk, coin, flags);
+}
+extern "C" int pqcgpu_newhope_cpapke_dec_batch(pqcgpu_ctx *c, size_t n, uint8_t *msg, const uint8_t *ct,
+                                               const uint8_t *sk, unsigned flags) {
+    return nh_cpa_dec(1024, c, n, msg, ct, sk, flags);
+}
+extern "C" int pqcgpu_newhope512_cpapke_keypair_batch(pqcgpu_ctx *c, size_t n, uint8_t *pk, uint8_t *sk,
+                                                      const uint8_t *seed, unsigned flags) {
+    return nh_cpa_keypair(512, c, n, pk, sk, seed, flags);
+}
+extern "C" int pqcgpu_newhope512_cpapke_enc_batch(pqcgpu_ctx *c, size_t n, uint8_t *ct, const uint8_t *msg,
+                                                  const uint8_t *pk, const uint8_t *coin, unsigned flags) {
+    return nh_cpa_enc(512, c, n, ct, msg, pk, coin, flags);
+}
+extern "C" int pqcgpu_newhope512_cpapke_dec_batch(pqcgpu_ctx *c, size_t n, uint8_t *msg, const uint8_t *ct,
+                                                  const uint8_t *sk, unsigned flags) {
+    return nh_cpa_dec(512, c, n, msg, ct, sk, flags);
 }
 
 // ---- NIST single-instance API (default context on device 0) ----
@@ -1135,4 +1166,5 @@ PQC_NIST(kyber512, PQCGPU_KYBER512)
 PQC_NIST(kyber768, PQCGPU_KYBER768)
 PQC_NIST(kyber1024, PQCGPU_KYBER1024)
 PQC_NIST(newhope1024, PQCGPU_NEWHOPE1024)
+PQC_NIST(newhope512, PQCGPU_NEWHOPE512)
 PQC_NIST(frodo976, PQCGPU_FRODO976)

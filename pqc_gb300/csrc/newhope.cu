@@ -1,4 +1,4 @@
-// Batched NewHope-1024 CPA-PKE and CPA-KEM for sm_103a.
+// Batched NewHope-1024 and NewHope-512 CPA-PKE and CPA-KEM for sm_103a.
 //
 // Replaces cpapke_keypair / cpapke_enc / cpapke_dec (NewHope_NIST_GPU/cpapke.cu:265-476, one thread
 // per instance, every polynomial in HBM in a coefficient-major layout) with one core kernel per
@@ -7,13 +7,17 @@
 //     per thread (poly_sample / poly_uniform, NewHope_NIST_GPU/poly.cu:332-444), written straight
 //     into shared memory or consumed on the spot (a-hat never exists whole);
 //   - the 1024-point NTT by one warp per polynomial, 32 coefficients per lane, two passes of five
-//     layers in registers with one transpose through shared memory;
+//     layers in registers with one transpose through shared memory; the 512-point NTT by a
+//     half-warp per polynomial (two polynomials per warp), 32 coefficients per lane, five + four
+//     layers;
 //   - packing by one warp per instance;
 //   - Keccak with the round loop rolled (keccak_f1600_rolled): the kernels have several sampler
 //     call sites, and the unrolled copies stalled instruction fetch (encapsulation +2.5 %).
 // Arithmetic mirrors the reference operation for operation (NewHope_NIST_GPU/reduce.cu:22-47,
 // ntt.cu:92-234, poly.cu:19-508), uint16 truncations and uint32 wrap-around included, so every
-// intermediate value equals the reference's.
+// intermediate value equals the reference's.  For n = 512 the transform follows the reference's
+// scalar 512-point ntt (ntt.cu:143-181), which reduces odd layers with `% q` where the 1024-point
+// one uses barrett_reduce; each message bit occupies n / 256 coefficients (poly.cu:226-291).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -23,15 +27,25 @@
 namespace pqc {
 namespace newhope {
 
-constexpr int N = 1024;
 constexpr uint32_t Q = 12289;
-constexpr int POLYBYTES = 1792, PKB = 1824, SKB = 1792, CTB = 2176, COMPB = 384;
-constexpr int PITCH = 1280;  // uint16 per shared polynomial: 8 pad after every 32 coefficients
 
-// Tables generated on the host (g = 7, mont = 2^18 mod q; NewHope_NIST_GPU/precomp.cu:27-29).
-static __device__ uint16_t d_gammas_bitrev[N];
-static __device__ uint16_t d_omegas_inv_bitrev[N / 2];
-static __device__ uint16_t d_gammas_inv[N];
+// Sizes of the parameter set with n coefficients (NewHope_NIST_GPU/params.h:25-31).
+// PITCH = uint16 per shared polynomial: 8 pad after every 32 coefficients; for n = 512 another 16
+// so that the two polynomials of a warp's half-warps start 8 banks apart.
+template <int N>
+struct Nh {
+    static constexpr int POLYBYTES = 14 * N / 8, PKB = POLYBYTES + 32, SKB = POLYBYTES, COMPB = 3 * N / 8,
+                         CTB = POLYBYTES + COMPB, NCH = N / 64, PITCH = N + N / 4 + (N == 512 ? 16 : 0);
+};
+
+// Tables generated on the host (g = 7 for n = 1024, g = 10968 for n = 512; mont = 2^18 mod q;
+// NewHope_NIST_GPU/precomp.cu:27-29, :75-183).
+static __device__ uint16_t d_gammas_bitrev[1024];
+static __device__ uint16_t d_omegas_inv_bitrev[512];
+static __device__ uint16_t d_gammas_inv[1024];
+static __device__ uint16_t d_gammas_bitrev512[512];
+static __device__ uint16_t d_omegas_inv_bitrev512[256];
+static __device__ uint16_t d_gammas_inv512[512];
 
 __device__ __forceinline__ int phys(int i) { return i + ((i >> 5) << 3); }
 
@@ -60,16 +74,21 @@ __device__ __forceinline__ uint32_t flipabs(uint32_t x) {
     const int32_t m = (int16_t)r >> 15;
     return (uint32_t)((r + m) ^ m) & 0xffffu;
 }
-// butterfly of ntt(): a <- a + b (even layer) or barrett(a + b) (odd layer); b <- mont(W (a + 3q - b))
+// butterfly of ntt(): a <- a + b (even layer) or, on odd layers, barrett(a + b) (n = 1024) /
+// (a + b) % q (n = 512); b <- mont(W (a + 3q - b))
+template <int N>
 __device__ __forceinline__ void bfly(uint32_t &a, uint32_t &b, uint32_t W, bool odd) {
     const uint32_t temp = a;
-    a = odd ? barrett(temp + b) : ((temp + b) & 0xffffu);
+    if (N == 1024)
+        a = odd ? barrett(temp + b) : ((temp + b) & 0xffffu);
+    else
+        a = odd ? (temp + b) % Q : ((temp + b) & 0xffffu);
     b = mont(W * (temp + 3 * Q - b));
 }
 
 // Forward transform (poly_ntt, poly.cu:519-531): mul_coefficients(gammas_bitrev) then
 // ntt(gammas_bitrev as omega).  Layer i pairs j, j + 2^i with twiddle omega[j >> (i + 1)].
-__device__ void ntt_warp(uint16_t *p, int lane) {
+__device__ void ntt_warp(uint16_t *p, int lane) {  // n = 1024
     uint32_t r[32];
     uint16_t *pa = p + phys(32 * lane);
 #pragma unroll
@@ -88,7 +107,7 @@ __device__ void ntt_warp(uint16_t *p, int lane) {
     for (int i = 0; i < 5; i++)
 #pragma unroll
         for (int q = 0; q < 32; q++)
-            if (!((q >> i) & 1)) bfly(r[q], r[q + (1 << i)], __ldg(&d_gammas_bitrev[(32 * lane + q) >> (i + 1)]), i & 1);
+            if (!((q >> i) & 1)) bfly<1024>(r[q], r[q + (1 << i)], __ldg(&d_gammas_bitrev[(32 * lane + q) >> (i + 1)]), i & 1);
 #pragma unroll
     for (int v = 0; v < 4; v++)
         reinterpret_cast<uint4 *>(pa)[v] =
@@ -101,7 +120,7 @@ __device__ void ntt_warp(uint16_t *p, int lane) {
     for (int i = 5; i < 10; i++)
 #pragma unroll
         for (int q = 0; q < 32; q++)
-            if (!((q >> (i - 5)) & 1)) bfly(r[q], r[q + (1 << (i - 5))], __ldg(&d_gammas_bitrev[q >> (i - 4)]), i & 1);
+            if (!((q >> (i - 5)) & 1)) bfly<1024>(r[q], r[q + (1 << (i - 5))], __ldg(&d_gammas_bitrev[q >> (i - 4)]), i & 1);
 #pragma unroll
     for (int q = 0; q < 32; q++) p[phys(lane + 32 * q)] = (uint16_t)r[q];
     __syncwarp();
@@ -109,7 +128,7 @@ __device__ void ntt_warp(uint16_t *p, int lane) {
 
 // Inverse transform (poly_invntt, poly.cu:541-547): bitrev_vector, ntt(omegas_inv_bitrev),
 // mul_coefficients(gammas_inv).  The bit reversal is folded into the first pass's loads.
-__device__ void invntt_warp(uint16_t *p, int lane) {
+__device__ void invntt_warp(uint16_t *p, int lane) {  // n = 1024
     uint32_t r[32];
     const int lrev = __brev(lane) >> 27;
 #pragma unroll
@@ -123,7 +142,7 @@ __device__ void invntt_warp(uint16_t *p, int lane) {
 #pragma unroll
         for (int q = 0; q < 32; q++)
             if (!((q >> i) & 1))
-                bfly(r[q], r[q + (1 << i)], __ldg(&d_omegas_inv_bitrev[(32 * lane + q) >> (i + 1)]), i & 1);
+                bfly<1024>(r[q], r[q + (1 << i)], __ldg(&d_omegas_inv_bitrev[(32 * lane + q) >> (i + 1)]), i & 1);
     uint16_t *pa = p + phys(32 * lane);
 #pragma unroll
     for (int v = 0; v < 4; v++)
@@ -138,9 +157,102 @@ __device__ void invntt_warp(uint16_t *p, int lane) {
 #pragma unroll
         for (int q = 0; q < 32; q++)
             if (!((q >> (i - 5)) & 1))
-                bfly(r[q], r[q + (1 << (i - 5))], __ldg(&d_omegas_inv_bitrev[q >> (i - 4)]), i & 1);
+                bfly<1024>(r[q], r[q + (1 << (i - 5))], __ldg(&d_omegas_inv_bitrev[q >> (i - 4)]), i & 1);
 #pragma unroll
     for (int q = 0; q < 32; q++) p[phys(lane + 32 * q)] = (uint16_t)mont(r[q] * __ldg(&d_gammas_inv[lane + 32 * q]));
+    __syncwarp();
+}
+
+// n = 512 transforms by a half-warp: lane l (0..15) of each half holds 32 coefficients.  Pass 1
+// (layers 0-4, distances 1..16) on the 32 consecutive coefficients 32 l + q, pass 2 (layers 5-8,
+// distances 32..256) on the coefficients l + 16 q.  Both halves call together (the __syncwarp
+// calls need all 32 lanes); a half with act == false touches no memory.
+__device__ void ntt512_half(uint16_t *p, int l, bool act) {
+    uint32_t r[32];
+    if (act) {
+        uint16_t *pa = p + phys(32 * l);
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            const uint4 w = reinterpret_cast<const uint4 *>(pa)[v];
+            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                r[8 * v + 2 * h] = ws[h] & 0xffffu;
+                r[8 * v + 2 * h + 1] = ws[h] >> 16;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 32; q++) r[q] = mont(r[q] * __ldg(&d_gammas_bitrev512[32 * l + q]));
+#pragma unroll
+        for (int i = 0; i < 5; i++)
+#pragma unroll
+            for (int q = 0; q < 32; q++)
+                if (!((q >> i) & 1))
+                    bfly<512>(r[q], r[q + (1 << i)], __ldg(&d_gammas_bitrev512[(32 * l + q) >> (i + 1)]), i & 1);
+#pragma unroll
+        for (int v = 0; v < 4; v++)
+            reinterpret_cast<uint4 *>(pa)[v] =
+                make_uint4(r[8 * v] | (r[8 * v + 1] << 16), r[8 * v + 2] | (r[8 * v + 3] << 16),
+                           r[8 * v + 4] | (r[8 * v + 5] << 16), r[8 * v + 6] | (r[8 * v + 7] << 16));
+    }
+    __syncwarp();
+    if (act) {
+#pragma unroll
+        for (int q = 0; q < 32; q++) r[q] = p[phys(l + 16 * q)];
+        // layer i pairs j, j + 2^i; with j = l + 16 q that is q, q + 2^(i-4), twiddle j >> (i+1) = q >> (i-3)
+#pragma unroll
+        for (int i = 5; i < 9; i++)
+#pragma unroll
+            for (int q = 0; q < 32; q++)
+                if (!((q >> (i - 4)) & 1))
+                    bfly<512>(r[q], r[q + (1 << (i - 4))], __ldg(&d_gammas_bitrev512[q >> (i - 3)]), i & 1);
+#pragma unroll
+        for (int q = 0; q < 32; q++) p[phys(l + 16 * q)] = (uint16_t)r[q];
+    }
+    __syncwarp();
+}
+
+// Inverse (poly_invntt): bit reversal folded into the first loads, x'[32 l + q] = x[brv9(32 l + q)]
+// = x[16 brv5(q) + brv4(l)], then the two passes with omegas_inv, then gammas_inv.
+__device__ void invntt512_half(uint16_t *p, int l, bool act) {
+    uint32_t r[32];
+    if (act) {
+        const int lrev = __brev(l) >> 28;
+#pragma unroll
+        for (int q = 0; q < 32; q++) {
+            const int qrev = __brev(q) >> 27;
+            r[q] = p[phys(16 * qrev + lrev)];
+        }
+    }
+    __syncwarp();
+    if (act) {
+#pragma unroll
+        for (int i = 0; i < 5; i++)
+#pragma unroll
+            for (int q = 0; q < 32; q++)
+                if (!((q >> i) & 1))
+                    bfly<512>(r[q], r[q + (1 << i)], __ldg(&d_omegas_inv_bitrev512[(32 * l + q) >> (i + 1)]), i & 1);
+        uint16_t *pa = p + phys(32 * l);
+#pragma unroll
+        for (int v = 0; v < 4; v++)
+            reinterpret_cast<uint4 *>(pa)[v] =
+                make_uint4(r[8 * v] | (r[8 * v + 1] << 16), r[8 * v + 2] | (r[8 * v + 3] << 16),
+                           r[8 * v + 4] | (r[8 * v + 5] << 16), r[8 * v + 6] | (r[8 * v + 7] << 16));
+    }
+    __syncwarp();
+    if (act) {
+#pragma unroll
+        for (int q = 0; q < 32; q++) r[q] = p[phys(l + 16 * q)];
+#pragma unroll
+        for (int i = 5; i < 9; i++)
+#pragma unroll
+            for (int q = 0; q < 32; q++)
+                if (!((q >> (i - 4)) & 1))
+                    bfly<512>(r[q], r[q + (1 << (i - 4))], __ldg(&d_omegas_inv_bitrev512[q >> (i - 3)]), i & 1);
+#pragma unroll
+        for (int q = 0; q < 32; q++)
+            p[phys(l + 16 * q)] = (uint16_t)mont(r[q] * __ldg(&d_gammas_inv512[l + 16 * q]));
+    }
     __syncwarp();
 }
 
@@ -209,8 +321,10 @@ __device__ __forceinline__ uint32_t coeff_from_bytes(const uint8_t *bytes, int i
     frombytes4(c, bytes + 7 * (i >> 2));
     return c[i & 3];
 }
+template <int N>
 __device__ __forceinline__ uint32_t decompress_coeff(const uint8_t *cb, int i) {
     // 3-bit values packed LSB-first, 8 per 3 bytes (poly_decompress, poly.cu:197-216)
+    constexpr int COMPB = Nh<N>::COMPB;
     const int bit = 3 * i;
     const uint32_t w = cb[bit >> 3] | ((uint32_t)cb[(bit >> 3) + 1 < COMPB ? (bit >> 3) + 1 : (bit >> 3)] << 8);
     const uint32_t t = (w >> (bit & 7)) & 7;
@@ -241,15 +355,19 @@ struct DecArgs {
     int kem;
 };
 
+template <int N>
 __device__ __forceinline__ uint16_t *npoly(uint16_t *polys, int per, int li, int s) {
-    return polys + ((size_t)li * per + s) * PITCH;
+    return polys + ((size_t)li * per + s) * Nh<N>::PITCH;
 }
 
 // keypair: slots 0 s-hat, 1 e-hat -> b-hat
+template <int N>
 __global__ void __launch_bounds__(256) nh_kp_core(KpArgs a, int NI) {
+    using P = Nh<N>;
+    constexpr int NCH = P::NCH;
     extern __shared__ __align__(16) uint8_t smem[];
     uint16_t *polys = reinterpret_cast<uint16_t *>(smem);
-    uint8_t *seeds = smem + (size_t)NI * 2 * PITCH * 2;
+    uint8_t *seeds = smem + (size_t)NI * 2 * P::PITCH * 2;
     const int base = blockIdx.x * NI, ni = min(NI, a.n - base);
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
     // publicseed || noiseseed = SHAKE256(seed, 64)
@@ -263,20 +381,24 @@ __global__ void __launch_bounds__(256) nh_kp_core(KpArgs a, int NI) {
         for (int i = 0; i < 8; i++) o[i] = A[i];
     }
     __syncthreads();
-    for (int job = tid; job < ni * 32; job += nthr) {
-        const int li = job >> 5, pl = (job >> 4) & 1, ch = job & 15;
-        uint16_t *dst = npoly(polys, 2, li, pl);
+    for (int job = tid; job < ni * 2 * NCH; job += nthr) {
+        const int li = job / (2 * NCH), pl = (job / NCH) & 1, ch = job % NCH;
+        uint16_t *dst = npoly<N>(polys, 2, li, pl);
         sample_chunk(reinterpret_cast<const uint2 *>(seeds + li * 128 + 32), pl, ch, [&](int j, uint32_t c0, uint32_t c1) {
             *reinterpret_cast<uint32_t *>(dst + phys(64 * ch + j)) = (c0 & 0xffff) | (c1 << 16);
         });
     }
     __syncthreads();
-    for (int w = warp; w < ni * 2; w += nwarp) ntt_warp(npoly(polys, 2, w >> 1, w & 1), lane);
+    if constexpr (N == 1024) {
+        for (int w = warp; w < ni * 2; w += nwarp) ntt_warp(npoly<N>(polys, 2, w >> 1, w & 1), lane);
+    } else {  // one instance per warp: s-hat on lanes 0-15, e-hat on lanes 16-31
+        for (int w = warp; w < ni; w += nwarp) ntt512_half(npoly<N>(polys, 2, w, lane >> 4), lane & 15, true);
+    }
     __syncthreads();
     // b-hat = e-hat + pointwise(s-hat, a-hat), a-hat generated chunk by chunk
-    for (int job = tid; job < ni * 16; job += nthr) {
-        const int li = job >> 4, ch = job & 15;
-        uint16_t *s = npoly(polys, 2, li, 0), *e = npoly(polys, 2, li, 1);
+    for (int job = tid; job < ni * NCH; job += nthr) {
+        const int li = job / NCH, ch = job % NCH;
+        uint16_t *s = npoly<N>(polys, 2, li, 0), *e = npoly<N>(polys, 2, li, 1);
         uniform_chunk(reinterpret_cast<const uint2 *>(seeds + li * 128), ch, [&](int j, uint32_t av) {
             const int idx = phys(64 * ch + j);
             const uint32_t t = mont(3186u * av);
@@ -286,8 +408,8 @@ __global__ void __launch_bounds__(256) nh_kp_core(KpArgs a, int NI) {
     }
     __syncthreads();
     for (int li = warp; li < ni; li += nwarp) {
-        uint8_t *sk = a.sk + (size_t)(base + li) * SKB, *pk = a.pk + (size_t)(base + li) * PKB;
-        const uint16_t *s = npoly(polys, 2, li, 0), *b = npoly(polys, 2, li, 1);
+        uint8_t *sk = a.sk + (size_t)(base + li) * P::SKB, *pk = a.pk + (size_t)(base + li) * P::PKB;
+        const uint16_t *s = npoly<N>(polys, 2, li, 0), *b = npoly<N>(polys, 2, li, 1);
         for (int g = lane; g < N / 4; g += 32) {
             uint8_t o[7];
             tobytes4(o, s[phys(4 * g)], s[phys(4 * g + 1)], s[phys(4 * g + 2)], s[phys(4 * g + 3)]);
@@ -297,33 +419,40 @@ __global__ void __launch_bounds__(256) nh_kp_core(KpArgs a, int NI) {
 #pragma unroll
             for (int q = 0; q < 7; q++) pk[7 * g + q] = o[q];
         }
-        if (lane < 4) reinterpret_cast<uint2 *>(pk + POLYBYTES)[lane] = reinterpret_cast<const uint2 *>(seeds + li * 128)[lane];
+        if (lane < 4) reinterpret_cast<uint2 *>(pk + P::POLYBYTES)[lane] = reinterpret_cast<const uint2 *>(seeds + li * 128)[lane];
     }
 }
 
 // encryption: slots 0 s', 1 e' -> u-hat, 2 v'
+template <int N>
 __global__ void __launch_bounds__(256) nh_enc_core(EncArgs a, int NI) {
+    using P = Nh<N>;
+    constexpr int NCH = P::NCH;
     extern __shared__ __align__(16) uint8_t smem[];
     uint16_t *polys = reinterpret_cast<uint16_t *>(smem);
     const int base = blockIdx.x * NI, ni = min(NI, a.n - base);
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
-    for (int job = tid; job < ni * 32; job += nthr) {
-        const int li = job >> 5, pl = (job >> 4) & 1, ch = job & 15;
-        uint16_t *dst = npoly(polys, 3, li, pl);
+    for (int job = tid; job < ni * 2 * NCH; job += nthr) {
+        const int li = job / (2 * NCH), pl = (job / NCH) & 1, ch = job % NCH;
+        uint16_t *dst = npoly<N>(polys, 3, li, pl);
         sample_chunk(reinterpret_cast<const uint2 *>(a.coin + (size_t)(base + li) * a.coin_stride), pl, ch,
                      [&](int j, uint32_t c0, uint32_t c1) {
                          *reinterpret_cast<uint32_t *>(dst + phys(64 * ch + j)) = (c0 & 0xffff) | (c1 << 16);
                      });
     }
     __syncthreads();
-    for (int w = warp; w < ni * 2; w += nwarp) ntt_warp(npoly(polys, 3, w >> 1, w & 1), lane);
+    if constexpr (N == 1024) {
+        for (int w = warp; w < ni * 2; w += nwarp) ntt_warp(npoly<N>(polys, 3, w >> 1, w & 1), lane);
+    } else {  // one instance per warp: s' on lanes 0-15, e' on lanes 16-31
+        for (int w = warp; w < ni; w += nwarp) ntt512_half(npoly<N>(polys, 3, w, lane >> 4), lane & 15, true);
+    }
     __syncthreads();
     // u-hat = pointwise(a-hat, s') + e' (a-hat chunk by chunk); v' = pointwise(b-hat, s')
-    for (int job = tid; job < ni * 16; job += nthr) {
-        const int li = job >> 4, ch = job & 15;
-        const uint8_t *pk = a.pk + (size_t)(base + li) * PKB;
-        uint16_t *s = npoly(polys, 3, li, 0), *e = npoly(polys, 3, li, 1), *v = npoly(polys, 3, li, 2);
-        uniform_chunk(reinterpret_cast<const uint2 *>(pk + POLYBYTES), ch, [&](int j, uint32_t av) {
+    for (int job = tid; job < ni * NCH; job += nthr) {
+        const int li = job / NCH, ch = job % NCH;
+        const uint8_t *pk = a.pk + (size_t)(base + li) * P::PKB;
+        uint16_t *s = npoly<N>(polys, 3, li, 0), *e = npoly<N>(polys, 3, li, 1), *v = npoly<N>(polys, 3, li, 2);
+        uniform_chunk(reinterpret_cast<const uint2 *>(pk + P::POLYBYTES), ch, [&](int j, uint32_t av) {
             const int idx = phys(64 * ch + j);
             const uint32_t t = mont(3186u * s[idx]);
             const uint32_t u = mont(av * t);
@@ -341,12 +470,19 @@ __global__ void __launch_bounds__(256) nh_enc_core(EncArgs a, int NI) {
         }
     }
     __syncthreads();
-    for (int w = warp; w < ni; w += nwarp) invntt_warp(npoly(polys, 3, w, 2), lane);
+    if constexpr (N == 1024) {
+        for (int w = warp; w < ni; w += nwarp) invntt_warp(npoly<N>(polys, 3, w, 2), lane);
+    } else {  // two instances per warp
+        for (int w = warp; 2 * w < ni; w += nwarp) {
+            const int li = 2 * w + (lane >> 4);
+            invntt512_half(npoly<N>(polys, 3, li < ni ? li : 0, 2), lane & 15, li < ni);
+        }
+    }
     __syncthreads();
     // v' = v' + e'' + msg, compress (chunk jobs, noise nonce 2)
-    for (int job = tid; job < ni * 16; job += nthr) {
-        const int li = job >> 4, ch = job & 15;
-        uint16_t *v = npoly(polys, 3, li, 2);
+    for (int job = tid; job < ni * NCH; job += nthr) {
+        const int li = job / NCH, ch = job % NCH;
+        uint16_t *v = npoly<N>(polys, 3, li, 2);
         const uint8_t *m = a.m + (size_t)(base + li) * a.m_stride;
         sample_chunk(reinterpret_cast<const uint2 *>(a.coin + (size_t)(base + li) * a.coin_stride), 2, ch,
                      [&](int j, uint32_t c0, uint32_t c1) {
@@ -363,8 +499,8 @@ __global__ void __launch_bounds__(256) nh_enc_core(EncArgs a, int NI) {
     }
     __syncthreads();
     for (int li = warp; li < ni; li += nwarp) {
-        uint8_t *ct = a.ct + (size_t)(base + li) * CTB;
-        const uint16_t *u = npoly(polys, 3, li, 1), *v = npoly(polys, 3, li, 2);
+        uint8_t *ct = a.ct + (size_t)(base + li) * P::CTB;
+        const uint16_t *u = npoly<N>(polys, 3, li, 1), *v = npoly<N>(polys, 3, li, 2);
         for (int g = lane; g < N / 4; g += 32) {
             uint8_t o[7];
             tobytes4(o, u[phys(4 * g)], u[phys(4 * g + 1)], u[phys(4 * g + 2)], u[phys(4 * g + 3)]);
@@ -375,7 +511,7 @@ __global__ void __launch_bounds__(256) nh_enc_core(EncArgs a, int NI) {
             uint32_t t[8];
 #pragma unroll
             for (int q = 0; q < 8; q++) t[q] = v[phys(8 * g + q)];
-            uint8_t *r = ct + POLYBYTES + 3 * g;
+            uint8_t *r = ct + P::POLYBYTES + 3 * g;
             r[0] = (uint8_t)(t[0] | (t[1] << 3) | (t[2] << 6));
             r[1] = (uint8_t)((t[2] >> 2) | (t[3] << 1) | (t[4] << 4) | (t[5] << 7));
             r[2] = (uint8_t)((t[5] >> 1) | (t[6] << 2) | (t[7] << 5));
@@ -384,14 +520,18 @@ __global__ void __launch_bounds__(256) nh_enc_core(EncArgs a, int NI) {
 }
 
 // decryption: tmp = invntt(pointwise(s-hat, u-hat)); m = tomsg(tmp - v')
+// n = 1024: one warp per instance.  n = 512: one half-warp per instance (two per warp).
+template <int N>
 __global__ void __launch_bounds__(256) nh_dec_core(DecArgs d, int NI) {
+    using P = Nh<N>;
+    if constexpr (N == 1024) {
     extern __shared__ __align__(16) uint8_t smem[];
     uint16_t *polys = reinterpret_cast<uint16_t *>(smem);
     const int base = blockIdx.x * NI, ni = min(NI, d.n - base);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
     for (int li = warp; li < ni; li += nwarp) {
-        const uint8_t *sk = d.sk + (size_t)(base + li) * SKB, *ct = d.ct + (size_t)(base + li) * CTB;
-        uint16_t *t = npoly(polys, 1, li, 0);
+        const uint8_t *sk = d.sk + (size_t)(base + li) * P::SKB, *ct = d.ct + (size_t)(base + li) * P::CTB;
+        uint16_t *t = npoly<N>(polys, 1, li, 0);
         for (int g = lane; g < N / 4; g += 32) {
             uint32_t s[4], u[4];
             frombytes4(s, sk + 7 * g);
@@ -402,7 +542,7 @@ __global__ void __launch_bounds__(256) nh_dec_core(DecArgs d, int NI) {
         __syncwarp();
         invntt_warp(t, lane);
         // lane = message byte: bits 8 lane + b use coefficients i, i+256, i+512, i+768
-        const uint8_t *cv = ct + POLYBYTES;
+        const uint8_t *cv = ct + P::POLYBYTES;
         uint32_t byte = 0;
 #pragma unroll
         for (int b = 0; b < 8; b++) {
@@ -411,7 +551,7 @@ __global__ void __launch_bounds__(256) nh_dec_core(DecArgs d, int NI) {
 #pragma unroll
             for (int qq = 0; qq < 4; qq++) {
                 const int c = i + 256 * qq;
-                const uint32_t x = (t[phys(c)] + 3 * Q - decompress_coeff(cv, c)) % Q;
+                const uint32_t x = (t[phys(c)] + 3 * Q - decompress_coeff<N>(cv, c)) % Q;
                 acc = (acc + flipabs(x)) & 0xffff;
             }
             acc = (acc - Q) & 0xffff;
@@ -444,6 +584,77 @@ __global__ void __launch_bounds__(256) nh_dec_core(DecArgs d, int NI) {
             }
         }
     }
+    } else {
+        extern __shared__ __align__(16) uint8_t smem[];
+        uint16_t *polys = reinterpret_cast<uint16_t *>(smem);
+        const int base = blockIdx.x * NI, ni = min(NI, d.n - base);
+        const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+        const int l = lane & 15, half = lane >> 4;
+        for (int w = warp; 2 * w < ni; w += nwarp) {
+            const int li = 2 * w + half;
+            const bool act = li < ni;
+            const int lc = act ? li : 0;
+            const uint8_t *sk = d.sk + (size_t)(base + lc) * P::SKB, *ct = d.ct + (size_t)(base + lc) * P::CTB;
+            uint16_t *t = npoly<N>(polys, 1, lc, 0);
+            if (act)
+                for (int g = l; g < N / 4; g += 16) {
+                    uint32_t s[4], u[4];
+                    frombytes4(s, sk + 7 * g);
+                    frombytes4(u, ct + 7 * g);
+#pragma unroll
+                    for (int q = 0; q < 4; q++) t[phys(4 * g + q)] = (uint16_t)mont(s[q] * mont(3186u * u[q]));
+                }
+            __syncwarp();
+            invntt512_half(t, l, act);
+            // lane l of the half = message bytes 2l, 2l+1: bit 8 byte + b uses coefficients i, i+256
+            const uint8_t *cv = ct + P::POLYBYTES;
+            uint32_t bytes2 = 0;
+            if (act)
+#pragma unroll
+                for (int b = 0; b < 16; b++) {
+                    const int i = 16 * l + b;
+                    uint32_t acc = 0;
+#pragma unroll
+                    for (int qq = 0; qq < 2; qq++) {
+                        const int c = i + 256 * qq;
+                        const uint32_t x = (t[phys(c)] + 3 * Q - decompress_coeff<N>(cv, c)) % Q;
+                        acc = (acc + flipabs(x)) & 0xffff;
+                    }
+                    acc = (acc - Q / 2) & 0xffff;
+                    bytes2 |= (acc >> 15) << b;
+                }
+            uint8_t *out = d.m_out + (size_t)(base + lc) * 32;
+            if (!d.kem) {
+                if (act) {
+                    out[2 * l] = (uint8_t)bytes2;
+                    out[2 * l + 1] = (uint8_t)(bytes2 >> 8);
+                }
+            } else {
+                // ss = SHAKE256(m', 32): the half's lane 0 gathers its 32 message bytes (two per lane)
+                uint2 A[25];
+                keccak_zero(A);
+#pragma unroll
+                for (int w4 = 0; w4 < 4; w4++) {
+                    uint32_t lo = 0, hi = 0;
+#pragma unroll
+                    for (int b = 0; b < 2; b++) {
+                        lo |= (__shfl_sync(0xffffffffu, bytes2, 16 * half + 4 * w4 + b) & 0xffff) << (16 * b);
+                        hi |= (__shfl_sync(0xffffffffu, bytes2, 16 * half + 4 * w4 + 2 + b) & 0xffff) << (16 * b);
+                    }
+                    A[w4] = make_uint2(lo, hi);
+                }
+                if (act && l == 0) {
+                    A[4].x ^= DOM_SHAKE;
+                    A[SHAKE256_LANES - 1].y ^= 0x80000000u;
+                    keccak_f1600_rolled(A);
+                    uint2 *o = reinterpret_cast<uint2 *>(out);
+#pragma unroll
+                    for (int w4 = 0; w4 < 4; w4++) o[w4] = A[w4];
+                }
+            }
+            __syncwarp();
+        }
+    }
 }
 
 // CPA-KEM encapsulation prologue: buf = SHAKE256(coins, 64) -> m || coin; ss = SHAKE256(m, 32)
@@ -469,7 +680,9 @@ __global__ void __launch_bounds__(128) nh_enc_hash_pre(int n, const uint8_t *coi
     for (int i = 0; i < 4; i++) s[i] = A[i];
 }
 
-static int g_shape[3][2] = {{8, 128}, {4, 64}, {4, 128}};  // [op] = {instances per CTA, threads}
+// [n index: 0 = 1024, 1 = 512][op] = {instances per CTA, threads}
+static int g_shape[2][3][2] = {{{8, 128}, {4, 64}, {4, 128}}, {{16, 128}, {8, 64}, {16, 128}}};
+static int nidx(int N) { return N == 1024 ? 0 : 1; }
 
 template <class Kern>
 static int prep(Kern k, size_t sm) {
@@ -479,14 +692,14 @@ static int prep(Kern k, size_t sm) {
     return PQCGPU_ECUDA;
 }
 // per-instance shared memory of the core kernel of op (0 keypair, 1 encaps, 2 decaps)
-static size_t smem_per_instance(int op) { return op == 0 ? 2 * PITCH * 2 + 128 : op == 1 ? 3 * PITCH * 2 : PITCH * 2; }
+static size_t smem_per_instance(int N, int op) {
+    const size_t pitch = N == 1024 ? Nh<1024>::PITCH : Nh<512>::PITCH;
+    return op == 0 ? 2 * pitch * 2 + 128 : op == 1 ? 3 * pitch * 2 : pitch * 2;
+}
 
-}  // namespace newhope
-
-using namespace newhope;
-
-int newhope_init_constants() {
-    const long q = Q, g = 7, mont = (1L << 18) % q;
+// twiddle tables of the n-point transform (formulas of NewHope_NIST_GPU/precomp.cu:27-29)
+static void make_tables(int n, int logn, long g, uint16_t *gb, uint16_t *oi, uint16_t *gi) {
+    const long q = Q, mont = (1L << 18) % q;
     auto pw = [&](long b, long e) {
         long r = 1;
         b %= q;
@@ -497,69 +710,108 @@ int newhope_init_constants() {
         }
         return r;
     };
-    const long ginv = pw(g, q - 2), ninv = pw(N, q - 2);
-    static uint16_t gb[N], oi[N / 2], gi[N];
-    auto brv = [](int i) { int r = 0; for (int b = 0; b < 10; b++) r |= ((i >> b) & 1) << (9 - b); return r; };
-    for (int i = 0; i < N; i++) gb[i] = (uint16_t)(pw(g, brv(i)) * mont % q);
-    for (int i = 0; i < N / 2; i++) oi[i] = (uint16_t)(pw(ginv, 2L * brv(2 * i)) * mont % q);
-    for (int i = 0; i < N; i++) gi[i] = (uint16_t)(pw(ginv, i) * ninv % q * mont % q);
+    const long ginv = pw(g, q - 2), ninv = pw(n, q - 2);
+    auto brv = [&](int i) {
+        int r = 0;
+        for (int b = 0; b < logn; b++) r |= ((i >> b) & 1) << (logn - 1 - b);
+        return r;
+    };
+    for (int i = 0; i < n; i++) gb[i] = (uint16_t)(pw(g, brv(i)) * mont % q);
+    for (int i = 0; i < n / 2; i++) oi[i] = (uint16_t)(pw(ginv, 2L * brv(2 * i)) * mont % q);
+    for (int i = 0; i < n; i++) gi[i] = (uint16_t)(pw(ginv, i) * ninv % q * mont % q);
+}
+
+}  // namespace newhope
+
+using namespace newhope;
+
+int newhope_init_constants() {
+    static uint16_t gb[1024], oi[512], gi[1024], gb5[512], oi5[256], gi5[512];
+    make_tables(1024, 10, 7, gb, oi, gi);
+    make_tables(512, 9, 10968, gb5, oi5, gi5);
     uint2 rc[24];
     keccak_rc_host(rc);
     if (cudaMemcpyToSymbol(c_keccak_rc, rc, sizeof rc) != cudaSuccess) return PQCGPU_ECUDA;
     if (cudaMemcpyToSymbol(d_gammas_bitrev, gb, sizeof gb) != cudaSuccess) return PQCGPU_ECUDA;
     if (cudaMemcpyToSymbol(d_omegas_inv_bitrev, oi, sizeof oi) != cudaSuccess) return PQCGPU_ECUDA;
     if (cudaMemcpyToSymbol(d_gammas_inv, gi, sizeof gi) != cudaSuccess) return PQCGPU_ECUDA;
+    if (cudaMemcpyToSymbol(d_gammas_bitrev512, gb5, sizeof gb5) != cudaSuccess) return PQCGPU_ECUDA;
+    if (cudaMemcpyToSymbol(d_omegas_inv_bitrev512, oi5, sizeof oi5) != cudaSuccess) return PQCGPU_ECUDA;
+    if (cudaMemcpyToSymbol(d_gammas_inv512, gi5, sizeof gi5) != cudaSuccess) return PQCGPU_ECUDA;
     return PQCGPU_OK;
 }
 
-int newhope_set_shape(int op, int ni, int threads) {
-    if (op < 0 || op > 2 || ni < 1 || ni > 64 || threads < 32 || threads > 256 || threads % 32) return PQCGPU_EINVAL;
-    if ((size_t)ni * smem_per_instance(op) > MAX_SMEM_PER_CTA) return PQCGPU_EINVAL;
-    g_shape[op][0] = ni;
-    g_shape[op][1] = threads;
+int newhope_set_shape(int N, int op, int ni, int threads) {
+    if ((N != 1024 && N != 512) || op < 0 || op > 2 || ni < 1 || ni > 64 || threads < 32 || threads > 256 || threads % 32)
+        return PQCGPU_EINVAL;
+    if ((size_t)ni * smem_per_instance(N, op) > MAX_SMEM_PER_CTA) return PQCGPU_EINVAL;
+    g_shape[nidx(N)][op][0] = ni;
+    g_shape[nidx(N)][op][1] = threads;
     return PQCGPU_OK;
 }
 
-int newhope_get_shape(int op, int *ni, int *threads) {
-    if (op < 0 || op > 2) return PQCGPU_EINVAL;
-    *ni = g_shape[op][0];
-    *threads = g_shape[op][1];
+int newhope_get_shape(int N, int op, int *ni, int *threads) {
+    if ((N != 1024 && N != 512) || op < 0 || op > 2) return PQCGPU_EINVAL;
+    *ni = g_shape[nidx(N)][op][0];
+    *threads = g_shape[nidx(N)][op][1];
     return PQCGPU_OK;
 }
 
-int newhope_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st) {
-    const int NI = g_shape[0][0], NT = g_shape[0][1];
-    const size_t sm = (size_t)NI * smem_per_instance(0);
-    if (prep(nh_kp_core, sm)) return PQCGPU_ECUDA;
+template <int N>
+static int keypair_n(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st) {
+    const int NI = g_shape[nidx(N)][0][0], NT = g_shape[nidx(N)][0][1];
+    const size_t sm = (size_t)NI * smem_per_instance(N, 0);
+    if (prep(nh_kp_core<N>, sm)) return PQCGPU_ECUDA;
     KpArgs a{n, pk, sk, seed, seed_stride};
-    PQC_LAUNCH(st, "nh_kp_core", 1024, 0, nh_kp_core<<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
+    PQC_LAUNCH(st, "nh_kp_core", N, 0, nh_kp_core<N><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
-// kem: coins 32 B per instance -> (m, coin) via the prologue into scratch (64 B / instance), ss
-int newhope_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
-                    uint8_t *scratch, int kem, cudaStream_t st) {
-    const int NI = g_shape[1][0], NT = g_shape[1][1];
-    const size_t sm = (size_t)NI * smem_per_instance(1);
-    if (prep(nh_enc_core, sm)) return PQCGPU_ECUDA;
+template <int N>
+static int enc_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
+                 uint8_t *scratch, int kem, cudaStream_t st) {
+    const int NI = g_shape[nidx(N)][1][0], NT = g_shape[nidx(N)][1][1];
+    const size_t sm = (size_t)NI * smem_per_instance(N, 1);
+    if (prep(nh_enc_core<N>, sm)) return PQCGPU_ECUDA;
     EncArgs a{n, ct, pk, m, coins, 32, 32};
     if (kem) {
-        PQC_LAUNCH(st, "nh_enc_hash_pre", 1024, 0, nh_enc_hash_pre<<<(n + 127) / 128, 128, 0, st>>>(n, coins, scratch, ss));
+        PQC_LAUNCH(st, "nh_enc_hash_pre", N, 0, nh_enc_hash_pre<<<(n + 127) / 128, 128, 0, st>>>(n, coins, scratch, ss));
         a.m = scratch;
         a.coin = scratch + 32;
         a.m_stride = a.coin_stride = 64;
     }
-    PQC_LAUNCH(st, "nh_enc_core", 1024, 0, nh_enc_core<<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
+    PQC_LAUNCH(st, "nh_enc_core", N, 0, nh_enc_core<N><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
-int newhope_dec_dev(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st) {
-    const int NI = g_shape[2][0], NT = g_shape[2][1];
-    const size_t sm = (size_t)NI * smem_per_instance(2);
-    if (prep(nh_dec_core, sm)) return PQCGPU_ECUDA;
+template <int N>
+static int dec_n(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st) {
+    const int NI = g_shape[nidx(N)][2][0], NT = g_shape[nidx(N)][2][1];
+    const size_t sm = (size_t)NI * smem_per_instance(N, 2);
+    if (prep(nh_dec_core<N>, sm)) return PQCGPU_ECUDA;
     DecArgs d{n, out, ct, sk, kem};
-    PQC_LAUNCH(st, "nh_dec_core", 1024, 0, nh_dec_core<<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));
+    PQC_LAUNCH(st, "nh_dec_core", N, 0, nh_dec_core<N><<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
+int newhope_keypair_dev(int N, int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st) {
+    if (N == 1024) return keypair_n<1024>(n, pk, sk, seed, seed_stride, st);
+    if (N == 512) return keypair_n<512>(n, pk, sk, seed, seed_stride, st);
+    return PQCGPU_EINVAL;
+}
+
+// kem: coins 32 B per instance -> (m, coin) via the prologue into scratch (64 B / instance), ss
+int newhope_enc_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
+                    uint8_t *scratch, int kem, cudaStream_t st) {
+    if (N == 1024) return enc_n<1024>(n, ct, ss, pk, m, coins, scratch, kem, st);
+    if (N == 512) return enc_n<512>(n, ct, ss, pk, m, coins, scratch, kem, st);
+    return PQCGPU_EINVAL;
+}
+
+int newhope_dec_dev(int N, int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st) {
+    if (N == 1024) return dec_n<1024>(n, out, ct, sk, kem, st);
+    if (N == 512) return dec_n<512>(n, out, ct, sk, kem, st);
+    return PQCGPU_EINVAL;
 }
 
 }  // namespace pqc

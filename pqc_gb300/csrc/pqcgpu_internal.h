@@ -87,16 +87,16 @@ int kyber_enc_dev(int variant, int k, int n, uint8_t *ct, uint8_t *ss, const uin
 int kyber_dec_dev(int variant, int k, int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch,
                   int kem, int plain, cudaStream_t st);
 
-// ---- NewHope-1024 (newhope.cu) ----
+// ---- NewHope-1024 and NewHope-512 (newhope.cu); N = 1024 or 512 coefficients ----
 int newhope_init_constants();
-int newhope_set_shape(int op, int ni, int threads);
-int newhope_get_shape(int op, int *ni, int *threads);
-int newhope_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st);
+int newhope_set_shape(int N, int op, int ni, int threads);
+int newhope_get_shape(int N, int op, int *ni, int *threads);
+int newhope_keypair_dev(int N, int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st);
 // kem=1: coins 32 B/instance, scratch >= 64 B/instance, ss written; kem=0: CPA with m and coins
-int newhope_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
+int newhope_enc_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
                     uint8_t *scratch, int kem, cudaStream_t st);
 // kem=1: out = ss (32 B); kem=0: out = message
-int newhope_dec_dev(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st);
+int newhope_dec_dev(int N, int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st);
 
 // ---- FrodoKEM-976 (frodo.cu) ----
 int frodo_init_constants();

@@ -23,7 +23,7 @@ from . import _lib, kem
 
 ALG_NAMES = {
     "kyber512": "Kyber512", "kyber768": "Kyber768", "kyber1024": "Kyber1024",
-    "kyber1024r2": "Kyber1024-round2", "newhope1024": "NewHope1024-CPAKEM",
+    "kyber1024r2": "Kyber1024-round2", "newhope1024": "NewHope1024-CPAKEM", "newhope512": "NewHope512-CPAKEM",
     "frodo976": "FrodoKEM-976-SHAKE", "mlkem512": "ML-KEM-512", "mlkem768": "ML-KEM-768",
     "mlkem1024": "ML-KEM-1024",
 }

@@ -10,7 +10,7 @@ import json
 from . import _lib
 
 ALGS = {"kyber512": 0, "kyber768": 1, "kyber1024": 2, "kyber1024r2": 3, "newhope1024": 4, "frodo976": 5,
-        "mlkem512": 6, "mlkem768": 7, "mlkem1024": 8}
+        "mlkem512": 6, "mlkem768": 7, "mlkem1024": 8, "newhope512": 9}
 DEVICE_PTRS = 0x1
 PLAIN = 0x2
 STAGE_KERNELS = 0x4
@@ -25,6 +25,12 @@ def sizes(alg):
     v = [ctypes.c_size_t() for _ in range(6)]
     _lib.check(lib.pqcgpu_alg_sizes(alg_id(alg), *[ctypes.byref(x) for x in v]))
     return dict(zip(("pk", "sk", "ct", "ss", "kp_coins", "enc_coins"), (x.value for x in v)))
+
+
+def newhope_cpa_sizes(poly_n):
+    """NewHope CPA-PKE byte sizes for n = 1024 or 512 coefficients."""
+    pb = 14 * poly_n // 8
+    return {"pk": pb + 32, "sk": pb, "ct": pb + 3 * poly_n // 8}
 
 
 def kyber_cpa_sizes(variant, k):
@@ -172,20 +178,25 @@ class Context:
         _lib.check(self.lib.pqcgpu_kyber_indcpa_dec_batch(self.h, variant, k, n, m, ct, sk, flags))
         return m.raw
 
-    def newhope_cpa_keypair(self, n, seed, flags=0):
-        pk = ctypes.create_string_buffer(n * 1824)
-        sk = ctypes.create_string_buffer(n * 1792)
-        _lib.check(self.lib.pqcgpu_newhope_cpapke_keypair_batch(self.h, n, pk, sk, seed, flags))
+    # NewHope CPA-PKE; poly_n = 1024 (pqcgpu_newhope_*) or 512 (pqcgpu_newhope512_*)
+    def _nh(self, poly_n, what):
+        return getattr(self.lib, "pqcgpu_newhope%s_cpapke_%s_batch" % ("" if poly_n == 1024 else "512", what))
+
+    def newhope_cpa_keypair(self, n, seed, flags=0, poly_n=1024):
+        s = newhope_cpa_sizes(poly_n)
+        pk = ctypes.create_string_buffer(n * s["pk"])
+        sk = ctypes.create_string_buffer(n * s["sk"])
+        _lib.check(self._nh(poly_n, "keypair")(self.h, n, pk, sk, seed, flags))
         return pk.raw, sk.raw
 
-    def newhope_cpa_enc(self, n, m, pk, coin, flags=0):
-        ct = ctypes.create_string_buffer(n * 2176)
-        _lib.check(self.lib.pqcgpu_newhope_cpapke_enc_batch(self.h, n, ct, m, pk, coin, flags))
+    def newhope_cpa_enc(self, n, m, pk, coin, flags=0, poly_n=1024):
+        ct = ctypes.create_string_buffer(n * newhope_cpa_sizes(poly_n)["ct"])
+        _lib.check(self._nh(poly_n, "enc")(self.h, n, ct, m, pk, coin, flags))
         return ct.raw
 
-    def newhope_cpa_dec(self, n, ct, sk, flags=0):
+    def newhope_cpa_dec(self, n, ct, sk, flags=0, poly_n=1024):
         m = ctypes.create_string_buffer(n * 32)
-        _lib.check(self.lib.pqcgpu_newhope_cpapke_dec_batch(self.h, n, m, ct, sk, flags))
+        _lib.check(self._nh(poly_n, "dec")(self.h, n, m, ct, sk, flags))
         return m.raw
 
     # ---- device tensors (torch.uint8 on this context's device), asynchronous ----

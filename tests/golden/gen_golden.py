@@ -169,6 +169,7 @@ if __name__ == "__main__":
     restated("mlkem512", O.MLKEM512, 16, 0)
     restated("mlkem768", O.MLKEM768, 16, 0)
     restated("mlkem1024", O.MLKEM1024, 16, 0)
-    for name in ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976", "mlkem512", "mlkem768", "mlkem1024"):
+    for name in ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976", "mlkem512", "mlkem768", "mlkem1024",
+                 "newhope512"):
         kat_rsp(name, O.ALG_NAMES[name], 1 if name == "frodo976" else 3)
     print("fixtures written to", HERE)

@@ -1,5 +1,6 @@
-"""NewHope-1024 on the GPU through the C ABI: CPA-PKE against the reference's own golden vectors
-and the oracle, CPA-KEM against the oracle."""
+"""NewHope-1024 and NewHope-512 on the GPU through the C ABI: CPA-PKE against the reference's own
+golden vectors (n = 512: the reference built with NEWHOPE_N=512) and the oracle, CPA-KEM against the
+oracle."""
 import hashlib
 
 import pytest
@@ -8,6 +9,8 @@ from conftest import load_golden
 from pqc_gb300 import drbg
 
 pytestmark = pytest.mark.gpu
+
+ALG = {1024: "newhope1024", 512: "newhope512"}
 
 
 def sha(b):
@@ -26,39 +29,48 @@ def ctx():
     c.close()
 
 
-def test_cpa_matches_reference_vectors(ctx):
-    g = load_golden("ref_newhope1024_cpa.json")
+@pytest.mark.parametrize("poly_n", [1024, 512])
+def test_cpa_matches_reference_vectors(ctx, poly_n):
+    from pqc_gb300.kem import newhope_cpa_sizes
+    s = newhope_cpa_sizes(poly_n)
+    g = load_golden("ref_newhope%d_cpa.json" % poly_n)
     n = g["n"]
     seed, m, coins = (bytes.fromhex(g[x]) for x in ("seed", "m", "coins"))
-    pk, sk = ctx.newhope_cpa_keypair(n, seed)
-    assert [sha(x) for x in split(pk, 1824)] == g["pk_sha256"]
-    assert [sha(x) for x in split(sk, 1792)] == g["sk_sha256"]
-    ct = ctx.newhope_cpa_enc(n, m, pk, coins)
-    assert [sha(x) for x in split(ct, 2176)] == g["ct_sha256"]
-    assert ctx.newhope_cpa_dec(n, ct, sk).hex() == g["m_dec"]
+    pk, sk = ctx.newhope_cpa_keypair(n, seed, poly_n=poly_n)
+    assert [sha(x) for x in split(pk, s["pk"])] == g["pk_sha256"]
+    assert [sha(x) for x in split(sk, s["sk"])] == g["sk_sha256"]
+    ct = ctx.newhope_cpa_enc(n, m, pk, coins, poly_n=poly_n)
+    assert [sha(x) for x in split(ct, s["ct"])] == g["ct_sha256"]
+    assert ctx.newhope_cpa_dec(n, ct, sk, poly_n=poly_n).hex() == g["m_dec"]
 
 
+@pytest.mark.parametrize("poly_n", [1024, 512])
 @pytest.mark.parametrize("n", [1, 5, 33, 257])
-def test_cpa_matches_oracle(ctx, oracle, n):
-    seed = drbg.seed48(500 + n)
+def test_cpa_matches_oracle(ctx, oracle, n, poly_n):
+    from pqc_gb300.kem import newhope_cpa_sizes
+    s = newhope_cpa_sizes(poly_n)
+    P, S, C = s["pk"], s["sk"], s["ct"]
+    seed = drbg.seed48(500 + n + poly_n)
     d = drbg.stream(seed, b"d", 32 * n)
     m = drbg.stream(seed, b"m", 32 * n)
     coins = drbg.stream(seed, b"coins", 32 * n)
-    pk, sk = ctx.newhope_cpa_keypair(n, d)
-    ct = ctx.newhope_cpa_enc(n, m, pk, coins)
+    pk, sk = ctx.newhope_cpa_keypair(n, d, poly_n=poly_n)
+    ct = ctx.newhope_cpa_enc(n, m, pk, coins, poly_n=poly_n)
     for x in range(n):
-        opk, osk = oracle.newhope_cpapke_keypair(d[32 * x:32 * x + 32])
-        assert pk[1824 * x:1824 * (x + 1)] == opk, x
-        assert sk[1792 * x:1792 * (x + 1)] == osk, x
-        assert ct[2176 * x:2176 * (x + 1)] == oracle.newhope_cpapke_enc(m[32 * x:32 * x + 32], opk, coins[32 * x:32 * x + 32]), x
-    assert ctx.newhope_cpa_dec(n, ct, sk) == m
+        opk, osk = oracle.newhope_cpapke_keypair(d[32 * x:32 * x + 32], poly_n)
+        assert pk[P * x:P * (x + 1)] == opk, x
+        assert sk[S * x:S * (x + 1)] == osk, x
+        oct_ = oracle.newhope_cpapke_enc(m[32 * x:32 * x + 32], opk, coins[32 * x:32 * x + 32], poly_n)
+        assert ct[C * x:C * (x + 1)] == oct_, x
+    assert ctx.newhope_cpa_dec(n, ct, sk, poly_n=poly_n) == m
 
 
+@pytest.mark.parametrize("poly_n", [1024, 512])
 @pytest.mark.parametrize("n", [1, 63, 1000])
-def test_kem_matches_oracle(ctx, oracle, n):
-    alg = "newhope1024"
-    a = oracle.NEWHOPE1024
-    seed = drbg.seed48(600 + n)
+def test_kem_matches_oracle(ctx, oracle, n, poly_n):
+    alg = ALG[poly_n]
+    a = oracle.ALG_NAMES[alg]
+    seed = drbg.seed48(600 + n + poly_n)
     kc = drbg.stream(seed, b"kp", n * 32)
     ec = drbg.stream(seed, b"enc", n * 32)
     pk, sk = ctx.keypair(alg, n, kc)
@@ -72,13 +84,48 @@ def test_kem_matches_oracle(ctx, oracle, n):
     assert ctx.dec(alg, n, bytes(bad), sk) == oracle.batch_dec(a, n, bytes(bad), sk)
 
 
-def test_restated_fixture(ctx):
+@pytest.mark.parametrize("poly_n", [1024, 512])
+def test_restated_fixture(ctx, poly_n):
     from pqc_gb300 import kem
-    g = load_golden("restated_newhope1024.json")
+    alg = ALG[poly_n]
+    s = kem.sizes(alg)
+    g = load_golden("restated_%s.json" % alg)
     n = g["n"]
     seed = drbg.seed48(g["drbg_seed"])
-    pk, sk = ctx.keypair("newhope1024", n, drbg.stream(seed, b"kp", n * 32))
-    ct, ss = ctx.enc("newhope1024", n, pk, drbg.stream(seed, b"enc", n * 32))
-    assert [sha(x) for x in split(pk, 1824)] == g["pk_sha256"]
-    assert [sha(x) for x in split(ct, 2176)] == g["ct_sha256"]
+    pk, sk = ctx.keypair(alg, n, drbg.stream(seed, b"kp", n * 32))
+    ct, ss = ctx.enc(alg, n, pk, drbg.stream(seed, b"enc", n * 32))
+    assert [sha(x) for x in split(pk, s["pk"])] == g["pk_sha256"]
+    assert [sha(x) for x in split(ct, s["ct"])] == g["ct_sha256"]
     assert ss.hex() == g["ss"]
+
+
+@pytest.mark.parametrize("shape", [(1, 32), (3, 96), (7, 64), (32, 256)])
+def test_newhope512_launch_shapes_match_oracle(ctx, oracle, shape):
+    """Odd and even instance counts per CTA (the half-warp NTT pairs two instances per warp and idles
+    a half when the count is odd) give the same bytes at every shape."""
+    import ctypes
+
+    from pqc_gb300 import _lib, kem
+    lib = _lib.load()
+    alg = "newhope512"
+    a = oracle.ALG_NAMES[alg]
+    n = 45
+    seed = drbg.seed48(77)
+    kc = drbg.stream(seed, b"kp", n * 32)
+    ec = drbg.stream(seed, b"enc", n * 32)
+    opk, osk = oracle.batch_keypair(a, n, kc)
+    oct_, oss = oracle.batch_enc(a, n, opk, ec)
+    saved = []
+    for op in range(3):
+        ni, thr = ctypes.c_int(), ctypes.c_int()
+        assert lib.pqcgpu_get_launch_shape(kem.alg_id(alg), op, ctypes.byref(ni), ctypes.byref(thr)) == 0
+        saved.append((ni.value, thr.value))
+    try:
+        for op in range(3):
+            assert lib.pqcgpu_set_launch_shape(kem.alg_id(alg), op, *shape) == 0
+        assert ctx.keypair(alg, n, kc) == (opk, osk)
+        assert ctx.enc(alg, n, opk, ec) == (oct_, oss)
+        assert ctx.dec(alg, n, oct_, osk) == oss
+    finally:
+        for op in range(3):
+            lib.pqcgpu_set_launch_shape(kem.alg_id(alg), op, *saved[op])
