@@ -58,7 +58,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--slots", type=int, default=12, help="serving: batches in flight (worker threads)")
     p.add_argument("--config", default=None,
-                   choices=["kyber512", "newhope1024", "frodo976", "mixed", "serving", "refgpu", "latency", "all"],
+                   choices=["kyber512", "newhope1024", "frodo976", "newhope512", "mixed", "serving", "refgpu", "latency",
+                            "all"],
                    help="measure another configuration (extra JSON lines) instead of the headline")
     return p.parse_args()
 
@@ -226,8 +227,8 @@ def run_configs(args):
     ctx = kem.Context(0)
     st = torch.cuda.ExternalStream(ctx.stream, device=dev)
     up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
-    which = (["kyber512", "newhope1024", "frodo976", "mixed", "serving", "refgpu", "latency"] if args.config == "all"
-             else [args.config])
+    which = (["kyber512", "newhope1024", "frodo976", "newhope512", "mixed", "serving", "refgpu", "latency"]
+             if args.config == "all" else [args.config])
 
     def timed(fn, reps):
         fn()
@@ -241,9 +242,9 @@ def run_configs(args):
         return e0.elapsed_time(e1) / reps
 
     for cfg in which:
-        if cfg in ("kyber512", "newhope1024", "frodo976"):
+        if cfg in ("kyber512", "newhope1024", "frodo976", "newhope512"):
             alg = cfg
-            n = {"kyber512": 65536, "newhope1024": 16384, "frodo976": 2048}[cfg]
+            n = {"kyber512": 65536, "newhope1024": 16384, "frodo976": 2048, "newhope512": 16384}[cfg]
             s = kem.sizes(alg)
             seed = drbg.seed48(5)
             kc, ec = up(drbg.stream(seed, b"kp", n * s["kp_coins"])), up(drbg.stream(seed, b"enc", n * s["enc_coins"]))
@@ -347,7 +348,7 @@ def run_latency(ctx, dev, up, reps=50):
     from pqc_gb300 import drbg, kem
     st = torch.cuda.ExternalStream(ctx.stream, device=dev)
     out = {}
-    for alg in ("kyber512", "kyber768", "kyber1024", "mlkem768", "newhope1024", "frodo976"):
+    for alg in ("kyber512", "kyber768", "kyber1024", "mlkem768", "newhope1024", "newhope512", "frodo976"):
         s = kem.sizes(alg)
         seed = drbg.seed48(77)
         kc, ec = up(drbg.stream(seed, b"kp", s["kp_coins"])), up(drbg.stream(seed, b"enc", s["enc_coins"]))

@@ -17,7 +17,7 @@ import os
 from . import _lib, drbg, kem
 
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "tuning.json")
-TUNABLE = ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976")
+TUNABLE = ("kyber512", "kyber768", "kyber1024", "newhope1024", "newhope512", "frodo976")
 
 
 def candidates(alg, op):
@@ -38,6 +38,8 @@ def candidates(alg, op):
         if op == 0:
             return [(0, thr) for thr in (64, 128, 256)]
         return [(parts, thr) for parts in (1, 2, 4, 8, 16) for thr in (128, 256)]
+    if alg == "newhope512":  # half the shared memory per instance of NewHope-1024
+        return [(ni, thr) for ni in (2, 4, 8, 12, 16, 24, 32) for thr in (32, 64, 128, 256)]
     return [(ni, thr) for ni in (1, 2, 4, 8) for thr in (64, 128, 256) if thr // 32 >= 1]
 
 
@@ -57,7 +59,8 @@ def tune(batch=65536, algs=TUNABLE, reps=3, device=0, log=print):
     result = {}
     for alg in algs:
         s = kem.sizes(alg)
-        n = {"newhope1024": min(batch, 16384), "frodo976": min(batch, 256)}.get(alg, batch)
+        n = {"newhope1024": min(batch, 16384), "newhope512": min(batch, 16384),
+             "frodo976": min(batch, 256)}.get(alg, batch)
         seed = drbg.seed48(99)
         up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
         kc = up(drbg.stream(seed, b"kp", n * s["kp_coins"]))

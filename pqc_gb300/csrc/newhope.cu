@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(128) nh_enc_hash_pre(int n, const uint8_t *coi
 }
 
 // [n index: 0 = 1024, 1 = 512][op] = {instances per CTA, threads}
-static int g_shape[2][3][2] = {{{8, 128}, {4, 64}, {4, 128}}, {{16, 128}, {8, 64}, {16, 128}}};
+static int g_shape[2][3][2] = {{{8, 128}, {4, 64}, {4, 128}}, {{16, 128}, {16, 128}, {4, 64}}};
 static int nidx(int N) { return N == 1024 ? 0 : 1; }
 
 template <class Kern>
