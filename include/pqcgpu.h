@@ -50,7 +50,9 @@ typedef enum {
     PQCGPU_MLKEM768 = 7,     /*   rejection key J(z || c); same sizes as the round-3 sets.  The FIPS 203 */
     PQCGPU_MLKEM1024 = 8,    /*   input checks (ek modulus, dk hash) are left to the caller. */
     PQCGPU_NEWHOPE512 = 9,   /* NewHope512-CPAKEM (NewHope_NIST_GPU built with NEWHOPE_N = 512) */
-    PQCGPU_NUM_ALGS = 10
+    PQCGPU_FRODO640 = 10,    /* FrodoKEM-640, SHAKE: the FrodoKEM-976 flow with the 640 parameter set */
+    PQCGPU_FRODO1344 = 11,   /* FrodoKEM-1344, SHAKE: the same with the 1344 parameter set */
+    PQCGPU_NUM_ALGS = 12
 } pqcgpu_alg;
 
 typedef enum {
@@ -298,6 +300,12 @@ int pqcgpu_newhope512_crypto_kem_dec(unsigned char *ss, const unsigned char *ct,
 int pqcgpu_frodo976_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
 int pqcgpu_frodo976_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
 int pqcgpu_frodo976_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+int pqcgpu_frodo640_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+int pqcgpu_frodo640_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+int pqcgpu_frodo640_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
+int pqcgpu_frodo1344_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
+int pqcgpu_frodo1344_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
+int pqcgpu_frodo1344_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);
 int pqcgpu_mlkem512_crypto_kem_keypair(unsigned char *pk, unsigned char *sk);
 int pqcgpu_mlkem512_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk);
 int pqcgpu_mlkem512_crypto_kem_dec(unsigned char *ss, const unsigned char *ct, const unsigned char *sk);

@@ -27,6 +27,12 @@ int oracle_alg_sizes(int alg, size_t *pk, size_t *sk, size_t *ct, size_t *ss, si
     case 9:
         a = 928; b = 896; c = 1088; e = 32;
         break;
+    case 10:
+        a = 9616; b = 19888; c = 9720; d = 16; e = 48; f = 16;
+        break;
+    case 11:
+        a = 21520; b = 43088; c = 21632; d = 32; e = 80; f = 32;
+        break;
     default:
         return -1;
     }
@@ -44,6 +50,8 @@ static int one_keypair(int alg, uint8_t *pk, uint8_t *sk, const uint8_t *coins) 
     if (alg == 3) return oracle_kyber_kem_keypair(2, 4, pk, sk, coins);
     if (alg == 4) return oracle_newhope_kem_keypair(pk, sk, coins);
     if (alg == 9) return oracle_newhope512_kem_keypair(pk, sk, coins);
+    if (alg == 10) return oracle_frodo640_kem_keypair(pk, sk, coins);
+    if (alg == 11) return oracle_frodo1344_kem_keypair(pk, sk, coins);
     if (alg >= 6) return oracle_mlkem_keypair(alg - 4, pk, sk, coins);
     return oracle_frodo_kem_keypair(pk, sk, coins);
 }
@@ -52,6 +60,8 @@ static int one_enc(int alg, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const u
     if (alg == 3) return oracle_kyber_kem_enc(2, 4, ct, ss, pk, coins);
     if (alg == 4) return oracle_newhope_kem_enc(ct, ss, pk, coins);
     if (alg == 9) return oracle_newhope512_kem_enc(ct, ss, pk, coins);
+    if (alg == 10) return oracle_frodo640_kem_enc(ct, ss, pk, coins);
+    if (alg == 11) return oracle_frodo1344_kem_enc(ct, ss, pk, coins);
     if (alg >= 6) return oracle_mlkem_enc(alg - 4, ct, ss, pk, coins);
     return oracle_frodo_kem_enc(ct, ss, pk, coins);
 }
@@ -60,6 +70,8 @@ static int one_dec(int alg, uint8_t *ss, const uint8_t *ct, const uint8_t *sk) {
     if (alg == 3) return oracle_kyber_kem_dec(2, 4, ss, ct, sk);
     if (alg == 4) return oracle_newhope_kem_dec(ss, ct, sk);
     if (alg == 9) return oracle_newhope512_kem_dec(ss, ct, sk);
+    if (alg == 10) return oracle_frodo640_kem_dec(ss, ct, sk);
+    if (alg == 11) return oracle_frodo1344_kem_dec(ss, ct, sk);
     if (alg >= 6) return oracle_mlkem_dec(alg - 4, ss, ct, sk);
     return oracle_frodo_kem_dec(ss, ct, sk);
 }

@@ -71,14 +71,23 @@ int oracle_newhope512_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t coins[
 int oracle_newhope512_kem_enc(uint8_t *ct, uint8_t ss[32], const uint8_t *pk, const uint8_t coins[32]);
 int oracle_newhope512_kem_dec(uint8_t ss[32], const uint8_t *ct, const uint8_t *sk);
 
-/* ---- FrodoKEM-976 (SHAKE) -------------------------------------------------------------- */
-int oracle_frodo_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t coins[64]);
-int oracle_frodo_kem_enc(uint8_t *ct, uint8_t ss[24], const uint8_t *pk, const uint8_t coins[24]);
-int oracle_frodo_kem_dec(uint8_t ss[24], const uint8_t *ct, const uint8_t *sk);
+/* ---- FrodoKEM-976 (oracle_frodo_*), -640 and -1344 (SHAKE) ------------------------------
+ * keypair coins = s || seedSE || z (2 ss + 16 bytes), encapsulation coins = mu (ss bytes), with
+ * ss = 24 / 16 / 32 bytes for n = 976 / 640 / 1344 */
+int oracle_frodo_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t *coins);
+int oracle_frodo_kem_enc(uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *coins);
+int oracle_frodo_kem_dec(uint8_t *ss, const uint8_t *ct, const uint8_t *sk);
+int oracle_frodo640_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t *coins);
+int oracle_frodo640_kem_enc(uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *coins);
+int oracle_frodo640_kem_dec(uint8_t *ss, const uint8_t *ct, const uint8_t *sk);
+int oracle_frodo1344_kem_keypair(uint8_t *pk, uint8_t *sk, const uint8_t *coins);
+int oracle_frodo1344_kem_enc(uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *coins);
+int oracle_frodo1344_kem_dec(uint8_t *ss, const uint8_t *ct, const uint8_t *sk);
 
 /* ---- Batched drivers (OpenMP over instances; nthreads <= 0 means all cores) -------------
  * alg: 0..2 = Kyber-512/768/1024 (round 3), 3 = Kyber-1024 round 2, 4 = NewHope-1024 CPA-KEM,
- * 5 = FrodoKEM-976, 6..8 = ML-KEM-512/768/1024 (FIPS 203), 9 = NewHope-512 CPA-KEM.
+ * 5 = FrodoKEM-976, 6..8 = ML-KEM-512/768/1024 (FIPS 203), 9 = NewHope-512 CPA-KEM,
+ * 10 = FrodoKEM-640, 11 = FrodoKEM-1344.
  * Buffers are instance-major, each instance at a fixed stride. */
 int oracle_batch_keypair(int alg, size_t n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int nthreads);
 int oracle_batch_enc(int alg, size_t n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *coins,

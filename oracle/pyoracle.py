@@ -13,9 +13,11 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 # alg ids shared with the batched drivers in batch.c
 KYBER512, KYBER768, KYBER1024, KYBER1024_R2, NEWHOPE1024, FRODO976 = range(6)
 MLKEM512, MLKEM768, MLKEM1024 = 6, 7, 8
-NEWHOPE512 = 9
+NEWHOPE512, FRODO640, FRODO1344 = 9, 10, 11
 ALG_NAMES = {
     "newhope512": NEWHOPE512,
+    "frodo640": FRODO640,
+    "frodo1344": FRODO1344,
     "mlkem512": MLKEM512,
     "mlkem768": MLKEM768,
     "mlkem1024": MLKEM1024,

@@ -61,7 +61,7 @@ SIGNATURES = {
     "pqcgpu_nist_coins": (_int, [_int, _int, _u8p]),
 }
 for _alg in ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976", "mlkem512", "mlkem768", "mlkem1024",
-             "newhope512"):
+             "newhope512", "frodo640", "frodo1344"):
     SIGNATURES["pqcgpu_%s_crypto_kem_keypair" % _alg] = (_int, [_u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_enc" % _alg] = (_int, [_u8p, _u8p, _u8p])
     SIGNATURES["pqcgpu_%s_crypto_kem_dec" % _alg] = (_int, [_u8p, _u8p, _u8p])

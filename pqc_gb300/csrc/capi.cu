@@ -192,6 +192,8 @@ bool alg_info(int alg, AlgInfo *a) {
     case PQCGPU_NEWHOPE1024: *a = {1824, 1792, 2176, 32, 32, 32}; return true;
     case PQCGPU_NEWHOPE512: *a = {928, 896, 1088, 32, 32, 32}; return true;
     case PQCGPU_FRODO976: *a = {15632, 31296, 15744, 24, 64, 24}; return true;
+    case PQCGPU_FRODO640: *a = {9616, 19888, 9720, 16, 48, 16}; return true;
+    case PQCGPU_FRODO1344: *a = {21520, 43088, 21632, 32, 80, 32}; return true;
     default: return false;
     }
 }
@@ -211,6 +213,9 @@ bool kyber_alg(int alg, int *variant, int *k) {
 namespace pqc {
 // KEM layer of a Kyber-family algorithm: 1 = Fujisaki-Okamoto as in rounds 2 / 3, 2 = FIPS 203
 int kyber_kem_mode(int alg) { return (alg >= PQCGPU_MLKEM512 && alg <= PQCGPU_MLKEM1024) ? 2 : 1; }
+int frodo_n(int alg) {
+    return alg == PQCGPU_FRODO976 ? 976 : alg == PQCGPU_FRODO640 ? 640 : alg == PQCGPU_FRODO1344 ? 1344 : 0;
+}
 }  // namespace pqc
 
 // ---------------------------------------------------------------------------------------------
@@ -647,7 +652,7 @@ size_t op_scratch_bytes(int alg, int op, int plain) {
     int variant, k;
     if (kyber_alg(alg, &variant, &k)) return kyber_scratch_bytes(k, op, plain);
     if (alg == PQCGPU_NEWHOPE1024 || alg == PQCGPU_NEWHOPE512) return op == 1 ? 64 : 0;
-    if (alg == PQCGPU_FRODO976) return frodo_scratch_bytes();
+    if (frodo_n(alg)) return frodo_scratch_bytes(frodo_n(alg));
     return 0;
 }
 int op_dev(int alg, int op, int n, const uint8_t *in0, const uint8_t *in1, uint8_t *out0, uint8_t *out1,
@@ -669,9 +674,10 @@ int op_dev(int alg, int op, int n, const uint8_t *in0, const uint8_t *in1, uint8
         if (op == 1) return newhope_enc_dev(N, n, out0, out1, in0, nullptr, in1, scr, 1, s);
         return newhope_dec_dev(N, n, out0, in0, in1, 1, s);
     }
-    if (op == 0) return frodo_keypair_dev(n, out0, out1, in0, (int)ai.kpc, scr, s);
-    if (op == 1) return frodo_enc_dev(n, out0, out1, in0, in1, scr, s);
-    return frodo_dec_dev(n, out0, in0, in1, scr, s);
+    const int fn = frodo_n(alg);
+    if (op == 0) return frodo_keypair_dev(fn, n, out0, out1, in0, (int)ai.kpc, scr, s);
+    if (op == 1) return frodo_enc_dev(fn, n, out0, out1, in0, in1, scr, s);
+    return frodo_dec_dev(fn, n, out0, in0, in1, scr, s);
 }
 // Per-instance byte sizes of the op's buffers (in0, in1, out0, out1; 0 = unused).
 void op_io_sizes(int alg, int op, size_t sz[4]) {
@@ -912,7 +918,7 @@ extern "C" int pqcgpu_set_launch_shape(pqcgpu_alg alg, int op, int ni, int threa
     if (kyber_alg(alg, &variant, &k)) rc = kyber_set_shape(op, k, ni, threads);
     else if (alg == PQCGPU_NEWHOPE1024) rc = newhope_set_shape(1024, op, ni, threads);
     else if (alg == PQCGPU_NEWHOPE512) rc = newhope_set_shape(512, op, ni, threads);
-    else if (alg == PQCGPU_FRODO976) rc = frodo_set_shape(op, ni, threads);
+    else if (frodo_n(alg)) rc = frodo_set_shape(op, ni, threads);
     else rc = PQCGPU_EUNSUPPORTED;
     return rc ? set_err(rc, "launch shape not accepted") : PQCGPU_OK;
 }
@@ -922,7 +928,7 @@ extern "C" int pqcgpu_get_launch_shape(pqcgpu_alg alg, int op, int *ni, int *thr
     if (kyber_alg(alg, &variant, &k)) return kyber_get_shape(op, k, ni, threads);
     if (alg == PQCGPU_NEWHOPE1024) return newhope_get_shape(1024, op, ni, threads);
     if (alg == PQCGPU_NEWHOPE512) return newhope_get_shape(512, op, ni, threads);
-    if (alg == PQCGPU_FRODO976) return frodo_get_shape(op, ni, threads);
+    if (frodo_n(alg)) return frodo_get_shape(op, ni, threads);
     return set_err(PQCGPU_EUNSUPPORTED, "no tunable launch shape for this algorithm");
 }
 
@@ -1143,14 +1149,14 @@ extern "C" int pqcgpu_nist_coins(pqcgpu_alg alg, int op, uint8_t *coins) {
 #define PQC_NIST(NAME, ALG)                                                                              \
     extern "C" int pqcgpu_##NAME##_crypto_kem_keypair(unsigned char *pk, unsigned char *sk) {             \
         pqcgpu_ctx *c = default_ctx();                                                                   \
-        uint8_t coins[64];                                                                               \
+        uint8_t coins[128]; /* >= every kp_coins / enc_coins size (at most 80) */                         \
         if (!c) return PQCGPU_ECUDA;                                                                     \
         if (int rc_ = pqcgpu_nist_coins(ALG, 0, coins)) return rc_;                                      \
         return pqcgpu_kem_keypair_batch(c, ALG, 1, pk, sk, coins, 0);                                    \
     }                                                                                                    \
     extern "C" int pqcgpu_##NAME##_crypto_kem_enc(unsigned char *ct, unsigned char *ss, const unsigned char *pk) { \
         pqcgpu_ctx *c = default_ctx();                                                                   \
-        uint8_t coins[64];                                                                               \
+        uint8_t coins[128]; /* >= every kp_coins / enc_coins size (at most 80) */                         \
         if (!c) return PQCGPU_ECUDA;                                                                     \
         if (int rc_ = pqcgpu_nist_coins(ALG, 1, coins)) return rc_;                                      \
         return pqcgpu_kem_enc_batch(c, ALG, 1, ct, ss, pk, coins, 0);                                    \
@@ -1168,3 +1174,5 @@ PQC_NIST(kyber1024, PQCGPU_KYBER1024)
 PQC_NIST(newhope1024, PQCGPU_NEWHOPE1024)
 PQC_NIST(newhope512, PQCGPU_NEWHOPE512)
 PQC_NIST(frodo976, PQCGPU_FRODO976)
+PQC_NIST(frodo640, PQCGPU_FRODO640)
+PQC_NIST(frodo1344, PQCGPU_FRODO1344)

@@ -1,10 +1,10 @@
-// Batched FrodoKEM-976 (SHAKE) for sm_103a.
+// Batched FrodoKEM-640 / 976 / 1344 (SHAKE) for sm_103a.
 //
 // Replaces crypto_kem_keypair_gpu / enc / dec (FrodoKEM_GPU/frodo976.cu:87-690: one instance per
 // call, A written to and re-read from HBM, host SHAKE for pk / ct) with, per operation:
 //   * a warp-per-instance kernel for the serial sponges -- the S/E noise stream
-//     (SHAKE256(0x5F / 0x96 || seedSE), 230-231 permutations), G1 = SHAKE256(pk) (115), G2 and
-//     the final F = SHAKE256(ct || k) (116) -- with the Keccak state spread over the warp to cut
+//     (SHAKE(0x5F / 0x96 || seedSE), 230-231 permutations for n = 976), G1 = SHAKE(pk) (115), G2
+//     and the final F = SHAKE(ct || k) (116) -- with the Keccak state spread over the warp to cut
 //     the latency of these chains, the noise sampled with the CDF table on the fly;
 //   * a core kernel that regenerates A row by row from SHAKE128(le16(i) || seedA) and multiplies
 //     it as it appears, so A (1.9 MB per key) never exists in HBM or whole in shared memory:
@@ -13,9 +13,14 @@
 //         round into shared memory, then the CTA contracts the staged 84 columns over its rows
 //         (exact mod 2^16 with uint32 multiply-accumulate) and adds the partial sums into the
 //         8 x 976 accumulator with shared-memory atomics;
-//   * codecs (16-bit big-endian pack, 3-bit key encode / decode) inside the same kernels.
+//   * codecs (log q-bit MSB-first pack, B-bit key encode / decode) inside the same kernels.
 // Host flow and arithmetic follow FrodoKEM_GPU/kem.c:13-214, frodo_macrify_reference.cu:55-360,
-// util.cu:18-113, noise.c:10-29 and the CDF table of frodo976.cu:21.
+// util.cu:18-113, noise.c:10-29 and the CDF table of frodo976.cu:21.  The reference builds only
+// n = 976 (FrodoKEM_GPU/params.h:17-30); FrodoKEM-640 and -1344 run the same flow with the other
+// parameter sets of the FrodoKEM specification: n, log q (15 for 640), B (2 / 3 / 4 encoded bits),
+// 16 / 24 / 32-byte seeds and keys, SHAKE128 (640) or SHAKE256 (976, 1344) for every hash and for
+// the noise stream, and their CDF tables.  Every value is computed mod 2^16 and reduced mod q when
+// packed, compared or decoded.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -25,26 +30,80 @@
 namespace pqc {
 namespace frodo {
 
-constexpr int N = 976, NB = 8;
-constexpr int PKB = 15632, SKB = 31296, CTB = 15744, SSB = 24, SEEDA = 16, MUB = 24;
-constexpr int C1B = 2 * N * NB;  // 15616: packed N x NBAR (or NBAR x N) matrix
-constexpr int ROW_BLOCKS = 12;   // 1952 bytes of SHAKE128 per row = 11 full blocks + 104 bytes
-// scratch per instance: noise (Sp 7808 + Ep 7808 + Epp 64 u16) + seeds (seedSE/k 48, mu 24, flag),
-// then the u32 accumulator of B' (8 x N) used when the rows of A are split over several CTAs
-constexpr int NOISE_U16 = 2 * N * NB + NB * NB;
-constexpr size_t GACC_OFF = (size_t)NOISE_U16 * 2 + 128;
-constexpr size_t SCRATCH = GACC_OFF + (size_t)NB * N * 4;
+constexpr int NB = 8, SEEDA = 16;
 
-static __constant__ uint16_t c_cdf[11];
+// Parameter set with n = N: LOGQ bits per value, B encoded bits, SSB = length of s, seedSE, k, pkh
+// and ss (= MUB, the length of mu), RATE = Keccak rate in 64-bit lanes of the hash (SHAKE128 for
+// n = 640, SHAKE256 otherwise), CDF table length.
+template <int N>
+struct FP {
+    static constexpr int LOGQ = N == 640 ? 15 : 16, B = N == 640 ? 2 : N == 976 ? 3 : 4;
+    static constexpr int SSB = 8 * B, MUB = 8 * B, NW = SSB / 8;
+    static constexpr int RATE = N == 640 ? SHAKE128_LANES : SHAKE256_LANES;
+    static constexpr int CDF_LEN = N == 640 ? 13 : N == 976 ? 11 : 7;
+    static constexpr uint32_t MASKQ = (1u << LOGQ) - 1;
+    static constexpr int C1B = LOGQ * N * NB / 8;   // packed N x NBAR (or NBAR x N) matrix
+    static constexpr int C2B = LOGQ * NB * NB / 8;  // packed NBAR x NBAR matrix
+    static constexpr int PKB = SEEDA + C1B, CTB = C1B + C2B, SKB = SSB + PKB + 2 * N * NB + SSB;
+    static constexpr int ROW_BLOCKS = (2 * N + 167) / 168;  // SHAKE128 blocks per row of A
+    // scratch per instance: noise (Sp, Ep: N x 8, Epp: 8 x 8 u16) + seeds (k at +0, mu at +32,
+    // fail flag at +64, the F key at +72), then the u32 accumulator of B' (8 x N) used when the
+    // rows of A are split over several CTAs
+    static constexpr int NOISE_U16 = 2 * N * NB + NB * NB;
+    static constexpr size_t GACC_OFF = (size_t)NOISE_U16 * 2 + 128;
+    static constexpr size_t SCRATCH = GACC_OFF + (size_t)NB * N * 4;
+};
+static_assert(FP<976>::PKB == 15632 && FP<976>::SKB == 31296 && FP<976>::CTB == 15744, "FrodoKEM-976 sizes");
+static_assert(FP<640>::PKB == 9616 && FP<640>::SKB == 19888 && FP<640>::CTB == 9720, "FrodoKEM-640 sizes");
+static_assert(FP<1344>::PKB == 21520 && FP<1344>::SKB == 43088 && FP<1344>::CTB == 21632, "FrodoKEM-1344 sizes");
+
+static __constant__ uint16_t c_cdf640[13], c_cdf976[11], c_cdf1344[7];
 
 // ---- helpers ---------------------------------------------------------------------------------
 // CDF sampler of one 16-bit value (noise.c:10-29)
+template <int N>
 __device__ __forceinline__ uint16_t cdf_sample(uint32_t r) {
+    const uint16_t *cdf = N == 640 ? c_cdf640 : N == 976 ? c_cdf976 : c_cdf1344;
     uint32_t sample = 0;
     const uint32_t prnd = (r & 0xffff) >> 1, sign = r & 1;
 #pragma unroll
-    for (int j = 0; j < 10; j++) sample += ((uint32_t)c_cdf[j] - prnd) >> 31 & 1;
+    for (int j = 0; j < FP<N>::CDF_LEN - 1; j++) sample += ((uint32_t)cdf[j] - prnd) >> 31 & 1;
     return (uint16_t)((((0u - sign) ^ sample) + sign) & 0xffff);
+}
+
+// Pack / unpack of 8 consecutive values (util.cu:18-113, MSB first): LOGQ bytes.  For LOGQ = 16
+// this is big-endian u16.
+template <int LOGQ>
+__device__ __forceinline__ void pack8(uint8_t *o, const uint32_t (&v)[8]) {
+    if (LOGQ == 16) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            o[2 * k] = (uint8_t)(v[k] >> 8);
+            o[2 * k + 1] = (uint8_t)v[k];
+        }
+    } else {
+        uint64_t hi = 0, lo = 0;  // 8 x LOGQ <= 128 bits, value 0 first (most significant)
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint64_t x = v[k] & ((1u << LOGQ) - 1);
+            hi = (hi << LOGQ) | (lo >> (64 - LOGQ));
+            lo = (lo << LOGQ) | x;
+        }
+        // 8 * LOGQ bits, left-aligned at bit 8*LOGQ - 1 of (hi:lo)
+#pragma unroll
+        for (int b = 0; b < LOGQ; b++) {
+            const int sh = 8 * (LOGQ - 1 - b);  // bit offset of byte b from the right
+            o[b] = (uint8_t)(sh >= 64 ? (hi >> (sh - 64)) : ((lo >> sh) | (sh > 0 ? (hi << (64 - sh)) : 0)));
+        }
+    }
+}
+// value k (0..7) of the 8-value group packed at p
+template <int LOGQ>
+__device__ __forceinline__ uint32_t unpack_at(const uint8_t *p, int k) {
+    if (LOGQ == 16) return ((uint32_t)p[2 * k] << 8) | p[2 * k + 1];
+    const int bit = LOGQ * k, byte = bit >> 3, off = bit & 7;  // MSB-first bit offset
+    const uint32_t w = ((uint32_t)p[byte] << 16) | ((uint32_t)p[byte + 1] << 8) | (byte + 2 < LOGQ ? p[byte + 2] : 0u);
+    return (w >> (24 - off - LOGQ)) & ((1u << LOGQ) - 1);
 }
 
 // SHAKE128 row generator for A: absorb le16(row) || seedA, squeeze block by block.
@@ -58,47 +117,57 @@ __device__ __forceinline__ void row_absorb(uint2 (&A)[25], int row, const uint2 
     A[SHAKE128_LANES - 1].y ^= 0x80000000u;
 }
 
-__device__ __forceinline__ uint32_t ld_be16(const uint8_t *p) { return ((uint32_t)p[0] << 8) | p[1]; }
+// element e of a packed matrix (8-value groups of LOGQ bytes)
+template <int LOGQ>
+__device__ __forceinline__ uint32_t ld_packed(const uint8_t *base, int e) {
+    return unpack_at<LOGQ>(base + (size_t)LOGQ * (e >> 3), e & 7);
+}
 
 // ---------------------------------------------------------------------------------------------
 // Serial sponges: one warp per instance (warp-cooperative Keccak, keccak.cuh)
 // ---------------------------------------------------------------------------------------------
-// Message lane m (0..3) of prefix || seed (25 bytes) followed by the SHAKE domain byte, where the
-// 24-byte seed is given as three little-endian 64-bit words.
-__device__ __forceinline__ uint2 prefixed_lane(int m, uint32_t prefix, uint64_t s0, uint64_t s1, uint64_t s2) {
-    uint64_t v;
-    if (m == 0) v = prefix | (s0 << 8);
-    else if (m == 1) v = (s0 >> 56) | (s1 << 8);
-    else if (m == 2) v = (s1 >> 56) | (s2 << 8);
-    else v = (s2 >> 56) | ((uint64_t)DOM_SHAKE << 8);
+// Message lane m of prefix || seed (1 + 8 NW bytes) followed by the SHAKE domain byte, where the
+// seed is given as NW little-endian 64-bit words (lane m < NW holds seed word m shifted by a byte).
+template <int NW>
+__device__ __forceinline__ uint2 prefixed_lane(int m, uint32_t prefix, const uint64_t (&s)[NW]) {
+    uint64_t v = m == 0 ? prefix : 0;
+#pragma unroll
+    for (int i = 0; i < NW; i++) {
+        if (m == i) v |= s[i] << 8;
+        if (m == i + 1) v |= s[i] >> 56;
+    }
+    if (m == NW) v |= (uint64_t)DOM_SHAKE << 8;
     return make_uint2((uint32_t)v, (uint32_t)(v >> 32));
 }
 __device__ __forceinline__ uint64_t u64(uint2 v) { return (uint64_t)v.x | ((uint64_t)v.y << 32); }
 
 // State absorbing prefix || seed (one block, not yet permuted).
-__device__ __forceinline__ uint2 seeded_state(uint32_t prefix, uint64_t s0, uint64_t s1, uint64_t s2, const WarpKeccak &w) {
-    uint2 a = w.lane < 4 ? prefixed_lane(w.lane, prefix, s0, s1, s2) : make_uint2(0, 0);
-    if (w.lane == SHAKE256_LANES - 1) a.y ^= 0x80000000u;
+template <int N>
+__device__ __forceinline__ uint2 seeded_state(uint32_t prefix, const uint64_t (&s)[FP<N>::NW], const WarpKeccak &w) {
+    uint2 a = w.lane <= FP<N>::NW ? prefixed_lane<FP<N>::NW>(w.lane, prefix, s) : make_uint2(0, 0);
+    if (w.lane == FP<N>::RATE - 1) a.y ^= 0x80000000u;
     return a;
 }
 
-// Squeeze the noise stream (state absorbed, not permuted): lanes 0..16 hold 4 u16 values each per
-// block; value at stream position p is CDF-sampled and handed to emit(p, v).
-template <class F>
+// Squeeze the noise stream (state absorbed, not permuted): lanes 0..RATE-1 hold 4 u16 values each
+// per block; value at stream position p is CDF-sampled and handed to emit(p, v).
+template <int N, class F>
 __device__ __forceinline__ void warp_noise_stream(uint2 &a, int count, const WarpKeccak &w, F emit) {
-    for (int base = 0; base < count; base += 68) {
+    constexpr int R = FP<N>::RATE;
+    for (int base = 0; base < count; base += 4 * R) {
         keccak_f1600_warp(a, w);
-        if (w.lane < 17) {
+        if (w.lane < R) {
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const int p = base + 4 * w.lane + q;
                 const uint32_t word = q < 2 ? a.x : a.y;
-                if (p < count) emit(p, cdf_sample((word >> (16 * (q & 1))) & 0xffff));
+                if (p < count) emit(p, cdf_sample<N>((word >> (16 * (q & 1))) & 0xffff));
             }
         }
     }
 }
 
+template <int N>
 __device__ __forceinline__ void write_spt(uint8_t *scr, int p, uint16_t v) {
     uint16_t *Spt = reinterpret_cast<uint16_t *>(scr), *Ep = Spt + N * NB, *Epp = Ep + N * NB;
     if (p < N * NB) Spt[(p % N) * NB + p / N] = v;  // stream S'[i*N + k] -> Spt[k*8 + i]
@@ -111,78 +180,94 @@ __device__ __forceinline__ void write_spt(uint8_t *scr, int p, uint16_t v) {
     if (x >= n) return;                                          \
     const WarpKeccak w(threadIdx.x & 31)
 
-// keypair: seedA = SHAKE256(z, 16) -> pk[0..16); S (as St[j][k], N x 8) and E (N x 8) -> scratch
+// keypair: seedA = SHAKE(z, 16) -> pk[0..16); S (as St[j][k], N x 8) and E (N x 8) -> scratch
+template <int N>
 __global__ void __launch_bounds__(128) fr_kp_pre(int n, const uint8_t *coins, int cstride, uint8_t *pk, uint8_t *scratch) {
+    using P = FP<N>;
     FR_WARP_INSTANCE;
-    const uint8_t *c = coins + (size_t)x * cstride;  // s(24) || seedSE(24) || z(16)
+    const uint8_t *c = coins + (size_t)x * cstride;  // s(SSB) || seedSE(SSB) || z(16)
     uint2 a;
-    warp_absorb2<SHAKE256_LANES>(a, reinterpret_cast<const uint2 *>(c + 48), 2, nullptr, 0, DOM_SHAKE, w);
+    warp_absorb2<P::RATE>(a, reinterpret_cast<const uint2 *>(c + 2 * P::SSB), 2, nullptr, 0, DOM_SHAKE, w);
     keccak_f1600_warp(a, w);
-    if (w.lane < 2) reinterpret_cast<uint2 *>(pk + (size_t)x * PKB)[w.lane] = a;
-    const uint64_t *sd = reinterpret_cast<const uint64_t *>(c + 24);
-    a = seeded_state(0x5F, sd[0], sd[1], sd[2], w);
-    uint16_t *St = reinterpret_cast<uint16_t *>(scratch + (size_t)x * SCRATCH), *E = St + N * NB;
+    if (w.lane < 2) reinterpret_cast<uint2 *>(pk + (size_t)x * P::PKB)[w.lane] = a;
+    const uint64_t *sd = reinterpret_cast<const uint64_t *>(c + P::SSB);
+    uint64_t seed[P::NW];
+#pragma unroll
+    for (int i = 0; i < P::NW; i++) seed[i] = sd[i];
+    a = seeded_state<N>(0x5F, seed, w);
+    uint16_t *St = reinterpret_cast<uint16_t *>(scratch + (size_t)x * P::SCRATCH), *E = St + N * NB;
     // stream order: S[k*N + j] (k < 8, j < N) then E[i*8 + k]
-    warp_noise_stream(a, 2 * N * NB, w, [&](int p, uint16_t v) {
+    warp_noise_stream<N>(a, 2 * N * NB, w, [&](int p, uint16_t v) {
         if (p < N * NB) St[(p % N) * NB + p / N] = v;
         else E[p - N * NB] = v;
     });
 }
 
-// G2(pkh || mu) with pkh in lanes 0..2 of `a`, mu at `mu`; then the S' / E' / E'' noise stream.
-// Writes k (24 B) and mu (24 B) into the scratch seed area.
+// G2(pkh || mu) with pkh in lanes 0..NW-1 of `a`, mu at `mu`; then the S' / E' / E'' noise stream.
+// Writes k (SSB bytes) and mu (MUB bytes) into the scratch seed area.
+template <int N>
 __device__ __forceinline__ void g2_and_noise(uint2 a, const uint8_t *mu, uint8_t *scr, const WarpKeccak &w) {
+    using P = FP<N>;
+    constexpr int NW = P::NW;
     const uint2 *m = reinterpret_cast<const uint2 *>(mu);
-    uint2 g = w.lane < 3 ? a : (w.lane < 6 ? m[w.lane - 3] : make_uint2(0, 0));
-    if (w.lane == 6) g.x ^= DOM_SHAKE;
-    if (w.lane == SHAKE256_LANES - 1) g.y ^= 0x80000000u;
+    uint2 g = w.lane < NW ? a : (w.lane < 2 * NW ? m[w.lane - NW] : make_uint2(0, 0));
+    if (w.lane == 2 * NW) g.x ^= DOM_SHAKE;
+    if (w.lane == P::RATE - 1) g.y ^= 0x80000000u;
     keccak_f1600_warp(g, w);
-    uint2 *kk = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2), *mm = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2 + 32);
-    if (w.lane >= 3 && w.lane < 6) kk[w.lane - 3] = g;
-    const uint2 mv = w.lane < 3 ? m[w.lane] : make_uint2(0, 0);
+    uint2 *kk = reinterpret_cast<uint2 *>(scr + P::NOISE_U16 * 2), *mm = reinterpret_cast<uint2 *>(scr + P::NOISE_U16 * 2 + 32);
+    if (w.lane >= NW && w.lane < 2 * NW) kk[w.lane - NW] = g;
+    const uint2 mv = w.lane < NW ? m[w.lane] : make_uint2(0, 0);
     __syncwarp();
-    if (w.lane < 3 && mu != scr + NOISE_U16 * 2 + 32) mm[w.lane] = mv;
-    const uint64_t s0 = u64(shfl2(g, 0)), s1 = u64(shfl2(g, 1)), s2 = u64(shfl2(g, 2));
-    uint2 st = seeded_state(0x96, s0, s1, s2, w);
-    warp_noise_stream(st, NOISE_U16, w, [&](int p, uint16_t v) { write_spt(scr, p, v); });
+    if (w.lane < NW && mu != scr + P::NOISE_U16 * 2 + 32) mm[w.lane] = mv;
+    uint64_t seed[NW];
+#pragma unroll
+    for (int i = 0; i < NW; i++) seed[i] = u64(shfl2(g, i));
+    uint2 st = seeded_state<N>(0x96, seed, w);
+    warp_noise_stream<N>(st, P::NOISE_U16, w, [&](int p, uint16_t v) { write_spt<N>(scr, p, v); });
 }
 
 // encaps prologue: pkh = G1(pk); (seedSE || k) = G2(pkh || mu); S', E', E'' sampled -> scratch.
 // scratch: Spt (N x 8: Spt[k][i] = S'[i][k]), Ep (8 x N), Epp (8 x 8), then k (24) at +NOISE*2,
 // mu (24) at +NOISE*2 + 32.
+template <int N>
 __device__ __forceinline__ void zero_gacc(uint8_t *scr, int lane) {
-    uint4 *g = reinterpret_cast<uint4 *>(scr + GACC_OFF);
+    uint4 *g = reinterpret_cast<uint4 *>(scr + FP<N>::GACC_OFF);
     for (int i = lane; i < NB * N / 4; i += 32) g[i] = make_uint4(0, 0, 0, 0);
 }
 
-// pkh != nullptr: pkh = SHAKE256(pk, 24) is given (the tail of a resident secret key, 24 bytes at
-// pkh + x * 24), which skips the 115 serial permutations of hashing the public key.
+// pkh != nullptr: pkh = SHAKE(pk, SSB) is given (the tail of a resident secret key, SSB bytes at
+// pkh + x * SSB), which skips the serial permutations of hashing the public key.
+template <int N>
 __global__ void __launch_bounds__(128) fr_enc_pre(int n, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
                                                   int split, const uint8_t *pkh) {
+    using P = FP<N>;
     FR_WARP_INSTANCE;
-    if (split > 1) zero_gacc(scratch + (size_t)x * SCRATCH, w.lane);
+    if (split > 1) zero_gacc<N>(scratch + (size_t)x * P::SCRATCH, w.lane);
     uint2 a;
     if (pkh) {
-        const uint2 *h = reinterpret_cast<const uint2 *>(pkh + (size_t)x * 24);
-        a = w.lane < 3 ? h[w.lane] : make_uint2(0, 0);
+        const uint2 *h = reinterpret_cast<const uint2 *>(pkh + (size_t)x * P::SSB);
+        a = w.lane < P::NW ? h[w.lane] : make_uint2(0, 0);
     } else {
-        warp_absorb2<SHAKE256_LANES>(a, reinterpret_cast<const uint2 *>(pk + (size_t)x * PKB), PKB / 8, nullptr, 0,
-                                     DOM_SHAKE, w);
+        warp_absorb2<P::RATE>(a, reinterpret_cast<const uint2 *>(pk + (size_t)x * P::PKB), P::PKB / 8, nullptr, 0,
+                              DOM_SHAKE, w);
         keccak_f1600_warp(a, w);
     }
-    g2_and_noise(a, mu + (size_t)x * MUB, scratch + (size_t)x * SCRATCH, w);
+    g2_and_noise<N>(a, mu + (size_t)x * P::MUB, scratch + (size_t)x * P::SCRATCH, w);
 }
 
 // decaps, step 1 (CTA per instance): W = C - B' S (frodo_mul_bs + frodo_sub), mu' = decode(W)
 // -> scratch mu' slot.  B' and S are staged in shared memory with coalesced loads.
+template <int N>
 __global__ void __launch_bounds__(256) fr_dec_w(int n, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch) {
+    using P = FP<N>;
+    constexpr int LOGQ = P::LOGQ, B = P::B;
     __shared__ __align__(16) uint16_t Bp[NB * N];
     __shared__ __align__(16) uint16_t S[NB * N];
     __shared__ uint32_t W[64];
     const int x = blockIdx.x, tid = threadIdx.x;
-    const uint8_t *c = ct + (size_t)x * CTB, *sS = sk + (size_t)x * SKB + SSB + PKB;
+    const uint8_t *c = ct + (size_t)x * P::CTB, *sS = sk + (size_t)x * P::SKB + P::SSB + P::PKB;
     for (int e = tid; e < NB * N; e += blockDim.x) {
-        Bp[e] = (uint16_t)ld_be16(c + 2 * e);
+        Bp[e] = (uint16_t)ld_packed<LOGQ>(c, e);
         S[e] = (uint16_t)(sS[2 * e] | (sS[2 * e + 1] << 8));
     }
     if (tid < 64) W[tid] = 0;
@@ -195,93 +280,103 @@ __global__ void __launch_bounds__(256) fr_dec_w(int n, const uint8_t *ct, const 
         atomicAdd(&W[o], sum);
     }
     __syncthreads();
-    if (tid < 8) {  // word g = tid: 8 pieces of 3 bits (key_decode)
+    if (tid < 8) {  // word g = tid: 8 pieces of B bits (key_decode)
         const int g = tid;
         uint32_t templong = 0;
         for (int jj = 0; jj < 8; jj++) {
-            const uint32_t wv = (ld_be16(c + C1B + 2 * (g * NB + jj)) - W[g * NB + jj]) & 0xffff;
-            const uint32_t t = (wv + (1u << 12)) >> 13;
-            templong |= (t & 7) << (3 * jj);
+            const uint32_t wv = (ld_packed<LOGQ>(c + P::C1B, g * NB + jj) - W[g * NB + jj]) & P::MASKQ;
+            const uint32_t t = (wv + (1u << (LOGQ - B - 1))) >> (LOGQ - B);
+            templong |= (t & ((1u << B) - 1)) << (B * jj);
         }
-        uint8_t *mu = scratch + (size_t)x * SCRATCH + NOISE_U16 * 2 + 32;
-        mu[3 * g] = (uint8_t)templong;
-        mu[3 * g + 1] = (uint8_t)(templong >> 8);
-        mu[3 * g + 2] = (uint8_t)(templong >> 16);
+        uint8_t *mu = scratch + (size_t)x * P::SCRATCH + P::NOISE_U16 * 2 + 32;
+#pragma unroll
+        for (int b = 0; b < B; b++) mu[B * g + b] = (uint8_t)(templong >> (8 * b));
     }
 }
 
 // decaps, step 2 (warp per instance): (seedSE' || k') = G2(pkh || mu'); S', E', E'' -> scratch
+template <int N>
 __global__ void __launch_bounds__(128) fr_dec_pre(int n, const uint8_t *sk, uint8_t *scratch, int split) {
+    using P = FP<N>;
     FR_WARP_INSTANCE;
-    uint8_t *scr = scratch + (size_t)x * SCRATCH;
-    if (split > 1) zero_gacc(scr, w.lane);
-    const uint2 *pkh = reinterpret_cast<const uint2 *>(sk + (size_t)x * SKB + SSB + PKB + C1B);
-    const uint2 a = w.lane < 3 ? pkh[w.lane] : make_uint2(0, 0);
-    g2_and_noise(a, scr + NOISE_U16 * 2 + 32, scr, w);
+    uint8_t *scr = scratch + (size_t)x * P::SCRATCH;
+    if (split > 1) zero_gacc<N>(scr, w.lane);
+    const uint2 *pkh = reinterpret_cast<const uint2 *>(sk + (size_t)x * P::SKB + P::SSB + P::PKB + 2 * N * NB);
+    const uint2 a = w.lane < P::NW ? pkh[w.lane] : make_uint2(0, 0);
+    g2_and_noise<N>(a, scr + P::NOISE_U16 * 2 + 32, scr, w);
 }
 
-// F = SHAKE256(ct || key, 24): encaps key = k; decaps key = fail ? s : k' (constant-time select)
+// F = SHAKE(ct || key, SSB): encaps key = k; decaps key = fail ? s : k' (constant-time select)
+template <int N>
 __global__ void __launch_bounds__(128) fr_post(int n, const uint8_t *ct, uint8_t *scratch, const uint8_t *sk, uint8_t *ss) {
+    using P = FP<N>;
     FR_WARP_INSTANCE;
-    uint8_t *scr = scratch + (size_t)x * SCRATCH;
-    const uint2 *k = reinterpret_cast<const uint2 *>(scr + NOISE_U16 * 2);
-    uint2 *key = reinterpret_cast<uint2 *>(scr + NOISE_U16 * 2 + 72);
-    if (w.lane < 3) {
+    uint8_t *scr = scratch + (size_t)x * P::SCRATCH;
+    const uint2 *k = reinterpret_cast<const uint2 *>(scr + P::NOISE_U16 * 2);
+    uint2 *key = reinterpret_cast<uint2 *>(scr + P::NOISE_U16 * 2 + 72);
+    if (w.lane < P::NW) {
         uint2 kv = k[w.lane];
         if (sk) {
-            const uint32_t mask = 0u - (uint32_t)(scr[NOISE_U16 * 2 + 64] != 0);
-            const uint2 sv = reinterpret_cast<const uint2 *>(sk + (size_t)x * SKB)[w.lane];
+            const uint32_t mask = 0u - (uint32_t)(scr[P::NOISE_U16 * 2 + 64] != 0);
+            const uint2 sv = reinterpret_cast<const uint2 *>(sk + (size_t)x * P::SKB)[w.lane];
             kv = make_uint2(kv.x ^ (mask & (kv.x ^ sv.x)), kv.y ^ (mask & (kv.y ^ sv.y)));
         }
         key[w.lane] = kv;
     }
     __syncwarp();
     uint2 a;
-    warp_absorb2<SHAKE256_LANES>(a, reinterpret_cast<const uint2 *>(ct + (size_t)x * CTB), CTB / 8, key, 3, DOM_SHAKE, w);
+    warp_absorb2<P::RATE>(a, reinterpret_cast<const uint2 *>(ct + (size_t)x * P::CTB), P::CTB / 8, key, P::NW, DOM_SHAKE,
+                          w);
     keccak_f1600_warp(a, w);
-    if (w.lane < 3) reinterpret_cast<uint2 *>(ss + (size_t)x * SSB)[w.lane] = a;
+    if (w.lane < P::NW) reinterpret_cast<uint2 *>(ss + (size_t)x * P::SSB)[w.lane] = a;
 }
 
-// keypair epilogue: sk = s || pk || S (u16 LE, S[k*N + j]) || SHAKE256(pk, 24)
+// keypair epilogue: sk = s || pk || S (u16 LE, S[k*N + j]) || SHAKE(pk, SSB)
+template <int N>
 __global__ void __launch_bounds__(128) fr_kp_post(int n, const uint8_t *coins, int cstride, const uint8_t *pk,
                                                   const uint8_t *scratch, uint8_t *sk) {
+    using P = FP<N>;
     FR_WARP_INSTANCE;
-    uint8_t *s = sk + (size_t)x * SKB;
-    const uint8_t *p = pk + (size_t)x * PKB;
-    const uint16_t *St = reinterpret_cast<const uint16_t *>(scratch + (size_t)x * SCRATCH);
-    if (w.lane < 3) reinterpret_cast<uint2 *>(s)[w.lane] = reinterpret_cast<const uint2 *>(coins + (size_t)x * cstride)[w.lane];
-    for (int i = w.lane; i < PKB / 8; i += 32) reinterpret_cast<uint2 *>(s + SSB)[i] = reinterpret_cast<const uint2 *>(p)[i];
-    uint16_t *dS = reinterpret_cast<uint16_t *>(s + SSB + PKB);
+    uint8_t *s = sk + (size_t)x * P::SKB;
+    const uint8_t *p = pk + (size_t)x * P::PKB;
+    const uint16_t *St = reinterpret_cast<const uint16_t *>(scratch + (size_t)x * P::SCRATCH);
+    if (w.lane < P::NW)
+        reinterpret_cast<uint2 *>(s)[w.lane] = reinterpret_cast<const uint2 *>(coins + (size_t)x * cstride)[w.lane];
+    for (int i = w.lane; i < P::PKB / 8; i += 32)
+        reinterpret_cast<uint2 *>(s + P::SSB)[i] = reinterpret_cast<const uint2 *>(p)[i];
+    uint16_t *dS = reinterpret_cast<uint16_t *>(s + P::SSB + P::PKB);
     for (int e = w.lane; e < N * NB; e += 32) {
         const int k = e / N, j = e % N;
         dS[e] = St[j * NB + k];
     }
     uint2 a;
-    warp_absorb2<SHAKE256_LANES>(a, reinterpret_cast<const uint2 *>(p), PKB / 8, nullptr, 0, DOM_SHAKE, w);
+    warp_absorb2<P::RATE>(a, reinterpret_cast<const uint2 *>(p), P::PKB / 8, nullptr, 0, DOM_SHAKE, w);
     keccak_f1600_warp(a, w);
-    if (w.lane < 3) reinterpret_cast<uint2 *>(s + SSB + PKB + C1B)[w.lane] = a;
+    if (w.lane < P::NW) reinterpret_cast<uint2 *>(s + P::SSB + P::PKB + 2 * N * NB)[w.lane] = a;
 }
 
 // ---------------------------------------------------------------------------------------------
 // Core kernels: A generated on the fly
 // ---------------------------------------------------------------------------------------------
 // B = A S + E, one thread per row of A; CTA = (instance, group of rows); St in shared memory.
+template <int N>
 __global__ void __launch_bounds__(256) fr_kp_core(int n, uint8_t *pk, const uint8_t *scratch) {
+    using P = FP<N>;
     __shared__ __align__(16) uint16_t St[N * NB];
     const int x = blockIdx.y;
-    const uint16_t *gSt = reinterpret_cast<const uint16_t *>(scratch + (size_t)x * SCRATCH), *E = gSt + N * NB;
+    const uint16_t *gSt = reinterpret_cast<const uint16_t *>(scratch + (size_t)x * P::SCRATCH), *E = gSt + N * NB;
     for (int i = threadIdx.x; i < N * NB / 8; i += blockDim.x)
         reinterpret_cast<uint4 *>(St)[i] = reinterpret_cast<const uint4 *>(gSt)[i];
     __syncthreads();
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= N) return;
-    uint8_t *p = pk + (size_t)x * PKB;
+    uint8_t *p = pk + (size_t)x * P::PKB;
     uint2 A[25];
     row_absorb(A, row, reinterpret_cast<const uint2 *>(p));
     uint32_t acc[NB];
 #pragma unroll
     for (int k = 0; k < NB; k++) acc[k] = E[row * NB + k];
-    for (int blk = 0; blk < ROW_BLOCKS; blk++) {
+    for (int blk = 0; blk < P::ROW_BLOCKS; blk++) {
         keccak_f1600(A);
         const int j0 = blk * 84;
 #pragma unroll
@@ -305,56 +400,67 @@ __global__ void __launch_bounds__(256) fr_kp_core(int n, uint8_t *pk, const uint
             }
         }
     }
-    // pack B row (8 values, 16-bit big-endian) at pk[16 + 16 row]
-    uint8_t *o = p + SEEDA + 16 * row;
-#pragma unroll
-    for (int k = 0; k < NB; k++) {
-        o[2 * k] = (uint8_t)(acc[k] >> 8);
-        o[2 * k + 1] = (uint8_t)acc[k];
-    }
+    // pack B row (8 values, LOGQ bits each, MSB first) at pk[16 + LOGQ row]
+    pack8<P::LOGQ>(p + SEEDA + P::LOGQ * row, acc);
 }
 
 // Epilogue of B' = S' A + E': V = S' B + E'' (B = unpack(pk_b), N x 8; 64 outputs, k split over
-// the CTA, into acc[NB*N ..]), then B' -> c1 and C = V + encode(mu) -> c2, 16-bit big-endian, or
-// compared with the received ciphertext (cmp != nullptr; the fail flag goes to scratch).
-// acc holds B' (8 x N, u32, wrapped mod 2^32) and E'' in its last 64 words; Spt is S' (N x 8).
+// the CTA, into acc[NB*N ..]), then B' -> c1 and C = V + encode(mu) -> c2, packed LOGQ bits MSB
+// first, or compared mod q with the received ciphertext (cmp != nullptr; the fail flag goes to
+// scratch).  acc holds B' (8 x N, u32, wrapped mod 2^32) and E'' in its last 64 words; Spt is S'
+// (N x 8).  Packing works on groups of 8 consecutive values (LOGQ bytes each).
+template <int N>
 __device__ void sa_epilogue(uint32_t *acc, const uint16_t *Spt, const uint8_t *p, uint8_t *scr, uint8_t *ct,
                             const uint8_t *ct_cmp, int x) {
+    using P = FP<N>;
+    constexpr int LOGQ = P::LOGQ, B = P::B;
     const int tid = threadIdx.x, nthr = blockDim.x;
     {
         const uint8_t *pb = p + SEEDA;
         for (int t = tid; t < 64 * 4; t += nthr) {
             const int o = t & 63, part = t >> 6, i = o >> 3, l = o & 7;
             uint32_t sum = 0;
-            for (int k = part; k < N; k += 4) sum += (uint32_t)Spt[k * NB + i] * ld_be16(pb + 2 * (k * NB + l));
+            for (int k = part; k < N; k += 4)
+                sum += (uint32_t)Spt[k * NB + i] * unpack_at<LOGQ>(pb + (size_t)LOGQ * k, l);
             atomicAdd(acc + NB * N + o, sum);
         }
     }
     __syncthreads();
-    const uint8_t *mu = scr + NOISE_U16 * 2 + 32;
+    const uint8_t *mu = scr + P::NOISE_U16 * 2 + 32;
     uint32_t diff = 0;
-    for (int e = tid; e < NB * N; e += nthr) {
-        const uint32_t v = acc[e] & 0xffff;
-        if (ct_cmp) diff |= v ^ ld_be16(ct_cmp + (size_t)x * CTB + 2 * e);
-        else {
-            ct[(size_t)x * CTB + 2 * e] = (uint8_t)(v >> 8);
-            ct[(size_t)x * CTB + 2 * e + 1] = (uint8_t)v;
+    for (int g8 = tid; g8 < NB * N / 8; g8 += nthr) {  // groups of 8 values of B'
+        uint32_t v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = acc[8 * g8 + k] & P::MASKQ;
+        if (ct_cmp) {
+            const uint8_t *c = ct_cmp + (size_t)x * P::CTB + (size_t)LOGQ * g8;
+#pragma unroll
+            for (int k = 0; k < 8; k++) diff |= v[k] ^ unpack_at<LOGQ>(c, k);
+        } else {
+            pack8<LOGQ>(ct + (size_t)x * P::CTB + (size_t)LOGQ * g8, v);
         }
     }
-    for (int e = tid; e < 64; e += nthr) {
-        const int g = e >> 3, j = e & 7;
-        const uint32_t temp = (uint32_t)mu[3 * g] | ((uint32_t)mu[3 * g + 1] << 8) | ((uint32_t)mu[3 * g + 2] << 16);
-        const uint32_t enc = ((temp >> (3 * j)) & 7) << 13;
-        const uint32_t v = (acc[NB * N + e] + enc) & 0xffff;
-        if (ct_cmp) diff |= v ^ ld_be16(ct_cmp + (size_t)x * CTB + C1B + 2 * e);
-        else {
-            ct[(size_t)x * CTB + C1B + 2 * e] = (uint8_t)(v >> 8);
-            ct[(size_t)x * CTB + C1B + 2 * e + 1] = (uint8_t)v;
+    for (int g = tid; g < 8; g += nthr) {  // C = V + encode(mu), row g: B bytes of mu -> 8 values
+        uint32_t temp = 0;
+#pragma unroll
+        for (int b = 0; b < B; b++) temp |= (uint32_t)mu[B * g + b] << (8 * b);
+        uint32_t v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const uint32_t enc = ((temp >> (B * j)) & ((1u << B) - 1)) << (LOGQ - B);
+            v[j] = (acc[NB * N + 8 * g + j] + enc) & P::MASKQ;
+        }
+        if (ct_cmp) {
+            const uint8_t *c = ct_cmp + (size_t)x * P::CTB + P::C1B + (size_t)LOGQ * g;
+#pragma unroll
+            for (int j = 0; j < 8; j++) diff |= v[j] ^ unpack_at<LOGQ>(c, j);
+        } else {
+            pack8<LOGQ>(ct + (size_t)x * P::CTB + P::C1B + (size_t)LOGQ * g, v);
         }
     }
     if (ct_cmp) {
         const int any = __syncthreads_or(diff != 0);
-        if (tid == 0) scr[NOISE_U16 * 2 + 64] = (uint8_t)any;
+        if (tid == 0) scr[P::NOISE_U16 * 2 + 64] = (uint8_t)any;
     }
 }
 
@@ -366,15 +472,17 @@ __device__ void sa_epilogue(uint32_t *acc, const uint16_t *Spt, const uint8_t *p
 constexpr int SA_THREADS = 256;
 constexpr int STAGE_PITCH = 86;  // u16 per staged row block (84 used; odd word pitch)
 constexpr int BLK_COLS = 84;     // u16 values per SHAKE128 block
+template <int N>
 __global__ void __launch_bounds__(SA_THREADS) fr_sa_core(int n, uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *pk,
                                                          int pk_stride, uint8_t *scratch) {
+    using P = FP<N>;
     extern __shared__ __align__(16) uint8_t smem[];
     uint16_t *Spt = reinterpret_cast<uint16_t *>(smem);                       // N x 8
     uint32_t *acc = reinterpret_cast<uint32_t *>(smem + N * NB * 2);          // 8 x N (+64 for V)
     uint16_t *stage = reinterpret_cast<uint16_t *>(smem + N * NB * 2 + (NB * N + 64) * 4);  // threads x 86
     const int x = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x, parts = gridDim.y;
     const int rows_per = (N + parts - 1) / parts, rbeg = blockIdx.y * rows_per, rend = min(N, rbeg + rows_per);
-    uint8_t *scr = scratch + (size_t)x * SCRATCH;
+    uint8_t *scr = scratch + (size_t)x * P::SCRATCH;
     const uint16_t *gSpt = reinterpret_cast<const uint16_t *>(scr), *Ep = gSpt + N * NB, *Epp = Ep + N * NB;
     const uint8_t *p = pk + (size_t)x * pk_stride;
     for (int i = tid; i < N * NB / 8; i += nthr) reinterpret_cast<uint4 *>(Spt)[i] = reinterpret_cast<const uint4 *>(gSpt)[i];
@@ -388,7 +496,7 @@ __global__ void __launch_bounds__(SA_THREADS) fr_sa_core(int n, uint8_t *ct, con
         const int rows = min(nthr, rend - r0);
         uint2 A[25];
         if (tid < rows) row_absorb(A, r0 + tid, reinterpret_cast<const uint2 *>(p));
-        for (int blk = 0; blk < ROW_BLOCKS; blk++) {
+        for (int blk = 0; blk < P::ROW_BLOCKS; blk++) {
             if (tid < rows) {
                 keccak_f1600(A);
                 uint32_t *st = reinterpret_cast<uint32_t *>(stage + tid * STAGE_PITCH);
@@ -421,51 +529,63 @@ __global__ void __launch_bounds__(SA_THREADS) fr_sa_core(int n, uint8_t *ct, con
         }
     }
     if (parts > 1) {
-        uint32_t *g = reinterpret_cast<uint32_t *>(scr + GACC_OFF);
+        uint32_t *g = reinterpret_cast<uint32_t *>(scr + P::GACC_OFF);
         for (int i = tid; i < NB * N; i += nthr) atomicAdd(g + i, acc[i]);
         return;
     }
-    sa_epilogue(acc, Spt, p, scr, ct, ct_cmp, x);
+    sa_epilogue<N>(acc, Spt, p, scr, ct, ct_cmp, x);
 }
 
 // Finish a split product: acc = (sum of the parts) + E', then the same epilogue.  CTA per instance.
+template <int N>
 __global__ void __launch_bounds__(SA_THREADS) fr_sa_final(int n, uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *pk,
                                                           int pk_stride, uint8_t *scratch) {
+    using P = FP<N>;
     extern __shared__ __align__(16) uint8_t smem[];
     uint16_t *Spt = reinterpret_cast<uint16_t *>(smem);
     uint32_t *acc = reinterpret_cast<uint32_t *>(smem + N * NB * 2);
     const int x = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x;
-    uint8_t *scr = scratch + (size_t)x * SCRATCH;
+    uint8_t *scr = scratch + (size_t)x * P::SCRATCH;
     const uint16_t *gSpt = reinterpret_cast<const uint16_t *>(scr), *Ep = gSpt + N * NB, *Epp = Ep + N * NB;
-    const uint32_t *g = reinterpret_cast<const uint32_t *>(scr + GACC_OFF);
+    const uint32_t *g = reinterpret_cast<const uint32_t *>(scr + P::GACC_OFF);
     for (int i = tid; i < N * NB / 8; i += nthr) reinterpret_cast<uint4 *>(Spt)[i] = reinterpret_cast<const uint4 *>(gSpt)[i];
     for (int i = tid; i < NB * N; i += nthr) acc[i] = g[i] + Ep[i];
     for (int i = tid; i < 64; i += nthr) acc[NB * N + i] = Epp[i];
     __syncthreads();
-    sa_epilogue(acc, Spt, pk + (size_t)x * pk_stride, scr, ct, ct_cmp, x);
+    sa_epilogue<N>(acc, Spt, pk + (size_t)x * pk_stride, scr, ct, ct_cmp, x);
 }
 
-static size_t sa_smem(int threads) { return (size_t)N * NB * 2 + ((size_t)NB * N + 64) * 4 + (size_t)threads * STAGE_PITCH * 2; }
-static size_t sa_final_smem() { return (size_t)N * NB * 2 + ((size_t)NB * N + 64) * 4; }
+static size_t sa_smem(int N, int threads) {
+    return (size_t)N * NB * 2 + ((size_t)NB * N + 64) * 4 + (size_t)threads * STAGE_PITCH * 2;
+}
+static size_t sa_final_smem(int N) { return (size_t)N * NB * 2 + ((size_t)NB * N + 64) * 4; }
 
 }  // namespace frodo
 
 using namespace frodo;
 
 int frodo_init_constants() {
-    const uint16_t cdf[11] = {5638, 15915, 23689, 28571, 31116, 32217, 32613, 32731, 32760, 32766, 32767};
+    // CDF tables of the FrodoKEM parameter sets (n = 976: FrodoKEM_GPU/frodo976.cu:21)
+    const uint16_t cdf640[13] = {4643, 13363, 20579, 25843, 29227, 31145, 32103, 32525, 32689, 32745, 32762, 32766, 32767};
+    const uint16_t cdf976[11] = {5638, 15915, 23689, 28571, 31116, 32217, 32613, 32731, 32760, 32766, 32767};
+    const uint16_t cdf1344[7] = {9142, 23462, 30338, 32361, 32725, 32765, 32767};
     uint2 rc[24];
     keccak_rc_host(rc);
     if (cudaMemcpyToSymbol(c_keccak_rc, rc, sizeof rc) != cudaSuccess) return PQCGPU_ECUDA;
-    if (cudaMemcpyToSymbol(c_cdf, cdf, sizeof cdf) != cudaSuccess) return PQCGPU_ECUDA;
+    if (cudaMemcpyToSymbol(c_cdf640, cdf640, sizeof cdf640) != cudaSuccess) return PQCGPU_ECUDA;
+    if (cudaMemcpyToSymbol(c_cdf976, cdf976, sizeof cdf976) != cudaSuccess) return PQCGPU_ECUDA;
+    if (cudaMemcpyToSymbol(c_cdf1344, cdf1344, sizeof cdf1344) != cudaSuccess) return PQCGPU_ECUDA;
     return PQCGPU_OK;
 }
-size_t frodo_scratch_bytes() { return SCRATCH; }
+size_t frodo_scratch_bytes(int N) {
+    return N == 640 ? FP<640>::SCRATCH : N == 976 ? FP<976>::SCRATCH : N == 1344 ? FP<1344>::SCRATCH : 0;
+}
 
 // Launch shapes.  Keypair: threads per CTA of fr_kp_core (one row of A per thread).  Encaps /
 // decaps: row parts per instance for B' = S' A + E' and threads per CTA of fr_sa_core.  0 = chosen
 // by batch size: small batches split an instance over several CTAs (latency), large ones keep one
-// CTA per instance (no split traffic).  Set through pqcgpu_set_launch_shape (the autotuner).
+// CTA per instance (no split traffic).  Set through pqcgpu_set_launch_shape (the autotuner); the
+// settings apply to every FrodoKEM parameter set.
 static int g_fr_parts[3] = {0, 0, 0}, g_fr_threads[3] = {0, 0, 0};
 
 static void fr_shape(int op, int n, int *parts, int *threads) {
@@ -510,57 +630,89 @@ int frodo_get_shape(int op, int *parts, int *threads) {
     return PQCGPU_OK;
 }
 
-int frodo_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
-                      cudaStream_t st) {
+namespace {
+template <int N>
+int keypair_n(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch, cudaStream_t st) {
     int parts, thr;
     fr_shape(0, n, &parts, &thr);
-    PQC_LAUNCH(st, "fr_kp_pre", 976, 0, fr_kp_pre<<<(n + 3) / 4, 128, 0, st>>>(n, coins, cstride, pk, scratch));
-    PQC_LAUNCH(st, "fr_kp_core", 976, 0, fr_kp_core<<<dim3((N + thr - 1) / thr, n), thr, 0, st>>>(n, pk, scratch));
-    PQC_LAUNCH(st, "fr_kp_post", 976, 0, fr_kp_post<<<(n + 3) / 4, 128, 0, st>>>(n, coins, cstride, pk, scratch, sk));
+    PQC_LAUNCH(st, "fr_kp_pre", N, 0, fr_kp_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, coins, cstride, pk, scratch));
+    PQC_LAUNCH(st, "fr_kp_core", N, 0, fr_kp_core<N><<<dim3((N + thr - 1) / thr, n), thr, 0, st>>>(n, pk, scratch));
+    PQC_LAUNCH(st, "fr_kp_post", N, 0, fr_kp_post<N><<<(n + 3) / 4, 128, 0, st>>>(n, coins, cstride, pk, scratch, sk));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
 // B' = S' A + E' and the ciphertext epilogue: one CTA per instance, or `parts` CTAs per instance
 // plus fr_sa_final.
-static void launch_sa(int n, uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *pk, int pk_stride, uint8_t *scratch,
-                      int parts, int thr, cudaStream_t st) {
-    PQC_LAUNCH(st, "fr_sa_core", 976, 0,
-               fr_sa_core<<<dim3(n, parts), thr, sa_smem(thr), st>>>(n, ct, ct_cmp, pk, pk_stride, scratch));
+template <int N>
+void launch_sa(int n, uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *pk, int pk_stride, uint8_t *scratch, int parts,
+               int thr, cudaStream_t st) {
+    PQC_LAUNCH(st, "fr_sa_core", N, 0,
+               fr_sa_core<N><<<dim3(n, parts), thr, sa_smem(N, thr), st>>>(n, ct, ct_cmp, pk, pk_stride, scratch));
     if (parts > 1)
-        PQC_LAUNCH(st, "fr_sa_final", 976, 0,
-                   fr_sa_final<<<n, SA_THREADS, sa_final_smem(), st>>>(n, ct, ct_cmp, pk, pk_stride, scratch));
+        PQC_LAUNCH(st, "fr_sa_final", N, 0,
+                   fr_sa_final<N><<<n, SA_THREADS, sa_final_smem(N), st>>>(n, ct, ct_cmp, pk, pk_stride, scratch));
 }
 
-static int sa_attrs() {
+template <int N>
+int sa_attrs() {
     if (capturing()) return PQCGPU_OK;
-    if (cudaFuncSetAttribute(fr_sa_core, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sa_smem(SA_THREADS)) !=
-        cudaSuccess) {
+    if (cudaFuncSetAttribute(fr_sa_core<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sa_smem(N, SA_THREADS)) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(fr_sa_final<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sa_final_smem(N)) !=
+            cudaSuccess) {
         cudaGetLastError();
         return PQCGPU_ECUDA;
     }
     return PQCGPU_OK;
 }
 
-int frodo_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
-                  cudaStream_t st, const uint8_t *pkh) {
-    if (sa_attrs()) return PQCGPU_ECUDA;
+template <int N>
+int enc_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch, cudaStream_t st,
+          const uint8_t *pkh) {
+    if (sa_attrs<N>()) return PQCGPU_ECUDA;
     int parts, thr;
     fr_shape(1, n, &parts, &thr);
-    PQC_LAUNCH(st, "fr_enc_pre", 976, 0, fr_enc_pre<<<(n + 3) / 4, 128, 0, st>>>(n, pk, mu, scratch, parts, pkh));
-    launch_sa(n, ct, nullptr, pk, PKB, scratch, parts, thr, st);
-    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, nullptr, ss));
+    PQC_LAUNCH(st, "fr_enc_pre", N, 0, fr_enc_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, pk, mu, scratch, parts, pkh));
+    launch_sa<N>(n, ct, nullptr, pk, FP<N>::PKB, scratch, parts, thr, st);
+    PQC_LAUNCH(st, "fr_post", N, 0, fr_post<N><<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, nullptr, ss));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
-int frodo_dec_dev(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, cudaStream_t st) {
-    if (sa_attrs()) return PQCGPU_ECUDA;
+template <int N>
+int dec_n(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, cudaStream_t st) {
+    using P = FP<N>;
+    if (sa_attrs<N>()) return PQCGPU_ECUDA;
     int parts, thr;
     fr_shape(2, n, &parts, &thr);
-    PQC_LAUNCH(st, "fr_dec_w", 976, 0, fr_dec_w<<<n, 256, 0, st>>>(n, ct, sk, scratch));
-    PQC_LAUNCH(st, "fr_dec_pre", 976, 0, fr_dec_pre<<<(n + 3) / 4, 128, 0, st>>>(n, sk, scratch, parts));
-    launch_sa(n, nullptr, ct, sk + SSB, SKB, scratch, parts, thr, st);
-    PQC_LAUNCH(st, "fr_post", 976, 0, fr_post<<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, sk, ss));
+    PQC_LAUNCH(st, "fr_dec_w", N, 0, fr_dec_w<N><<<n, 256, 0, st>>>(n, ct, sk, scratch));
+    PQC_LAUNCH(st, "fr_dec_pre", N, 0, fr_dec_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, sk, scratch, parts));
+    launch_sa<N>(n, nullptr, ct, sk + P::SSB, P::SKB, scratch, parts, thr, st);
+    PQC_LAUNCH(st, "fr_post", N, 0, fr_post<N><<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, sk, ss));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+}  // namespace
+
+int frodo_keypair_dev(int N, int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
+                      cudaStream_t st) {
+    if (N == 640) return keypair_n<640>(n, pk, sk, coins, cstride, scratch, st);
+    if (N == 976) return keypair_n<976>(n, pk, sk, coins, cstride, scratch, st);
+    if (N == 1344) return keypair_n<1344>(n, pk, sk, coins, cstride, scratch, st);
+    return PQCGPU_EINVAL;
+}
+
+int frodo_enc_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
+                  cudaStream_t st, const uint8_t *pkh) {
+    if (N == 640) return enc_n<640>(n, ct, ss, pk, mu, scratch, st, pkh);
+    if (N == 976) return enc_n<976>(n, ct, ss, pk, mu, scratch, st, pkh);
+    if (N == 1344) return enc_n<1344>(n, ct, ss, pk, mu, scratch, st, pkh);
+    return PQCGPU_EINVAL;
+}
+
+int frodo_dec_dev(int N, int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, cudaStream_t st) {
+    if (N == 640) return dec_n<640>(n, ss, ct, sk, scratch, st);
+    if (N == 976) return dec_n<976>(n, ss, ct, sk, scratch, st);
+    if (N == 1344) return dec_n<1344>(n, ss, ct, sk, scratch, st);
+    return PQCGPU_EINVAL;
 }
 
 }  // namespace pqc

@@ -98,15 +98,17 @@ int newhope_enc_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, c
 // kem=1: out = ss (32 B); kem=0: out = message
 int newhope_dec_dev(int N, int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st);
 
-// ---- FrodoKEM-976 (frodo.cu) ----
+// ---- FrodoKEM-640 / 976 / 1344 (frodo.cu); N = 640, 976 or 1344 ----
 int frodo_init_constants();
-size_t frodo_scratch_bytes();  // per instance, all three operations
-int frodo_keypair_dev(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
+size_t frodo_scratch_bytes(int N);  // per instance, all three operations
+int frodo_keypair_dev(int N, int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
                       cudaStream_t st);
-// pkh: optional SHAKE256(pk, 24) per instance (24-byte stride), e.g. from a resident secret key
-int frodo_enc_dev(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
+// pkh: optional SHAKE(pk, ss bytes) per instance (ss-size stride), e.g. from a resident secret key
+int frodo_enc_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
                   cudaStream_t st, const uint8_t *pkh = nullptr);
-int frodo_dec_dev(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, cudaStream_t st);
+int frodo_dec_dev(int N, int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, cudaStream_t st);
+// FrodoKEM parameter n of an algorithm id, 0 if it is not FrodoKEM
+int frodo_n(int alg);
 int frodo_set_shape(int op, int parts, int threads);
 int frodo_get_shape(int op, int *parts, int *threads);
 

@@ -245,7 +245,7 @@ struct pqcgpu_server {
         for (int a = 0; a < PQCGPU_NUM_ALGS; a++)
             for (int o = 0; o < 3; o++) {
                 auto &g = groups[a][o];
-                if (g.empty() || (a == PQCGPU_FRODO976 && heavy_running >= heavy_max)) continue;
+                if (g.empty() || (frodo_n(a) && heavy_running >= heavy_max)) continue;
                 if (alg < 0 || g.front()->t0 < oldest) {
                     alg = a;
                     op = o;
@@ -253,7 +253,7 @@ struct pqcgpu_server {
                 }
             }
         if (alg < 0) return false;
-        const int cap = (alg == PQCGPU_FRODO976) ? std::min(max_batch, 256) : max_batch;
+        const int cap = frodo_n(alg) ? std::min(max_batch, 256) : max_batch;
         auto &grp = groups[alg][op];
         KeyStore &k = ks[alg];
         const size_t take_n = std::min<size_t>(grp.size(), (size_t)cap);
@@ -317,10 +317,11 @@ struct pqcgpu_server {
         const size_t h2d = d;
         if (op == PQCGPU_OP_ENC && by_handle) { in0 = d; d += r256(sz[0] * n); }   // pk gathered
         if (op == PQCGPU_OP_DEC) { in1 = d; d += r256(sz[1] * n); }                // sk gathered
-        // FrodoKEM keeps pkh = SHAKE256(pk, 24) as the last 24 bytes of its secret key
-        const bool use_pkh = alg == PQCGPU_FRODO976 && op == PQCGPU_OP_ENC && by_handle;
+        // FrodoKEM keeps pkh = SHAKE(pk) as the last ss-size bytes of its secret key
+        const bool use_pkh = frodo_n(alg) && op == PQCGPU_OP_ENC && by_handle;
+        const size_t pkhb = sz[3];  // the shared-secret size = the pkh size
         size_t pkh = 0;
-        if (use_pkh) { pkh = d; d += r256(24 * (size_t)n); }
+        if (use_pkh) { pkh = d; d += r256(pkhb * (size_t)n); }
         const size_t out0 = d;
         d += r256(sz[2] * n);
         const size_t out1 = d;
@@ -391,10 +392,10 @@ struct pqcgpu_server {
         s.off_pkh = pkh;
         s.h2d_bytes = h2d;
         s.d2h_bytes = d2h;
-        s.stream = (alg == PQCGPU_FRODO976) ? s.lo : s.hi;
+        s.stream = frodo_n(alg) ? s.lo : s.hi;
         s.busy = true;
         s.has_job = true;
-        if (alg == PQCGPU_FRODO976) heavy_running++;
+        if (frodo_n(alg)) heavy_running++;
         s.cv.notify_one();
         return true;
     }
@@ -437,12 +438,14 @@ struct pqcgpu_server {
         } else if (op == PQCGPU_OP_ENC) {
             if (s.by_handle) launch_rows(true, D + s.off_in0, s.kpk, didx, n, s.pkb, st);
             if (s.use_pkh) {
-                const int words = 3;
+                size_t io[4];
+                op_io_sizes(alg, op, io);
+                const int words = (int)(io[3] / 8);  // pkh = ss size
                 PQC_LAUNCH(st, "rows_tail_gather", 0, 0,
                            rows_tail_gather<<<(n * words + 255) / 256, 256, 0, st>>>(
-                               (uint2 *)(D + s.off_pkh), s.ksk, didx, n, s.skb, s.skb - 24, words));
-                rc = frodo_enc_dev(n, D + s.off_out0, D + s.off_out1, D + s.off_in0, D + s.off_in1, D + s.off_scr, st,
-                                   D + s.off_pkh);
+                               (uint2 *)(D + s.off_pkh), s.ksk, didx, n, s.skb, s.skb - 8 * words, words));
+                rc = frodo_enc_dev(frodo_n(alg), n, D + s.off_out0, D + s.off_out1, D + s.off_in0, D + s.off_in1,
+                                   D + s.off_scr, st, D + s.off_pkh);
             } else {
                 rc = op_dev(alg, op, n, D + s.off_in0, D + s.off_in1, D + s.off_out0, D + s.off_out1, D + s.off_scr, 0,
                             st);
@@ -486,7 +489,7 @@ struct pqcgpu_server {
         if (rc && error.empty()) error = "a batch failed on the device";
         s.reqs.clear();
         s.busy = false;
-        if (s.alg == PQCGPU_FRODO976) heavy_running--;
+        if (frodo_n(s.alg)) heavy_running--;
         batches++;
         events++;
         cv_work.notify_one();

@@ -24,7 +24,8 @@ from . import _lib, kem
 ALG_NAMES = {
     "kyber512": "Kyber512", "kyber768": "Kyber768", "kyber1024": "Kyber1024",
     "kyber1024r2": "Kyber1024-round2", "newhope1024": "NewHope1024-CPAKEM", "newhope512": "NewHope512-CPAKEM",
-    "frodo976": "FrodoKEM-976-SHAKE", "mlkem512": "ML-KEM-512", "mlkem768": "ML-KEM-768",
+    "frodo976": "FrodoKEM-976-SHAKE", "frodo640": "FrodoKEM-640-SHAKE", "frodo1344": "FrodoKEM-1344-SHAKE",
+    "mlkem512": "ML-KEM-512", "mlkem768": "ML-KEM-768",
     "mlkem1024": "ML-KEM-1024",
 }
 
@@ -47,8 +48,8 @@ def coins_for(alg, seed):
     lib = _lib.load()
     s = kem.sizes(alg)
     _lib.check(lib.pqcgpu_randombytes_init_nist(seed, None))
-    kc = ctypes.create_string_buffer(64)
-    ec = ctypes.create_string_buffer(64)
+    kc = ctypes.create_string_buffer(s["kp_coins"])
+    ec = ctypes.create_string_buffer(s["enc_coins"])
     _lib.check(lib.pqcgpu_nist_coins(kem.alg_id(alg), 0, kc))
     _lib.check(lib.pqcgpu_nist_coins(kem.alg_id(alg), 1, ec))
     return kc.raw[:s["kp_coins"]], ec.raw[:s["enc_coins"]]

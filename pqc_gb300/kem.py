@@ -10,7 +10,7 @@ import json
 from . import _lib
 
 ALGS = {"kyber512": 0, "kyber768": 1, "kyber1024": 2, "kyber1024r2": 3, "newhope1024": 4, "frodo976": 5,
-        "mlkem512": 6, "mlkem768": 7, "mlkem1024": 8, "newhope512": 9}
+        "mlkem512": 6, "mlkem768": 7, "mlkem1024": 8, "newhope512": 9, "frodo640": 10, "frodo1344": 11}
 DEVICE_PTRS = 0x1
 PLAIN = 0x2
 STAGE_KERNELS = 0x4

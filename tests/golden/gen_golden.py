@@ -165,11 +165,13 @@ if __name__ == "__main__":
     restated("kyber1024r2", O.KYBER1024_R2, 16, 0)
     restated("newhope1024", O.NEWHOPE1024, 16, 0)
     restated("newhope512", O.NEWHOPE512, 16, 0)
+    restated("frodo640", O.FRODO640, 4, 0)
+    restated("frodo1344", O.FRODO1344, 2, 0)
     restated("frodo976", O.FRODO976, 4, 0)
     restated("mlkem512", O.MLKEM512, 16, 0)
     restated("mlkem768", O.MLKEM768, 16, 0)
     restated("mlkem1024", O.MLKEM1024, 16, 0)
     for name in ("kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976", "mlkem512", "mlkem768", "mlkem1024",
-                 "newhope512"):
-        kat_rsp(name, O.ALG_NAMES[name], 1 if name == "frodo976" else 3)
+                 "newhope512", "frodo640", "frodo1344"):
+        kat_rsp(name, O.ALG_NAMES[name], 1 if name.startswith("frodo") else 3)
     print("fixtures written to", HERE)

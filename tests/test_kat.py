@@ -7,7 +7,7 @@ import pytest
 from conftest import GOLDEN
 
 ALGS = ["kyber512", "kyber768", "kyber1024", "newhope1024", "frodo976", "mlkem512", "mlkem768", "mlkem1024",
-        "newhope512"]
+        "newhope512", "frodo640", "frodo1344"]
 
 
 def _fixture(name):

@@ -56,7 +56,7 @@ def test_newhope_cpa_matches_reference(oracle, poly_n):
 
 
 @pytest.mark.parametrize("name", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "newhope1024", "frodo976",
-                                  "mlkem512", "mlkem768", "mlkem1024", "newhope512"])
+                                  "mlkem512", "mlkem768", "mlkem1024", "newhope512", "frodo640", "frodo1344"])
 def test_restated_kem_vectors(oracle, name):
     g = load_golden("restated_%s.json" % name)
     alg = oracle.ALG_NAMES[name]
