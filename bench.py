@@ -58,8 +58,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--slots", type=int, default=12, help="serving: batches in flight (worker threads)")
     p.add_argument("--config", default=None,
-                   choices=["kyber512", "newhope1024", "frodo976", "newhope512", "mixed", "serving", "refgpu", "latency",
-                            "all"],
+                   choices=["kyber512", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344", "mixed", "serving",
+                            "refgpu", "latency", "all"],
                    help="measure another configuration (extra JSON lines) instead of the headline")
     return p.parse_args()
 
@@ -227,8 +227,8 @@ def run_configs(args):
     ctx = kem.Context(0)
     st = torch.cuda.ExternalStream(ctx.stream, device=dev)
     up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
-    which = (["kyber512", "newhope1024", "frodo976", "newhope512", "mixed", "serving", "refgpu", "latency"]
-             if args.config == "all" else [args.config])
+    which = (["kyber512", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344", "mixed", "serving", "refgpu",
+              "latency"] if args.config == "all" else [args.config])
 
     def timed(fn, reps):
         fn()
@@ -242,16 +242,17 @@ def run_configs(args):
         return e0.elapsed_time(e1) / reps
 
     for cfg in which:
-        if cfg in ("kyber512", "newhope1024", "frodo976", "newhope512"):
+        if cfg in ("kyber512", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344"):
             alg = cfg
-            n = {"kyber512": 65536, "newhope1024": 16384, "frodo976": 2048, "newhope512": 16384}[cfg]
+            n = {"kyber512": 65536, "newhope1024": 16384, "frodo976": 2048, "newhope512": 16384, "frodo640": 2048,
+                 "frodo1344": 2048}[cfg]
             s = kem.sizes(alg)
             seed = drbg.seed48(5)
             kc, ec = up(drbg.stream(seed, b"kp", n * s["kp_coins"])), up(drbg.stream(seed, b"enc", n * s["enc_coins"]))
             pk, sk, ct = (torch.empty(n * s[x], dtype=torch.uint8, device=dev) for x in ("pk", "sk", "ct"))
             ss, ss2 = (torch.empty(n * s["ss"], dtype=torch.uint8, device=dev) for _ in range(2))
             torch.cuda.synchronize()
-            reps = 3 if alg == "frodo976" else 10
+            reps = 3 if alg.startswith("frodo") else 10
             tk = timed(lambda: ctx.keypair_dev(alg, n, pk, sk, kc), reps)
             te = timed(lambda: ctx.enc_dev(alg, n, ct, ss, pk, ec), reps)
             td = timed(lambda: ctx.dec_dev(alg, n, ss2, ct, sk), reps)
@@ -348,7 +349,8 @@ def run_latency(ctx, dev, up, reps=50):
     from pqc_gb300 import drbg, kem
     st = torch.cuda.ExternalStream(ctx.stream, device=dev)
     out = {}
-    for alg in ("kyber512", "kyber768", "kyber1024", "mlkem768", "newhope1024", "newhope512", "frodo976"):
+    for alg in ("kyber512", "kyber768", "kyber1024", "mlkem768", "newhope1024", "newhope512", "frodo640", "frodo976",
+                "frodo1344"):
         s = kem.sizes(alg)
         seed = drbg.seed48(77)
         kc, ec = up(drbg.stream(seed, b"kp", s["kp_coins"])), up(drbg.stream(seed, b"enc", s["enc_coins"]))
