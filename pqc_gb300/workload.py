@@ -1,12 +1,14 @@
 """Fixed-size batched KEM workload on one GPU, for throughput checks and profiler captures.
 
     python -m pqc_gb300.workload --alg kyber768 --n 16384 --reps 2
+    python -m pqc_gb300.workload --alg newhope512,frodo640 --n 16384,256 --reps 1
 
-Generates n key pairs once, then runs `reps` rounds of encapsulation + decapsulation of n
-instances through the C ABI with device buffers (`PQCGPU_DEVICE_PTRS`), timing each operation with
-CUDA events on the library stream.  Inputs come from the seeded SHAKE-256 DRBG, so every run of the
-same command launches the same kernels on the same data.  Exits non-zero if any decapsulated key
-differs from the encapsulated one.
+For each algorithm in turn (a comma list, with one batch size each or one for all): generates n key
+pairs once, then runs `reps` rounds of encapsulation + decapsulation of n instances through the C
+ABI with device buffers (`PQCGPU_DEVICE_PTRS`), timing each operation with CUDA events on the
+library stream.  Inputs come from the seeded SHAKE-256 DRBG, so every run of the same command
+launches the same kernels on the same data.  Exits non-zero if any decapsulated key differs from
+the encapsulated one.
 """
 import argparse
 import sys
@@ -16,16 +18,7 @@ import torch
 from . import drbg, kem
 
 
-def main(argv=None):
-    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("--alg", default="kyber768", choices=sorted(kem.ALGS))
-    ap.add_argument("--n", type=int, default=16384)
-    ap.add_argument("--reps", type=int, default=2)
-    ap.add_argument("--ops", default="enc,dec", help="comma list of keypair, enc, dec to repeat")
-    ap.add_argument("--plain", action="store_true", help="per-stage path instead of the fused kernels")
-    args = ap.parse_args(argv)
-
-    n, alg = args.n, args.alg
+def run(alg, n, reps, want, fl):
     ctx = kem.Context(0)
     s = kem.sizes(alg)
     dev = torch.device("cuda:0")
@@ -42,7 +35,6 @@ def main(argv=None):
     ss = torch.empty(n * s["ss"], dtype=torch.uint8, device=dev)
     ss2 = torch.empty_like(ss)
     torch.cuda.synchronize()
-    fl = kem.PLAIN if args.plain else 0
     st = torch.cuda.ExternalStream(ctx.stream)
     ops = {
         "keypair": lambda: ctx.keypair_dev(alg, n, pk, sk, kc, fl),
@@ -51,12 +43,8 @@ def main(argv=None):
     }
     ops["keypair"]()
     ctx.wait()
-    want = [o for o in args.ops.split(",") if o]
-    for o in want:
-        if o not in ops:
-            ap.error("unknown op %r" % o)
     ok = True
-    for rep in range(args.reps):
+    for rep in range(reps):
         line = []
         for o in want:
             e0 = torch.cuda.Event(enable_timing=True)
@@ -73,6 +61,34 @@ def main(argv=None):
             ok = ok and same
             line.append("ss match %s" % same)
         print("%s n=%d rep %d: %s" % (alg, n, rep, ", ".join(line)), flush=True)
+    ctx.close()
+    return ok
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--alg", default="kyber768", help="algorithm or comma list of: " + ", ".join(sorted(kem.ALGS)))
+    ap.add_argument("--n", default="16384", help="batch size, or one per algorithm (comma list)")
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--ops", default="enc,dec", help="comma list of keypair, enc, dec to repeat")
+    ap.add_argument("--plain", action="store_true", help="per-stage path instead of the fused kernels")
+    args = ap.parse_args(argv)
+    algs = [a for a in args.alg.split(",") if a]
+    ns = [int(x) for x in args.n.split(",") if x]
+    if any(a not in kem.ALGS for a in algs):
+        ap.error("unknown algorithm in %r" % args.alg)
+    if len(ns) == 1:
+        ns = ns * len(algs)
+    if len(ns) != len(algs):
+        ap.error("give one batch size, or one per algorithm")
+    want = [o for o in args.ops.split(",") if o]
+    for o in want:
+        if o not in ("keypair", "enc", "dec"):
+            ap.error("unknown op %r" % o)
+    fl = kem.PLAIN if args.plain else 0
+    ok = True
+    for alg, n in zip(algs, ns):
+        ok = run(alg, n, args.reps, want, fl) and ok
     return 0 if ok else 1
 
 
