@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(256) nh_kp_core(KpArgs a, int NI) {
 
 // encryption: slots 0 s', 1 e' -> u-hat, 2 v'
 template <int N>
-__global__ void __launch_bounds__(256) nh_enc_core(EncArgs a, int NI) {
+__global__ void __launch_bounds__(256, 1) nh_enc_core(EncArgs a, int NI) {  // (256, 1): no register cap below 255 (the n = 512 instance spilled at 128)
     using P = Nh<N>;
     constexpr int NCH = P::NCH;
     extern __shared__ __align__(16) uint8_t smem[];
