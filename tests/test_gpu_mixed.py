@@ -62,11 +62,12 @@ def check(jobs, expected):
 def test_mixed_batch_all_algorithms(env):
     ctx, torch, dev = env
     rng = random.Random(5)
-    algs = ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "newhope1024", "frodo976"]
+    algs = ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "newhope1024", "frodo976", "mlkem768", "newhope512",
+            "frodo640", "frodo1344"]
     spec = []
     for alg in algs:
         for op in ("keypair", "enc", "dec"):
-            spec.append((alg, op, rng.randint(1, 3) if alg == "frodo976" else rng.randint(1, 700)))
+            spec.append((alg, op, rng.randint(1, 3) if alg.startswith("frodo") else rng.randint(1, 700)))
     rng.shuffle(spec)
     jobs, expected = build_jobs(ctx, torch, dev, spec, 3000)
     torch.cuda.synchronize()

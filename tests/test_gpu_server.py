@@ -20,7 +20,8 @@ def server():
 def test_keypair_enc_dec_match_batched_api(server):
     from pqc_gb300 import kem
     ctx = kem.Context(0)
-    for alg in ("kyber512", "kyber768", "kyber1024", "kyber1024r2", "newhope1024", "frodo976", "mlkem768"):
+    for alg in ("kyber512", "kyber768", "kyber1024", "kyber1024r2", "newhope1024", "frodo976", "mlkem768", "newhope512",
+                "frodo640", "frodo1344"):
         s = kem.sizes(alg)
         seed = drbg.seed48(hash(alg) & 0xffff)
         kc = drbg.stream(seed, b"kp", s["kp_coins"])
