@@ -15,6 +15,14 @@ Multi-GPU (torchrun): every rank runs an independent replica on its own GPU (KEM
 independent; no collective on the data path), `value` = pairs of all ranks / max rank time.
 --impl reference: times the CPU restatement of the same workload (the reference has no round-3
 Kyber-768 KEM code) on all host cores of rank 0 and prints the reference line.
+
+--config prints one line per configuration instead:
+* kyber512, newhope1024, frodo976, newhope512, frodo640, frodo1344: keypair / enc / dec rates;
+* mixed: concurrent mixed Kyber batches, stage kernels, graph replay;
+* serving: continuous batching at 10-90 % of the measured peak;
+* refgpu: the reference's own Kyber kernels recompiled for sm_103a, beside ours;
+* latency: single-instance latencies;
+* all: every one of them.
 """
 import argparse
 import json
