@@ -81,3 +81,29 @@ def test_host_path_with_a_small_budget(ctx, budget):
         assert small.dec(alg, n, ct, sk) == ss
     finally:
         small.close()
+
+
+def test_profile_trace_of_a_host_buffer_call(ctx):
+    """The Chrome-trace timeline of a chunked host-buffer call holds its copies in and out and its
+    kernels, on several streams, with well-formed times; reading it clears the records."""
+    from pqc_gb300 import kem
+    alg, n = "kyber768", 20000
+    s = kem.sizes(alg)
+    seed = drbg.seed48(31)
+    pk, _ = ctx.keypair(alg, n, drbg.stream(seed, b"kp", n * s["kp_coins"]))
+    kem.profile_trace()  # drop anything recorded before
+    kem.profile_enable(True)
+    try:
+        ctx.enc(alg, n, pk, drbg.stream(seed, b"enc", n * s["enc_coins"]))
+    finally:
+        kem.profile_enable(False)
+    ev = kem.profile_trace()["traceEvents"]
+    names = {e["name"] for e in ev}
+    assert {"copy H2D", "copy D2H", "kyber_enc_core<3,3>"} <= names
+    assert len({e["tid"] for e in ev}) >= 3  # copies in, copies out, compute streams
+    assert all(e["ph"] == "X" and e["ts"] >= 0 and e["dur"] >= 0 for e in ev)
+    assert min(e["ts"] for e in ev) == 0
+    # every chunk's kernels start after its copy in began
+    first_h2d = min(e["ts"] for e in ev if e["name"] == "copy H2D")
+    assert all(e["ts"] >= first_h2d for e in ev if e["name"].startswith("kyber_"))
+    assert kem.profile_trace() == {"traceEvents": []}
