@@ -67,6 +67,41 @@ __device__ __forceinline__ int16_t pair_zeta(const int16_t *sz, int p) {
     return (p & 1) ? (int16_t)-z : z;
 }
 
+// 32-bit forms for the NTTs.  The reference computes in int16, but no value of its transforms leaves
+// the int16 range (forward inputs |x| < q grow by at most q per layer: < 8q after 7 layers; the
+// inverse reduces every layer), so its truncations never take effect and the same arithmetic on
+// 32-bit values gives the same numbers without a sign extension after every add and subtract.
+// Only Montgomery's mod-2^16 step truncates.
+__device__ __forceinline__ int32_t fqmul32(int32_t a, int32_t b) {
+    const int32_t x = a * b;
+    const int32_t u = (int16_t)((uint32_t)x * 62209u);
+    return (x - u * Q) >> 16;
+}
+__device__ __forceinline__ int32_t barrett32(int32_t a) { return a - ((20159 * a) >> 26) * Q; }
+__device__ __forceinline__ void ct_bfly32(int32_t &a, int32_t &b, int32_t z) {
+    const int32_t t = fqmul32(z, b);
+    b = a - t;
+    a = a + t;
+}
+__device__ __forceinline__ void gs_bfly32(int32_t &a, int32_t &b, int32_t z) {
+    const int32_t t = a;
+    a = barrett32(t + b);
+    b = fqmul32(z, t - b);
+}
+__device__ __forceinline__ void load8(int32_t (&r)[8], const int16_t *p) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(p);
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        r[2 * i] = (int16_t)(w[i] & 0xffff);
+        r[2 * i + 1] = (int32_t)w[i] >> 16;
+    }
+}
+__device__ __forceinline__ void store8(int16_t *p, const int32_t (&r)[8]) {
+    auto pk2 = [](int32_t lo, int32_t hi) { return ((uint32_t)lo & 0xffffu) | ((uint32_t)hi << 16); };
+    *reinterpret_cast<uint4 *>(p) = make_uint4(pk2(r[0], r[1]), pk2(r[2], r[3]), pk2(r[4], r[5]), pk2(r[6], r[7]));
+}
+
 __device__ __forceinline__ void ct_bfly(int16_t &a, int16_t &b, int16_t z) {
     const int16_t t = fqmul(z, b);
     b = (int16_t)(a - t);
@@ -98,21 +133,21 @@ __device__ __forceinline__ void store8(int16_t *p, const int16_t (&r)[8]) {
 //   pass 3: lane = bits 7..3, registers = bits 2,1,0   -> layers len 4, 2, then Barrett
 // `sz` is the zetas table in shared memory (lane-dependent indices in passes 2 and 3).
 __device__ __forceinline__ void ntt_warp(int16_t *p, const int16_t *sz, int lane) {
-    int16_t r[8];
+    int32_t r[8];
 #pragma unroll
     for (int m = 0; m < 8; m++) r[m] = p[phys(32 * m + lane)];
     {
-        const int16_t z = sz[1];
+        const int32_t z = sz[1];
 #pragma unroll
-        for (int m = 0; m < 4; m++) ct_bfly(r[m], r[m + 4], z);
+        for (int m = 0; m < 4; m++) ct_bfly32(r[m], r[m + 4], z);
     }
 #pragma unroll
     for (int m = 0; m < 8; m++)
-        if (!(m & 2)) ct_bfly(r[m], r[m + 2], sz[2 + (m >> 2)]);
+        if (!(m & 2)) ct_bfly32(r[m], r[m + 2], sz[2 + (m >> 2)]);
 #pragma unroll
-    for (int m = 0; m < 8; m += 2) ct_bfly(r[m], r[m + 1], sz[4 + (m >> 1)]);
+    for (int m = 0; m < 8; m += 2) ct_bfly32(r[m], r[m + 1], sz[4 + (m >> 1)]);
 #pragma unroll
-    for (int m = 0; m < 8; m++) p[phys(32 * m + lane)] = r[m];
+    for (int m = 0; m < 8; m++) p[phys(32 * m + lane)] = (int16_t)r[m];
     __syncwarp();
 
     const int l65 = lane >> 3, l210 = lane & 7;
@@ -121,26 +156,26 @@ __device__ __forceinline__ void ntt_warp(int16_t *p, const int16_t *sz, int lane
         r[q] = p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)];
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        if (!(q & 2)) ct_bfly(r[q], r[q + 2], sz[8 + 4 * (q >> 2) + l65]);
+        if (!(q & 2)) ct_bfly32(r[q], r[q + 2], sz[8 + 4 * (q >> 2) + l65]);
 #pragma unroll
-    for (int q = 0; q < 8; q += 2) ct_bfly(r[q], r[q + 1], sz[16 + 8 * (q >> 2) + 2 * l65 + ((q >> 1) & 1)]);
+    for (int q = 0; q < 8; q += 2) ct_bfly32(r[q], r[q + 1], sz[16 + 8 * (q >> 2) + 2 * l65 + ((q >> 1) & 1)]);
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)] = r[q];
+        p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)] = (int16_t)r[q];
     __syncwarp();
 
     int16_t *p8 = p + phys(8 * lane);
     load8(r, p8);
     {
-        const int16_t z = sz[32 + lane];
+        const int32_t z = sz[32 + lane];
 #pragma unroll
-        for (int q = 0; q < 4; q++) ct_bfly(r[q], r[q + 4], z);
+        for (int q = 0; q < 4; q++) ct_bfly32(r[q], r[q + 4], z);
     }
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        if (!(q & 2)) ct_bfly(r[q], r[q + 2], sz[64 + 2 * lane + (q >> 2)]);
+        if (!(q & 2)) ct_bfly32(r[q], r[q + 2], sz[64 + 2 * lane + (q >> 2)]);
 #pragma unroll
-    for (int q = 0; q < 8; q++) r[q] = barrett(r[q]);
+    for (int q = 0; q < 8; q++) r[q] = barrett32(r[q]);
     store8(p8, r);
     __syncwarp();
 }
@@ -148,16 +183,16 @@ __device__ __forceinline__ void ntt_warp(int16_t *p, const int16_t *sz, int lane
 // Inverse NTT including the final multiplication by mont^2/128 (invntt, ntt.cu:194-224);
 // the passes mirror ntt_warp in reverse order.  `szi` is zetas_inv in shared memory.
 __device__ __forceinline__ void invntt_warp(int16_t *p, const int16_t *szi, int lane) {
-    int16_t r[8];
+    int32_t r[8];
     int16_t *p8 = p + phys(8 * lane);
     load8(r, p8);
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        if (!(q & 2)) gs_bfly(r[q], r[q + 2], szi[2 * lane + (q >> 2)]);
+        if (!(q & 2)) gs_bfly32(r[q], r[q + 2], szi[2 * lane + (q >> 2)]);
     {
-        const int16_t z = szi[64 + lane];
+        const int32_t z = szi[64 + lane];
 #pragma unroll
-        for (int q = 0; q < 4; q++) gs_bfly(r[q], r[q + 4], z);
+        for (int q = 0; q < 4; q++) gs_bfly32(r[q], r[q + 4], z);
     }
     store8(p8, r);
     __syncwarp();
@@ -167,30 +202,30 @@ __device__ __forceinline__ void invntt_warp(int16_t *p, const int16_t *szi, int 
     for (int q = 0; q < 8; q++)
         r[q] = p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)];
 #pragma unroll
-    for (int q = 0; q < 8; q += 2) gs_bfly(r[q], r[q + 1], szi[96 + 8 * (q >> 2) + 2 * l65 + ((q >> 1) & 1)]);
+    for (int q = 0; q < 8; q += 2) gs_bfly32(r[q], r[q + 1], szi[96 + 8 * (q >> 2) + 2 * l65 + ((q >> 1) & 1)]);
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        if (!(q & 2)) gs_bfly(r[q], r[q + 2], szi[112 + 4 * (q >> 2) + l65]);
+        if (!(q & 2)) gs_bfly32(r[q], r[q + 2], szi[112 + 4 * (q >> 2) + l65]);
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)] = r[q];
+        p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)] = (int16_t)r[q];
     __syncwarp();
 
 #pragma unroll
     for (int m = 0; m < 8; m++) r[m] = p[phys(32 * m + lane)];
 #pragma unroll
-    for (int m = 0; m < 8; m += 2) gs_bfly(r[m], r[m + 1], szi[120 + (m >> 1)]);
+    for (int m = 0; m < 8; m += 2) gs_bfly32(r[m], r[m + 1], szi[120 + (m >> 1)]);
 #pragma unroll
     for (int m = 0; m < 8; m++)
-        if (!(m & 2)) gs_bfly(r[m], r[m + 2], szi[124 + (m >> 2)]);
+        if (!(m & 2)) gs_bfly32(r[m], r[m + 2], szi[124 + (m >> 2)]);
     {
-        const int16_t z = szi[126];
+        const int32_t z = szi[126];
 #pragma unroll
-        for (int m = 0; m < 4; m++) gs_bfly(r[m], r[m + 4], z);
+        for (int m = 0; m < 4; m++) gs_bfly32(r[m], r[m + 4], z);
     }
-    const int16_t f = szi[127];
+    const int32_t f = szi[127];
 #pragma unroll
-    for (int m = 0; m < 8; m++) p[phys(32 * m + lane)] = fqmul(r[m], f);
+    for (int m = 0; m < 8; m++) p[phys(32 * m + lane)] = (int16_t)fqmul32(r[m], f);
     __syncwarp();
 }
 
