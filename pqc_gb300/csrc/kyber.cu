@@ -65,6 +65,7 @@ int kyber_set_shape(int op, int k, int ni, int threads) {
     if (op < 0 || op > 3 || k < 2 || k > 4 || ni <= 0 || ni > 128 || threads < 32 || threads > 512 || threads % 32)
         return PQCGPU_EINVAL;
     if (op == 3) {  // decapsulation, decryption stage: NI instances' polynomials, no staging
+        if (threads > 384) return PQCGPU_EINVAL;  // the stage kernel's launch bound
         const size_t sm1 = (k == 2 ? kyber::smem_2_3(2, ni, 0) : k == 3 ? kyber::smem_3_3(2, ni, 0) : kyber::smem_4_3(2, ni, 0));
         if (sm1 > MAX_SMEM_PER_CTA) return PQCGPU_EINVAL;
         kyber::g_dec1[k - 2][0] = ni;

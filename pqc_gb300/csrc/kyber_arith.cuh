@@ -88,6 +88,13 @@ __device__ __forceinline__ void gs_bfly32(int32_t &a, int32_t &b, int32_t z) {
     a = barrett32(t + b);
     b = fqmul32(z, t - b);
 }
+// basemul of the 32-bit forms: each Montgomery product is below q in magnitude, so r0 < 2q and
+// r1 < 2q, the bounds of the reference's int16 basemul, and sums of K <= 4 of them stay below 8q.
+__device__ __forceinline__ void basemul32(int32_t &r0, int32_t &r1, int32_t a0, int32_t a1, int32_t b0, int32_t b1,
+                                          int32_t zeta) {
+    r0 = fqmul32(fqmul32(a1, b1), zeta) + fqmul32(a0, b0);
+    r1 = fqmul32(a0, b1) + fqmul32(a1, b0);
+}
 __device__ __forceinline__ void load8(int32_t (&r)[8], const int16_t *p) {
     const uint4 v = *reinterpret_cast<const uint4 *>(p);
     const uint32_t w[4] = {v.x, v.y, v.z, v.w};

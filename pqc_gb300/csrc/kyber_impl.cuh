@@ -223,8 +223,12 @@ __device__ __forceinline__ void matrix_entry(const uint2 *rho, int row, int col,
 
 // Undo the accumulator bias of K terms and apply pointwise_acc's Barrett.
 template <int K>
-__device__ __forceinline__ int16_t unbias(int16_t biased) {
-    return barrett((int16_t)((int)(uint16_t)biased - (int)(K * ACC_BIAS)));
+__device__ __forceinline__ int32_t unbias(int32_t biased) {
+    return barrett32((biased & 0xffff) - (int32_t)(K * ACC_BIAS));
+}
+__device__ __forceinline__ int32_t csubq32(int32_t a) {
+    a -= Q;
+    return a + ((a >> 31) & Q);
 }
 
 // Zero `npoly` consecutive shared polynomials starting at p (all threads of the CTA).
@@ -238,10 +242,12 @@ __device__ __forceinline__ void zero_polys(int16_t *p, int npoly) {
 // Codecs (warp per instance, lane = group of 8 coefficients)
 // ---------------------------------------------------------------------------------------------
 template <int D>
-__device__ __forceinline__ uint32_t compress_d(int16_t x) {
+__device__ __forceinline__ uint32_t compress_u(uint32_t x) {
     // x canonical in [0, q)
-    return ((((uint32_t)(uint16_t)x << D) + Q / 2) / Q) & ((1u << D) - 1);
+    return (((x << D) + Q / 2) / Q) & ((1u << D) - 1);
 }
+template <int D>
+__device__ __forceinline__ uint32_t compress_d(int16_t x) { return compress_u<D>((uint16_t)x); }
 template <int D>
 __device__ __forceinline__ int16_t decompress_d(uint32_t t) {
     return (int16_t)((t * Q + (1u << (D - 1))) >> D);
@@ -368,11 +374,27 @@ __device__ __forceinline__ void tobytes8(uint8_t *out, const int16_t (&c)[8]) {
         out[3 * i + 2] = (uint8_t)(t1 >> 4);
     }
 }
+__device__ __forceinline__ void tobytes8(uint8_t *out, const int32_t (&c)[8]) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const uint32_t t0 = (uint32_t)c[2 * i], t1 = (uint32_t)c[2 * i + 1];
+        out[3 * i] = (uint8_t)t0;
+        out[3 * i + 1] = (uint8_t)((t0 >> 8) | (t1 << 4));
+        out[3 * i + 2] = (uint8_t)(t1 >> 4);
+    }
+}
 __device__ __forceinline__ void frombytes8(int16_t (&c)[8], const uint8_t *in) {
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         c[2 * i] = (int16_t)(in[3 * i] | (((uint16_t)in[3 * i + 1] & 0x0f) << 8));
         c[2 * i + 1] = (int16_t)((in[3 * i + 1] >> 4) | ((uint16_t)in[3 * i + 2] << 4));
+    }
+}
+__device__ __forceinline__ void frombytes8(int32_t (&c)[8], const uint8_t *in) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        c[2 * i] = in[3 * i] | ((in[3 * i + 1] & 0x0f) << 8);
+        c[2 * i + 1] = (in[3 * i + 1] >> 4) | (in[3 * i + 2] << 4);
     }
 }
 
@@ -549,6 +571,7 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
 // Kernels
 // ---------------------------------------------------------------------------------------------
 constexpr int CORE_MAX_THREADS = 512;
+constexpr int DEC1_MAX_THREADS = 384;
 
 // Encapsulation of instances [base, base + NI) of `a` by the calling CTA (dynamic shared memory
 // laid out for NI instances of this K).
@@ -611,19 +634,20 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
     // (c) mp = s-hat o u-hat -> slot 0
     for (int li = warp; li < ni; li += nwarp) {
         const uint8_t *sk = d.sk + (size_t)(base + li) * sks;
-        int16_t acc[8];
+        int32_t acc[8];
         for (int j = 0; j < K; j++) {
-            int16_t s[8], b[8], r[8];
+            int32_t s[8], b[8], r[8];
             frombytes8(s, sk + 384 * j + 12 * lane);
             load8(b, slot<K, V>(polys, li, K + j) + phys(8 * lane));
 #pragma unroll
-            for (int q = 0; q < 4; q++) basemul(r[2 * q], r[2 * q + 1], s[2 * q], s[2 * q + 1], b[2 * q], b[2 * q + 1],
-                                                 pair_zeta(sz, 4 * lane + q));
+            for (int q = 0; q < 4; q++)
+                basemul32(r[2 * q], r[2 * q + 1], s[2 * q], s[2 * q + 1], b[2 * q], b[2 * q + 1],
+                          pair_zeta(sz, 4 * lane + q));
 #pragma unroll
-            for (int q = 0; q < 8; q++) acc[q] = (j == 0) ? r[q] : (int16_t)(acc[q] + r[q]);
+            for (int q = 0; q < 8; q++) acc[q] = (j == 0) ? r[q] : acc[q] + r[q];
         }
 #pragma unroll
-        for (int q = 0; q < 8; q++) acc[q] = barrett(acc[q]);
+        for (int q = 0; q < 8; q++) acc[q] = barrett32(acc[q]);
         store8(slot<K, V>(polys, li, 0) + phys(8 * lane), acc);
     }
     __syncthreads();
@@ -631,15 +655,12 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
     __syncthreads();
     // (d) m' = tomsg(reduce(v - mp)), lane = message byte
     for (int li = warp; li < ni; li += nwarp) {
-        int16_t v[8], mp[8];
+        int32_t v[8], mp[8];
         load8(v, slot<K, V>(polys, li, 2 * K) + phys(8 * lane));
         load8(mp, slot<K, V>(polys, li, 0) + phys(8 * lane));
         uint32_t byte = 0;
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-            const int16_t x = csubq(barrett((int16_t)(v[q] - mp[q])));
-            byte |= (((((uint32_t)x << 1) + Q / 2) / Q) & 1) << q;
-        }
+        for (int q = 0; q < 8; q++) byte |= compress_u<1>((uint32_t)csubq32(barrett32(v[q] - mp[q]))) << q;
         seeds[li * SB + lane] = (uint8_t)byte;
         if (!d.kem) d.m_out[(size_t)(base + li) * 32 + lane] = (uint8_t)byte;
     }
@@ -734,6 +755,12 @@ template <int K, int V, int STAGE>
 __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, int NI) {
     dec_core_body<K, V, STAGE>(d, NI, blockIdx.x * NI);
 }
+// The decryption stage alone: up to DEC1_MAX_THREADS threads, with the register budget of two such
+// CTAs per SM (80 a thread), so that its 384-thread shapes keep two CTAs per SM.
+template <int K, int V>
+__global__ void __launch_bounds__(DEC1_MAX_THREADS, 2) kyber_dec_decrypt(DecArgs d, int NI) {
+    dec_core_body<K, V, DEC_DECRYPT>(d, NI, blockIdx.x * NI);
+}
 
 
 // Keypair: slots [0,K) s, [K,2K) e, [2K,3K) t-hat; seeds [0,32) rho, [32,64) sigma.
@@ -786,14 +813,14 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int 
         uint8_t *pk = a.pk + (size_t)(base + li) * Pp::PKB;
         uint8_t *sk = a.sk + (size_t)(base + li) * (a.kem ? Pp::SKB : Pp::SKCPA);
         for (int i = 0; i < K; i++) {
-            int16_t t[8], e[8], s[8];
+            int32_t t[8], e[8], s[8];
             load8(t, kslot(li, 2 * K + i) + phys(8 * lane));
             load8(e, kslot(li, K + i) + phys(8 * lane));
             load8(s, kslot(li, i) + phys(8 * lane));
 #pragma unroll
             for (int q = 0; q < 8; q++) {
-                t[q] = csubq(barrett((int16_t)(mont_reduce((int32_t)unbias<K>(t[q]) * 1353) + e[q])));
-                s[q] = csubq(s[q]);
+                t[q] = csubq32(barrett32(fqmul32(unbias<K>(t[q]), 1353) + e[q]));
+                s[q] = csubq32(s[q]);
             }
             uint8_t bt[12], bs[12];
             tobytes8(bt, t);
@@ -1040,7 +1067,7 @@ template <int K, int V>
 static void prefer_shared_all() {
     prefer_shared(kyber_enc_core<K, V>);
     prefer_shared(kyber_dec_core<K, V, DEC_FUSED>);
-    prefer_shared(kyber_dec_core<K, V, DEC_DECRYPT>);
+    prefer_shared(kyber_dec_decrypt<K, V>);
     prefer_shared(kyber_dec_core<K, V, DEC_REENCRYPT>);
     prefer_shared(kyber_kp_core<K, V>);
     prefer_shared(kyber_enc_hash_pre<K, V>);
@@ -1153,10 +1180,10 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
                    kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, sk, scratch, kem));
     const int NI1 = g_dec1[K - 2][0], NT1 = g_dec1[K - 2][1];
     const size_t sm1 = Layout<2 * K + 1, enc_seed_bytes<K, V>()>::bytes(NI1, 0);
-    if (ensure_smem(kyber_dec_core<K, V, DEC_DECRYPT>, sm1) != cudaSuccess) return PQCGPU_ECUDA;
+    if (ensure_smem(kyber_dec_decrypt<K, V>, sm1) != cudaSuccess) return PQCGPU_ECUDA;
     if (ensure_smem(kyber_dec_core<K, V, DEC_REENCRYPT>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     PQC_LAUNCH(st, "kyber_dec_decrypt", K, V,
-               kyber_dec_core<K, V, DEC_DECRYPT><<<(n + NI1 - 1) / NI1, NT1, sm1, st>>>(d, NI1));
+               kyber_dec_decrypt<K, V><<<(n + NI1 - 1) / NI1, NT1, sm1, st>>>(d, NI1));
     PQC_LAUNCH(st, "kyber_dec_reencrypt", K, V,
                kyber_dec_core<K, V, DEC_REENCRYPT><<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
