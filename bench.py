@@ -17,7 +17,8 @@ independent; no collective on the data path), `value` = pairs of all ranks / max
 Kyber-768 KEM code) on all host cores of rank 0 and prints the reference line.
 
 --config prints one line per configuration instead:
-* kyber512, newhope1024, frodo976, newhope512, frodo640, frodo1344: keypair / enc / dec rates;
+* kyber512, kyber1024, newhope1024, frodo976, newhope512, frodo640, frodo1344: keypair / enc / dec
+  rates;
 * mixed: concurrent mixed Kyber batches, stage kernels, graph replay;
 * serving: continuous batching at 10-90 % of the measured peak;
 * refgpu: the reference's own Kyber kernels recompiled for sm_103a, beside ours;
@@ -66,7 +67,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--slots", type=int, default=12, help="serving: batches in flight (worker threads)")
     p.add_argument("--config", default=None,
-                   choices=["kyber512", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344", "mixed", "serving",
+                   choices=["kyber512", "kyber1024", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344", "mixed", "serving",
                             "refgpu", "latency", "all"],
                    help="measure another configuration (extra JSON lines) instead of the headline")
     return p.parse_args()
@@ -235,7 +236,7 @@ def run_configs(args):
     ctx = kem.Context(0)
     st = torch.cuda.ExternalStream(ctx.stream, device=dev)
     up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
-    which = (["kyber512", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344", "mixed", "serving", "refgpu",
+    which = (["kyber512", "kyber1024", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344", "mixed", "serving", "refgpu",
               "latency"] if args.config == "all" else [args.config])
 
     def timed(fn, reps):
@@ -250,9 +251,9 @@ def run_configs(args):
         return e0.elapsed_time(e1) / reps
 
     for cfg in which:
-        if cfg in ("kyber512", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344"):
+        if cfg in ("kyber512", "kyber1024", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344"):
             alg = cfg
-            n = {"kyber512": 65536, "newhope1024": 16384, "frodo976": 2048, "newhope512": 16384, "frodo640": 2048,
+            n = {"kyber512": 65536, "kyber1024": 65536, "newhope1024": 16384, "frodo976": 2048, "newhope512": 16384, "frodo640": 2048,
                  "frodo1344": 2048}[cfg]
             s = kem.sizes(alg)
             seed = drbg.seed48(5)

@@ -230,8 +230,9 @@ int pqcgpu_server_run_poisson(pqcgpu_server *server, const pqcgpu_mix_entry *mix
 /* ---- launch-shape tuning (used by the autotuner, pqc_gb300/autotune.py) --------------------
  * Core-kernel launch shape per (algorithm, operation): ni = instances per CTA, threads per CTA
  * (multiple of 32).  Kyber also takes op 3: the decryption stage of decapsulation (op 2 is then
- * its re-encryption stage).  Kyber: ni 1..128, threads 32..512, 32..384 for op 3 (shared by the round-2
- * and round-3 sets of the same k); NewHope: ni 1..64, threads 32..256.  FrodoKEM: keypair ni 0 or 1, threads 64 / 128 /
+ * its re-encryption stage).  Kyber: ni 1..128, threads from 32 up to the core kernel's launch bound
+ * (keypair 512, encapsulation 256, re-encryption 192 for k = 3 and 256 otherwise, decryption stage
+ * 384; shared by the round-2 and round-3 sets of the same k); NewHope: ni 1..64, threads 32..256.  FrodoKEM: keypair ni 0 or 1, threads 64 / 128 /
  * 256 (one row of A per thread); encaps / decaps ni = CTAs per instance sharing the rows of A
  * (1, 2, 4, 8, 16) with threads 128 / 256, or ni = 0 to choose by batch size (the default).
  * Applies to all contexts of the process. */

@@ -6,9 +6,9 @@ namespace kyber {
 // Launch shape of the core kernels, [op][k-2] with op 0 keypair, 1 enc, 2 dec (its re-encryption
 // stage).  One thread per matrix entry (NI * k^2 jobs) sized against the shared memory each instance
 // needs.  g_dec1: the decryption stage of decapsulation.  Defaults: the autotuner's GB300 optimum.
-int g_ni[3][3] = {{16, 14, 8}, {28, 14, 14}, {28, 18, 14}};
-int g_threads[3][3] = {{64, 160, 128}, {128, 128, 256}, {128, 192, 256}};
-int g_dec1[3][2] = {{32, 384}, {24, 384}, {6, 128}};
+int g_ni[3][3] = {{16, 10, 8}, {28, 12, 8}, {24, 12, 8}};
+int g_threads[3][3] = {{64, 96, 128}, {128, 128, 128}, {128, 128, 128}};
+int g_dec1[3][2] = {{32, 384}, {23, 384}, {12, 256}};
 
 #define PQC_KYBER_DECL(K, V)                                                                               \
     int keypair_##K##_##V(int, uint8_t *, uint8_t *, const uint8_t *, int, int, uint8_t *, int, cudaStream_t); \
@@ -62,10 +62,10 @@ int kyber_init_constants() {
     return kyber_mixed_init();
 }
 int kyber_set_shape(int op, int k, int ni, int threads) {
-    if (op < 0 || op > 3 || k < 2 || k > 4 || ni <= 0 || ni > 128 || threads < 32 || threads > 512 || threads % 32)
+    if (op < 0 || op > 3 || k < 2 || k > 4 || ni <= 0 || ni > 128 || threads < 32 || threads % 32 ||
+        threads > kyber_bound_threads(op, k))
         return PQCGPU_EINVAL;
     if (op == 3) {  // decapsulation, decryption stage: NI instances' polynomials, no staging
-        if (threads > 384) return PQCGPU_EINVAL;  // the stage kernel's launch bound
         const size_t sm1 = (k == 2 ? kyber::smem_2_3(2, ni, 0) : k == 3 ? kyber::smem_3_3(2, ni, 0) : kyber::smem_4_3(2, ni, 0));
         if (sm1 > MAX_SMEM_PER_CTA) return PQCGPU_EINVAL;
         kyber::g_dec1[k - 2][0] = ni;

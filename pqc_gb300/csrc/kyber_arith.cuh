@@ -1,9 +1,14 @@
 // Kyber modular arithmetic and warp-cooperative NTT for sm_103a.
 //
-// The reductions are the reference's (Kyber_GPU_Batched/reduce.cu:21-66): Montgomery with
-// R = 2^16 and QINV = 62209, Barrett with v = floor(2^26 / q) + 1, conditional subtraction.
-// The butterflies follow ntt.cu:152-259 operation for operation (int16 wrap-around included), so
-// every intermediate coefficient equals the reference's.
+// Two families.  The int16 functions are the reference's (Kyber_GPU_Batched/reduce.cu:21-66:
+// Montgomery with R = 2^16 and QINV = 62209, Barrett with v = floor(2^26 / q) + 1, conditional
+// subtraction; ntt.cu:152-259 butterflies) and serve the per-stage path.  The fused kernels use
+// plain residues with reductions that run on the multiply pipe (IMAD / IMAD.HI) instead of the
+// integer ALU, which Keccak saturates: multiplication by a twiddle is Shoup's multiplication by a
+// precomputed constant and a product is reduced by a Barrett high multiply.  These compute the same polynomials modulo q as the reference, with other representatives
+// in between; every value that leaves a kernel (packed keys, compressed ciphertexts, messages) is
+// first brought to [0, q) by the reference's Barrett and conditional subtraction, so the bytes are
+// the reference's.
 #pragma once
 #include <stdint.h>
 
@@ -16,6 +21,10 @@ constexpr int POLY_PITCH = 296;  // int16 per shared-memory polynomial (256 + 8 
 
 static __constant__ int16_t c_zetas[128];
 static __constant__ int16_t c_zetas_inv[128];
+// Twiddles of the fused kernels as Shoup pairs {w, floor(w 2^32 / q)}, w the representative of the
+// plain twiddle in (-q/2, q/2); entry 127 of the inverse table is 1/128 mod q.
+static __constant__ int2 c_tw[128];
+static __constant__ int2 c_twi[128];
 
 // zetas[i] = MONT * 17^brv7(i) mod q and the inverse-NTT table of the reference's generation
 // recipe (Kyber_GPU_Batched/ntt.cu:8-48), computed on the host at init.
@@ -31,6 +40,29 @@ static inline void kyber_twiddles_host(int16_t zetas[128], int16_t zetas_inv[128
     for (int i = 64; i >= 1; i >>= 1)
         for (int j = i; j < 2 * i; j++) zetas_inv[k++] = modq(-MONT * pw[128 - brv7(j)]);
     zetas_inv[127] = (int16_t)((MONT * ((MONT * (Q - 1) * ((Q - 1) / 128)) % Q)) % Q);
+}
+
+// Plain twiddles of the forward and inverse NTT (the reference's tables without the Montgomery
+// factor) as Shoup pairs, and 1/128 for the end of the inverse transform.
+static inline void kyber_twiddles_shoup_host(int2 tw[128], int2 twi[128]) {
+    long pw[129];
+    pw[0] = 1;
+    for (int i = 1; i <= 128; i++) pw[i] = (pw[i - 1] * 17) % Q;
+    auto brv7 = [](int x) { int r = 0; for (int i = 0; i < 7; i++) r |= ((x >> i) & 1) << (6 - i); return r; };
+    auto pair = [](long v) {
+        long w = v % Q;
+        if (w < 0) w += Q;
+        if (w > Q / 2) w -= Q;
+        const long long num = (long long)w << 32;
+        long long ws = num / Q;
+        if (num % Q != 0 && num < 0) ws -= 1;  // floor
+        return make_int2((int)w, (int)ws);
+    };
+    for (int i = 0; i < 128; i++) tw[i] = pair(pw[brv7(i)]);
+    int k = 0;
+    for (int i = 64; i >= 1; i >>= 1)
+        for (int j = i; j < 2 * i; j++) twi[k++] = pair(-pw[128 - brv7(j)]);
+    twi[127] = pair(3303);  // 128 * 3303 = 1 mod q
 }
 
 __device__ __forceinline__ int16_t mont_reduce(int32_t a) {
@@ -67,6 +99,13 @@ __device__ __forceinline__ int16_t pair_zeta(const int16_t *sz, int p) {
     return (p & 1) ? (int16_t)-z : z;
 }
 
+// Plain twiddle of coefficient pair p for the fused kernels' basemul: +w[64 + p/2] for even p, minus
+// for odd.
+__device__ __forceinline__ int32_t pair_w(const int2 *tw, int p) {
+    const int32_t w = tw[64 + (p >> 1)].x;
+    return (p & 1) ? -w : w;
+}
+
 // 32-bit forms for the NTTs.  The reference computes in int16, but no value of its transforms leaves
 // the int16 range (forward inputs |x| < q grow by at most q per layer: < 8q after 7 layers; the
 // inverse reduces every layer), so its truncations never take effect and the same arithmetic on
@@ -94,6 +133,37 @@ __device__ __forceinline__ void basemul32(int32_t &r0, int32_t &r1, int32_t a0, 
                                           int32_t zeta) {
     r0 = fqmul32(fqmul32(a1, b1), zeta) + fqmul32(a0, b0);
     r1 = fqmul32(a0, b1) + fqmul32(a1, b0);
+}
+// Multiplication by a twiddle (Shoup, "NTL: MulModPrecon"): for |b| < 2^15 the estimated quotient
+// floor(b w' / 2^32), w' = floor(w 2^32 / q), is off by less than 2^-17, so the result is the
+// representative of b w in [0, q].  Three multiply-pipe instructions.
+__device__ __forceinline__ int32_t mulc(int32_t b, int2 w) { return b * w.x - __mulhi(b, w.y) * Q; }
+// Barrett reduction of a product sum |x| < 2^25 by a high multiply with floor(2^32 / q): result in
+// [-11, q + 11].
+__device__ __forceinline__ int32_t red_prod(int32_t x) { return x - __mulhi(x, 1290167) * Q; }
+// The reference's Barrett, floor(20159 a / 2^26) taken as the high word of a * (20159 * 2^6):
+// the same quotient, result in [0, q].
+__device__ __forceinline__ int32_t barrett_hi(int32_t a) { return a - __mulhi(a, 20159 << 6) * Q; }
+// basemul in Z_q[X]/(X^2 - zeta) on plain residues (ntt.cu:249-259 without the Montgomery factor):
+// one reduction per product sum.  |a| < 2^12 (packed 12-bit or sampled coefficients), b in [0, q]
+// (reduced NTT output), |zeta| < q/2: results in [-11, q + 11].
+__device__ __forceinline__ void basemul_plain(int32_t &r0, int32_t &r1, int32_t a0, int32_t a1, int32_t b0, int32_t b1,
+                                              int32_t zeta) {
+    r0 = red_prod(red_prod(a1 * b1) * zeta + a0 * b0);
+    r1 = red_prod(a0 * b1 + a1 * b0);
+}
+// Forward butterfly: t in [0, q], so a coefficient grows by at most q a layer (< 8q after seven
+// layers from |x| <= q, within int16 for the shared-memory passes).
+__device__ __forceinline__ void ct_bfly_s(int32_t &a, int32_t &b, int2 w) {
+    const int32_t t = mulc(b, w);
+    b = a - t;
+    a = a + t;
+}
+// Inverse butterfly (ntt.cu:194-224 without the Montgomery factor): both outputs in [0, q].
+__device__ __forceinline__ void gs_bfly_s(int32_t &a, int32_t &b, int2 w) {
+    const int32_t t = a;
+    a = barrett_hi(t + b);
+    b = mulc(t - b, w);
 }
 __device__ __forceinline__ void load8(int32_t (&r)[8], const int16_t *p) {
     const uint4 v = *reinterpret_cast<const uint4 *>(p);
@@ -133,26 +203,27 @@ __device__ __forceinline__ void store8(int16_t *p, const int16_t (&r)[8]) {
     *reinterpret_cast<uint4 *>(p) = make_uint4(pack2(r[0], r[1]), pack2(r[2], r[3]), pack2(r[4], r[5]), pack2(r[6], r[7]));
 }
 
-// Forward NTT + Barrett (poly_ntt, poly.cu:153-157) of one shared-memory polynomial by one warp.
+// Forward NTT + Barrett (poly_ntt, poly.cu:153-157) of one shared-memory polynomial by one warp,
+// on plain residues (output in [0, q]).
 // Three passes, each doing the butterflies of a 3-bit (or 2-bit) slice of the index in registers:
 //   pass 1: lane = bits 4..0, registers = bits 7,6,5   -> layers len 128, 64, 32
 //   pass 2: lane = bits 6,5,2,1,0, registers = 7,4,3   -> layers len 16, 8
 //   pass 3: lane = bits 7..3, registers = bits 2,1,0   -> layers len 4, 2, then Barrett
-// `sz` is the zetas table in shared memory (lane-dependent indices in passes 2 and 3).
-__device__ __forceinline__ void ntt_warp(int16_t *p, const int16_t *sz, int lane) {
+// `tw` is the twiddle table in shared memory (lane-dependent indices in passes 2 and 3).
+__device__ __forceinline__ void ntt_warp(int16_t *p, const int2 *tw, int lane) {
     int32_t r[8];
 #pragma unroll
     for (int m = 0; m < 8; m++) r[m] = p[phys(32 * m + lane)];
     {
-        const int32_t z = sz[1];
+        const int2 z = tw[1];
 #pragma unroll
-        for (int m = 0; m < 4; m++) ct_bfly32(r[m], r[m + 4], z);
+        for (int m = 0; m < 4; m++) ct_bfly_s(r[m], r[m + 4], z);
     }
 #pragma unroll
     for (int m = 0; m < 8; m++)
-        if (!(m & 2)) ct_bfly32(r[m], r[m + 2], sz[2 + (m >> 2)]);
+        if (!(m & 2)) ct_bfly_s(r[m], r[m + 2], tw[2 + (m >> 2)]);
 #pragma unroll
-    for (int m = 0; m < 8; m += 2) ct_bfly32(r[m], r[m + 1], sz[4 + (m >> 1)]);
+    for (int m = 0; m < 8; m += 2) ct_bfly_s(r[m], r[m + 1], tw[4 + (m >> 1)]);
 #pragma unroll
     for (int m = 0; m < 8; m++) p[phys(32 * m + lane)] = (int16_t)r[m];
     __syncwarp();
@@ -163,9 +234,9 @@ __device__ __forceinline__ void ntt_warp(int16_t *p, const int16_t *sz, int lane
         r[q] = p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)];
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        if (!(q & 2)) ct_bfly32(r[q], r[q + 2], sz[8 + 4 * (q >> 2) + l65]);
+        if (!(q & 2)) ct_bfly_s(r[q], r[q + 2], tw[8 + 4 * (q >> 2) + l65]);
 #pragma unroll
-    for (int q = 0; q < 8; q += 2) ct_bfly32(r[q], r[q + 1], sz[16 + 8 * (q >> 2) + 2 * l65 + ((q >> 1) & 1)]);
+    for (int q = 0; q < 8; q += 2) ct_bfly_s(r[q], r[q + 1], tw[16 + 8 * (q >> 2) + 2 * l65 + ((q >> 1) & 1)]);
 #pragma unroll
     for (int q = 0; q < 8; q++)
         p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)] = (int16_t)r[q];
@@ -174,32 +245,33 @@ __device__ __forceinline__ void ntt_warp(int16_t *p, const int16_t *sz, int lane
     int16_t *p8 = p + phys(8 * lane);
     load8(r, p8);
     {
-        const int32_t z = sz[32 + lane];
+        const int2 z = tw[32 + lane];
 #pragma unroll
-        for (int q = 0; q < 4; q++) ct_bfly32(r[q], r[q + 4], z);
+        for (int q = 0; q < 4; q++) ct_bfly_s(r[q], r[q + 4], z);
     }
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        if (!(q & 2)) ct_bfly32(r[q], r[q + 2], sz[64 + 2 * lane + (q >> 2)]);
+        if (!(q & 2)) ct_bfly_s(r[q], r[q + 2], tw[64 + 2 * lane + (q >> 2)]);
 #pragma unroll
-    for (int q = 0; q < 8; q++) r[q] = barrett32(r[q]);
+    for (int q = 0; q < 8; q++) r[q] = barrett_hi(r[q]);
     store8(p8, r);
     __syncwarp();
 }
 
-// Inverse NTT including the final multiplication by mont^2/128 (invntt, ntt.cu:194-224);
-// the passes mirror ntt_warp in reverse order.  `szi` is zetas_inv in shared memory.
-__device__ __forceinline__ void invntt_warp(int16_t *p, const int16_t *szi, int lane) {
+// Inverse NTT including the final multiplication by 1/128 (invntt, ntt.cu:194-224, whose mont^2/128
+// also undoes the Montgomery factor of its basemul); the passes mirror ntt_warp in reverse order.
+// `twi` is the inverse twiddle table in shared memory.  Output in [0, q].
+__device__ __forceinline__ void invntt_warp(int16_t *p, const int2 *twi, int lane) {
     int32_t r[8];
     int16_t *p8 = p + phys(8 * lane);
     load8(r, p8);
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        if (!(q & 2)) gs_bfly32(r[q], r[q + 2], szi[2 * lane + (q >> 2)]);
+        if (!(q & 2)) gs_bfly_s(r[q], r[q + 2], twi[2 * lane + (q >> 2)]);
     {
-        const int32_t z = szi[64 + lane];
+        const int2 z = twi[64 + lane];
 #pragma unroll
-        for (int q = 0; q < 4; q++) gs_bfly32(r[q], r[q + 4], z);
+        for (int q = 0; q < 4; q++) gs_bfly_s(r[q], r[q + 4], z);
     }
     store8(p8, r);
     __syncwarp();
@@ -209,10 +281,10 @@ __device__ __forceinline__ void invntt_warp(int16_t *p, const int16_t *szi, int 
     for (int q = 0; q < 8; q++)
         r[q] = p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)];
 #pragma unroll
-    for (int q = 0; q < 8; q += 2) gs_bfly32(r[q], r[q + 1], szi[96 + 8 * (q >> 2) + 2 * l65 + ((q >> 1) & 1)]);
+    for (int q = 0; q < 8; q += 2) gs_bfly_s(r[q], r[q + 1], twi[96 + 8 * (q >> 2) + 2 * l65 + ((q >> 1) & 1)]);
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        if (!(q & 2)) gs_bfly32(r[q], r[q + 2], szi[112 + 4 * (q >> 2) + l65]);
+        if (!(q & 2)) gs_bfly_s(r[q], r[q + 2], twi[112 + 4 * (q >> 2) + l65]);
 #pragma unroll
     for (int q = 0; q < 8; q++)
         p[phys(128 * (q >> 2) + 32 * l65 + 16 * ((q >> 1) & 1) + 8 * (q & 1) + l210)] = (int16_t)r[q];
@@ -221,18 +293,18 @@ __device__ __forceinline__ void invntt_warp(int16_t *p, const int16_t *szi, int 
 #pragma unroll
     for (int m = 0; m < 8; m++) r[m] = p[phys(32 * m + lane)];
 #pragma unroll
-    for (int m = 0; m < 8; m += 2) gs_bfly32(r[m], r[m + 1], szi[120 + (m >> 1)]);
+    for (int m = 0; m < 8; m += 2) gs_bfly_s(r[m], r[m + 1], twi[120 + (m >> 1)]);
 #pragma unroll
     for (int m = 0; m < 8; m++)
-        if (!(m & 2)) gs_bfly32(r[m], r[m + 2], szi[124 + (m >> 2)]);
+        if (!(m & 2)) gs_bfly_s(r[m], r[m + 2], twi[124 + (m >> 2)]);
     {
-        const int32_t z = szi[126];
+        const int2 z = twi[126];
 #pragma unroll
-        for (int m = 0; m < 4; m++) gs_bfly32(r[m], r[m + 4], z);
+        for (int m = 0; m < 4; m++) gs_bfly_s(r[m], r[m + 4], z);
     }
-    const int32_t f = szi[127];
+    const int2 f = twi[127];
 #pragma unroll
-    for (int m = 0; m < 8; m++) p[phys(32 * m + lane)] = (int16_t)fqmul32(r[m], f);
+    for (int m = 0; m < 8; m++) p[phys(32 * m + lane)] = (int16_t)mulc(r[m], f);
     __syncwarp();
 }
 

@@ -125,11 +125,11 @@ __device__ __forceinline__ void noise_poly(const uint2 *seed, int nonce, F emit)
 
 // One matrix entry per thread: stream SHAKE128(rho || x || y), rejection-sample in order, and as
 // soon as a coefficient pair (2p, 2p+1) is complete multiply it with b (basemul) and add it into
-// the shared accumulator with one 32-bit shared-memory atomic.  The two int16 products are packed
-// with a bias of 2q each: a basemul output lies in (-2q, 2q), so a biased term lies in (0, 4q) and
-// the sum of at most four terms stays below 2^16 -- the halves never carry into each other.  The
-// consumer subtracts K * 2q from each half, which yields exactly the reference's int16 sum of the
-// K products (that sum cannot wrap: |sum| < 8q < 2^15), before the Barrett of pointwise_acc.
+// the shared accumulator with one 32-bit shared-memory atomic.  The two products are packed with a
+// bias of 2q each: a basemul output lies in [-11, q + 11], so a biased term lies in (q, 4q) and the
+// sum of at most four terms stays below 2^16 -- the halves never carry into each other.  The
+// consumer subtracts K * 2q from each half, which yields the sum of the K products, before the
+// Barrett of pointwise_acc.
 constexpr uint32_t ACC_BIAS = 2 * Q;
 
 // Per-thread staging of accepted candidates in shared memory: each Keccak block is parsed in two
@@ -179,16 +179,17 @@ __device__ __forceinline__ void compact_half(const uint2 (&A)[25], int16_t *stg,
 // Multiply the complete pairs staged in stg[0..n) into the accumulator (pair index from ctr),
 // stopping at 256 coefficients; an unpaired last coefficient moves to stg[0].
 __device__ __forceinline__ void consume_pairs(int16_t *stg, int &n, int &ctr, const int16_t *b, uint32_t *acc,
-                                              const int16_t *sz) {
+                                              const int2 *tw) {
     int i = 0;
     for (; i + 1 < n && ctr < N; i += 2, ctr += 2) {
         const uint32_t av = *reinterpret_cast<const uint32_t *>(stg + i);
         const int p = ctr >> 1, o = phys(2 * p);
         const uint32_t bb = *reinterpret_cast<const uint32_t *>(b + o);
-        int16_t r0, r1;
-        basemul(r0, r1, (int16_t)(av & 0xffff), (int16_t)(av >> 16), (int16_t)(bb & 0xffff), (int16_t)(bb >> 16),
-                pair_zeta(sz, p));
-        atomicAdd(acc + (o >> 1), (uint32_t)((int)r0 + (int)ACC_BIAS) | ((uint32_t)((int)r1 + (int)ACC_BIAS) << 16));
+        // staged coefficients are in [0, 2^12) and the NTT output b in [0, q]: no sign extension
+        int32_t r0, r1;
+        basemul_plain(r0, r1, (int32_t)(av & 0xffff), (int32_t)(av >> 16), (int32_t)(bb & 0xffff), (int32_t)(bb >> 16),
+                      pair_w(tw, p));
+        atomicAdd(acc + (o >> 1), (uint32_t)(r0 + (int32_t)ACC_BIAS) | ((uint32_t)(r1 + (int32_t)ACC_BIAS) << 16));
     }
     const bool carry = (i < n) && (ctr < N);
     if (carry) stg[0] = stg[i];
@@ -201,7 +202,7 @@ __device__ __forceinline__ void consume_pairs(int16_t *stg, int &n, int &ctr, co
 // reference's rejection sampling coefficient for coefficient.
 template <int V>
 __device__ __forceinline__ void matrix_entry(const uint2 *rho, int row, int col, bool transposed, const int16_t *b,
-                                             int16_t *acc16, const int16_t *sz, int16_t *stg) {
+                                             int16_t *acc16, const int2 *tw, int16_t *stg) {
     uint2 A[25];
     keccak_zero(A);
 #pragma unroll
@@ -214,17 +215,17 @@ __device__ __forceinline__ void matrix_entry(const uint2 *rho, int row, int col,
     while (ctr < N) {
         keccak_f1600(A);
         compact_half<V, 0>(A, stg, n);
-        consume_pairs(stg, n, ctr, b, acc, sz);
+        consume_pairs(stg, n, ctr, b, acc, tw);
         if (ctr >= N) break;
         compact_half<V, 1>(A, stg, n);
-        consume_pairs(stg, n, ctr, b, acc, sz);
+        consume_pairs(stg, n, ctr, b, acc, tw);
     }
 }
 
 // Undo the accumulator bias of K terms and apply pointwise_acc's Barrett.
 template <int K>
 __device__ __forceinline__ int32_t unbias(int32_t biased) {
-    return barrett32((biased & 0xffff) - (int32_t)(K * ACC_BIAS));
+    return barrett_hi((biased & 0xffff) - (int32_t)(K * ACC_BIAS));
 }
 __device__ __forceinline__ int32_t csubq32(int32_t a) {
     a -= Q;
@@ -339,7 +340,7 @@ constexpr int DEC_FUSED = 0, DEC_DECRYPT = 1, DEC_REENCRYPT = 2;
 template <int NPOLY, int SEEDB>
 struct Layout {
     static __host__ __device__ constexpr size_t bytes(int ni, int threads) {
-        return 2 * 128 * sizeof(int16_t) + (size_t)ni * NPOLY * POLY_PITCH * sizeof(int16_t) + (size_t)ni * SEEDB +
+        return 2 * 128 * sizeof(int2) + (size_t)ni * NPOLY * POLY_PITCH * sizeof(int16_t) + (size_t)ni * SEEDB +
                (size_t)threads * STAGE_INT16 * sizeof(int16_t);
     }
 };
@@ -357,10 +358,10 @@ __host__ __device__ constexpr int enc_seed_bytes() {
     return 128 + 128 * (K + 1);
 }
 
-__device__ __forceinline__ void load_twiddles(int16_t *sz, int16_t *szi) {
+__device__ __forceinline__ void load_twiddles(int2 *tw, int2 *twi) {
     for (int i = threadIdx.x; i < 128; i += blockDim.x) {
-        sz[i] = c_zetas[i];
-        szi[i] = c_zetas_inv[i];
+        tw[i] = c_tw[i];
+        twi[i] = c_twi[i];
     }
 }
 
@@ -408,7 +409,7 @@ __device__ __forceinline__ int16_t *slot(int16_t *polys, int li, int s) {
 }
 
 template <int K, int V, bool DEC>
-__device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz, const int16_t *szi, int ni,
+__device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int2 *tw, const int2 *twi, int ni,
                                int ni_alloc, int base, const EncArgs &a, const uint8_t *ct_cmp) {
     using Pp = P<K, V>;
     constexpr int SB = enc_seed_bytes<K, V>();
@@ -472,7 +473,7 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
         __syncwarp();
         uint4 *uz = reinterpret_cast<uint4 *>(u);
         for (int q = lane; q < POLY_PITCH / 8; q += 32) uz[q] = make_uint4(0, 0, 0, 0);
-        ntt_warp(p, sz, lane);
+        ntt_warp(p, tw, lane);
     }
     __syncthreads();
     // (3) u_i += A^T[i][j] o r-hat_j, streamed from SHAKE128, one thread per matrix entry
@@ -480,24 +481,25 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
         const int li = job / (K * K), i = (job / K) % K, j = job % K;
         const uint8_t *pk = a.pk + (size_t)(base + li) * a.pk_stride;
         matrix_entry<V>(reinterpret_cast<const uint2 *>(pk + Pp::POLYVECBYTES), i, j, true, slot<K, V>(polys, li, j),
-                        slot<K, V>(polys, li, K + i), sz, stage_of<SB>(seeds, ni_alloc));
+                        slot<K, V>(polys, li, K + i), tw, stage_of<SB>(seeds, ni_alloc));
     }
     //     v = t-hat o r-hat (warp per instance, t-hat decoded from pk bytes; independent of (3))
     for (int li = warp; li < ni; li += nwarp) {
         const uint8_t *pk = a.pk + (size_t)(base + li) * a.pk_stride;
-        int16_t acc[8];
+        int32_t acc[8];
         for (int j = 0; j < K; j++) {
-            int16_t t[8], b[8], r[8];
+            int32_t t[8], b[8], r[8];
             frombytes8(t, pk + 384 * j + 12 * lane);
             load8(b, slot<K, V>(polys, li, j) + phys(8 * lane));
 #pragma unroll
-            for (int q = 0; q < 4; q++) basemul(r[2 * q], r[2 * q + 1], t[2 * q], t[2 * q + 1], b[2 * q], b[2 * q + 1],
-                                                 pair_zeta(sz, 4 * lane + q));
+            for (int q = 0; q < 4; q++)
+                basemul_plain(r[2 * q], r[2 * q + 1], t[2 * q], t[2 * q + 1], b[2 * q], b[2 * q + 1],
+                              pair_w(tw, 4 * lane + q));
 #pragma unroll
-            for (int q = 0; q < 8; q++) acc[q] = (j == 0) ? r[q] : (int16_t)(acc[q] + r[q]);
+            for (int q = 0; q < 8; q++) acc[q] = (j == 0) ? r[q] : acc[q] + r[q];
         }
 #pragma unroll
-        for (int q = 0; q < 8; q++) acc[q] = barrett(acc[q]);
+        for (int q = 0; q < 8; q++) acc[q] = barrett_hi(acc[q]);
         store8(slot<K, V>(polys, li, 2 * K) + phys(8 * lane), acc);
     }
     __syncthreads();
@@ -512,7 +514,7 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
             store8(p + phys(8 * lane), c);
             __syncwarp();
         }
-        invntt_warp(p, szi, lane);
+        invntt_warp(p, twi, lane);
     }
     __syncthreads();
     // (5) warp per instance, lane = 8 coefficients: u += e1, v += e2 + msg (CBD_eta2 of the stored
@@ -571,22 +573,22 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int16_t *sz
 // Kernels
 // ---------------------------------------------------------------------------------------------
 constexpr int CORE_MAX_THREADS = 512;
-constexpr int DEC1_MAX_THREADS = 384;
 
 // Encapsulation of instances [base, base + NI) of `a` by the calling CTA (dynamic shared memory
 // laid out for NI instances of this K).
 template <int K, int V>
 __device__ __forceinline__ void enc_core_body(const EncArgs &a, int NI, int base) {
     extern __shared__ __align__(16) uint8_t smem[];
-    int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
+    int2 *tw = reinterpret_cast<int2 *>(smem), *twi = tw + 128;
+    int16_t *polys = reinterpret_cast<int16_t *>(twi + 128);
     uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (2 * K + 1) * POLY_PITCH);
     const int ni = min(NI, a.n - base);
-    load_twiddles(sz, szi);
+    load_twiddles(tw, twi);
     __syncthreads();
-    encrypt_phases<K, V, false>(polys, seeds, sz, szi, ni, NI, base, a, nullptr);
+    encrypt_phases<K, V, false>(polys, seeds, tw, twi, ni, NI, base, a, nullptr);
 }
 template <int K, int V>
-__global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_enc_core(EncArgs a, int NI) {
+__global__ void __launch_bounds__(kyber_bound_threads(1, K), kyber_bound_ctas(1, K)) kyber_enc_core(EncArgs a, int NI) {
     enc_core_body<K, V>(a, NI, blockIdx.x * NI);
 }
 
@@ -596,12 +598,13 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
     using Pp = P<K, V>;
     constexpr int SB = enc_seed_bytes<K, V>();
     extern __shared__ __align__(16) uint8_t smem[];
-    int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
+    int2 *tw = reinterpret_cast<int2 *>(smem), *twi = tw + 128;
+    int16_t *polys = reinterpret_cast<int16_t *>(twi + 128);
     uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (2 * K + 1) * POLY_PITCH);
     const int ni = min(NI, d.n - base);
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
     const int sks = d.kem ? Pp::SKB : Pp::SKCPA;
-    load_twiddles(sz, szi);
+    load_twiddles(tw, twi);
     if constexpr (STAGE == DEC_REENCRYPT) {
         // m', r', K-bar' of the CTA's instances from the decryption stage
         for (int t = tid; t < ni * 12; t += nthr)
@@ -629,7 +632,7 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
     }
     __syncthreads();
     // (b) u-hat = NTT(u')
-    for (int w = warp; w < ni * K; w += nwarp) ntt_warp(slot<K, V>(polys, w / K, K + w % K), sz, lane);
+    for (int w = warp; w < ni * K; w += nwarp) ntt_warp(slot<K, V>(polys, w / K, K + w % K), tw, lane);
     __syncthreads();
     // (c) mp = s-hat o u-hat -> slot 0
     for (int li = warp; li < ni; li += nwarp) {
@@ -641,17 +644,17 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
             load8(b, slot<K, V>(polys, li, K + j) + phys(8 * lane));
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                basemul32(r[2 * q], r[2 * q + 1], s[2 * q], s[2 * q + 1], b[2 * q], b[2 * q + 1],
-                          pair_zeta(sz, 4 * lane + q));
+                basemul_plain(r[2 * q], r[2 * q + 1], s[2 * q], s[2 * q + 1], b[2 * q], b[2 * q + 1],
+                              pair_w(tw, 4 * lane + q));
 #pragma unroll
             for (int q = 0; q < 8; q++) acc[q] = (j == 0) ? r[q] : acc[q] + r[q];
         }
 #pragma unroll
-        for (int q = 0; q < 8; q++) acc[q] = barrett32(acc[q]);
+        for (int q = 0; q < 8; q++) acc[q] = barrett_hi(acc[q]);
         store8(slot<K, V>(polys, li, 0) + phys(8 * lane), acc);
     }
     __syncthreads();
-    for (int w = warp; w < ni; w += nwarp) invntt_warp(slot<K, V>(polys, w, 0), szi, lane);
+    for (int w = warp; w < ni; w += nwarp) invntt_warp(slot<K, V>(polys, w, 0), twi, lane);
     __syncthreads();
     // (d) m' = tomsg(reduce(v - mp)), lane = message byte
     for (int li = warp; li < ni; li += nwarp) {
@@ -660,7 +663,7 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
         load8(mp, slot<K, V>(polys, li, 0) + phys(8 * lane));
         uint32_t byte = 0;
 #pragma unroll
-        for (int q = 0; q < 8; q++) byte |= compress_u<1>((uint32_t)csubq32(barrett32(v[q] - mp[q]))) << q;
+        for (int q = 0; q < 8; q++) byte |= compress_u<1>((uint32_t)csubq32(barrett_hi(v[q] - mp[q]))) << q;
         seeds[li * SB + lane] = (uint8_t)byte;
         if (!d.kem) d.m_out[(size_t)(base + li) * 32 + lane] = (uint8_t)byte;
     }
@@ -711,7 +714,7 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
     e.m_stride = 0;
     e.r = nullptr;
     e.r_stride = 0;
-    encrypt_phases<K, V, true>(polys, seeds, sz, szi, ni, NI, base, e, d.ct);
+    encrypt_phases<K, V, true>(polys, seeds, tw, twi, ni, NI, base, e, d.ct);
     __syncthreads();
     // (g) ML-KEM: ss = fail ? J(z || c) : K' (constant-time select, no hashing)
     if (d.kem == KEM_MLKEM) {
@@ -752,13 +755,12 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
     }
 }
 template <int K, int V, int STAGE>
-__global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_dec_core(DecArgs d, int NI) {
+__global__ void __launch_bounds__(kyber_bound_threads(2, K), kyber_bound_ctas(2, K)) kyber_dec_core(DecArgs d, int NI) {
     dec_core_body<K, V, STAGE>(d, NI, blockIdx.x * NI);
 }
-// The decryption stage alone: up to DEC1_MAX_THREADS threads, with the register budget of two such
-// CTAs per SM (80 a thread), so that its 384-thread shapes keep two CTAs per SM.
+// The decryption stage alone: its bound keeps two 384-thread CTAs per SM (80 registers a thread).
 template <int K, int V>
-__global__ void __launch_bounds__(DEC1_MAX_THREADS, 2) kyber_dec_decrypt(DecArgs d, int NI) {
+__global__ void __launch_bounds__(kyber_bound_threads(3, K), kyber_bound_ctas(3, K)) kyber_dec_decrypt(DecArgs d, int NI) {
     dec_core_body<K, V, DEC_DECRYPT>(d, NI, blockIdx.x * NI);
 }
 
@@ -768,13 +770,14 @@ template <int K, int V>
 __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int NI) {
     using Pp = P<K, V>;
     extern __shared__ __align__(16) uint8_t smem[];
-    int16_t *sz = reinterpret_cast<int16_t *>(smem), *szi = sz + 128, *polys = szi + 128;
+    int2 *tw = reinterpret_cast<int2 *>(smem), *twi = tw + 128;
+    int16_t *polys = reinterpret_cast<int16_t *>(twi + 128);
     uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (3 * K) * POLY_PITCH);
     auto kslot = [&](int li, int s) { return polys + ((size_t)li * (3 * K) + s) * POLY_PITCH; };
     const int base = blockIdx.x * NI;
     const int ni = min(NI, a.n - base);
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
-    load_twiddles(sz, szi);
+    load_twiddles(tw, twi);
     // (a) (rho, sigma) = G(d); ML-KEM: G(d || k) with the module rank as one byte (FIPS 203)
     for (int li = tid; li < ni; li += nthr) {
         const uint2 *dd = reinterpret_cast<const uint2 *>(a.coins + (size_t)(base + li) * a.coins_stride);
@@ -799,13 +802,13 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int 
                              [&](int g, const int16_t(&c)[8]) { store8(dst + phys(8 * g), c); });
     }
     __syncthreads();
-    for (int w = warp; w < ni * 2 * K; w += nwarp) ntt_warp(kslot(w / (2 * K), w % (2 * K)), sz, lane);
+    for (int w = warp; w < ni * 2 * K; w += nwarp) ntt_warp(kslot(w / (2 * K), w % (2 * K)), tw, lane);
     __syncthreads();
     // (c) t-hat_i += A[i][j] o s-hat_j (not transposed), one thread per matrix entry
     for (int job = tid; job < ni * K * K; job += nthr) {
         const int li = job / (K * K), i = (job / K) % K, j = job % K;
         matrix_entry<V>(reinterpret_cast<const uint2 *>(seeds + li * 128), i, j, false, kslot(li, j), kslot(li, 2 * K + i),
-                        sz, stage_of<128>(seeds, NI));
+                        tw, stage_of<128>(seeds, NI));
     }
     __syncthreads();
     // (d) t = reduce(frommont(t) + e); pack pk = t || rho and sk_cpa = s (warp per instance)
@@ -819,7 +822,8 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int 
             load8(s, kslot(li, i) + phys(8 * lane));
 #pragma unroll
             for (int q = 0; q < 8; q++) {
-                t[q] = csubq32(barrett32(fqmul32(unbias<K>(t[q]), 1353) + e[q]));
+                // the plain basemul has no Montgomery factor for poly_tomont to undo
+                t[q] = csubq32(barrett_hi(unbias<K>(t[q]) + e[q]));
                 s[q] = csubq32(s[q]);
             }
             uint8_t bt[12], bs[12];
@@ -1217,6 +1221,10 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
         if (cudaMemcpyToSymbol(c_keccak_rc, rc, sizeof rc) != cudaSuccess) return PQCGPU_ECUDA;           \
         if (cudaMemcpyToSymbol(c_zetas, z, sizeof z) != cudaSuccess) return PQCGPU_ECUDA;                 \
         if (cudaMemcpyToSymbol(c_zetas_inv, zi, sizeof zi) != cudaSuccess) return PQCGPU_ECUDA;           \
+        int2 tw[128], twi[128];                                                                            \
+        kyber_twiddles_shoup_host(tw, twi);                                                                \
+        if (cudaMemcpyToSymbol(c_tw, tw, sizeof tw) != cudaSuccess) return PQCGPU_ECUDA;                  \
+        if (cudaMemcpyToSymbol(c_twi, twi, sizeof twi) != cudaSuccess) return PQCGPU_ECUDA;               \
         prefer_shared_all<K, V>();                                                                         \
         return PQCGPU_OK;                                                                                  \
     }                                                                                                      \

@@ -172,6 +172,10 @@ int kyber_mixed_init() {
     if (cudaMemcpyToSymbol(c_keccak_rc, rc, sizeof rc) != cudaSuccess) return PQCGPU_ECUDA;
     if (cudaMemcpyToSymbol(kyber::c_zetas, z, sizeof z) != cudaSuccess) return PQCGPU_ECUDA;
     if (cudaMemcpyToSymbol(kyber::c_zetas_inv, zi, sizeof zi) != cudaSuccess) return PQCGPU_ECUDA;
+    int2 tw[128], twi[128];
+    kyber::kyber_twiddles_shoup_host(tw, twi);
+    if (cudaMemcpyToSymbol(kyber::c_tw, tw, sizeof tw) != cudaSuccess) return PQCGPU_ECUDA;
+    if (cudaMemcpyToSymbol(kyber::c_twi, twi, sizeof twi) != cudaSuccess) return PQCGPU_ECUDA;
     kyber::prefer_shared(kyber::kyber_enc_core_mixed);
     kyber::prefer_shared(kyber::kyber_dec_core_mixed<kyber::DEC_DECRYPT>);
     kyber::prefer_shared(kyber::kyber_dec_core_mixed<kyber::DEC_REENCRYPT>);

@@ -152,8 +152,9 @@ def test_launch_shapes_that_exceed_shared_memory_are_refused():
     ni, thr = ctypes.c_int(), ctypes.c_int()
     assert lib.pqcgpu_get_launch_shape(k768, 2, ctypes.byref(ni), ctypes.byref(thr)) == 0
     try:
-        assert lib.pqcgpu_set_launch_shape(k768, 2, 48, 384) != 0  # 48 x 4.8 KB + staging > 227 KB
-        assert lib.pqcgpu_set_launch_shape(k768, 2, 30, 384) == 0
+        assert lib.pqcgpu_set_launch_shape(k768, 2, 48, 192) != 0  # 48 x 4.8 KB + staging > 227 KB
+        assert lib.pqcgpu_set_launch_shape(k768, 2, 30, 192) == 0
+        assert lib.pqcgpu_set_launch_shape(k768, 2, 8, 256) != 0   # above the kernel's launch bound
         assert lib.pqcgpu_set_launch_shape(nh, 1, 64, 256) != 0   # 64 x 7.5 KB
     finally:
         lib.pqcgpu_set_launch_shape(k768, 2, ni.value, thr.value)
