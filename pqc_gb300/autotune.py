@@ -26,7 +26,7 @@ def candidates(alg, op):
     if alg.startswith("kyber"):
         k = {"kyber512": 2, "kyber768": 3, "kyber1024": 4}[alg]
         out = []
-        for ni in (4, 6, 8, 10, 12, 14, 16, 18, 20, 24, 28, 32, 40, 48):
+        for ni in (4, 6, 8, 10, 11, 12, 13, 14, 15, 16, 18, 20, 24, 28, 30, 32, 36, 40, 48):
             jobs = ni * k * k
             for thr in (64, 96, 128, 160, 192, 224, 256, 288, 320, 384):
                 lo = min(((jobs + 31) // 32) * 32, 384) - 64

@@ -6,8 +6,8 @@ namespace kyber {
 // Launch shape of the core kernels, [op][k-2] with op 0 keypair, 1 enc, 2 dec (its re-encryption
 // stage).  One thread per matrix entry (NI * k^2 jobs) sized against the shared memory each instance
 // needs.  g_dec1: the decryption stage of decapsulation.  Defaults: the autotuner's GB300 optimum.
-int g_ni[3][3] = {{16, 10, 8}, {28, 12, 8}, {24, 12, 8}};
-int g_threads[3][3] = {{64, 96, 128}, {128, 128, 128}, {128, 128, 128}};
+int g_ni[3][3] = {{16, 12, 8}, {30, 14, 8}, {30, 14, 16}};
+int g_threads[3][3] = {{64, 128, 160}, {128, 128, 128}, {128, 128, 256}};
 int g_dec1[3][2] = {{32, 384}, {23, 384}, {12, 256}};
 
 #define PQC_KYBER_DECL(K, V)                                                                               \

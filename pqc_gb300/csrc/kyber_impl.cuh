@@ -132,20 +132,27 @@ __device__ __forceinline__ void noise_poly(const uint2 *seed, int nonce, F emit)
 // Barrett of pointwise_acc.
 constexpr uint32_t ACC_BIAS = 2 * Q;
 
-// Per-thread staging of accepted candidates in shared memory: each Keccak block is parsed in two
-// halves; a half yields at most 56 accepted coefficients, plus one carried over from the previous
-// half (an unpaired even coefficient), so 58 int16 per thread suffice.
-constexpr int STAGE_INT16 = 58;
+// Per-thread staging of accepted candidates in shared memory: each Keccak block is parsed in parts
+// of 28 candidates (round 3: 4 parts of 14 triplets; round 2: 3 parts of 14 little-endian words),
+// consumed after each part.  A part yields at most 28 accepted coefficients, plus one carried over
+// from the previous part (an unpaired even coefficient), so 30 int16 per thread suffice (29, kept
+// even for the 32-bit pair loads).  Parts of 28 rather than halves of a block halve this area, which
+// fits a 13th instance into a 128-thread CTA at three CTAs per SM (Kyber-768 encryption).
+constexpr int STAGE_INT16 = 30;
+template <int V>
+__host__ __device__ constexpr int parts_per_block() {
+    return V == 3 ? 4 : 3;
+}
 
-// Append the accepted candidates of one half-block to stg[n...] without branches (the store is
-// unconditional, the count advances only on acceptance), in the order of the byte stream.
-template <int V, int HALF>
-__device__ __forceinline__ void compact_half(const uint2 (&A)[25], int16_t *stg, int &n) {
+// Append the accepted candidates of part PART of a block to stg[n...] without branches (the store
+// is unconditional, the count advances only on acceptance), in the order of the byte stream.
+template <int V, int PART>
+__device__ __forceinline__ void compact_part(const uint2 (&A)[25], int16_t *stg, int &n) {
     if (V == 3) {
-        // 56 triplets per block, two 12-bit candidates each (round-3 Parse); this half: 28 triplets
+        // 56 triplets per block, two 12-bit candidates each (round-3 Parse); this part: 14 triplets
 #pragma unroll
-        for (int tt = 0; tt < 28; tt++) {
-            const int t = 28 * HALF + tt, o = 3 * t, wi = o >> 2, sh = 8 * (o & 3);
+        for (int tt = 0; tt < 14; tt++) {
+            const int t = 14 * PART + tt, o = 3 * t, wi = o >> 2, sh = 8 * (o & 3);
             const uint32_t w0 = (wi & 1) ? A[wi >> 1].y : A[wi >> 1].x;
             uint32_t v;
             if (sh <= 8) {
@@ -162,10 +169,10 @@ __device__ __forceinline__ void compact_half(const uint2 (&A)[25], int16_t *stg,
         }
     } else {
         // 84 little-endian 16-bit candidates per block, v < 19q kept as v - (v >> 12) q
-        // (rej_uniform, indcpa.cu:290-322); this half: 42 candidates
+        // (rej_uniform, indcpa.cu:290-322); this part: 14 words, 28 candidates
 #pragma unroll
-        for (int tt = 0; tt < 21; tt++) {
-            const int t = 21 * HALF + tt;
+        for (int tt = 0; tt < 14; tt++) {
+            const int t = 14 * PART + tt;
             const uint32_t w0 = (t & 1) ? A[t >> 1].y : A[t >> 1].x;
             const uint32_t d0 = w0 & 0xffff, d1 = w0 >> 16;
             stg[n] = (int16_t)(d0 - (d0 >> 12) * Q);
@@ -214,11 +221,19 @@ __device__ __forceinline__ void matrix_entry(const uint2 *rho, int row, int col,
     int ctr = 0, n = 0;
     while (ctr < N) {
         keccak_f1600(A);
-        compact_half<V, 0>(A, stg, n);
+        compact_part<V, 0>(A, stg, n);
         consume_pairs(stg, n, ctr, b, acc, tw);
         if (ctr >= N) break;
-        compact_half<V, 1>(A, stg, n);
+        compact_part<V, 1>(A, stg, n);
         consume_pairs(stg, n, ctr, b, acc, tw);
+        if (ctr >= N) break;
+        compact_part<V, 2>(A, stg, n);
+        consume_pairs(stg, n, ctr, b, acc, tw);
+        if constexpr (parts_per_block<V>() == 4) {
+            if (ctr >= N) break;
+            compact_part<V, 3>(A, stg, n);
+            consume_pairs(stg, n, ctr, b, acc, tw);
+        }
     }
 }
 
