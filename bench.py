@@ -600,8 +600,10 @@ def main():
             perms, bfly = w["enc_perms"] - ENC_HASH_PERMS, w["enc_bfly"]
         elif "dec_core" in name:
             perms, bfly = w["dec_perms"] - DEC_HASH_PRE_PERMS, w["dec_bfly"]
-        elif "dec_reencrypt" in name:  # re-encryption stage: all but G and the decryption NTTs
-            perms, bfly = w["dec_perms"] - DEC_HASH_PRE_PERMS - 1, w["dec_bfly"] - dec_stage1_bfly
+        elif "dec_reencrypt" in name:  # re-encryption stage: all but G, the decryption NTTs and the
+            # KDF when kyber_dec_hash_post runs it (batches above 1024)
+            kdf_out = 1 if any("dec_hash_post" in k for k in prof) else 0
+            perms, bfly = w["dec_perms"] - DEC_HASH_PRE_PERMS - 1 - kdf_out, w["dec_bfly"] - dec_stage1_bfly
         elif "dec_decrypt" in name:
             perms, bfly = 1, dec_stage1_bfly
         else:

@@ -8,7 +8,7 @@ namespace kyber {
 // needs.  g_dec1: the decryption stage of decapsulation.  Defaults: the autotuner's GB300 optimum.
 int g_ni[3][3] = {{16, 12, 8}, {30, 14, 8}, {30, 14, 16}};
 int g_threads[3][3] = {{64, 128, 160}, {128, 128, 128}, {128, 128, 256}};
-int g_dec1[3][2] = {{32, 384}, {23, 384}, {12, 256}};
+int g_dec1[3][2] = {{16, 256}, {15, 256}, {8, 256}};
 
 #define PQC_KYBER_DECL(K, V)                                                                               \
     int keypair_##K##_##V(int, uint8_t *, uint8_t *, const uint8_t *, int, int, uint8_t *, int, cudaStream_t); \

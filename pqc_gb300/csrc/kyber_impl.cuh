@@ -341,6 +341,10 @@ struct DecArgs {
     const uint8_t *hct;      // KEM only: H(c) per instance (32 B); ML-KEM: J(z || c)
     int kem;                 // 0 CPA, KEM_FO, KEM_MLKEM
     uint8_t *mr;             // two-stage decapsulation: m' || r' || K-bar' per instance (96 B)
+    int kdf_post;            // KEM_FO: 1 = the re-encryption stage leaves the selected key (K-bar'
+                             // or z) in mr + 64 and kyber_dec_hash_post derives ss from it
+    int g_post;              // KEM: 1 = the decryption stage leaves m' in mr and kyber_dec_hash_mid
+                             // computes (K-bar', r') = G(m' || h) into mr + 64 / mr + 32
 };
 
 // Decapsulation stages.  A KEM decapsulation runs as two kernels: decryption + G (warp-level
@@ -541,6 +545,26 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int2 *tw, c
         const uint8_t *msg = DEC ? seeds + li * SB : a.m + (size_t)(base + li) * a.m_stride;
         const uint8_t mb = msg[lane];
         uint32_t diff = 0;
+        // With even DU and DV (k = 2, 3) every lane's byte group starts at an even offset of a
+        // 16-byte-aligned row of even length, so the ciphertext moves as 16-bit words.  Decaps loads
+        // the lane's words of the received ciphertext before the arithmetic, so their latency
+        // overlaps it instead of following each polynomial (measured: the byte loads cost 5 % of
+        // the Kyber-768 re-encryption stage).
+        constexpr bool W16 = (Pp::DU % 2 == 0) && (Pp::DV % 2 == 0);
+        constexpr int NW = K * (Pp::DU / 2) + Pp::DV / 2;
+        uint32_t cw[DEC && W16 ? NW : 1];
+        if constexpr (DEC && W16) {
+#pragma unroll
+            for (int i = 0; i < K; i++)
+#pragma unroll
+                for (int q = 0; q < Pp::DU / 2; q++)
+                    cw[i * (Pp::DU / 2) + q] =
+                        reinterpret_cast<const uint16_t *>(cmp + (size_t)i * Pp::DU * 32 + (size_t)lane * Pp::DU)[q];
+#pragma unroll
+            for (int q = 0; q < Pp::DV / 2; q++)
+                cw[K * (Pp::DU / 2) + q] = reinterpret_cast<const uint16_t *>(cmp + (size_t)Pp::CTU + (size_t)lane * Pp::DV)[q];
+        }
+#pragma unroll
         for (int i = 0; i <= K; i++) {
             const uint32_t t = reinterpret_cast<const uint32_t *>(seeds + li * SB + 128 + 128 * i)[lane];
             uint32_t d = t & 0x55555555u;
@@ -560,19 +584,37 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int2 *tw, c
                 uint8_t b[Pp::DU];
                 pack8<Pp::DU>(b, cv);
                 const size_t off = (size_t)i * Pp::DU * 32 + (size_t)lane * Pp::DU;
+                if constexpr (W16) {
 #pragma unroll
-                for (int q = 0; q < Pp::DU; q++) {
-                    if (DEC) diff |= (uint32_t)(b[q] ^ cmp[off + q]);
-                    else out[off + q] = b[q];
+                    for (int q = 0; q < Pp::DU / 2; q++) {
+                        const uint32_t w = (uint32_t)b[2 * q] | ((uint32_t)b[2 * q + 1] << 8);
+                        if constexpr (DEC) diff |= w ^ cw[i * (Pp::DU / 2) + q];
+                        else reinterpret_cast<uint16_t *>(out + off)[q] = (uint16_t)w;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < Pp::DU; q++) {
+                        if (DEC) diff |= (uint32_t)(b[q] ^ cmp[off + q]);
+                        else out[off + q] = b[q];
+                    }
                 }
             } else {
                 uint8_t b[Pp::DV];
                 pack8<Pp::DV>(b, cv);
                 const size_t off = (size_t)Pp::CTU + (size_t)lane * Pp::DV;
+                if constexpr (W16) {
 #pragma unroll
-                for (int q = 0; q < Pp::DV; q++) {
-                    if (DEC) diff |= (uint32_t)(b[q] ^ cmp[off + q]);
-                    else out[off + q] = b[q];
+                    for (int q = 0; q < Pp::DV / 2; q++) {
+                        const uint32_t w = (uint32_t)b[2 * q] | ((uint32_t)b[2 * q + 1] << 8);
+                        if constexpr (DEC) diff |= w ^ cw[K * (Pp::DU / 2) + q];
+                        else reinterpret_cast<uint16_t *>(out + off)[q] = (uint16_t)w;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < Pp::DV; q++) {
+                        if (DEC) diff |= (uint32_t)(b[q] ^ cmp[off + q]);
+                        else out[off + q] = b[q];
+                    }
                 }
             }
         }
@@ -681,8 +723,12 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
         for (int q = 0; q < 8; q++) byte |= compress_u<1>((uint32_t)csubq32(barrett_hi(v[q] - mp[q]))) << q;
         seeds[li * SB + lane] = (uint8_t)byte;
         if (!d.kem) d.m_out[(size_t)(base + li) * 32 + lane] = (uint8_t)byte;
+        if (STAGE == DEC_DECRYPT && d.g_post) d.mr[(size_t)(base + li) * 96 + lane] = (uint8_t)byte;
     }
     if (!d.kem) return;
+    // For large batches G leaves this CTA: one permutation on NI of its threads at its end moves to
+    // kyber_dec_hash_mid, a thread per instance over the whole batch.
+    if (STAGE == DEC_DECRYPT && d.g_post) return;
     __syncthreads();
     // (e) (K-bar', r') = G(m' || h)
     for (int li = tid; li < ni; li += nthr) {
@@ -746,7 +792,21 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
         }
         return;
     }
-    // (g) ss = SHAKE256(fail ? z : K-bar' || H(c)), with a constant-time select
+    // (g) ss = SHAKE256(fail ? z : K-bar' || H(c)), with a constant-time select.  For large
+    //     batches only the select runs here: one permutation on NI threads at the end of every CTA
+    //     (measured: 11 % of this kernel at 65536 Kyber-768 instances) moves to kyber_dec_hash_post,
+    //     a thread per instance over the whole batch.
+    if (d.kdf_post) {
+        for (int t = tid; t < ni * 4; t += nthr) {
+            const int li = t >> 2, i = t & 3;
+            const uint32_t mask = 0u - (uint32_t)(seeds[li * SB + 96] != 0);
+            const uint2 zk = reinterpret_cast<const uint2 *>(d.sk + (size_t)(base + li) * Pp::SKB + Pp::SKB - 32)[i];
+            const uint2 kk = reinterpret_cast<const uint2 *>(seeds + li * SB + 64)[i];
+            reinterpret_cast<uint2 *>(d.mr + (size_t)(base + li) * 96 + 64)[i] =
+                make_uint2(kk.x ^ (mask & (kk.x ^ zk.x)), kk.y ^ (mask & (kk.y ^ zk.y)));
+        }
+        return;
+    }
     for (int li = tid; li < ni; li += nthr) {
         const uint8_t *sk = d.sk + (size_t)(base + li) * Pp::SKB;
         const uint32_t mask = 0u - (uint32_t)(seeds[li * SB + 96] != 0);
@@ -952,6 +1012,53 @@ __global__ void __launch_bounds__(128) kyber_dec_hash_pre(int n, const uint8_t *
         keccak_absorb_lanes<SHA3_256_LANES>(A, c, Pp::CTB / 8, DOM_SHA3);
     keccak_f1600(A);
     uint2 *o = reinterpret_cast<uint2 *>(hct + (size_t)x * 32);
+#pragma unroll
+    for (int i = 0; i < 4; i++) o[i] = A[i];
+}
+// decaps, between the two stages (large batches): (K-bar', r') = G(m' || h) with m' from the
+// decryption stage and h = H(pk) from the secret key; mr = m' || r' || K-bar' per instance
+template <int K, int V>
+__global__ void __launch_bounds__(128) kyber_dec_hash_mid(int n, const uint8_t *sk, uint8_t *mr) {
+    using Pp = P<K, V>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    uint2 *row = reinterpret_cast<uint2 *>(mr + (size_t)x * 96);
+    const uint2 *h = reinterpret_cast<const uint2 *>(sk + (size_t)x * Pp::SKB + Pp::SKB - 64);
+    uint2 A[25];
+    keccak_zero(A);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        A[i] = row[i];
+        A[4 + i] = h[i];
+    }
+    A[8].x ^= DOM_SHA3;
+    A[SHA3_512_LANES - 1].y ^= 0x80000000u;
+    keccak_f1600(A);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        row[4 + i] = A[4 + i];  // r'
+        row[8 + i] = A[i];      // K-bar'
+    }
+}
+// decaps epilogue (round-2 / round-3 KEM, large batches): ss = SHAKE256(key || H(c)), key being the
+// constant-time selection (K-bar' or z) the re-encryption stage left in mr + 64
+template <int K, int V>
+__global__ void __launch_bounds__(128) kyber_dec_hash_post(int n, const uint8_t *mr, const uint8_t *hct, uint8_t *ss) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    const uint2 *key = reinterpret_cast<const uint2 *>(mr + (size_t)x * 96 + 64);
+    const uint2 *hc = reinterpret_cast<const uint2 *>(hct + (size_t)x * 32);
+    uint2 A[25];
+    keccak_zero(A);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        A[i] = key[i];
+        A[4 + i] = hc[i];
+    }
+    A[8].x ^= DOM_SHAKE;
+    A[SHAKE256_LANES - 1].y ^= 0x80000000u;
+    keccak_f1600(A);
+    uint2 *o = reinterpret_cast<uint2 *>(ss + (size_t)x * 32);
 #pragma unroll
     for (int i = 0; i < 4; i++) o[i] = A[i];
 }
@@ -1185,6 +1292,8 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
     d.hct = scratch;
     d.kem = kem;
     d.mr = scratch + (size_t)n * 32;
+    d.kdf_post = (kem == KEM_FO && n > WARP_HASH_MAX) ? 1 : 0;
+    d.g_post = (kem && n > WARP_HASH_MAX) ? 1 : 0;
     if (!kem) {
         if (ensure_smem(kyber_dec_core<K, V, DEC_FUSED>, sm) != cudaSuccess) return PQCGPU_ECUDA;
         PQC_LAUNCH(st, "kyber_dec_core", K, V,
@@ -1203,8 +1312,14 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
     if (ensure_smem(kyber_dec_core<K, V, DEC_REENCRYPT>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     PQC_LAUNCH(st, "kyber_dec_decrypt", K, V,
                kyber_dec_decrypt<K, V><<<(n + NI1 - 1) / NI1, NT1, sm1, st>>>(d, NI1));
+    if (d.g_post)
+        PQC_LAUNCH(st, "kyber_dec_hash_mid", K, V,
+                   kyber_dec_hash_mid<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, d.sk, d.mr));
     PQC_LAUNCH(st, "kyber_dec_reencrypt", K, V,
                kyber_dec_core<K, V, DEC_REENCRYPT><<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));
+    if (d.kdf_post)
+        PQC_LAUNCH(st, "kyber_dec_hash_post", K, V,
+                   kyber_dec_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, d.mr, d.hct, d.ss));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 

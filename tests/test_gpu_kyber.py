@@ -84,11 +84,11 @@ def test_kem_matches_oracle(ctx, oracle, alg, n):
 
 @pytest.mark.parametrize("alg", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "mlkem512", "mlkem768",
                                  "mlkem1024"])
-def test_kem_implicit_rejection(ctx, oracle, alg):
+@pytest.mark.parametrize("n", [64, 2048])  # 2048: the key selection leaves the CTA, the KDF runs after it
+def test_kem_implicit_rejection(ctx, oracle, alg, n):
     from pqc_gb300 import kem
     s = kem.sizes(alg)
     a = oracle.ALG_NAMES[alg]
-    n = 64
     seed = drbg.seed48(77)
     pk, sk = ctx.keypair(alg, n, drbg.stream(seed, b"kp", n * s["kp_coins"]))
     ct, ss = ctx.enc(alg, n, pk, drbg.stream(seed, b"enc", n * s["enc_coins"]))
