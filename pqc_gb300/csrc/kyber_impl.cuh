@@ -3,7 +3,7 @@
 // sm_103a: keypair, encapsulation and decapsulation.
 //
 // Each operation is a short chain of kernels over the batch:
-//   *_hash kernels: one thread per instance, the long serial sponges (H(pk), H(c), G, KDF);
+//   *_hash kernels: one thread per instance, the serial sponges (H(pk), H(c), G, KDF);
 //   *_core kernels: one CTA per group of NI instances.  Inside the CTA the work of the CPA
 //     scheme runs as phases separated by __syncthreads:
 //       - noise (PRF + CBD), one thread per polynomial, written straight into shared memory;
@@ -350,8 +350,11 @@ struct DecArgs {
 // Decapsulation stages.  A KEM decapsulation runs as two kernels: decryption + G (warp-level
 // phases, its own launch shape), then re-encryption + comparison + key selection, whose phases are
 // those of encapsulation and which therefore runs at an encapsulation-like shape and efficiency.
-// Measured on GB300 (Kyber-768, 65536): 0.29 + 1.54 ms against 2.03 ms as one kernel.  CPA
-// decryption alone (DEC_FUSED) stops after the message.
+// Measured on GB300 (Kyber-768, 65536): 0.29 + 1.54 ms against 2.03 ms as one kernel.  For
+// batches above 1024 the two single-permutation hashes at the ends of the stages (G, the KDF) run
+// as thread-per-instance kernels between and after them (DecArgs::g_post, kdf_post): inside a CTA
+// each held its shared memory while NI threads permuted (0.26 -> 0.19 ms and 1.27 -> 1.10 ms for
+// the two stages, 24 us per hash kernel).  CPA decryption alone (DEC_FUSED) stops after the message.
 constexpr int DEC_FUSED = 0, DEC_DECRYPT = 1, DEC_REENCRYPT = 2;
 
 // Shared-memory layout for a CTA of NI instances: twiddles, NPOLY polynomials per instance,
