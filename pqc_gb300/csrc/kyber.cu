@@ -50,7 +50,8 @@ int kyber_dec_dev(int variant, int k, int n, uint8_t *out, const uint8_t *ct, co
 }
 size_t kyber_scratch_bytes(int k, int op, int plain) {
     if (plain) return (size_t)(k * k + 4 * k + 4) * 256 * 2 + 208;
-    return op == 1 ? 96 : (op == 2 ? 128 : 0);  // decaps: H(c) (32) + m' r' K-bar' (96)
+    // keypair: rho || sigma (64); encaps: m || r || K-bar (96); decaps: H(c) (32) + m' r' K-bar' (96)
+    return op == 1 ? 96 : (op == 2 ? 128 : 64);
 }
 int kyber_init_constants() {
     int (*inits[])() = {kyber::init_2_3, kyber::init_3_3, kyber::init_4_3,

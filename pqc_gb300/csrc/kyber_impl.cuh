@@ -321,6 +321,8 @@ struct KpArgs {
     const uint8_t *coins;    // d (and z for KEM) per instance
     int coins_stride;
     int kem;                 // 1: write sk = sk_cpa || pk || (H(pk) later) || z
+    const uint8_t *g_in;     // batches above 1024: (rho, sigma) per instance (64 B) computed by
+                             // kyber_kp_hash_pre; null: the core kernel computes G itself
 };
 struct EncArgs {
     int n;
@@ -856,8 +858,15 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int 
     const int ni = min(NI, a.n - base);
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
     load_twiddles(tw, twi);
-    // (a) (rho, sigma) = G(d); ML-KEM: G(d || k) with the module rank as one byte (FIPS 203)
-    for (int li = tid; li < ni; li += nthr) {
+    // (a) (rho, sigma) = G(d); ML-KEM: G(d || k) with the module rank as one byte (FIPS 203).  For
+    //     large batches kyber_kp_hash_pre has computed them (a permutation on NI threads at the
+    //     head of the CTA would hold its shared memory meanwhile): load them.
+    if (a.g_in) {
+        for (int t = tid; t < ni * 8; t += nthr)
+            reinterpret_cast<uint2 *>(seeds + (t >> 3) * 128)[t & 7] =
+                reinterpret_cast<const uint2 *>(a.g_in + (size_t)(base + (t >> 3)) * 64)[t & 7];
+    }
+    for (int li = tid; li < ni && !a.g_in; li += nthr) {
         const uint2 *dd = reinterpret_cast<const uint2 *>(a.coins + (size_t)(base + li) * a.coins_stride);
         uint2 A[25];
         keccak_zero(A);
@@ -1065,6 +1074,25 @@ __global__ void __launch_bounds__(128) kyber_dec_hash_post(int n, const uint8_t 
 #pragma unroll
     for (int i = 0; i < 4; i++) o[i] = A[i];
 }
+// keypair prologue (large batches): (rho, sigma) = G(d) per instance into out (64 B each);
+// ML-KEM: G(d || k)
+template <int K, int V>
+__global__ void __launch_bounds__(128) kyber_kp_hash_pre(int n, const uint8_t *coins, int coins_stride, int kem,
+                                                         uint8_t *out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    const uint2 *dd = reinterpret_cast<const uint2 *>(coins + (size_t)x * coins_stride);
+    uint2 A[25];
+    keccak_zero(A);
+#pragma unroll
+    for (int i = 0; i < 4; i++) A[i] = dd[i];
+    A[4].x = kem == KEM_MLKEM ? ((uint32_t)K | (DOM_SHA3 << 8)) : DOM_SHA3;
+    A[SHA3_512_LANES - 1].y ^= 0x80000000u;
+    keccak_f1600(A);
+    uint2 *o = reinterpret_cast<uint2 *>(out + (size_t)x * 64);
+#pragma unroll
+    for (int i = 0; i < 8; i++) o[i] = A[i];
+}
 // keypair epilogue: sk[SKB-64 .. SKB-32) = H(pk)
 template <int K, int V>
 __global__ void __launch_bounds__(128) kyber_kp_hash_post(int n, const uint8_t *pk, uint8_t *sk) {
@@ -1203,6 +1231,9 @@ static void prefer_shared_all() {
     prefer_shared(kyber_enc_hash_post<K, V>);
     prefer_shared(kyber_dec_hash_pre<K, V>);
     prefer_shared(kyber_kp_hash_post<K, V>);
+    prefer_shared(kyber_kp_hash_pre<K, V>);
+    prefer_shared(kyber_dec_hash_mid<K, V>);
+    prefer_shared(kyber_dec_hash_post<K, V>);
     prefer_shared(kyber_enc_hash_pre_w<K, V>);
     prefer_shared(kyber_enc_hash_post_w<K, V>);
     prefer_shared(kyber_dec_hash_pre_w<K, V>);
@@ -1230,7 +1261,11 @@ static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins,
     const int NI = g_ni[0][K - 2], NT = g_threads[0][K - 2];
     const size_t sm = Layout<3 * K, 128>::bytes(NI, NT);
     if (ensure_smem(kyber_kp_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
-    KpArgs a{n, pk, sk, coins, coins_stride, kem};
+    const bool g_pre = scratch && n > WARP_HASH_MAX;  // G as its own kernel (scratch: 64 B per instance)
+    KpArgs a{n, pk, sk, coins, coins_stride, kem, g_pre ? scratch : nullptr};
+    if (g_pre)
+        PQC_LAUNCH(st, "kyber_kp_hash_pre", K, V,
+                   kyber_kp_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, coins, coins_stride, kem, scratch));
     PQC_LAUNCH(st, "kyber_kp_core", K, V, kyber_kp_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
     if (kem && n <= WARP_HASH_MAX)
         PQC_LAUNCH(st, "kyber_kp_hash_post", K, V, kyber_kp_hash_post_w<K, V><<<(n + 3) / 4, 128, 0, st>>>(n, pk, sk));
