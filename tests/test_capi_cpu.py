@@ -154,7 +154,7 @@ def test_launch_shapes_that_exceed_shared_memory_are_refused():
     try:
         assert lib.pqcgpu_set_launch_shape(k768, 2, 48, 192) != 0  # 48 x 4.8 KB + staging > 227 KB
         assert lib.pqcgpu_set_launch_shape(k768, 2, 30, 192) == 0
-        assert lib.pqcgpu_set_launch_shape(k768, 2, 8, 256) != 0   # above the kernel's launch bound
+        assert lib.pqcgpu_set_launch_shape(k768, 2, 8, 288) != 0   # above the kernel's launch bound (256)
         assert lib.pqcgpu_set_launch_shape(nh, 1, 64, 256) != 0   # 64 x 7.5 KB
     finally:
         lib.pqcgpu_set_launch_shape(k768, 2, ni.value, thr.value)
