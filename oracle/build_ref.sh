@@ -5,49 +5,69 @@
 # n = 512 build adds oracle/ref_glue_newhope512.cpp for the one function the reference leaves
 # undefined at that size.
 #
-# Reads the sources where they lie under the reference tree (default /root/reference, or $1).
-# The only transformation is mechanical and lands in oracle/_ref/src (git-ignored): the kernel
-# launches `K<<<g, b, ...>>>(args)` in the two orchestration files are rewritten into
-# `host_launch(g, b, K, args)`.  Nothing from the reference is committed.
+# Usage: build_ref.sh [REFERENCE_TREE]   (or REFERENCE_TREE in $PQC_REFERENCE_DIR)
+# Step 1, only when a reference tree is given: stage the source files into oracle/_ref/src
+# (git-ignored).  The only transformation is mechanical: the kernel launches
+# `K<<<g, b, ...>>>(args)` in the two orchestration files become `host_launch(g, b, K, args)`.
+# Step 2: compile the staged copy.  The staged copy travels with the working tree, so step 2 also
+# runs on a machine that has no reference tree.  Nothing from the reference is committed.
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${PQC_REFERENCE_DIR:-}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
-if [ ! -d "$REF/Kyber_GPU_Batched" ]; then
-  echo "reference tree not found at $REF; skipping oracle/_ref" >&2
-  exit 0
-fi
 CXX="${CXX:-g++}"
 CXXFLAGS="-std=c++17 -O2 -fPIC -w -I$HERE/ref_shim"
 LAUNCH_SED='s/([A-Za-z_0-9]+) *<< *<\s*([^,]+),\s*([^,>]+)[^>]*>> *>\s*\(/host_launch(\2, \3, \1, /'
 
-build_one() {  # name srcdir "files" orchestration-file "driver files" kdefine
-  local name="$1" srcdir="$2" files="$3" orch="$4" driver="$5" defs="$6"
+stage_one() {  # name srcdir "files" orchestration-file
+  local name="$1" srcdir="$2" files="$3" orch="$4"
   local w="$OUT/src/$name"
   rm -rf "$w"; mkdir -p "$w"
   cp "$REF/$srcdir"/*.h "$w/"
   for f in $files; do cp "$REF/$srcdir/$f" "$w/${f%.cu}.cpp"; done
   sed -E -i "$LAUNCH_SED" "$w/${orch%.cu}.cpp"
-  local objs=()
+}
+
+build_one() {  # name "files" "driver files" defines
+  local name="$1" files="$2" driver="$3" defs="$4"
+  local w="$OUT/src/$name"
+  local objs=() pids=()
   for f in $files; do
-    "$CXX" $CXXFLAGS $defs -I"$w" -c "$w/${f%.cu}.cpp" -o "$w/${f%.cu}.o"
+    "$CXX" $CXXFLAGS $defs -I"$w" -c "$w/${f%.cu}.cpp" -o "$w/${f%.cu}.o" &
+    pids+=($!)
     objs+=("$w/${f%.cu}.o")
   done
+  for p in "${pids[@]}"; do wait "$p"; done
   local drv=()
   for f in $driver; do drv+=("$HERE/$f"); done
   "$CXX" $CXXFLAGS $defs -I"$w" -shared -o "$OUT/lib$name.so" "${drv[@]}" "${objs[@]}"
 }
 
+KYBER_FILES="cbd.cu fips202.cu ntt.cu poly.cu polyvec.cu reduce.cu symmetric-fips202.cu indcpa.cu"
+NEWHOPE_FILES="fips202.cu ntt.cu poly.cu precomp.cu reduce.cu cpapke.cu"
+
+if [ -n "$REF" ]; then
+  if [ ! -d "$REF/Kyber_GPU_Batched" ]; then
+    echo "no Kyber_GPU_Batched under $REF" >&2
+    exit 1
+  fi
+  for K in 2 3 4; do stage_one "refkyber$K" Kyber_GPU_Batched "$KYBER_FILES" indcpa.cu; done
+  stage_one refnewhope NewHope_NIST_GPU "$NEWHOPE_FILES" cpapke.cu
+  stage_one refnewhope512 NewHope_NIST_GPU "$NEWHOPE_FILES" cpapke.cu
+fi
+if [ ! -f "$OUT/src/refkyber3/indcpa.cpp" ]; then
+  echo "reference sources not staged (give the reference tree as \$1 or PQC_REFERENCE_DIR); skipping oracle/_ref" >&2
+  exit 0
+fi
 mkdir -p "$OUT"
+jobs_=()
 for K in 2 3 4; do
-  build_one "refkyber$K" Kyber_GPU_Batched \
-    "cbd.cu fips202.cu ntt.cu poly.cu polyvec.cu reduce.cu symmetric-fips202.cu indcpa.cu" \
-    indcpa.cu ref_driver_kyber.cpp "-DKYBER_K=$K"
+  build_one "refkyber$K" "$KYBER_FILES" ref_driver_kyber.cpp "-DKYBER_K=$K" &
+  jobs_+=($!)
 done
-build_one refnewhope NewHope_NIST_GPU \
-  "fips202.cu ntt.cu poly.cu precomp.cu reduce.cu cpapke.cu" \
-  cpapke.cu ref_driver_newhope.cpp ""
-build_one refnewhope512 NewHope_NIST_GPU \
-  "fips202.cu ntt.cu poly.cu precomp.cu reduce.cu cpapke.cu" \
-  cpapke.cu "ref_driver_newhope.cpp ref_glue_newhope512.cpp" "-DNEWHOPE_N=512"
+build_one refnewhope "$NEWHOPE_FILES" ref_driver_newhope.cpp "" &
+jobs_+=($!)
+build_one refnewhope512 "$NEWHOPE_FILES" "ref_driver_newhope.cpp ref_glue_newhope512.cpp" "-DNEWHOPE_N=512" &
+jobs_+=($!)
+for p in "${jobs_[@]}"; do wait "$p"; done
 echo "built: $(ls "$OUT"/*.so | xargs -n1 basename | tr '\n' ' ')"

@@ -18,6 +18,20 @@ import torch
 from . import drbg, kem
 
 
+def mixed_kyber_spec(njobs=24, seed=12):
+    """The mixed Kyber batch: per launch (job) a parameter set k = 2 / 3 / 4 with probabilities
+    0.4 / 0.4 / 0.2, an operation keypair / enc / dec with 1/3 each, and a batch size drawn uniformly
+    from 1..65536.  Returns [(alg, op, n)]; job j draws its inputs from DRBG seed 200 + j."""
+    import random
+    rng = random.Random(seed)
+    spec = []
+    for _ in range(njobs):
+        alg = rng.choices(["kyber512", "kyber768", "kyber1024"], [0.4, 0.4, 0.2])[0]
+        op = rng.choice(["keypair", "enc", "dec"])
+        spec.append((alg, op, rng.randint(1, 65536)))
+    return spec
+
+
 def run(alg, n, reps, want, fl):
     ctx = kem.Context(0)
     s = kem.sizes(alg)

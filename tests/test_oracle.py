@@ -132,3 +132,62 @@ def test_mlkem_hash_layer_against_hashlib(oracle, k):
     # the module rank in G separates ML-KEM keys from round-3 keys of the same seed
     kpk, _ = oracle.batch_keypair(alg - 6, 1, coins)
     assert kpk != pk
+
+
+def _fips203_tamper(ct, i):
+    b = bytearray(ct)
+    b[(37 * i) % len(b)] ^= 1 << (i % 8)
+    return bytes(b)
+
+
+@pytest.mark.parametrize("name", ["mlkem768", "mlkem1024"])
+def test_mlkem_oracle_against_fips203_fixtures(oracle, name):
+    """The oracle against the committed answers of an independent FIPS 203 implementation (the
+    `cryptography` package, tests/golden/gen_fips203.py): encapsulation keys, the encapsulation of
+    sampled instances (whose ciphertexts that implementation decapsulated to the same key), its own
+    ciphertexts decapsulated here, and its implicit-rejection keys for tampered ciphertexts."""
+    import base64
+    g = load_golden("fips203_%s.json" % name)
+    alg = oracle.ALG_NAMES[name]
+    sz = oracle.alg_sizes(alg)
+    for case in g["cases"]:
+        n = case["n"]
+        seed = drbg.seed48(case["drbg_seed"])
+        kc = drbg.stream(seed, b"kp", n * sz["kp_coins"])
+        ec = drbg.stream(seed, b"enc", n * sz["enc_coins"])
+        keys = {}
+        for r in case["samples"][:64]:
+            i = r["i"]
+            pk, sk = oracle.batch_keypair(alg, 1, kc[i * 64:(i + 1) * 64])
+            keys[i] = sk
+            assert sha(pk) == r["pk_sha256"], (n, i)
+            ct, ss = oracle.batch_enc(alg, 1, pk, ec[i * 32:(i + 1) * 32])
+            assert sha(ct) == r["ct_sha256"], (n, i)
+            assert ss.hex() == r["ss"], (n, i)
+        for f in case["foreign"][:8]:
+            i = f["i"]
+            sk = keys.get(i) or oracle.batch_keypair(alg, 1, kc[i * 64:(i + 1) * 64])[1]
+            ct = base64.b64decode(f["ct_b64"])
+            assert oracle.batch_dec(alg, 1, ct, sk).hex() == f["ss"], (n, i)
+            assert oracle.batch_dec(alg, 1, _fips203_tamper(ct, i), sk).hex() == f["tampered_ss"], (n, i)
+
+
+@pytest.mark.parametrize("name", ["mlkem768", "mlkem1024"])
+def test_mlkem_oracle_against_cryptography_live(oracle, name):
+    """The same four checks against the `cryptography` package itself, on 20 fresh seeds, where it is
+    installed (it is not on every machine that runs these tests)."""
+    import os
+    mlkem = pytest.importorskip("cryptography.hazmat.primitives.asymmetric.mlkem")
+    cls = {"mlkem768": mlkem.MLKEM768PrivateKey, "mlkem1024": mlkem.MLKEM1024PrivateKey}[name]
+    alg = oracle.ALG_NAMES[name]
+    for t in range(20):
+        d_z, m = os.urandom(64), os.urandom(32)
+        key = cls.from_seed_bytes(d_z)
+        pk, sk = oracle.batch_keypair(alg, 1, d_z)
+        assert pk == key.public_key().public_bytes_raw()
+        ct, ss = oracle.batch_enc(alg, 1, pk, m)
+        assert key.decapsulate(ct) == ss
+        ss_c, ct_c = key.public_key().encapsulate()
+        assert oracle.batch_dec(alg, 1, ct_c, sk) == ss_c
+        bad = _fips203_tamper(ct_c, t)
+        assert oracle.batch_dec(alg, 1, bad, sk) == key.decapsulate(bad)
