@@ -13,8 +13,14 @@ shared secrets inside the timed region).  The fused path is the headline; the pl
 
 Multi-GPU (torchrun): every rank runs an independent replica on its own GPU (KEM instances are
 independent; no collective on the data path), `value` = pairs of all ranks / max rank time.
---impl reference: times the CPU restatement of the same workload (the reference has no round-3
-Kyber-768 KEM code) on all host cores of rank 0 and prints the reference line.
+--impl reference: times the reference's own code on the host cores of rank 0 -- its Kyber device
+code (round-2 arithmetic; it has no KEM layer) compiled for the host by oracle/build_ref.sh, one
+process per core, Kyber-768 CPA encryption + decryption pairs -- and prints the reference line;
+where that build is missing, the CPU restatement of the KEM workload (oracle/) instead.
+
+The default line also carries three secondary measurements, each with its own clock record:
+serving at 50 % of the measured peak (p50 / p99), the mixed Kyber batch (k = 2/3/4, n ~
+U{1..65536}), and Kyber-768 single-instance latency.  --no-extras leaves them out.
 
 --config prints one line per configuration instead:
 * kyber512, kyber1024, newhope1024, frodo976, newhope512, frodo640, frodo1344: keypair / enc / dec
@@ -65,6 +71,7 @@ def parse():
     p.add_argument("--path", default="fused", choices=["fused", "plain"])
     p.add_argument("--no-plain", action="store_true", help="skip timing the plain path beside the fused one")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-extras", action="store_true", help="skip the serving / mixed / latency keys of the default line")
     p.add_argument("--slots", type=int, default=12, help="serving: batches in flight (worker threads)")
     p.add_argument("--config", default=None,
                    choices=["kyber512", "kyber1024", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344", "mixed", "serving",
@@ -147,8 +154,8 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_baseline(nsample=16384, nthreads=0):
-    """The CPU restatement (oracle/, C with OpenMP) on a bounded sample of the same workload."""
+def cpu_baseline_port(nsample=16384, nthreads=0):
+    """The CPU restatement (oracle/, C with OpenMP) of the Kyber-768 KEM on a bounded sample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
     from pqc_gb300 import drbg
@@ -164,8 +171,41 @@ def cpu_baseline(nsample=16384, nthreads=0):
     assert ss == ss2
     cores = nthreads if nthreads > 0 else os.cpu_count()
     return {"value": nsample / el, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d Kyber-768 enc+dec pairs, keys pre-generated, OpenMP over instances" % nsample,
-            "seconds": el}
+            "sample": "%d Kyber-768 KEM enc+dec pairs (round 3) by the CPU restatement, keys pre-generated, "
+                      "OpenMP over instances" % nsample, "seconds": el}
+
+
+REF_SAMPLE = ("Kyber-768 CPA encryption + decryption pairs by the reference's own code (Kyber_GPU_Batched "
+              "indcpa_enc / indcpa_dec, round-2 arithmetic; the reference has no KEM layer), host-compiled "
+              "from its sources (oracle/build_ref.sh), one process per core, %d pairs per round")
+
+
+def reference_cpu(reps=4, chunk=256):
+    """The reference's own host-compiled Kyber code on all host cores (oracle/refcpu.py), or None
+    where its build is missing."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import refcpu
+    if not refcpu.available(3):
+        return None
+    r = refcpu.RefKyberCPU(3, chunk=chunk)
+    try:
+        r.run(1)  # warm-up: the processes allocate their state
+        pairs, el, ok = r.run(reps)
+    finally:
+        r.close()
+    return {"value": pairs / el, "unit": UNIT, "cores": r.procs, "kind": "reference",
+            "sample": REF_SAMPLE % (r.procs * chunk), "pairs": pairs, "seconds": el, "roundtrip_ok": ok,
+            "cpu": refcpu.cpu_model()}
+
+
+def cpu_baseline():
+    """The reference's own code where it built (kind "reference"), with the port beside it."""
+    port = cpu_baseline_port()
+    ref = reference_cpu()
+    if ref is None:
+        return port
+    ref["port"] = port
+    return ref
 
 
 def work_per_pair():
@@ -192,52 +232,75 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    nthreads = 0
-    sample = 16384
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle as O
-    from pqc_gb300 import drbg
-    a = O.KYBER768
-    s = O.alg_sizes(a)
-    seed = drbg.seed48(777)
-    pk, sk = O.batch_keypair(a, sample, drbg.stream(seed, b"kp", sample * s["kp_coins"]), nthreads)
-    times = []
-    for step in range(args.warmup + args.steps):
-        ec = drbg.stream(seed, b"enc%d" % step, sample * s["enc_coins"])
-        t0 = time.perf_counter()
-        ct, ss = O.batch_enc(a, sample, pk, ec, nthreads)
-        ss2 = O.batch_dec(a, sample, ct, sk, nthreads)
-        el = time.perf_counter() - t0
-        assert ss == ss2
-        if step >= args.warmup:
-            times.append(el)
+    import refcpu
+    if refcpu.available(3):
+        chunk = 256
+        r = refcpu.RefKyberCPU(3, chunk=chunk)
+        times, pairs, ok = [], 0, True
+        try:
+            for step in range(args.warmup + args.steps):
+                n, el, good = r.run(1)
+                ok = ok and good
+                if step >= args.warmup:
+                    times.append(el)
+                    pairs += n
+        finally:
+            r.close()
+        kind, cores, sample = "reference", r.procs, REF_SAMPLE % (r.procs * chunk)
+        extra = {"roundtrip_ok": ok, "cpu": refcpu.cpu_model(), "port_kem": cpu_baseline_port()}
+    else:
+        import pyoracle as O
+        from pqc_gb300 import drbg
+        a = O.KYBER768
+        s = O.alg_sizes(a)
+        sample_n = 16384
+        seed = drbg.seed48(777)
+        pk, sk = O.batch_keypair(a, sample_n, drbg.stream(seed, b"kp", sample_n * s["kp_coins"]))
+        times, pairs = [], 0
+        for step in range(args.warmup + args.steps):
+            ec = drbg.stream(seed, b"enc%d" % step, sample_n * s["enc_coins"])
+            t0 = time.perf_counter()
+            ct, ss = O.batch_enc(a, sample_n, pk, ec)
+            ss2 = O.batch_dec(a, sample_n, ct, sk)
+            el = time.perf_counter() - t0
+            assert ss == ss2
+            if step >= args.warmup:
+                times.append(el)
+                pairs += sample_n
+        kind, cores = "port", os.cpu_count()
+        sample = ("%d Kyber-768 KEM pairs per step by the CPU restatement (oracle/, C + OpenMP): the reference's "
+                  "host build is missing" % sample_n)
+        extra = {}
     tot = sum(times)
-    v = sample * len(times) / tot
+    v = pairs / tot
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
         "data": "synthetic (SHAKE-256 DRBG seeded coins)",
-        "config": {"workload": "kyber768 enc+dec, %d-pair sample per step on host cores" % sample,
-                   "alg": ALG, "batch": args.batch, "parallelism": "host threads"},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                         "sample": "%d pairs per step; the reference tree has no round-3 Kyber-768 KEM, so its "
-                                   "CPU restatement (oracle/, C + OpenMP) is timed" % sample},
+        "config": {"workload": "kyber768 enc+dec, a bounded sample per step on the host cores",
+                   "alg": ALG, "batch": args.batch, "parallelism": "host processes"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    line.update(extra)
     print(json.dumps(line), flush=True)
 
 
-def run_configs(args):
-    """Secondary configurations, one JSON line each (not the headline metric)."""
+def clocked(fn, device=0):
+    """Run fn() with the nvidia-smi clock sampler around it; returns (result, clocks)."""
+    c = ClockSampler(device)
+    c.start()
+    try:
+        r = fn()
+    finally:
+        clk = c.stop()
+    return r, clk
+
+
+def make_timer(ctx, st):
     import torch
-    from pqc_gb300 import drbg, kem
-    dev = torch.device("cuda", 0)
-    ctx = kem.Context(0)
-    st = torch.cuda.ExternalStream(ctx.stream, device=dev)
-    up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
-    which = (["kyber512", "kyber1024", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344", "mixed", "serving", "refgpu",
-              "latency"] if args.config == "all" else [args.config])
 
     def timed(fn, reps):
         fn()
@@ -249,6 +312,100 @@ def run_configs(args):
         e1.record(st)
         e1.synchronize()
         return e0.elapsed_time(e1) / reps
+    return timed
+
+
+def measure_mixed(ctx, dev, up, timed, reps=3):
+    """The mixed Kyber batch (pqc_gb300.workload.mixed_kyber_spec: 24 launches, k = 2/3/4 at
+    40/40/20, n ~ U{1..65536}, ops 1/3 each) through the mixed-batch call, its graph replay, one
+    kernel per stage, and the single-job calls one after another."""
+    import torch
+    from pqc_gb300 import drbg, kem
+    from pqc_gb300.workload import mixed_kyber_spec
+    jobs, total, keep = [], 0, []
+    for j, (alg, op, n) in enumerate(mixed_kyber_spec()):
+        s = kem.sizes(alg)
+        seed = drbg.seed48(200 + j)
+        kc = up(drbg.stream(seed, b"kp", n * s["kp_coins"]))
+        pk, sk = (torch.empty(n * s[x], dtype=torch.uint8, device=dev) for x in ("pk", "sk"))
+        ctx.keypair_dev(alg, n, pk, sk, kc)
+        if op == "keypair":
+            jobs.append((alg, op, n, kc, None, torch.empty_like(pk), torch.empty_like(sk)))
+        else:
+            ec = up(drbg.stream(seed, b"enc", n * s["enc_coins"]))
+            ct = torch.empty(n * s["ct"], dtype=torch.uint8, device=dev)
+            ss = torch.empty(n * s["ss"], dtype=torch.uint8, device=dev)
+            ctx.enc_dev(alg, n, ct, ss, pk, ec)
+            if op == "enc":
+                jobs.append((alg, op, n, pk, ec, torch.empty_like(ct), torch.empty_like(ss)))
+            else:
+                jobs.append((alg, op, n, ct, sk, torch.empty_like(ss), None))
+                keep.append((len(jobs) - 1, ss))
+        total += n
+    ctx.wait()
+    t_mixed = timed(lambda: ctx.mixed_dev(jobs), reps)
+    ok = all(torch.equal(jobs[i][5], ss) for i, ss in keep)
+    t_stage = timed(lambda: ctx.mixed_dev(jobs, kem.STAGE_KERNELS), reps)
+    ok = ok and all(torch.equal(jobs[i][5], ss) for i, ss in keep)
+    g = ctx.graph(jobs)
+    t_graph = timed(g.launch, reps)
+    ok = ok and all(torch.equal(jobs[i][5], ss) for i, ss in keep)
+    g.close()
+
+    def sequential():
+        for alg, op, n, in0, in1, out0, out1 in jobs:
+            if op == "keypair":
+                ctx.keypair_dev(alg, n, out0, out1, in0)
+            elif op == "enc":
+                ctx.enc_dev(alg, n, out0, out1, in0, in1)
+            else:
+                ctx.dec_dev(alg, n, out0, in0, in1)
+
+    t_seq = timed(sequential, reps)
+    return {"metric": "mixed Kyber batch ops/s", "jobs": len(jobs), "instances": total,
+            "mixed_batch_per_s": total / t_mixed * 1e3, "graph_replay_per_s": total / t_graph * 1e3,
+            "sequential_per_s": total / t_seq * 1e3, "stage_kernels_per_s": total / t_stage * 1e3,
+            "what": "mixed_batch (default): every job's own kernels over 8 streams; stage_kernels: one kernel per "
+                    "Kyber core stage for all jobs; sequential: the single-job calls one after another",
+            "mix": "k=2/3/4 at 40/40/20, n ~ U{1..65536}, ops 1/3 each", "bit_exact_decaps": bool(ok)}
+
+
+def measure_serving(slots, fractions=(0.1, 0.3, 0.5, 0.7, 0.9), seconds=1.5):
+    """Continuous batching under Poisson load at fractions of the measured peak (native load
+    generator, pqcgpu_server_run_poisson); the peak is the rate achieved at saturation."""
+    from pqc_gb300 import serve
+    with serve.Server(0, budget=16 << 30, max_inflight=slots, max_batch=4096) as srv:
+        sat = srv.run_poisson(serve.SERVING_MIX, rate=2e6, seconds=1.0, seed=1)
+        peak = sat["achieved_per_s"]
+        # Saturation forms only large batches; a short low-load pass (discarded) makes the first
+        # launches of the small-batch kernels (and their lazy module loads) before any timed point.
+        srv.run_poisson(serve.SERVING_MIX, rate=0.05 * peak, seconds=0.5, seed=7)
+        points = []
+        for frac in fractions:
+            r = srv.run_poisson(serve.SERVING_MIX, rate=frac * peak, seconds=seconds, seed=int(frac * 100))
+            groups = {"%s/%s" % (alg, op): srv.group_stats(alg, op) for alg, op, _ in serve.SERVING_MIX}
+            points.append({"load": frac, "offered_per_s": r["offered_per_s"], "achieved_per_s": r["achieved_per_s"],
+                           "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "max_ms": r["max_ms"],
+                           "batches": r["batches"],
+                           "p99_ms_by_group": {g: round(v["p99_ms"], 3) for g, v in groups.items()},
+                           "p50_ms_by_group": {g: round(v["p50_ms"], 3) for g, v in groups.items()}})
+    return {"metric": "KEM serving latency under Poisson load", "slots": slots,
+            "mix": "60% Kyber-512/768/1024, 20% NewHope-1024, 20% FrodoKEM-976, ops equiprobable",
+            "keys": "resident on the device", "hbm_budget_gb": 16, "measured_peak_per_s": peak, "points": points}
+
+
+def run_configs(args):
+    """Secondary configurations, one JSON line each (not the headline metric), each with the clock
+    record of its own measurement."""
+    import torch
+    from pqc_gb300 import drbg, kem
+    dev = torch.device("cuda", 0)
+    ctx = kem.Context(0)
+    st = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
+    which = (["kyber512", "kyber1024", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344", "mixed", "serving", "refgpu",
+              "latency"] if args.config == "all" else [args.config])
+    timed = make_timer(ctx, st)
 
     for cfg in which:
         if cfg in ("kyber512", "kyber1024", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344"):
@@ -262,107 +419,48 @@ def run_configs(args):
             ss, ss2 = (torch.empty(n * s["ss"], dtype=torch.uint8, device=dev) for _ in range(2))
             torch.cuda.synchronize()
             reps = 3 if alg.startswith("frodo") else 10
-            tk = timed(lambda: ctx.keypair_dev(alg, n, pk, sk, kc), reps)
-            te = timed(lambda: ctx.enc_dev(alg, n, ct, ss, pk, ec), reps)
-            td = timed(lambda: ctx.dec_dev(alg, n, ss2, ct, sk), reps)
+
+            def rates():
+                tk = timed(lambda: ctx.keypair_dev(alg, n, pk, sk, kc), reps)
+                te = timed(lambda: ctx.enc_dev(alg, n, ct, ss, pk, ec), reps)
+                td = timed(lambda: ctx.dec_dev(alg, n, ss2, ct, sk), reps)
+                return tk, te, td
+
+            (tk, te, td), clk = clocked(rates)
             ctx.wait()
             print(json.dumps({"config": cfg, "batch": n, "metric": "%s ops/s per operation (device-resident)" % alg,
                               "keypair_per_s": n / tk * 1e3, "enc_per_s": n / te * 1e3, "dec_per_s": n / td * 1e3,
                               "keypair_enc_dec_chains_per_s": n / (tk + te + td) * 1e3,
-                              "bit_exact_roundtrip": bool(torch.equal(ss, ss2))}), flush=True)
+                              "bit_exact_roundtrip": bool(torch.equal(ss, ss2)), "clocks": clk}), flush=True)
         elif cfg == "mixed":
-            import random
-            rng = random.Random(12)
-            jobs, total = [], 0
-            keep = []
-            for j in range(24):
-                alg = rng.choices(["kyber512", "kyber768", "kyber1024"], [0.4, 0.4, 0.2])[0]
-                op = rng.choice(["keypair", "enc", "dec"])
-                n = rng.randint(1, 65536)
-                s = kem.sizes(alg)
-                seed = drbg.seed48(200 + j)
-                kc = up(drbg.stream(seed, b"kp", n * s["kp_coins"]))
-                pk, sk = (torch.empty(n * s[x], dtype=torch.uint8, device=dev) for x in ("pk", "sk"))
-                ctx.keypair_dev(alg, n, pk, sk, kc)
-                if op == "keypair":
-                    jobs.append((alg, op, n, kc, None, torch.empty_like(pk), torch.empty_like(sk)))
-                else:
-                    ec = up(drbg.stream(seed, b"enc", n * s["enc_coins"]))
-                    ct = torch.empty(n * s["ct"], dtype=torch.uint8, device=dev)
-                    ss = torch.empty(n * s["ss"], dtype=torch.uint8, device=dev)
-                    ctx.enc_dev(alg, n, ct, ss, pk, ec)
-                    if op == "enc":
-                        jobs.append((alg, op, n, pk, ec, torch.empty_like(ct), torch.empty_like(ss)))
-                    else:
-                        jobs.append((alg, op, n, ct, sk, torch.empty_like(ss), None))
-                        keep.append((len(jobs) - 1, ss))
-                total += n
-            ctx.wait()
-            t_mixed = timed(lambda: ctx.mixed_dev(jobs), 3)
-            ok = all(torch.equal(jobs[i][5], ss) for i, ss in keep)
-            t_stage = timed(lambda: ctx.mixed_dev(jobs, kem.STAGE_KERNELS), 3)
-            ok = ok and all(torch.equal(jobs[i][5], ss) for i, ss in keep)
-            g = ctx.graph(jobs)
-            t_graph = timed(g.launch, 3)
-            ok = ok and all(torch.equal(jobs[i][5], ss) for i, ss in keep)
-            g.close()
-            def sequential():
-                for alg, op, n, in0, in1, out0, out1 in jobs:
-                    if op == "keypair":
-                        ctx.keypair_dev(alg, n, out0, out1, in0)
-                    elif op == "enc":
-                        ctx.enc_dev(alg, n, out0, out1, in0, in1)
-                    else:
-                        ctx.dec_dev(alg, n, out0, in0, in1)
-
-            t_seq = timed(sequential, 3)
-            print(json.dumps({"config": "mixed", "metric": "mixed Kyber batch ops/s", "jobs": len(jobs),
-                              "instances": total, "mixed_batch_per_s": total / t_mixed * 1e3,
-                              "graph_replay_per_s": total / t_graph * 1e3, "sequential_per_s": total / t_seq * 1e3,
-                              "stage_kernels_per_s": total / t_stage * 1e3,
-                              "what": "mixed_batch (default): every job's own kernels over 8 streams; stage_kernels: "
-                                      "one kernel per Kyber core stage for all jobs; sequential: the single-job "
-                                      "calls one after another",
-                              "mix": "k=2/3/4 at 40/40/20, n ~ U{1..65536}, ops 1/3 each",
-                              "bit_exact_decaps": bool(ok)}), flush=True)
+            r, clk = clocked(lambda: measure_mixed(ctx, dev, up, timed))
+            r.update({"config": "mixed", "clocks": clk})
+            print(json.dumps(r), flush=True)
         elif cfg == "refgpu":
             run_refgpu(ctx, dev, up, timed)
         elif cfg == "latency":
-            run_latency(ctx, dev, up)
+            r, clk = clocked(lambda: measure_latency(ctx, dev, up))
+            r.update({"config": "latency", "clocks": clk})
+            print(json.dumps(r), flush=True)
         elif cfg == "serving":
-            from pqc_gb300 import serve
-            with serve.Server(0, budget=16 << 30, max_inflight=args.slots, max_batch=4096) as srv:
-                sat = srv.run_poisson(serve.SERVING_MIX, rate=2e6, seconds=1.0, seed=1)
-                peak = sat["achieved_per_s"]
-                # Saturation forms only large batches; a short low-load pass (discarded) makes the first
-                # launches of the small-batch kernels (and their lazy module loads) before any timed point.
-                srv.run_poisson(serve.SERVING_MIX, rate=0.05 * peak, seconds=0.5, seed=7)
-                points = []
-                for frac in (0.1, 0.3, 0.5, 0.7, 0.9):
-                    r = srv.run_poisson(serve.SERVING_MIX, rate=frac * peak, seconds=1.5, seed=int(frac * 100))
-                    groups = {"%s/%s" % (alg, op): srv.group_stats(alg, op) for alg, op, _ in serve.SERVING_MIX}
-                    points.append({"load": frac, "offered_per_s": r["offered_per_s"], "achieved_per_s": r["achieved_per_s"],
-                                   "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "max_ms": r["max_ms"],
-                                   "batches": r["batches"],
-                                   "p99_ms_by_group": {g: round(v["p99_ms"], 3) for g, v in groups.items()},
-                                   "p50_ms_by_group": {g: round(v["p50_ms"], 3) for g, v in groups.items()}})
-            print(json.dumps({"config": "serving", "metric": "KEM serving latency under Poisson load",
-                              "slots": args.slots,
-                              "mix": "60% Kyber-512/768/1024, 20% NewHope-1024, 20% FrodoKEM-976, ops equiprobable",
-                              "keys": "resident on the device", "hbm_budget_gb": 16,
-                              "measured_peak_per_s": peak, "points": points}), flush=True)
+            r, clk = clocked(lambda: measure_serving(args.slots))
+            r.update({"config": "serving", "clocks": clk})
+            print(json.dumps(r), flush=True)
     ctx.close()
 
 
-def run_latency(ctx, dev, up, reps=50):
-    """Single-instance latency (n = 1) of every operation of every algorithm, device-resident buffers,
-    CUDA events around each call on the library stream: p50 and p99 over `reps` calls."""
+LATENCY_ALGS = ("kyber512", "kyber768", "kyber1024", "mlkem768", "newhope1024", "newhope512", "frodo640", "frodo976",
+                "frodo1344")
+
+
+def measure_latency(ctx, dev, up, algs=LATENCY_ALGS, reps=50):
+    """Single-instance latency (n = 1) of every operation, device-resident buffers, CUDA events
+    around each call on the library stream: p50 and p99 over `reps` calls."""
     import torch
     from pqc_gb300 import drbg, kem
     st = torch.cuda.ExternalStream(ctx.stream, device=dev)
     out = {}
-    for alg in ("kyber512", "kyber768", "kyber1024", "mlkem768", "newhope1024", "newhope512", "frodo640", "frodo976",
-                "frodo1344"):
+    for alg in algs:
         s = kem.sizes(alg)
         seed = drbg.seed48(77)
         kc, ec = up(drbg.stream(seed, b"kp", s["kp_coins"])), up(drbg.stream(seed, b"enc", s["enc_coins"]))
@@ -387,8 +485,7 @@ def run_latency(ctx, dev, up, reps=50):
         ctx.wait()
         res["roundtrip_ok"] = bool(torch.equal(ss, ss2))
         out[alg] = res
-    print(json.dumps({"config": "latency", "metric": "single-instance latency (n = 1), device-resident",
-                      "reps": reps, "algs": out}), flush=True)
+    return {"metric": "single-instance latency (n = 1), device-resident", "reps": reps, "algs": out}
 
 
 def run_refgpu(ctx, dev, up, timed):
@@ -529,6 +626,9 @@ def main():
     prof = json.loads(buf.value.decode())
     clk = clocks.stop()
     ok = ok and torch.equal(ss, ss2)
+    # the last timed step's outputs against the oracle on a sample spread over the batch
+    oracle_ok = oracle_sample_check(ALG, B, pk, coins[W + K - 1], ct, ss)
+    ok = ok and oracle_ok
     step_ms = [a.elapsed_time(b) for a, b in evs]
     total_ms = evs[0][0].elapsed_time(evs[-1][1])
     total_ms = max_over_ranks(total_ms, world, dev)
@@ -622,9 +722,31 @@ def main():
                 "peak_source": "measured in this run: LOP3 throughput probe (pqcgpu_probe_peaks)",
                 "algorithmic_ops_per_launch": ops, "launch_ms": per_launch_ms,
                 "keccak_perms_per_s": B * perms / (per_launch_ms * 1e-3),
-                "keccak_perm_peak_per_s": io["keccak_perms_per_s"],
-                "hbm_gbs_io": None}
+                "keccak_perm_peak_per_s": io["keccak_perms_per_s"]}
+    io_bytes = B * (s["pk"] + s["enc_coins"] + s["ct"] + s["ss"] + s["ct"] + s["sk"] + s["ss"])
+    hbm_peak = measured_hbm_peak()
+    io_gbs = io_bytes / (total_ms / K * 1e-3) / 1e9
+    hbm_io = {"gbs": io_gbs, "bytes_per_step": io_bytes, "peak_gbs": hbm_peak,
+              "frac": (io_gbs / hbm_peak) if hbm_peak else None,
+              "what": "batch I/O of one step (enc: pk, coins in, ct, ss out; dec: ct, sk in, ss out) over the step "
+                      "time; peak = MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    if roof:
+        roof["hbm_gbs_io"] = hbm_io
     base = cpu_baseline()
+    extras = {}
+    if not args.no_extras:
+        timed = make_timer(ctx, st)
+        r, clk = clocked(lambda: measure_serving(args.slots, fractions=(0.5,)), local)
+        p50 = r["points"][0]
+        extras["serving"] = {"load": 0.5, "measured_peak_per_s": r["measured_peak_per_s"],
+                             "achieved_per_s": p50["achieved_per_s"], "p50_ms": p50["p50_ms"], "p99_ms": p50["p99_ms"],
+                             "max_ms": p50["max_ms"], "slots": args.slots, "mix": r["mix"], "clocks": clk}
+        r, clk = clocked(lambda: measure_mixed(ctx, dev, up, timed), local)
+        extras["mixed"] = {k: r[k] for k in ("instances", "jobs", "mixed_batch_per_s", "graph_replay_per_s",
+                                             "stage_kernels_per_s", "sequential_per_s", "bit_exact_decaps", "mix")}
+        extras["mixed"]["clocks"] = clk
+        r, clk = clocked(lambda: measure_latency(ctx, dev, up, algs=(ALG,)), local)
+        extras["latency_n1"] = dict(r["algs"][ALG], clocks=clk, alg=ALG)
     lat = sorted(step_ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -635,6 +757,7 @@ def main():
                    "l2": "inputs larger than L2 (%.0f MB of pk/sk/ct/coins per step)" %
                          (B * (s["pk"] + s["sk"] + s["ct"] + s["enc_coins"]) / 1e6)},
         "bit_exact_check": bool(ok),
+        "bit_exact_vs_oracle_sample": bool(oracle_ok),
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
                        "what": "one enc+dec batch of %d" % B},
         "plain": plain,
@@ -646,9 +769,36 @@ def main():
         "cpu_baseline": base,
         "clocks": clk,
     }
+    line.update(extras)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def oracle_sample_check(alg, n, pk, coins, ct, ss, count=256):
+    """The ciphertexts and shared secrets of one batched encapsulation (device tensors) against the
+    CPU oracle at `count` instance indices spread over the batch (instances are independent)."""
+    import random
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    from pqc_gb300 import kem
+    s = kem.sizes(alg)
+    rng = random.Random(n)
+    idx = sorted({0, n - 1} | {rng.randrange(i * n // count, (i + 1) * n // count) for i in range(count)})
+    hb = lambda t: bytes(t.cpu().numpy())  # noqa: E731
+    pkh, ch, cth, ssh = hb(pk), hb(coins), hb(ct), hb(ss)
+    rows = lambda b, sz: b"".join(b[i * sz:(i + 1) * sz] for i in idx)  # noqa: E731
+    oct_, oss = O.batch_enc(O.ALG_NAMES[alg], len(idx), rows(pkh, s["pk"]), rows(ch, s["enc_coins"]))
+    return oct_ == rows(cth, s["ct"]) and oss == rows(ssh, s["ss"])
+
+
+def measured_hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return None
 
 
 def ctypes_peaks(lib, device):

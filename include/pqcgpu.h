@@ -112,9 +112,24 @@ int pqcgpu_kem_dec_batch(pqcgpu_ctx *ctx, pqcgpu_alg alg, size_t n, uint8_t *ss,
  * threads) race and must be serialised by the caller.  Each call writes every scratch byte it
  * reads before reading it, so nothing left by an earlier call needs clearing.  The first call on
  * a device does the set-up (constant tables, lookup of the array's device address); make that
- * first call before any stream capture.  Leave the launch profiler off for this call. */
+ * first call before any stream capture.  The address is kept for the life of the process, so a
+ * device reset (cudaDeviceReset) between calls is not supported.  Leave the launch profiler off
+ * for this call. */
 int pqcgpu_kem_enc_batch_noalloc(pqcgpu_alg alg, size_t n, uint8_t *ct, uint8_t *ss, const uint8_t *pk,
                                  const uint8_t *coins, void *stream);
+
+/* ---- many FrodoKEM encapsulations to one public key --------------------------------------------
+ * n encapsulations to the one public key pk (alg = a FrodoKEM algorithm, pk = one key of
+ * CRYPTO_PUBLICKEYBYTES), coins = mu per instance (NULL: library DRBG, host buffers only): ct and ss
+ * per instance, the same bytes as pqcgpu_kem_enc_batch with pk repeated n times.  Replaces n calls of
+ * crypto_kem_enc (FrodoKEM_GPU/kem.c:66-131 via frodo976.cu:229-425), each of which regenerates
+ * the key's matrix A: here A is generated once per call, and the products B'_x = S'_x A of all
+ * instances (frodo_macrify_reference.cu:102-159) run as one matrix product, on the CUDA cores or on
+ * the tensor cores (launch-shape op 3 of the FrodoKEM algorithms: ni = 1 CUDA cores, 2 tensor
+ * cores, 0 the measured default).  Host buffers: synchronous; PQCGPU_DEVICE_PTRS: asynchronous on
+ * the context stream. */
+int pqcgpu_frodo_enc_shared_key_batch(pqcgpu_ctx *ctx, pqcgpu_alg alg, size_t n, uint8_t *ct, uint8_t *ss,
+                                      const uint8_t *pk, const uint8_t *coins, unsigned flags);
 
 /* ---- batched CPA-PKE (replaces indcpa_* of Kyber_GPU_Batched/indcpa.h:16-26) -------------
  * variant 2 = the reference's round-2 arithmetic, variant 3 = round-3 parameter sets; k = 2..4.
@@ -230,12 +245,15 @@ int pqcgpu_server_run_poisson(pqcgpu_server *server, const pqcgpu_mix_entry *mix
 /* ---- launch-shape tuning (used by the autotuner, pqc_gb300/autotune.py) --------------------
  * Core-kernel launch shape per (algorithm, operation): ni = instances per CTA, threads per CTA
  * (multiple of 32).  Kyber also takes op 3: the decryption stage of decapsulation (op 2 is then
- * its re-encryption stage).  Kyber: ni 1..128, threads from 32 up to the core kernel's launch bound
- * (keypair 512, encapsulation 256, re-encryption 192 for k = 3 and 256 otherwise, decryption stage
- * 384; shared by the round-2 and round-3 sets of the same k); NewHope: ni 1..64, threads 32..256.  FrodoKEM: keypair ni 0 or 1, threads 64 / 128 /
- * 256 (one row of A per thread); encaps / decaps ni = CTAs per instance sharing the rows of A
- * (1, 2, 4, 8, 16) with threads 128 / 256, or ni = 0 to choose by batch size (the default).
- * Applies to all contexts of the process. */
+ * its re-encryption stage), and op 4: ni = the largest KEM batch that runs on the single-instance
+ * kernels (one CTA per instance, every operation and k; 0 = never; threads ignored).  Kyber: ni
+ * 1..128, threads from 32 up to the core kernel's launch bound (keypair 512, encapsulation 256,
+ * re-encryption 256, decryption stage 384; shared by the round-2 and round-3 sets of the same k);
+ * NewHope: ni 1..64, threads 32..256.  FrodoKEM: keypair ni 0 or 1, threads 64 / 128 / 256 (one
+ * row of A per thread); encaps / decaps ni = CTAs per instance sharing the rows of A (1, 2, 4, 8,
+ * 16) with threads 128 / 256, or ni = 0 to choose by batch size (the default); op 3: ni = the
+ * product of pqcgpu_frodo_enc_shared_key_batch (1 CUDA cores, 2 tensor cores, 0 default).
+ * Applies to all contexts of the process; a launch reads the pair atomically. */
 int pqcgpu_set_launch_shape(pqcgpu_alg alg, int op, int ni, int threads);
 int pqcgpu_get_launch_shape(pqcgpu_alg alg, int op, int *ni, int *threads);
 

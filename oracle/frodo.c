@@ -16,6 +16,9 @@
  *                                                       table of FrodoKEM_GPU/frodo976.cu:21
  * The S / E stream is the standard SHAKE256(0x5F || seedSE) of kem.c:39 (resp. 0x96 at kem.c:96),
  * not the reference GPU path's shake256_kernel_single.
+ * FrodoKEM-976 is pinned to the reference's own code: tests/golden/ref_frodo976_kem.json holds the
+ * outputs of kem.c run with the reference's sampler, codecs, SHAKE and matrix kernels
+ * (oracle/ref_glue_frodo.cpp), and this restatement reproduces them.
  * All arithmetic is mod 2^16 (uint16 wrap-around), so the matrix products are exact; for log q = 15
  * values are reduced mod q where they are packed, compared or decoded.
  *

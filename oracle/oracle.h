@@ -8,13 +8,19 @@
  * load it.  The product library (libpqcgpu) never links or calls it.
  *
  * Parity status:
- *   - Keccak family: pinned against Python hashlib (tests/test_oracle_fips202.py).
- *   - Kyber round-2 CPA (k=4) and NewHope-1024 CPA: pinned against golden vectors produced by the
- *     reference's own device code compiled for the host (oracle/build_ref.sh, tests/golden/).
- *   - Kyber round-3 parameter sets, all KEM (Fujisaki-Okamoto) layers, NewHope CPA-KEM and
- *     FrodoKEM-976: restated from the published algorithms and the reference's host flow
- *     (FrodoKEM_GPU/kem.c); parity unpinned by reference outputs (no KAT files exist in the
- *     reference tree).
+ *   - Keccak family: pinned against Python hashlib (tests/golden/keccak.json).
+ *   - Kyber round-2 CPA (k = 2, 3, 4) and NewHope-1024 / -512 CPA: pinned against golden vectors
+ *     produced by the reference's own device code compiled for the host (oracle/build_ref.sh,
+ *     tests/golden/ref_*.json).
+ *   - FrodoKEM-976: pinned against the reference's own host KEM flow (FrodoKEM_GPU/kem.c) run with
+ *     the reference's sampler, pack / unpack, SHAKE, A generation and matrix kernels
+ *     (oracle/ref_glue_frodo.cpp, tests/golden/ref_frodo976_kem.json).
+ *   - ML-KEM-768 / -1024 (FIPS 203): pinned against an independent implementation, the
+ *     `cryptography` package (tests/golden/gen_fips203.py); this also pins the K-PKE arithmetic
+ *     that round-3 Kyber shares with ML-KEM.
+ *   - Round-3 Kyber's KEM hash layer, ML-KEM-512, NewHope CPA-KEM and FrodoKEM-640 / -1344:
+ *     restated from the published algorithms; parity unpinned by outputs of other code (the
+ *     reference tree has no code or KAT files for them).
  */
 #ifndef PQC_ORACLE_H
 #define PQC_ORACLE_H

@@ -101,3 +101,28 @@ extern "C" int ref_kyber_cpa_dec(int count, unsigned char *m, unsigned char *ct,
     free_set(&ps);
     return 0;
 }
+
+// The same two calls on a state allocated once (a CPU timing baseline: one state per host thread,
+// each thread on its own range of instances; the reference's kernels keep no other mutable state,
+// and the shim's thread indices are thread-local).
+extern "C" void *ref_kyber_state_new(void) {
+    poly_set4 *ps = (poly_set4 *)calloc(1, sizeof(poly_set4));
+    if (ps) alloc_set(ps);
+    return ps;
+}
+extern "C" void ref_kyber_state_free(void *st) {
+    if (!st) return;
+    free_set((poly_set4 *)st);
+    free(st);
+}
+extern "C" int ref_kyber_cpa_enc_state(void *st, int count, unsigned char *ct, unsigned char *m, unsigned char *pk,
+                                       unsigned char *coins) {
+    if (!st || count <= 0 || count > N_TESTS) return -1;
+    indcpa_enc(count, (poly_set4 *)st, ct, m, pk, coins, 0);
+    return 0;
+}
+extern "C" int ref_kyber_cpa_dec_state(void *st, int count, unsigned char *m, unsigned char *ct, unsigned char *sk) {
+    if (!st || count <= 0 || count > N_TESTS) return -1;
+    indcpa_dec(count, (poly_set4 *)st, m, ct, sk, 0);
+    return 0;
+}

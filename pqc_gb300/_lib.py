@@ -25,6 +25,7 @@ SIGNATURES = {
     "pqcgpu_kem_enc_batch": (_int, [_vp, _int, _sz, _u8p, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_kem_dec_batch": (_int, [_vp, _int, _sz, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_kem_enc_batch_noalloc": (_int, [_int, _sz, _u8p, _u8p, _u8p, _u8p, _vp]),
+    "pqcgpu_frodo_enc_shared_key_batch": (_int, [_vp, _int, _sz, _u8p, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_kyber_indcpa_keypair_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_kyber_indcpa_enc_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _u8p, _uint]),
     "pqcgpu_kyber_indcpa_dec_batch": (_int, [_vp, _int, _int, _sz, _u8p, _u8p, _u8p, _uint]),

@@ -4,8 +4,10 @@ Replaces the reference's ANALYSIS_MODE block-size sweep (Kyber_GPU_Batched/indcp
 re-ran every launch over ten block sizes and printed the best: here each (algorithm, operation) is
 timed with CUDA events over a candidate grid at a given batch size (FrodoKEM: the split of an
 instance's rows of A over CTAs, at serving-size batches), the fastest shape is applied
-through pqcgpu_set_launch_shape, and the choice is persisted in a JSON cache keyed by GPU name so
-later processes load it instead of re-tuning.
+through pqcgpu_set_launch_shape, and the choice is persisted in a JSON cache keyed by GPU name and
+library version so later processes load it instead of re-tuning.  A candidate counts only if its
+outputs equal the outputs at the shape in force when tuning started (byte for byte); a candidate
+that is refused, fails or differs is skipped, and an operation keeps its shape when none is left.
 
     python -m pqc_gb300.autotune [--batch 65536] [--out tuning.json]
 """
@@ -72,16 +74,30 @@ def tune(batch=65536, algs=TUNABLE, reps=3, device=0, log=print):
         ctx.keypair_dev(alg, n, pk, sk, kc)
         ctx.enc_dev(alg, n, ct, ss, pk, ec)
         ctx.wait()
+        # a tampered copy of every third ciphertext, so that the decapsulation check also runs
+        # the implicit-rejection path at each candidate shape
+        ct_bad = ct.clone()
+        ct_bad[::3 * s["ct"]] ^= 1
         fns = {0: lambda: ctx.keypair_dev(alg, n, pk, sk, kc), 1: lambda: ctx.enc_dev(alg, n, ct, ss, pk, ec),
-               2: lambda: ctx.dec_dev(alg, n, ss2, ct, sk), 3: lambda: ctx.dec_dev(alg, n, ss2, ct, sk)}
+               2: lambda: ctx.dec_dev(alg, n, ss2, ct_bad, sk), 3: lambda: ctx.dec_dev(alg, n, ss2, ct_bad, sk)}
+        outs = {0: (pk, sk), 1: (ct, ss), 2: (ss2,), 3: (ss2,)}
         for op in ((0, 1, 3, 2) if alg.startswith("kyber") else (0, 1, 2)):
+            start = get_shape(lib, alg, op)
+            fns[op]()
+            ctx.wait()
+            want = [t.clone() for t in outs[op]]
             best = None
             for ni, thr in candidates(alg, op):
                 if lib.pqcgpu_set_launch_shape(kem.alg_id(alg), op, ni, thr) != 0:
                     continue
                 try:
+                    for t in outs[op]:
+                        t.zero_()
                     fns[op]()
                     ctx.wait()
+                    if not all(torch.equal(t, w) for t, w in zip(outs[op], want)):
+                        log("%s op %d: ni=%d threads=%d gives different outputs; skipped" % (alg, op, ni, thr))
+                        continue
                     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                     e0.record(st)
                     for _ in range(reps):
@@ -93,11 +109,20 @@ def tune(batch=65536, algs=TUNABLE, reps=3, device=0, log=print):
                     continue
                 if best is None or ms < best[0]:
                     best = (ms, ni, thr)
+            if best is None:
+                if start is not None:
+                    lib.pqcgpu_set_launch_shape(kem.alg_id(alg), op, start[0], start[1])
+                log("%s op %d: no candidate ran; shape kept at %s" % (alg, op, start))
+                continue
             lib.pqcgpu_set_launch_shape(kem.alg_id(alg), op, best[1], best[2])
             result["%s/%d" % (alg, op)] = {"ni": best[1], "threads": best[2], "ms": best[0], "batch": n}
             log("%s op %d: ni=%d threads=%d  %.3f ms" % (alg, op, best[1], best[2], best[0]))
     ctx.close()
-    return {"gpu": torch.cuda.get_device_name(dev), "shapes": result}
+    return {"gpu": torch.cuda.get_device_name(dev), "library": library_version(), "shapes": result}
+
+
+def library_version():
+    return _lib.load().pqcgpu_version().decode()
 
 
 def save(tuning, path=DEFAULT_CACHE):
@@ -106,25 +131,30 @@ def save(tuning, path=DEFAULT_CACHE):
         json.dump(tuning, f, indent=1)
 
 
-def apply(tuning):
-    """Apply a tuning dict (or a path to its JSON) to the loaded library."""
+def apply(tuning, log=print):
+    """Apply a tuning dict (or a path to its JSON) to the loaded library.  An entry the library
+    refuses (e.g. a shape outside the current kernels' launch bounds) is skipped with a message."""
     if isinstance(tuning, str):
         with open(tuning) as f:
             tuning = json.load(f)
     lib = _lib.load()
     for key, v in tuning["shapes"].items():
         alg, op = key.split("/")
-        _lib.check(lib.pqcgpu_set_launch_shape(kem.alg_id(alg), int(op), v["ni"], v["threads"]))
+        if lib.pqcgpu_set_launch_shape(kem.alg_id(alg), int(op), v["ni"], v["threads"]) != 0:
+            log("tuning entry %s (%d, %d) refused by this library; default kept" % (key, v["ni"], v["threads"]))
     return tuning
 
 
 def load_cached(path=DEFAULT_CACHE, gpu_name=None):
-    """Apply the cached tuning if it exists and was made on this GPU model; returns it or None."""
+    """Apply the cached tuning if it exists and was made on this GPU model with this library
+    version; returns it or None."""
     if not os.path.exists(path):
         return None
     with open(path) as f:
         t = json.load(f)
     if gpu_name is not None and t.get("gpu") != gpu_name:
+        return None
+    if t.get("library") != library_version():
         return None
     return apply(t)
 

@@ -235,7 +235,7 @@ struct pqcgpu_ctx {
     cudaStream_t pipe[NPAR] = {};
     cudaEvent_t in_ev[NSLOT] = {}, done_ev[NSLOT] = {}, free_ev[NSLOT] = {};
     cudaEvent_t fork_ev = nullptr, join_ev[NPAR] = {};
-    cudaEvent_t stage_ev[NPAR] = {}, core_ev = nullptr;  // mixed Kyber stages: hashes -> core -> hashes
+    cudaEvent_t stage_ev[NPAR] = {}, stage_ev2[NPAR] = {}, core_ev = nullptr;  // mixed Kyber waves and their hashes
     bool own_stream = true;
     size_t budget = 0;
     uint8_t *arena = nullptr;
@@ -318,7 +318,8 @@ extern "C" int pqcgpu_ctx_create(pqcgpu_ctx **out, int device, size_t budget) {
     for (int i = 0; i < pqcgpu_ctx::NPAR; i++) {
         if ((rc = cuda_err(cudaStreamCreateWithFlags(&c->par[i], cudaStreamNonBlocking), "stream")) ||
             (rc = cuda_err(cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming), "event")) ||
-            (rc = cuda_err(cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming), "event"))) {
+            (rc = cuda_err(cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming), "event")) ||
+            (rc = cuda_err(cudaEventCreateWithFlags(&c->stage_ev2[i], cudaEventDisableTiming), "event"))) {
             pqcgpu_ctx_destroy(c);
             return rc;
         }
@@ -372,6 +373,7 @@ extern "C" int pqcgpu_ctx_destroy(pqcgpu_ctx *c) {
         if (c->par[i]) cudaStreamDestroy(c->par[i]);
         if (c->join_ev[i]) cudaEventDestroy(c->join_ev[i]);
         if (c->stage_ev[i]) cudaEventDestroy(c->stage_ev[i]);
+        if (c->stage_ev2[i]) cudaEventDestroy(c->stage_ev2[i]);
     }
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->core_ev) cudaEventDestroy(c->core_ev);
@@ -764,6 +766,7 @@ static int check_jobs(const pqcgpu_job *jobs, size_t njobs, int plain, size_t *s
         if (offs) offs[i] = tot;
         tot += (op_scratch_bytes(j.alg, j.op, plain) * j.n + 255) & ~(size_t)255;
     }
+    if (offs) offs[njobs] = tot;  // 256 bytes past the jobs' scratch: the persistent waves' counters
     *scratch_total = tot;
     return PQCGPU_OK;
 }
@@ -776,24 +779,24 @@ static int launch_jobs(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, uint
     const int used = pqcgpu_ctx::NPAR;  // every parallel stream joins back (some may stay idle)
     for (int i = 0; i < used; i++)
         if ((rc = cuda_err(cudaStreamWaitEvent(c->par[i], c->fork_ev, 0), "wait event"))) return rc;
-    // With stage_kernels, the Kyber encapsulations / decapsulations of round-3 arithmetic (all k, FO
-    // or ML-KEM) get one kernel per core stage for all of them: their per-job hash kernels spread
-    // over the first HS parallel streams, the core launches run on par[0] once those are done, and
-    // the other jobs round-robin over the remaining streams.  Otherwise every job's own kernels
-    // round-robin over all streams (measured faster on GB300: each k keeps its tuned shape).
+    // With stage_kernels, the Kyber key generations, encapsulations and decapsulations of round-3
+    // arithmetic (all k, FO or ML-KEM) run their core stages as two persistent waves for all of them
+    // (kyber_mixed.cu) on par[0]; their per-job hash kernels spread over the first HS parallel
+    // streams around the waves, and the other jobs round-robin over the remaining streams.
+    // Otherwise every job's own kernels round-robin over all streams.
     constexpr int HS = pqcgpu_ctx::NPAR / 2;
     std::vector<MixedKyberJob> mix[3];
     std::vector<size_t> rest;
     for (size_t i = 0; i < njobs; i++) {
         const pqcgpu_job &j = jobs[i];
         int variant = 0, k = 0;
-        if (!plain && stage_kernels && (j.op == 1 || j.op == 2) && kyber_alg(j.alg, &variant, &k) && variant == 3)
+        if (!plain && stage_kernels && kyber_alg(j.alg, &variant, &k) && variant == 3 && j.n > 0)
             mix[j.op].push_back(MixedKyberJob{k, kyber_kem_mode(j.alg), (int)j.n, j.in0, j.in1, j.out0, j.out1,
                                               scratch + offs[i]});
         else
             rest.push_back(i);
     }
-    const bool mixed = mix[1].size() + mix[2].size() >= 2;
+    const bool mixed = mix[0].size() + mix[1].size() + mix[2].size() >= 2;
     if (!mixed) {
         rest.clear();
         for (size_t i = 0; i < njobs; i++) rest.push_back(i);
@@ -806,24 +809,43 @@ static int launch_jobs(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, uint
         if (rc) return set_err(rc, "job launch failed");
     }
     if (mixed) {
+        unsigned *counters = reinterpret_cast<unsigned *>(scratch + offs[njobs]);
+        auto join_into_main = [&](cudaEvent_t *evs) {  // par[0] waits for par[1 .. HS)
+            for (int i = 1; i < HS; i++) {
+                int r = cuda_err(cudaEventRecord(evs[i], c->par[i]), "event record");
+                if (!r) r = cuda_err(cudaStreamWaitEvent(c->par[0], evs[i], 0), "wait event");
+                if (r) return r;
+            }
+            return (int)PQCGPU_OK;
+        };
+        auto fork_from_main = [&]() {  // par[1 .. HS) wait for par[0]
+            int r = cuda_err(cudaEventRecord(c->core_ev, c->par[0]), "event record");
+            for (int i = 1; i < HS && !r; i++) r = cuda_err(cudaStreamWaitEvent(c->par[i], c->core_ev, 0), "wait event");
+            return r;
+        };
         int q = 0;
-        for (int op = 1; op <= 2; op++)
+        for (int op = 0; op <= 2; op++)  // phase 0 hashes
             for (const auto &j : mix[op])
-                if ((rc = kyber_mixed_hash(op, true, j, c->par[q++ % HS]))) return set_err(rc, "job launch failed");
-        for (int i = 1; i < HS; i++) {
-            if ((rc = cuda_err(cudaEventRecord(c->stage_ev[i], c->par[i]), "event record"))) return rc;
-            if ((rc = cuda_err(cudaStreamWaitEvent(c->par[0], c->stage_ev[i], 0), "wait event"))) return rc;
+                if ((rc = kyber_mixed_hash(op, 0, j, c->par[q++ % HS]))) return set_err(rc, "job launch failed");
+        if ((rc = join_into_main(c->stage_ev))) return rc;
+        if ((rc = kyber_mixed_wave(0, mix, counters, c->par[0]))) return set_err(rc, "mixed Kyber launch failed");
+        if ((rc = fork_from_main())) return rc;
+        q = 1;
+        for (const auto &j : mix[2])  // decapsulation's G between the waves, on par[1 .. HS)
+            if ((rc = kyber_mixed_hash(2, 1, j, c->par[1 + (q++ - 1) % (HS - 1)]))) return set_err(rc, "job launch failed");
+        if (!mix[2].empty()) {
+            if ((rc = join_into_main(c->stage_ev2))) return rc;
+            if ((rc = kyber_mixed_wave(1, mix, counters, c->par[0]))) return set_err(rc, "mixed Kyber launch failed");
         }
-        for (int op = 1; op <= 2; op++)
-            if (!mix[op].empty() && (rc = kyber_mixed_core(op, mix[op].data(), (int)mix[op].size(), c->par[0])))
-                return set_err(rc, "mixed Kyber launch failed");
-        if (!mix[1].empty()) {
-            if ((rc = cuda_err(cudaEventRecord(c->core_ev, c->par[0]), "event record"))) return rc;
-            for (int i = 1; i < HS; i++)
-                if ((rc = cuda_err(cudaStreamWaitEvent(c->par[i], c->core_ev, 0), "wait event"))) return rc;
-            q = 0;
-            for (const auto &j : mix[1])
-                if ((rc = kyber_mixed_hash(1, false, j, c->par[q++ % HS]))) return set_err(rc, "job launch failed");
+        q = 1;
+        for (int op = 0; op <= 1; op++)  // keypair / encapsulation phase 2 hashes, after wave 0
+            for (const auto &j : mix[op])
+                if ((rc = kyber_mixed_hash(op, 2, j, c->par[1 + (q++ - 1) % (HS - 1)]))) return set_err(rc, "job launch failed");
+        if (!mix[2].empty()) {
+            if ((rc = fork_from_main())) return rc;
+            q = 1;
+            for (const auto &j : mix[2])
+                if ((rc = kyber_mixed_hash(2, 2, j, c->par[1 + (q++ - 1) % (HS - 1)]))) return set_err(rc, "job launch failed");
         }
     }
     for (int i = 0; i < used; i++) {
@@ -909,6 +931,54 @@ extern "C" int pqcgpu_graph_destroy(pqcgpu_graph *g) {
     if (g->graph) cudaGraphDestroy(g->graph);
     if (g->scratch) cudaFree(g->scratch);
     delete g;
+    return PQCGPU_OK;
+}
+
+// ---- many FrodoKEM encapsulations to one public key ----
+extern "C" int pqcgpu_frodo_enc_shared_key_batch(pqcgpu_ctx *c, pqcgpu_alg alg, size_t n, uint8_t *ct, uint8_t *ss,
+                                                 const uint8_t *pk, const uint8_t *coins, unsigned flags) {
+    AlgInfo ai;
+    const int N = frodo_n(alg);
+    if (!c || !N || !alg_info(alg, &ai)) return set_err(PQCGPU_EINVAL, "bad context, or not a FrodoKEM algorithm");
+    if (n == 0) return PQCGPU_OK;
+    if (n > ((size_t)1 << 20)) return set_err(PQCGPU_EINVAL, "n above 2^20");
+    if (!ct || !ss || !pk) return set_err(PQCGPU_EINVAL, "null buffer");
+    CoinsHolder h;
+    int rc = coins_or_drbg(c, coins, n * ai.encc, flags, h, nullptr, 0);
+    if (rc) return rc;
+    const bool dev = (flags & PQCGPU_DEVICE_PTRS) != 0;
+    if (dev && (((uintptr_t)ct | (uintptr_t)ss | (uintptr_t)pk | (uintptr_t)coins) & 15))
+        return set_err(PQCGPU_EINVAL, "device buffers must be 16-byte aligned");
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    if ((rc = cuda_err(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t scr = up(n * frodo_scratch_bytes(N)), extra = up(frodo_shared_extra_bytes(N));
+    const size_t io = dev ? 0 : up(ai.pk) + up(n * ai.encc) + up(n * ai.ct) + up(n * ai.ss);
+    if ((rc = c->reserve(scr + extra + io))) return rc;
+    uint8_t *b = c->arena, *scratch = b, *ex = b + scr;
+    const uint8_t *dpk = pk, *dmu = coins;
+    uint8_t *dct = ct, *dss = ss;
+    cudaStream_t st = c->stream;
+    if (!dev) {
+        uint8_t *q = b + scr + extra;
+        uint8_t *bpk = q, *bmu = q + up(ai.pk);
+        dct = bmu + up(n * ai.encc);
+        dss = dct + up(n * ai.ct);
+        if ((rc = cuda_err(cudaMemcpyAsync(bpk, pk, ai.pk, cudaMemcpyHostToDevice, st), "copy in")) ||
+            (rc = cuda_err(cudaMemcpyAsync(bmu, coins, n * ai.encc, cudaMemcpyHostToDevice, st), "copy in")))
+            return rc;
+        dpk = bpk;
+        dmu = bmu;
+    }
+    if ((rc = frodo_enc_shared_dev(N, (int)n, dct, dss, dpk, dmu, scratch, ex, st))) return set_err(rc, "launch failed");
+    if (dev) return PQCGPU_OK;
+    unsigned err = 0;
+    if ((rc = cuda_err(cudaMemcpyAsync(ct, dct, n * ai.ct, cudaMemcpyDeviceToHost, st), "copy out")) ||
+        (rc = cuda_err(cudaMemcpyAsync(ss, dss, n * ai.ss, cudaMemcpyDeviceToHost, st), "copy out")) ||
+        (rc = cuda_err(cudaMemcpyAsync(&err, ex + 64, sizeof err, cudaMemcpyDeviceToHost, st), "copy out")) ||
+        (rc = cuda_err(cudaStreamSynchronize(st), "synchronize")))
+        return rc;
+    if (err) return set_err(PQCGPU_ECUDA, "tensor-core product: a wait ran out");
     return PQCGPU_OK;
 }
 

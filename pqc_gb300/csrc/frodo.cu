@@ -21,6 +21,7 @@
 // 16 / 24 / 32-byte seeds and keys, SHAKE128 (640) or SHAKE256 (976, 1344) for every hash and for
 // the noise stream, and their CDF tables.  Every value is computed mod 2^16 and reduced mod q when
 // packed, compared or decoded.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -236,16 +237,17 @@ __device__ __forceinline__ void zero_gacc(uint8_t *scr, int lane) {
 }
 
 // pkh != nullptr: pkh = SHAKE(pk, SSB) is given (the tail of a resident secret key, SSB bytes at
-// pkh + x * SSB), which skips the serial permutations of hashing the public key.
+// pkh + x * pkh_stride; stride 0 when every instance encapsulates to one key), which skips the
+// serial permutations of hashing the public key.
 template <int N>
 __global__ void __launch_bounds__(128) fr_enc_pre(int n, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
-                                                  int split, const uint8_t *pkh) {
+                                                  int split, const uint8_t *pkh, int pkh_stride) {
     using P = FP<N>;
     FR_WARP_INSTANCE;
     if (split > 1) zero_gacc<N>(scratch + (size_t)x * P::SCRATCH, w.lane);
     uint2 a;
     if (pkh) {
-        const uint2 *h = reinterpret_cast<const uint2 *>(pkh + (size_t)x * P::SSB);
+        const uint2 *h = reinterpret_cast<const uint2 *>(pkh + (size_t)x * pkh_stride);
         a = w.lane < P::NW ? h[w.lane] : make_uint2(0, 0);
     } else {
         warp_absorb2<P::RATE>(a, reinterpret_cast<const uint2 *>(pk + (size_t)x * P::PKB), P::PKB / 8, nullptr, 0,
@@ -555,6 +557,102 @@ __global__ void __launch_bounds__(SA_THREADS) fr_sa_final(int n, uint8_t *ct, co
     sa_epilogue<N>(acc, Spt, pk + (size_t)x * pk_stride, scr, ct, ct_cmp, x);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Many encapsulations to one public key: A is generated once for the whole batch and the products
+// of every instance form one matrix product, [S'_0; S'_1; ...] (8n x N) times A (N x N).
+// ---------------------------------------------------------------------------------------------
+// A (N x N, u16, row-major) from seedA, one thread per row (frodo_macrify_reference.cu:164-188);
+// with planes != nullptr also the transposed tensor-core operands: planes[0][j][i] = A[i][j] & 1023
+// and planes[1][j][i] = A[i][j] >> 10 as fp16 bit patterns (exact: both below 2048).  CTA 0's first
+// warp computes pkh = SHAKE(pk, SSB) meanwhile (fr_pkh_one's work, 115 serial permutations for
+// n = 976), so the two fixed latencies of a shared-key batch overlap.
+template <int N>
+__global__ void __launch_bounds__(128) fr_gen_a(const uint8_t *pk, uint16_t *A, uint16_t *planes, uint8_t *pkh) {
+    using P = FP<N>;
+    if (blockIdx.x == 0) {
+        if (threadIdx.x >= 32) return;
+        const WarpKeccak w(threadIdx.x);
+        uint2 a;
+        warp_absorb2<P::RATE>(a, reinterpret_cast<const uint2 *>(pk), P::PKB / 8, nullptr, 0, DOM_SHAKE, w);
+        keccak_f1600_warp(a, w);
+        if (w.lane < P::NW) reinterpret_cast<uint2 *>(pkh)[w.lane] = a;
+        return;
+    }
+    const int row = (blockIdx.x - 1) * blockDim.x + threadIdx.x;
+    if (row >= N) return;
+    uint2 S[25];
+    row_absorb(S, row, reinterpret_cast<const uint2 *>(pk));
+    for (int blk = 0; blk < P::ROW_BLOCKS; blk++) {
+        keccak_f1600(S);
+#pragma unroll
+        for (int w = 0; w < 42; w++) {
+            const uint32_t t = (w & 1) ? S[w >> 1].y : S[w >> 1].x;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int j = blk * BLK_COLS + 2 * w + h;
+                if (j < N) {
+                    const uint32_t a = h ? (t >> 16) : (t & 0xffff);
+                    A[(size_t)row * N + j] = (uint16_t)a;
+                    if (planes) {
+                        planes[(size_t)j * N + row] = __half_as_ushort(__uint2half_rn(a & 1023));
+                        planes[(size_t)N * N + (size_t)j * N + row] = __half_as_ushort(__uint2half_rn(a >> 10));
+                    }
+                }
+            }
+        }
+    }
+}
+
+// CUDA-core product: G[x][i][j] = sum_k S'[x][i][k] A[k][j] (mod 2^32, exact mod 2^16) into the
+// instances' u32 accumulators (scratch, GACC_OFF).  CTA = 4 instances x 128 columns, thread =
+// one instance's 8 rows x 2 columns; A and S' staged through shared memory in chunks of 32 k.
+constexpr int SH_INST = 4, SH_COLS = 128, SH_KC = 32, SH_THREADS = 256;
+template <int N>
+__global__ void __launch_bounds__(SH_THREADS) fr_sa_shared_simt(int n, const uint16_t *A, uint8_t *scratch) {
+    using P = FP<N>;
+    __shared__ __align__(16) uint16_t sA[SH_KC][SH_COLS];
+    __shared__ __align__(16) uint16_t sS[SH_INST][SH_KC][NB];
+    const int x0 = blockIdx.x * SH_INST, c0 = blockIdx.y * SH_COLS, tid = threadIdx.x;
+    const int li = tid >> 6, cc = (tid & 63) * 2;  // instance in the CTA, first of its two columns
+    uint32_t acc[NB][2];
+#pragma unroll
+    for (int i = 0; i < NB; i++) acc[i][0] = acc[i][1] = 0;
+    for (int k0 = 0; k0 < N; k0 += SH_KC) {
+        for (int t = tid; t < SH_KC * SH_COLS / 2; t += SH_THREADS) {  // A rows k0.., 2 columns a thread
+            const int kk = t / (SH_COLS / 2), j = c0 + 2 * (t % (SH_COLS / 2)), k = k0 + kk;
+            uint32_t v = 0;
+            if (k < N && j < N) v = *reinterpret_cast<const uint32_t *>(A + (size_t)k * N + j);  // N even
+            reinterpret_cast<uint32_t *>(&sA[kk][0])[t % (SH_COLS / 2)] = v;
+        }
+        for (int t = tid; t < SH_INST * SH_KC; t += SH_THREADS) {  // S'^T rows: 8 values per (instance, k)
+            const int xi = t / SH_KC, kk = t % SH_KC, x = x0 + xi, k = k0 + kk;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (x < n && k < N) v = reinterpret_cast<const uint4 *>(scratch + (size_t)x * P::SCRATCH)[k];
+            *reinterpret_cast<uint4 *>(&sS[xi][kk][0]) = v;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < SH_KC; kk++) {
+            const uint4 sv = *reinterpret_cast<const uint4 *>(&sS[li][kk][0]);
+            const uint32_t a2 = *reinterpret_cast<const uint32_t *>(&sA[kk][cc]);
+            const uint32_t a0 = a2 & 0xffff, a1 = a2 >> 16;
+            const uint32_t s[NB] = {sv.x & 0xffff, sv.x >> 16, sv.y & 0xffff, sv.y >> 16,
+                                    sv.z & 0xffff, sv.z >> 16, sv.w & 0xffff, sv.w >> 16};
+#pragma unroll
+            for (int i = 0; i < NB; i++) {
+                acc[i][0] += s[i] * a0;
+                acc[i][1] += s[i] * a1;
+            }
+        }
+        __syncthreads();
+    }
+    const int x = x0 + li, j = c0 + cc;
+    if (x >= n || j >= N) return;
+    uint32_t *g = reinterpret_cast<uint32_t *>(scratch + (size_t)x * P::SCRATCH + P::GACC_OFF);
+#pragma unroll
+    for (int i = 0; i < NB; i++) *reinterpret_cast<uint2 *>(g + (size_t)i * N + j) = make_uint2(acc[i][0], acc[i][1]);
+}
+
 static size_t sa_smem(int N, int threads) {
     return (size_t)N * NB * 2 + ((size_t)NB * N + 64) * 4 + (size_t)threads * STAGE_PITCH * 2;
 }
@@ -586,17 +684,22 @@ size_t frodo_scratch_bytes(int N) {
 // by batch size: small batches split an instance over several CTAs (latency), large ones keep one
 // CTA per instance (no split traffic).  Set through pqcgpu_set_launch_shape (the autotuner); the
 // settings apply to every FrodoKEM parameter set.
-static int g_fr_parts[3] = {0, 0, 0}, g_fr_threads[3] = {0, 0, 0};
+int frodo_set_shared_product(int product);
+int frodo_get_shared_product();
+// (parts, threads) per operation, one atomic word each; parts 0 = chosen by batch size.
+static LaunchShape g_fr_shape[3] = {{0, 0}, {0, 0}, {0, 0}};
 
 static void fr_shape(int op, int n, int *parts, int *threads) {
+    int p, t;
+    g_fr_shape[op].get(p, t);
     if (op == 0) {
         *parts = 1;
-        *threads = g_fr_threads[0] ? g_fr_threads[0] : (n >= 152 ? 256 : 64);
+        *threads = t ? t : (n >= 152 ? 256 : 64);
         return;
     }
-    if (g_fr_parts[op]) {
-        *parts = g_fr_parts[op];
-        *threads = g_fr_threads[op];
+    if (p) {
+        *parts = p;
+        *threads = t;
         return;
     }
     if (n >= 304) *parts = 1, *threads = 256;
@@ -606,27 +709,34 @@ static void fr_shape(int op, int n, int *parts, int *threads) {
 }
 
 int frodo_set_shape(int op, int parts, int threads) {
+    if (op == 3) return frodo_set_shared_product(parts);  // the shared-key product
     if (op == 0) {
         if (parts > 1 || !(threads == 0 || threads == 64 || threads == 128 || threads == 256)) return PQCGPU_EINVAL;
-        g_fr_threads[0] = threads;
+        g_fr_shape[0].set(0, threads);
         return PQCGPU_OK;
     }
     if (op != 1 && op != 2) return PQCGPU_EINVAL;
     if (parts == 0) {
-        g_fr_parts[op] = g_fr_threads[op] = 0;
+        g_fr_shape[op].set(0, 0);
         return PQCGPU_OK;
     }
     if (!(parts == 1 || parts == 2 || parts == 4 || parts == 8 || parts == 16) || !(threads == 128 || threads == 256))
         return PQCGPU_EINVAL;
-    g_fr_parts[op] = parts;
-    g_fr_threads[op] = threads;
+    g_fr_shape[op].set(parts, threads);
     return PQCGPU_OK;
 }
 
 int frodo_get_shape(int op, int *parts, int *threads) {
+    if (op == 3) {
+        *parts = frodo_get_shared_product();
+        *threads = 0;
+        return PQCGPU_OK;
+    }
     if (op < 0 || op > 2) return PQCGPU_EINVAL;
-    *parts = op == 0 ? 1 : g_fr_parts[op];
-    *threads = g_fr_threads[op];
+    int p, t;
+    g_fr_shape[op].get(p, t);
+    *parts = op == 0 ? 1 : p;
+    *threads = t;
     return PQCGPU_OK;
 }
 
@@ -672,7 +782,8 @@ int enc_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu,
     if (sa_attrs<N>()) return PQCGPU_ECUDA;
     int parts, thr;
     fr_shape(1, n, &parts, &thr);
-    PQC_LAUNCH(st, "fr_enc_pre", N, 0, fr_enc_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, pk, mu, scratch, parts, pkh));
+    PQC_LAUNCH(st, "fr_enc_pre", N, 0,
+               fr_enc_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, pk, mu, scratch, parts, pkh, FP<N>::SSB));
     launch_sa<N>(n, ct, nullptr, pk, FP<N>::PKB, scratch, parts, thr, st);
     PQC_LAUNCH(st, "fr_post", N, 0, fr_post<N><<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, nullptr, ss));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
@@ -691,6 +802,63 @@ int dec_n(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scr
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 }  // namespace
+
+// Product of a shared-key batch: 1 CUDA cores (mad.lo, fr_sa_shared_simt), 2 tensor cores
+// (tcgen05 kind::f16 on split A, fr_sa_shared_tc); 0 = the default below, chosen by measurement.
+static LaunchShape g_fr_shared = {0, 0};
+constexpr int FR_SHARED_DEFAULT = 1;
+
+int frodo_set_shared_product(int product) {
+    if (product < 0 || product > 2) return PQCGPU_EINVAL;
+    g_fr_shared.set(product, 0);
+    return PQCGPU_OK;
+}
+int frodo_get_shared_product() {
+    int p, t;
+    g_fr_shared.get(p, t);
+    return p;
+}
+size_t frodo_shared_extra_bytes(int N) { return 256 + (size_t)N * N * 2 * 3; }
+
+namespace {
+template <int N>
+int enc_shared_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch, uint8_t *extra,
+                 cudaStream_t st) {
+    if (sa_attrs<N>()) return PQCGPU_ECUDA;
+    int product = frodo_get_shared_product();
+    if (product == 0) product = FR_SHARED_DEFAULT;
+    uint8_t *pkh = extra;
+    uint16_t *A = reinterpret_cast<uint16_t *>(extra + 256), *planes = A + (size_t)N * N;
+    PQC_LAUNCH(st, "fr_gen_a", N, 0,
+               fr_gen_a<N><<<1 + (N + 127) / 128, 128, 0, st>>>(pk, A, product == 2 ? planes : nullptr, pkh));
+    PQC_LAUNCH(st, "fr_enc_pre", N, 0, fr_enc_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, pk, mu, scratch, 1, pkh, 0));
+    unsigned *error = reinterpret_cast<unsigned *>(extra + 64);
+    if (cudaMemsetAsync(error, 0, sizeof(unsigned), st) != cudaSuccess) return PQCGPU_ECUDA;
+    if (product == 2) {
+        const int rc = frodo_shared_tc_launch(N, n, planes, scratch, error, st);
+        if (rc) return rc;
+    } else {
+        PQC_LAUNCH(st, "fr_sa_shared_simt", N, 0,
+                   fr_sa_shared_simt<N><<<dim3((n + SH_INST - 1) / SH_INST, (N + SH_COLS - 1) / SH_COLS), SH_THREADS, 0,
+                                          st>>>(n, A, scratch));
+    }
+    PQC_LAUNCH(st, "fr_sa_final", N, 0,
+               fr_sa_final<N><<<n, SA_THREADS, sa_final_smem(N), st>>>(n, ct, nullptr, pk, 0, scratch));
+    PQC_LAUNCH(st, "fr_post", N, 0, fr_post<N><<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, nullptr, ss));
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+}  // namespace
+
+// n encapsulations to one public key pk (PKB bytes), mu per instance; scratch: n x
+// frodo_scratch_bytes(N), extra: frodo_shared_extra_bytes(N) (256-byte aligned): pkh at +0, the
+// tensor product's error word at +64, A (N x N u16) at +256, then its two fp16 planes.
+int frodo_enc_shared_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
+                         uint8_t *extra, cudaStream_t st) {
+    if (N == 640) return enc_shared_n<640>(n, ct, ss, pk, mu, scratch, extra, st);
+    if (N == 976) return enc_shared_n<976>(n, ct, ss, pk, mu, scratch, extra, st);
+    if (N == 1344) return enc_shared_n<1344>(n, ct, ss, pk, mu, scratch, extra, st);
+    return PQCGPU_EINVAL;
+}
 
 int frodo_keypair_dev(int N, int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
                       cudaStream_t st) {

@@ -1,0 +1,238 @@
+// FrodoKEM shared-key product on the tensor cores (tcgen05, sm_103a).
+//
+// For n encapsulations to one public key the products B'_x = S'_x A (frodo_macrify_reference.cu:
+// 102-159, matMulKernelSA) form one matrix product: the 8-row blocks S'_x stacked into an 8n x N
+// matrix times A (N x N), all mod 2^16.  The tensor cores of this GPU take no 8-bit integer MMA
+// (ptxas for sm_103a refuses tcgen05.mma kind::i8), so the product runs exactly in fp16 with fp32
+// accumulation:
+//   A = 1024 A_hi + A_lo with A_lo = A & 1023 and A_hi = A >> 10, both exact in fp16 (< 2048);
+//   S' entries are small signed integers (|s| <= 12 for every FrodoKEM parameter set), exact;
+//   every partial sum of S' A_lo is below 1344 * 12 * 1023 < 2^24 and of S' A_hi below
+//   1344 * 12 * 63, so the fp32 accumulators hold exact integers;
+//   G = 1024 round(D_hi) + round(D_lo) (mod 2^32) equals S' A mod 2^16 in its low half.
+// The result goes to each instance's u32 accumulator in scratch, which fr_sa_final turns into
+// B' + E', V, C and the ciphertext.
+//
+// Kernel layout: CTA = 128 rows of the stacked S' (16 instances) x 128 columns of A, 4 warps.
+// For each K chunk of 64 the warps convert S' (scratch, u16 two's complement, N x 8 per instance)
+// and copy the two planes of A (fr_gen_a: transposed fp16, column j of A contiguous in k) into
+// shared memory in the no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix;
+// LBO = 128 bytes between core matrices along K, SBO = 1024 bytes between 8-row groups); one
+// thread issues the tcgen05.mma kind::f16 instructions (M = 128, N = 128, K = 16 each) into two
+// fp32 accumulators in tensor memory and commits them to an mbarrier that the CTA waits on.
+// The epilogue reads the accumulators with tcgen05.ld (warp w: lanes 32w..32w+31 = rows).
+// Every wait is bounded: a wait that runs out sets an error word (extra buffer) and the CTA frees
+// its tensor memory and returns.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pqcgpu_internal.h"
+
+namespace pqc {
+namespace frodo_tc {
+
+constexpr int NB = 8;
+constexpr int TC_M = 128, TC_N = 128, TC_KC = 64, TC_THREADS = 128;
+constexpr int TC_TMEM_COLS = 2 * TC_N;  // two fp32 accumulators
+constexpr uint32_t LBO = 128, SBO = (TC_KC / 8) * 128;
+constexpr int OP_BYTES = TC_M * TC_KC * 2;  // one 128 x 64 fp16 operand tile
+// Dynamic shared memory requested per CTA: three operand tiles (48 KB) padded so that at most two
+// CTAs share an SM, whose 512 tensor-memory columns then always hold both CTAs' 256.
+constexpr int TC_SMEM = 96 * 1024;
+constexpr int WAIT_LIMIT = 1 << 22;
+
+// Scratch layout per instance (frodo.cu FP<N>): S'^T (N x 8 u16) first, the u32 accumulator at GACC_OFF.
+__host__ __device__ constexpr size_t gacc_off(int N) { return (size_t)(2 * N * NB + NB * NB) * 2 + 128; }
+__host__ __device__ constexpr size_t scratch_bytes(int N) { return gacc_off(N) + (size_t)NB * N * 4; }
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor, no swizzle (sm_100-family descriptor, version field 1).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((LBO >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((SBO >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+// Instruction descriptor of kind::f16: D f32 (bits 4-5 = 1), A and B f16 (0), both K-major, N >> 3
+// at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(IDESC), "r"(accumulate));
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int i = 0; i < WAIT_LIMIT; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// planes: [2][N][N] fp16 bit patterns, plane 0 = A_lo^T, plane 1 = A_hi^T; error: a word set on a
+// wait that ran out.
+template <int N>
+__global__ void __launch_bounds__(TC_THREADS, 1) fr_sa_shared_tc(int n, const uint16_t *planes, uint8_t *scratch,
+                                                                 unsigned *error) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_abort;
+    uint8_t *opA = smem, *opLo = smem + OP_BYTES, *opHi = smem + 2 * OP_BYTES;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * TC_M, x0 = m0 / NB, n0 = blockIdx.y * TC_N;
+    const uint32_t bar_a = smem_addr(&bar);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot, d_lo = tmem, d_hi = tmem + TC_N;
+    const int nchunks = (N + TC_KC - 1) / TC_KC;
+    for (int c = 0; c < nchunks; c++) {
+        const int k0 = c * TC_KC;
+        // S' rows: task = (instance group g of 8 rows, k block kb of 8): 8 x 8 values, a register
+        // transpose, then one 16-byte store per row
+        {
+            const int g = tid >> 3, kb = tid & 7, x = x0 + g, k = k0 + 8 * kb;
+            uint16_t v[8][8];  // v[i][kk] = S'[x][i][k + kk]
+            if (x < n && k < N) {
+                const uint4 *src = reinterpret_cast<const uint4 *>(scratch + (size_t)x * scratch_bytes(N)) + k;
+#pragma unroll
+                for (int kk = 0; kk < 8; kk++) {
+                    const uint4 s = src[kk];
+                    const uint32_t w[4] = {s.x, s.y, s.z, s.w};
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        const int16_t sv = (int16_t)((w[i >> 1] >> (16 * (i & 1))) & 0xffff);
+                        v[i][kk] = __half_as_ushort(__short2half_rn(sv));
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; i++)
+#pragma unroll
+                    for (int kk = 0; kk < 8; kk++) v[i][kk] = 0;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                uint4 o;
+                o.x = v[i][0] | ((uint32_t)v[i][1] << 16);
+                o.y = v[i][2] | ((uint32_t)v[i][3] << 16);
+                o.z = v[i][4] | ((uint32_t)v[i][5] << 16);
+                o.w = v[i][6] | ((uint32_t)v[i][7] << 16);
+                *reinterpret_cast<uint4 *>(opA + g * SBO + kb * LBO + i * 16) = o;
+            }
+        }
+        // the planes: row j of each operand tile = column n0 + j of A, 8 k values per 16 bytes
+        for (int t = tid; t < 2 * TC_N * (TC_KC / 8); t += TC_THREADS) {
+            const int plane = t / (TC_N * (TC_KC / 8)), r = (t / (TC_KC / 8)) % TC_N, kb = t % (TC_KC / 8);
+            const int j = n0 + r, k = k0 + 8 * kb;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (j < N && k < N) v = *reinterpret_cast<const uint4 *>(planes + (size_t)plane * N * N + (size_t)j * N + k);
+            *reinterpret_cast<uint4 *>((plane ? opHi : opLo) + (r >> 3) * SBO + kb * LBO + (r & 7) * 16) = v;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int ks = 0; ks < TC_KC / 16; ks++) {
+                const uint32_t off = ks * 2 * LBO;  // K = 16: two core matrices
+                const uint32_t acc = (c > 0 || ks > 0) ? 1u : 0u;
+                mma_f16(d_lo, sdesc(smem_addr(opA) + off), sdesc(smem_addr(opLo) + off), acc);
+                mma_f16(d_hi, sdesc(smem_addr(opA) + off), sdesc(smem_addr(opHi) + off), acc);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_a)
+                         : "memory");
+        }
+        if (!mbar_wait(bar_a, (uint32_t)(c & 1))) {
+            if (tid == 0) {
+                atomicOr(error, 1u);
+                s_abort = 1;
+            }
+        }
+        __syncthreads();
+        if (s_abort) break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!s_abort) {
+        // epilogue: warp w holds rows 32w .. 32w + 31 (tensor-memory lanes)
+        const int r = 32 * warp + lane, x = x0 + (r >> 3), i = r & 7;
+        uint32_t *g = reinterpret_cast<uint32_t *>(scratch + (size_t)x * scratch_bytes(N) + gacc_off(N)) + (size_t)i * N;
+        const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+        for (int c0 = 0; c0 < TC_N; c0 += 16) {
+            uint32_t lo[16], hi[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                : "=r"(lo[0]), "=r"(lo[1]), "=r"(lo[2]), "=r"(lo[3]), "=r"(lo[4]), "=r"(lo[5]), "=r"(lo[6]), "=r"(lo[7]),
+                  "=r"(lo[8]), "=r"(lo[9]), "=r"(lo[10]), "=r"(lo[11]), "=r"(lo[12]), "=r"(lo[13]), "=r"(lo[14]),
+                  "=r"(lo[15])
+                : "r"(d_lo + lane_base + c0));
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                : "=r"(hi[0]), "=r"(hi[1]), "=r"(hi[2]), "=r"(hi[3]), "=r"(hi[4]), "=r"(hi[5]), "=r"(hi[6]), "=r"(hi[7]),
+                  "=r"(hi[8]), "=r"(hi[9]), "=r"(hi[10]), "=r"(hi[11]), "=r"(hi[12]), "=r"(hi[13]), "=r"(hi[14]),
+                  "=r"(hi[15])
+                : "r"(d_hi + lane_base + c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            const int j = n0 + c0;
+            if (x < n && j < N) {
+                uint32_t o[16];
+#pragma unroll
+                for (int q = 0; q < 16; q++)
+                    o[q] = ((uint32_t)__float2int_rn(__uint_as_float(hi[q])) << 10) +
+                           (uint32_t)__float2int_rn(__uint_as_float(lo[q]));
+#pragma unroll
+                for (int q = 0; q < 16; q += 4)
+                    if (j + q < N) *reinterpret_cast<uint4 *>(g + j + q) = make_uint4(o[q], o[q + 1], o[q + 2], o[q + 3]);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+}
+
+template <int N>
+int launch(int n, const uint16_t *planes, uint8_t *scratch, unsigned *error, cudaStream_t st) {
+    if (!capturing() &&
+        cudaFuncSetAttribute(fr_sa_shared_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) != cudaSuccess) {
+        cudaGetLastError();
+        return PQCGPU_ECUDA;
+    }
+    const dim3 grid((8 * n + TC_M - 1) / TC_M, (N + TC_N - 1) / TC_N);
+    PQC_LAUNCH(st, "fr_sa_shared_tc", N, 0, fr_sa_shared_tc<N><<<grid, TC_THREADS, TC_SMEM, st>>>(n, planes, scratch, error));
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
+}  // namespace frodo_tc
+
+// error: a device word the caller zeroed; set when a wait in the kernel runs out
+int frodo_shared_tc_launch(int N, int n, const uint16_t *planes, uint8_t *scratch, unsigned *error, cudaStream_t st) {
+    if (N == 640) return frodo_tc::launch<640>(n, planes, scratch, error, st);
+    if (N == 976) return frodo_tc::launch<976>(n, planes, scratch, error, st);
+    if (N == 1344) return frodo_tc::launch<1344>(n, planes, scratch, error, st);
+    return PQCGPU_EINVAL;
+}
+
+}  // namespace pqc

@@ -3,12 +3,17 @@
 
 namespace pqc {
 namespace kyber {
-// Launch shape of the core kernels, [op][k-2] with op 0 keypair, 1 enc, 2 dec (its re-encryption
-// stage).  One thread per matrix entry (NI * k^2 jobs) sized against the shared memory each instance
+// Launch shape (instances per CTA, threads) of the core kernels, [op][k-2] with op 0 keypair, 1 enc,
+// 2 dec (its re-encryption stage).  One thread per matrix entry (NI * k^2 jobs) sized against the shared memory each instance
 // needs.  g_dec1: the decryption stage of decapsulation.  Defaults: the autotuner's GB300 optimum.
-int g_ni[3][3] = {{16, 12, 8}, {30, 14, 8}, {30, 14, 16}};
-int g_threads[3][3] = {{64, 128, 160}, {128, 128, 128}, {128, 128, 256}};
-int g_dec1[3][2] = {{16, 256}, {15, 256}, {8, 256}};
+LaunchShape g_shape[3][3] = {{{16, 64}, {12, 128}, {4, 64}}, {{30, 128}, {14, 128}, {6, 96}},
+                             {{30, 128}, {14, 128}, {8, 128}}};
+LaunchShape g_dec1[3] = {{16, 256}, {4, 128}, {4, 128}};
+// KEM batches of at most this many instances run on the single-instance kernels (one CTA per
+// instance, kyber_single.cuh); larger ones on the batched chains.  Measured on GB300 (Kyber-512 /
+// 768 / 1024 and ML-KEM-768, every operation): the single-instance kernels are faster up to 256
+// instances (Kyber-768 encapsulation 75.6 against 121 us) and slower from 608 (139.5 against 122).
+LaunchShape g_single = {384, 0};
 
 #define PQC_KYBER_DECL(K, V)                                                                               \
     int keypair_##K##_##V(int, uint8_t *, uint8_t *, const uint8_t *, int, int, uint8_t *, int, cudaStream_t); \
@@ -63,33 +68,38 @@ int kyber_init_constants() {
     return kyber_mixed_init();
 }
 int kyber_set_shape(int op, int k, int ni, int threads) {
+    if (op == 4) {  // the largest batch that takes the single-instance kernels (all k); 0 = never
+        if (ni < 0 || ni > 4096) return PQCGPU_EINVAL;
+        kyber::g_single.set(ni, 0);
+        return PQCGPU_OK;
+    }
     if (op < 0 || op > 3 || k < 2 || k > 4 || ni <= 0 || ni > 128 || threads < 32 || threads % 32 ||
         threads > kyber_bound_threads(op, k))
         return PQCGPU_EINVAL;
     if (op == 3) {  // decapsulation, decryption stage: NI instances' polynomials, no staging
         const size_t sm1 = (k == 2 ? kyber::smem_2_3(2, ni, 0) : k == 3 ? kyber::smem_3_3(2, ni, 0) : kyber::smem_4_3(2, ni, 0));
         if (sm1 > MAX_SMEM_PER_CTA) return PQCGPU_EINVAL;
-        kyber::g_dec1[k - 2][0] = ni;
-        kyber::g_dec1[k - 2][1] = threads;
+        kyber::g_dec1[k - 2].set(ni, threads);
         return PQCGPU_OK;
     }
     // the CTA's dynamic shared memory must fit the 227 KB a CTA may opt into on sm_103a
     const size_t sm = k == 2 ? kyber::smem_2_3(op, ni, threads) : k == 3 ? kyber::smem_3_3(op, ni, threads)
                                                                          : kyber::smem_4_3(op, ni, threads);
     if (sm > MAX_SMEM_PER_CTA) return PQCGPU_EINVAL;
-    kyber::g_ni[op][k - 2] = ni;
-    kyber::g_threads[op][k - 2] = threads;
+    kyber::g_shape[op][k - 2].set(ni, threads);
     return PQCGPU_OK;
 }
 int kyber_get_shape(int op, int k, int *ni, int *threads) {
-    if (op < 0 || op > 3 || k < 2 || k > 4) return PQCGPU_EINVAL;
-    if (op == 3) {
-        *ni = kyber::g_dec1[k - 2][0];
-        *threads = kyber::g_dec1[k - 2][1];
+    if (op == 4) {
+        kyber::g_single.get(*ni, *threads);
         return PQCGPU_OK;
     }
-    *ni = kyber::g_ni[op][k - 2];
-    *threads = kyber::g_threads[op][k - 2];
+    if (op < 0 || op > 3 || k < 2 || k > 4) return PQCGPU_EINVAL;
+    if (op == 3) {
+        kyber::g_dec1[k - 2].get(*ni, *threads);
+        return PQCGPU_OK;
+    }
+    kyber::g_shape[op][k - 2].get(*ni, *threads);
     return PQCGPU_OK;
 }
 

@@ -46,6 +46,14 @@ struct P {
 // Sponge helpers on a register state
 // ---------------------------------------------------------------------------------------------
 
+// The permutation of the core kernels' PRF and matrix phases runs its round loop rolled (one round
+// of code instead of two).  Those kernels carry several phases of unrolled code, and the smaller
+// loop body keeps the hot code within the instruction cache: measured on GB300 (Kyber-768
+// encapsulation core at 65536 instances, the same kernel otherwise), 1.039x over the two-round body,
+// with ncu's no-instruction stall halved (0.18 -> 0.09 warps per issue) and the ALU pipe busy
+// 71.4 % of active cycles instead of 68.3 %; a four-round body was 7 % slower.
+__device__ __forceinline__ void keccak_f1600_core(uint2 (&A)[25]) { keccak_f1600_rolled(A); }
+
 // PRF(seed, nonce) = SHAKE256(seed || nonce); `seed` 8-byte aligned (global or shared).
 __device__ __forceinline__ void prf_absorb(uint2 (&A)[25], const uint2 *seed, int nonce) {
     keccak_zero(A);
@@ -53,7 +61,7 @@ __device__ __forceinline__ void prf_absorb(uint2 (&A)[25], const uint2 *seed, in
     for (int i = 0; i < 4; i++) A[i] = seed[i];
     A[4].x = (uint32_t)nonce | (DOM_SHAKE << 8);
     A[SHAKE256_LANES - 1].y ^= 0x80000000u;
-    keccak_f1600(A);
+    keccak_f1600_core(A);
 }
 
 // CBD eta=2 from the first 128 squeezed bytes: word w (bytes 4w..4w+3) gives coefficients
@@ -109,7 +117,7 @@ __device__ __forceinline__ void noise_poly(const uint2 *seed, int nonce, F emit)
             w[2 * i] = A[i].x;
             w[2 * i + 1] = A[i].y;
         }
-        keccak_f1600(A);
+        keccak_f1600_core(A);
 #pragma unroll
         for (int i = 0; i < 7; i++) {
             w[34 + 2 * i] = A[i].x;
@@ -220,7 +228,7 @@ __device__ __forceinline__ void matrix_entry(const uint2 *rho, int row, int col,
     uint32_t *acc = reinterpret_cast<uint32_t *>(acc16);
     int ctr = 0, n = 0;
     while (ctr < N) {
-        keccak_f1600(A);
+        keccak_f1600_core(A);
         compact_part<V, 0>(A, stg, n);
         consume_pairs(stg, n, ctr, b, acc, tw);
         if (ctr >= N) break;
@@ -456,7 +464,7 @@ __device__ void encrypt_phases(int16_t *polys, uint8_t *seeds, const int2 *tw, c
         if (Pp::ETA1 == 3 && rj) {  // 192 bytes: the first squeeze (136) and 56 of the second
 #pragma unroll
             for (int q = 0; q < 17; q++) o[q] = A[q];
-            keccak_f1600(A);
+            keccak_f1600_core(A);
 #pragma unroll
             for (int q = 0; q < 7; q++) o[17 + q] = A[q];
         } else {
@@ -749,7 +757,7 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
         }
         A[8].x ^= DOM_SHA3;
         A[SHA3_512_LANES - 1].y ^= 0x80000000u;
-        keccak_f1600(A);
+        keccak_f1600_core(A);
         if constexpr (STAGE == DEC_DECRYPT) {
             uint2 *o = reinterpret_cast<uint2 *>(d.mr + (size_t)(base + li) * 96);
 #pragma unroll
@@ -828,7 +836,7 @@ __device__ __forceinline__ void dec_core_body(const DecArgs &d, int NI, int base
         }
         A[8].x ^= DOM_SHAKE;
         A[SHAKE256_LANES - 1].y ^= 0x80000000u;
-        keccak_f1600(A);
+        keccak_f1600_core(A);
         uint2 *out = reinterpret_cast<uint2 *>(d.ss + (size_t)(base + li) * 32);
 #pragma unroll
         for (int i = 0; i < 4; i++) out[i] = A[i];
@@ -845,16 +853,16 @@ __global__ void __launch_bounds__(kyber_bound_threads(3, K), kyber_bound_ctas(3,
 }
 
 
-// Keypair: slots [0,K) s, [K,2K) e, [2K,3K) t-hat; seeds [0,32) rho, [32,64) sigma.
+// Keypair of instances [base, base + NI) of `a` by the calling CTA.
+// Slots [0,K) s, [K,2K) e, [2K,3K) t-hat; seeds [0,32) rho, [32,64) sigma.
 template <int K, int V>
-__global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int NI) {
+__device__ __forceinline__ void kp_core_body(const KpArgs &a, int NI, int base) {
     using Pp = P<K, V>;
     extern __shared__ __align__(16) uint8_t smem[];
     int2 *tw = reinterpret_cast<int2 *>(smem), *twi = tw + 128;
     int16_t *polys = reinterpret_cast<int16_t *>(twi + 128);
     uint8_t *seeds = reinterpret_cast<uint8_t *>(polys + (size_t)NI * (3 * K) * POLY_PITCH);
     auto kslot = [&](int li, int s) { return polys + ((size_t)li * (3 * K) + s) * POLY_PITCH; };
-    const int base = blockIdx.x * NI;
     const int ni = min(NI, a.n - base);
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
     load_twiddles(tw, twi);
@@ -874,7 +882,7 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int 
         for (int i = 0; i < 4; i++) A[i] = dd[i];
         A[4].x = a.kem == KEM_MLKEM ? ((uint32_t)K | (DOM_SHA3 << 8)) : DOM_SHA3;
         A[SHA3_512_LANES - 1].y ^= 0x80000000u;
-        keccak_f1600(A);
+        keccak_f1600_core(A);
         uint2 *o = reinterpret_cast<uint2 *>(seeds + li * 128);
 #pragma unroll
         for (int i = 0; i < 8; i++) o[i] = A[i];
@@ -934,6 +942,10 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int 
             }
         }
     }
+}
+template <int K, int V>
+__global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int NI) {
+    kp_core_body<K, V>(a, NI, blockIdx.x * NI);
 }
 
 // ---- flat hash kernels: one thread per instance ----
@@ -1200,15 +1212,23 @@ __global__ void __launch_bounds__(128) kyber_kp_hash_post_w(int n, const uint8_t
 
 }  // namespace kyber
 }  // namespace pqc
+#include "kyber_single.cuh"
 #include "kyber_plain.cuh"
 namespace pqc {
 namespace kyber {
 // ---------------------------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------------------------
-extern int g_ni[3][3];       // [op][k-2]: instances per CTA (kyber.cu)
-extern int g_threads[3][3];  // [op][k-2]: threads per CTA (kyber.cu)
-extern int g_dec1[3][2];     // [k-2]: {instances, threads} of the decapsulation's decryption stage
+extern LaunchShape g_shape[3][3];  // [op][k-2]: instances per CTA, threads per CTA (kyber.cu)
+extern LaunchShape g_dec1[3];      // [k-2]: the same for the decapsulation's decryption stage
+extern LaunchShape g_single;       // KEM batches of at most this many instances take the
+                                   // single-instance kernels (count field; kyber.cu)
+
+static inline int single_max() {
+    int a, b;
+    g_single.get(a, b);
+    return a;
+}
 
 // Every Kyber kernel asks for the largest shared-memory carveout of the SM's unified L1 / shared
 // storage.  Kernels that run concurrently (the chunks of a host-buffer call, the jobs of a mixed
@@ -1238,6 +1258,9 @@ static void prefer_shared_all() {
     prefer_shared(kyber_enc_hash_post_w<K, V>);
     prefer_shared(kyber_dec_hash_pre_w<K, V>);
     prefer_shared(kyber_kp_hash_post_w<K, V>);
+    prefer_shared(kyber_kp_single<K, V>);
+    prefer_shared(kyber_enc_single<K, V>);
+    prefer_shared(kyber_dec_single<K, V>);
 }
 
 template <class Kern>
@@ -1258,7 +1281,14 @@ template <int K, int V>
 static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int coins_stride, int kem,
                           uint8_t *scratch, int plain, cudaStream_t st) {
     if (plain) return kem == KEM_FO ? plain_keypair<K, V>(n, pk, sk, coins, coins_stride, scratch, st) : PQCGPU_EUNSUPPORTED;
-    const int NI = g_ni[0][K - 2], NT = g_threads[0][K - 2];
+    if (kem && n <= single_max()) {
+        PQC_LAUNCH(st, "kyber_kp_single", K, V,
+                   kyber_kp_single<K, V><<<n, SINGLE_THREADS, SingleSmem<K, V>::bytes(), st>>>(coins, coins_stride, pk, sk,
+                                                                                              kem));
+        return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+    }
+    int NI, NT;
+    g_shape[0][K - 2].get(NI, NT);
     const size_t sm = Layout<3 * K, 128>::bytes(NI, NT);
     if (ensure_smem(kyber_kp_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     const bool g_pre = scratch && n > WARP_HASH_MAX;  // G as its own kernel (scratch: 64 B per instance)
@@ -1278,7 +1308,13 @@ template <int K, int V>
 static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
                       uint8_t *scratch, int kem, int plain, cudaStream_t st) {
     if (plain) return kem == KEM_FO ? plain_enc<K, V>(n, ct, ss, pk, coins, scratch, st) : PQCGPU_EUNSUPPORTED;
-    const int NI = g_ni[1][K - 2], NT = g_threads[1][K - 2];
+    if (kem && n <= single_max()) {
+        PQC_LAUNCH(st, "kyber_enc_single", K, V,
+                   kyber_enc_single<K, V><<<n, SINGLE_THREADS, SingleSmem<K, V>::bytes(), st>>>(pk, coins, ct, ss, kem));
+        return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+    }
+    int NI, NT;
+    g_shape[1][K - 2].get(NI, NT);
     const size_t sm = Layout<2 * K + 1, enc_seed_bytes<K, V>()>::bytes(NI, NT);
     if (ensure_smem(kyber_enc_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
     EncArgs a;
@@ -1319,7 +1355,13 @@ template <int K, int V>
 static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, int kem,
                       int plain, cudaStream_t st) {
     if (plain) return kem == KEM_FO ? plain_dec<K, V>(n, out, ct, sk, scratch, st) : PQCGPU_EUNSUPPORTED;
-    const int NI = g_ni[2][K - 2], NT = g_threads[2][K - 2];
+    if (kem && n <= single_max()) {
+        PQC_LAUNCH(st, "kyber_dec_single", K, V,
+                   kyber_dec_single<K, V><<<n, SINGLE_THREADS, SingleSmem<K, V>::bytes(), st>>>(ct, sk, out, kem));
+        return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+    }
+    int NI, NT;
+    g_shape[2][K - 2].get(NI, NT);
     const size_t sm = Layout<2 * K + 1, enc_seed_bytes<K, V>()>::bytes(NI, NT);
     DecArgs d;
     d.n = n;
@@ -1344,7 +1386,8 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
     else
         PQC_LAUNCH(st, "kyber_dec_hash_pre", K, V,
                    kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, sk, scratch, kem));
-    const int NI1 = g_dec1[K - 2][0], NT1 = g_dec1[K - 2][1];
+    int NI1, NT1;
+    g_dec1[K - 2].get(NI1, NT1);
     const size_t sm1 = Layout<2 * K + 1, enc_seed_bytes<K, V>()>::bytes(NI1, 0);
     if (ensure_smem(kyber_dec_decrypt<K, V>, sm1) != cudaSuccess) return PQCGPU_ECUDA;
     if (ensure_smem(kyber_dec_core<K, V, DEC_REENCRYPT>, sm) != cudaSuccess) return PQCGPU_ECUDA;

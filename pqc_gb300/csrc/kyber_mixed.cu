@@ -1,12 +1,25 @@
-// One kernel per stage for the Kyber jobs of a mixed batch.
+// Persistent per-stage kernels for the Kyber jobs of a mixed batch.
 //
-// A mixed batch (pqcgpu_kem_mixed_batch) may hold Kyber encapsulations and decapsulations of all
-// three module ranks (round 3 and ML-KEM) with uneven batch sizes.  Instead of one chain of kernels
-// per job, the core stages of all such jobs run as single launches: each CTA looks up its job in a
-// small table passed as a __grid_constant__ kernel parameter (the job's k, instances per CTA and
-// buffers) and runs that k's stage body on its instances.  Jobs are ordered by k, heaviest first,
-// so the long CTAs start early and the short ones fill the tail.  The per-job serial hash kernels
-// (H(pk), G, H(c), KDF) stay per job; the caller spreads them over streams.
+// A mixed batch (pqcgpu_kem_mixed_batch with PQCGPU_STAGE_KERNELS) may hold Kyber key generations,
+// encapsulations and decapsulations of all three module ranks (round 3 and ML-KEM) with uneven
+// batch sizes.  Instead of one chain of kernels per job, their core stages run in two persistent
+// launches:
+//   wave A: every keypair core, encapsulation core and decapsulation's decryption stage;
+//   wave B: every decapsulation's re-encryption stage (after G, which needs wave A's m').
+// Each wave launches the SMs x (CTAs per SM) that fit at once.  A CTA takes a tile (a job and a
+// group of NI instances) from a global atomic counter, runs that job's stage body for its k on it,
+// and takes the next, so uneven jobs share the GPU without a tail per job and without a launch
+// per job.  The tiles are ordered heaviest first (encapsulation, then keypair, then decryption;
+// larger k first), so the long tiles start early and the short ones fill the end.
+// The per-job serial hash kernels (G(d), H(pk), G, H(c), KDF) stay per job on the caller's streams
+// between the waves (thread or warp per instance, as in the single-job path).
+//
+// One launch has one block size and one dynamic shared-memory size: every stage runs at 128
+// threads, with instances per CTA chosen per (stage, k) so that every tile needs at most the
+// 76.7 KB of Kyber-768 encapsulation's tuned shape (three CTAs per SM).
+//
+// Replaces the reference's fixed per-operation launch chains, one parameter set per build
+// (Kyber_GPU_Batched/indcpa.cu:474-733).
 #include <algorithm>
 #include <vector>
 
@@ -16,147 +29,185 @@ namespace pqc {
 namespace kyber {
 namespace {
 
-constexpr int MIX_MAX_JOBS = 32;  // jobs per table (a kernel parameter of about 4.6 KB)
-constexpr int MIX_THREADS = 128, MIX_THREADS_DEC1 = 384;
-// instances per CTA by k (index k - 2): at 128 threads about one thread per matrix entry of the
-// encryption phases; the decryption stage is warp-level and runs 12 warps per CTA
-constexpr int MIX_NI_ENC[3] = {24, 14, 8};
-constexpr int MIX_NI_DEC1[3] = {32, 24, 12};
+constexpr int MIX_MAX_JOBS = 40;  // jobs per wave table (a kernel parameter, about 6.5 KB)
+constexpr int MIX_THREADS = 128;
+enum StageKind { ST_ENC = 0, ST_KP = 1, ST_DEC1 = 2, ST_DEC2 = 3 };
+// instances per CTA by stage and k (index k - 2), every tile within 76.7 KB of shared memory
+constexpr int MIX_NI[4][3] = {{19, 14, 8}, {16, 12, 8}, {21, 15, 12}, {19, 14, 8}};
 
 struct MixJob {
-    int k, ni, first;  // module rank, instances per CTA, first CTA of the job
-    EncArgs e;         // encapsulation jobs
-    DecArgs d;         // decapsulation jobs
+    int kind, k, ni, first;  // stage, module rank, instances per CTA, first tile of the job
+    KpArgs kp;
+    EncArgs e;
+    DecArgs d;
 };
 struct MixTable {
-    int njobs;
+    int njobs, tiles;
     MixJob j[MIX_MAX_JOBS];
 };
 
-__device__ __forceinline__ const MixJob &mix_job(const MixTable &t, int b) {
-    int j = 0;
-    while (j + 1 < t.njobs && b >= t.j[j + 1].first) j++;
-    return t.j[j];
-}
-
-__global__ void __launch_bounds__(MIX_THREADS) kyber_enc_core_mixed(const __grid_constant__ MixTable t) {
-    const MixJob &m = mix_job(t, blockIdx.x);
-    const int base = (blockIdx.x - m.first) * m.ni;
-    if (m.k == 2) enc_core_body<2, 3>(m.e, m.ni, base);
-    else if (m.k == 3) enc_core_body<3, 3>(m.e, m.ni, base);
-    else enc_core_body<4, 3>(m.e, m.ni, base);
-}
-
-template <int STAGE>
-__global__ void __launch_bounds__(MIX_THREADS_DEC1) kyber_dec_core_mixed(const __grid_constant__ MixTable t) {
-    const MixJob &m = mix_job(t, blockIdx.x);
-    const int base = (blockIdx.x - m.first) * m.ni;
-    if (m.k == 2) dec_core_body<2, 3, STAGE>(m.d, m.ni, base);
-    else if (m.k == 3) dec_core_body<3, 3, STAGE>(m.d, m.ni, base);
-    else dec_core_body<4, 3, STAGE>(m.d, m.ni, base);
+__device__ __forceinline__ int mix_find(const MixTable &t, int tile) {
+    int lo = 0, hi = t.njobs - 1;  // the last job whose first tile <= tile
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (t.j[mid].first <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 template <int K>
-size_t enc_smem(int ni) { return Layout<2 * K + 1, enc_seed_bytes<K, 3>()>::bytes(ni, MIX_THREADS); }
+__device__ __forceinline__ void mix_run(const MixJob &m, int base) {
+    switch (m.kind) {
+    case ST_ENC: enc_core_body<K, 3>(m.e, m.ni, base); break;
+    case ST_KP: kp_core_body<K, 3>(m.kp, m.ni, base); break;
+    case ST_DEC1: dec_core_body<K, 3, DEC_DECRYPT>(m.d, m.ni, base); break;
+    default: dec_core_body<K, 3, DEC_REENCRYPT>(m.d, m.ni, base); break;
+    }
+}
+
+// counter: a zeroed word of device memory for this launch
+__global__ void __launch_bounds__(MIX_THREADS, 3) kyber_stage_persistent(const __grid_constant__ MixTable t,
+                                                                      unsigned *counter) {
+    __shared__ int s_tile;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int tile = s_tile;
+        if (tile >= t.tiles) break;
+        const MixJob &m = t.j[mix_find(t, tile)];
+        const int base = (tile - m.first) * m.ni;
+        if (m.k == 2) mix_run<2>(m, base);
+        else if (m.k == 3) mix_run<3>(m, base);
+        else mix_run<4>(m, base);
+        __syncthreads();  // the next tile reuses shared memory (and s_tile)
+    }
+}
+
 template <int K>
-size_t dec1_smem(int ni) { return Layout<2 * K + 1, enc_seed_bytes<K, 3>()>::bytes(ni, 0); }
-size_t stage_smem(int k, bool dec1) {
-    const int ni = (dec1 ? MIX_NI_DEC1 : MIX_NI_ENC)[k - 2];
-    if (k == 2) return dec1 ? dec1_smem<2>(ni) : enc_smem<2>(ni);
-    if (k == 3) return dec1 ? dec1_smem<3>(ni) : enc_smem<3>(ni);
-    return dec1 ? dec1_smem<4>(ni) : enc_smem<4>(ni);
+size_t tile_smem(int kind, int ni) {
+    switch (kind) {
+    case ST_KP: return Layout<3 * K, 128>::bytes(ni, MIX_THREADS);
+    case ST_DEC1: return Layout<2 * K + 1, enc_seed_bytes<K, 3>()>::bytes(ni, 0);
+    default: return Layout<2 * K + 1, enc_seed_bytes<K, 3>()>::bytes(ni, MIX_THREADS);
+    }
+}
+size_t tile_smem(int kind, int k, int ni) {
+    return k == 2 ? tile_smem<2>(kind, ni) : k == 3 ? tile_smem<3>(kind, ni) : tile_smem<4>(kind, ni);
+}
+
+int pkb(int k) { return k * 384 + 32; }
+int skb(int k) { return 2 * k * 384 + 96; }
+
+void fill_job(MixJob &m, int kind, const MixedKyberJob &j) {
+    m.kind = kind;
+    m.k = j.k;
+    m.ni = MIX_NI[kind][j.k - 2];
+    m.kp = KpArgs{};
+    m.e = EncArgs{};
+    m.d = DecArgs{};
+    if (kind == ST_KP) {
+        m.kp = KpArgs{j.n, j.out0, j.out1, j.in0, 64, j.kem, j.scratch};
+    } else if (kind == ST_ENC) {
+        m.e.n = j.n;
+        m.e.ct = j.out0;
+        m.e.pk = j.in0;
+        m.e.pk_stride = pkb(j.k);
+        m.e.m = j.scratch;
+        m.e.m_stride = 96;
+        m.e.r = j.scratch + 32;
+        m.e.r_stride = 96;
+    } else {
+        m.d.n = j.n;
+        m.d.ct = j.in0;
+        m.d.sk = j.in1;
+        m.d.ss = j.out0;
+        m.d.hct = j.scratch;
+        m.d.kem = j.kem;
+        m.d.mr = j.scratch + (size_t)j.n * 32;
+        m.d.g_post = 1;                              // G runs between the waves (kyber_dec_hash_mid)
+        m.d.kdf_post = j.kem == KEM_FO ? 1 : 0;      // the KDF after wave B (kyber_dec_hash_post)
+    }
+}
+
+// One persistent launch over `items` (kind, job) on st; counter = a zeroed word of device memory.
+int launch_wave(const std::vector<std::pair<int, const MixedKyberJob *>> &items, unsigned *counter, cudaStream_t st) {
+    for (size_t from = 0; from < items.size(); from += MIX_MAX_JOBS) {
+        const size_t to = std::min(items.size(), from + MIX_MAX_JOBS);
+        MixTable t;
+        t.njobs = (int)(to - from);
+        t.tiles = 0;
+        size_t sm = 0;
+        for (size_t i = from; i < to; i++) {
+            MixJob &m = t.j[i - from];
+            fill_job(m, items[i].first, *items[i].second);
+            m.first = t.tiles;
+            t.tiles += (items[i].second->n + m.ni - 1) / m.ni;
+            sm = std::max(sm, tile_smem(m.kind, m.k, m.ni));
+        }
+        if (!capturing() &&
+            cudaFuncSetAttribute(kyber_stage_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            return PQCGPU_ECUDA;
+        }
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kyber_stage_persistent, MIX_THREADS, sm) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        const int grid = std::min(t.tiles, sms * per_sm);
+        unsigned *ctr = counter + from / MIX_MAX_JOBS;
+        if (cudaMemsetAsync(ctr, 0, sizeof(unsigned), st) != cudaSuccess) return PQCGPU_ECUDA;
+        PQC_LAUNCH(st, "kyber_stage_persistent", 0, 3, kyber_stage_persistent<<<grid, MIX_THREADS, sm, st>>>(t, ctr));
+        if (cudaGetLastError() != cudaSuccess) return PQCGPU_ECUDA;
+    }
+    return PQCGPU_OK;
 }
 
 // the per-job hash kernels, thread or warp per instance as in the single-job path
 template <int K>
-void enc_hashes(bool pre, const MixedKyberJob &j, cudaStream_t st) {
+void job_hash(int op, int phase, const MixedKyberJob &j, cudaStream_t st) {
     const int n = j.n;
-    if (pre) {
-        if (n <= WARP_HASH_MAX)
+    const bool w = n <= WARP_HASH_MAX;
+    if (op == 0) {
+        if (phase == 0)
+            PQC_LAUNCH(st, "kyber_kp_hash_pre", K, 3,
+                       kyber_kp_hash_pre<K, 3><<<(n + 127) / 128, 128, 0, st>>>(n, j.in0, 64, j.kem, j.scratch));
+        else if (phase == 2 && w)
+            PQC_LAUNCH(st, "kyber_kp_hash_post", K, 3, kyber_kp_hash_post_w<K, 3><<<(n + 3) / 4, 128, 0, st>>>(n, j.out0, j.out1));
+        else if (phase == 2)
+            PQC_LAUNCH(st, "kyber_kp_hash_post", K, 3,
+                       kyber_kp_hash_post<K, 3><<<(n + 127) / 128, 128, 0, st>>>(n, j.out0, j.out1));
+    } else if (op == 1) {
+        if (phase == 0 && w)
             PQC_LAUNCH(st, "kyber_enc_hash_pre", K, 3,
                        kyber_enc_hash_pre_w<K, 3><<<(n + 3) / 4, 128, 0, st>>>(n, j.in0, j.in1, j.scratch, j.kem));
-        else
+        else if (phase == 0)
             PQC_LAUNCH(st, "kyber_enc_hash_pre", K, 3,
                        kyber_enc_hash_pre<K, 3><<<(n + 127) / 128, 128, 0, st>>>(n, j.in0, j.in1, j.scratch, j.kem));
-    } else {
-        if (n <= WARP_HASH_MAX)
+        else if (phase == 2 && w)
             PQC_LAUNCH(st, "kyber_enc_hash_post", K, 3,
                        kyber_enc_hash_post_w<K, 3><<<(n + 3) / 4, 128, 0, st>>>(n, j.out0, j.scratch, j.out1, j.kem));
-        else
+        else if (phase == 2)
             PQC_LAUNCH(st, "kyber_enc_hash_post", K, 3,
                        kyber_enc_hash_post<K, 3><<<(n + 127) / 128, 128, 0, st>>>(n, j.out0, j.scratch, j.out1, j.kem));
+    } else {
+        if (phase == 0 && w)
+            PQC_LAUNCH(st, "kyber_dec_hash_pre", K, 3,
+                       kyber_dec_hash_pre_w<K, 3><<<(n + 3) / 4, 128, 0, st>>>(n, j.in0, j.in1, j.scratch, j.kem));
+        else if (phase == 0)
+            PQC_LAUNCH(st, "kyber_dec_hash_pre", K, 3,
+                       kyber_dec_hash_pre<K, 3><<<(n + 127) / 128, 128, 0, st>>>(n, j.in0, j.in1, j.scratch, j.kem));
+        else if (phase == 1)
+            PQC_LAUNCH(st, "kyber_dec_hash_mid", K, 3,
+                       kyber_dec_hash_mid<K, 3><<<(n + 127) / 128, 128, 0, st>>>(n, j.in1, j.scratch + (size_t)n * 32));
+        else if (j.kem == KEM_FO)
+            PQC_LAUNCH(st, "kyber_dec_hash_post", K, 3,
+                       kyber_dec_hash_post<K, 3><<<(n + 127) / 128, 128, 0, st>>>(n, j.scratch + (size_t)n * 32, j.scratch,
+                                                                                 j.out0));
     }
-}
-template <int K>
-void dec_hash(const MixedKyberJob &j, cudaStream_t st) {
-    const int n = j.n;
-    if (n <= WARP_HASH_MAX)
-        PQC_LAUNCH(st, "kyber_dec_hash_pre", K, 3,
-                   kyber_dec_hash_pre_w<K, 3><<<(n + 3) / 4, 128, 0, st>>>(n, j.in0, j.in1, j.scratch, j.kem));
-    else
-        PQC_LAUNCH(st, "kyber_dec_hash_pre", K, 3,
-                   kyber_dec_hash_pre<K, 3><<<(n + 127) / 128, 128, 0, st>>>(n, j.in0, j.in1, j.scratch, j.kem));
-}
-void hashes(int op, bool pre, const MixedKyberJob &j, cudaStream_t st) {
-    if (op == 1) {
-        if (j.k == 2) enc_hashes<2>(pre, j, st);
-        else if (j.k == 3) enc_hashes<3>(pre, j, st);
-        else enc_hashes<4>(pre, j, st);
-    } else if (pre) {
-        if (j.k == 2) dec_hash<2>(j, st);
-        else if (j.k == 3) dec_hash<3>(j, st);
-        else dec_hash<4>(j, st);
-    }
-}
-
-int pkb(int k) { return k * 384 + 32; }
-
-// Fill a table with jobs [from, to) of `js` (sorted by k, heaviest first) for the stage.
-int fill_table(MixTable &t, int op, bool dec1, const MixedKyberJob *js, int from, int to, size_t *smem) {
-    t.njobs = to - from;
-    int blocks = 0;
-    *smem = 0;
-    for (int i = from; i < to; i++) {
-        const MixedKyberJob &j = js[i];
-        MixJob &m = t.j[i - from];
-        m.k = j.k;
-        m.ni = (dec1 ? MIX_NI_DEC1 : MIX_NI_ENC)[j.k - 2];
-        m.first = blocks;
-        blocks += (j.n + m.ni - 1) / m.ni;
-        *smem = std::max(*smem, stage_smem(j.k, dec1));
-        if (op == 1) {
-            m.e = EncArgs{};
-            m.e.n = j.n;
-            m.e.ct = j.out0;
-            m.e.pk = j.in0;
-            m.e.pk_stride = pkb(j.k);
-            m.e.m = j.scratch;
-            m.e.m_stride = 96;
-            m.e.r = j.scratch + 32;
-            m.e.r_stride = 96;
-        } else {
-            m.d = DecArgs{};
-            m.d.n = j.n;
-            m.d.ct = j.in0;
-            m.d.sk = j.in1;
-            m.d.m_out = nullptr;
-            m.d.ss = j.out0;
-            m.d.hct = j.scratch;
-            m.d.kem = j.kem;
-            m.d.mr = j.scratch + (size_t)j.n * 32;
-        }
-    }
-    return blocks;
-}
-
-template <class Kern>
-int launch_stage(Kern kern, const char *name, const MixTable &t, int blocks, int threads, size_t sm, cudaStream_t st) {
-    if (!capturing() && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) {
-        cudaGetLastError();
-        return PQCGPU_ECUDA;
-    }
-    PQC_LAUNCH(st, name, 0, 3, kern<<<blocks, threads, sm, st>>>(t));
-    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
 }  // namespace
@@ -176,47 +227,40 @@ int kyber_mixed_init() {
     kyber::kyber_twiddles_shoup_host(tw, twi);
     if (cudaMemcpyToSymbol(kyber::c_tw, tw, sizeof tw) != cudaSuccess) return PQCGPU_ECUDA;
     if (cudaMemcpyToSymbol(kyber::c_twi, twi, sizeof twi) != cudaSuccess) return PQCGPU_ECUDA;
-    kyber::prefer_shared(kyber::kyber_enc_core_mixed);
-    kyber::prefer_shared(kyber::kyber_dec_core_mixed<kyber::DEC_DECRYPT>);
-    kyber::prefer_shared(kyber::kyber_dec_core_mixed<kyber::DEC_REENCRYPT>);
+    kyber::prefer_shared(kyber::kyber_stage_persistent);
     return PQCGPU_OK;
 }
 
-int kyber_mixed_hash(int op, bool pre, const MixedKyberJob &j, cudaStream_t st) {
-    if (op != 1 && op != 2) return PQCGPU_EINVAL;
-    if (j.n > 0) kyber::hashes(op, pre, j, st);
+int kyber_mixed_hash(int op, int phase, const MixedKyberJob &j, cudaStream_t st) {
+    if (op < 0 || op > 2 || phase < 0 || phase > 3) return PQCGPU_EINVAL;
+    if (j.n > 0) {
+        if (j.k == 2) kyber::job_hash<2>(op, phase, j, st);
+        else if (j.k == 3) kyber::job_hash<3>(op, phase, j, st);
+        else kyber::job_hash<4>(op, phase, j, st);
+    }
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
-int kyber_mixed_core(int op, const MixedKyberJob *jobs_in, int njobs, cudaStream_t st) {
+// wave 0: keypair cores, encapsulation cores, decryption stages; wave 1: re-encryption stages.
+// jobs[op] lists the jobs of operation op; counters: MIXED_COUNTER_WORDS zeroable words.
+int kyber_mixed_wave(int wave, const std::vector<MixedKyberJob> (&jobs)[3], unsigned *counters, cudaStream_t st) {
     using namespace kyber;
-    if (op != 1 && op != 2) return PQCGPU_EINVAL;
-    std::vector<MixedKyberJob> js;
-    for (int i = 0; i < njobs; i++)
-        if (jobs_in[i].n > 0) js.push_back(jobs_in[i]);
-    std::stable_sort(js.begin(), js.end(), [](const MixedKyberJob &a, const MixedKyberJob &b) { return a.k > b.k; });
-    const int nj = (int)js.size();
-    for (int from = 0; from < nj; from += MIX_MAX_JOBS) {
-        const int to = std::min(nj, from + MIX_MAX_JOBS);
-        MixTable t;
-        size_t sm = 0;
-        int rc;
-        if (op == 1) {
-            const int blocks = fill_table(t, 1, false, js.data(), from, to, &sm);
-            rc = launch_stage(kyber_enc_core_mixed, "kyber_enc_core_mixed", t, blocks, MIX_THREADS, sm, st);
-        } else {
-            int blocks = fill_table(t, 2, true, js.data(), from, to, &sm);
-            rc = launch_stage(kyber_dec_core_mixed<DEC_DECRYPT>, "kyber_dec_decrypt_mixed", t, blocks, MIX_THREADS_DEC1, sm,
-                              st);
-            if (!rc) {
-                blocks = fill_table(t, 2, false, js.data(), from, to, &sm);
-                rc = launch_stage(kyber_dec_core_mixed<DEC_REENCRYPT>, "kyber_dec_reencrypt_mixed", t, blocks, MIX_THREADS,
-                                  sm, st);
-            }
-        }
-        if (rc) return rc;
+    std::vector<std::pair<int, const MixedKyberJob *>> items;
+    auto add = [&](int kind, int op) {
+        for (int k = 4; k >= 2; k--)  // heavier k first
+            for (const auto &j : jobs[op])
+                if (j.k == k && j.n > 0) items.push_back({kind, &j});
+    };
+    if (wave == 0) {
+        add(ST_ENC, 1);
+        add(ST_KP, 0);
+        add(ST_DEC1, 2);
+    } else {
+        add(ST_DEC2, 2);
     }
-    return PQCGPU_OK;
+    if (items.empty()) return PQCGPU_OK;
+    if (items.size() > (size_t)MIX_MAX_JOBS * (MIXED_COUNTER_WORDS / 2)) return PQCGPU_EINVAL;
+    return launch_wave(items, counters + wave * (MIXED_COUNTER_WORDS / 2), st);
 }
 
 }  // namespace pqc

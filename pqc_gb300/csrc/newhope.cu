@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(128) nh_enc_hash_pre(int n, const uint8_t *coi
 }
 
 // [n index: 0 = 1024, 1 = 512][op] = {instances per CTA, threads}
-static int g_shape[2][3][2] = {{{8, 128}, {4, 64}, {4, 128}}, {{16, 128}, {16, 128}, {4, 64}}};
+static LaunchShape g_shape[2][3] = {{{8, 128}, {4, 64}, {4, 128}}, {{16, 128}, {16, 128}, {4, 64}}};
 static int nidx(int N) { return N == 1024 ? 0 : 1; }
 
 template <class Kern>
@@ -745,21 +745,20 @@ int newhope_set_shape(int N, int op, int ni, int threads) {
     if ((N != 1024 && N != 512) || op < 0 || op > 2 || ni < 1 || ni > 64 || threads < 32 || threads > 256 || threads % 32)
         return PQCGPU_EINVAL;
     if ((size_t)ni * smem_per_instance(N, op) > MAX_SMEM_PER_CTA) return PQCGPU_EINVAL;
-    g_shape[nidx(N)][op][0] = ni;
-    g_shape[nidx(N)][op][1] = threads;
+    g_shape[nidx(N)][op].set(ni, threads);
     return PQCGPU_OK;
 }
 
 int newhope_get_shape(int N, int op, int *ni, int *threads) {
     if ((N != 1024 && N != 512) || op < 0 || op > 2) return PQCGPU_EINVAL;
-    *ni = g_shape[nidx(N)][op][0];
-    *threads = g_shape[nidx(N)][op][1];
+    g_shape[nidx(N)][op].get(*ni, *threads);
     return PQCGPU_OK;
 }
 
 template <int N>
 static int keypair_n(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st) {
-    const int NI = g_shape[nidx(N)][0][0], NT = g_shape[nidx(N)][0][1];
+    int NI, NT;
+    g_shape[nidx(N)][0].get(NI, NT);
     const size_t sm = (size_t)NI * smem_per_instance(N, 0);
     if (prep(nh_kp_core<N>, sm)) return PQCGPU_ECUDA;
     KpArgs a{n, pk, sk, seed, seed_stride};
@@ -770,7 +769,8 @@ static int keypair_n(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int s
 template <int N>
 static int enc_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
                  uint8_t *scratch, int kem, cudaStream_t st) {
-    const int NI = g_shape[nidx(N)][1][0], NT = g_shape[nidx(N)][1][1];
+    int NI, NT;
+    g_shape[nidx(N)][1].get(NI, NT);
     const size_t sm = (size_t)NI * smem_per_instance(N, 1);
     if (prep(nh_enc_core<N>, sm)) return PQCGPU_ECUDA;
     EncArgs a{n, ct, pk, m, coins, 32, 32};
@@ -786,7 +786,8 @@ static int enc_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8
 
 template <int N>
 static int dec_n(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st) {
-    const int NI = g_shape[nidx(N)][2][0], NT = g_shape[nidx(N)][2][1];
+    int NI, NT;
+    g_shape[nidx(N)][2].get(NI, NT);
     const size_t sm = (size_t)NI * smem_per_instance(N, 2);
     if (prep(nh_dec_core<N>, sm)) return PQCGPU_ECUDA;
     DecArgs d{n, out, ct, sk, kem};

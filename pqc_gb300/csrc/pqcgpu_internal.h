@@ -5,6 +5,7 @@
 
 #include <atomic>
 #include <string>
+#include <vector>
 
 #include "pqcgpu.h"
 
@@ -14,6 +15,21 @@ constexpr size_t MAX_SMEM_PER_CTA = 232448;
 
 // Kernel launches issued by this library (all contexts); contexts report deltas.
 extern std::atomic<uint64_t> g_launch_count;
+
+// A launch shape -- a count (instances or row parts per CTA) and a thread count -- published as
+// one 32-bit atomic word: a launch that reads it while pqcgpu_set_launch_shape changes it on
+// another host thread sees the old pair or the new one, never half of each.  Shapes are
+// process-wide: every context and device launches with them.
+struct LaunchShape {
+    std::atomic<uint32_t> w;
+    constexpr LaunchShape(int count, int threads) : w(((uint32_t)count << 16) | (uint32_t)threads) {}
+    void set(int count, int threads) { w.store(((uint32_t)count << 16) | (uint32_t)threads, std::memory_order_relaxed); }
+    void get(int &count, int &threads) const {
+        const uint32_t v = w.load(std::memory_order_relaxed);
+        count = (int)(v >> 16);
+        threads = (int)(v & 0xffffu);
+    }
+};
 
 // Launch profiler (probe.cu): CUDA events around each launch on its stream when enabled.
 // Set while a CUDA graph is being captured on this host thread: launch helpers then skip the
@@ -74,17 +90,20 @@ struct CtrDrbg {
     void update(const uint8_t *provided);
 };
 // One Kyber job of a mixed batch (round-3 arithmetic, k = 2, 3, 4; kem 1 FO or 2 ML-KEM), device
-// pointers as in op_dev; scratch per kyber_scratch_bytes.  For encapsulation (op 1) or
-// decapsulation (op 2) jobs: kyber_mixed_hash issues one job's hash kernels before (pre) or after
-// the core stages; kyber_mixed_core runs the core stages of all the jobs, one kernel per stage
-// (kyber_mixed.cu).
+// pointers as in op_dev; scratch per kyber_scratch_bytes.  With PQCGPU_STAGE_KERNELS the core
+// stages of all such jobs run as two persistent waves (kyber_mixed.cu): wave 0 holds every
+// keypair core, encapsulation core and decryption stage, wave 1 every re-encryption stage; each
+// job's serial hash kernels run around them through kyber_mixed_hash: phase 0 before wave 0
+// (G(d) / H(pk), G / H(c)), phase 1 between the waves (decapsulation's G), phase 2 after its last
+// wave (H(pk) into sk / the KDF).
 struct MixedKyberJob {
     int k, kem, n;
     const uint8_t *in0, *in1;
     uint8_t *out0, *out1, *scratch;
 };
-int kyber_mixed_hash(int op, bool pre, const MixedKyberJob &job, cudaStream_t st);
-int kyber_mixed_core(int op, const MixedKyberJob *jobs, int njobs, cudaStream_t st);
+constexpr int MIXED_COUNTER_WORDS = 8;  // zeroable device words a mixed batch gives its waves
+int kyber_mixed_hash(int op, int phase, const MixedKyberJob &job, cudaStream_t st);
+int kyber_mixed_wave(int wave, const std::vector<MixedKyberJob> (&jobs)[3], unsigned *counters, cudaStream_t st);
 int kyber_mixed_init();  // constant tables of kyber_mixed.cu
 int kyber_kem_mode(int alg);  // 1: round-2 / round-3 FO KEM, 2: ML-KEM (FIPS 203)
 int kyber_keypair_dev(int variant, int k, int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int coins_stride,
@@ -120,5 +139,15 @@ int frodo_dec_dev(int N, int n, uint8_t *ss, const uint8_t *ct, const uint8_t *s
 int frodo_n(int alg);
 int frodo_set_shape(int op, int parts, int threads);
 int frodo_get_shape(int op, int *parts, int *threads);
+// Many encapsulations to one public key (A generated once, one matrix product for the batch).
+// product: 1 CUDA cores, 2 tensor cores (tcgen05), 0 the measured default.
+int frodo_set_shared_product(int product);
+int frodo_get_shared_product();
+size_t frodo_shared_extra_bytes(int N);
+int frodo_enc_shared_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
+                         uint8_t *extra, cudaStream_t st);
+// The tensor-core product G[x] = S'[x] A (frodo_tc.cu): planes = the split, transposed A from fr_gen_a;
+// error = a zeroed device word, set if a wait in the kernel runs out.
+int frodo_shared_tc_launch(int N, int n, const uint16_t *planes, uint8_t *scratch, unsigned *error, cudaStream_t st);
 
 }  // namespace pqc

@@ -88,6 +88,27 @@ def make_jobs(jobs):
     return arr
 
 
+class shared_product:
+    """Context manager: the product of FrodoKEM shared-key encapsulation (1 CUDA cores, 2 tensor cores)
+    for the duration of a block, restored afterwards; None leaves it unchanged."""
+
+    def __init__(self, alg, product):
+        self.alg, self.product, self.old = alg, product, None
+
+    def __enter__(self):
+        if self.product is not None:
+            lib = _lib.load()
+            a, b = ctypes.c_int(), ctypes.c_int()
+            _lib.check(lib.pqcgpu_get_launch_shape(alg_id(self.alg), 3, ctypes.byref(a), ctypes.byref(b)))
+            self.old = a.value
+            _lib.check(lib.pqcgpu_set_launch_shape(alg_id(self.alg), 3, self.product, 0))
+        return self
+
+    def __exit__(self, *exc):
+        if self.old is not None:
+            _lib.load().pqcgpu_set_launch_shape(alg_id(self.alg), 3, self.old, 0)
+
+
 class Graph:
     """A captured mixed job list (pqcgpu_graph_capture); launch() replays it on the context stream."""
 
@@ -159,6 +180,20 @@ class Context:
         ss = ctypes.create_string_buffer(n * s["ss"])
         _lib.check(self.lib.pqcgpu_kem_dec_batch(self.h, alg_id(alg), n, ss, ct, sk, flags))
         return ss.raw
+
+    def frodo_enc_shared(self, alg, n, pk, coins=None, product=None, flags=0):
+        """n FrodoKEM encapsulations to the one public key pk (host bytes); product: None (default),
+        1 CUDA cores, 2 tensor cores.  Returns (ct, ss)."""
+        s = sizes(alg)
+        ct = ctypes.create_string_buffer(n * s["ct"])
+        ss = ctypes.create_string_buffer(n * s["ss"])
+        with shared_product(alg, product):
+            _lib.check(self.lib.pqcgpu_frodo_enc_shared_key_batch(self.h, alg_id(alg), n, ct, ss, pk, coins, flags))
+        return ct.raw, ss.raw
+
+    def frodo_enc_shared_dev(self, alg, n, ct, ss, pk, coins, flags=0):
+        _lib.check(self.lib.pqcgpu_frodo_enc_shared_key_batch(self.h, alg_id(alg), n, _ptr(ct), _ptr(ss), _ptr(pk),
+                                                              _ptr(coins), flags | DEVICE_PTRS))
 
     def kyber_cpa_keypair(self, variant, k, n, d, flags=0):
         s = kyber_cpa_sizes(variant, k)

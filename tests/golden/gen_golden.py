@@ -8,7 +8,9 @@ Fixture kinds:
   * ref_*.json      -- outputs of the reference's OWN device code (Kyber_GPU_Batched for k = 2/3/4,
                        round-2 semantics; NewHope_NIST_GPU for n = 1024 and n = 512), compiled for
                        the host by oracle/build_ref.sh and driven with the NIST per-instance seed
-                       layout.
+                       layout; and of the reference's FrodoKEM-976 host KEM flow (FrodoKEM_GPU/
+                       kem.c with its sampler, pack / unpack, SHAKE and matrix kernels, run with
+                       CTA barriers through oracle/ref_shim_sync).
   * kat_*.rsp       -- NIST-format KAT records (AES-256 CTR_DRBG seeds and coins, oracle outputs).
   * restated_*.json -- outputs of the CPU oracle for paths the reference has no code for (Kyber
                        round-3 KEM, NewHope CPA-KEM, FrodoKEM-976, ML-KEM): regression pins, parity
@@ -115,6 +117,39 @@ def ref_newhope(n=16, s=2, poly_n=1024):
     })
 
 
+def ref_frodo976(n=3, s=6):
+    """FrodoKEM-976 keypair / encapsulation / decapsulation by the reference's own code
+    (oracle/_ref/librefrodo976.so, about 10 s per keypair: A.S runs 1024 CTAs of 128 host threads),
+    plus the decapsulation of a tampered ciphertext (byte (37 i + 11) mod |ct|, bit i mod 8)."""
+    L = ctypes.CDLL(os.path.join(REF, "librefrodo976.so"))
+    sz = O.alg_sizes(O.FRODO976)
+    seed = drbg.seed48(s)
+    kc = drbg.stream(seed, b"kp", n * sz["kp_coins"])
+    ec = drbg.stream(seed, b"enc", n * sz["enc_coins"])
+    pks, sks, cts, sss, rej = [], [], [], [], []
+    for i in range(n):
+        pk = ctypes.create_string_buffer(sz["pk"])
+        sk = ctypes.create_string_buffer(sz["sk"])
+        ct = ctypes.create_string_buffer(sz["ct"])
+        ss = ctypes.create_string_buffer(sz["ss"])
+        ss2 = ctypes.create_string_buffer(sz["ss"])
+        assert L.ref_frodo976_keypair(pk, sk, kc[i * sz["kp_coins"]:(i + 1) * sz["kp_coins"]]) == 0
+        assert L.ref_frodo976_enc(ct, ss, pk.raw, ec[i * sz["enc_coins"]:(i + 1) * sz["enc_coins"]]) == 0
+        assert L.ref_frodo976_dec(ss2, ct.raw, sk.raw) == 0 and ss2.raw == ss.raw
+        bad = bytearray(ct.raw)
+        bad[(37 * i + 11) % len(bad)] ^= 1 << (i % 8)
+        assert L.ref_frodo976_dec(ss2, bytes(bad), sk.raw) == 0 and ss2.raw != ss.raw
+        pks.append(h(pk.raw)), sks.append(h(sk.raw)), cts.append(h(ct.raw)), sss.append(ss.raw.hex())
+        rej.append(ss2.raw.hex())
+    dump("ref_frodo976_kem.json", {
+        "source": "reference FrodoKEM_GPU host KEM flow (kem.c) with its sampler, pack/unpack, SHAKE and "
+                  "matrix kernels, host-compiled via oracle/build_ref.sh (CTA barriers: oracle/ref_shim_sync)",
+        "n": n, "drbg_seed": s, "labels": {"keypair_coins": "kp", "enc_coins": "enc"},
+        "tamper": "byte (37 i + 11) mod len(ct), bit i mod 8",
+        "pk_sha256": pks, "sk_sha256": sks, "ct_sha256": cts, "ss": sss, "tampered_ss": rej,
+    })
+
+
 def restated(name, alg, n, s):
     sz = O.alg_sizes(alg)
     seed = drbg.seed48(s)
@@ -159,6 +194,7 @@ if __name__ == "__main__":
         ref_kyber(k)
     ref_newhope()
     ref_newhope(16, 3, 512)
+    ref_frodo976()
     restated("kyber512", O.KYBER512, 16, 0)
     restated("kyber768", O.KYBER768, 16, 0)
     restated("kyber1024", O.KYBER1024, 16, 0)

@@ -198,3 +198,42 @@ def test_plain_path_matches_oracle(ctx, oracle, alg):
     bad = bytearray(ct)
     bad[7] ^= 4
     assert ctx.dec(alg, n, bytes(bad), sk, flags=kem.PLAIN) == oracle.batch_dec(a, n, bytes(bad), sk)
+
+
+@pytest.mark.parametrize("alg", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "mlkem512", "mlkem768",
+                                  "mlkem1024"])
+@pytest.mark.parametrize("n", [1, 33, 300])
+def test_single_instance_and_batched_paths_match_oracle(ctx, oracle, alg, n):
+    """Small KEM batches run on the single-instance kernels (one CTA per instance) up to a size
+    threshold (launch-shape op 4); both that path and the batched chains must give the oracle's
+    bytes, including implicit rejection."""
+    from pqc_gb300 import _lib, kem
+    lib = _lib.load()
+    s = kem.sizes(alg)
+    a = oracle.ALG_NAMES[alg]
+    seed = drbg.seed48(7000 + n)
+    kc = drbg.stream(seed, b"kp", n * s["kp_coins"])
+    ec = drbg.stream(seed, b"enc", n * s["enc_coins"])
+    opk, osk = oracle.batch_keypair(a, n, kc)
+    oct_, oss = oracle.batch_enc(a, n, opk, ec)
+    bad = bytearray(oct_)
+    for x in range(0, n, 2):
+        bad[x * s["ct"] + (x * 53) % s["ct"]] ^= 1 << (x % 8)
+    orej = oracle.batch_dec(a, n, bytes(bad), osk)
+    before = ctypes_shape(lib)
+    try:
+        for limit in (4096, 0):  # every batch single-instance, then never
+            assert lib.pqcgpu_set_launch_shape(kem.alg_id(alg), 4, limit, 0) == 0
+            assert ctx.keypair(alg, n, kc) == (opk, osk), limit
+            assert ctx.enc(alg, n, opk, ec) == (oct_, oss), limit
+            assert ctx.dec(alg, n, oct_, osk) == oss, limit
+            assert ctx.dec(alg, n, bytes(bad), osk) == orej, limit
+    finally:
+        assert lib.pqcgpu_set_launch_shape(kem.alg_id(alg), 4, before, 0) == 0
+
+
+def ctypes_shape(lib):
+    import ctypes
+    a, b = ctypes.c_int(), ctypes.c_int()
+    assert lib.pqcgpu_get_launch_shape(1, 4, ctypes.byref(a), ctypes.byref(b)) == 0
+    return a.value

@@ -125,15 +125,56 @@ def test_graph_replay(env, stage_kernels):
 
 
 def test_autotune_roundtrip(env, tmp_path):
-    from pqc_gb300 import autotune
-    t = autotune.tune(batch=2048, algs=("kyber768",), reps=1, log=lambda *a: None)
-    assert set(t["shapes"]) == {"kyber768/0", "kyber768/1", "kyber768/2", "kyber768/3"}
-    p = str(tmp_path / "tuning.json")
-    autotune.save(t, p)
-    assert autotune.load_cached(p, gpu_name=t["gpu"]) is not None
+    """Tunes Kyber-768 at a small batch, saves and reloads the cache, and runs a mixed batch at the
+    tuned shapes; the shapes in force before are restored afterwards, so later tests do not depend
+    on this one's timing noise."""
+    from pqc_gb300 import _lib, autotune
+    lib = _lib.load()
+    before = {op: autotune.get_shape(lib, "kyber768", op) for op in range(4)}
+    try:
+        t = autotune.tune(batch=2048, algs=("kyber768",), reps=1, log=lambda *a: None)
+        assert set(t["shapes"]) == {"kyber768/0", "kyber768/1", "kyber768/2", "kyber768/3"}
+        p = str(tmp_path / "tuning.json")
+        autotune.save(t, p)
+        assert autotune.load_cached(p, gpu_name=t["gpu"]) is not None
+        ctx, torch, dev = env
+        jobs, expected = build_jobs(ctx, torch, dev, [("kyber768", "enc", 999), ("kyber768", "dec", 999)], 7000)
+        torch.cuda.synchronize()
+        ctx.mixed_dev(jobs)
+        ctx.wait()
+        check(jobs, expected)
+    finally:
+        for op, sh in before.items():
+            assert lib.pqcgpu_set_launch_shape(1, op, sh[0], sh[1]) == 0
+
+
+@pytest.mark.parametrize("op,shape", [(1, (8, 96)), (1, (20, 192)), (2, (14, 256)), (2, (6, 64)), (3, (4, 64)),
+                                      (3, (24, 384)), (0, (6, 96))])
+def test_kyber768_non_default_shapes_match_oracle(env, oracle, op, shape):
+    """Kyber-768 at launch shapes other than the defaults (including re-encryption at its 256-thread
+    bound), against the oracle, with tampered ciphertexts for decapsulation."""
+    from pqc_gb300 import _lib, autotune, kem
     ctx, torch, dev = env
-    jobs, expected = build_jobs(ctx, torch, dev, [("kyber768", "enc", 999), ("kyber768", "dec", 999)], 7000)
-    torch.cuda.synchronize()
-    ctx.mixed_dev(jobs)
-    ctx.wait()
-    check(jobs, expected)
+    lib = _lib.load()
+    before = autotune.get_shape(lib, "kyber768", op)
+    alg, n = "kyber768", 777
+    s = kem.sizes(alg)
+    a = oracle.KYBER768
+    seed = drbg.seed48(8800 + op)
+    kc = drbg.stream(seed, b"kp", n * s["kp_coins"])
+    ec = drbg.stream(seed, b"enc", n * s["enc_coins"])
+    opk, osk = oracle.batch_keypair(a, n, kc)
+    oct_, oss = oracle.batch_enc(a, n, opk, ec)
+    bad = bytearray(oct_)
+    for x in range(0, n, 4):
+        bad[x * s["ct"] + (x * 13) % s["ct"]] ^= 0x08
+    try:
+        assert lib.pqcgpu_set_launch_shape(kem.alg_id(alg), op, shape[0], shape[1]) == 0
+        if op == 0:
+            assert ctx.keypair(alg, n, kc) == (opk, osk)
+        elif op == 1:
+            assert ctx.enc(alg, n, opk, ec) == (oct_, oss)
+        else:
+            assert ctx.dec(alg, n, bytes(bad), osk) == oracle.batch_dec(a, n, bytes(bad), osk)
+    finally:
+        assert lib.pqcgpu_set_launch_shape(kem.alg_id(alg), op, before[0], before[1]) == 0

@@ -191,3 +191,26 @@ def test_mlkem_oracle_against_cryptography_live(oracle, name):
         assert oracle.batch_dec(alg, 1, ct_c, sk) == ss_c
         bad = _fips203_tamper(ct_c, t)
         assert oracle.batch_dec(alg, 1, bad, sk) == key.decapsulate(bad)
+
+
+def test_frodo976_oracle_matches_reference(oracle):
+    """The FrodoKEM-976 restatement against the reference's own host KEM flow (FrodoKEM_GPU/kem.c)
+    with the reference's sampler, pack / unpack, SHAKE, A generation and matrix kernels
+    (tests/golden/ref_frodo976_kem.json): keys, ciphertexts, shared secrets, and the implicit
+    rejection of a tampered ciphertext."""
+    g = load_golden("ref_frodo976_kem.json")
+    a = oracle.FRODO976
+    sz = oracle.alg_sizes(a)
+    n = g["n"]
+    seed = drbg.seed48(g["drbg_seed"])
+    pk, sk = oracle.batch_keypair(a, n, drbg.stream(seed, b"kp", n * sz["kp_coins"]))
+    ct, ss = oracle.batch_enc(a, n, pk, drbg.stream(seed, b"enc", n * sz["enc_coins"]))
+    assert [sha(x) for x in split(pk, sz["pk"])] == g["pk_sha256"]
+    assert [sha(x) for x in split(sk, sz["sk"])] == g["sk_sha256"]
+    assert [sha(x) for x in split(ct, sz["ct"])] == g["ct_sha256"]
+    assert [x.hex() for x in split(ss, sz["ss"])] == g["ss"]
+    bad = bytearray(ct)
+    for i in range(n):
+        bad[i * sz["ct"] + (37 * i + 11) % sz["ct"]] ^= 1 << (i % 8)
+    got = oracle.batch_dec(a, n, bytes(bad), sk)
+    assert [x.hex() for x in split(got, sz["ss"])] == g["tampered_ss"]

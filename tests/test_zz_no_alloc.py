@@ -3,8 +3,10 @@
 It serves callers that cannot call cudaMalloc -- code running inside another framework's memory
 pool or allocator callback, plugins handed fixed device buffers, real-time paths that forbid
 allocation after start-up.  Its scratch is a fixed device array shared by all calls.  This test
-calls it through the C ABI twice in a row, with different batches, and checks each result byte for
-byte against the regular batched encapsulation.  It runs last (file name) and needs a GPU.
+calls it through the C ABI several times in a row -- batches above 1024 instances (thread-per-
+instance hash kernels) and at or below it (warp-per-instance hash kernels, 1000 and 1) -- and checks
+each result byte for byte against the regular batched encapsulation.  It runs last (file name) and
+needs a GPU.
 """
 import ctypes
 
@@ -35,7 +37,7 @@ def test_noalloc_encaps_matches_batched_encaps():
     ctx.wait()
     stream = torch.cuda.current_stream(dev)
     p = lambda t: ctypes.c_void_p(t.data_ptr())
-    for call, n in enumerate((nmax, 1234)):  # two calls in a row share the scratch array
+    for call, n in enumerate((nmax, 1234, 1000, 1)):  # calls in a row share the scratch array
         coins = up(drbg.stream(seed, b"enc%d" % call, n * s["enc_coins"]))
         ct = torch.empty(n * s["ct"], dtype=torch.uint8, device=dev)
         ss = torch.empty(n * s["ss"], dtype=torch.uint8, device=dev)
