@@ -29,6 +29,7 @@ U{1..65536}), and Kyber-768 single-instance latency.  --no-extras leaves them ou
 * serving: continuous batching at 10-90 % of the measured peak;
 * refgpu: the reference's own Kyber kernels recompiled for sm_103a, beside ours;
 * latency: single-instance latencies;
+* frodo_shared: FrodoKEM encapsulations to one public key, CUDA-core vs tensor-core product;
 * all: every one of them.
 """
 import argparse
@@ -75,7 +76,7 @@ def parse():
     p.add_argument("--slots", type=int, default=12, help="serving: batches in flight (worker threads)")
     p.add_argument("--config", default=None,
                    choices=["kyber512", "kyber1024", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344", "mixed", "serving",
-                            "refgpu", "latency", "all"],
+                            "refgpu", "latency", "frodo_shared", "all"],
                    help="measure another configuration (extra JSON lines) instead of the headline")
     return p.parse_args()
 
@@ -370,6 +371,48 @@ def measure_mixed(ctx, dev, up, timed, reps=3):
             "mix": "k=2/3/4 at 40/40/20, n ~ U{1..65536}, ops 1/3 each", "bit_exact_decaps": bool(ok)}
 
 
+def measure_frodo_shared(ctx, dev, up, timed, n=2048, algs=("frodo640", "frodo976", "frodo1344")):
+    """n FrodoKEM encapsulations to one public key: A generated once and one matrix product for the
+    batch, on the CUDA cores (mad.lo) or the tensor cores (tcgen05 kind::f16 on the split A), beside
+    the per-instance path (A regenerated by every encapsulation); outputs compared byte for byte.
+    The product kernels' own times come from the library's launch profiler."""
+    import ctypes
+
+    import torch
+    from pqc_gb300 import _lib, drbg, kem
+    lib = _lib.load()
+    out = {}
+    for alg in algs:
+        s = kem.sizes(alg)
+        seed = drbg.seed48(17)
+        pk1 = torch.empty(s["pk"], dtype=torch.uint8, device=dev)
+        sk1 = torch.empty(s["sk"], dtype=torch.uint8, device=dev)
+        ctx.keypair_dev(alg, 1, pk1, sk1, up(drbg.stream(seed, b"kp", s["kp_coins"])))
+        mu = up(drbg.stream(seed, b"enc", n * s["enc_coins"]))
+        pkn = pk1.repeat(n)
+        ct, ss = (torch.empty(n * s[x], dtype=torch.uint8, device=dev) for x in ("ct", "ss"))
+        res = {}
+        t_inst = timed(lambda: ctx.enc_dev(alg, n, ct, ss, pkn, mu), 3)
+        ref = (ct.clone(), ss.clone())
+        res["per_instance_per_s"] = n / t_inst * 1e3
+        for name, product in (("cuda_cores", 1), ("tensor_cores", 2)):
+            with kem.shared_product(alg, product):
+                t = timed(lambda: ctx.frodo_enc_shared_dev(alg, n, ct, ss, pk1, mu), 3)
+                same = torch.equal(ct, ref[0]) and torch.equal(ss, ref[1])
+                lib.pqcgpu_profile_enable(1)
+                ctx.frodo_enc_shared_dev(alg, n, ct, ss, pk1, mu)
+                ctx.wait()
+                lib.pqcgpu_profile_enable(0)
+                buf = ctypes.create_string_buffer(1 << 16)
+                _lib.check(lib.pqcgpu_profile_read(buf, len(buf)))
+                prof = json.loads(buf.value.decode())
+            kern = {k: round(v[1], 4) for k, v in prof.items()}
+            res[name] = {"per_s": n / t * 1e3, "ms": t, "bit_exact_vs_per_instance": bool(same), "kernels_ms": kern}
+        out[alg] = res
+    return {"metric": "FrodoKEM encapsulations to one public key, per second (device-resident)", "batch": n,
+            "algs": out}
+
+
 def measure_serving(slots, fractions=(0.1, 0.3, 0.5, 0.7, 0.9), seconds=1.5):
     """Continuous batching under Poisson load at fractions of the measured peak (native load
     generator, pqcgpu_server_run_poisson); the peak is the rate achieved at saturation."""
@@ -404,7 +447,7 @@ def run_configs(args):
     st = torch.cuda.ExternalStream(ctx.stream, device=dev)
     up = lambda b: torch.frombuffer(bytearray(b), dtype=torch.uint8).to(dev)
     which = (["kyber512", "kyber1024", "newhope1024", "frodo976", "newhope512", "frodo640", "frodo1344", "mixed", "serving", "refgpu",
-              "latency"] if args.config == "all" else [args.config])
+              "latency", "frodo_shared"] if args.config == "all" else [args.config])
     timed = make_timer(ctx, st)
 
     for cfg in which:
@@ -435,6 +478,10 @@ def run_configs(args):
         elif cfg == "mixed":
             r, clk = clocked(lambda: measure_mixed(ctx, dev, up, timed))
             r.update({"config": "mixed", "clocks": clk})
+            print(json.dumps(r), flush=True)
+        elif cfg == "frodo_shared":
+            r, clk = clocked(lambda: measure_frodo_shared(ctx, dev, up, timed))
+            r.update({"config": "frodo_shared", "clocks": clk})
             print(json.dumps(r), flush=True)
         elif cfg == "refgpu":
             run_refgpu(ctx, dev, up, timed)

@@ -786,6 +786,7 @@ static int launch_jobs(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, uint
     // Otherwise every job's own kernels round-robin over all streams.
     constexpr int HS = pqcgpu_ctx::NPAR / 2;
     std::vector<MixedKyberJob> mix[3];
+    std::vector<NhMixedJob> nhmix;
     std::vector<size_t> rest;
     for (size_t i = 0; i < njobs; i++) {
         const pqcgpu_job &j = jobs[i];
@@ -793,10 +794,13 @@ static int launch_jobs(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, uint
         if (!plain && stage_kernels && kyber_alg(j.alg, &variant, &k) && variant == 3 && j.n > 0)
             mix[j.op].push_back(MixedKyberJob{k, kyber_kem_mode(j.alg), (int)j.n, j.in0, j.in1, j.out0, j.out1,
                                               scratch + offs[i]});
+        else if (!plain && stage_kernels && (j.alg == PQCGPU_NEWHOPE1024 || j.alg == PQCGPU_NEWHOPE512) && j.n > 0)
+            nhmix.push_back(NhMixedJob{j.alg == PQCGPU_NEWHOPE1024 ? 1024 : 512, j.op, (int)j.n, j.in0, j.in1, j.out0,
+                                       j.out1, scratch + offs[i]});
         else
             rest.push_back(i);
     }
-    const bool mixed = mix[0].size() + mix[1].size() + mix[2].size() >= 2;
+    const bool mixed = mix[0].size() + mix[1].size() + mix[2].size() + nhmix.size() >= 2;
     if (!mixed) {
         rest.clear();
         for (size_t i = 0; i < njobs; i++) rest.push_back(i);
@@ -827,9 +831,16 @@ static int launch_jobs(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, uint
         for (int op = 0; op <= 2; op++)  // phase 0 hashes
             for (const auto &j : mix[op])
                 if ((rc = kyber_mixed_hash(op, 0, j, c->par[q++ % HS]))) return set_err(rc, "job launch failed");
+        for (const auto &j : nhmix)
+            if ((rc = newhope_mixed_pre(j, c->par[q++ % HS]))) return set_err(rc, "job launch failed");
         if ((rc = join_into_main(c->stage_ev))) return rc;
         if ((rc = kyber_mixed_wave(0, mix, counters, c->par[0]))) return set_err(rc, "mixed Kyber launch failed");
         if ((rc = fork_from_main())) return rc;
+        // the NewHope wave follows Kyber's first wave on par[0], while the Kyber jobs' G kernels run
+        // on the other streams
+        if (!nhmix.empty() &&
+            (rc = newhope_mixed_wave(nhmix, counters + MIXED_COUNTER_WORDS, MIXED_NH_COUNTER_WORDS, c->par[0])))
+            return set_err(rc, "mixed NewHope launch failed");
         q = 1;
         for (const auto &j : mix[2])  // decapsulation's G between the waves, on par[1 .. HS)
             if ((rc = kyber_mixed_hash(2, 1, j, c->par[1 + (q++ - 1) % (HS - 1)]))) return set_err(rc, "job launch failed");

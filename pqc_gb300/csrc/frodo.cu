@@ -804,9 +804,12 @@ int dec_n(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scr
 }  // namespace
 
 // Product of a shared-key batch: 1 CUDA cores (mad.lo, fr_sa_shared_simt), 2 tensor cores
-// (tcgen05 kind::f16 on split A, fr_sa_shared_tc); 0 = the default below, chosen by measurement.
+// (tcgen05 kind::f16 on split A, fr_sa_shared_tc); 0 = the default below, chosen by measurement on
+// GB300 at 2048 encapsulations to one key (product kernel, CUDA cores -> tensor cores):
+// FrodoKEM-640 0.432 -> 0.176 ms, -976 1.071 -> 0.356 ms, -1344 1.959 -> 0.574 ms, the whole batch
+// 1.39 -> 1.69, 0.67 -> 0.87 and 0.44 -> 0.63 M encapsulations/s.
 static LaunchShape g_fr_shared = {0, 0};
-constexpr int FR_SHARED_DEFAULT = 1;
+constexpr int FR_SHARED_DEFAULT = 2;
 
 int frodo_set_shared_product(int product) {
     if (product < 0 || product > 2) return PQCGPU_EINVAL;

@@ -53,6 +53,26 @@ int kyber_dec_dev(int variant, int k, int n, uint8_t *out, const uint8_t *ct, co
                   int kem, int plain, cudaStream_t st) {
     PQC_KYBER_DISPATCH(dec, n, out, ct, sk, scratch, kem, plain, st)
 }
+SideStream *side_stream() {
+    static thread_local SideStream tbl[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    SideStream &ss = tbl[dev];
+    if (!ss.s) {
+        if (cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            ss = SideStream{};
+            return nullptr;
+        }
+    }
+    return &ss;
+}
+
 size_t kyber_scratch_bytes(int k, int op, int plain) {
     if (plain) return (size_t)(k * k + 4 * k + 4) * 256 * 2 + 208;
     // keypair: rho || sigma (64); encaps: m || r || K-bar (96); decaps: H(c) (32) + m' r' K-bar' (96)

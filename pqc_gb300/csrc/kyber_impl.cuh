@@ -1380,12 +1380,21 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
                    kyber_dec_core<K, V, DEC_FUSED><<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));
         return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
     }
+    // With the KDF after the re-encryption stage (round-2 / round-3 KEM, batches above 1024), H(c)
+    // is needed only by kyber_dec_hash_post: it runs on a side stream beside the decryption and
+    // re-encryption stages, whose integer pipe it shares.
+    SideStream *side = d.kdf_post ? side_stream() : nullptr;
+    if (side && (cudaEventRecord(side->fork, st) != cudaSuccess || cudaStreamWaitEvent(side->s, side->fork, 0) != cudaSuccess)) {
+        cudaGetLastError();
+        side = nullptr;
+    }
+    const cudaStream_t hs = side ? side->s : st;
     if (n <= WARP_HASH_MAX)
-        PQC_LAUNCH(st, "kyber_dec_hash_pre", K, V,
-                   kyber_dec_hash_pre_w<K, V><<<(n + 3) / 4, 128, 0, st>>>(n, ct, sk, scratch, kem));
+        PQC_LAUNCH(hs, "kyber_dec_hash_pre", K, V,
+                   kyber_dec_hash_pre_w<K, V><<<(n + 3) / 4, 128, 0, hs>>>(n, ct, sk, scratch, kem));
     else
-        PQC_LAUNCH(st, "kyber_dec_hash_pre", K, V,
-                   kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, ct, sk, scratch, kem));
+        PQC_LAUNCH(hs, "kyber_dec_hash_pre", K, V,
+                   kyber_dec_hash_pre<K, V><<<(n + 127) / 128, 128, 0, hs>>>(n, ct, sk, scratch, kem));
     int NI1, NT1;
     g_dec1[K - 2].get(NI1, NT1);
     const size_t sm1 = Layout<2 * K + 1, enc_seed_bytes<K, V>()>::bytes(NI1, 0);
@@ -1398,6 +1407,8 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
                    kyber_dec_hash_mid<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, d.sk, d.mr));
     PQC_LAUNCH(st, "kyber_dec_reencrypt", K, V,
                kyber_dec_core<K, V, DEC_REENCRYPT><<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));
+    if (side && (cudaEventRecord(side->join, side->s) != cudaSuccess || cudaStreamWaitEvent(st, side->join, 0) != cudaSuccess))
+        return PQCGPU_ECUDA;
     if (d.kdf_post)
         PQC_LAUNCH(st, "kyber_dec_hash_post", K, V,
                    kyber_dec_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, d.mr, d.hct, d.ss));

@@ -19,6 +19,9 @@
 // scalar 512-point ntt (ntt.cu:143-181), which reduces odd layers with `% q` where the 1024-point
 // one uses barrett_reduce; each message bit occupies n / 256 coefficients (poly.cu:226-291).
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
 #include <stdint.h>
 
 #include "keccak.cuh"
@@ -362,13 +365,13 @@ __device__ __forceinline__ uint16_t *npoly(uint16_t *polys, int per, int li, int
 
 // keypair: slots 0 s-hat, 1 e-hat -> b-hat
 template <int N>
-__global__ void __launch_bounds__(256) nh_kp_core(KpArgs a, int NI) {
+__device__ __forceinline__ void nh_kp_body(const KpArgs &a, int NI, int base) {
     using P = Nh<N>;
     constexpr int NCH = P::NCH;
     extern __shared__ __align__(16) uint8_t smem[];
     uint16_t *polys = reinterpret_cast<uint16_t *>(smem);
     uint8_t *seeds = smem + (size_t)NI * 2 * P::PITCH * 2;
-    const int base = blockIdx.x * NI, ni = min(NI, a.n - base);
+    const int ni = min(NI, a.n - base);
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
     // publicseed || noiseseed = SHAKE256(seed, 64)
     for (int li = tid; li < ni; li += nthr) {
@@ -425,12 +428,12 @@ __global__ void __launch_bounds__(256) nh_kp_core(KpArgs a, int NI) {
 
 // encryption: slots 0 s', 1 e' -> u-hat, 2 v'
 template <int N>
-__global__ void __launch_bounds__(256, 1) nh_enc_core(EncArgs a, int NI) {  // (256, 1): no register cap below 255 (the n = 512 instance spilled at 128)
+__device__ __forceinline__ void nh_enc_body(const EncArgs &a, int NI, int base) {
     using P = Nh<N>;
     constexpr int NCH = P::NCH;
     extern __shared__ __align__(16) uint8_t smem[];
     uint16_t *polys = reinterpret_cast<uint16_t *>(smem);
-    const int base = blockIdx.x * NI, ni = min(NI, a.n - base);
+    const int ni = min(NI, a.n - base);
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
     for (int job = tid; job < ni * 2 * NCH; job += nthr) {
         const int li = job / (2 * NCH), pl = (job / NCH) & 1, ch = job % NCH;
@@ -522,12 +525,12 @@ __global__ void __launch_bounds__(256, 1) nh_enc_core(EncArgs a, int NI) {  // (
 // decryption: tmp = invntt(pointwise(s-hat, u-hat)); m = tomsg(tmp - v')
 // n = 1024: one warp per instance.  n = 512: one half-warp per instance (two per warp).
 template <int N>
-__global__ void __launch_bounds__(256) nh_dec_core(DecArgs d, int NI) {
+__device__ __forceinline__ void nh_dec_body(const DecArgs &d, int NI, int base) {
     using P = Nh<N>;
     if constexpr (N == 1024) {
     extern __shared__ __align__(16) uint8_t smem[];
     uint16_t *polys = reinterpret_cast<uint16_t *>(smem);
-    const int base = blockIdx.x * NI, ni = min(NI, d.n - base);
+    const int ni = min(NI, d.n - base);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
     for (int li = warp; li < ni; li += nwarp) {
         const uint8_t *sk = d.sk + (size_t)(base + li) * P::SKB, *ct = d.ct + (size_t)(base + li) * P::CTB;
@@ -587,7 +590,7 @@ __global__ void __launch_bounds__(256) nh_dec_core(DecArgs d, int NI) {
     } else {
         extern __shared__ __align__(16) uint8_t smem[];
         uint16_t *polys = reinterpret_cast<uint16_t *>(smem);
-        const int base = blockIdx.x * NI, ni = min(NI, d.n - base);
+        const int ni = min(NI, d.n - base);
         const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
         const int l = lane & 15, half = lane >> 4;
         for (int w = warp; 2 * w < ni; w += nwarp) {
@@ -655,6 +658,20 @@ __global__ void __launch_bounds__(256) nh_dec_core(DecArgs d, int NI) {
             __syncwarp();
         }
     }
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) nh_kp_core(KpArgs a, int NI) {
+    nh_kp_body<N>(a, NI, blockIdx.x * NI);
+}
+// (256, 1): no register cap below 255 (the n = 512 instance spilled at 128)
+template <int N>
+__global__ void __launch_bounds__(256, 1) nh_enc_core(EncArgs a, int NI) {
+    nh_enc_body<N>(a, NI, blockIdx.x * NI);
+}
+template <int N>
+__global__ void __launch_bounds__(256) nh_dec_core(DecArgs d, int NI) {
+    nh_dec_body<N>(d, NI, blockIdx.x * NI);
 }
 
 // CPA-KEM encapsulation prologue: buf = SHAKE256(coins, 64) -> m || coin; ss = SHAKE256(m, 32)
@@ -792,6 +809,101 @@ static int dec_n(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int 
     if (prep(nh_dec_core<N>, sm)) return PQCGPU_ECUDA;
     DecArgs d{n, out, ct, sk, kem};
     PQC_LAUNCH(st, "nh_dec_core", N, 0, nh_dec_core<N><<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
+// ---- persistent wave for the NewHope jobs of a mixed batch ----
+// One launch holds the keypair, encapsulation and decapsulation tiles of every NewHope job (n = 1024
+// and 512): SMs x (CTAs per SM) CTAs of 128 threads take tiles from a global counter, heaviest first,
+// as the Kyber waves do (kyber_mixed.cu).  Instances per CTA per (n, op) at 128 threads.
+namespace {
+constexpr int NHW_MAX_JOBS = 40, NHW_THREADS = 128;
+constexpr int NHW_NI[2][3] = {{8, 4, 4}, {16, 16, 8}};  // [n index][op]
+struct NhWaveJob {
+    int nidx, op, ni, first;
+    KpArgs kp;
+    EncArgs e;
+    DecArgs d;
+};
+struct NhWaveTable {
+    int njobs, tiles;
+    NhWaveJob j[NHW_MAX_JOBS];
+};
+template <int N>
+__device__ __forceinline__ void nhw_run(const NhWaveJob &m, int base) {
+    if (m.op == 0) nh_kp_body<N>(m.kp, m.ni, base);
+    else if (m.op == 1) nh_enc_body<N>(m.e, m.ni, base);
+    else nh_dec_body<N>(m.d, m.ni, base);
+}
+__global__ void __launch_bounds__(NHW_THREADS, 2) nh_stage_persistent(const __grid_constant__ NhWaveTable t,
+                                                                      unsigned *counter) {
+    __shared__ int s_tile;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int tile = s_tile;
+        if (tile >= t.tiles) break;
+        int lo = 0, hi = t.njobs - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (t.j[mid].first <= tile) lo = mid;
+            else hi = mid - 1;
+        }
+        const NhWaveJob &m = t.j[lo];
+        const int base = (tile - m.first) * m.ni;
+        if (m.nidx == 0) nhw_run<1024>(m, base);
+        else nhw_run<512>(m, base);
+        __syncthreads();
+    }
+}
+}  // namespace
+
+int newhope_mixed_wave(const std::vector<NhMixedJob> &jobs, unsigned *counters, int ncounters, cudaStream_t st) {
+    std::vector<const NhMixedJob *> order;
+    for (int op : {1, 0, 2})  // encapsulation tiles are the heaviest, decapsulation the lightest
+        for (int N : {1024, 512})
+            for (const auto &j : jobs)
+                if (j.op == op && j.N == N && j.n > 0) order.push_back(&j);
+    for (size_t from = 0, w = 0; from < order.size(); from += NHW_MAX_JOBS, w++) {
+        if ((int)w >= ncounters) return PQCGPU_EINVAL;
+        const size_t to = std::min(order.size(), from + NHW_MAX_JOBS);
+        NhWaveTable t;
+        t.njobs = (int)(to - from);
+        t.tiles = 0;
+        size_t sm = 0;
+        for (size_t i = from; i < to; i++) {
+            const NhMixedJob &j = *order[i];
+            NhWaveJob &m = t.j[i - from];
+            m.nidx = nidx(j.N);
+            m.op = j.op;
+            m.ni = NHW_NI[m.nidx][j.op];
+            m.first = t.tiles;
+            m.kp = KpArgs{j.n, j.out0, j.out1, j.in0, 32};
+            m.e = EncArgs{j.n, j.out0, j.in0, j.scratch, j.scratch + 32, 64, 64};
+            m.d = DecArgs{j.n, j.out0, j.in0, j.in1, 1};
+            t.tiles += (j.n + m.ni - 1) / m.ni;
+            sm = std::max(sm, (size_t)m.ni * smem_per_instance(j.N, j.op));
+        }
+        if (prep(nh_stage_persistent, sm)) return PQCGPU_ECUDA;
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nh_stage_persistent, NHW_THREADS, sm) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        if (cudaMemsetAsync(counters + w, 0, sizeof(unsigned), st) != cudaSuccess) return PQCGPU_ECUDA;
+        PQC_LAUNCH(st, "nh_stage_persistent", 0, 0,
+                   nh_stage_persistent<<<std::min(t.tiles, sms * per_sm), NHW_THREADS, sm, st>>>(t, counters + w));
+        if (cudaGetLastError() != cudaSuccess) return PQCGPU_ECUDA;
+    }
+    return PQCGPU_OK;
+}
+
+// The CPA-KEM encapsulation prologue of one job of a mixed batch (before its wave).
+int newhope_mixed_pre(const NhMixedJob &j, cudaStream_t st) {
+    if (j.op != 1 || j.n <= 0) return PQCGPU_OK;
+    PQC_LAUNCH(st, "nh_enc_hash_pre", j.N, 0,
+               nh_enc_hash_pre<<<(j.n + 127) / 128, 128, 0, st>>>(j.n, j.in1, j.scratch, j.out1));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 

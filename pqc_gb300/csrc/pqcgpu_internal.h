@@ -64,6 +64,16 @@ void op_io_sizes(int alg, int op, size_t sz[4]);
 int device_ready(int device);
 int set_error(int code, const char *what);
 
+// A second stream of the calling host thread on the current device, for work of one call that may
+// overlap the rest of the call: forked from and joined back into the call's stream with its events
+// (stream capture follows them).  nullptr when it cannot be created (e.g. during a capture that
+// forbids it): the caller then stays on its own stream.
+struct SideStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+SideStream *side_stream();
+
 // ---- Kyber (kyber.cu) ----
 int kyber_init_constants();
 // op: 0 keypair, 1 enc, 2 dec.  ni = instances per CTA of the core kernel, threads per CTA.
@@ -101,7 +111,8 @@ struct MixedKyberJob {
     const uint8_t *in0, *in1;
     uint8_t *out0, *out1, *scratch;
 };
-constexpr int MIXED_COUNTER_WORDS = 8;  // zeroable device words a mixed batch gives its waves
+constexpr int MIXED_COUNTER_WORDS = 8;  // zeroable device words a mixed batch gives its Kyber waves
+constexpr int MIXED_NH_COUNTER_WORDS = 4;  // and its NewHope wave (after those 8)
 int kyber_mixed_hash(int op, int phase, const MixedKyberJob &job, cudaStream_t st);
 int kyber_mixed_wave(int wave, const std::vector<MixedKyberJob> (&jobs)[3], unsigned *counters, cudaStream_t st);
 int kyber_mixed_init();  // constant tables of kyber_mixed.cu
@@ -125,6 +136,16 @@ int newhope_enc_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, c
                     uint8_t *scratch, int kem, cudaStream_t st);
 // kem=1: out = ss (32 B); kem=0: out = message
 int newhope_dec_dev(int N, int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st);
+// One NewHope CPA-KEM job of a mixed batch (device pointers as in op_dev; scratch 64 B per instance
+// for encapsulation).  With PQCGPU_STAGE_KERNELS their core kernels run as one persistent wave
+// (newhope_mixed_wave), after each encapsulation job's prologue (newhope_mixed_pre).
+struct NhMixedJob {
+    int N, op, n;
+    const uint8_t *in0, *in1;
+    uint8_t *out0, *out1, *scratch;
+};
+int newhope_mixed_pre(const NhMixedJob &j, cudaStream_t st);
+int newhope_mixed_wave(const std::vector<NhMixedJob> &jobs, unsigned *counters, int ncounters, cudaStream_t st);
 
 // ---- FrodoKEM-640 / 976 / 1344 (frodo.cu); N = 640, 976 or 1344 ----
 int frodo_init_constants();

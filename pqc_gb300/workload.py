@@ -2,13 +2,15 @@
 
     python -m pqc_gb300.workload --alg kyber768 --n 16384 --reps 2
     python -m pqc_gb300.workload --alg newhope512,frodo640 --n 16384,256 --reps 1
+    python -m pqc_gb300.workload --alg frodo976 --n 2048 --ops shared --product 2
 
 For each algorithm in turn (a comma list, with one batch size each or one for all): generates n key
 pairs once, then runs `reps` rounds of encapsulation + decapsulation of n instances through the C
 ABI with device buffers (`PQCGPU_DEVICE_PTRS`), timing each operation with CUDA events on the
 library stream.  Inputs come from the seeded SHAKE-256 DRBG, so every run of the same command
 launches the same kernels on the same data.  Exits non-zero if any decapsulated key differs from
-the encapsulated one.
+the encapsulated one.  `--ops shared` (FrodoKEM) runs n encapsulations to the first key with the
+shared-key call instead, on the CUDA-core or tensor-core product (`--product`).
 """
 import argparse
 import sys
@@ -32,7 +34,7 @@ def mixed_kyber_spec(njobs=24, seed=12):
     return spec
 
 
-def run(alg, n, reps, want, fl):
+def run(alg, n, reps, want, fl, product=None):
     ctx = kem.Context(0)
     s = kem.sizes(alg)
     dev = torch.device("cuda:0")
@@ -54,9 +56,15 @@ def run(alg, n, reps, want, fl):
         "keypair": lambda: ctx.keypair_dev(alg, n, pk, sk, kc, fl),
         "enc": lambda: ctx.enc_dev(alg, n, ct, ss, pk, ec, fl),
         "dec": lambda: ctx.dec_dev(alg, n, ss2, ct, sk, fl),
+        # FrodoKEM: n encapsulations to instance 0's key (pqcgpu_frodo_enc_shared_key_batch)
+        "shared": lambda: ctx.frodo_enc_shared_dev(alg, n, ct, ss, pk[:s["pk"]], ec),
     }
     ops["keypair"]()
     ctx.wait()
+    if product is not None:
+        from ctypes import c_int
+        from . import _lib
+        _lib.check(_lib.load().pqcgpu_set_launch_shape(kem.alg_id(alg), 3, c_int(product), 0))
     ok = True
     for rep in range(reps):
         line = []
@@ -86,6 +94,8 @@ def main(argv=None):
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--ops", default="enc,dec", help="comma list of keypair, enc, dec to repeat")
     ap.add_argument("--plain", action="store_true", help="per-stage path instead of the fused kernels")
+    ap.add_argument("--product", type=int, default=None,
+                    help="FrodoKEM shared-key product for --ops shared: 1 CUDA cores, 2 tensor cores")
     args = ap.parse_args(argv)
     algs = [a for a in args.alg.split(",") if a]
     ns = [int(x) for x in args.n.split(",") if x]
@@ -97,12 +107,12 @@ def main(argv=None):
         ap.error("give one batch size, or one per algorithm")
     want = [o for o in args.ops.split(",") if o]
     for o in want:
-        if o not in ("keypair", "enc", "dec"):
+        if o not in ("keypair", "enc", "dec", "shared"):
             ap.error("unknown op %r" % o)
     fl = kem.PLAIN if args.plain else 0
     ok = True
     for alg, n in zip(algs, ns):
-        ok = run(alg, n, args.reps, want, fl) and ok
+        ok = run(alg, n, args.reps, want, fl, args.product) and ok
     return 0 if ok else 1
 
 

@@ -59,7 +59,12 @@ def check(jobs, expected):
             assert bytes(o1.cpu().numpy()) == e1, (alg, op, n)
 
 
-def test_mixed_batch_all_algorithms(env):
+@pytest.mark.parametrize("stage_kernels", [False, True])
+def test_mixed_batch_all_algorithms(env, stage_kernels):
+    """Every algorithm and operation in one mixed batch: each job's own kernels over the streams, or
+    (STAGE_KERNELS) the persistent waves for the Kyber and NewHope jobs with the FrodoKEM jobs on
+    the streams; every output equal to the single-algorithm calls'."""
+    from pqc_gb300 import kem
     ctx, torch, dev = env
     rng = random.Random(5)
     algs = ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "newhope1024", "frodo976", "mlkem768", "newhope512",
@@ -71,7 +76,7 @@ def test_mixed_batch_all_algorithms(env):
     rng.shuffle(spec)
     jobs, expected = build_jobs(ctx, torch, dev, spec, 3000)
     torch.cuda.synchronize()
-    ctx.mixed_dev(jobs)
+    ctx.mixed_dev(jobs, kem.STAGE_KERNELS if stage_kernels else 0)
     ctx.wait()
     check(jobs, expected)
 
