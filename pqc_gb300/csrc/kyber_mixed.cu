@@ -130,6 +130,15 @@ void fill_job(MixJob &m, int kind, const MixedKyberJob &j) {
     }
 }
 
+// The largest tile of any job kind: the kernel's dynamic shared-memory bound, set once at init so
+// that no launch (captured into a graph or not) depends on an earlier launch having raised it.
+size_t max_tile_smem() {
+    size_t sm = 0;
+    for (int kind = 0; kind < 4; kind++)
+        for (int k = 2; k <= 4; k++) sm = std::max(sm, tile_smem(kind, k, MIX_NI[kind][k - 2]));
+    return sm;
+}
+
 // One persistent launch over `items` (kind, job) on st; counter = a zeroed word of device memory.
 int launch_wave(const std::vector<std::pair<int, const MixedKyberJob *>> &items, unsigned *counter, cudaStream_t st) {
     for (size_t from = 0; from < items.size(); from += MIX_MAX_JOBS) {
@@ -145,12 +154,7 @@ int launch_wave(const std::vector<std::pair<int, const MixedKyberJob *>> &items,
             t.tiles += (items[i].second->n + m.ni - 1) / m.ni;
             sm = std::max(sm, tile_smem(m.kind, m.k, m.ni));
         }
-        if (!capturing() &&
-            cudaFuncSetAttribute(kyber_stage_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
-                cudaSuccess) {
-            cudaGetLastError();
-            return PQCGPU_ECUDA;
-        }
+        if (sm > max_tile_smem()) return PQCGPU_EINVAL;  // the bound set at init covers every job kind
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -228,6 +232,9 @@ int kyber_mixed_init() {
     if (cudaMemcpyToSymbol(kyber::c_tw, tw, sizeof tw) != cudaSuccess) return PQCGPU_ECUDA;
     if (cudaMemcpyToSymbol(kyber::c_twi, twi, sizeof twi) != cudaSuccess) return PQCGPU_ECUDA;
     kyber::prefer_shared(kyber::kyber_stage_persistent);
+    if (cudaFuncSetAttribute(kyber::kyber_stage_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kyber::max_tile_smem()) != cudaSuccess)
+        return PQCGPU_ECUDA;
     return PQCGPU_OK;
 }
 

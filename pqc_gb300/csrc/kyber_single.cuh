@@ -39,7 +39,8 @@ struct SingleSmem {
     int16_t *A;      // K*K sampled matrix entries (NTT domain), entry i*K + j
     int16_t *polys;  // NPOLY polynomials
     uint8_t *prf;    // (2K + 1) PRF outputs
-    uint8_t *buf;    // ciphertext (encapsulation / comparison) or public key (keypair) bytes
+    uint8_t *buf;    // encapsulation: pk copy, then the ciphertext; decapsulation: ct copy; keypair: pk
+    static_assert(P<K, V>::PKB <= 1600 && P<K, V>::CTB <= 1600, "buf holds a public key or a ciphertext");
     uint2 *seeds;    // 32 lanes: [0,4) m, [4,8) h, [8,12) K-bar, [12,16) r, [16,20) rho, [20,24) sigma,
                      // [24,28) H(c) or J(z || c), [28] fail flag
     __device__ __forceinline__ explicit SingleSmem(uint8_t *s) {
@@ -293,7 +294,12 @@ __global__ void __launch_bounds__(SINGLE_THREADS) kyber_enc_single(const uint8_t
     const WarpKeccak w(lane);
     const uint8_t *pki = pk + (size_t)x * Pp::PKB;
     load_twiddles(S.tw, S.twi);
-    if (tid < 4) S.seeds[16 + tid] = reinterpret_cast<const uint2 *>(pki + Pp::POLYVECBYTES)[tid];  // rho
+    // the public key to shared memory in one coalesced pass: H(pk), the matrix seed rho and t-hat
+    // are read from there, so no global-load latency sits inside the serial H(pk) sponge (the
+    // ciphertext overwrites this copy only after t-hat has been used)
+    for (int i = tid; i < Pp::PKB / 8; i += SINGLE_THREADS)
+        reinterpret_cast<uint2 *>(S.buf)[i] = reinterpret_cast<const uint2 *>(pki)[i];
+    const uint2 *rho = reinterpret_cast<const uint2 *>(S.buf + Pp::POLYVECBYTES);
     __syncthreads();
     if (warp == 0) {  // m
         const uint2 *cn = reinterpret_cast<const uint2 *>(coins + (size_t)x * 32);
@@ -307,12 +313,12 @@ __global__ void __launch_bounds__(SINGLE_THREADS) kyber_enc_single(const uint8_t
         if (lane < 4) S.seeds[lane] = m;
     } else if (warp == 1) {  // H(pk)
         uint2 h;
-        warp_absorb2<SHA3_256_LANES>(h, reinterpret_cast<const uint2 *>(pki), Pp::PKB / 8, nullptr, 0, DOM_SHA3, w);
+        warp_absorb2<SHA3_256_LANES>(h, reinterpret_cast<const uint2 *>(S.buf), Pp::PKB / 8, nullptr, 0, DOM_SHA3, w);
         keccak_f1600_warp(h, w);
         if (lane < 4) S.seeds[4 + lane] = h;
     } else {  // the matrix entries A^T[i][j] = XOF(rho || i || j), meanwhile
         for (int e = warp - 2; e < K * K; e += SINGLE_WARPS - 2)
-            warp_sample_entry<V>(S.seeds + 16, e / K, e % K, S.A + e * POLY_PITCH, w);
+            warp_sample_entry<V>(rho, e / K, e % K, S.A + e * POLY_PITCH, w);
     }
     __syncthreads();
     if (warp == 0) {  // (K-bar, r) = G(m || H(pk))
@@ -325,7 +331,7 @@ __global__ void __launch_bounds__(SINGLE_THREADS) kyber_enc_single(const uint8_t
         if (lane < 8) S.seeds[8 + lane] = g;  // lanes 0-3 K-bar, 4-7 r
     }
     __syncthreads();
-    single_encrypt<K, V, false>(S, pki, nullptr, 0, SINGLE_WARPS, [] { __syncthreads(); });
+    single_encrypt<K, V, false>(S, S.buf, nullptr, 0, SINGLE_WARPS, [] { __syncthreads(); });
     __syncthreads();
     uint8_t *cti = ct + (size_t)x * Pp::CTB;
     for (int i = tid; i < Pp::CTB / 8; i += SINGLE_THREADS)
@@ -359,9 +365,14 @@ __global__ void __launch_bounds__(SINGLE_THREADS) kyber_dec_single(const uint8_t
     const SingleSmem<K, V> S(smem);
     const int x = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const WarpKeccak w(lane);
-    const uint8_t *cti = ct + (size_t)x * Pp::CTB, *ski = sk + (size_t)x * Pp::SKB;
+    const uint8_t *cti, *ski = sk + (size_t)x * Pp::SKB;
     const uint8_t *pki = ski + Pp::SKCPA;
     load_twiddles(S.tw, S.twi);
+    // the ciphertext to shared memory in one coalesced pass: H(c), the decryption and the
+    // comparison read it from there (the serial H(c) sponge then waits on no global load)
+    for (int i = tid; i < Pp::CTB / 8; i += SINGLE_THREADS)
+        reinterpret_cast<uint2 *>(S.buf)[i] = reinterpret_cast<const uint2 *>(ct + (size_t)x * Pp::CTB)[i];
+    cti = S.buf;
     if (tid < 4) {
         S.seeds[16 + tid] = reinterpret_cast<const uint2 *>(pki + Pp::POLYVECBYTES)[tid];  // rho
         S.seeds[4 + tid] = reinterpret_cast<const uint2 *>(ski + Pp::SKB - 64)[tid];       // h = H(pk)
