@@ -418,13 +418,44 @@ __device__ void sa_epilogue(uint32_t *acc, const uint16_t *Spt, const uint8_t *p
     constexpr int LOGQ = P::LOGQ, B = P::B;
     const int tid = threadIdx.x, nthr = blockDim.x;
     {
+        // V = S' B (8 x 8, sums over N): thread = (row i of S', k residue kb mod KS); each step reads
+        // one whole row of B (8 values; 16 bytes when LOGQ = 16) and updates the thread's 8 sums;
+        // the KS / 4 residues of a warp are summed by shuffles, then one shared atomic per output
         const uint8_t *pb = p + SEEDA;
-        for (int t = tid; t < 64 * 4; t += nthr) {
-            const int o = t & 63, part = t >> 6, i = o >> 3, l = o & 7;
-            uint32_t sum = 0;
-            for (int k = part; k < N; k += 4)
-                sum += (uint32_t)Spt[k * NB + i] * unpack_at<LOGQ>(pb + (size_t)LOGQ * k, l);
-            atomicAdd(acc + NB * N + o, sum);
+        const int ks = nthr / NB, i = tid % NB, kb = tid / NB;
+        // 16-bit rows as two 8-byte loads when B is 8-byte aligned (the public key inside a
+        // FrodoKEM-976 secret key starts 24 bytes in, so 16-byte alignment is not given)
+        const bool wide = LOGQ == 16 && (reinterpret_cast<uintptr_t>(pb) & 7) == 0;
+        uint32_t v[NB];
+#pragma unroll
+        for (int l = 0; l < NB; l++) v[l] = 0;
+        for (int k = kb; k < N; k += ks) {
+            const uint32_t sv = Spt[k * NB + i];
+            uint32_t b[NB];
+            if (wide) {
+                const uint2 r0 = reinterpret_cast<const uint2 *>(pb + (size_t)16 * k)[0];
+                const uint2 r1 = reinterpret_cast<const uint2 *>(pb + (size_t)16 * k)[1];
+                const uint32_t w[4] = {r0.x, r0.y, r1.x, r1.y};
+#pragma unroll
+                for (int l = 0; l < NB; l++) {  // big-endian 16-bit values
+                    const uint32_t h = (w[l >> 1] >> (16 * (l & 1))) & 0xffff;
+                    b[l] = ((h & 0xff) << 8) | (h >> 8);
+                }
+            } else {
+#pragma unroll
+                for (int l = 0; l < NB; l++) b[l] = unpack_at<LOGQ>(pb + (size_t)LOGQ * k, l);
+            }
+#pragma unroll
+            for (int l = 0; l < NB; l++) v[l] += sv * b[l];
+        }
+#pragma unroll
+        for (int l = 0; l < NB; l++) {
+            v[l] += __shfl_xor_sync(0xffffffffu, v[l], 8);
+            v[l] += __shfl_xor_sync(0xffffffffu, v[l], 16);
+        }
+        if ((tid & 31) < NB) {
+#pragma unroll
+            for (int l = 0; l < NB; l++) atomicAdd(acc + NB * N + i * NB + l, v[l]);
         }
     }
     __syncthreads();
@@ -562,8 +593,8 @@ __global__ void __launch_bounds__(SA_THREADS) fr_sa_final(int n, uint8_t *ct, co
 // of every instance form one matrix product, [S'_0; S'_1; ...] (8n x N) times A (N x N).
 // ---------------------------------------------------------------------------------------------
 // A (N x N, u16, row-major) from seedA, one thread per row (frodo_macrify_reference.cu:164-188);
-// with planes != nullptr also the transposed tensor-core operands: planes[0][j][i] = A[i][j] & 1023
-// and planes[1][j][i] = A[i][j] >> 10 as fp16 bit patterns (exact: both below 2048).  CTA 0's first
+// with planes != nullptr also the tensor-core operands: plane 0 = A & 1023 and plane 1 = A >> 10 as fp16
+// bit patterns (exact: both below 2048), column j / row k of A at fr_tc_plane_index.  CTA 0's first
 // warp computes pkh = SHAKE(pk, SSB) meanwhile (fr_pkh_one's work, 115 serial permutations for
 // n = 976), so the two fixed latencies of a shared-key batch overlap.
 template <int N>
@@ -594,8 +625,8 @@ __global__ void __launch_bounds__(128) fr_gen_a(const uint8_t *pk, uint16_t *A, 
                     const uint32_t a = h ? (t >> 16) : (t & 0xffff);
                     A[(size_t)row * N + j] = (uint16_t)a;
                     if (planes) {
-                        planes[(size_t)j * N + row] = __half_as_ushort(__uint2half_rn(a & 1023));
-                        planes[(size_t)N * N + (size_t)j * N + row] = __half_as_ushort(__uint2half_rn(a >> 10));
+                        planes[fr_tc_plane_index(N, 0, j, row)] = __half_as_ushort(__uint2half_rn(a & 1023));
+                        planes[fr_tc_plane_index(N, 1, j, row)] = __half_as_ushort(__uint2half_rn(a >> 10));
                     }
                 }
             }
@@ -806,8 +837,8 @@ int dec_n(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scr
 // Product of a shared-key batch: 1 CUDA cores (mad.lo, fr_sa_shared_simt), 2 tensor cores
 // (tcgen05 kind::f16 on split A, fr_sa_shared_tc); 0 = the default below, chosen by measurement on
 // GB300 at 2048 encapsulations to one key (product kernel, CUDA cores -> tensor cores):
-// FrodoKEM-640 0.432 -> 0.176 ms, -976 1.071 -> 0.356 ms, -1344 1.959 -> 0.574 ms, the whole batch
-// 1.39 -> 1.69, 0.67 -> 0.87 and 0.44 -> 0.63 M encapsulations/s.
+// FrodoKEM-976 product kernel 1.070 -> 0.158 ms; the whole batch, FrodoKEM-640 / 976 / 1344:
+// 1.38 -> 1.84, 0.66 -> 0.99 and 0.44 -> 0.71 M encapsulations/s.
 static LaunchShape g_fr_shared = {0, 0};
 constexpr int FR_SHARED_DEFAULT = 2;
 
@@ -821,7 +852,7 @@ int frodo_get_shared_product() {
     g_fr_shared.get(p, t);
     return p;
 }
-size_t frodo_shared_extra_bytes(int N) { return 256 + (size_t)N * N * 2 * 3; }
+size_t frodo_shared_extra_bytes(int N) { return 256 + (size_t)N * N * 2 + fr_tc_planes_elems(N) * 2; }
 
 namespace {
 template <int N>
@@ -832,6 +863,7 @@ int enc_shared_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8
     if (product == 0) product = FR_SHARED_DEFAULT;
     uint8_t *pkh = extra;
     uint16_t *A = reinterpret_cast<uint16_t *>(extra + 256), *planes = A + (size_t)N * N;
+    if (product == 2 && cudaMemsetAsync(planes, 0, fr_tc_planes_elems(N) * 2, st) != cudaSuccess) return PQCGPU_ECUDA;
     PQC_LAUNCH(st, "fr_gen_a", N, 0,
                fr_gen_a<N><<<1 + (N + 127) / 128, 128, 0, st>>>(pk, A, product == 2 ? planes : nullptr, pkh));
     PQC_LAUNCH(st, "fr_enc_pre", N, 0, fr_enc_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, pk, mu, scratch, 1, pkh, 0));
@@ -854,7 +886,7 @@ int enc_shared_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8
 
 // n encapsulations to one public key pk (PKB bytes), mu per instance; scratch: n x
 // frodo_scratch_bytes(N), extra: frodo_shared_extra_bytes(N) (256-byte aligned): pkh at +0, the
-// tensor product's error word at +64, A (N x N u16) at +256, then its two fp16 planes.
+// tensor product's error word at +64, A (N x N u16) at +256, then its two tiled fp16 planes.
 int frodo_enc_shared_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
                          uint8_t *extra, cudaStream_t st) {
     if (N == 640) return enc_shared_n<640>(n, ct, ss, pk, mu, scratch, extra, st);

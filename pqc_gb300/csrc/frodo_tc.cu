@@ -13,13 +13,20 @@
 // The result goes to each instance's u32 accumulator in scratch, which fr_sa_final turns into
 // B' + E', V, C and the ciphertext.
 //
-// Kernel layout: CTA = 128 rows of the stacked S' (16 instances) x 128 columns of A, 4 warps.
-// For each K chunk of 64 the warps convert S' (scratch, u16 two's complement, N x 8 per instance)
-// and copy the two planes of A (fr_gen_a: transposed fp16, column j of A contiguous in k) into
-// shared memory in the no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix;
-// LBO = 128 bytes between core matrices along K, SBO = 1024 bytes between 8-row groups); one
-// thread issues the tcgen05.mma kind::f16 instructions (M = 128, N = 128, K = 16 each) into two
-// fp32 accumulators in tensor memory and commits them to an mbarrier that the CTA waits on.
+// Kernel layout: CTA = 128 rows of the stacked S' (16 instances) x 128 columns of A, 4 warps, K in
+// chunks of 64 through two shared-memory stages, so that chunk c + 1 is fetched while the tensor
+// cores work on chunk c:
+//   * A's planes come pre-tiled from fr_gen_a (fr_tc_plane_index): each chunk's two 16 KB operand
+//     tiles are single bulk copies (cp.async.bulk, completion counted in bytes on the stage's
+//     mbarrier), issued by one thread;
+//   * S' (scratch, u16 two's complement, N x 8 per instance) is loaded into registers, converted
+//     to fp16, transposed and stored by all threads in the no-swizzle K-major core-matrix layout
+//     (8 rows x 16 bytes per core matrix; LBO = 128 bytes between core matrices along K, SBO = 1024
+//     bytes between 8-row groups), each thread's 8 row stores rotated by its k block so that a
+//     warp's 16-byte stores spread over all banks;
+//   * one thread issues the tcgen05.mma kind::f16 instructions (M = 128, N = 128, K = 16 each) into
+//     two fp32 accumulators in tensor memory and commits them to the stage's second mbarrier,
+//     which says when the stage may be refilled.
 // The epilogue reads the accumulators with tcgen05.ld (warp w: lanes 32w..32w+31 = rows).
 // Every wait is bounded: a wait that runs out sets an error word (extra buffer) and the CTA frees
 // its tensor memory and returns.
@@ -37,7 +44,7 @@ constexpr int TC_M = 128, TC_N = 128, TC_KC = 64, TC_THREADS = 128;
 constexpr int TC_TMEM_COLS = 2 * TC_N;  // two fp32 accumulators
 constexpr uint32_t LBO = 128, SBO = (TC_KC / 8) * 128;
 constexpr int OP_BYTES = TC_M * TC_KC * 2;  // one 128 x 64 fp16 operand tile
-// Dynamic shared memory requested per CTA: three operand tiles (48 KB) padded so that at most two
+// Dynamic shared memory requested per CTA: two stages of three operand tiles (96 KB), so that at most two
 // CTAs share an SM, whose 512 tensor-memory columns then always hold both CTAs' 256.
 constexpr int TC_SMEM = 96 * 1024;
 constexpr int WAIT_LIMIT = 1 << 22;
@@ -79,19 +86,37 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-// planes: [2][N][N] fp16 bit patterns, plane 0 = A_lo^T, plane 1 = A_hi^T; error: a word set on a
-// wait that ran out.
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+// The stage's two plane tiles of chunk c: one bulk copy each, completion counted in bytes on `bar`.
+__device__ __forceinline__ void issue_planes(uint32_t bar, uint32_t dst_lo, uint32_t dst_hi, const uint16_t *src_lo,
+                                             const uint16_t *src_hi) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(2 * OP_BYTES) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst_lo),
+                 "l"(src_lo), "r"(OP_BYTES), "r"(bar)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst_hi),
+                 "l"(src_hi), "r"(OP_BYTES), "r"(bar)
+                 : "memory");
+}
+
+// planes: A's two fp16 planes tiled by fr_tc_plane_index; error: a word set on a wait that ran out.
 template <int N>
 __global__ void __launch_bounds__(TC_THREADS, 1) fr_sa_shared_tc(int n, const uint16_t *planes, uint8_t *scratch,
                                                                  unsigned *error) {
-    extern __shared__ __align__(128) uint8_t smem[];
-    __shared__ __align__(8) uint64_t bar;
+    constexpr int NT = fr_tc_ntiles(N), KCH = fr_tc_kchunks(N);
+    static_assert(FR_TC_N == TC_N && FR_TC_KC == TC_KC, "tiles of fr_gen_a are the operand tiles");
+    static_assert(N % 16 == 0, "whole K = 16 steps");
+    extern __shared__ __align__(128) uint8_t smem[];  // stage s: S' tile, plane-lo tile, plane-hi tile
+    __shared__ __align__(8) uint64_t full[2], mdone[2];
     __shared__ uint32_t tmem_slot;
     __shared__ int s_abort;
-    uint8_t *opA = smem, *opLo = smem + OP_BYTES, *opHi = smem + 2 * OP_BYTES;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.x * TC_M, x0 = m0 / NB, n0 = blockIdx.y * TC_N;
-    const uint32_t bar_a = smem_addr(&bar);
+    const int m0 = blockIdx.x * TC_M, x0 = m0 / NB, nt = blockIdx.y, n0 = nt * TC_N;
+    auto opA = [&](int st) { return smem + st * 3 * OP_BYTES; };
+    auto full_a = [&](int st) { return smem_addr(&full[st]); };
+    auto mdone_a = [&](int st) { return smem_addr(&mdone[st]); };
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
                      "r"(TC_TMEM_COLS)
@@ -99,7 +124,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fr_sa_shared_tc(int n, const ui
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+        for (int i = 0; i < 2; i++) {
+            mbar_init(full_a(i));
+            mbar_init(mdone_a(i));
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
@@ -107,78 +135,119 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fr_sa_shared_tc(int n, const ui
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot, d_lo = tmem, d_hi = tmem + TC_N;
-    const int nchunks = (N + TC_KC - 1) / TC_KC;
-    for (int c = 0; c < nchunks; c++) {
-        const int k0 = c * TC_KC;
-        // S' rows: task = (instance group g of 8 rows, k block kb of 8): 8 x 8 values, a register
-        // transpose, then one 16-byte store per row
-        {
-            const int g = tid >> 3, kb = tid & 7, x = x0 + g, k = k0 + 8 * kb;
-            uint16_t v[8][8];  // v[i][kk] = S'[x][i][k + kk]
-            if (x < n && k < N) {
-                const uint4 *src = reinterpret_cast<const uint4 *>(scratch + (size_t)x * scratch_bytes(N)) + k;
+    auto plane_src = [&](int p, int c) { return planes + ((size_t)(p * NT + nt) * KCH + c) * FR_TC_TILE; };
+
+    // S' of chunk c: thread = (instance g of the tile, k block kb of 8)
+    const int g = tid >> 3, kb = tid & 7, x = x0 + g;
+    const uint4 *sp = reinterpret_cast<const uint4 *>(scratch + (size_t)x * scratch_bytes(N));
+    uint4 v[8];  // v[kk] = S'^T row k0 + 8 kb + kk (8 u16: i = 0..7)
+    auto load_s = [&](int c) {
+        const int k = c * TC_KC + 8 * kb;
 #pragma unroll
-                for (int kk = 0; kk < 8; kk++) {
-                    const uint4 s = src[kk];
-                    const uint32_t w[4] = {s.x, s.y, s.z, s.w};
+        for (int kk = 0; kk < 8; kk++) v[kk] = (x < n && k + kk < N) ? sp[k + kk] : make_uint4(0, 0, 0, 0);
+    };
+    auto store_s = [&](int st) {
+        uint4 o[8];  // o[i] = 8 fp16 of row i: S'[i][k0 + 8 kb + kk], kk = 0..7
 #pragma unroll
-                    for (int i = 0; i < 8; i++) {
-                        const int16_t sv = (int16_t)((w[i >> 1] >> (16 * (i & 1))) & 0xffff);
-                        v[i][kk] = __half_as_ushort(__short2half_rn(sv));
-                    }
-                }
-            } else {
+        for (int i = 0; i < 8; i++) {
+            uint32_t h[8];
 #pragma unroll
-                for (int i = 0; i < 8; i++)
-#pragma unroll
-                    for (int kk = 0; kk < 8; kk++) v[i][kk] = 0;
+            for (int kk = 0; kk < 8; kk++) {
+                const uint32_t w = (i < 2 ? v[kk].x : i < 4 ? v[kk].y : i < 6 ? v[kk].z : v[kk].w) >> (16 * (i & 1));
+                h[kk] = __half_as_ushort(__short2half_rn((int16_t)(w & 0xffff)));
             }
+            o[i] = make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16), h[6] | (h[7] << 16));
+        }
+        // rotate by kb (three conditional stages) so that store q writes row (q + kb) & 7: the 8
+        // threads of one instance then hit 8 different 16-byte bank groups
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
-                uint4 o;
-                o.x = v[i][0] | ((uint32_t)v[i][1] << 16);
-                o.y = v[i][2] | ((uint32_t)v[i][3] << 16);
-                o.z = v[i][4] | ((uint32_t)v[i][5] << 16);
-                o.w = v[i][6] | ((uint32_t)v[i][7] << 16);
-                *reinterpret_cast<uint4 *>(opA + g * SBO + kb * LBO + i * 16) = o;
-            }
-        }
-        // the planes: row j of each operand tile = column n0 + j of A, 8 k values per 16 bytes
-        for (int t = tid; t < 2 * TC_N * (TC_KC / 8); t += TC_THREADS) {
-            const int plane = t / (TC_N * (TC_KC / 8)), r = (t / (TC_KC / 8)) % TC_N, kb = t % (TC_KC / 8);
-            const int j = n0 + r, k = k0 + 8 * kb;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (j < N && k < N) v = *reinterpret_cast<const uint4 *>(planes + (size_t)plane * N * N + (size_t)j * N + k);
-            *reinterpret_cast<uint4 *>((plane ? opHi : opLo) + (r >> 3) * SBO + kb * LBO + (r & 7) * 16) = v;
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int b = 1; b < 8; b <<= 1) {
+            if (kb & b) {
+                uint4 t[8];
 #pragma unroll
-            for (int ks = 0; ks < TC_KC / 16; ks++) {
-                const uint32_t off = ks * 2 * LBO;  // K = 16: two core matrices
-                const uint32_t acc = (c > 0 || ks > 0) ? 1u : 0u;
-                mma_f16(d_lo, sdesc(smem_addr(opA) + off), sdesc(smem_addr(opLo) + off), acc);
-                mma_f16(d_hi, sdesc(smem_addr(opA) + off), sdesc(smem_addr(opHi) + off), acc);
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_a)
-                         : "memory");
-        }
-        if (!mbar_wait(bar_a, (uint32_t)(c & 1))) {
-            if (tid == 0) {
-                atomicOr(error, 1u);
-                s_abort = 1;
+                for (int q = 0; q < 8; q++) t[q] = o[(q + b) & 7];
+#pragma unroll
+                for (int q = 0; q < 8; q++) o[q] = t[q];
             }
         }
+        uint8_t *base = opA(st) + g * SBO + kb * LBO;
+#pragma unroll
+        for (int q = 0; q < 8; q++) *reinterpret_cast<uint4 *>(base + ((q + kb) & 7) * 16) = o[q];
+    };
+
+    // prologue: chunk 0 into stage 0
+    if (tid == 0)
+        issue_planes(full_a(0), smem_addr(opA(0) + OP_BYTES), smem_addr(opA(0) + 2 * OP_BYTES), plane_src(0, 0),
+                     plane_src(1, 0));
+    load_s(0);
+    store_s(0);
+    int pend0 = 0, pend1 = -1;  // thread 0's view: the chunk whose bulk copy into stage 0 / 1 is in flight
+    int last_commit = -1;      // the last chunk whose MMAs were committed
+    for (int c = 0; c < KCH; c++) {
+        const int st = c & 1;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // S' stores -> the tensor cores
         __syncthreads();
         if (s_abort) break;
+        if (tid == 0) {
+            if (!mbar_wait(full_a(st), (uint32_t)((c >> 1) & 1))) {
+                atomicOr(error, 1u);
+                s_abort = 1;
+            } else {
+                (st ? pend1 : pend0) = -1;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const int steps = min(TC_KC, N - c * TC_KC) / 16;
+                const uint32_t a = smem_addr(opA(st)), lo = a + OP_BYTES, hi = a + 2 * OP_BYTES;
+                for (int ks = 0; ks < steps; ks++) {
+                    const uint32_t off = ks * 2 * LBO;  // K = 16: two core matrices
+                    const uint32_t acc = (c > 0 || ks > 0) ? 1u : 0u;
+                    mma_f16(d_lo, sdesc(a + off), sdesc(lo + off), acc);
+                    mma_f16(d_hi, sdesc(a + off), sdesc(hi + off), acc);
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 mdone_a(st))
+                             : "memory");
+                last_commit = c;
+            }
+        }
+        if (c + 1 < KCH) {
+            const int ns = st ^ 1;
+            load_s(c + 1);  // global loads in flight while the stage frees up
+            // stage ns was read by the MMAs of chunk c - 1
+            bool ok = c < 1 || mbar_wait(mdone_a(ns), (uint32_t)(((c - 1) >> 1) & 1));
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicOr(error, 1u);
+                    s_abort = 1;
+                }
+                __syncthreads();
+                break;
+            }
+            if (tid == 0 && !s_abort) {
+                issue_planes(full_a(ns), smem_addr(opA(ns) + OP_BYTES), smem_addr(opA(ns) + 2 * OP_BYTES),
+                             plane_src(0, c + 1), plane_src(1, c + 1));
+                (ns ? pend1 : pend0) = c + 1;
+            }
+            store_s(ns);
+        }
     }
+    __syncthreads();
+    bool ok = !s_abort;
+    if (ok) {  // the last commit covers every MMA issued before it
+        const int c = KCH - 1;
+        ok = mbar_wait(mdone_a(c & 1), (uint32_t)((c >> 1) & 1));
+        if (!ok) atomicOr(error, 1u);
+    } else if (tid == 0) {
+        // leave nothing in flight: wait (bounded) for pending copies and the last committed MMAs
+        if (pend0 >= 0) mbar_wait(full_a(0), (uint32_t)((pend0 >> 1) & 1));
+        if (pend1 >= 0) mbar_wait(full_a(1), (uint32_t)((pend1 >> 1) & 1));
+        if (last_commit >= 0) mbar_wait(mdone_a(last_commit & 1), (uint32_t)((last_commit >> 1) & 1));
+    }
+    ok = !__syncthreads_or(!ok);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (!s_abort) {
+    if (ok) {
         // epilogue: warp w holds rows 32w .. 32w + 31 (tensor-memory lanes)
         const int r = 32 * warp + lane, x = x0 + (r >> 3), i = r & 7;
-        uint32_t *g = reinterpret_cast<uint32_t *>(scratch + (size_t)x * scratch_bytes(N) + gacc_off(N)) + (size_t)i * N;
+        uint32_t *gacc = reinterpret_cast<uint32_t *>(scratch + (size_t)x * scratch_bytes(N) + gacc_off(N)) + (size_t)i * N;
         const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
         for (int c0 = 0; c0 < TC_N; c0 += 16) {
             uint32_t lo[16], hi[16];
@@ -204,7 +273,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fr_sa_shared_tc(int n, const ui
                            (uint32_t)__float2int_rn(__uint_as_float(lo[q]));
 #pragma unroll
                 for (int q = 0; q < 16; q += 4)
-                    if (j + q < N) *reinterpret_cast<uint4 *>(g + j + q) = make_uint4(o[q], o[q + 1], o[q + 2], o[q + 3]);
+                    if (j + q < N) *reinterpret_cast<uint4 *>(gacc + j + q) = make_uint4(o[q], o[q + 1], o[q + 2], o[q + 3]);
             }
         }
     }

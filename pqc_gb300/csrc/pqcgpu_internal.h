@@ -167,8 +167,24 @@ int frodo_get_shared_product();
 size_t frodo_shared_extra_bytes(int N);
 int frodo_enc_shared_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
                          uint8_t *extra, cudaStream_t st);
-// The tensor-core product G[x] = S'[x] A (frodo_tc.cu): planes = the split, transposed A from fr_gen_a;
-// error = a zeroed device word, set if a wait in the kernel runs out.
+// The tensor-core product G[x] = S'[x] A (frodo_tc.cu): planes = the split A from fr_gen_a, tiled as
+// below; error = a zeroed device word, set if a wait in the kernel runs out.
 int frodo_shared_tc_launch(int N, int n, const uint16_t *planes, uint8_t *scratch, unsigned *error, cudaStream_t st);
+// A's two fp16 planes (A & 1023, A >> 10) as the product kernel reads them: one 16 KB tile per
+// (plane, 128 output columns, 64 k), each tile already in the no-swizzle K-major core-matrix layout
+// of a tcgen05 operand (8 columns x 8 k = 16-byte rows of one core matrix; core matrices 128 bytes
+// apart along k and 1024 bytes apart along the columns), so the kernel moves a tile with one bulk
+// copy.  Entries beyond N are zero (the buffer is cleared before fr_gen_a fills it).
+constexpr int FR_TC_N = 128, FR_TC_KC = 64, FR_TC_TILE = FR_TC_N * FR_TC_KC;  // tile: u16 elements
+__host__ __device__ constexpr int fr_tc_ntiles(int N) { return (N + FR_TC_N - 1) / FR_TC_N; }
+__host__ __device__ constexpr int fr_tc_kchunks(int N) { return (N + FR_TC_KC - 1) / FR_TC_KC; }
+__host__ __device__ constexpr size_t fr_tc_planes_elems(int N) {
+    return (size_t)2 * fr_tc_ntiles(N) * fr_tc_kchunks(N) * FR_TC_TILE;
+}
+// u16 index of plane p's entry for output column j and k
+__host__ __device__ constexpr size_t fr_tc_plane_index(int N, int p, int j, int k) {
+    return ((size_t)(p * fr_tc_ntiles(N) + j / FR_TC_N) * fr_tc_kchunks(N) + k / FR_TC_KC) * FR_TC_TILE +
+           ((j % FR_TC_N) >> 3) * 512 + ((k % FR_TC_KC) >> 3) * 64 + (j & 7) * 8 + (k & 7);
+}
 
 }  // namespace pqc
