@@ -267,7 +267,8 @@ int pqcgpu_get_launch_shape(pqcgpu_alg alg, int op, int *ni, int *threads);
  * Copies in run in order on one stream and copies out on another. Each chunk's kernels start as
  * soon as its inputs are in, on one of `streams` compute streams (1..8) in turn. Each chunk has
  * its own device buffers, up to 16 chunks and the context budget; later chunks reuse them.
- * Zeros select the defaults: chunk_max 16384, chunk_first = chunk_last = chunk_max / 4, 8 streams.
+ * Zeros select the defaults: chunk_max 16384, chunk_first = chunk_max / 8, chunk_last =
+ * chunk_max / 4, 8 streams (measured best on GB300 for Kyber-768 at 65536 instances).
  * Applies to all contexts of the process. */
 int pqcgpu_set_host_pipeline(size_t chunk_max, size_t chunk_first, size_t chunk_last, int streams);
 int pqcgpu_get_host_pipeline(size_t *chunk_max, size_t *chunk_first, size_t *chunk_last, int *streams);

@@ -452,7 +452,7 @@ struct OpDesc {
 // the first and the last chunk, and the number of compute streams.  A chunk's device buffers are
 // also capped at SLOT_BYTES_MAX, which caps FrodoKEM chunks at 2048 instances.
 struct PipeShape {
-    size_t chunk_max = 16384, chunk_first = 4096, chunk_last = 4096;
+    size_t chunk_max = 16384, chunk_first = 2048, chunk_last = 4096;
     int streams = 8;
 };
 PipeShape g_pipe;
@@ -462,8 +462,12 @@ constexpr size_t SLOT_BYTES_MAX = (size_t)256 << 20;
 // Chunk sizes for a host-buffer call of n instances.  The first chunk's copies in and the last
 // chunk's copies out overlap no kernels, so chunks may start at `first` and double up to cmax, and
 // shrink from cmax to `last` at the end; the middle is split evenly into chunks of at most cmax.
-// 65536 instances with cmax = 16384, first = last = 4096 (the default): 4096, 8192, 13654, 13654,
-// 13652, 8192, 4096; with cmax = 8192, first = 4096, last = 8192: 4096, 8 x 7680.
+// 65536 instances with cmax = 16384, first = 2048, last = 4096 (the default): 2048, 4096, 8192,
+// 12971, 12971, 12970, 8192, 4096; with cmax = 8192, first = 4096, last = 8192: 4096, 8 x 7680.
+// The default was measured on GB300 (Kyber-768 encapsulation + decapsulation of 65536 instances
+// through host buffers, median of three): first / last chunk 2048 / 4096 3.37 ms a step, 4096 /
+// 4096 3.42 ms, 1024 / 4096 3.47 ms, 1024 / 8192 3.40 ms, 512 / 4096 3.64 ms; chunks of at most
+// 24576 or 12288 instances 3.45 and 3.66 ms.
 std::vector<size_t> chunk_plan(size_t n, size_t cmax, size_t first, size_t last) {
     std::vector<size_t> head, tail;
     size_t ramp = 0;
@@ -1075,7 +1079,7 @@ extern "C" int pqcgpu_kyber_indcpa_dec_batch(pqcgpu_ctx *c, int variant, int k, 
 extern "C" int pqcgpu_set_host_pipeline(size_t chunk_max, size_t chunk_first, size_t chunk_last, int streams) {
     PipeShape p;
     if (chunk_max) p.chunk_max = chunk_max;
-    p.chunk_first = chunk_first ? chunk_first : p.chunk_max / 4;
+    p.chunk_first = chunk_first ? chunk_first : p.chunk_max / 8;
     p.chunk_last = chunk_last ? chunk_last : p.chunk_max / 4;
     if (streams) p.streams = streams;
     if (p.chunk_max < 64 || p.chunk_max > ((size_t)1 << 24))

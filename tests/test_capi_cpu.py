@@ -167,10 +167,10 @@ def test_host_pipeline_shape_validation():
     from pqc_gb300 import _lib
     lib = _lib.load()
     default = kem.get_host_pipeline()
-    assert default == (16384, 4096, 4096, 8)
+    assert default == (16384, 2048, 4096, 8)
     try:
         kem.set_host_pipeline(32768, 0, 0, 4)
-        assert kem.get_host_pipeline() == (32768, 8192, 8192, 4)
+        assert kem.get_host_pipeline() == (32768, 4096, 8192, 4)
         kem.set_host_pipeline(8192, 2048, 8192, 8)
         assert kem.get_host_pipeline() == (8192, 2048, 8192, 8)
         assert lib.pqcgpu_set_host_pipeline(32, 0, 0, 0) != 0         # chunk_max < 64
