@@ -122,6 +122,12 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi takes a moment to print its first line: wait for it (at most 3 s), so that
+            # a short region still has the sample taken as it starts, then one every 200 ms
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.first = max(0, len(self.lines) - 1)
         except OSError:
             self.proc = None
 
@@ -139,7 +145,7 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in self.lines:
+        for l in self.lines[getattr(self, "first", 0):]:
             f = [x.strip() for x in l.split(",")]
             if len(f) < 9:
                 continue

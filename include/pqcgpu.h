@@ -128,7 +128,9 @@ int pqcgpu_kem_enc_batch_noalloc(pqcgpu_alg alg, size_t n, uint8_t *ct, uint8_t 
  * instances (frodo_macrify_reference.cu:102-159) run as one matrix product, on the CUDA cores or on
  * the tensor cores (launch-shape op 3 of the FrodoKEM algorithms: ni = 1 CUDA cores, 2 tensor
  * cores, 0 the measured default).  Host buffers: synchronous; PQCGPU_DEVICE_PTRS: asynchronous on
- * the context stream. */
+ * the context stream.  Every wait inside the tensor-core product is bounded: one that runs out (a
+ * device fault, never seen in normal operation) makes the call (host buffers) or the next
+ * pqcgpu_ctx_wait (device pointers) return PQCGPU_ECUDA, and that call's outputs are undefined. */
 int pqcgpu_frodo_enc_shared_key_batch(pqcgpu_ctx *ctx, pqcgpu_alg alg, size_t n, uint8_t *ct, uint8_t *ss,
                                       const uint8_t *pk, const uint8_t *coins, unsigned flags);
 

@@ -241,7 +241,25 @@ struct pqcgpu_ctx {
     uint8_t *arena = nullptr;
     size_t arena_size = 0;
     uint64_t launches_at_create = 0;
+    // a device word set by kernels whose bounded waits ran out (FrodoKEM's tensor-core product);
+    // allocated on first use, read and cleared by the call (host buffers) or by pqcgpu_ctx_wait
+    unsigned *dev_err = nullptr;
+    bool dev_err_pending = false;
     std::recursive_mutex mu;
+
+    // Read and clear the device error word (the stream must be synchronised).
+    int take_dev_err() {
+        dev_err_pending = false;
+        if (!dev_err) return PQCGPU_OK;
+        unsigned e = 0;
+        if (cudaMemcpy(&e, dev_err, sizeof e, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(PQCGPU_ECUDA, "reading the device error word failed");
+        }
+        if (!e) return PQCGPU_OK;
+        cudaMemset(dev_err, 0, sizeof e);
+        return set_err(PQCGPU_ECUDA, "tensor-core product: a wait ran out (outputs of that call are undefined)");
+    }
 
     // Arena: one device allocation, grown on demand within the budget; sub-buffers are carved
     // per call (calls on a context are serialised, so a call owns the whole arena).
@@ -359,6 +377,7 @@ extern "C" int pqcgpu_ctx_destroy(pqcgpu_ctx *c) {
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
     if (c->arena) cudaFree(c->arena);
+    if (c->dev_err) cudaFree(c->dev_err);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     if (c->copy_in) cudaStreamDestroy(c->copy_in);
     for (auto s : c->pipe)
@@ -392,7 +411,10 @@ extern "C" int pqcgpu_ctx_set_stream(pqcgpu_ctx *c, void *s) {
 extern "C" void *pqcgpu_ctx_stream(pqcgpu_ctx *c) { return c ? (void *)c->stream : nullptr; }
 extern "C" int pqcgpu_ctx_wait(pqcgpu_ctx *c) {
     if (!c) return PQCGPU_EINVAL;
-    return cuda_err(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    std::lock_guard<std::recursive_mutex> lk(c->mu);
+    const int rc = cuda_err(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    if (rc) return rc;
+    return c->dev_err_pending ? c->take_dev_err() : PQCGPU_OK;
 }
 extern "C" uint64_t pqcgpu_ctx_launches(pqcgpu_ctx *c) { return c ? g_launch_count.load() - c->launches_at_create : 0; }
 extern "C" const char *pqcgpu_last_error(void) { return g_last_error.c_str(); }
@@ -985,16 +1007,22 @@ extern "C" int pqcgpu_frodo_enc_shared_key_batch(pqcgpu_ctx *c, pqcgpu_alg alg, 
         dpk = bpk;
         dmu = bmu;
     }
-    if ((rc = frodo_enc_shared_dev(N, (int)n, dct, dss, dpk, dmu, scratch, ex, st))) return set_err(rc, "launch failed");
-    if (dev) return PQCGPU_OK;
-    unsigned err = 0;
+    if (!c->dev_err) {
+        if (cudaMalloc(&c->dev_err, 256) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(PQCGPU_ENOMEM, "cudaMalloc of the error word failed");
+        }
+        if ((rc = cuda_err(cudaMemsetAsync(c->dev_err, 0, sizeof(unsigned), st), "memset"))) return rc;
+    }
+    if ((rc = frodo_enc_shared_dev(N, (int)n, dct, dss, dpk, dmu, scratch, ex, c->dev_err, st)))
+        return set_err(rc, "launch failed");
+    c->dev_err_pending = true;
+    if (dev) return PQCGPU_OK;  // pqcgpu_ctx_wait reports a wait that ran out
     if ((rc = cuda_err(cudaMemcpyAsync(ct, dct, n * ai.ct, cudaMemcpyDeviceToHost, st), "copy out")) ||
         (rc = cuda_err(cudaMemcpyAsync(ss, dss, n * ai.ss, cudaMemcpyDeviceToHost, st), "copy out")) ||
-        (rc = cuda_err(cudaMemcpyAsync(&err, ex + 64, sizeof err, cudaMemcpyDeviceToHost, st), "copy out")) ||
         (rc = cuda_err(cudaStreamSynchronize(st), "synchronize")))
         return rc;
-    if (err) return set_err(PQCGPU_ECUDA, "tensor-core product: a wait ran out");
-    return PQCGPU_OK;
+    return c->take_dev_err();
 }
 
 // ---- launch shapes (autotuner) ----

@@ -857,7 +857,7 @@ size_t frodo_shared_extra_bytes(int N) { return 256 + (size_t)N * N * 2 + fr_tc_
 namespace {
 template <int N>
 int enc_shared_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch, uint8_t *extra,
-                 cudaStream_t st) {
+                 unsigned *error, cudaStream_t st) {
     if (sa_attrs<N>()) return PQCGPU_ECUDA;
     int product = frodo_get_shared_product();
     if (product == 0) product = FR_SHARED_DEFAULT;
@@ -867,8 +867,6 @@ int enc_shared_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8
     PQC_LAUNCH(st, "fr_gen_a", N, 0,
                fr_gen_a<N><<<1 + (N + 127) / 128, 128, 0, st>>>(pk, A, product == 2 ? planes : nullptr, pkh));
     PQC_LAUNCH(st, "fr_enc_pre", N, 0, fr_enc_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, pk, mu, scratch, 1, pkh, 0));
-    unsigned *error = reinterpret_cast<unsigned *>(extra + 64);
-    if (cudaMemsetAsync(error, 0, sizeof(unsigned), st) != cudaSuccess) return PQCGPU_ECUDA;
     if (product == 2) {
         const int rc = frodo_shared_tc_launch(N, n, planes, scratch, error, st);
         if (rc) return rc;
@@ -885,13 +883,13 @@ int enc_shared_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8
 }  // namespace
 
 // n encapsulations to one public key pk (PKB bytes), mu per instance; scratch: n x
-// frodo_scratch_bytes(N), extra: frodo_shared_extra_bytes(N) (256-byte aligned): pkh at +0, the
-// tensor product's error word at +64, A (N x N u16) at +256, then its two tiled fp16 planes.
+// frodo_scratch_bytes(N), extra: frodo_shared_extra_bytes(N) (256-byte aligned): pkh at +0, A
+// (N x N u16) at +256, then its two tiled fp16 planes.
 int frodo_enc_shared_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
-                         uint8_t *extra, cudaStream_t st) {
-    if (N == 640) return enc_shared_n<640>(n, ct, ss, pk, mu, scratch, extra, st);
-    if (N == 976) return enc_shared_n<976>(n, ct, ss, pk, mu, scratch, extra, st);
-    if (N == 1344) return enc_shared_n<1344>(n, ct, ss, pk, mu, scratch, extra, st);
+                         uint8_t *extra, unsigned *error, cudaStream_t st) {
+    if (N == 640) return enc_shared_n<640>(n, ct, ss, pk, mu, scratch, extra, error, st);
+    if (N == 976) return enc_shared_n<976>(n, ct, ss, pk, mu, scratch, extra, error, st);
+    if (N == 1344) return enc_shared_n<1344>(n, ct, ss, pk, mu, scratch, extra, error, st);
     return PQCGPU_EINVAL;
 }
 

@@ -165,8 +165,9 @@ int frodo_get_shape(int op, int *parts, int *threads);
 int frodo_set_shared_product(int product);
 int frodo_get_shared_product();
 size_t frodo_shared_extra_bytes(int N);
+// error: a device word that the tensor-core product sets (never clears) when one of its waits runs out
 int frodo_enc_shared_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
-                         uint8_t *extra, cudaStream_t st);
+                         uint8_t *extra, unsigned *error, cudaStream_t st);
 // The tensor-core product G[x] = S'[x] A (frodo_tc.cu): planes = the split A from fr_gen_a, tiled as
 // below; error = a zeroed device word, set if a wait in the kernel runs out.
 int frodo_shared_tc_launch(int N, int n, const uint16_t *planes, uint8_t *scratch, unsigned *error, cudaStream_t st);
