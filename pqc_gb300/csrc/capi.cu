@@ -990,14 +990,16 @@ extern "C" int pqcgpu_frodo_enc_shared_key_batch(pqcgpu_ctx *c, pqcgpu_alg alg, 
     if ((rc = cuda_err(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t scr = up(n * frodo_scratch_bytes(N)), extra = up(frodo_shared_extra_bytes(N));
+    const size_t s16b = up(fr_tc_s_bytes(N, (int)n));
     const size_t io = dev ? 0 : up(ai.pk) + up(n * ai.encc) + up(n * ai.ct) + up(n * ai.ss);
-    if ((rc = c->reserve(scr + extra + io))) return rc;
+    if ((rc = c->reserve(scr + extra + s16b + io))) return rc;
     uint8_t *b = c->arena, *scratch = b, *ex = b + scr;
+    uint16_t *s16 = reinterpret_cast<uint16_t *>(b + scr + extra);
     const uint8_t *dpk = pk, *dmu = coins;
     uint8_t *dct = ct, *dss = ss;
     cudaStream_t st = c->stream;
     if (!dev) {
-        uint8_t *q = b + scr + extra;
+        uint8_t *q = b + scr + extra + s16b;
         uint8_t *bpk = q, *bmu = q + up(ai.pk);
         dct = bmu + up(n * ai.encc);
         dss = dct + up(n * ai.ct);
@@ -1014,7 +1016,7 @@ extern "C" int pqcgpu_frodo_enc_shared_key_batch(pqcgpu_ctx *c, pqcgpu_alg alg, 
         }
         if ((rc = cuda_err(cudaMemsetAsync(c->dev_err, 0, sizeof(unsigned), st), "memset"))) return rc;
     }
-    if ((rc = frodo_enc_shared_dev(N, (int)n, dct, dss, dpk, dmu, scratch, ex, c->dev_err, st)))
+    if ((rc = frodo_enc_shared_dev(N, (int)n, dct, dss, dpk, dmu, scratch, ex, s16, c->dev_err, st)))
         return set_err(rc, "launch failed");
     c->dev_err_pending = true;
     if (dev) return PQCGPU_OK;  // pqcgpu_ctx_wait reports a wait that ran out

@@ -837,8 +837,8 @@ int dec_n(int n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk, uint8_t *scr
 // Product of a shared-key batch: 1 CUDA cores (mad.lo, fr_sa_shared_simt), 2 tensor cores
 // (tcgen05 kind::f16 on split A, fr_sa_shared_tc); 0 = the default below, chosen by measurement on
 // GB300 at 2048 encapsulations to one key (product kernel, CUDA cores -> tensor cores):
-// FrodoKEM-976 product kernel 1.070 -> 0.158 ms; the whole batch, FrodoKEM-640 / 976 / 1344:
-// 1.38 -> 1.84, 0.66 -> 0.99 and 0.44 -> 0.71 M encapsulations/s.
+// FrodoKEM-976 product 1.070 -> 0.116 ms (S' conversion included); the whole batch, FrodoKEM-640 /
+// 976 / 1344: 1.43 -> 1.88, 0.70 -> 1.01 and 0.45 -> 0.73 M encapsulations/s.
 static LaunchShape g_fr_shared = {0, 0};
 constexpr int FR_SHARED_DEFAULT = 2;
 
@@ -857,7 +857,7 @@ size_t frodo_shared_extra_bytes(int N) { return 256 + (size_t)N * N * 2 + fr_tc_
 namespace {
 template <int N>
 int enc_shared_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch, uint8_t *extra,
-                 unsigned *error, cudaStream_t st) {
+                 uint16_t *s16, unsigned *error, cudaStream_t st) {
     if (sa_attrs<N>()) return PQCGPU_ECUDA;
     int product = frodo_get_shared_product();
     if (product == 0) product = FR_SHARED_DEFAULT;
@@ -868,7 +868,7 @@ int enc_shared_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8
                fr_gen_a<N><<<1 + (N + 127) / 128, 128, 0, st>>>(pk, A, product == 2 ? planes : nullptr, pkh));
     PQC_LAUNCH(st, "fr_enc_pre", N, 0, fr_enc_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, pk, mu, scratch, 1, pkh, 0));
     if (product == 2) {
-        const int rc = frodo_shared_tc_launch(N, n, planes, scratch, error, st);
+        const int rc = frodo_shared_tc_launch(N, n, planes, s16, scratch, error, st);
         if (rc) return rc;
     } else {
         PQC_LAUNCH(st, "fr_sa_shared_simt", N, 0,
@@ -886,10 +886,10 @@ int enc_shared_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8
 // frodo_scratch_bytes(N), extra: frodo_shared_extra_bytes(N) (256-byte aligned): pkh at +0, A
 // (N x N u16) at +256, then its two tiled fp16 planes.
 int frodo_enc_shared_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
-                         uint8_t *extra, unsigned *error, cudaStream_t st) {
-    if (N == 640) return enc_shared_n<640>(n, ct, ss, pk, mu, scratch, extra, error, st);
-    if (N == 976) return enc_shared_n<976>(n, ct, ss, pk, mu, scratch, extra, error, st);
-    if (N == 1344) return enc_shared_n<1344>(n, ct, ss, pk, mu, scratch, extra, error, st);
+                         uint8_t *extra, uint16_t *s16, unsigned *error, cudaStream_t st) {
+    if (N == 640) return enc_shared_n<640>(n, ct, ss, pk, mu, scratch, extra, s16, error, st);
+    if (N == 976) return enc_shared_n<976>(n, ct, ss, pk, mu, scratch, extra, s16, error, st);
+    if (N == 1344) return enc_shared_n<1344>(n, ct, ss, pk, mu, scratch, extra, s16, error, st);
     return PQCGPU_EINVAL;
 }
 

@@ -15,18 +15,16 @@
 //
 // Kernel layout: CTA = 128 rows of the stacked S' (16 instances) x 128 columns of A, 4 warps, K in
 // chunks of 64 through two shared-memory stages, so that chunk c + 1 is fetched while the tensor
-// cores work on chunk c:
-//   * A's planes come pre-tiled from fr_gen_a (fr_tc_plane_index): each chunk's two 16 KB operand
-//     tiles are single bulk copies (cp.async.bulk, completion counted in bytes on the stage's
-//     mbarrier), issued by one thread;
-//   * S' (scratch, u16 two's complement, N x 8 per instance) is loaded into registers, converted
-//     to fp16, transposed and stored by all threads in the no-swizzle K-major core-matrix layout
-//     (8 rows x 16 bytes per core matrix; LBO = 128 bytes between core matrices along K, SBO = 1024
-//     bytes between 8-row groups), each thread's 8 row stores rotated by its k block so that a
-//     warp's 16-byte stores spread over all banks;
-//   * one thread issues the tcgen05.mma kind::f16 instructions (M = 128, N = 128, K = 16 each) into
-//     two fp32 accumulators in tensor memory and commits them to the stage's second mbarrier,
-//     which says when the stage may be refilled.
+// cores work on chunk c.  Every operand tile is 16 KB, stored pre-tiled in global memory in the
+// no-swizzle K-major core-matrix layout of a tcgen05 operand (8 rows x 16 bytes per core matrix;
+// LBO = 128 bytes between core matrices along K, SBO = 1024 bytes between 8-row groups):
+//   * A's two fp16 planes by fr_gen_a (fr_tc_plane_index), once per batch;
+//   * S' in fp16 by fr_s16_tiles (fr_tc_s_index) from the instances' u16 copies, a tile per CTA
+//     with coalesced loads and stores, once (each S' tile feeds all the CTAs of its row);
+// so one thread moves a chunk's three tiles with three bulk copies (cp.async.bulk, completion
+// counted in bytes on the stage's mbarrier), issues the tcgen05.mma kind::f16 instructions
+// (M = 128, N = 128, K = 16 each) into two fp32 accumulators in tensor memory, and commits them to
+// the stage's second mbarrier, which says when the stage may be refilled.
 // The epilogue reads the accumulators with tcgen05.ld (warp w: lanes 32w..32w+31 = rows).
 // Every wait is bounded: a wait that runs out sets an error word (extra buffer) and the CTA frees
 // its tensor memory and returns.
@@ -44,9 +42,10 @@ constexpr int TC_M = 128, TC_N = 128, TC_KC = 64, TC_THREADS = 128;
 constexpr int TC_TMEM_COLS = 2 * TC_N;  // two fp32 accumulators
 constexpr uint32_t LBO = 128, SBO = (TC_KC / 8) * 128;
 constexpr int OP_BYTES = TC_M * TC_KC * 2;  // one 128 x 64 fp16 operand tile
-// Dynamic shared memory requested per CTA: two stages of three operand tiles (96 KB), so that at most two
-// CTAs share an SM, whose 512 tensor-memory columns then always hold both CTAs' 256.
-constexpr int TC_SMEM = 96 * 1024;
+// Operand stages (three 16 KB tiles each).  Dynamic shared memory per CTA: two stages, 96 KB, so
+// that at most two CTAs share an SM, whose 512 tensor-memory columns then hold both CTAs' 256.
+constexpr int NSTAGE = 2;
+constexpr int TC_SMEM = NSTAGE * 3 * (TC_M * TC_KC * 2);
 constexpr int WAIT_LIMIT = 1 << 22;
 
 // Scratch layout per instance (frodo.cu FP<N>): S'^T (N x 8 u16) first, the u32 accumulator at GACC_OFF.
@@ -89,31 +88,60 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 __device__ __forceinline__ void mbar_init(uint32_t bar) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
 }
-// The stage's two plane tiles of chunk c: one bulk copy each, completion counted in bytes on `bar`.
-__device__ __forceinline__ void issue_planes(uint32_t bar, uint32_t dst_lo, uint32_t dst_hi, const uint16_t *src_lo,
-                                             const uint16_t *src_hi) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(2 * OP_BYTES) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst_lo),
-                 "l"(src_lo), "r"(OP_BYTES), "r"(bar)
-                 : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst_hi),
-                 "l"(src_hi), "r"(OP_BYTES), "r"(bar)
+// The stage's three operand tiles of chunk c: one bulk copy each, completion counted in bytes on `bar`.
+__device__ __forceinline__ void bulk_tile(uint32_t dst, const uint16_t *src, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(OP_BYTES), "r"(bar)
                  : "memory");
 }
+__device__ __forceinline__ void issue_tiles(uint32_t bar, uint32_t dst, const uint16_t *s_src, const uint16_t *lo_src,
+                                            const uint16_t *hi_src) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(3 * OP_BYTES) : "memory");
+    bulk_tile(dst, s_src, bar);
+    bulk_tile(dst + OP_BYTES, lo_src, bar);
+    bulk_tile(dst + 2 * OP_BYTES, hi_src, bar);
+}
 
-// planes: A's two fp16 planes tiled by fr_tc_plane_index; error: a word set on a wait that ran out.
+// S'^T (scratch, u16 two's complement, N x 8 per instance) -> the fp16 operand tiles of S'
+// (fr_tc_s_index).  CTA = one 16 KB tile (16 instances x 64 k): thread = (instance g, k block kb)
+// loads the instance's 8 S'^T rows of its k block (128 contiguous bytes), converts and transposes
+// them in registers, and stores 8 rows of 16 bytes; entries beyond n or N are written as zero.
 template <int N>
-__global__ void __launch_bounds__(TC_THREADS, 1) fr_sa_shared_tc(int n, const uint16_t *planes, uint8_t *scratch,
-                                                                 unsigned *error) {
+__global__ void __launch_bounds__(128) fr_s16_tiles(int n, const uint8_t *scratch, uint16_t *s16) {
+    constexpr int KCH = fr_tc_kchunks(N);
+    const int mt = blockIdx.x / KCH, c = blockIdx.x % KCH, tid = threadIdx.x, g = tid >> 3, kb = tid & 7;
+    const int x = mt * 16 + g, k = c * TC_KC + 8 * kb;
+    const uint4 *sp = reinterpret_cast<const uint4 *>(scratch + (size_t)x * scratch_bytes(N));
+    uint4 v[8];  // v[kk] = S'^T row k + kk (8 u16: i = 0..7)
+#pragma unroll
+    for (int kk = 0; kk < 8; kk++) v[kk] = (x < n && k + kk < N) ? sp[k + kk] : make_uint4(0, 0, 0, 0);
+    uint4 *out = reinterpret_cast<uint4 *>(s16 + fr_tc_s_index(N, mt * 16 + g, 0, k));  // row i at +8 i
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        uint32_t h[8];
+#pragma unroll
+        for (int kk = 0; kk < 8; kk++) {
+            const uint32_t w = (i < 2 ? v[kk].x : i < 4 ? v[kk].y : i < 6 ? v[kk].z : v[kk].w) >> (16 * (i & 1));
+            h[kk] = __half_as_ushort(__short2half_rn((int16_t)(w & 0xffff)));
+        }
+        out[i] = make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16), h[6] | (h[7] << 16));
+    }
+}
+
+// planes: A's two fp16 planes (fr_tc_plane_index); s16: S' in fp16 (fr_tc_s_index); error: a word
+// set on a wait that ran out.
+template <int N>
+__global__ void __launch_bounds__(TC_THREADS, 1) fr_sa_shared_tc(int n, const uint16_t *planes, const uint16_t *s16,
+                                                                 uint8_t *scratch, unsigned *error) {
     constexpr int NT = fr_tc_ntiles(N), KCH = fr_tc_kchunks(N);
-    static_assert(FR_TC_N == TC_N && FR_TC_KC == TC_KC, "tiles of fr_gen_a are the operand tiles");
+    static_assert(FR_TC_N == TC_N && FR_TC_KC == TC_KC && FR_TC_TILE * 2 == OP_BYTES, "tiles are the operand tiles");
     static_assert(N % 16 == 0, "whole K = 16 steps");
     extern __shared__ __align__(128) uint8_t smem[];  // stage s: S' tile, plane-lo tile, plane-hi tile
-    __shared__ __align__(8) uint64_t full[2], mdone[2];
+    __shared__ __align__(8) uint64_t full[NSTAGE], mdone[NSTAGE];
     __shared__ uint32_t tmem_slot;
     __shared__ int s_abort;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.x * TC_M, x0 = m0 / NB, nt = blockIdx.y, n0 = nt * TC_N;
+    const int mt = blockIdx.x, x0 = mt * (TC_M / NB), nt = blockIdx.y, n0 = nt * TC_N;
     auto opA = [&](int st) { return smem + st * 3 * OP_BYTES; };
     auto full_a = [&](int st) { return smem_addr(&full[st]); };
     auto mdone_a = [&](int st) { return smem_addr(&mdone[st]); };
@@ -124,7 +152,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fr_sa_shared_tc(int n, const ui
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        for (int i = 0; i < 2; i++) {
+        for (int i = 0; i < NSTAGE; i++) {
             mbar_init(full_a(i));
             mbar_init(mdone_a(i));
         }
@@ -135,114 +163,61 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fr_sa_shared_tc(int n, const ui
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot, d_lo = tmem, d_hi = tmem + TC_N;
-    auto plane_src = [&](int p, int c) { return planes + ((size_t)(p * NT + nt) * KCH + c) * FR_TC_TILE; };
 
-    // S' of chunk c: thread = (instance g of the tile, k block kb of 8)
-    const int g = tid >> 3, kb = tid & 7, x = x0 + g;
-    const uint4 *sp = reinterpret_cast<const uint4 *>(scratch + (size_t)x * scratch_bytes(N));
-    uint4 v[8];  // v[kk] = S'^T row k0 + 8 kb + kk (8 u16: i = 0..7)
-    auto load_s = [&](int c) {
-        const int k = c * TC_KC + 8 * kb;
-#pragma unroll
-        for (int kk = 0; kk < 8; kk++) v[kk] = (x < n && k + kk < N) ? sp[k + kk] : make_uint4(0, 0, 0, 0);
-    };
-    auto store_s = [&](int st) {
-        uint4 o[8];  // o[i] = 8 fp16 of row i: S'[i][k0 + 8 kb + kk], kk = 0..7
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            uint32_t h[8];
-#pragma unroll
-            for (int kk = 0; kk < 8; kk++) {
-                const uint32_t w = (i < 2 ? v[kk].x : i < 4 ? v[kk].y : i < 6 ? v[kk].z : v[kk].w) >> (16 * (i & 1));
-                h[kk] = __half_as_ushort(__short2half_rn((int16_t)(w & 0xffff)));
-            }
-            o[i] = make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16), h[6] | (h[7] << 16));
-        }
-        // rotate by kb (three conditional stages) so that store q writes row (q + kb) & 7: the 8
-        // threads of one instance then hit 8 different 16-byte bank groups
-#pragma unroll
-        for (int b = 1; b < 8; b <<= 1) {
-            if (kb & b) {
-                uint4 t[8];
-#pragma unroll
-                for (int q = 0; q < 8; q++) t[q] = o[(q + b) & 7];
-#pragma unroll
-                for (int q = 0; q < 8; q++) o[q] = t[q];
-            }
-        }
-        uint8_t *base = opA(st) + g * SBO + kb * LBO;
-#pragma unroll
-        for (int q = 0; q < 8; q++) *reinterpret_cast<uint4 *>(base + ((q + kb) & 7) * 16) = o[q];
-    };
-
-    // prologue: chunk 0 into stage 0
-    if (tid == 0)
-        issue_planes(full_a(0), smem_addr(opA(0) + OP_BYTES), smem_addr(opA(0) + 2 * OP_BYTES), plane_src(0, 0),
-                     plane_src(1, 0));
-    load_s(0);
-    store_s(0);
-    int pend0 = 0, pend1 = -1;  // thread 0's view: the chunk whose bulk copy into stage 0 / 1 is in flight
-    int last_commit = -1;      // the last chunk whose MMAs were committed
-    for (int c = 0; c < KCH; c++) {
-        const int st = c & 1;
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // S' stores -> the tensor cores
-        __syncthreads();
-        if (s_abort) break;
-        if (tid == 0) {
-            if (!mbar_wait(full_a(st), (uint32_t)((c >> 1) & 1))) {
-                atomicOr(error, 1u);
-                s_abort = 1;
-            } else {
-                (st ? pend1 : pend0) = -1;
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const int steps = min(TC_KC, N - c * TC_KC) / 16;
-                const uint32_t a = smem_addr(opA(st)), lo = a + OP_BYTES, hi = a + 2 * OP_BYTES;
-                for (int ks = 0; ks < steps; ks++) {
-                    const uint32_t off = ks * 2 * LBO;  // K = 16: two core matrices
-                    const uint32_t acc = (c > 0 || ks > 0) ? 1u : 0u;
-                    mma_f16(d_lo, sdesc(a + off), sdesc(lo + off), acc);
-                    mma_f16(d_hi, sdesc(a + off), sdesc(hi + off), acc);
-                }
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                 mdone_a(st))
-                             : "memory");
-                last_commit = c;
-            }
-        }
-        if (c + 1 < KCH) {
-            const int ns = st ^ 1;
-            load_s(c + 1);  // global loads in flight while the stage frees up
-            // stage ns was read by the MMAs of chunk c - 1
-            bool ok = c < 1 || mbar_wait(mdone_a(ns), (uint32_t)(((c - 1) >> 1) & 1));
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) {
-                    atomicOr(error, 1u);
-                    s_abort = 1;
-                }
-                __syncthreads();
+    if (tid == 0) {
+        // one thread moves the tiles and issues the MMAs; stage c % NSTAGE holds chunk c.  The MMAs
+        // of chunk c are queued before the thread waits for those of chunk c - 1, whose stage then
+        // takes chunk c - 1 + NSTAGE, so the tensor cores always have the next chunk queued.
+        auto issue = [&](int c) {
+            issue_tiles(full_a(c % NSTAGE), smem_addr(opA(c % NSTAGE)), s16 + ((size_t)mt * KCH + c) * FR_TC_TILE,
+                        planes + ((size_t)nt * KCH + c) * FR_TC_TILE, planes + ((size_t)(NT + nt) * KCH + c) * FR_TC_TILE);
+        };
+        int issued = 0, landed = 0, committed = -1;  // copies issued / waited for: chunks [0, issued) / [0, landed)
+        bool ok = true;
+        for (; issued < NSTAGE && issued < KCH; issued++) issue(issued);
+        for (int c = 0; c < KCH; c++) {
+            const int st = c % NSTAGE;
+            if (!mbar_wait(full_a(st), (uint32_t)((c / NSTAGE) & 1))) {
+                ok = false;
                 break;
             }
-            if (tid == 0 && !s_abort) {
-                issue_planes(full_a(ns), smem_addr(opA(ns) + OP_BYTES), smem_addr(opA(ns) + 2 * OP_BYTES),
-                             plane_src(0, c + 1), plane_src(1, c + 1));
-                (ns ? pend1 : pend0) = c + 1;
+            landed = c + 1;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int steps = min(TC_KC, N - c * TC_KC) / 16;
+            const uint32_t a = smem_addr(opA(st)), lo = a + OP_BYTES, hi = a + 2 * OP_BYTES;
+            for (int ks = 0; ks < steps; ks++) {
+                const uint32_t off = ks * 2 * LBO;  // K = 16: two core matrices
+                const uint32_t acc = (c > 0 || ks > 0) ? 1u : 0u;
+                mma_f16(d_lo, sdesc(a + off), sdesc(lo + off), acc);
+                mma_f16(d_hi, sdesc(a + off), sdesc(hi + off), acc);
             }
-            store_s(ns);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mdone_a(st))
+                         : "memory");
+            committed = c;
+            if (c >= 1 && issued < KCH) {  // refill the stage of chunk c - 1 once its MMAs are done
+                const int p = c - 1;
+                if (!mbar_wait(mdone_a(p % NSTAGE), (uint32_t)((p / NSTAGE) & 1))) {
+                    ok = false;
+                    break;
+                }
+                issue(issued++);
+            }
+        }
+        if (ok) {  // the last commit covers every MMA issued before it
+            ok = mbar_wait(mdone_a((KCH - 1) % NSTAGE), (uint32_t)(((KCH - 1) / NSTAGE) & 1));
+        } else {
+            // leave nothing in flight: wait (bounded) for the copies not yet consumed and the
+            // last committed MMAs
+            for (int c = landed; c < issued; c++) mbar_wait(full_a(c % NSTAGE), (uint32_t)((c / NSTAGE) & 1));
+            if (committed >= 0) mbar_wait(mdone_a(committed % NSTAGE), (uint32_t)((committed / NSTAGE) & 1));
+        }
+        if (!ok) {
+            atomicOr(error, 1u);
+            s_abort = 1;
         }
     }
     __syncthreads();
-    bool ok = !s_abort;
-    if (ok) {  // the last commit covers every MMA issued before it
-        const int c = KCH - 1;
-        ok = mbar_wait(mdone_a(c & 1), (uint32_t)((c >> 1) & 1));
-        if (!ok) atomicOr(error, 1u);
-    } else if (tid == 0) {
-        // leave nothing in flight: wait (bounded) for pending copies and the last committed MMAs
-        if (pend0 >= 0) mbar_wait(full_a(0), (uint32_t)((pend0 >> 1) & 1));
-        if (pend1 >= 0) mbar_wait(full_a(1), (uint32_t)((pend1 >> 1) & 1));
-        if (last_commit >= 0) mbar_wait(mdone_a(last_commit & 1), (uint32_t)((last_commit >> 1) & 1));
-    }
-    ok = !__syncthreads_or(!ok);
+    const bool ok = !s_abort;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (ok) {
         // epilogue: warp w holds rows 32w .. 32w + 31 (tensor-memory lanes)
@@ -283,24 +258,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fr_sa_shared_tc(int n, const ui
 }
 
 template <int N>
-int launch(int n, const uint16_t *planes, uint8_t *scratch, unsigned *error, cudaStream_t st) {
+int launch(int n, const uint16_t *planes, uint16_t *s16, uint8_t *scratch, unsigned *error, cudaStream_t st) {
     if (!capturing() &&
         cudaFuncSetAttribute(fr_sa_shared_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) != cudaSuccess) {
         cudaGetLastError();
         return PQCGPU_ECUDA;
     }
-    const dim3 grid((8 * n + TC_M - 1) / TC_M, (N + TC_N - 1) / TC_N);
-    PQC_LAUNCH(st, "fr_sa_shared_tc", N, 0, fr_sa_shared_tc<N><<<grid, TC_THREADS, TC_SMEM, st>>>(n, planes, scratch, error));
+    const int mtiles = (8 * n + TC_M - 1) / TC_M;
+    PQC_LAUNCH(st, "fr_s16_tiles", N, 0,
+               fr_s16_tiles<N><<<mtiles * fr_tc_kchunks(N), 128, 0, st>>>(n, scratch, s16));
+    const dim3 grid(mtiles, (N + TC_N - 1) / TC_N);
+    PQC_LAUNCH(st, "fr_sa_shared_tc", N, 0, fr_sa_shared_tc<N><<<grid, TC_THREADS, TC_SMEM, st>>>(n, planes, s16, scratch, error));
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
 }  // namespace frodo_tc
 
 // error: a device word the caller zeroed; set when a wait in the kernel runs out
-int frodo_shared_tc_launch(int N, int n, const uint16_t *planes, uint8_t *scratch, unsigned *error, cudaStream_t st) {
-    if (N == 640) return frodo_tc::launch<640>(n, planes, scratch, error, st);
-    if (N == 976) return frodo_tc::launch<976>(n, planes, scratch, error, st);
-    if (N == 1344) return frodo_tc::launch<1344>(n, planes, scratch, error, st);
+int frodo_shared_tc_launch(int N, int n, const uint16_t *planes, uint16_t *s16, uint8_t *scratch, unsigned *error,
+                           cudaStream_t st) {
+    if (N == 640) return frodo_tc::launch<640>(n, planes, s16, scratch, error, st);
+    if (N == 976) return frodo_tc::launch<976>(n, planes, s16, scratch, error, st);
+    if (N == 1344) return frodo_tc::launch<1344>(n, planes, s16, scratch, error, st);
     return PQCGPU_EINVAL;
 }
 

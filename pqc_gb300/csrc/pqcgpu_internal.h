@@ -166,11 +166,13 @@ int frodo_set_shared_product(int product);
 int frodo_get_shared_product();
 size_t frodo_shared_extra_bytes(int N);
 // error: a device word that the tensor-core product sets (never clears) when one of its waits runs out
+// s16: fr_tc_s_bytes(N, n) bytes of device memory for the tensor-core product's S' tiles
 int frodo_enc_shared_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *mu, uint8_t *scratch,
-                         uint8_t *extra, unsigned *error, cudaStream_t st);
+                         uint8_t *extra, uint16_t *s16, unsigned *error, cudaStream_t st);
 // The tensor-core product G[x] = S'[x] A (frodo_tc.cu): planes = the split A from fr_gen_a, tiled as
 // below; error = a zeroed device word, set if a wait in the kernel runs out.
-int frodo_shared_tc_launch(int N, int n, const uint16_t *planes, uint8_t *scratch, unsigned *error, cudaStream_t st);
+int frodo_shared_tc_launch(int N, int n, const uint16_t *planes, uint16_t *s16, uint8_t *scratch, unsigned *error,
+                           cudaStream_t st);
 // A's two fp16 planes (A & 1023, A >> 10) as the product kernel reads them: one 16 KB tile per
 // (plane, 128 output columns, 64 k), each tile already in the no-swizzle K-major core-matrix layout
 // of a tcgen05 operand (8 columns x 8 k = 16-byte rows of one core matrix; core matrices 128 bytes
@@ -186,6 +188,17 @@ __host__ __device__ constexpr size_t fr_tc_planes_elems(int N) {
 __host__ __device__ constexpr size_t fr_tc_plane_index(int N, int p, int j, int k) {
     return ((size_t)(p * fr_tc_ntiles(N) + j / FR_TC_N) * fr_tc_kchunks(N) + k / FR_TC_KC) * FR_TC_TILE +
            ((j % FR_TC_N) >> 3) * 512 + ((k % FR_TC_KC) >> 3) * 64 + (j & 7) * 8 + (k & 7);
+}
+// The stacked S' (8 rows per instance) as fp16 in the same tiled layout: one 16 KB tile per (16
+// instances, 64 k), converted from the instances' u16 copies by fr_s16_tiles (frodo_tc.cu); entries
+// beyond n or N are zero.
+__host__ __device__ constexpr size_t fr_tc_s_bytes(int N, int n) {
+    return (size_t)((n + 15) / 16) * fr_tc_kchunks(N) * FR_TC_TILE * 2;
+}
+// u16 index of S'[i][k] of instance x
+__host__ __device__ constexpr size_t fr_tc_s_index(int N, int x, int i, int k) {
+    return ((size_t)(x / 16) * fr_tc_kchunks(N) + k / FR_TC_KC) * FR_TC_TILE + (x % 16) * 512 +
+           ((k % FR_TC_KC) >> 3) * 64 + i * 8 + (k & 7);
 }
 
 }  // namespace pqc
