@@ -236,6 +236,7 @@ struct pqcgpu_ctx {
     cudaEvent_t in_ev[NSLOT] = {}, done_ev[NSLOT] = {}, free_ev[NSLOT] = {};
     cudaEvent_t fork_ev = nullptr, join_ev[NPAR] = {};
     cudaEvent_t stage_ev[NPAR] = {}, stage_ev2[NPAR] = {}, core_ev = nullptr;  // mixed Kyber waves and their hashes
+    cudaEvent_t fr_ev[NPAR] = {}, fr_core_ev = nullptr;                        // the FrodoKEM wave and its sponges
     bool own_stream = true;
     size_t budget = 0;
     uint8_t *arena = nullptr;
@@ -337,7 +338,8 @@ extern "C" int pqcgpu_ctx_create(pqcgpu_ctx **out, int device, size_t budget) {
         if ((rc = cuda_err(cudaStreamCreateWithFlags(&c->par[i], cudaStreamNonBlocking), "stream")) ||
             (rc = cuda_err(cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming), "event")) ||
             (rc = cuda_err(cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming), "event")) ||
-            (rc = cuda_err(cudaEventCreateWithFlags(&c->stage_ev2[i], cudaEventDisableTiming), "event"))) {
+            (rc = cuda_err(cudaEventCreateWithFlags(&c->stage_ev2[i], cudaEventDisableTiming), "event")) ||
+            (rc = cuda_err(cudaEventCreateWithFlags(&c->fr_ev[i], cudaEventDisableTiming), "event"))) {
             pqcgpu_ctx_destroy(c);
             return rc;
         }
@@ -363,7 +365,8 @@ extern "C" int pqcgpu_ctx_create(pqcgpu_ctx **out, int device, size_t budget) {
         }
     }
     if ((rc = cuda_err(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming), "event")) ||
-        (rc = cuda_err(cudaEventCreateWithFlags(&c->core_ev, cudaEventDisableTiming), "event"))) {
+        (rc = cuda_err(cudaEventCreateWithFlags(&c->core_ev, cudaEventDisableTiming), "event")) ||
+        (rc = cuda_err(cudaEventCreateWithFlags(&c->fr_core_ev, cudaEventDisableTiming), "event"))) {
         pqcgpu_ctx_destroy(c);
         return rc;
     }
@@ -393,9 +396,11 @@ extern "C" int pqcgpu_ctx_destroy(pqcgpu_ctx *c) {
         if (c->join_ev[i]) cudaEventDestroy(c->join_ev[i]);
         if (c->stage_ev[i]) cudaEventDestroy(c->stage_ev[i]);
         if (c->stage_ev2[i]) cudaEventDestroy(c->stage_ev2[i]);
+        if (c->fr_ev[i]) cudaEventDestroy(c->fr_ev[i]);
     }
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->core_ev) cudaEventDestroy(c->core_ev);
+    if (c->fr_core_ev) cudaEventDestroy(c->fr_core_ev);
     delete c;
     return PQCGPU_OK;
 }
@@ -807,12 +812,15 @@ static int launch_jobs(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, uint
         if ((rc = cuda_err(cudaStreamWaitEvent(c->par[i], c->fork_ev, 0), "wait event"))) return rc;
     // With stage_kernels, the Kyber key generations, encapsulations and decapsulations of round-3
     // arithmetic (all k, FO or ML-KEM) run their core stages as two persistent waves for all of them
-    // (kyber_mixed.cu) on par[0]; their per-job hash kernels spread over the first HS parallel
-    // streams around the waves, and the other jobs round-robin over the remaining streams.
+    // (kyber_mixed.cu) on par[0], followed there by the NewHope jobs' wave; their per-job hash
+    // kernels spread over the first HS parallel streams around the waves.  The FrodoKEM jobs' serial
+    // sponges run per job on the remaining streams before and after the FrodoKEM waves (frodo.cu),
+    // which run on the last stream; the other jobs round-robin over the remaining streams.
     // Otherwise every job's own kernels round-robin over all streams.
     constexpr int HS = pqcgpu_ctx::NPAR / 2;
     std::vector<MixedKyberJob> mix[3];
     std::vector<NhMixedJob> nhmix;
+    std::vector<FrMixedJob> frmix;
     std::vector<size_t> rest;
     for (size_t i = 0; i < njobs; i++) {
         const pqcgpu_job &j = jobs[i];
@@ -823,10 +831,15 @@ static int launch_jobs(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, uint
         else if (!plain && stage_kernels && (j.alg == PQCGPU_NEWHOPE1024 || j.alg == PQCGPU_NEWHOPE512) && j.n > 0)
             nhmix.push_back(NhMixedJob{j.alg == PQCGPU_NEWHOPE1024 ? 1024 : 512, j.op, (int)j.n, j.in0, j.in1, j.out0,
                                        j.out1, scratch + offs[i]});
-        else
+        else if (!plain && stage_kernels && frodo_n(j.alg) && j.n > 0) {
+            AlgInfo ai;
+            alg_info(j.alg, &ai);
+            frmix.push_back(FrMixedJob{frodo_n(j.alg), j.op, (int)j.n, (int)ai.kpc, j.in0, j.in1, j.out0, j.out1,
+                                       scratch + offs[i]});
+        } else
             rest.push_back(i);
     }
-    const bool mixed = mix[0].size() + mix[1].size() + mix[2].size() + nhmix.size() >= 2;
+    const bool mixed = mix[0].size() + mix[1].size() + mix[2].size() + nhmix.size() + frmix.size() >= 2;
     if (!mixed) {
         rest.clear();
         for (size_t i = 0; i < njobs; i++) rest.push_back(i);
@@ -837,6 +850,28 @@ static int launch_jobs(pqcgpu_ctx *c, const pqcgpu_job *jobs, size_t njobs, uint
         rc = op_dev(j.alg, j.op, (int)j.n, j.in0, j.in1, j.out0, j.out1, scratch + offs[rest[q]], plain,
                     c->par[first + (int)(q % (size_t)nrest)]);
         if (rc) return set_err(rc, "job launch failed");
+    }
+    if (mixed && !frmix.empty()) {
+        // FrodoKEM: per-job sponges on par[HS ..), the waves on par[NPAR - 1] once all of them are
+        // done, the per-job sponges after the waves once those are
+        unsigned *fr_counters =
+            reinterpret_cast<unsigned *>(scratch + offs[njobs]) + MIXED_COUNTER_WORDS + MIXED_NH_COUNTER_WORDS;
+        constexpr int FL = pqcgpu_ctx::NPAR - 1;
+        int q = 0;
+        for (const auto &j : frmix)
+            if ((rc = frodo_mixed_pre(j, c->par[HS + q++ % (pqcgpu_ctx::NPAR - HS)]))) return set_err(rc, "job launch failed");
+        for (int i = HS; i < FL; i++)
+            if ((rc = cuda_err(cudaEventRecord(c->fr_ev[i], c->par[i]), "event record")) ||
+                (rc = cuda_err(cudaStreamWaitEvent(c->par[FL], c->fr_ev[i], 0), "wait event")))
+                return rc;
+        if ((rc = frodo_mixed_wave(frmix, fr_counters, MIXED_FR_COUNTER_WORDS, c->par[FL])))
+            return set_err(rc, "mixed FrodoKEM launch failed");
+        if ((rc = cuda_err(cudaEventRecord(c->fr_core_ev, c->par[FL]), "event record"))) return rc;
+        for (int i = HS; i < FL; i++)
+            if ((rc = cuda_err(cudaStreamWaitEvent(c->par[i], c->fr_core_ev, 0), "wait event"))) return rc;
+        q = 0;
+        for (const auto &j : frmix)
+            if ((rc = frodo_mixed_post(j, c->par[HS + q++ % (pqcgpu_ctx::NPAR - HS)]))) return set_err(rc, "job launch failed");
     }
     if (mixed) {
         unsigned *counters = reinterpret_cast<unsigned *>(scratch + offs[njobs]);

@@ -22,6 +22,9 @@
 // the noise stream, and their CDF tables.  Every value is computed mod 2^16 and reduced mod q when
 // packed, compared or decoded.
 #include <cuda_fp16.h>
+
+#include <algorithm>
+#include <vector>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -362,15 +365,13 @@ __global__ void __launch_bounds__(128) fr_kp_post(int n, const uint8_t *coins, i
 // ---------------------------------------------------------------------------------------------
 // B = A S + E, one thread per row of A; CTA = (instance, group of rows); St in shared memory.
 template <int N>
-__global__ void __launch_bounds__(256) fr_kp_core(int n, uint8_t *pk, const uint8_t *scratch) {
+__device__ __forceinline__ void fr_kp_core_body(uint8_t *pk, const uint8_t *scratch, int x, int rb, uint16_t *St) {
     using P = FP<N>;
-    __shared__ __align__(16) uint16_t St[N * NB];
-    const int x = blockIdx.y;
     const uint16_t *gSt = reinterpret_cast<const uint16_t *>(scratch + (size_t)x * P::SCRATCH), *E = gSt + N * NB;
     for (int i = threadIdx.x; i < N * NB / 8; i += blockDim.x)
         reinterpret_cast<uint4 *>(St)[i] = reinterpret_cast<const uint4 *>(gSt)[i];
     __syncthreads();
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = rb * blockDim.x + threadIdx.x;
     if (row >= N) return;
     uint8_t *p = pk + (size_t)x * P::PKB;
     uint2 A[25];
@@ -404,6 +405,11 @@ __global__ void __launch_bounds__(256) fr_kp_core(int n, uint8_t *pk, const uint
     }
     // pack B row (8 values, LOGQ bits each, MSB first) at pk[16 + LOGQ row]
     pack8<P::LOGQ>(p + SEEDA + P::LOGQ * row, acc);
+}
+template <int N>
+__global__ void __launch_bounds__(256) fr_kp_core(int n, uint8_t *pk, const uint8_t *scratch) {
+    __shared__ __align__(16) uint16_t St[N * NB];
+    fr_kp_core_body<N>(pk, scratch, blockIdx.y, blockIdx.x, St);
 }
 
 // Epilogue of B' = S' A + E': V = S' B + E'' (B = unpack(pk_b), N x 8; 64 outputs, k split over
@@ -506,15 +512,14 @@ constexpr int SA_THREADS = 256;
 constexpr int STAGE_PITCH = 86;  // u16 per staged row block (84 used; odd word pitch)
 constexpr int BLK_COLS = 84;     // u16 values per SHAKE128 block
 template <int N>
-__global__ void __launch_bounds__(SA_THREADS) fr_sa_core(int n, uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *pk,
-                                                         int pk_stride, uint8_t *scratch) {
+__device__ __forceinline__ void fr_sa_core_body(uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *pk, int pk_stride,
+                                                uint8_t *scratch, int x, int part, int parts, uint8_t *smem) {
     using P = FP<N>;
-    extern __shared__ __align__(16) uint8_t smem[];
     uint16_t *Spt = reinterpret_cast<uint16_t *>(smem);                       // N x 8
     uint32_t *acc = reinterpret_cast<uint32_t *>(smem + N * NB * 2);          // 8 x N (+64 for V)
     uint16_t *stage = reinterpret_cast<uint16_t *>(smem + N * NB * 2 + (NB * N + 64) * 4);  // threads x 86
-    const int x = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x, parts = gridDim.y;
-    const int rows_per = (N + parts - 1) / parts, rbeg = blockIdx.y * rows_per, rend = min(N, rbeg + rows_per);
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int rows_per = (N + parts - 1) / parts, rbeg = part * rows_per, rend = min(N, rbeg + rows_per);
     uint8_t *scr = scratch + (size_t)x * P::SCRATCH;
     const uint16_t *gSpt = reinterpret_cast<const uint16_t *>(scr), *Ep = gSpt + N * NB, *Epp = Ep + N * NB;
     const uint8_t *p = pk + (size_t)x * pk_stride;
@@ -567,6 +572,12 @@ __global__ void __launch_bounds__(SA_THREADS) fr_sa_core(int n, uint8_t *ct, con
         return;
     }
     sa_epilogue<N>(acc, Spt, p, scr, ct, ct_cmp, x);
+}
+template <int N>
+__global__ void __launch_bounds__(SA_THREADS) fr_sa_core(int n, uint8_t *ct, const uint8_t *ct_cmp, const uint8_t *pk,
+                                                         int pk_stride, uint8_t *scratch) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    fr_sa_core_body<N>(ct, ct_cmp, pk, pk_stride, scratch, blockIdx.x, blockIdx.y, gridDim.y, smem);
 }
 
 // Finish a split product: acc = (sum of the parts) + E', then the same epilogue.  CTA per instance.
@@ -689,6 +700,82 @@ static size_t sa_smem(int N, int threads) {
 }
 static size_t sa_final_smem(int N) { return (size_t)N * NB * 2 + ((size_t)NB * N + 64) * 4; }
 
+// ---- persistent wave for the FrodoKEM jobs of a mixed batch ----
+// One launch holds the products of every FrodoKEM job (n = 640, 976 and 1344): key generation's
+// B = AS + E in tiles of 256 rows of one instance, and the B' = S'A + E' of encapsulation and
+// decapsulation in tiles of one instance or one part of it (the job's row split, as in its own
+// launch).  SMs x 2 CTAs of 256 threads take tiles from a global counter, products first.
+constexpr int FRW_THREADS = 256, FRW_MAX_JOBS = 32;
+struct FrWaveJob {
+    int kind;                // 0 key generation rows, 1 B' = S'A + E'
+    int N, first, per;       // first tile; tiles per instance (row blocks or parts)
+    uint8_t *pk;             // kind 0: the public keys being formed
+    uint8_t *ct;             // kind 1: ciphertexts out (encapsulation) or nullptr
+    const uint8_t *cmp;      // kind 1: received ciphertexts (decapsulation) or nullptr
+    const uint8_t *pkp;      // kind 1: public keys (stride pk_stride)
+    int pk_stride;
+    uint8_t *scratch;
+};
+struct FrWaveTable {
+    int njobs, tiles;
+    FrWaveJob j[FRW_MAX_JOBS];
+};
+
+// counter: a zeroed word of device memory for this launch.  One kernel per stage (KIND 0: key
+// generation rows; KIND 1: B' = S'A + E' of encapsulations and decapsulations) and parameter set:
+// with several bodies in one kernel they spilled at the 128 registers that two CTAs per SM allow.
+template <int KIND, int N>
+__global__ void __launch_bounds__(FRW_THREADS, 2) fr_stage_persistent(const __grid_constant__ FrWaveTable t,
+                                                                     unsigned *counter) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ int s_tile;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int tile = s_tile;
+        if (tile >= t.tiles) break;
+        int lo = 0, hi = t.njobs - 1;  // the job whose tiles start at or before `tile`
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (t.j[mid].first <= tile) lo = mid;
+            else hi = mid - 1;
+        }
+        const int per = t.j[lo].per, local = tile - t.j[lo].first, x = local / per, sub = local % per;
+        if constexpr (KIND == 0)
+            fr_kp_core_body<N>(t.j[lo].pk, t.j[lo].scratch, x, sub, reinterpret_cast<uint16_t *>(smem));
+        else
+            fr_sa_core_body<N>(t.j[lo].ct, t.j[lo].cmp, t.j[lo].pkp, t.j[lo].pk_stride, t.j[lo].scratch, x, sub, per,
+                               smem);
+        __syncthreads();  // the next tile reuses shared memory (and s_tile)
+    }
+}
+
+// A wave's dynamic shared memory.
+static size_t frw_smem(int kind, int N) { return kind == 0 ? (size_t)N * NB * 2 : sa_smem(N, FRW_THREADS); }
+template <int KIND, int N>
+static cudaError_t frw_attr() {
+    return cudaFuncSetAttribute(fr_stage_persistent<KIND, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)frw_smem(KIND, N));
+}
+// One persistent launch of stage KIND of parameter set N over the table's jobs.
+template <int KIND, int N>
+static int frw_launch(const FrWaveTable &t, unsigned *counter, cudaStream_t st) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fr_stage_persistent<KIND, N>, FRW_THREADS,
+                                                      frw_smem(KIND, N)) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    if (cudaMemsetAsync(counter, 0, sizeof(unsigned), st) != cudaSuccess) return PQCGPU_ECUDA;
+    const int grid = std::min(t.tiles, sms * per_sm);
+    PQC_LAUNCH(st, "fr_stage_persistent", N, KIND,
+               fr_stage_persistent<KIND, N><<<grid, FRW_THREADS, frw_smem(KIND, N), st>>>(t, counter));
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
 }  // namespace frodo
 
 using namespace frodo;
@@ -704,6 +791,11 @@ int frodo_init_constants() {
     if (cudaMemcpyToSymbol(c_cdf640, cdf640, sizeof cdf640) != cudaSuccess) return PQCGPU_ECUDA;
     if (cudaMemcpyToSymbol(c_cdf976, cdf976, sizeof cdf976) != cudaSuccess) return PQCGPU_ECUDA;
     if (cudaMemcpyToSymbol(c_cdf1344, cdf1344, sizeof cdf1344) != cudaSuccess) return PQCGPU_ECUDA;
+    // the FrodoKEM wave's shared-memory bound, once, so that no launch (captured or not) depends on
+    // an earlier one having set it
+    if (frw_attr<0, 640>() || frw_attr<0, 976>() || frw_attr<0, 1344>() || frw_attr<1, 640>() || frw_attr<1, 976>() ||
+        frw_attr<1, 1344>())
+        return PQCGPU_ECUDA;
     return PQCGPU_OK;
 }
 size_t frodo_scratch_bytes(int N) {
@@ -914,6 +1006,127 @@ int frodo_dec_dev(int N, int n, uint8_t *ss, const uint8_t *ct, const uint8_t *s
     if (N == 976) return dec_n<976>(n, ss, ct, sk, scratch, st);
     if (N == 1344) return dec_n<1344>(n, ss, ct, sk, scratch, st);
     return PQCGPU_EINVAL;
+}
+
+// ---- the FrodoKEM jobs of a mixed batch (persistent wave: fr_stage_persistent) ----
+namespace {
+template <int N>
+int mixed_pre_n(const FrMixedJob &j, cudaStream_t st) {
+    using P = FP<N>;
+    const int n = j.n;
+    int parts, thr;
+    if (j.op == 0) {
+        PQC_LAUNCH(st, "fr_kp_pre", N, 0, fr_kp_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, j.in0, j.kpc, j.out0, j.scratch));
+    } else if (j.op == 1) {
+        fr_shape(1, n, &parts, &thr);
+        PQC_LAUNCH(st, "fr_enc_pre", N, 0,
+                   fr_enc_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, j.in0, j.in1, j.scratch, parts, nullptr, P::SSB));
+    } else {
+        fr_shape(2, n, &parts, &thr);
+        PQC_LAUNCH(st, "fr_dec_w", N, 0, fr_dec_w<N><<<n, 256, 0, st>>>(n, j.in0, j.in1, j.scratch));
+        PQC_LAUNCH(st, "fr_dec_pre", N, 0, fr_dec_pre<N><<<(n + 3) / 4, 128, 0, st>>>(n, j.in1, j.scratch, parts));
+    }
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
+template <int N>
+int mixed_post_n(const FrMixedJob &j, cudaStream_t st) {
+    using P = FP<N>;
+    const int n = j.n;
+    int parts, thr;
+    if (j.op == 0) {
+        PQC_LAUNCH(st, "fr_kp_post", N, 0,
+                   fr_kp_post<N><<<(n + 3) / 4, 128, 0, st>>>(n, j.in0, j.kpc, j.out0, j.scratch, j.out1));
+        return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+    }
+    if (sa_attrs<N>()) return PQCGPU_ECUDA;
+    fr_shape(j.op, n, &parts, &thr);
+    const bool enc = j.op == 1;
+    uint8_t *ct = enc ? j.out0 : nullptr;
+    const uint8_t *cmp = enc ? nullptr : j.in0, *pkp = enc ? j.in0 : j.in1 + P::SSB;
+    const int pk_stride = enc ? P::PKB : P::SKB;
+    if (parts > 1)
+        PQC_LAUNCH(st, "fr_sa_final", N, 0,
+                   fr_sa_final<N><<<n, SA_THREADS, sa_final_smem(N), st>>>(n, ct, cmp, pkp, pk_stride, j.scratch));
+    if (enc)
+        PQC_LAUNCH(st, "fr_post", N, 0, fr_post<N><<<(n + 3) / 4, 128, 0, st>>>(n, j.out0, j.scratch, nullptr, j.out1));
+    else
+        PQC_LAUNCH(st, "fr_post", N, 0, fr_post<N><<<(n + 3) / 4, 128, 0, st>>>(n, j.in0, j.scratch, j.in1, j.out0));
+    return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+}
+
+}  // namespace
+
+int frodo_mixed_pre(const FrMixedJob &j, cudaStream_t st) {
+    if (j.n <= 0) return PQCGPU_OK;
+    if (j.N == 640) return mixed_pre_n<640>(j, st);
+    if (j.N == 976) return mixed_pre_n<976>(j, st);
+    if (j.N == 1344) return mixed_pre_n<1344>(j, st);
+    return PQCGPU_EINVAL;
+}
+int frodo_mixed_post(const FrMixedJob &j, cudaStream_t st) {
+    if (j.n <= 0) return PQCGPU_OK;
+    if (j.N == 640) return mixed_post_n<640>(j, st);
+    if (j.N == 976) return mixed_post_n<976>(j, st);
+    if (j.N == 1344) return mixed_post_n<1344>(j, st);
+    return PQCGPU_EINVAL;
+}
+
+// The persistent launches of the FrodoKEM jobs: per stage (products first) and parameter set, one
+// launch per FRW_MAX_JOBS jobs; counters: ncounters zeroable words, one per launch.
+int frodo_mixed_wave(const std::vector<FrMixedJob> &jobs, unsigned *counters, int ncounters, cudaStream_t st) {
+    std::vector<FrWaveJob> items;
+    for (const FrMixedJob &j : jobs) {
+        if (j.n <= 0) continue;
+        FrWaveJob m{};
+        m.N = j.N;
+        m.scratch = j.scratch;
+        if (j.op == 0) {
+            m.kind = 0;
+            m.per = (j.N + FRW_THREADS - 1) / FRW_THREADS;
+            m.pk = j.out0;
+        } else {
+            int parts, thr;
+            fr_shape(j.op, j.n, &parts, &thr);
+            m.kind = 1;
+            m.per = parts;
+            const bool enc = j.op == 1;
+            const int pkb = (int)(j.N == 640 ? FP<640>::PKB : j.N == 976 ? FP<976>::PKB : FP<1344>::PKB);
+            const int ssb = (int)(j.N == 640 ? FP<640>::SSB : j.N == 976 ? FP<976>::SSB : FP<1344>::SSB);
+            const int skb = (int)(j.N == 640 ? FP<640>::SKB : j.N == 976 ? FP<976>::SKB : FP<1344>::SKB);
+            m.ct = enc ? j.out0 : nullptr;
+            m.cmp = enc ? nullptr : j.in0;
+            m.pkp = enc ? j.in0 : j.in1 + ssb;
+            m.pk_stride = enc ? pkb : skb;
+        }
+        m.first = j.n;  // instances, for the ordering below; replaced by the first tile
+        items.push_back(m);
+    }
+    int w = 0;
+    for (int kind = 1; kind >= 0; kind--)  // the products first; one launch per (stage, N, FRW_MAX_JOBS jobs)
+        for (int N : {1344, 976, 640}) {
+            std::vector<FrWaveJob> ks;
+            for (const FrWaveJob &m : items)
+                if (m.kind == kind && m.N == N) ks.push_back(m);
+            for (size_t from = 0; from < ks.size(); from += FRW_MAX_JOBS, w++) {
+                if (w >= ncounters) return PQCGPU_EINVAL;
+                FrWaveTable t{};
+                t.njobs = (int)std::min(ks.size() - from, (size_t)FRW_MAX_JOBS);
+                for (int i = 0; i < t.njobs; i++) {
+                    t.j[i] = ks[from + i];
+                    const int n = t.j[i].first;
+                    t.j[i].first = t.tiles;
+                    t.tiles += n * t.j[i].per;
+                }
+                int rc;
+                if (kind) rc = N == 640 ? frw_launch<1, 640>(t, counters + w, st)
+                               : N == 976 ? frw_launch<1, 976>(t, counters + w, st) : frw_launch<1, 1344>(t, counters + w, st);
+                else rc = N == 640 ? frw_launch<0, 640>(t, counters + w, st)
+                          : N == 976 ? frw_launch<0, 976>(t, counters + w, st) : frw_launch<0, 1344>(t, counters + w, st);
+                if (rc) return rc;
+            }
+        }
+    return PQCGPU_OK;
 }
 
 }  // namespace pqc

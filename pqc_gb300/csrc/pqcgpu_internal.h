@@ -149,6 +149,19 @@ int newhope_mixed_wave(const std::vector<NhMixedJob> &jobs, unsigned *counters, 
 
 // ---- FrodoKEM-640 / 976 / 1344 (frodo.cu); N = 640, 976 or 1344 ----
 int frodo_init_constants();
+// The FrodoKEM jobs of a mixed batch with PQCGPU_STAGE_KERNELS: each job's serial sponges run as
+// its own kernels before (frodo_mixed_pre) and after (frodo_mixed_post) one persistent wave that
+// holds the products of every job (frodo_mixed_wave: key generation rows of B = AS + E, and
+// B' = S'A + E' of encapsulation and decapsulation).  kpc: keypair coins per instance.
+struct FrMixedJob {
+    int N, op, n, kpc;
+    const uint8_t *in0, *in1;
+    uint8_t *out0, *out1, *scratch;
+};
+constexpr int MIXED_FR_COUNTER_WORDS = 16;  // zeroable device words of the FrodoKEM waves (after the NewHope words)
+int frodo_mixed_pre(const FrMixedJob &j, cudaStream_t st);
+int frodo_mixed_wave(const std::vector<FrMixedJob> &jobs, unsigned *counters, int ncounters, cudaStream_t st);
+int frodo_mixed_post(const FrMixedJob &j, cudaStream_t st);
 size_t frodo_scratch_bytes(int N);  // per instance, all three operations
 int frodo_keypair_dev(int N, int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int cstride, uint8_t *scratch,
                       cudaStream_t st);

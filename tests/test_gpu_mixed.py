@@ -62,8 +62,8 @@ def check(jobs, expected):
 @pytest.mark.parametrize("stage_kernels", [False, True])
 def test_mixed_batch_all_algorithms(env, stage_kernels):
     """Every algorithm and operation in one mixed batch: each job's own kernels over the streams, or
-    (STAGE_KERNELS) the persistent waves for the Kyber and NewHope jobs with the FrodoKEM jobs on
-    the streams; every output equal to the single-algorithm calls'."""
+    (STAGE_KERNELS) the persistent waves of the Kyber, NewHope and FrodoKEM jobs; every output equal
+    to the single-algorithm calls'."""
     from pqc_gb300 import kem
     ctx, torch, dev = env
     rng = random.Random(5)
@@ -77,6 +77,21 @@ def test_mixed_batch_all_algorithms(env, stage_kernels):
     jobs, expected = build_jobs(ctx, torch, dev, spec, 3000)
     torch.cuda.synchronize()
     ctx.mixed_dev(jobs, kem.STAGE_KERNELS if stage_kernels else 0)
+    ctx.wait()
+    check(jobs, expected)
+
+
+def test_mixed_frodo_waves_every_split(env):
+    """FrodoKEM jobs of all three parameter sets in the persistent waves (STAGE_KERNELS) at batch
+    sizes that take each row split of B' = S'A + E' (1, 2, 4 and 8 tiles an instance) and the
+    key generation's row tiles; outputs equal to the single-algorithm calls'."""
+    from pqc_gb300 import kem
+    ctx, torch, dev = env
+    spec = [("frodo640", "enc", 320), ("frodo976", "dec", 160), ("frodo1344", "enc", 80), ("frodo640", "dec", 9),
+            ("frodo976", "keypair", 40), ("frodo1344", "keypair", 5), ("frodo976", "enc", 17), ("frodo1344", "dec", 2)]
+    jobs, expected = build_jobs(ctx, torch, dev, spec, 4600)
+    torch.cuda.synchronize()
+    ctx.mixed_dev(jobs, kem.STAGE_KERNELS)
     ctx.wait()
     check(jobs, expected)
 
