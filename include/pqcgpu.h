@@ -69,7 +69,7 @@ typedef enum {
 #define PQCGPU_DEVICE_PTRS 0x1u /* all buffer arguments are device pointers; asynchronous */
 #define PQCGPU_PLAIN 0x2u       /* use the plain per-stage path (one kernel per stage, thread per
                                    instance, intermediates in HBM) instead of the fused path */
-#define PQCGPU_STAGE_KERNELS 0x4u /* mixed batches: persistent per-stage kernels for all Kyber and
+#define PQCGPU_STAGE_KERNELS 0x4u /* mixed batches: persistent per-stage kernels for all Kyber, FrodoKEM and
                                      NewHope jobs instead of every job's own kernels on the
                                      concurrent streams */
 
@@ -173,10 +173,11 @@ int pqcgpu_newhope512_cpapke_dec_batch(pqcgpu_ctx *ctx, size_t n, uint8_t *msg, 
  * device pointers only, PQCGPU_DEVICE_PTRS): every job's kernels run on the context's concurrent
  * streams.  With PQCGPU_STAGE_KERNELS the core stages of the Kyber jobs (round 3 and ML-KEM, all
  * k, every operation) run instead as two persistent waves -- keypair, encapsulation and decryption
- * tiles, then re-encryption tiles -- and those of the NewHope jobs (n = 1024 and 512) as one more:
- * SMs x (CTAs per SM) CTAs take (job, instance group) tiles from an atomic counter, heaviest first
- * (the per-job hash kernels and the other jobs still spread over the streams).  The default is
- * the faster of the two on GB300 (`bench.py --config mixed` reports both).
+ * tiles, then re-encryption tiles -- those of the NewHope jobs (n = 1024 and 512) as one more, and
+ * the products of the FrodoKEM jobs as one wave per stage and parameter set: SMs x (CTAs per SM)
+ * CTAs take (job, instance group) tiles from an atomic counter, heaviest first (the per-job hash
+ * kernels and the other jobs still spread over the streams).  The default is the faster of the
+ * two on GB300 (`bench.py --config mixed` reports both).
  * pqcgpu_graph_capture records such a job list once into a CUDA graph (with its own scratch) and
  * pqcgpu_graph_launch replays it on the context stream: same buffers, no per-kernel launch cost. */
 #define PQCGPU_OP_KEYPAIR 0
