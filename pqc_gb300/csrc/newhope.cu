@@ -660,6 +660,12 @@ __device__ __forceinline__ void nh_dec_body(const DecArgs &d, int NI, int base) 
     }
 }
 
+}  // namespace newhope
+}  // namespace pqc
+#include "newhope_single.cuh"
+namespace pqc {
+namespace newhope {
+
 template <int N>
 __global__ void __launch_bounds__(256) nh_kp_core(KpArgs a, int NI) {
     nh_kp_body<N>(a, NI, blockIdx.x * NI);
@@ -699,6 +705,17 @@ __global__ void __launch_bounds__(128) nh_enc_hash_pre(int n, const uint8_t *coi
 
 // [n index: 0 = 1024, 1 = 512][op] = {instances per CTA, threads}
 static LaunchShape g_shape[2][3] = {{{8, 128}, {4, 64}, {4, 128}}, {{16, 128}, {16, 128}, {4, 64}}};
+// Key generations and KEM encapsulations of at most this many instances run on the single-instance
+// kernels (newhope_single.cuh); larger batches on the batched core kernels.  Measured on GB300
+// (NewHope-1024, single-instance / batched, us): keypair 22.0 / 31.4 and encapsulation 26.5 / 58.2
+// at n = 1; 23.0 / 43.4 and 28.8 / 72.1 at 128; 37.5 / 43.2 and 47.7 / 72.4 at 256 (NewHope-512
+// alike).
+static LaunchShape g_nh_single = {256, 0};
+static int nh_single_max() {
+    int v, t;
+    g_nh_single.get(v, t);
+    return v;
+}
 static int nidx(int N) { return N == 1024 ? 0 : 1; }
 
 template <class Kern>
@@ -759,6 +776,11 @@ int newhope_init_constants() {
 }
 
 int newhope_set_shape(int N, int op, int ni, int threads) {
+    if (op == 3) {  // the largest batch that takes the single-instance kernels (both n); 0 = never
+        if ((N != 1024 && N != 512) || ni < 0 || ni > 4096) return PQCGPU_EINVAL;
+        g_nh_single.set(ni, 0);
+        return PQCGPU_OK;
+    }
     if ((N != 1024 && N != 512) || op < 0 || op > 2 || ni < 1 || ni > 64 || threads < 32 || threads > 256 || threads % 32)
         return PQCGPU_EINVAL;
     if ((size_t)ni * smem_per_instance(N, op) > MAX_SMEM_PER_CTA) return PQCGPU_EINVAL;
@@ -767,6 +789,10 @@ int newhope_set_shape(int N, int op, int ni, int threads) {
 }
 
 int newhope_get_shape(int N, int op, int *ni, int *threads) {
+    if (op == 3 && (N == 1024 || N == 512)) {
+        g_nh_single.get(*ni, *threads);
+        return PQCGPU_OK;
+    }
     if ((N != 1024 && N != 512) || op < 0 || op > 2) return PQCGPU_EINVAL;
     g_shape[nidx(N)][op].get(*ni, *threads);
     return PQCGPU_OK;
@@ -774,6 +800,11 @@ int newhope_get_shape(int N, int op, int *ni, int *threads) {
 
 template <int N>
 static int keypair_n(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st) {
+    if (n <= nh_single_max()) {
+        PQC_LAUNCH(st, "nh_kp_single", N, 0,
+                   nh_kp_single<N><<<n, NHS_THREADS, NhSingleSmem<N>::bytes(), st>>>(seed, seed_stride, pk, sk));
+        return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+    }
     int NI, NT;
     g_shape[nidx(N)][0].get(NI, NT);
     const size_t sm = (size_t)NI * smem_per_instance(N, 0);
@@ -790,6 +821,11 @@ static int enc_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8
     g_shape[nidx(N)][1].get(NI, NT);
     const size_t sm = (size_t)NI * smem_per_instance(N, 1);
     if (prep(nh_enc_core<N>, sm)) return PQCGPU_ECUDA;
+    if (kem && n <= nh_single_max()) {
+        PQC_LAUNCH(st, "nh_enc_single", N, 0,
+                   nh_enc_single<N><<<n, NHS_THREADS, NhSingleSmem<N>::bytes(), st>>>(pk, coins, ct, ss));
+        return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
+    }
     EncArgs a{n, ct, pk, m, coins, 32, 32};
     if (kem) {
         PQC_LAUNCH(st, "nh_enc_hash_pre", N, 0, nh_enc_hash_pre<<<(n + 127) / 128, 128, 0, st>>>(n, coins, scratch, ss));

@@ -85,6 +85,34 @@ def test_kem_matches_oracle(ctx, oracle, n, poly_n):
 
 
 @pytest.mark.parametrize("poly_n", [1024, 512])
+@pytest.mark.parametrize("n", [1, 7, 64])
+def test_single_instance_kernels_equal_batched(ctx, poly_n, n):
+    """Key generations and KEM encapsulations of small batches run on the single-instance kernels
+    (one 512-thread CTA per operation); the bytes equal the batched kernels' (launch-shape op 3 = 0
+    forces those), and decapsulation recovers the key."""
+    import ctypes
+    from pqc_gb300 import _lib, kem
+    lib = _lib.load()
+    alg = ALG[poly_n]
+    a = kem.alg_id(alg)
+    seed = drbg.seed48(700 + n + poly_n)
+    kc = drbg.stream(seed, b"kp", n * 32)
+    ec = drbg.stream(seed, b"enc", n * 32)
+    single, t = ctypes.c_int(), ctypes.c_int()
+    assert lib.pqcgpu_get_launch_shape(a, 3, ctypes.byref(single), ctypes.byref(t)) == 0
+    assert n <= single.value
+    pk, sk = ctx.keypair(alg, n, kc)
+    ct, ss = ctx.enc(alg, n, pk, ec)
+    try:
+        assert lib.pqcgpu_set_launch_shape(a, 3, 0, 0) == 0
+        assert ctx.keypair(alg, n, kc) == (pk, sk)
+        assert ctx.enc(alg, n, pk, ec) == (ct, ss)
+    finally:
+        lib.pqcgpu_set_launch_shape(a, 3, single.value, 0)
+    assert ctx.dec(alg, n, ct, sk) == ss
+
+
+@pytest.mark.parametrize("poly_n", [1024, 512])
 def test_restated_fixture(ctx, poly_n):
     from pqc_gb300 import kem
     alg = ALG[poly_n]
