@@ -255,9 +255,9 @@ int pqcgpu_server_run_poisson(pqcgpu_server *server, const pqcgpu_mix_entry *mix
  * kernels (one CTA per instance, every operation and k; 0 = never; threads ignored).  Kyber: ni
  * 1..128, threads from 32 up to the core kernel's launch bound (keypair 512, encapsulation 256,
  * re-encryption 256, decryption stage 384; shared by the round-2 and round-3 sets of the same k);
- * NewHope: ni 1..64, threads 32..256; op 3: ni = the largest batch whose key generations and KEM
- * encapsulations run on the single-instance kernels (one CTA per instance; 0 = never; both n).  FrodoKEM: keypair ni 0 or 1, threads 64 / 128 / 256 (one
- * row of A per thread); encaps / decaps ni = CTAs per instance sharing the rows of A (1, 2, 4, 8,
+ * NewHope: ni 1..64, threads 32..256; op 3: ni = the largest batch whose key generations and
+ * encapsulations (CPA and KEM) run on the single-instance kernels (one CTA per instance; 0 =
+ * never; both n).  FrodoKEM: keypair ni 0 or 1, threads 64 / 128 / 256 (one row of A per thread); encaps / decaps ni = CTAs per instance sharing the rows of A (1, 2, 4, 8,
  * 16) with threads 128 / 256, or ni = 0 to choose by batch size (the default); op 3: ni = the
  * product of pqcgpu_frodo_enc_shared_key_batch (1 CUDA cores, 2 tensor cores, 0 default).
  * Applies to all contexts of the process; a launch reads the pair atomically. */

@@ -705,8 +705,8 @@ __global__ void __launch_bounds__(128) nh_enc_hash_pre(int n, const uint8_t *coi
 
 // [n index: 0 = 1024, 1 = 512][op] = {instances per CTA, threads}
 static LaunchShape g_shape[2][3] = {{{8, 128}, {4, 64}, {4, 128}}, {{16, 128}, {16, 128}, {4, 64}}};
-// Key generations and KEM encapsulations of at most this many instances run on the single-instance
-// kernels (newhope_single.cuh); larger batches on the batched core kernels.  Measured on GB300
+// Key generations and encapsulations (CPA and KEM) of at most this many instances run on the
+// single-instance kernels (newhope_single.cuh); larger batches on the batched core kernels.  Measured on GB300
 // (NewHope-1024, single-instance / batched, us): keypair 22.0 / 31.4 and encapsulation 26.5 / 58.2
 // at n = 1; 23.0 / 43.4 and 28.8 / 72.1 at 128; 37.5 / 43.2 and 47.7 / 72.4 at 256 (NewHope-512
 // alike).
@@ -821,9 +821,13 @@ static int enc_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8
     g_shape[nidx(N)][1].get(NI, NT);
     const size_t sm = (size_t)NI * smem_per_instance(N, 1);
     if (prep(nh_enc_core<N>, sm)) return PQCGPU_ECUDA;
-    if (kem && n <= nh_single_max()) {
-        PQC_LAUNCH(st, "nh_enc_single", N, 0,
-                   nh_enc_single<N><<<n, NHS_THREADS, NhSingleSmem<N>::bytes(), st>>>(pk, coins, ct, ss));
+    if (n <= nh_single_max()) {
+        if (kem)
+            PQC_LAUNCH(st, "nh_enc_single", N, 0,
+                       nh_enc_single<N, true><<<n, NHS_THREADS, NhSingleSmem<N>::bytes(), st>>>(pk, coins, nullptr, ct, ss));
+        else
+            PQC_LAUNCH(st, "nh_enc_single", N, 0,
+                       nh_enc_single<N, false><<<n, NHS_THREADS, NhSingleSmem<N>::bytes(), st>>>(pk, coins, m, ct, nullptr));
         return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
     }
     EncArgs a{n, ct, pk, m, coins, 32, 32};

@@ -149,12 +149,13 @@ __global__ void __launch_bounds__(NHS_THREADS) nh_kp_single(const uint8_t *seed,
     if (tid < 4) reinterpret_cast<uint2 *>(pki + P::POLYBYTES)[tid] = S.seeds[tid];
 }
 
-// CPA-KEM encapsulation: (m, coin) = SHAKE256(coins, 64), ss = SHAKE256(m, 32); s', e', e'' noise
-// from coin; a-hat; u-hat = a-hat o s'-hat + e'-hat, v = invNTT(b-hat o s'-hat) + e'' + encode(m);
-// ct = u-hat || compress(v) (cpapke_enc, NewHope_NIST_GPU/cpapke.cu:333-404).
-template <int N>
-__global__ void __launch_bounds__(NHS_THREADS) nh_enc_single(const uint8_t *pk, const uint8_t *coins, uint8_t *ct,
-                                                             uint8_t *ss) {
+// Encryption: s', e', e'' noise from coin; a-hat; u-hat = a-hat o s'-hat + e'-hat, v = invNTT(b-hat o
+// s'-hat) + e'' + encode(m); ct = u-hat || compress(v) (cpapke_enc, NewHope_NIST_GPU/cpapke.cu:
+// 333-404).  KEM: (m, coin) = SHAKE256(coins, 64) and ss = SHAKE256(m, 32) (the CPA-KEM); CPA: m and
+// coin are given (32 bytes each per instance at coins and m_in), ss is not written.
+template <int N, bool KEM>
+__global__ void __launch_bounds__(NHS_THREADS) nh_enc_single(const uint8_t *pk, const uint8_t *coins, const uint8_t *m_in,
+                                                             uint8_t *ct, uint8_t *ss) {
     using P = Nh<N>;
     constexpr int NCH = P::NCH;
     extern __shared__ __align__(16) uint8_t smem[];
@@ -165,14 +166,20 @@ __global__ void __launch_bounds__(NHS_THREADS) nh_enc_single(const uint8_t *pk, 
     for (int i = tid; i < P::PKB / 8; i += NHS_THREADS)  // the public key, coalesced
         reinterpret_cast<uint2 *>(S.pk)[i] = reinterpret_cast<const uint2 *>(pki)[i];
     if (warp == 0) {
-        const uint2 h = warp_shake256_32(reinterpret_cast<const uint2 *>(coins + (size_t)x * 32), w);
-        if (lane < 8) S.seeds[4 + lane] = h;  // [4, 8) m, [8, 12) coin
+        if constexpr (KEM) {
+            const uint2 h = warp_shake256_32(reinterpret_cast<const uint2 *>(coins + (size_t)x * 32), w);
+            if (lane < 8) S.seeds[4 + lane] = h;  // [4, 8) m, [8, 12) coin
+        } else if (lane < 8) {
+            S.seeds[4 + lane] = reinterpret_cast<const uint2 *>(lane < 4 ? m_in + (size_t)x * 32 : coins + (size_t)x * 32)[lane & 3];
+        }
     }
     __syncthreads();
     const uint2 *m2 = S.seeds + 4, *coin = S.seeds + 8;
-    if (warp == 0) {  // ss = SHAKE256(m, 32), then e'' (nonce 2): a chunk per thread
-        const uint2 h = warp_shake256_32(m2, w);
-        if (lane < 4) reinterpret_cast<uint2 *>(ss + (size_t)x * 32)[lane] = h;
+    if (warp == 0) {  // KEM: ss = SHAKE256(m, 32); then e'' (nonce 2): a chunk per thread
+        if constexpr (KEM) {
+            const uint2 h = warp_shake256_32(m2, w);
+            if (lane < 4) reinterpret_cast<uint2 *>(ss + (size_t)x * 32)[lane] = h;
+        }
         if (lane < NCH)
             sample_chunk(coin, 2, lane, [&](int j, uint32_t c0, uint32_t c1) {
                 *reinterpret_cast<uint32_t *>(S.e2 + phys(64 * lane + j)) = (c0 & 0xffff) | (c1 << 16);
