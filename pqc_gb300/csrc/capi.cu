@@ -689,9 +689,10 @@ size_t op_scratch_bytes(int alg, int op, int plain) {
     return 0;
 }
 int op_dev(int alg, int op, int n, const uint8_t *in0, const uint8_t *in1, uint8_t *out0, uint8_t *out1,
-           uint8_t *scr, int plain, cudaStream_t s) {
+           uint8_t *scr, int flags, cudaStream_t s) {
     AlgInfo ai;
     if (!alg_info(alg, &ai) || op < 0 || op > 2) return PQCGPU_EINVAL;
+    const int plain = flags & OP_PLAIN;
     if (n <= 0) return PQCGPU_OK;
     int variant, k;
     if (kyber_alg(alg, &variant, &k)) {
@@ -703,8 +704,9 @@ int op_dev(int alg, int op, int n, const uint8_t *in0, const uint8_t *in1, uint8
     if (plain) return PQCGPU_EUNSUPPORTED;
     if (alg == PQCGPU_NEWHOPE1024 || alg == PQCGPU_NEWHOPE512) {
         const int N = alg == PQCGPU_NEWHOPE1024 ? 1024 : 512;
-        if (op == 0) return newhope_keypair_dev(N, n, out0, out1, in0, 32, s);
-        if (op == 1) return newhope_enc_dev(N, n, out0, out1, in0, nullptr, in1, scr, 1, s);
+        const bool single_ok = !(flags & OP_NH_BATCHED);
+        if (op == 0) return newhope_keypair_dev(N, n, out0, out1, in0, 32, s, single_ok);
+        if (op == 1) return newhope_enc_dev(N, n, out0, out1, in0, nullptr, in1, scr, 1, s, single_ok);
         return newhope_dec_dev(N, n, out0, in0, in1, 1, s);
     }
     const int fn = frodo_n(alg);

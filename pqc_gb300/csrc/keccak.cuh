@@ -152,6 +152,53 @@ __device__ __forceinline__ void keccak_absorb_lanes(uint2 (&A)[25], const uint2 
     keccak_pad<RATE_LANES>(A, nlanes, dom);
 }
 
+// Asynchronous 8-byte copy global -> shared (LDGSTS: no register holds the data in flight).
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory");
+}
+
+// keccak_absorb_lanes for a long message in global memory, one sponge per thread: block b + 1 is
+// copied into shared memory while block b is permuted, so the loads' latency hides behind the
+// permutation instead of stalling before each block.  `stage` is [2][RATE_LANES][nslots] uint2 of
+// shared memory, of which this thread uses column `slot` (consecutive threads, consecutive 8-byte
+// words: no bank conflicts); each thread reads only what its own copies wrote.
+template <int RATE_LANES>
+__device__ __forceinline__ void keccak_absorb_lanes_staged(uint2 (&A)[25], const uint2 *in, int nlanes, uint32_t dom,
+                                                           uint2 *stage, int slot, int nslots) {
+    keccak_zero(A);
+    const int nb = nlanes / RATE_LANES;
+    auto fetch = [&](int buf, const uint2 *src, int cnt) {
+        uint2 *d = stage + buf * RATE_LANES * nslots + slot;
+#pragma unroll
+        for (int i = 0; i < RATE_LANES; i++)
+            if (i < cnt) cp_async8(d + i * nslots, src + i);
+        cp_async_commit();
+    };
+    fetch(0, in, nlanes < RATE_LANES ? nlanes : RATE_LANES);
+    for (int b = 0; b < nb; b++) {
+        const int left = nlanes - (b + 1) * RATE_LANES;
+        fetch((b + 1) & 1, in + (b + 1) * RATE_LANES, left < RATE_LANES ? left : RATE_LANES);
+        cp_async_wait<1>();
+        const uint2 *s = stage + (b & 1) * RATE_LANES * nslots + slot;
+#pragma unroll
+        for (int i = 0; i < RATE_LANES; i++) A[i] = xor2(A[i], s[i * nslots]);
+        keccak_f1600(A);
+    }
+    cp_async_wait<0>();
+    const int rem = nlanes - nb * RATE_LANES;
+    const uint2 *s = stage + (nb & 1) * RATE_LANES * nslots + slot;
+#pragma unroll
+    for (int i = 0; i < RATE_LANES; i++)
+        if (i < rem) A[i] = xor2(A[i], s[i * nslots]);
+    keccak_pad<RATE_LANES>(A, rem, dom);
+}
+
 // Absorb pre[0..npre) || in[0..nlanes) (whole lanes) and pad; the state is ready to permute.
 template <int RATE_LANES>
 __device__ __forceinline__ void keccak_absorb_lanes2(uint2 (&A)[25], const uint2 *pre, int npre, const uint2 *in,

@@ -949,12 +949,17 @@ __global__ void __launch_bounds__(CORE_MAX_THREADS) kyber_kp_core(KpArgs a, int 
 }
 
 // ---- flat hash kernels: one thread per instance ----
+// The long absorbs (H(pk), H(c)) stage their input blocks through shared memory, a column per
+// thread of a 128-thread CTA (keccak_absorb_lanes_staged).
+constexpr int HASH_THREADS = 128;
+#define KY_HASH_STAGE __shared__ uint2 hstage[2 * SHA3_256_LANES * HASH_THREADS]
 // encaps prologue: m = H(coins); (K-bar, r) = G(m || H(pk)); scratch = m || r || K-bar
 // ML-KEM: m = coins (no pre-hash)
 template <int K, int V>
-__global__ void __launch_bounds__(128) kyber_enc_hash_pre(int n, const uint8_t *pk, const uint8_t *coins, uint8_t *scratch,
-                                                          int kem) {
+__global__ void __launch_bounds__(HASH_THREADS) kyber_enc_hash_pre(int n, const uint8_t *pk, const uint8_t *coins,
+                                                                   uint8_t *scratch, int kem) {
     using Pp = P<K, V>;
+    KY_HASH_STAGE;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
     uint2 A[25], mh[8];
@@ -968,7 +973,8 @@ __global__ void __launch_bounds__(128) kyber_enc_hash_pre(int n, const uint8_t *
 #pragma unroll
         for (int i = 0; i < 4; i++) mh[i] = A[i];
     }
-    keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(pk + (size_t)x * Pp::PKB), Pp::PKB / 8, DOM_SHA3);
+    keccak_absorb_lanes_staged<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(pk + (size_t)x * Pp::PKB), Pp::PKB / 8,
+                                               DOM_SHA3, hstage, threadIdx.x, HASH_THREADS);
     keccak_f1600(A);
 #pragma unroll
     for (int i = 0; i < 4; i++) mh[4 + i] = A[i];
@@ -989,9 +995,10 @@ __global__ void __launch_bounds__(128) kyber_enc_hash_pre(int n, const uint8_t *
 // encaps epilogue: ss = KDF(K-bar || H(c))
 // ML-KEM: ss = K (copied, no hashing)
 template <int K, int V>
-__global__ void __launch_bounds__(128) kyber_enc_hash_post(int n, const uint8_t *ct, const uint8_t *scratch, uint8_t *ss,
-                                                           int kem) {
+__global__ void __launch_bounds__(HASH_THREADS) kyber_enc_hash_post(int n, const uint8_t *ct, const uint8_t *scratch,
+                                                                    uint8_t *ss, int kem) {
     using Pp = P<K, V>;
+    KY_HASH_STAGE;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
     if (kem == KEM_MLKEM) {
@@ -1002,7 +1009,8 @@ __global__ void __launch_bounds__(128) kyber_enc_hash_post(int n, const uint8_t 
         return;
     }
     uint2 A[25], hc[4];
-    keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(ct + (size_t)x * Pp::CTB), Pp::CTB / 8, DOM_SHA3);
+    keccak_absorb_lanes_staged<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(ct + (size_t)x * Pp::CTB), Pp::CTB / 8,
+                                               DOM_SHA3, hstage, threadIdx.x, HASH_THREADS);
     keccak_f1600(A);
 #pragma unroll
     for (int i = 0; i < 4; i++) hc[i] = A[i];
@@ -1022,9 +1030,10 @@ __global__ void __launch_bounds__(128) kyber_enc_hash_post(int n, const uint8_t 
 }
 // decaps prologue: H(c); ML-KEM: the rejection key J(z || c) = SHAKE256(z || c, 32)
 template <int K, int V>
-__global__ void __launch_bounds__(128) kyber_dec_hash_pre(int n, const uint8_t *ct, const uint8_t *sk, uint8_t *hct,
-                                                          int kem) {
+__global__ void __launch_bounds__(HASH_THREADS) kyber_dec_hash_pre(int n, const uint8_t *ct, const uint8_t *sk,
+                                                                   uint8_t *hct, int kem) {
     using Pp = P<K, V>;
+    KY_HASH_STAGE;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
     uint2 A[25];
@@ -1033,7 +1042,7 @@ __global__ void __launch_bounds__(128) kyber_dec_hash_pre(int n, const uint8_t *
         keccak_absorb_lanes2<SHAKE256_LANES>(A, reinterpret_cast<const uint2 *>(sk + (size_t)x * Pp::SKB + Pp::SKB - 32), 4,
                                              c, Pp::CTB / 8, DOM_SHAKE);
     else
-        keccak_absorb_lanes<SHA3_256_LANES>(A, c, Pp::CTB / 8, DOM_SHA3);
+        keccak_absorb_lanes_staged<SHA3_256_LANES>(A, c, Pp::CTB / 8, DOM_SHA3, hstage, threadIdx.x, HASH_THREADS);
     keccak_f1600(A);
     uint2 *o = reinterpret_cast<uint2 *>(hct + (size_t)x * 32);
 #pragma unroll
@@ -1107,12 +1116,14 @@ __global__ void __launch_bounds__(128) kyber_kp_hash_pre(int n, const uint8_t *c
 }
 // keypair epilogue: sk[SKB-64 .. SKB-32) = H(pk)
 template <int K, int V>
-__global__ void __launch_bounds__(128) kyber_kp_hash_post(int n, const uint8_t *pk, uint8_t *sk) {
+__global__ void __launch_bounds__(HASH_THREADS) kyber_kp_hash_post(int n, const uint8_t *pk, uint8_t *sk) {
     using Pp = P<K, V>;
+    KY_HASH_STAGE;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= n) return;
     uint2 A[25];
-    keccak_absorb_lanes<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(pk + (size_t)x * Pp::PKB), Pp::PKB / 8, DOM_SHA3);
+    keccak_absorb_lanes_staged<SHA3_256_LANES>(A, reinterpret_cast<const uint2 *>(pk + (size_t)x * Pp::PKB), Pp::PKB / 8,
+                                               DOM_SHA3, hstage, threadIdx.x, HASH_THREADS);
     keccak_f1600(A);
     uint2 *o = reinterpret_cast<uint2 *>(sk + (size_t)x * Pp::SKB + Pp::SKB - 64);
 #pragma unroll

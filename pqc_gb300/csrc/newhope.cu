@@ -799,8 +799,9 @@ int newhope_get_shape(int N, int op, int *ni, int *threads) {
 }
 
 template <int N>
-static int keypair_n(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st) {
-    if (n <= nh_single_max()) {
+static int keypair_n(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, bool single_ok,
+                     cudaStream_t st) {
+    if (single_ok && n <= nh_single_max()) {
         PQC_LAUNCH(st, "nh_kp_single", N, 0,
                    nh_kp_single<N><<<n, NHS_THREADS, NhSingleSmem<N>::bytes(), st>>>(seed, seed_stride, pk, sk));
         return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
@@ -816,12 +817,12 @@ static int keypair_n(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int s
 
 template <int N>
 static int enc_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
-                 uint8_t *scratch, int kem, cudaStream_t st) {
+                 uint8_t *scratch, int kem, bool single_ok, cudaStream_t st) {
     int NI, NT;
     g_shape[nidx(N)][1].get(NI, NT);
     const size_t sm = (size_t)NI * smem_per_instance(N, 1);
     if (prep(nh_enc_core<N>, sm)) return PQCGPU_ECUDA;
-    if (n <= nh_single_max()) {
+    if (single_ok && n <= nh_single_max()) {
         if (kem)
             PQC_LAUNCH(st, "nh_enc_single", N, 0,
                        nh_enc_single<N, true><<<n, NHS_THREADS, NhSingleSmem<N>::bytes(), st>>>(pk, coins, nullptr, ct, ss));
@@ -947,17 +948,18 @@ int newhope_mixed_pre(const NhMixedJob &j, cudaStream_t st) {
     return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
 }
 
-int newhope_keypair_dev(int N, int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st) {
-    if (N == 1024) return keypair_n<1024>(n, pk, sk, seed, seed_stride, st);
-    if (N == 512) return keypair_n<512>(n, pk, sk, seed, seed_stride, st);
+int newhope_keypair_dev(int N, int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st,
+                        bool single_ok) {
+    if (N == 1024) return keypair_n<1024>(n, pk, sk, seed, seed_stride, single_ok, st);
+    if (N == 512) return keypair_n<512>(n, pk, sk, seed, seed_stride, single_ok, st);
     return PQCGPU_EINVAL;
 }
 
 // kem: coins 32 B per instance -> (m, coin) via the prologue into scratch (64 B / instance), ss
 int newhope_enc_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
-                    uint8_t *scratch, int kem, cudaStream_t st) {
-    if (N == 1024) return enc_n<1024>(n, ct, ss, pk, m, coins, scratch, kem, st);
-    if (N == 512) return enc_n<512>(n, ct, ss, pk, m, coins, scratch, kem, st);
+                    uint8_t *scratch, int kem, cudaStream_t st, bool single_ok) {
+    if (N == 1024) return enc_n<1024>(n, ct, ss, pk, m, coins, scratch, kem, single_ok, st);
+    if (N == 512) return enc_n<512>(n, ct, ss, pk, m, coins, scratch, kem, single_ok, st);
     return PQCGPU_EINVAL;
 }
 

@@ -54,9 +54,13 @@ int probe_peaks(int device, double *int_ops, double *keccak_perms);
     } while (0)
 
 // One device KEM operation (capi.cu): op 0 keypair (in0 coins -> out0 pk, out1 sk), 1 encaps (in0 pk,
-// in1 coins -> out0 ct, out1 ss), 2 decaps (in0 ct, in1 sk -> out0 ss); device pointers.
+// in1 coins -> out0 ct, out1 ss), 2 decaps (in0 ct, in1 sk -> out0 ss); device pointers.  flags:
+// OP_PLAIN = Kyber's reference-style chain; OP_NH_BATCHED = NewHope on its batched kernels at every
+// batch size (the serving loop: under concurrent load, the single-instance kernels' 512-thread CTAs
+// raised the p99 latency of the FrodoKEM requests beside them).
+constexpr int OP_PLAIN = 1, OP_NH_BATCHED = 2;
 int op_dev(int alg, int op, int n, const uint8_t *in0, const uint8_t *in1, uint8_t *out0, uint8_t *out1,
-           uint8_t *scr, int plain, cudaStream_t s);
+           uint8_t *scr, int flags, cudaStream_t s);
 size_t op_scratch_bytes(int alg, int op, int plain);
 void op_io_sizes(int alg, int op, size_t sz[4]);
 
@@ -130,10 +134,12 @@ int kyber_dec_dev(int variant, int k, int n, uint8_t *out, const uint8_t *ct, co
 int newhope_init_constants();
 int newhope_set_shape(int N, int op, int ni, int threads);
 int newhope_get_shape(int N, int op, int *ni, int *threads);
-int newhope_keypair_dev(int N, int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st);
+// single_ok = false: the batched kernels even for batches that the single-instance kernels would take
+int newhope_keypair_dev(int N, int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, cudaStream_t st,
+                        bool single_ok = true);
 // kem=1: coins 32 B/instance, scratch >= 64 B/instance, ss written; kem=0: CPA with m and coins
 int newhope_enc_dev(int N, int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
-                    uint8_t *scratch, int kem, cudaStream_t st);
+                    uint8_t *scratch, int kem, cudaStream_t st, bool single_ok = true);
 // kem=1: out = ss (32 B); kem=0: out = message
 int newhope_dec_dev(int N, int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, int kem, cudaStream_t st);
 // One NewHope CPA-KEM job of a mixed batch (device pointers as in op_dev; scratch 64 B per instance

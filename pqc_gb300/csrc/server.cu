@@ -432,7 +432,8 @@ struct pqcgpu_server {
         cudaMemcpyAsync(D, H, s.h2d_bytes, cudaMemcpyHostToDevice, st);
         int rc = PQCGPU_OK;
         if (op == PQCGPU_OP_KEYPAIR) {
-            rc = op_dev(alg, op, n, D + s.off_in0, nullptr, D + s.off_out0, D + s.off_out1, D + s.off_scr, 0, st);
+            rc = op_dev(alg, op, n, D + s.off_in0, nullptr, D + s.off_out0, D + s.off_out1, D + s.off_scr, OP_NH_BATCHED,
+                        st);
             launch_rows(false, s.kpk, D + s.off_out0, didx, n, s.pkb, st);
             launch_rows(false, s.ksk, D + s.off_out1, didx, n, s.skb, st);
         } else if (op == PQCGPU_OP_ENC) {
@@ -447,12 +448,13 @@ struct pqcgpu_server {
                 rc = frodo_enc_dev(frodo_n(alg), n, D + s.off_out0, D + s.off_out1, D + s.off_in0, D + s.off_in1,
                                    D + s.off_scr, st, D + s.off_pkh);
             } else {
-                rc = op_dev(alg, op, n, D + s.off_in0, D + s.off_in1, D + s.off_out0, D + s.off_out1, D + s.off_scr, 0,
-                            st);
+                rc = op_dev(alg, op, n, D + s.off_in0, D + s.off_in1, D + s.off_out0, D + s.off_out1, D + s.off_scr,
+                            OP_NH_BATCHED, st);
             }
         } else {
             launch_rows(true, D + s.off_in1, s.ksk, didx, n, s.skb, st);
-            rc = op_dev(alg, op, n, D + s.off_in0, D + s.off_in1, D + s.off_out0, nullptr, D + s.off_scr, 0, st);
+            rc = op_dev(alg, op, n, D + s.off_in0, D + s.off_in1, D + s.off_out0, nullptr, D + s.off_scr, OP_NH_BATCHED,
+                        st);
         }
         cudaMemcpyAsync(H + s.off_out0, D + s.off_out0, s.d2h_bytes, cudaMemcpyDeviceToHost, st);
         cudaEventRecord(s.done, st);
