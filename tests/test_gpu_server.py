@@ -93,3 +93,55 @@ def test_poisson_load(server):
     rep = server.run_poisson(serve.SERVING_MIX, rate=2000, seconds=0.5, seed=1)
     assert rep["completed"] == rep["submitted"] > 0
     assert 0 < rep["p50_ms"] <= rep["p99_ms"]
+
+
+def _kernels_launched(lib, fn):
+    """Names of the library kernels launched while fn runs (the library's launch profiler)."""
+    import ctypes
+    import json
+
+    from pqc_gb300 import _lib
+    buf = ctypes.create_string_buffer(1 << 16)
+    _lib.check(lib.pqcgpu_profile_read(buf, len(buf)))  # drop older records
+    lib.pqcgpu_profile_enable(1)
+    try:
+        fn()
+    finally:
+        lib.pqcgpu_profile_enable(0)
+    _lib.check(lib.pqcgpu_profile_read(buf, len(buf)))
+    return set(json.loads(buf.value.decode()))
+
+
+def test_newhope_requests_take_the_batched_kernels(server):
+    """The serving loop runs NewHope on its batched kernels at every batch size: the
+    single-instance kernels, which a direct call of a small batch takes, crowd the FrodoKEM
+    requests beside them under load.  Same bytes either way."""
+    from pqc_gb300 import _lib, kem
+    lib = _lib.load()
+    alg = "newhope1024"
+    s = kem.sizes(alg)
+    seed = drbg.seed48(91)
+    kc, ec = drbg.stream(seed, b"kp", s["kp_coins"]), drbg.stream(seed, b"enc", s["enc_coins"])
+    out = {}
+
+    def served():
+        key, pk = server.keypair(alg, kc)
+        ct, ss = server.enc(alg, key=key, coins=ec)
+        out["served"] = (pk, ct, ss, server.dec(alg, key, ct))
+        server.release(key)
+
+    names = _kernels_launched(lib, served)
+    assert {"nh_kp_core<1024,0>", "nh_enc_core<1024,0>", "nh_dec_core<1024,0>"} <= names, names
+    assert not any("single" in n for n in names), names
+    ctx = kem.Context(0)
+
+    def direct():
+        pk, sk = ctx.keypair(alg, 1, kc)
+        ct, ss = ctx.enc(alg, 1, pk, ec)
+        out["direct"] = (pk, ct, ss, ctx.dec(alg, 1, ct, sk))
+
+    names = _kernels_launched(lib, direct)
+    ctx.close()
+    assert {"nh_kp_single<1024,0>", "nh_enc_single<1024,0>"} <= names, names
+    assert out["served"] == out["direct"]
+    assert out["served"][2] == out["served"][3]
