@@ -828,7 +828,10 @@ static void fr_shape(int op, int n, int *parts, int *threads) {
     if (n >= 304) *parts = 1, *threads = 256;
     else if (n >= 152) *parts = 2, *threads = 256;
     else if (n >= 76) *parts = 4, *threads = 256;
-    else *parts = 8, *threads = 128;
+    else if (n >= 10) *parts = 8, *threads = 128;
+    else *parts = 16, *threads = 256;  // at most 144 CTAs, one per SM (measured on GB300 at n = 1, 8 x 128 ->
+                                       // 16 x 256: FrodoKEM-1344 encapsulation 1884 -> 1775 us, decapsulation
+                                       // 1413 -> 1305 us; FrodoKEM-976 1267 -> 1248 and 981 -> 963 us)
 }
 
 int frodo_set_shape(int op, int parts, int threads) {
