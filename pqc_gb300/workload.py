@@ -3,6 +3,7 @@
     python -m pqc_gb300.workload --alg kyber768 --n 16384 --reps 2
     python -m pqc_gb300.workload --alg newhope512,frodo640 --n 16384,256 --reps 1
     python -m pqc_gb300.workload --alg frodo976 --n 2048 --ops shared --product 2
+    python -m pqc_gb300.workload --mixed 8 --with-others --stage --reps 2
 
 For each algorithm in turn (a comma list, with one batch size each or one for all): generates n key
 pairs once, then runs `reps` rounds of encapsulation + decapsulation of n instances through the C
@@ -10,7 +11,10 @@ ABI with device buffers (`PQCGPU_DEVICE_PTRS`), timing each operation with CUDA 
 library stream.  Inputs come from the seeded SHAKE-256 DRBG, so every run of the same command
 launches the same kernels on the same data.  Exits non-zero if any decapsulated key differs from
 the encapsulated one.  `--ops shared` (FrodoKEM) runs n encapsulations to the first key with the
-shared-key call instead, on the CUDA-core or tensor-core product (`--product`).
+shared-key call instead, on the CUDA-core or tensor-core product (`--product`).  `--mixed S` runs
+the mixed Kyber batch (`mixed_kyber_spec`, every batch size divided by S; `--with-others` adds
+NewHope-1024 / 512 and FrodoKEM-640 / 976 / 1344 jobs of every operation) through one mixed-batch
+call per round, on the per-job kernels or (`--stage`) the persistent per-stage waves.
 """
 import argparse
 import sys
@@ -87,6 +91,65 @@ def run(alg, n, reps, want, fl, product=None):
     return ok
 
 
+def mixed_jobs(scale, with_others):
+    """[(alg, op, n)]: the mixed Kyber spec with every n divided by `scale` (at least 1), and with
+    `with_others` one job of every operation of NewHope-1024 / 512 (4096 / scale instances) and of
+    FrodoKEM-640 / 976 / 1344 (256 / scale)."""
+    spec = [(alg, op, max(1, n // scale)) for alg, op, n in mixed_kyber_spec()]
+    if with_others:
+        for alg, n in (("newhope1024", 4096), ("newhope512", 4096), ("frodo640", 256), ("frodo976", 256),
+                       ("frodo1344", 256)):
+            spec += [(alg, op, max(1, n // scale)) for op in ("keypair", "enc", "dec")]
+    return spec
+
+
+def run_mixed(scale, with_others, stage, reps):
+    """One mixed-batch call per round over mixed_jobs(); the decapsulated keys are checked against
+    the encapsulations that made their ciphertexts."""
+    ctx = kem.Context(0)
+    dev = torch.device("cuda:0")
+    jobs, keep, total = [], [], 0
+
+    def dev_bytes(seed, label, nbytes):
+        return torch.frombuffer(bytearray(drbg.stream(seed, label, nbytes)), dtype=torch.uint8).to(dev)
+
+    for j, (alg, op, n) in enumerate(mixed_jobs(scale, with_others)):
+        s = kem.sizes(alg)
+        seed = drbg.seed48(200 + j)
+        kc = dev_bytes(seed, b"kp", n * s["kp_coins"])
+        pk, sk = (torch.empty(n * s[x], dtype=torch.uint8, device=dev) for x in ("pk", "sk"))
+        ctx.keypair_dev(alg, n, pk, sk, kc)
+        if op == "keypair":
+            jobs.append((alg, op, n, kc, None, torch.empty_like(pk), torch.empty_like(sk)))
+        else:
+            ec = dev_bytes(seed, b"enc", n * s["enc_coins"])
+            ct = torch.empty(n * s["ct"], dtype=torch.uint8, device=dev)
+            ss = torch.empty(n * s["ss"], dtype=torch.uint8, device=dev)
+            ctx.enc_dev(alg, n, ct, ss, pk, ec)
+            if op == "enc":
+                jobs.append((alg, op, n, pk, ec, torch.empty_like(ct), torch.empty_like(ss)))
+            else:
+                jobs.append((alg, op, n, ct, sk, torch.empty_like(ss), None))
+                keep.append((len(jobs) - 1, ss))
+        total += n
+    ctx.wait()
+    st = torch.cuda.ExternalStream(ctx.stream)
+    ok = True
+    for rep in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        ctx.mixed_dev(jobs, kem.STAGE_KERNELS if stage else 0)
+        e1.record(st)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        same = all(torch.equal(jobs[i][5], ss) for i, ss in keep)
+        ok = ok and same
+        print("mixed %d jobs, %d instances, %s rep %d: %.3f ms (%.2f M ops/s), decaps match %s" %
+              (len(jobs), total, "stage waves" if stage else "per job", rep, ms, total / ms / 1e3, same), flush=True)
+    ctx.close()
+    return ok
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--alg", default="kyber768", help="algorithm or comma list of: " + ", ".join(sorted(kem.ALGS)))
@@ -96,7 +159,13 @@ def main(argv=None):
     ap.add_argument("--plain", action="store_true", help="per-stage path instead of the fused kernels")
     ap.add_argument("--product", type=int, default=None,
                     help="FrodoKEM shared-key product for --ops shared: 1 CUDA cores, 2 tensor cores")
+    ap.add_argument("--mixed", type=int, default=0, metavar="S",
+                    help="run the mixed batch with every batch size divided by S instead")
+    ap.add_argument("--with-others", action="store_true", help="--mixed: add NewHope and FrodoKEM jobs")
+    ap.add_argument("--stage", action="store_true", help="--mixed: the persistent per-stage waves")
     args = ap.parse_args(argv)
+    if args.mixed:
+        return 0 if run_mixed(args.mixed, args.with_others, args.stage, args.reps) else 1
     algs = [a for a in args.alg.split(",") if a]
     ns = [int(x) for x in args.n.split(",") if x]
     if any(a not in kem.ALGS for a in algs):
