@@ -39,21 +39,23 @@ struct HostShake {
     uint64_t s[25];
     unsigned pos;  // squeeze position within the current block
     static uint64_t rol(uint64_t v, int n) { return n ? (v << n) | (v >> (64 - n)) : v; }
-    static void permute(uint64_t A[25]) {
-        static uint64_t RC[24];
-        static int R[25];
-        static bool init = false;
-        if (!init) {
-            uint2 rc[24];
-            // same LFSR as the device table
+    // round constants (FIPS 202 rc(t) LFSR) and rotation offsets, built once; a function-local
+    // static is initialised thread-safely, so concurrent first calls from several threads are fine
+    struct Tables {
+        uint64_t RC[24];
+        int R[25];
+    };
+    static const Tables &tables() {
+        static const Tables t = [] {
+            Tables tb{};
             for (int ir = 0; ir < 24; ir++) {
-                unsigned long long v = 0;
+                uint64_t v = 0;
                 for (int j = 0; j <= 6; j++) {
-                    const int t = j + 7 * ir;
+                    const int tt = j + 7 * ir;
                     int bit = 1;
-                    if (t % 255) {
+                    if (tt % 255) {
                         int Rr[9] = {1, 0, 0, 0, 0, 0, 0, 0, 0};
-                        for (int i = 1; i <= t % 255; i++) {
+                        for (int i = 1; i <= tt % 255; i++) {
                             int Rn[9];
                             Rn[0] = 0;
                             for (int b = 0; b < 8; b++) Rn[b + 1] = Rr[b];
@@ -67,20 +69,23 @@ struct HostShake {
                     }
                     if (bit) v |= 1ULL << ((1u << j) - 1);
                 }
-                rc[ir] = make_uint2((unsigned)v, (unsigned)(v >> 32));
-                RC[ir] = v;
+                tb.RC[ir] = v;
             }
-            R[0] = 0;
+            tb.R[0] = 0;
             int x = 1, y = 0;
-            for (int t = 0; t < 24; t++) {
-                R[x + 5 * y] = ((t + 1) * (t + 2) / 2) % 64;
+            for (int t2 = 0; t2 < 24; t2++) {
+                tb.R[x + 5 * y] = ((t2 + 1) * (t2 + 2) / 2) % 64;
                 const int nx = y, ny = (2 * x + 3 * y) % 5;
                 x = nx;
                 y = ny;
             }
-            (void)rc;
-            init = true;
-        }
+            return tb;
+        }();
+        return t;
+    }
+    static void permute(uint64_t A[25]) {
+        const uint64_t *RC = tables().RC;
+        const int *R = tables().R;
         for (int ir = 0; ir < 24; ir++) {
             uint64_t C[5], D[5], B[25];
             for (int i = 0; i < 5; i++) C[i] = A[i] ^ A[i + 5] ^ A[i + 10] ^ A[i + 15] ^ A[i + 20];

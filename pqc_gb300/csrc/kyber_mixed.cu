@@ -97,7 +97,6 @@ size_t tile_smem(int kind, int k, int ni) {
 }
 
 int pkb(int k) { return k * 384 + 32; }
-int skb(int k) { return 2 * k * 384 + 96; }
 
 void fill_job(MixJob &m, int kind, const MixedKyberJob &j) {
     m.kind = kind;

@@ -89,8 +89,8 @@ int kyber_set_shape(int op, int k, int ni, int threads);
 // pairs were the fastest measured on GB300 at 65536 instances (Kyber-768 re-encryption without the
 // KDF: 1.079 ms at (256, 2), 104 registers, against 1.094 ms at (192, 3), 88 registers; the
 // encapsulation kernel at (192, 3): 1.082 against 1.066 ms).  Shapes with more threads are refused.
-constexpr int kyber_bound_threads(int op, int k) { return op == 1 ? 256 : op == 2 ? 256 : op == 3 ? 384 : 512; }
-constexpr int kyber_bound_ctas(int op, int k) { return op == 1 ? 2 : op == 2 ? 2 : op == 3 ? 2 : 1; }
+constexpr int kyber_bound_threads(int op, int /*k*/) { return op == 1 ? 256 : op == 2 ? 256 : op == 3 ? 384 : 512; }
+constexpr int kyber_bound_ctas(int op, int /*k*/) { return op == 1 ? 2 : op == 2 ? 2 : op == 3 ? 2 : 1; }
 int kyber_get_shape(int op, int k, int *ni, int *threads);
 // Scratch bytes per instance (op 0 keypair, 1 enc, 2 dec; plain = the per-stage baseline path).
 size_t kyber_scratch_bytes(int k, int op, int plain);

@@ -759,10 +759,7 @@ extern "C" int pqcgpu_server_run_poisson(pqcgpu_server *s, const pqcgpu_mix_entr
     std::uniform_real_distribution<double> uni(0.0, wsum);
     // output sinks (results are discarded; one buffer per alg/op, largest sizes)
     static thread_local std::vector<uint8_t> sink0(1 << 16), sink1(1 << 16);
-    std::vector<uint64_t> new_keys;
-    new_keys.reserve(1024);
-    std::vector<uint64_t> *keyslots = &new_keys;
-    std::deque<uint64_t> key_outs;
+    std::deque<uint64_t> key_outs;  // handles of the keypairs the run made (a deque: stable addresses)
     const auto t_start = Clock::now();
     double t = 0;
     uint64_t submitted = 0;
@@ -811,7 +808,6 @@ extern "C" int pqcgpu_server_run_poisson(pqcgpu_server *s, const pqcgpu_mix_entr
     }
     for (uint64_t k : key_outs)
         if (k) pqcgpu_server_key_release(s, k);
-    (void)keyslots;
     out->offered_per_s = rate;
     out->seconds = std::chrono::duration<double>(t_end - t_start).count();
     out->submit_seconds = std::chrono::duration<double>(t_sub - t_start).count();
