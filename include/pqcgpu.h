@@ -252,7 +252,9 @@ int pqcgpu_server_run_poisson(pqcgpu_server *server, const pqcgpu_mix_entry *mix
  * Core-kernel launch shape per (algorithm, operation): ni = instances per CTA, threads per CTA
  * (multiple of 32).  Kyber also takes op 3: the decryption stage of decapsulation (op 2 is then
  * its re-encryption stage), and op 4: ni = the largest KEM batch that runs on the single-instance
- * kernels (one CTA per instance, every operation and k; 0 = never; threads ignored).  Kyber: ni
+ * kernels (one CTA per instance, every operation and k; 0 = never; threads ignored), and op 5:
+ * ni = the largest batch whose serial hashes (H(pk), G, H(c), the KDF) run one warp per instance
+ * instead of one thread (0..65535, default 2048; all k; threads ignored).  Kyber: ni
  * 1..128, threads from 32 up to the core kernel's launch bound (keypair 512, encapsulation 256,
  * re-encryption 256, decryption stage 384; shared by the round-2 and round-3 sets of the same k);
  * NewHope: ni 1..64, threads 32..256; op 3: ni = the largest batch whose key generations and

@@ -14,6 +14,13 @@ LaunchShape g_dec1[3] = {{16, 256}, {4, 128}, {4, 128}};
 // 768 / 1024 and ML-KEM-768, every operation): the single-instance kernels are faster up to 256
 // instances (Kyber-768 encapsulation 75.6 against 121 us) and slower from 608 (139.5 against 122).
 LaunchShape g_single = {384, 0};
+// Batches of at most this many instances run the serial hashes (H(pk), G, H(c), the KDF) with one
+// warp per instance (25-lane permutation) instead of one thread.  Measured on GB300 (Kyber-768,
+// device buffers, thread -> warp hash kernels): encapsulation 173 -> 139 us at 1536 instances and
+// 173 -> 156 us at 2048, but 204 -> 225 us at 3072 (the warp form's ~7x issue slots then cost more
+// than its shorter chain saves); the host-buffer step of 65536 pairs, whose first chunk is 2048,
+// measured the same at 1024 and 2048 (3.35 ms) and slower at 4096 (3.41 ms).
+LaunchShape g_warp_hash = {2048, 0};
 
 #define PQC_KYBER_DECL(K, V)                                                                               \
     int keypair_##K##_##V(int, uint8_t *, uint8_t *, const uint8_t *, int, int, uint8_t *, int, cudaStream_t); \
@@ -93,6 +100,11 @@ int kyber_set_shape(int op, int k, int ni, int threads) {
         kyber::g_single.set(ni, 0);
         return PQCGPU_OK;
     }
+    if (op == 5) {  // the largest batch whose serial hashes run a warp per instance (all k); 0 = never
+        if (ni < 0 || ni > 65535) return PQCGPU_EINVAL;  // a 16-bit field of the shape word
+        kyber::g_warp_hash.set(ni, 0);
+        return PQCGPU_OK;
+    }
     if (op < 0 || op > 3 || k < 2 || k > 4 || ni <= 0 || ni > 128 || threads < 32 || threads % 32 ||
         threads > kyber_bound_threads(op, k))
         return PQCGPU_EINVAL;
@@ -112,6 +124,10 @@ int kyber_set_shape(int op, int k, int ni, int threads) {
 int kyber_get_shape(int op, int k, int *ni, int *threads) {
     if (op == 4) {
         kyber::g_single.get(*ni, *threads);
+        return PQCGPU_OK;
+    }
+    if (op == 5) {
+        kyber::g_warp_hash.get(*ni, *threads);
         return PQCGPU_OK;
     }
     if (op < 0 || op > 3 || k < 2 || k > 4) return PQCGPU_EINVAL;

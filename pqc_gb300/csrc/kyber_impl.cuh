@@ -1133,8 +1133,10 @@ __global__ void __launch_bounds__(HASH_THREADS) kyber_kp_hash_post(int n, const 
 // ---- the same serial hashes with one warp per instance: the latency path for small batches ----
 // A thread-per-instance sponge of 9-11 permutations is a chain of ~50k dependent instructions; the
 // 25-lane warp permutation (keccak.cuh) runs each permutation in about 60 % of the time, at ~7x the
-// issue slots, so it is used while the batch is too small to fill the GPU (n <= WARP_HASH_MAX).
-constexpr int WARP_HASH_MAX = 1024;
+// issue slots, so it is used while the batch is too small to fill the GPU (n <= warp_hash_max(),
+// launch-shape op 5, default 2048).  Independently, batches of at most FUSED_HASH_MAX keep G and the KDF inside
+// the keypair and decapsulation CTAs (one launch fewer each).
+constexpr int FUSED_HASH_MAX = 1024;
 #define KY_WARP_INSTANCE                                         \
     const int x = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  \
     if (x >= n) return;                                          \
@@ -1232,9 +1234,15 @@ namespace kyber {
 // ---------------------------------------------------------------------------------------------
 extern LaunchShape g_shape[3][3];  // [op][k-2]: instances per CTA, threads per CTA (kyber.cu)
 extern LaunchShape g_dec1[3];      // [k-2]: the same for the decapsulation's decryption stage
+extern LaunchShape g_warp_hash;    // batches of at most this many instances take the warp hash kernels
 extern LaunchShape g_single;       // KEM batches of at most this many instances take the
                                    // single-instance kernels (count field; kyber.cu)
 
+static inline int warp_hash_max() {
+    int a, b;
+    g_warp_hash.get(a, b);
+    return a;
+}
 static inline int single_max() {
     int a, b;
     g_single.get(a, b);
@@ -1302,13 +1310,13 @@ static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins,
     g_shape[0][K - 2].get(NI, NT);
     const size_t sm = Layout<3 * K, 128>::bytes(NI, NT);
     if (ensure_smem(kyber_kp_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
-    const bool g_pre = scratch && n > WARP_HASH_MAX;  // G as its own kernel (scratch: 64 B per instance)
+    const bool g_pre = scratch && n > FUSED_HASH_MAX;  // G as its own kernel (scratch: 64 B per instance)
     KpArgs a{n, pk, sk, coins, coins_stride, kem, g_pre ? scratch : nullptr};
     if (g_pre)
         PQC_LAUNCH(st, "kyber_kp_hash_pre", K, V,
                    kyber_kp_hash_pre<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, coins, coins_stride, kem, scratch));
     PQC_LAUNCH(st, "kyber_kp_core", K, V, kyber_kp_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
-    if (kem && n <= WARP_HASH_MAX)
+    if (kem && n <= warp_hash_max())
         PQC_LAUNCH(st, "kyber_kp_hash_post", K, V, kyber_kp_hash_post_w<K, V><<<(n + 3) / 4, 128, 0, st>>>(n, pk, sk));
     else if (kem)
         PQC_LAUNCH(st, "kyber_kp_hash_post", K, V, kyber_kp_hash_post<K, V><<<(n + 127) / 128, 128, 0, st>>>(n, pk, sk));
@@ -1334,7 +1342,7 @@ static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const 
     a.pk = pk;
     a.pk_stride = P<K, V>::PKB;
     if (kem) {
-        if (n <= WARP_HASH_MAX)
+        if (n <= warp_hash_max())
             PQC_LAUNCH(st, "kyber_enc_hash_pre", K, V,
                        kyber_enc_hash_pre_w<K, V><<<(n + 3) / 4, 128, 0, st>>>(n, pk, coins, scratch, kem));
         else
@@ -1352,7 +1360,7 @@ static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const 
     }
     PQC_LAUNCH(st, "kyber_enc_core", K, V, kyber_enc_core<K, V><<<(n + NI - 1) / NI, NT, sm, st>>>(a, NI));
     if (kem) {
-        if (n <= WARP_HASH_MAX)
+        if (n <= warp_hash_max())
             PQC_LAUNCH(st, "kyber_enc_hash_post", K, V,
                        kyber_enc_hash_post_w<K, V><<<(n + 3) / 4, 128, 0, st>>>(n, ct, scratch, ss, kem));
         else
@@ -1383,8 +1391,8 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
     d.hct = scratch;
     d.kem = kem;
     d.mr = scratch + (size_t)n * 32;
-    d.kdf_post = (kem == KEM_FO && n > WARP_HASH_MAX) ? 1 : 0;
-    d.g_post = (kem && n > WARP_HASH_MAX) ? 1 : 0;
+    d.kdf_post = (kem == KEM_FO && n > FUSED_HASH_MAX) ? 1 : 0;
+    d.g_post = (kem && n > FUSED_HASH_MAX) ? 1 : 0;
     if (!kem) {
         if (ensure_smem(kyber_dec_core<K, V, DEC_FUSED>, sm) != cudaSuccess) return PQCGPU_ECUDA;
         PQC_LAUNCH(st, "kyber_dec_core", K, V,
@@ -1400,7 +1408,7 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
         side = nullptr;
     }
     const cudaStream_t hs = side ? side->s : st;
-    if (n <= WARP_HASH_MAX)
+    if (n <= warp_hash_max())
         PQC_LAUNCH(hs, "kyber_dec_hash_pre", K, V,
                    kyber_dec_hash_pre_w<K, V><<<(n + 3) / 4, 128, 0, hs>>>(n, ct, sk, scratch, kem));
     else

@@ -173,7 +173,7 @@ int launch_wave(const std::vector<std::pair<int, const MixedKyberJob *>> &items,
 template <int K>
 void job_hash(int op, int phase, const MixedKyberJob &j, cudaStream_t st) {
     const int n = j.n;
-    const bool w = n <= WARP_HASH_MAX;
+    const bool w = n <= warp_hash_max();
     if (op == 0) {
         if (phase == 0)
             PQC_LAUNCH(st, "kyber_kp_hash_pre", K, 3,

@@ -79,6 +79,28 @@ def test_frodo_launch_shape_validation():
     assert lib.pqcgpu_set_launch_shape(fr, 0, 0, 0) == 0
 
 
+def test_kyber_warp_hash_threshold():
+    """Kyber op 5 (the largest batch whose serial hashes run a warp per instance) takes 0..65535,
+    shared by every k; the setting round-trips and the default is restored."""
+    import ctypes
+
+    from pqc_gb300 import _lib, kem
+    lib = _lib.load()
+    ky = kem.alg_id("kyber768")
+    ni, thr = ctypes.c_int(), ctypes.c_int()
+    assert lib.pqcgpu_get_launch_shape(ky, 5, ctypes.byref(ni), ctypes.byref(thr)) == 0
+    default = ni.value
+    assert default == 2048
+    try:
+        assert lib.pqcgpu_set_launch_shape(ky, 5, 65536, 0) != 0
+        assert lib.pqcgpu_set_launch_shape(ky, 5, -1, 0) != 0
+        assert lib.pqcgpu_set_launch_shape(ky, 5, 4096, 0) == 0
+        assert lib.pqcgpu_get_launch_shape(kem.alg_id("kyber1024"), 5, ctypes.byref(ni), ctypes.byref(thr)) == 0
+        assert ni.value == 4096
+    finally:
+        lib.pqcgpu_set_launch_shape(ky, 5, default, 0)
+
+
 class _CtrDrbgRestated:
     """SP 800-90A AES-256 CTR_DRBG (no derivation function), restated over an independent AES
     (the `cryptography` package) to check the library's own AES and DRBG."""
