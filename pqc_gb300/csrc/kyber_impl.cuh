@@ -329,7 +329,7 @@ struct KpArgs {
     const uint8_t *coins;    // d (and z for KEM) per instance
     int coins_stride;
     int kem;                 // 1: write sk = sk_cpa || pk || (H(pk) later) || z
-    const uint8_t *g_in;     // batches above 1024: (rho, sigma) per instance (64 B) computed by
+    const uint8_t *g_in;     // batches above KP_FUSED_MAX: (rho, sigma) per instance (64 B) computed by
                              // kyber_kp_hash_pre; null: the core kernel computes G itself
 };
 struct EncArgs {
@@ -361,7 +361,7 @@ struct DecArgs {
 // phases, its own launch shape), then re-encryption + comparison + key selection, whose phases are
 // those of encapsulation and which therefore runs at an encapsulation-like shape and efficiency.
 // Measured on GB300 (Kyber-768, 65536): 0.29 + 1.54 ms against 2.03 ms as one kernel.  For
-// batches above 1024 the two single-permutation hashes at the ends of the stages (G, the KDF) run
+// batches above DEC_FUSED_MAX the two single-permutation hashes at the ends of the stages (G, the KDF) run
 // as thread-per-instance kernels between and after them (DecArgs::g_post, kdf_post): inside a CTA
 // each held its shared memory while NI threads permuted (0.26 -> 0.19 ms and 1.27 -> 1.10 ms for
 // the two stages, 24 us per hash kernel).  CPA decryption alone (DEC_FUSED) stops after the message.
@@ -1134,9 +1134,14 @@ __global__ void __launch_bounds__(HASH_THREADS) kyber_kp_hash_post(int n, const 
 // A thread-per-instance sponge of 9-11 permutations is a chain of ~50k dependent instructions; the
 // 25-lane warp permutation (keccak.cuh) runs each permutation in about 60 % of the time, at ~7x the
 // issue slots, so it is used while the batch is too small to fill the GPU (n <= warp_hash_max(),
-// launch-shape op 5, default 2048).  Independently, batches of at most FUSED_HASH_MAX keep G and the KDF inside
-// the keypair and decapsulation CTAs (one launch fewer each).
-constexpr int FUSED_HASH_MAX = 1024;
+// launch-shape op 5, default 2048).  Independently, keypair batches of at most KP_FUSED_MAX keep G(d)
+// inside the core CTAs, and decapsulation batches of at most DEC_FUSED_MAX keep G and the KDF inside
+// theirs (one launch fewer each).  Measured on GB300 (device buffers, fused -> split): Kyber-768
+// decapsulation 103.6 -> 90.1 us at 512 instances and 109.9 -> 96.3 us at 1024 (Kyber-1024 108.8 ->
+// 88.9 and 114.4 -> 96.5 us, Kyber-512 3 % faster), but keypair 93.5 -> 97.6 us at 512 (3-5 %
+// slower for every k): the single-thread tails cost the decapsulation stages more than a launch.
+constexpr int KP_FUSED_MAX = 1024;
+constexpr int DEC_FUSED_MAX = 384;
 #define KY_WARP_INSTANCE                                         \
     const int x = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  \
     if (x >= n) return;                                          \
@@ -1310,7 +1315,7 @@ static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins,
     g_shape[0][K - 2].get(NI, NT);
     const size_t sm = Layout<3 * K, 128>::bytes(NI, NT);
     if (ensure_smem(kyber_kp_core<K, V>, sm) != cudaSuccess) return PQCGPU_ECUDA;
-    const bool g_pre = scratch && n > FUSED_HASH_MAX;  // G as its own kernel (scratch: 64 B per instance)
+    const bool g_pre = scratch && n > KP_FUSED_MAX;  // G as its own kernel (scratch: 64 B per instance)
     KpArgs a{n, pk, sk, coins, coins_stride, kem, g_pre ? scratch : nullptr};
     if (g_pre)
         PQC_LAUNCH(st, "kyber_kp_hash_pre", K, V,
@@ -1391,15 +1396,16 @@ static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk,
     d.hct = scratch;
     d.kem = kem;
     d.mr = scratch + (size_t)n * 32;
-    d.kdf_post = (kem == KEM_FO && n > FUSED_HASH_MAX) ? 1 : 0;
-    d.g_post = (kem && n > FUSED_HASH_MAX) ? 1 : 0;
+    d.kdf_post = (kem == KEM_FO && n > DEC_FUSED_MAX) ? 1 : 0;
+    d.g_post = (kem && n > DEC_FUSED_MAX) ? 1 : 0;
     if (!kem) {
         if (ensure_smem(kyber_dec_core<K, V, DEC_FUSED>, sm) != cudaSuccess) return PQCGPU_ECUDA;
         PQC_LAUNCH(st, "kyber_dec_core", K, V,
                    kyber_dec_core<K, V, DEC_FUSED><<<(n + NI - 1) / NI, NT, sm, st>>>(d, NI));
         return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
     }
-    // With the KDF after the re-encryption stage (round-2 / round-3 KEM, batches above 1024), H(c)
+    // With the KDF after the re-encryption stage (round-2 / round-3 KEM, batches above
+    // DEC_FUSED_MAX), H(c)
     // is needed only by kyber_dec_hash_post: it runs on a side stream beside the decryption and
     // re-encryption stages, whose integer pipe it shares.
     SideStream *side = d.kdf_post ? side_stream() : nullptr;

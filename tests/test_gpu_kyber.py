@@ -63,7 +63,7 @@ def test_cpa_matches_oracle(ctx, oracle, variant, k, n):
 
 @pytest.mark.parametrize("alg", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "mlkem512", "mlkem768",
                                  "mlkem1024"])
-@pytest.mark.parametrize("n", [1, 31, 257, 1536, 4099])
+@pytest.mark.parametrize("n", [1, 31, 257, 768, 1536, 4099])
 def test_kem_matches_oracle(ctx, oracle, alg, n):
     from pqc_gb300 import kem
     s = kem.sizes(alg)
@@ -84,9 +84,9 @@ def test_kem_matches_oracle(ctx, oracle, alg, n):
 
 @pytest.mark.parametrize("alg", ["kyber512", "kyber768", "kyber1024", "kyber1024r2", "mlkem512", "mlkem768",
                                  "mlkem1024"])
-# 2048: the key selection leaves the CTA and the KDF runs after it, hashes a warp per instance;
-# 4096: the same with the hashes a thread per instance
-@pytest.mark.parametrize("n", [64, 2048, 4096])
+# 768 and 2048: the key selection leaves the CTA and the KDF runs after it, hashes a warp per
+# instance; 4096: the same with the hashes a thread per instance
+@pytest.mark.parametrize("n", [64, 768, 2048, 4096])
 def test_kem_implicit_rejection(ctx, oracle, alg, n):
     from pqc_gb300 import kem
     s = kem.sizes(alg)
