@@ -252,7 +252,8 @@ int pqcgpu_server_run_poisson(pqcgpu_server *server, const pqcgpu_mix_entry *mix
  * Core-kernel launch shape per (algorithm, operation): ni = instances per CTA, threads per CTA
  * (multiple of 32).  Kyber also takes op 3: the decryption stage of decapsulation (op 2 is then
  * its re-encryption stage), and op 4: ni = the largest KEM batch that runs on the single-instance
- * kernels (one CTA per instance, every operation and k; 0 = never; threads ignored), and op 5:
+ * kernels (one CTA per instance), set for every operation of this k (0 = never, -1 = the measured
+ * per-operation defaults; get returns the encapsulation's; threads ignored), and op 5:
  * ni = the largest batch whose serial hashes (H(pk), G, H(c), the KDF) run one warp per instance
  * instead of one thread (0..65535, default 2048; all k; threads ignored).  Kyber: ni
  * 1..128, threads from 32 up to the core kernel's launch bound (keypair 512, encapsulation 256,

@@ -9,11 +9,16 @@ namespace kyber {
 LaunchShape g_shape[3][3] = {{{16, 64}, {12, 128}, {4, 64}}, {{30, 128}, {14, 128}, {6, 96}},
                              {{30, 128}, {14, 128}, {8, 128}}};
 LaunchShape g_dec1[3] = {{16, 256}, {4, 128}, {4, 128}};
-// KEM batches of at most this many instances run on the single-instance kernels (one CTA per
-// instance, kyber_single.cuh); larger ones on the batched chains.  Measured on GB300 (Kyber-512 /
-// 768 / 1024 and ML-KEM-768, every operation): the single-instance kernels are faster up to 256
-// instances (Kyber-768 encapsulation 75.6 against 121 us) and slower from 608 (139.5 against 122).
-LaunchShape g_single = {384, 0};
+// [k-2][op 0 keypair, 1 encapsulation, 2 decapsulation]: KEM batches of at most this many
+// instances run on the single-instance kernels (one CTA per instance, kyber_single.cuh); larger ones
+// on the batched chains.  Measured on GB300 (device buffers, median of 15, single-instance /
+// batched, us): Kyber-512 single faster at every size up to 640 (encapsulation 57 / 124 at 448,
+// 103 / 129 at 640); Kyber-768 encapsulation 75 / 122 at 256 but 135 / 121 at 320 (past 304 = two
+// 512-thread CTAs per SM), keypair even at 320-384, decapsulation 87 / 93 at 512 and 113 / 95 at
+// 640; Kyber-1024 keypair 73 / 95 at 256 but 114 / 96 at 320, encapsulation 97 / 132 and 180 /
+// 133, decapsulation 103 / 107 at 384 and 103 / 89 at 448.
+static constexpr int SINGLE_DEFAULT[3][3] = {{640, 640, 640}, {304, 304, 512}, {304, 304, 384}};
+LaunchShape g_single[3][3] = {{{640, 0}, {640, 0}, {640, 0}}, {{304, 0}, {304, 0}, {512, 0}}, {{304, 0}, {304, 0}, {384, 0}}};
 // Batches of at most this many instances run the serial hashes (H(pk), G, H(c), the KDF) with one
 // warp per instance (25-lane permutation) instead of one thread.  Measured on GB300 (Kyber-768,
 // device buffers, thread -> warp hash kernels): encapsulation 173 -> 139 us at 1536 instances and
@@ -95,9 +100,10 @@ int kyber_init_constants() {
     return kyber_mixed_init();
 }
 int kyber_set_shape(int op, int k, int ni, int threads) {
-    if (op == 4) {  // the largest batch that takes the single-instance kernels (all k); 0 = never
-        if (ni < 0 || ni > 4096) return PQCGPU_EINVAL;
-        kyber::g_single.set(ni, 0);
+    if (op == 4) {  // the largest batch that takes the single-instance kernels, every operation of
+                    // this k; 0 = never, -1 = the measured per-operation defaults
+        if (k < 2 || k > 4 || ni < -1 || ni > 4096) return PQCGPU_EINVAL;
+        for (int o = 0; o < 3; o++) kyber::g_single[k - 2][o].set(ni < 0 ? kyber::SINGLE_DEFAULT[k - 2][o] : ni, 0);
         return PQCGPU_OK;
     }
     if (op == 5) {  // the largest batch whose serial hashes run a warp per instance (all k); 0 = never
@@ -122,8 +128,9 @@ int kyber_set_shape(int op, int k, int ni, int threads) {
     return PQCGPU_OK;
 }
 int kyber_get_shape(int op, int k, int *ni, int *threads) {
-    if (op == 4) {
-        kyber::g_single.get(*ni, *threads);
+    if (op == 4) {  // the encapsulation's threshold of this k
+        if (k < 2 || k > 4) return PQCGPU_EINVAL;
+        kyber::g_single[k - 2][1].get(*ni, *threads);
         return PQCGPU_OK;
     }
     if (op == 5) {

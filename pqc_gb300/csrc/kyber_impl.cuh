@@ -1240,17 +1240,17 @@ namespace kyber {
 extern LaunchShape g_shape[3][3];  // [op][k-2]: instances per CTA, threads per CTA (kyber.cu)
 extern LaunchShape g_dec1[3];      // [k-2]: the same for the decapsulation's decryption stage
 extern LaunchShape g_warp_hash;    // batches of at most this many instances take the warp hash kernels
-extern LaunchShape g_single;       // KEM batches of at most this many instances take the
-                                   // single-instance kernels (count field; kyber.cu)
+extern LaunchShape g_single[3][3];  // [k-2][op]: KEM batches of at most this many instances take
+                                    // the single-instance kernels (count field; kyber.cu)
 
 static inline int warp_hash_max() {
     int a, b;
     g_warp_hash.get(a, b);
     return a;
 }
-static inline int single_max() {
+static inline int single_max(int k, int op) {
     int a, b;
-    g_single.get(a, b);
+    g_single[k - 2][op].get(a, b);
     return a;
 }
 
@@ -1305,7 +1305,7 @@ template <int K, int V>
 static int launch_keypair(int n, uint8_t *pk, uint8_t *sk, const uint8_t *coins, int coins_stride, int kem,
                           uint8_t *scratch, int plain, cudaStream_t st) {
     if (plain) return kem == KEM_FO ? plain_keypair<K, V>(n, pk, sk, coins, coins_stride, scratch, st) : PQCGPU_EUNSUPPORTED;
-    if (kem && n <= single_max()) {
+    if (kem && n <= single_max(K, 0)) {
         PQC_LAUNCH(st, "kyber_kp_single", K, V,
                    kyber_kp_single<K, V><<<n, SINGLE_THREADS, SingleSmem<K, V>::bytes(), st>>>(coins, coins_stride, pk, sk,
                                                                                               kem));
@@ -1332,7 +1332,7 @@ template <int K, int V>
 static int launch_enc(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8_t *m, const uint8_t *coins,
                       uint8_t *scratch, int kem, int plain, cudaStream_t st) {
     if (plain) return kem == KEM_FO ? plain_enc<K, V>(n, ct, ss, pk, coins, scratch, st) : PQCGPU_EUNSUPPORTED;
-    if (kem && n <= single_max()) {
+    if (kem && n <= single_max(K, 1)) {
         PQC_LAUNCH(st, "kyber_enc_single", K, V,
                    kyber_enc_single<K, V><<<n, SINGLE_THREADS, SingleSmem<K, V>::bytes(), st>>>(pk, coins, ct, ss, kem));
         return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
@@ -1379,7 +1379,7 @@ template <int K, int V>
 static int launch_dec(int n, uint8_t *out, const uint8_t *ct, const uint8_t *sk, uint8_t *scratch, int kem,
                       int plain, cudaStream_t st) {
     if (plain) return kem == KEM_FO ? plain_dec<K, V>(n, out, ct, sk, scratch, st) : PQCGPU_EUNSUPPORTED;
-    if (kem && n <= single_max()) {
+    if (kem && n <= single_max(K, 2)) {
         PQC_LAUNCH(st, "kyber_dec_single", K, V,
                    kyber_dec_single<K, V><<<n, SINGLE_THREADS, SingleSmem<K, V>::bytes(), st>>>(ct, sk, out, kem));
         return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;

@@ -79,6 +79,31 @@ def test_frodo_launch_shape_validation():
     assert lib.pqcgpu_set_launch_shape(fr, 0, 0, 0) == 0
 
 
+def test_kyber_single_instance_thresholds():
+    """Kyber op 4 sets the single-instance threshold of every operation of one k (0 = never); -1
+    restores the measured per-operation defaults; get returns the encapsulation's."""
+    import ctypes
+
+    from pqc_gb300 import _lib, kem
+    lib = _lib.load()
+    ni, thr = ctypes.c_int(), ctypes.c_int()
+
+    def enc_limit(alg):
+        assert lib.pqcgpu_get_launch_shape(kem.alg_id(alg), 4, ctypes.byref(ni), ctypes.byref(thr)) == 0
+        return ni.value
+
+    assert (enc_limit("kyber512"), enc_limit("kyber768"), enc_limit("kyber1024")) == (640, 304, 304)
+    assert enc_limit("mlkem768") == 304  # shared by every variant of one k
+    try:
+        assert lib.pqcgpu_set_launch_shape(kem.alg_id("kyber768"), 4, 4097, 0) != 0
+        assert lib.pqcgpu_set_launch_shape(kem.alg_id("kyber768"), 4, -2, 0) != 0
+        assert lib.pqcgpu_set_launch_shape(kem.alg_id("kyber768"), 4, 0, 0) == 0
+        assert enc_limit("kyber768") == 0 and enc_limit("kyber512") == 640
+    finally:
+        assert lib.pqcgpu_set_launch_shape(kem.alg_id("kyber768"), 4, -1, 0) == 0
+    assert enc_limit("kyber768") == 304
+
+
 def test_kyber_warp_hash_threshold():
     """Kyber op 5 (the largest batch whose serial hashes run a warp per instance) takes 0..65535,
     shared by every k; the setting round-trips and the default is restored."""

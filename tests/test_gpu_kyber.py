@@ -207,8 +207,9 @@ def test_plain_path_matches_oracle(ctx, oracle, alg):
 @pytest.mark.parametrize("n", [1, 33, 300])
 def test_single_instance_and_batched_paths_match_oracle(ctx, oracle, alg, n):
     """Small KEM batches run on the single-instance kernels (one CTA per instance) up to a size
-    threshold (launch-shape op 4); both that path and the batched chains must give the oracle's
-    bytes, including implicit rejection."""
+    threshold per k and operation (launch-shape op 4 sets every operation of a k; -1 restores the
+    measured defaults); both that path and the batched chains must give the oracle's bytes,
+    including implicit rejection."""
     from pqc_gb300 import _lib, kem
     lib = _lib.load()
     s = kem.sizes(alg)
@@ -222,7 +223,6 @@ def test_single_instance_and_batched_paths_match_oracle(ctx, oracle, alg, n):
     for x in range(0, n, 2):
         bad[x * s["ct"] + (x * 53) % s["ct"]] ^= 1 << (x % 8)
     orej = oracle.batch_dec(a, n, bytes(bad), osk)
-    before = ctypes_shape(lib)
     try:
         for limit in (4096, 0):  # every batch single-instance, then never
             assert lib.pqcgpu_set_launch_shape(kem.alg_id(alg), 4, limit, 0) == 0
@@ -231,11 +231,4 @@ def test_single_instance_and_batched_paths_match_oracle(ctx, oracle, alg, n):
             assert ctx.dec(alg, n, oct_, osk) == oss, limit
             assert ctx.dec(alg, n, bytes(bad), osk) == orej, limit
     finally:
-        assert lib.pqcgpu_set_launch_shape(kem.alg_id(alg), 4, before, 0) == 0
-
-
-def ctypes_shape(lib):
-    import ctypes
-    a, b = ctypes.c_int(), ctypes.c_int()
-    assert lib.pqcgpu_get_launch_shape(1, 4, ctypes.byref(a), ctypes.byref(b)) == 0
-    return a.value
+        assert lib.pqcgpu_set_launch_shape(kem.alg_id(alg), 4, -1, 0) == 0
