@@ -259,8 +259,9 @@ int pqcgpu_server_run_poisson(pqcgpu_server *server, const pqcgpu_mix_entry *mix
  * 1..128, threads from 32 up to the core kernel's launch bound (keypair 512, encapsulation 256,
  * re-encryption 256, decryption stage 384; shared by the round-2 and round-3 sets of the same k);
  * NewHope: ni 1..64, threads 32..256; op 3: ni = the largest batch whose key generations and
- * encapsulations (CPA and KEM) run on the single-instance kernels (one CTA per instance; 0 =
- * never; both n).  FrodoKEM: keypair ni 0 or 1, threads 64 / 128 / 256 (one row of A per thread); encaps / decaps ni = CTAs per instance sharing the rows of A (1, 2, 4, 8,
+ * encapsulations (CPA and KEM) run on the single-instance kernels (one CTA per instance; both n;
+ * 0 = never, -1 = the measured defaults, 304 for keypair and 456 for encapsulation; get returns
+ * the encapsulation's).  FrodoKEM: keypair ni 0 or 1, threads 64 / 128 / 256 (one row of A per thread); encaps / decaps ni = CTAs per instance sharing the rows of A (1, 2, 4, 8,
  * 16) with threads 128 / 256, or ni = 0 to choose by batch size (the default); op 3: ni = the
  * product of pqcgpu_frodo_enc_shared_key_batch (1 CUDA cores, 2 tensor cores, 0 default).
  * Applies to all contexts of the process; a launch reads the pair atomically. */

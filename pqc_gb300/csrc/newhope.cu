@@ -705,15 +705,18 @@ __global__ void __launch_bounds__(128) nh_enc_hash_pre(int n, const uint8_t *coi
 
 // [n index: 0 = 1024, 1 = 512][op] = {instances per CTA, threads}
 static LaunchShape g_shape[2][3] = {{{8, 128}, {4, 64}, {4, 128}}, {{16, 128}, {16, 128}, {4, 64}}};
-// Key generations and encapsulations (CPA and KEM) of at most this many instances run on the
-// single-instance kernels (newhope_single.cuh); larger batches on the batched core kernels.  Measured on GB300
-// (NewHope-1024, single-instance / batched, us): keypair 22.0 / 31.4 and encapsulation 26.5 / 58.2
-// at n = 1; 23.0 / 43.4 and 28.8 / 72.1 at 128; 37.5 / 43.2 and 47.7 / 72.4 at 256 (NewHope-512
-// alike).
-static LaunchShape g_nh_single = {256, 0};
-static int nh_single_max() {
+// [0 keypair, 1 encapsulation]: key generations and encapsulations (CPA and KEM) of at most this
+// many instances run on the single-instance kernels (newhope_single.cuh); larger batches on the
+// batched core kernels (both n).  One 512-thread CTA per SM, so the single-instance time steps up
+// past each multiple of 152 instances.  Measured on GB300 (NewHope-1024, single-instance / batched,
+// us): keypair 22.0 / 31.4 and encapsulation 26.5 / 58.2 at n = 1; 38.9 / 43.1 and 49.0 / 70.5 at
+// 304; 52.7 / 42.8 and 66.2 / 70.6 at 384; 54.9 / 42.8 and 68.8 / 71.9 at 456; 67.5 / 43.3 and 84.3
+// / 72.5 at 512 (NewHope-512 alike).
+static constexpr int NH_SINGLE_DEFAULT[2] = {304, 456};
+static LaunchShape g_nh_single[2] = {{304, 0}, {456, 0}};
+static int nh_single_max(int op) {
     int v, t;
-    g_nh_single.get(v, t);
+    g_nh_single[op].get(v, t);
     return v;
 }
 static int nidx(int N) { return N == 1024 ? 0 : 1; }
@@ -776,9 +779,10 @@ int newhope_init_constants() {
 }
 
 int newhope_set_shape(int N, int op, int ni, int threads) {
-    if (op == 3) {  // the largest batch that takes the single-instance kernels (both n); 0 = never
-        if ((N != 1024 && N != 512) || ni < 0 || ni > 4096) return PQCGPU_EINVAL;
-        g_nh_single.set(ni, 0);
+    if (op == 3) {  // the largest batch that takes the single-instance kernels, keypair and
+                    // encapsulation, both n; 0 = never, -1 = the measured defaults
+        if ((N != 1024 && N != 512) || ni < -1 || ni > 4096) return PQCGPU_EINVAL;
+        for (int o = 0; o < 2; o++) g_nh_single[o].set(ni < 0 ? NH_SINGLE_DEFAULT[o] : ni, 0);
         return PQCGPU_OK;
     }
     if ((N != 1024 && N != 512) || op < 0 || op > 2 || ni < 1 || ni > 64 || threads < 32 || threads > 256 || threads % 32)
@@ -789,8 +793,8 @@ int newhope_set_shape(int N, int op, int ni, int threads) {
 }
 
 int newhope_get_shape(int N, int op, int *ni, int *threads) {
-    if (op == 3 && (N == 1024 || N == 512)) {
-        g_nh_single.get(*ni, *threads);
+    if (op == 3 && (N == 1024 || N == 512)) {  // the encapsulation's threshold
+        g_nh_single[1].get(*ni, *threads);
         return PQCGPU_OK;
     }
     if ((N != 1024 && N != 512) || op < 0 || op > 2) return PQCGPU_EINVAL;
@@ -801,7 +805,7 @@ int newhope_get_shape(int N, int op, int *ni, int *threads) {
 template <int N>
 static int keypair_n(int n, uint8_t *pk, uint8_t *sk, const uint8_t *seed, int seed_stride, bool single_ok,
                      cudaStream_t st) {
-    if (single_ok && n <= nh_single_max()) {
+    if (single_ok && n <= nh_single_max(0)) {
         PQC_LAUNCH(st, "nh_kp_single", N, 0,
                    nh_kp_single<N><<<n, NHS_THREADS, NhSingleSmem<N>::bytes(), st>>>(seed, seed_stride, pk, sk));
         return cudaGetLastError() == cudaSuccess ? PQCGPU_OK : PQCGPU_ECUDA;
@@ -822,7 +826,7 @@ static int enc_n(int n, uint8_t *ct, uint8_t *ss, const uint8_t *pk, const uint8
     g_shape[nidx(N)][1].get(NI, NT);
     const size_t sm = (size_t)NI * smem_per_instance(N, 1);
     if (prep(nh_enc_core<N>, sm)) return PQCGPU_ECUDA;
-    if (single_ok && n <= nh_single_max()) {
+    if (single_ok && n <= nh_single_max(1)) {
         if (kem)
             PQC_LAUNCH(st, "nh_enc_single", N, 0,
                        nh_enc_single<N, true><<<n, NHS_THREADS, NhSingleSmem<N>::bytes(), st>>>(pk, coins, nullptr, ct, ss));

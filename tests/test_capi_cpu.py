@@ -104,6 +104,28 @@ def test_kyber_single_instance_thresholds():
     assert enc_limit("kyber768") == 304
 
 
+def test_newhope_single_instance_thresholds():
+    """NewHope op 3 sets the single-instance threshold of keypair and encapsulation (both n); -1
+    restores the measured defaults (304 / 456); get returns the encapsulation's."""
+    import ctypes
+
+    from pqc_gb300 import _lib, kem
+    lib = _lib.load()
+    a = kem.alg_id("newhope1024")
+    ni, thr = ctypes.c_int(), ctypes.c_int()
+    assert lib.pqcgpu_get_launch_shape(a, 3, ctypes.byref(ni), ctypes.byref(thr)) == 0
+    assert ni.value == 456
+    try:
+        assert lib.pqcgpu_set_launch_shape(a, 3, -2, 0) != 0
+        assert lib.pqcgpu_set_launch_shape(a, 3, 0, 0) == 0
+        assert lib.pqcgpu_get_launch_shape(kem.alg_id("newhope512"), 3, ctypes.byref(ni), ctypes.byref(thr)) == 0
+        assert ni.value == 0
+    finally:
+        assert lib.pqcgpu_set_launch_shape(a, 3, -1, 0) == 0
+    assert lib.pqcgpu_get_launch_shape(a, 3, ctypes.byref(ni), ctypes.byref(thr)) == 0
+    assert ni.value == 456
+
+
 def test_kyber_warp_hash_threshold():
     """Kyber op 5 (the largest batch whose serial hashes run a warp per instance) takes 0..65535,
     shared by every k; the setting round-trips and the default is restored."""

@@ -66,7 +66,7 @@ def test_cpa_matches_oracle(ctx, oracle, n, poly_n):
 
 
 @pytest.mark.parametrize("poly_n", [1024, 512])
-@pytest.mark.parametrize("n", [1, 63, 1000])
+@pytest.mark.parametrize("n", [1, 63, 400, 1000])  # 400: batched keypair, single-instance encapsulation
 def test_kem_matches_oracle(ctx, oracle, n, poly_n):
     alg = ALG[poly_n]
     a = oracle.ALG_NAMES[alg]
@@ -108,7 +108,7 @@ def test_single_instance_kernels_equal_batched(ctx, poly_n, n):
         assert ctx.keypair(alg, n, kc) == (pk, sk)
         assert ctx.enc(alg, n, pk, ec) == (ct, ss)
     finally:
-        lib.pqcgpu_set_launch_shape(a, 3, single.value, 0)
+        lib.pqcgpu_set_launch_shape(a, 3, -1, 0)
     assert ctx.dec(alg, n, ct, sk) == ss
 
 
